@@ -1,0 +1,147 @@
+// af3d_cells.cu -- the sorted cell list: counting sort of clumps by (cell, id).
+//
+// Replaces the fixed-capacity slot table of cells.cu (clear_cell / clear_ocup / cell_locate).
+// The predictor kernel has already written every clump's bucket key and its atomic arrival rank
+// inside the bucket.  Here:
+//   1. exclusive scan of the bucket counts  -> start[b]      (three-kernel reduce-then-scan)
+//   2. scatter old slots by arrival          -> tmp_slot
+//   3. rank every clump inside its bucket by clump id (buckets hold a handful of clumps), which
+//      makes the final order deterministic and equal to the reference's ascending-id insertion
+//      order (cells.cu:60-109)                 -> perm[new slot] = old slot
+// Integer work only; HBM-bound.
+#include "af3d_internal.h"
+
+namespace af3d {
+
+namespace {
+
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 4;
+constexpr int kTile = kScanThreads * kScanItems;
+
+__device__ __forceinline__ int warp_incl_scan(int v) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    int u = __shfl_up_sync(0xffffffffu, v, off);
+    if (lane >= off) v += u;
+  }
+  return v;
+}
+
+// Exclusive scan of one value per thread across the block; returns the block total in *total.
+__device__ __forceinline__ int block_excl_scan(int v, int *total) {
+  __shared__ int warp_tot[kScanThreads / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int incl = warp_incl_scan(v);
+  if (lane == 31) warp_tot[wid] = incl;
+  __syncthreads();
+  if (wid == 0) {
+    int t = lane < kScanThreads / 32 ? warp_tot[lane] : 0;
+    int ti = warp_incl_scan(t);
+    if (lane < kScanThreads / 32) warp_tot[lane] = ti - t;
+    if (lane == kScanThreads / 32 - 1) *total = ti;
+  }
+  __syncthreads();
+  int r = incl - v + warp_tot[wid];
+  __syncthreads();
+  return r;
+}
+
+// Buckets in use: ncell3 cells plus one private bucket per clump for the clumps not binned.
+__device__ __forceinline__ long n_buckets(const DevScalars *d, long n) { return d->grid.ncell3 + n; }
+
+__global__ void k_scan_partials(const int *__restrict__ count, int *block_sums, const DevScalars *d,
+                                long n) {
+  const long nb = n_buckets(d, n);
+  const long base = blockIdx.x * (long)kTile + threadIdx.x * (long)kScanItems;
+  int v = 0;
+#pragma unroll
+  for (int i = 0; i < kScanItems; i++)
+    if (base + i < nb) v += count[base + i];
+  __shared__ int tot;
+  block_excl_scan(v, &tot);
+  if (threadIdx.x == 0) block_sums[blockIdx.x] = tot;
+}
+
+// One block scans the per-tile sums in place (exclusive), chunk by chunk.
+__global__ void k_scan_top(int *block_sums, long ntiles, int *start, const DevScalars *d, long n) {
+  const long nb = n_buckets(d, n);
+  __shared__ int tot;
+  int carry = 0;
+  for (long b0 = 0; b0 < ntiles; b0 += kScanThreads) {
+    const long i = b0 + threadIdx.x;
+    int v = i < ntiles ? block_sums[i] : 0;
+    int e = block_excl_scan(v, &tot);
+    if (i < ntiles) block_sums[i] = e + carry;
+    carry += tot;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) start[nb] = (int)n;   // every clump has exactly one bucket
+}
+
+__global__ void k_scan_final(const int *__restrict__ count, const int *__restrict__ block_sums,
+                             int *start, const DevScalars *d, long n) {
+  const long nb = n_buckets(d, n);
+  const long base = blockIdx.x * (long)kTile + threadIdx.x * (long)kScanItems;
+  int v[kScanItems];
+  int sum = 0;
+#pragma unroll
+  for (int i = 0; i < kScanItems; i++) {
+    v[i] = base + i < nb ? count[base + i] : 0;
+    sum += v[i];
+  }
+  __shared__ int tot;
+  int e = block_excl_scan(sum, &tot) + block_sums[blockIdx.x];
+#pragma unroll
+  for (int i = 0; i < kScanItems; i++) {
+    if (base + i < nb) start[base + i] = e;
+    e += v[i];
+  }
+}
+
+__global__ void k_scatter(const int *__restrict__ key, const int *__restrict__ rank_tmp,
+                          const int *__restrict__ start, int *tmp_slot, long n) {
+  const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  tmp_slot[start[key[s]] + rank_tmp[s]] = (int)s;
+}
+
+// Also returns the bucket count to zero, so the count array is all-zero at the next build
+// whatever the grid then is (the scan has consumed it already).
+__global__ void k_rank(const int *__restrict__ key, const int *__restrict__ start,
+                       const int *__restrict__ tmp_slot, const long long *__restrict__ id, int *perm,
+                       int *count, DevScalars *d, long ntags, long n) {
+  const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const long ncell3 = d->grid.ncell3;
+  const int k = key[s];
+  count[k] = 0;
+  const int b = start[k], e = start[k + 1];
+  const long long me = id[s];
+  int r = 0;
+  for (int j = b; j < e; j++) r += id[tmp_slot[j]] < me;
+  perm[b + r] = (int)s;
+  // cells.cu:96-102: a cell may hold at most ntags - 1 clumps
+  if (ntags > 0 && k < ncell3 && r == 0 && (e - b) >= ntags)
+    atomicOr(&d->status, 1 << AF3D_ERR_CELL_CAPACITY);
+}
+
+}  // namespace
+
+long scan_tiles(long bucket_cap) { return (bucket_cap + kTile - 1) / kTile; }
+
+void launch_sort(const Launch &L, DevScalars *d, Cells c, const long long *id, long ntags) {
+  // Launch sizes follow the capacity; the kernels read the bucket count in use from the device,
+  // so a captured graph stays valid across device-side re-grids.
+  const long ntiles = scan_tiles(c.cap);
+  k_scan_partials<<<(unsigned)ntiles, kScanThreads, 0, L.st>>>(c.count, c.block_sums, d, L.n);
+  k_scan_top<<<1, kScanThreads, 0, L.st>>>(c.block_sums, ntiles, c.start, d, L.n);
+  k_scan_final<<<(unsigned)ntiles, kScanThreads, 0, L.st>>>(c.count, c.block_sums, c.start, d, L.n);
+  if (L.n <= 0) return;
+  const unsigned g = (unsigned)((L.n + 127) / 128);
+  k_scatter<<<g, 128, 0, L.st>>>(c.key, c.rank_tmp, c.start, c.tmp_slot, L.n);
+  k_rank<<<g, 128, 0, L.st>>>(c.key, c.start, c.tmp_slot, id, c.perm, c.count, d, ntags, L.n);
+}
+
+}  // namespace af3d

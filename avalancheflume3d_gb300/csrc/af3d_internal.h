@@ -1,0 +1,127 @@
+// af3d_internal.h -- definitions shared by the device kernels and the host side of the C ABI.
+//
+// Device state layout (HBM): every per-clump scalar is one FP64 "plane" of length N, in the
+// (cell, id)-sorted order of the last cell build.  The cell build permutes every plane, so the
+// clumps of one cell -- and of neighbouring cells along x -- sit in consecutive slots and all
+// per-clump kernels read and write coalesced.  Two plane sets (cur / alt) are ping-ponged by the
+// permutation.  Neighbour-visible data is additionally packed per slot into an FP64 record
+// (NbrRec, 192 B) and an FP32 culling record (CullRec, 80 B) so that a neighbour gather touches
+// one or two 64-byte lines.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/af3d.h"
+
+namespace af3d {
+
+enum Plane : int {
+  RX, RY, RZ, VX, VY, VZ, WX, WY, WZ,
+  R00, R01, R02, R10, R11, R12, R20, R21, R22,   // Rmatx, Rmaty, Rmatz rows
+  AIX, AIY, AIZ, ALIX, ALIY, ALIZ,               // a_i, alpha_i
+  AFX, AFY, AFZ, ALFX, ALFY, ALFZ,               // a_f, alpha_f
+  S0X, S0Y, S0Z, S1X, S1Y, S1Z, S2X, S2Y, S2Z, S3X, S3Y, S3Z,   // sphere centres rr_a..rr_d
+  FX, FY, FZ, TX, TY, TZ,                        // force, torque accumulators
+  RAD, DEN, MASS, IXX, IYY, IZZ,                 // radius, density, clump mass, inertia
+  MSPH,                                          // SPH_FACT*density*r^3 (force_part.cu:58 order)
+  MWALL,                                         // SPH_FACT*r^3*density (force_walls.cu:47 order)
+  NPLANES
+};
+
+struct Planes {
+  double *p[NPLANES];
+};
+
+// Packed neighbour record: everything a partner clump contributes to a contact.
+struct __align__(64) NbrRec {
+  double rx, ry, rz, vx, vy, vz, wx, wy, wz;
+  double s[12];          // sphere k: s[3k], s[3k+1], s[3k+2]
+  double rad, msph, pad;
+};
+
+// FP32 culling record.  c = (centre, bound), sk = (sphere centre, inflated radius).  The bounds
+// are rounded up and inflated by 2^-21 times the largest coordinate magnitude, which covers the
+// FP32 rounding of every coordinate; the tests multiply by (1 + 2^-18) on top, so a pair the
+// FP64 test could accept is never culled.
+struct __align__(16) CullRec {
+  float4 c;
+  float4 s[4];
+};
+
+// Cell-list buffers.  Keys: cell index in [0, ncell3) for binned clumps, ncell3 + id for clumps
+// that are not binned (removed), so every bucket holds its clumps in id order after the rank
+// pass and no bucket is large.
+struct Cells {
+  int *key;         // [N]   key of old slot
+  int *rank_tmp;    // [N]   atomic arrival rank inside the bucket (nondeterministic)
+  int *tmp_slot;    // [N]   old slots scattered by arrival order
+  int *perm;        // [N]   new slot -> old slot, deterministic (cell, id) order
+  int *count;       // [cap] bucket sizes (all zero between builds)
+  int *start;       // [cap+1] exclusive scan of count
+  int *block_sums;  // [scan_tiles(cap)] scan scratch
+  long cap;         // buckets available (ncell3 + N must fit)
+};
+
+// Per-context device scalars (one struct in global memory).
+struct DevScalars {
+  af3d_system_par sys;      // time here is the CURRENT time (after the last advance)
+  af3d_funnel     fun;
+  af3d_cell_par   grid;
+  double          time_prev;  // time before the last advance (init_Verlet's removal test)
+  int             phase;      // AF3D_PHASE_*
+  int             variant;    // AF3D_FRICTION_*
+  int             status;     // bitmask of 1 << AF3D_ERR_*
+  int             pad;
+  unsigned long long bbox[8];  // regrid scratch: ordered-int min/max of x, y, z, max vx, min vz
+  unsigned long long contacts; // active sphere-sphere contacts of the last fused force pass
+  long long       pending_ncell3;  // grid derived on the device that did not fit the buffers
+  af3d_cell_par   pending;
+};
+
+// Which force routines a boundary kernel applies, in the reference's call order.
+enum Routine : int {
+  R_HOP0 = 0, R_HOP1, R_HOP2, R_FUNNEL, R_FCORNERS, R_WALLS, R_FLUME
+};
+
+// ---- kernel launchers (defined in the .cu files; all enqueue on `st`) ----
+struct Launch {
+  cudaStream_t st;
+  long n;
+};
+
+void launch_predict (const Launch &L, Planes cur, DevScalars *d, bool predict, bool keys, bool t_prev,
+                     Cells cells, const long long *id);
+// Exclusive scan of the bucket counts, scatter by arrival, then the deterministic (bucket, id)
+// rank: fills cells.start[0..nbuckets] and cells.perm, checks the ntags capacity and leaves the
+// count array zeroed.  nbuckets = grid.ncell3 + N is read on the device.
+void launch_sort (const Launch &L, DevScalars *d, Cells cells, const long long *id, long ntags);
+long scan_tiles (long bucket_cap);
+void launch_permute (const Launch &L, Planes src, Planes dst, const int *perm, long long *id_src,
+                     long long *id_dst);
+void launch_permute_records (const Launch &L, Planes src, Planes dst, const int *perm,
+                             long long *id_src, long long *id_dst, NbrRec *nbr, CullRec *cull);
+void launch_build_records (const Launch &L, Planes cur, NbrRec *nbr, CullRec *cull);
+void launch_fused_forces (const Launch &L, Planes cur, Planes out, DevScalars *d, const NbrRec *nbr,
+                          const CullRec *cull, const int *start, bool write_ft);
+void launch_boundary (const Launch &L, Planes cur, DevScalars *d, int routine);
+void launch_part (const Launch &L, Planes cur, DevScalars *d, const NbrRec *nbr, const CullRec *cull,
+                  const int *start, int sph_id);
+void launch_get_accel (const Launch &L, Planes cur, DevScalars *d);
+void launch_finish_verlet (const Launch &L, Planes cur, DevScalars *d);
+void launch_clear_forces (const Launch &L, Planes cur);
+void launch_advance_time (cudaStream_t st, DevScalars *d);
+void launch_regrid (const Launch &L, Planes cur, DevScalars *d, long bucket_cap);
+void launch_aos_to_planes (const Launch &L, const af3d_particle *aos, const double *acc,
+                           const double *anga, Planes cur, long long *id);
+void launch_planes_to_aos (const Launch &L, Planes cur, const long long *id, af3d_particle *aos,
+                           double *acc, double *anga, DevScalars *d);
+void launch_contact_pairs (const Launch &L, Planes cur, DevScalars *d, const NbrRec *nbr,
+                           const CullRec *cull, const int *start, const long long *id,
+                           long long *out, unsigned long long *count, long cap, int active);
+void launch_cells_by_id (const Launch &L, const int *key, const long long *id, long ncell3,
+                         long long *cell_of_id);
+// DFMA throughput microbenchmark (TFLOP/s, 2 flops per DFMA), bounded to ~0.1 s.
+cudaError_t measure_dfma (int sms, double *tflops);
+
+}  // namespace af3d

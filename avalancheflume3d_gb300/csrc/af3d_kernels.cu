@@ -1,0 +1,783 @@
+// af3d_kernels.cu -- the step kernels (compiled with -fmad=false: see af3d_physics.cuh).
+//
+// Kernels, per step of the fused path (af3d_step):
+//   k_predict      init_Verlet (+ cell key, bucket count)              one thread per clump
+//   (cells)        scan of bucket counts, scatter, deterministic rank  af3d_cells.cu
+//   k_permute      move every plane into (cell, id) order, build the packed neighbour records
+//   k_fused_forces boundaries + sphere contacts + bed + get_accel + finish_Verlet, per clump,
+//                  gathering (never scattering) contributions: no atomics on forces
+// The per-routine C-ABI entry points use k_boundary / k_part / k_get_accel / k_finish_verlet,
+// which apply the same device functions to the F, T planes one routine at a time.
+#include <cfloat>
+
+#include "af3d_physics.cuh"
+
+namespace af3d {
+
+namespace {
+
+constexpr int kBlock = 128;
+
+inline unsigned grid_for(long n, int block = kBlock) {
+  return (unsigned)((n + block - 1) / block);
+}
+
+__device__ __forceinline__ V3 load3(const Planes &P, int x, long s) {
+  return mk(P.p[x][s], P.p[x + 1][s], P.p[x + 2][s]);
+}
+__device__ __forceinline__ void store3(const Planes &P, int x, long s, V3 v) {
+  P.p[x][s] = v.x;
+  P.p[x + 1][s] = v.y;
+  P.p[x + 2][s] = v.z;
+}
+
+__device__ __forceinline__ void raise_status(DevScalars *d, int err) {
+  atomicOr(&d->status, 1 << err);
+}
+
+// ------------------------------------------------------------------ import / export
+
+__global__ void k_aos_to_planes(const af3d_particle *__restrict__ aos, const double *__restrict__ acc,
+                                const double *__restrict__ anga, Planes P, long long *id, long n) {
+  long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const af3d_particle &q = aos[s];
+  store3(P, RX, s, mk(q.rr.x, q.rr.y, q.rr.z));
+  store3(P, VX, s, mk(q.vv.x, q.vv.y, q.vv.z));
+  store3(P, WX, s, mk(q.ww.x, q.ww.y, q.ww.z));
+  store3(P, R00, s, mk(q.Rmatx.x, q.Rmatx.y, q.Rmatx.z));
+  store3(P, R10, s, mk(q.Rmaty.x, q.Rmaty.y, q.Rmaty.z));
+  store3(P, R20, s, mk(q.Rmatz.x, q.Rmatz.y, q.Rmatz.z));
+  for (int k = 0; k < 4; k++) store3(P, S0X + 3 * k, s, mk(q.rr_s[k].x, q.rr_s[k].y, q.rr_s[k].z));
+  V3 a = acc ? mk(acc[3 * s], acc[3 * s + 1], acc[3 * s + 2]) : mk(0.0, 0.0, 0.0);
+  V3 al = anga ? mk(anga[3 * s], anga[3 * s + 1], anga[3 * s + 2]) : mk(0.0, 0.0, 0.0);
+  store3(P, AIX, s, a);
+  store3(P, ALIX, s, al);
+  store3(P, AFX, s, mk(0.0, 0.0, 0.0));
+  store3(P, ALFX, s, mk(0.0, 0.0, 0.0));
+  store3(P, FX, s, mk(0.0, 0.0, 0.0));
+  store3(P, TX, s, mk(0.0, 0.0, 0.0));
+  const double r = q.radius, rho = q.density;
+  P.p[RAD][s] = r;
+  P.p[DEN][s] = rho;
+  P.p[MASS][s] = q.mass;
+  store3(P, IXX, s, mk(q.moment_of_inertia.x, q.moment_of_inertia.y, q.moment_of_inertia.z));
+  P.p[MSPH][s] = kSPH_FACT * rho * r * r * r;   // force_part.cu:58
+  P.p[MWALL][s] = kSPH_FACT * r * r * r * rho;  // force_walls.cu:47
+  id[s] = s;
+}
+
+__global__ void k_planes_to_aos(Planes P, const long long *__restrict__ id, af3d_particle *aos,
+                                double *acc, double *anga, const DevScalars *d, long n) {
+  long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const double cost = d->sys.cost, sint = d->sys.sint;
+  af3d_particle &q = aos[id[s]];
+  q.radius = P.p[RAD][s];
+  q.mass = P.p[MASS][s];
+  q.density = P.p[DEN][s];
+  V3 I = load3(P, IXX, s);
+  q.moment_of_inertia = {I.x, I.y, I.z};
+  V3 r = load3(P, RX, s);
+  q.rr = {r.x, r.y, r.z};
+  V3 rr = to_slope(r, cost, sint);
+  q.rrot = {rr.x, rr.y, rr.z};
+  for (int k = 0; k < 4; k++) {
+    V3 sk = load3(P, S0X + 3 * k, s);
+    q.rr_s[k] = {sk.x, sk.y, sk.z};
+    V3 qk = to_slope(sk, cost, sint);
+    q.rrot_s[k] = {qk.x, qk.y, qk.z};
+  }
+  V3 v = load3(P, VX, s), w = load3(P, WX, s);
+  q.vv = {v.x, v.y, v.z};
+  q.ww = {w.x, w.y, w.z};
+  V3 a = load3(P, R00, s), b = load3(P, R10, s), c = load3(P, R20, s);
+  q.Rmatx = {a.x, a.y, a.z};
+  q.Rmaty = {b.x, b.y, b.z};
+  q.Rmatz = {c.x, c.y, c.z};
+  if (acc) {
+    V3 ai = load3(P, AIX, s);
+    acc[3 * id[s]] = ai.x; acc[3 * id[s] + 1] = ai.y; acc[3 * id[s] + 2] = ai.z;
+  }
+  if (anga) {
+    V3 al = load3(P, ALIX, s);
+    anga[3 * id[s]] = al.x; anga[3 * id[s] + 1] = al.y; anga[3 * id[s] + 2] = al.z;
+  }
+}
+
+// ------------------------------------------------------------------ init_Verlet (+ cell keys)
+
+// Cell coordinate of cells.cu:69-77 (multiplication by cs_inv, then `== ncell -> ncell-1`).
+__device__ __forceinline__ long bin_axis(double x, double xmin, double inv, long n) {
+  long i = (long)(inv * (x - xmin));
+  if (i == n) i--;
+  return i;
+}
+
+// init_Verlet.cu:25-148 for one clump (PREDICT), and/or cell_locate's binning (cells.cu:60-92)
+// with the current time (KEYS): the bucket key, the bucket count and the clump's arrival rank.
+// Clumps that are not binned (removed, or non-finite) get the unique bucket ncell3 + id, so every
+// bucket holds its clumps in id order after the rank pass.  `t_prev`: init_Verlet's removal test
+// uses the time before the advance (the fused step advances time first).
+template <bool PREDICT, bool KEYS>
+__global__ void k_predict(Planes P, DevScalars *d, bool t_prev, Cells cells,
+                          const long long *__restrict__ id, long n) {
+  long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const double side_x = d->sys.side.x;
+  V3 r = load3(P, RX, s);
+  if (PREDICT) {
+    const double dt = d->sys.dt, hdt = d->sys.hdt;
+    const double t_init = t_prev ? d->time_prev : d->sys.time;
+    if (is_removed(t_init, r.x, side_x)) {
+      P.p[RAD][s] = 0.0;
+    } else {
+      V3 v = load3(P, VX, s), a = load3(P, AIX, s), w = load3(P, WX, s), al = load3(P, ALIX, s);
+      V3 Rx = load3(P, R00, s), Ry = load3(P, R10, s), Rz = load3(P, R20, s);
+      r.x += dt * (v.x + hdt * a.x);
+      r.y += dt * (v.y + hdt * a.y);
+      r.z += dt * (v.z + hdt * a.z);
+      v.x += dt * a.x;
+      v.y += dt * a.y;
+      v.z += dt * a.z;
+      V3 dO = mk(dt * (w.x + hdt * al.x), dt * (w.y + hdt * al.y), dt * (w.z + hdt * al.z));
+      double mag = sqrt(dO.x * dO.x + dO.y * dO.y + dO.z * dO.z);
+      V3 dRx, dRy, dRz;
+      if (mag > 0.0) {
+        // Rodrigues rotation about dO/|dO| by |dO| (init_Verlet.cu:63-83)
+        V3 u = mk(dO.x / mag, dO.y / mag, dO.z / mag);
+        double c = cos(mag), sn = sin(mag), omc = 1.0 - c;
+        dRx = mk(omc * u.x * u.x + c, omc * u.x * u.y - sn * u.z, omc * u.x * u.z + sn * u.y);
+        dRy = mk(omc * u.y * u.x + sn * u.z, omc * u.y * u.y + c, omc * u.y * u.z - sn * u.x);
+        dRz = mk(omc * u.z * u.x - sn * u.y, omc * u.z * u.y + sn * u.x, omc * u.z * u.z + c);
+      } else {
+        dRx = mk(1.0, 0.0, 0.0);
+        dRy = mk(0.0, 1.0, 0.0);
+        dRz = mk(0.0, 0.0, 1.0);
+      }
+      // R <- dR R (rows), then each column renormalised (init_Verlet.cu:92-114)
+      V3 Tx = mk(dRx.x * Rx.x + dRx.y * Ry.x + dRx.z * Rz.x, dRx.x * Rx.y + dRx.y * Ry.y + dRx.z * Rz.y,
+                 dRx.x * Rx.z + dRx.y * Ry.z + dRx.z * Rz.z);
+      V3 Ty = mk(dRy.x * Rx.x + dRy.y * Ry.x + dRy.z * Rz.x, dRy.x * Rx.y + dRy.y * Ry.y + dRy.z * Rz.y,
+                 dRy.x * Rx.z + dRy.y * Ry.z + dRy.z * Rz.z);
+      V3 Tz = mk(dRz.x * Rx.x + dRz.y * Ry.x + dRz.z * Rz.x, dRz.x * Rx.y + dRz.y * Ry.y + dRz.z * Rz.y,
+                 dRz.x * Rx.z + dRz.y * Ry.z + dRz.z * Rz.z);
+      double nrm = sqrt(Tx.x * Tx.x + Ty.x * Ty.x + Tz.x * Tz.x);
+      Rx.x = Tx.x / nrm; Ry.x = Ty.x / nrm; Rz.x = Tz.x / nrm;
+      nrm = sqrt(Tx.y * Tx.y + Ty.y * Ty.y + Tz.y * Tz.y);
+      Rx.y = Tx.y / nrm; Ry.y = Ty.y / nrm; Rz.y = Tz.y / nrm;
+      nrm = sqrt(Tx.z * Tx.z + Ty.z * Ty.z + Tz.z * Tz.z);
+      Rx.z = Tx.z / nrm; Ry.z = Ty.z / nrm; Rz.z = Tz.z / nrm;
+      w.x += dt * al.x;
+      w.y += dt * al.y;
+      w.z += dt * al.z;
+      store3(P, RX, s, r);
+      store3(P, VX, s, v);
+      store3(P, WX, s, w);
+      store3(P, R00, s, Rx);
+      store3(P, R10, s, Ry);
+      store3(P, R20, s, Rz);
+      // sphere centres r + (radius/sqrt2) R (+-1,+-1,+-1) (init_Verlet.cu:130-142)
+      const double pos = P.p[RAD][s] / kROOT2;
+      store3(P, S0X, s, mk(r.x + pos * (Rx.x + Rx.y + Rx.z), r.y + pos * (Ry.x + Ry.y + Ry.z),
+                           r.z + pos * (Rz.x + Rz.y + Rz.z)));
+      store3(P, S1X, s, mk(r.x + pos * (Rx.x - Rx.y - Rx.z), r.y + pos * (Ry.x - Ry.y - Ry.z),
+                           r.z + pos * (Rz.x - Rz.y - Rz.z)));
+      store3(P, S2X, s, mk(r.x + pos * (-Rx.x - Rx.y + Rx.z), r.y + pos * (-Ry.x - Ry.y + Ry.z),
+                           r.z + pos * (-Rz.x - Rz.y + Rz.z)));
+      store3(P, S3X, s, mk(r.x + pos * (-Rx.x + Rx.y - Rx.z), r.y + pos * (-Ry.x + Ry.y - Ry.z),
+                           r.z + pos * (-Rz.x + Rz.y - Rz.z)));
+    }
+  }
+  if (!KEYS) return;
+  const af3d_cell_par &g = d->grid;
+  const long ncell3 = g.ncell3;
+  long key;
+  if (is_removed(d->sys.time, r.x, side_x)) {
+    key = ncell3 + id[s];
+  } else if (!(isfinite(r.x) && isfinite(r.y) && isfinite(r.z))) {
+    raise_status(d, AF3D_ERR_NAN);
+    key = ncell3 + id[s];
+  } else {
+    long i = bin_axis(r.x, g.rr_min.x, g.cs_inv.x, g.ncell.x);
+    long j = bin_axis(r.y, g.rr_min.y, g.cs_inv.y, g.ncell.y);
+    long k = bin_axis(r.z, g.rr_min.z, g.cs_inv.z, g.ncell.z);
+    if (i < 0 || j < 0 || k < 0) {
+      raise_status(d, AF3D_ERR_NEGATIVE_CELL);
+      i = i < 0 ? 0 : i; j = j < 0 ? 0 : j; k = k < 0 ? 0 : k;
+    }
+    if (i >= g.ncell.x || j >= g.ncell.y || k >= g.ncell.z) {
+      raise_status(d, AF3D_ERR_GRID_ESCAPE);
+      i = i < g.ncell.x ? i : g.ncell.x - 1;
+      j = j < g.ncell.y ? j : g.ncell.y - 1;
+      k = k < g.ncell.z ? k : g.ncell.z - 1;
+    }
+    key = i + g.ncell.x * (j + k * g.ncell.y);
+  }
+  cells.key[s] = (int)key;
+  cells.rank_tmp[s] = atomicAdd(&cells.count[key], 1);
+}
+
+// ------------------------------------------------------------------ permutation + records
+
+__device__ __forceinline__ float f_up(double x) { return __double2float_ru(x); }
+
+// Packed FP64 neighbour record and conservative FP32 culling record of slot s.
+__device__ __forceinline__ void write_records(long s, V3 r, V3 v, V3 w, const V3 *sp, double rad,
+                                              double msph, NbrRec *nbr, CullRec *cull) {
+  NbrRec &q = nbr[s];
+  q.rx = r.x; q.ry = r.y; q.rz = r.z;
+  q.vx = v.x; q.vy = v.y; q.vz = v.z;
+  q.wx = w.x; q.wy = w.y; q.wz = w.z;
+  double M = fmax(fmax(fabs(r.x), fabs(r.y)), fabs(r.z));
+  double ext = 0.0;
+  for (int k = 0; k < 4; k++) {
+    q.s[3 * k] = sp[k].x; q.s[3 * k + 1] = sp[k].y; q.s[3 * k + 2] = sp[k].z;
+    M = fmax(M, fmax(fmax(fabs(sp[k].x), fabs(sp[k].y)), fabs(sp[k].z)));
+    double dx = sp[k].x - r.x, dy = sp[k].y - r.y, dz = sp[k].z - r.z;
+    ext = fmax(ext, sqrt(dx * dx + dy * dy + dz * dz));
+  }
+  q.rad = rad; q.msph = msph; q.pad = 0.0;
+  // 2^-21 * max|coordinate| bounds 4x the FP32 rounding of a coordinate difference.
+  const double mu = fmax(M, rad) * 4.76837158203125e-07 + 1e-30;
+  const float radf = f_up(rad + mu);
+  CullRec c;
+  c.c = make_float4((float)r.x, (float)r.y, (float)r.z, f_up(ext * (1.0 + 1e-12) + rad + mu));
+  for (int k = 0; k < 4; k++) c.s[k] = make_float4((float)sp[k].x, (float)sp[k].y, (float)sp[k].z, radf);
+  cull[s] = c;
+}
+
+// dst[p][s] = src[p][perm[s]] for every plane, plus the records of the new slot.
+__global__ void k_permute(Planes src, Planes dst, const int *__restrict__ perm,
+                          const long long *__restrict__ id_src, long long *id_dst, NbrRec *nbr,
+                          CullRec *cull, long n) {
+  long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const long o = perm ? perm[s] : s;
+  if (perm) {
+#pragma unroll 8
+    for (int p = 0; p < NPLANES; p++) dst.p[p][s] = src.p[p][o];
+    id_dst[s] = id_src[o];
+  }
+  if (nbr) {
+    V3 sp[4];
+    for (int k = 0; k < 4; k++) sp[k] = load3(dst, S0X + 3 * k, s);
+    write_records(s, load3(dst, RX, s), load3(dst, VX, s), load3(dst, WX, s), sp, dst.p[RAD][s],
+                  dst.p[MSPH][s], nbr, cull);
+  }
+}
+
+// ------------------------------------------------------------------ particle contacts
+
+constexpr int kCandCap = 48;
+constexpr float kCullSlack = 1.0f + 3.814697265625e-06f;  // 1 + 2^-18
+
+__device__ __forceinline__ float d2f(float4 a, float4 b) {
+  float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+  return dx * dx + dy * dy + dz * dz;
+}
+
+// 16-bit mask of the sphere pairs of own clump (cull record me) and partner m that the FP32
+// test cannot rule out; bit p = sph_id - 1 = 4 * (partner sphere) + (own sphere).
+__device__ __forceinline__ unsigned pair_mask(const CullRec &me, const CullRec &m) {
+  const float lim = me.c.w + m.c.w;
+  if (d2f(me.c, m.c) > lim * lim * kCullSlack) return 0u;
+  const float rl = me.s[0].w + m.s[0].w;
+  const float r2 = rl * rl * kCullSlack;
+  unsigned mask = 0u;
+#pragma unroll
+  for (int j = 0; j < 4; j++)
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+      if (d2f(me.s[k], m.s[j]) <= r2) mask |= 1u << (4 * j + k);
+  return mask;
+}
+
+struct Search {
+  long ci, cj, ck;
+};
+
+// Search-centre cell of force_part.cu:77-85 (division by cell_side).
+__device__ __forceinline__ long search_axis(double x, double xmin, double side, long n) {
+  long i = (long)((x - xmin) / side);
+  if (i == n) i--;
+  return i;
+}
+
+__device__ __forceinline__ Search search_centre(V3 r, const af3d_cell_par &g) {
+  Search q;
+  q.ci = search_axis(r.x, g.rr_min.x, g.cell_side.x, g.ncell.x);
+  q.cj = search_axis(r.y, g.rr_min.y, g.cell_side.y, g.ncell.y);
+  q.ck = search_axis(r.z, g.rr_min.z, g.cell_side.z, g.ncell.z);
+  return q;
+}
+
+// Visit the occupied slots of the 27 neighbour cells in the reference's order
+// (idel, jdel, kdel from -1 to 1; force_part.cu:88-106); slots inside a cell are in id order.
+template <typename F>
+__device__ __forceinline__ void for_neighbour_slots(const Search &q, const af3d_cell_par &g,
+                                                    const int *__restrict__ start, F &&f) {
+#pragma unroll 1
+  for (int di = -1; di <= 1; di++)
+#pragma unroll 1
+    for (int dj = -1; dj <= 1; dj++)
+#pragma unroll 1
+      for (int dk = -1; dk <= 1; dk++) {
+        const long in = q.ci + di, jn = q.cj + dj, kn = q.ck + dk;
+        if (in < 0 || jn < 0 || kn < 0 || in >= g.ncell.x || jn >= g.ncell.y || kn >= g.ncell.z)
+          continue;
+        const long c = in + g.ncell.x * (jn + g.ncell.y * kn);
+        const int t0 = __ldg(&start[c]), t1 = __ldg(&start[c + 1]);
+#pragma unroll 1
+        for (int t = t0; t < t1; t++) f(t);
+      }
+}
+
+// All sixteen sph_id passes of force_part for clump s, accumulated in the reference order:
+// sph_id outer, then cells, then slots.  Phase 1 walks the neighbour cells once and keeps the
+// FP32-surviving partners with their 16-bit pair masks; phase 2 runs the exact FP64 test and
+// contact law per sph_id over that list.  Returns the number of active contacts.
+__device__ __forceinline__ int particle_contacts(long s, const Own &o, const Consts &c,
+                                                 const af3d_cell_par &g, const NbrRec *__restrict__ nbr,
+                                                 const CullRec *__restrict__ cull,
+                                                 const int *__restrict__ start, int only_p, V3 &F,
+                                                 V3 &T) {
+  const bool xi0 = c.variant == AF3D_FRICTION_DEV;
+  const CullRec me = cull[s];
+  const Search q = search_centre(o.r, g);
+  int cand_t[kCandCap];
+  unsigned short cand_m[kCandCap];
+  int ncand = 0;
+  bool overflow = false;
+  const unsigned want = only_p < 0 ? 0xffffu : (1u << only_p);
+  for_neighbour_slots(q, g, start, [&](int t) {
+    if (t == s) return;
+    const unsigned m = pair_mask(me, cull[t]) & want;
+    if (!m) return;
+    if (ncand < kCandCap) {
+      cand_t[ncand] = t;
+      cand_m[ncand] = (unsigned short)m;
+      ncand++;
+    } else {
+      overflow = true;
+    }
+  });
+  int active = 0;
+  if (!overflow) {
+#pragma unroll 1
+    for (int p = 0; p < 16; p++) {
+      if (!((want >> p) & 1u)) continue;
+      const int sl = p & 3, sm = p >> 2;
+#pragma unroll 1
+      for (int k = 0; k < ncand; k++) {
+        if (!((cand_m[k] >> p) & 1u)) continue;
+        active += part_pair(o.r, o.v, o.w, o.s[sl], o.rad, o.msph, nbr[cand_t[k]], sm, c, xi0, F, T) == 2;
+      }
+    }
+  } else {
+    // More partners than the list holds: walk the cells once per sph_id (same order).
+#pragma unroll 1
+    for (int p = 0; p < 16; p++) {
+      if (!((want >> p) & 1u)) continue;
+      const int sl = p & 3, sm = p >> 2;
+      for_neighbour_slots(q, g, start, [&](int t) {
+        if (t == s) return;
+        if (!((pair_mask(me, cull[t]) >> p) & 1u)) return;
+        active += part_pair(o.r, o.v, o.w, o.s[sl], o.rad, o.msph, nbr[t], sm, c, xi0, F, T) == 2;
+      });
+    }
+  }
+  return active;
+}
+
+__device__ __forceinline__ Own own_from_record(const NbrRec &q, double mwall) {
+  Own o;
+  o.r = mk(q.rx, q.ry, q.rz);
+  o.v = mk(q.vx, q.vy, q.vz);
+  o.w = mk(q.wx, q.wy, q.wz);
+  for (int k = 0; k < 4; k++) o.s[k] = mk(q.s[3 * k], q.s[3 * k + 1], q.s[3 * k + 2]);
+  o.rad = q.rad;
+  o.msph = q.msph;
+  o.mwall = mwall;
+  return o;
+}
+
+__device__ __forceinline__ Own own_from_planes(const Planes &P, long s) {
+  Own o;
+  o.r = load3(P, RX, s);
+  o.v = load3(P, VX, s);
+  o.w = load3(P, WX, s);
+  for (int k = 0; k < 4; k++) o.s[k] = load3(P, S0X + 3 * k, s);
+  o.rad = P.p[RAD][s];
+  o.msph = P.p[MSPH][s];
+  o.mwall = P.p[MWALL][s];
+  return o;
+}
+
+__device__ __forceinline__ void warp_count(DevScalars *d, int active) {
+  unsigned v = (unsigned)active;
+  for (int off = 16; off; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  if ((threadIdx.x & 31) == 0 && v) atomicAdd(&d->contacts, (unsigned long long)v);
+}
+
+// The whole force pass of one step for clump s, in the reference's call order, then get_accel
+// and finish_Verlet.  Velocities after the corrector go to `out` (the other plane set), because
+// neighbours still read this step's predicted velocities from the records.
+template <bool WRITE_FT>
+__global__ void __launch_bounds__(kBlock) k_fused_forces(Planes P, Planes out, DevScalars *d,
+                                                         const NbrRec *__restrict__ nbr,
+                                                         const CullRec *__restrict__ cull,
+                                                         const int *__restrict__ start, long n) {
+  const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  int active = 0;
+  if (s < n) {
+    const Consts c = load_consts(d);
+    const af3d_cell_par g = d->grid;
+    const Own o = own_from_record(nbr[s], P.p[MWALL][s]);
+    const bool removed = is_removed(c.time, o.r.x, c.side_x);
+    V3 F = mk(0.0, 0.0, 0.0), T = mk(0.0, 0.0, 0.0);
+    if (c.phase == AF3D_PHASE_AVALANCHE) {
+      // hop x3, funnel, fcorners, walls (avalanche_hst.cu:688-696)
+      for (int rt = R_HOP0; rt <= R_WALLS; rt++) bnd_routine(rt, o, removed, c, F, T);
+      if (!removed) active = particle_contacts(s, o, c, g, nbr, cull, start, -1, F, T);
+      bnd_routine(R_FLUME, o, removed, c, F, T);
+    } else {
+      // part x16 then hop x3 (avalanche_hst.cu:455-461)
+      if (!removed) active = particle_contacts(s, o, c, g, nbr, cull, start, -1, F, T);
+      for (int rt = R_HOP0; rt <= R_HOP2; rt++) bnd_routine(rt, o, removed, c, F, T);
+    }
+    if (WRITE_FT) {
+      store3(P, FX, s, F);
+      store3(P, TX, s, T);
+    }
+    if (!removed) {
+      V3 a, al;
+      get_accel_one(F, T, o.v, o.w, load3(P, R00, s), load3(P, R10, s), load3(P, R20, s),
+                    P.p[MASS][s], o.rad, load3(P, IXX, s), a, al);
+      store3(P, AFX, s, a);
+      store3(P, ALFX, s, al);
+      const V3 ai = load3(P, AIX, s), ali = load3(P, ALIX, s);
+      // finish_Verlet.cu:43-48
+      store3(out, VX, s, mk(o.v.x + c.hdt * (a.x - ai.x), o.v.y + c.hdt * (a.y - ai.y),
+                            o.v.z + c.hdt * (a.z - ai.z)));
+      store3(out, WX, s, mk(o.w.x + c.hdt * (al.x - ali.x), o.w.y + c.hdt * (al.y - ali.y),
+                            o.w.z + c.hdt * (al.z - ali.z)));
+      if (!(isfinite(a.x) && isfinite(a.y) && isfinite(a.z) && isfinite(al.x) && isfinite(al.y) &&
+            isfinite(al.z)))
+        raise_status(d, AF3D_ERR_NAN);
+    } else {
+      store3(out, VX, s, mk(0.0, 0.0, 0.0));  // finish_Verlet.cu:28-32
+      store3(out, WX, s, o.w);
+    }
+  }
+  warp_count(d, active);
+}
+
+// One boundary routine added to the F, T planes (per-routine entry points).
+__global__ void k_boundary(Planes P, DevScalars *d, int routine, long n) {
+  const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const Consts c = load_consts(d);
+  const Own o = own_from_planes(P, s);
+  const bool removed = is_removed(c.time, o.r.x, c.side_x);
+  V3 F = load3(P, FX, s), T = load3(P, TX, s);
+  bnd_routine(routine, o, removed, c, F, T);
+  store3(P, FX, s, F);
+  store3(P, TX, s, T);
+}
+
+// force_part for one sph_id (1..16) or all sixteen (0), added to the F, T planes.
+__global__ void __launch_bounds__(kBlock) k_part(Planes P, DevScalars *d, const NbrRec *__restrict__ nbr,
+                                                 const CullRec *__restrict__ cull,
+                                                 const int *__restrict__ start, int sph_id, long n) {
+  const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const Consts c = load_consts(d);
+  const af3d_cell_par g = d->grid;
+  const Own o = own_from_planes(P, s);
+  if (is_removed(c.time, o.r.x, c.side_x)) return;
+  V3 F = load3(P, FX, s), T = load3(P, TX, s);
+  particle_contacts(s, o, c, g, nbr, cull, start, sph_id - 1, F, T);
+  store3(P, FX, s, F);
+  store3(P, TX, s, T);
+}
+
+__global__ void k_get_accel(Planes P, DevScalars *d, long n) {
+  const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  if (is_removed(d->sys.time, P.p[RX][s], d->sys.side.x)) return;
+  V3 a, al;
+  get_accel_one(load3(P, FX, s), load3(P, TX, s), load3(P, VX, s), load3(P, WX, s), load3(P, R00, s),
+                load3(P, R10, s), load3(P, R20, s), P.p[MASS][s], P.p[RAD][s], load3(P, IXX, s), a, al);
+  store3(P, AFX, s, a);
+  store3(P, ALFX, s, al);
+}
+
+__global__ void k_finish_verlet(Planes P, DevScalars *d, long n) {
+  const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const double hdt = d->sys.hdt;
+  if (is_removed(d->sys.time, P.p[RX][s], d->sys.side.x)) {
+    store3(P, VX, s, mk(0.0, 0.0, 0.0));
+    return;
+  }
+  V3 v = load3(P, VX, s), w = load3(P, WX, s);
+  V3 af = load3(P, AFX, s), ai = load3(P, AIX, s), alf = load3(P, ALFX, s), ali = load3(P, ALIX, s);
+  v.x += hdt * (af.x - ai.x);
+  v.y += hdt * (af.y - ai.y);
+  v.z += hdt * (af.z - ai.z);
+  w.x += hdt * (alf.x - ali.x);
+  w.y += hdt * (alf.y - ali.y);
+  w.z += hdt * (alf.z - ali.z);
+  store3(P, VX, s, v);
+  store3(P, WX, s, w);
+}
+
+__global__ void k_clear_forces(Planes P, long n) {
+  const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  store3(P, FX, s, mk(0.0, 0.0, 0.0));
+  store3(P, TX, s, mk(0.0, 0.0, 0.0));
+}
+
+// sys_par.time += dt (avalanche_hst.cu:672), keeping the previous value for init_Verlet.
+__global__ void k_advance_time(DevScalars *d) {
+  d->time_prev = d->sys.time;
+  d->sys.time = d->sys.time + d->sys.dt;
+}
+
+// ------------------------------------------------------------------ re-grid (cell_dim)
+
+__device__ __forceinline__ unsigned long long ord(double x) {
+  unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double unord(unsigned long long k) {
+  unsigned long long u = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+  return __longlong_as_double((long long)u);
+}
+
+__global__ void k_bbox_init(DevScalars *d) {
+  for (int i = 0; i < 3; i++) {
+    d->bbox[i] = ~0ull;    // min x, y, z
+    d->bbox[3 + i] = 0ull; // max x, y, z
+  }
+  d->bbox[6] = 0ull;       // max vx
+  d->bbox[7] = ~0ull;      // min vz
+}
+
+// Min/max of clump centres, max vx and min vz over every clump (cell_dim.cu:21-54).
+__global__ void k_bbox_reduce(Planes P, DevScalars *d, long n) {
+  const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  unsigned long long mn[3], mx[3], vx, vz;
+  if (s < n) {
+    for (int i = 0; i < 3; i++) mn[i] = mx[i] = ord(P.p[RX + i][s]);
+    vx = ord(P.p[VX][s]);
+    vz = ord(P.p[VZ][s]);
+  } else {
+    for (int i = 0; i < 3; i++) { mn[i] = ~0ull; mx[i] = 0ull; }
+    vx = 0ull;
+    vz = ~0ull;
+  }
+  for (int off = 16; off; off >>= 1) {
+    for (int i = 0; i < 3; i++) {
+      mn[i] = min(mn[i], __shfl_xor_sync(0xffffffffu, mn[i], off));
+      mx[i] = max(mx[i], __shfl_xor_sync(0xffffffffu, mx[i], off));
+    }
+    vx = max(vx, __shfl_xor_sync(0xffffffffu, vx, off));
+    vz = min(vz, __shfl_xor_sync(0xffffffffu, vz, off));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    for (int i = 0; i < 3; i++) {
+      atomicMin(&d->bbox[i], mn[i]);
+      atomicMax(&d->bbox[3 + i], mx[i]);
+    }
+    atomicMax(&d->bbox[6], vx);
+    atomicMin(&d->bbox[7], vz);
+  }
+}
+
+// cell_dim.cu:56-66 padding and the grid derivation of avalanche_hst.cu:314-333.  A grid whose
+// bucket count does not fit the cell buffers is parked in `pending` for the host to grow them.
+__global__ void k_grid_derive(DevScalars *d, long n, long bucket_cap) {
+  const af3d_system_par &sy = d->sys;
+  const double rgyr = 0.5 * sy.gyr_max, ddt = 2000.0 * sy.dt;
+  const double vxmax = unord(d->bbox[6]), vzmin = unord(d->bbox[7]);
+  V3 hi = mk(unord(d->bbox[3]), unord(d->bbox[4]), unord(d->bbox[5]));
+  V3 lo = mk(unord(d->bbox[0]), unord(d->bbox[1]), unord(d->bbox[2]));
+  hi.x += 1.05 * rgyr + vxmax * ddt;
+  lo.x -= 1.05 * rgyr;
+  hi.y += 1.05 * rgyr;
+  lo.y -= 1.05 * rgyr;
+  hi.z += 1.05 * rgyr;
+  lo.z -= 1.05 * rgyr - vzmin * ddt;
+  af3d_cell_par g = d->grid;
+  const double dist = kGYR + (double)0.05f;   // avalanche_hst.cu:115 adds a float literal
+  g.rr_max = {hi.x, hi.y, hi.z};
+  g.rr_min = {lo.x, lo.y, lo.z};
+  g.length = {hi.x - lo.x, hi.y - lo.y, hi.z - lo.z};
+  g.ncell.x = (long)(g.length.x / (dist * sy.rmax));
+  g.ncell.y = (long)(g.length.y / (dist * sy.rmax));
+  g.ncell.z = (long)(g.length.z / (dist * sy.rmax));
+  g.cell_side.x = g.length.x / ((double)g.ncell.x);
+  g.cell_side.y = g.length.y / ((double)g.ncell.y);
+  g.cell_side.z = g.length.z / ((double)g.ncell.z);
+  g.cs_inv.x = 1.0 / g.cell_side.x;
+  g.cs_inv.y = 1.0 / g.cell_side.y;
+  g.cs_inv.z = 1.0 / g.cell_side.z;
+  g.ncell3 = g.ncell.x * g.ncell.y * g.ncell.z;
+  g.ntot = g.ncell3 * g.ntags;
+  if (g.ncell3 + n + 1 <= bucket_cap && g.ncell3 > 0) {
+    d->grid = g;
+    d->pending_ncell3 = 0;
+  } else {
+    d->pending = g;
+    d->pending_ncell3 = g.ncell3 > 0 ? g.ncell3 : -1;
+  }
+}
+
+// ------------------------------------------------------------------ diagnostics
+
+__global__ void k_contact_pairs(Planes P, DevScalars *d, const NbrRec *__restrict__ nbr,
+                                const CullRec *__restrict__ cull, const int *__restrict__ start,
+                                const long long *__restrict__ id, long long *out,
+                                unsigned long long *count, long cap, int active_only, long n) {
+  const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const Consts c = load_consts(d);
+  const af3d_cell_par g = d->grid;
+  const Own o = own_from_planes(P, s);
+  if (is_removed(c.time, o.r.x, c.side_x)) return;
+  const CullRec me = cull[s];
+  const Search q = search_centre(o.r, g);
+  for_neighbour_slots(q, g, start, [&](int t) {
+    if (t == s) return;
+    unsigned m = pair_mask(me, cull[t]);
+    while (m) {
+      const int p = __ffs(m) - 1;
+      m &= m - 1;
+      V3 F = mk(0.0, 0.0, 0.0), T = mk(0.0, 0.0, 0.0);
+      const int r = part_pair(o.r, o.v, o.w, o.s[p & 3], o.rad, o.msph, nbr[t], p >> 2, c, false, F, T);
+      if (r == 2 || (r == 1 && !active_only)) {
+        unsigned long long k = atomicAdd(count, 1ull);
+        if ((long)k < cap) {
+          out[3 * k] = id[s];
+          out[3 * k + 1] = id[t];
+          out[3 * k + 2] = p + 1;
+        }
+      }
+    }
+  });
+}
+
+__global__ void k_cells_by_id(const int *__restrict__ key, const long long *__restrict__ id, long ncell3,
+                              long long *cell_of_id, long n) {
+  const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const int k = key[s];
+  cell_of_id[id[s]] = k < ncell3 ? k : -1;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ launchers
+
+void launch_predict(const Launch &L, Planes cur, DevScalars *d, bool predict, bool keys, bool t_prev,
+                    Cells cells, const long long *id) {
+  if (L.n <= 0) return;
+  const unsigned g = grid_for(L.n);
+  if (predict && keys)
+    k_predict<true, true><<<g, kBlock, 0, L.st>>>(cur, d, t_prev, cells, id, L.n);
+  else if (predict)
+    k_predict<true, false><<<g, kBlock, 0, L.st>>>(cur, d, t_prev, cells, id, L.n);
+  else if (keys)
+    k_predict<false, true><<<g, kBlock, 0, L.st>>>(cur, d, t_prev, cells, id, L.n);
+}
+
+void launch_permute(const Launch &L, Planes src, Planes dst, const int *perm, long long *id_src,
+                    long long *id_dst) {
+  if (L.n <= 0) return;
+  k_permute<<<grid_for(L.n), kBlock, 0, L.st>>>(src, dst, perm, id_src, id_dst, nullptr, nullptr, L.n);
+}
+
+void launch_permute_records(const Launch &L, Planes src, Planes dst, const int *perm,
+                            long long *id_src, long long *id_dst, NbrRec *nbr, CullRec *cull) {
+  if (L.n <= 0) return;
+  k_permute<<<grid_for(L.n), kBlock, 0, L.st>>>(src, dst, perm, id_src, id_dst, nbr, cull, L.n);
+}
+
+void launch_build_records(const Launch &L, Planes cur, NbrRec *nbr, CullRec *cull) {
+  if (L.n <= 0) return;
+  k_permute<<<grid_for(L.n), kBlock, 0, L.st>>>(cur, cur, nullptr, nullptr, nullptr, nbr, cull, L.n);
+}
+
+void launch_fused_forces(const Launch &L, Planes cur, Planes out, DevScalars *d, const NbrRec *nbr,
+                         const CullRec *cull, const int *start, bool write_ft) {
+  if (L.n <= 0) return;
+  if (write_ft)
+    k_fused_forces<true><<<grid_for(L.n), kBlock, 0, L.st>>>(cur, out, d, nbr, cull, start, L.n);
+  else
+    k_fused_forces<false><<<grid_for(L.n), kBlock, 0, L.st>>>(cur, out, d, nbr, cull, start, L.n);
+}
+
+void launch_boundary(const Launch &L, Planes cur, DevScalars *d, int routine) {
+  if (L.n <= 0) return;
+  k_boundary<<<grid_for(L.n), kBlock, 0, L.st>>>(cur, d, routine, L.n);
+}
+
+void launch_part(const Launch &L, Planes cur, DevScalars *d, const NbrRec *nbr, const CullRec *cull,
+                 const int *start, int sph_id) {
+  if (L.n <= 0) return;
+  k_part<<<grid_for(L.n), kBlock, 0, L.st>>>(cur, d, nbr, cull, start, sph_id, L.n);
+}
+
+void launch_get_accel(const Launch &L, Planes cur, DevScalars *d) {
+  if (L.n <= 0) return;
+  k_get_accel<<<grid_for(L.n), kBlock, 0, L.st>>>(cur, d, L.n);
+}
+
+void launch_finish_verlet(const Launch &L, Planes cur, DevScalars *d) {
+  if (L.n <= 0) return;
+  k_finish_verlet<<<grid_for(L.n), kBlock, 0, L.st>>>(cur, d, L.n);
+}
+
+void launch_clear_forces(const Launch &L, Planes cur) {
+  if (L.n <= 0) return;
+  k_clear_forces<<<grid_for(L.n), kBlock, 0, L.st>>>(cur, L.n);
+}
+
+void launch_advance_time(cudaStream_t st, DevScalars *d) { k_advance_time<<<1, 1, 0, st>>>(d); }
+
+void launch_regrid(const Launch &L, Planes cur, DevScalars *d, long bucket_cap) {
+  k_bbox_init<<<1, 1, 0, L.st>>>(d);
+  if (L.n > 0) k_bbox_reduce<<<grid_for(L.n, 256), 256, 0, L.st>>>(cur, d, L.n);
+  k_grid_derive<<<1, 1, 0, L.st>>>(d, L.n, bucket_cap);
+}
+
+void launch_aos_to_planes(const Launch &L, const af3d_particle *aos, const double *acc,
+                          const double *anga, Planes cur, long long *id) {
+  if (L.n <= 0) return;
+  k_aos_to_planes<<<grid_for(L.n), kBlock, 0, L.st>>>(aos, acc, anga, cur, id, L.n);
+}
+
+void launch_planes_to_aos(const Launch &L, Planes cur, const long long *id, af3d_particle *aos,
+                          double *acc, double *anga, DevScalars *d) {
+  if (L.n <= 0) return;
+  k_planes_to_aos<<<grid_for(L.n), kBlock, 0, L.st>>>(cur, id, aos, acc, anga, d, L.n);
+}
+
+void launch_contact_pairs(const Launch &L, Planes cur, DevScalars *d, const NbrRec *nbr,
+                          const CullRec *cull, const int *start, const long long *id,
+                          long long *out, unsigned long long *count, long cap, int active) {
+  if (L.n <= 0) return;
+  k_contact_pairs<<<grid_for(L.n), kBlock, 0, L.st>>>(cur, d, nbr, cull, start, id, out, count, cap,
+                                                      active, L.n);
+}
+
+void launch_cells_by_id(const Launch &L, const int *key, const long long *id, long ncell3,
+                        long long *cell_of_id) {
+  if (L.n <= 0) return;
+  k_cells_by_id<<<grid_for(L.n), kBlock, 0, L.st>>>(key, id, ncell3, cell_of_id, L.n);
+}
+
+}  // namespace af3d

@@ -1,0 +1,351 @@
+// af3d_physics.cuh -- per-clump FP64 physics of the reference step, as device functions.
+//
+// Every expression keeps the reference's FP64 evaluation order, and the translation units that
+// include this header are compiled with -fmad=false, so a force, torque or acceleration computed
+// here is bit-identical to the reference host routine on the same input (+, -, *, / and sqrt are
+// correctly rounded on both sides).  Only init_Verlet's sin/cos come from CUDA's libm, which may
+// differ from the host libm in the last bit.
+#pragma once
+
+#include "af3d_internal.h"
+
+namespace af3d {
+
+// cabecera.hu:5-19
+constexpr double kPI = 3.1415926535897932;
+constexpr double kGRAV = 981.0;
+constexpr double kGYR = 4.4494897427831781;
+constexpr double kSPH_FACT = 4.188790204786391;
+constexpr double kROOT2 = 1.414213562373095;
+constexpr double kDRAG = 1.895e-3;
+constexpr double kHOP_HEIGHT = 25.0;
+constexpr double kHOP_WIDTH = 15.0;
+constexpr double kYFUNNEL = 30.0;
+constexpr double kLFUNNEL = 70.0;
+constexpr double kYHOP_L = 7.5;
+constexpr double kYHOP_R = 22.5;
+
+struct V3 {
+  double x, y, z;
+};
+
+__device__ __forceinline__ V3 mk(double x, double y, double z) {
+  V3 r;
+  r.x = x; r.y = y; r.z = z;
+  return r;
+}
+
+// Scalars of system_par / Funnel used by the force routines, loaded once per thread.
+struct Consts {
+  double dt, hdt, time, time_prev;
+  double mu_pp, kappa_pp, gamma_pp, cns_pp;
+  double mu_pw, kappa_pw, gamma_pw, cns_pw;
+  double sint, cost, dy2, side_x, side_y;
+  double sinfi, cosfi, tanfi;
+  int phase, variant;
+};
+
+__device__ __forceinline__ Consts load_consts(const DevScalars *d) {
+  Consts c;
+  const af3d_system_par &s = d->sys;
+  c.dt = s.dt; c.hdt = s.hdt; c.time = s.time; c.time_prev = d->time_prev;
+  c.mu_pp = s.mu_pp; c.kappa_pp = s.kappa_pp; c.gamma_pp = s.gamma_pp; c.cns_pp = s.fr_fact_pp;
+  c.mu_pw = s.mu_pw; c.kappa_pw = s.kappa_pw; c.gamma_pw = s.gamma_pw; c.cns_pw = s.fr_fact_pw;
+  c.sint = s.sint; c.cost = s.cost; c.dy2 = s.dy2; c.side_x = s.side.x; c.side_y = s.side.y;
+  c.sinfi = d->fun.sinfi; c.cosfi = d->fun.cosfi; c.tanfi = d->fun.tanfi;
+  c.phase = d->phase; c.variant = d->variant;
+  return c;
+}
+
+// time > 0 && x > side.x (init_Verlet.cu:29, cells.cu:65, force_part.cu:47, ...)
+__device__ __forceinline__ bool is_removed(double time, double x, double side_x) {
+  return time > 0.0 && x > side_x;
+}
+
+// Spring-dashpot normal force + Cundall-Strack tangential force with the Coulomb cap; the common
+// tail of every contact type (force_part.cu:189-241, force_walls.cu:123-177, ...).
+//   xi0:  Coulomb branch also when xi was zeroed (walls; DEV particle variant)
+//   gate: false -> proceed when normal > 0; true -> proceed unless normal <= 0 (fcorners)
+__device__ __forceinline__ bool contact_law(V3 dvvc, V3 n, double comp, double km, double gm,
+                                            double mass_t, double mu, double cns_1, double dt,
+                                            bool xi0, bool gate, V3 &f) {
+  double vn = dvvc.x * n.x + dvvc.y * n.y + dvvc.z * n.z;
+  V3 vt;
+  vt.x = dvvc.x - vn * n.x;
+  vt.y = dvvc.y - vn * n.y;
+  vt.z = dvvc.z - vn * n.z;
+  double vt_mag = sqrt(vt.x * vt.x + vt.y * vt.y + vt.z * vt.z);
+  V3 tv;
+  tv.x = vt.x / vt_mag;
+  tv.y = vt.y / vt_mag;
+  tv.z = vt.z / vt_mag;
+  double vt_sig = dvvc.x * tv.x + dvvc.y * tv.y + dvvc.z * tv.z;
+  double normal = km * comp + gm * (-vn);
+  if (gate ? (normal <= 0.0) : !(normal > 0.0)) return false;
+  f.x = -normal * n.x;
+  f.y = -normal * n.y;
+  f.z = -normal * n.z;
+  double xi = dt * vt_sig;
+  if (cns_1 * normal < fabs(xi)) xi = 0.0;
+  double xi_dot = xi / dt;
+  double fsdt = 1.0e12 * mass_t * xi + 2.0e6 * mass_t * xi_dot;
+  if (vt_mag > 0.0) {
+    if (fabs(fsdt) > mu * normal || (xi0 && xi == 0.0)) {
+      double af = 0.8 * mu * normal / vt_mag;
+      double t0 = mass_t / af;
+      af /= (1.0 + (dt / t0) * (dt / t0));
+      f.x += af * vt.x;
+      f.y += af * vt.y;
+      f.z += af * vt.z;
+    } else {
+      if (vt.x != 0.0) f.x += fsdt * vt.x / vt_mag;
+      if (vt.y != 0.0) f.y += fsdt * vt.y / vt_mag;
+      if (vt.z != 0.0) f.z += fsdt * vt.z / vt_mag;
+    }
+  }
+  return true;
+}
+
+// v + w x (c - r) in the reference's operand order (force_part.cu:175-177).
+__device__ __forceinline__ V3 point_velocity(V3 v, V3 w, V3 c, V3 r) {
+  V3 u;
+  u.x = v.x + w.y * (c.z - r.z) - w.z * (c.y - r.y);
+  u.y = v.y + w.z * (c.x - r.x) - w.x * (c.z - r.z);
+  u.z = v.z + w.x * (c.y - r.y) - w.y * (c.x - r.x);
+  return u;
+}
+
+// T += (c - r) x fs; F += fs (force_part.cu:245-251).
+__device__ __forceinline__ void accumulate(V3 &F, V3 &T, V3 fs, V3 c, V3 r) {
+  T.x += (c.y - r.y) * fs.z - (c.z - r.z) * fs.y;
+  T.y += (c.z - r.z) * fs.x - (c.x - r.x) * fs.z;
+  T.z += (c.x - r.x) * fs.y - (c.y - r.y) * fs.x;
+  F.x += fs.x;
+  F.y += fs.y;
+  F.z += fs.z;
+}
+
+// The own clump as the force routines see it.
+struct Own {
+  V3 r, v, w;
+  V3 s[4];
+  double rad, mwall, msph;
+};
+
+__device__ __forceinline__ bool wall_contact(const Own &o, V3 rrc, V3 n, double comp, double km,
+                                             double gm, const Consts &c, bool gate, V3 &F, V3 &T) {
+  V3 vvc = point_velocity(o.v, o.w, rrc, o.r);
+  V3 dvvc = mk(-vvc.x, -vvc.y, -vvc.z);
+  V3 fs;
+  if (!contact_law(dvvc, n, comp, km, gm, o.mwall, c.mu_pw, c.cns_pw, c.dt, true, gate, fs))
+    return false;
+  accumulate(F, T, fs, rrc, o.r);
+  return true;
+}
+
+// rotate_vectors.cu:28-30 (lab -> slope frame) and force_funnel.cu:88-93 (slope -> lab).
+__device__ __forceinline__ V3 to_slope(V3 r, double cost, double sint) {
+  return mk(r.x * cost - r.z * sint, r.y, r.x * sint + r.z * cost);
+}
+__device__ __forceinline__ V3 to_lab(V3 q, double cost, double sint) {
+  return mk(q.x * cost + q.z * sint, q.y, q.z * cost - q.x * sint);
+}
+
+// force_hop.cu:9-244 for one wall group nw.
+__device__ __forceinline__ void bnd_hop(const Own &o, int nw, const Consts &c, V3 &F, V3 &T) {
+  const double ri = o.rad, km = 0.5 * c.kappa_pw * o.mwall, gm = 0.5 * c.gamma_pw * o.mwall;
+#pragma unroll 1
+  for (int ns = 0; ns < 4; ns++) {
+    V3 s = o.s[ns], rrc, n;
+    double dist, comp = 0.0;
+    int touch = 0;
+    if (s.z < kHOP_HEIGHT || s.x > kHOP_WIDTH) continue;
+    if (nw == 0) {
+      dist = s.x - 0.0;
+      if (dist <= ri) { touch = 1; rrc = mk(0.0, s.y, s.z); n = mk(-1.0, 0.0, 0.0); comp = ri - dist; }
+      dist = kHOP_WIDTH - s.x;
+      if (dist <= ri) { touch = 2; rrc = mk(kHOP_WIDTH, s.y, s.z); n = mk(1.0, 0.0, 0.0); comp = ri - dist; }
+    } else if (nw == 1) {
+      dist = s.y - kYHOP_L;
+      if (dist <= ri) { touch = 3; rrc = mk(s.x, kYHOP_L, s.z); n = mk(0.0, -1.0, 0.0); comp = ri - dist; }
+      dist = kYHOP_R - s.y;
+      if (dist <= ri) { touch = 4; rrc = mk(s.x, kYHOP_R, s.z); n = mk(0.0, 1.0, 0.0); comp = ri - dist; }
+    } else {
+      dist = s.z - kHOP_HEIGHT;
+      if (dist <= ri) {
+        touch = c.time < 0.0 ? 5 : 0;   // the door is open once time >= 0 (force_hop.cu:140-143)
+        rrc = mk(s.x, s.y, kHOP_HEIGHT); n = mk(0.0, 0.0, -1.0); comp = ri - dist;
+      }
+    }
+    if (touch) wall_contact(o, rrc, n, comp, km, gm, c, false, F, T);
+  }
+}
+
+// force_funnel.cu:9-213
+__device__ __forceinline__ void bnd_funnel(const Own &o, const Consts &c, V3 &F, V3 &T) {
+  const double ri = o.rad, km = 0.5 * c.kappa_pw * o.mwall, gm = 0.5 * c.gamma_pw * o.mwall;
+#pragma unroll 1
+  for (int ns = 0; ns < 4; ns++) {
+    V3 q = to_slope(o.s[ns], c.cost, c.sint), qc, nr, rrc, n;
+    double dist, comp = 0.0;
+    int touch = 0;
+    if (q.x > kLFUNNEL - ri * c.sinfi) continue;
+    dist = fabs(q.y - q.x * c.tanfi) * c.cosfi;
+    if (dist <= ri) {
+      touch = 1;
+      qc = mk(q.x + dist * c.sinfi, q.y - dist * c.cosfi, q.z);
+      nr = mk(c.sinfi, -c.cosfi, 0.0);
+      rrc = to_lab(qc, c.cost, c.sint);
+      n = to_lab(nr, c.cost, c.sint);
+      comp = ri - dist;
+    }
+    dist = fabs(kYFUNNEL - q.y - q.x * c.tanfi) * c.cosfi;
+    if (dist <= ri) {
+      touch = 2;
+      qc = mk(q.x + dist * c.sinfi, q.y + dist * c.cosfi, q.z);
+      nr = mk(c.sinfi, c.cosfi, 0.0);
+      rrc = to_lab(qc, c.cost, c.sint);
+      n = to_lab(nr, c.cost, c.sint);
+      comp = ri - dist;
+    }
+    if (touch) wall_contact(o, rrc, n, comp, km, gm, c, false, F, T);
+  }
+}
+
+// force_funnel.cu:216-404
+__device__ __forceinline__ void bnd_fcorners(const Own &o, const Consts &c, V3 &F, V3 &T) {
+  const double ri = o.rad, km = 0.5 * c.kappa_pw * o.mwall, gm = 0.5 * c.gamma_pw * o.mwall;
+  const double yfun_l = c.dy2, yfun_r = c.side_y + c.dy2, hsy = c.dy2 + c.side_y / 2.0;
+#pragma unroll 1
+  for (int ns = 0; ns < 4; ns++) {
+    V3 q = to_slope(o.s[ns], c.cost, c.sint);
+    if (q.x < kLFUNNEL - ri * c.sinfi || q.x > kLFUNNEL + ri) continue;
+    if (q.y > yfun_r || q.y < yfun_l) continue;
+    double yc = (q.y <= hsy) ? yfun_l : yfun_r;
+    double sep2 = ri * ri;
+    V3 d;
+    d.x = kLFUNNEL - q.x;
+    double dist2 = d.x * d.x;
+    if (dist2 > sep2) continue;
+    d.y = yc - q.y;
+    dist2 += d.y * d.y;
+    if (dist2 > sep2) continue;
+    double dist = sqrt(dist2);
+    V3 nr = mk(d.x / dist, d.y / dist, 0.0);
+    V3 qc = mk(q.x + ri * nr.x, q.y + ri * nr.y, q.z);
+    wall_contact(o, to_lab(qc, c.cost, c.sint), to_lab(nr, c.cost, c.sint), ri - dist, km, gm, c,
+                 true, F, T);
+  }
+}
+
+// force_walls.cu:9-199 (caller skips removed clumps)
+__device__ __forceinline__ void bnd_walls(const Own &o, const Consts &c, V3 &F, V3 &T) {
+  const double ri = o.rad, km = 0.5 * c.kappa_pw * o.mwall, gm = 0.5 * c.gamma_pw * o.mwall;
+  const double yleft = c.dy2, yright = c.side_y + c.dy2;
+#pragma unroll 1
+  for (int ns = 0; ns < 4; ns++) {
+    V3 s = o.s[ns], rrc, n;
+    if (to_slope(s, c.cost, c.sint).x <= kLFUNNEL) continue;
+    double dist, comp = 0.0;
+    int touch = 0;
+    dist = s.y - yleft;
+    if (dist <= ri) { touch = 1; rrc = mk(s.x, yleft, s.z); n = mk(0.0, -1.0, 0.0); comp = ri - dist; }
+    dist = yright - s.y;
+    if (dist <= ri) { touch = 2; rrc = mk(s.x, yright, s.z); n = mk(0.0, 1.0, 0.0); comp = ri - dist; }
+    if (touch) wall_contact(o, rrc, n, comp, km, gm, c, false, F, T);
+  }
+}
+
+// force_flume.cu:10-182 (caller skips removed clumps)
+__device__ __forceinline__ void bnd_flume(const Own &o, const Consts &c, V3 &F, V3 &T) {
+  const double ri = o.rad, km = 0.5 * c.kappa_pw * o.mwall, gm = 0.5 * c.gamma_pw * o.mwall;
+  const double tant = c.sint / c.cost;
+  const V3 n = mk(-c.sint, 0.0, -c.cost);
+#pragma unroll 1
+  for (int ns = 0; ns < 4; ns++) {
+    V3 s = o.s[ns];
+    double rect = -tant * s.x - s.z;
+    double dist = fabs(c.cost * rect);
+    if (dist <= ri) {
+      V3 rrc = mk(s.x - dist * c.sint, s.y, s.z - dist * c.cost);
+      wall_contact(o, rrc, n, ri - dist, km, gm, c, false, F, T);
+    }
+  }
+}
+
+// Apply one boundary routine with the reference's removed-clump rule for that routine.
+__device__ __forceinline__ void bnd_routine(int routine, const Own &o, bool removed, const Consts &c,
+                                            V3 &F, V3 &T) {
+  switch (routine) {
+    case R_HOP0: bnd_hop(o, 0, c, F, T); break;
+    case R_HOP1: bnd_hop(o, 1, c, F, T); break;
+    case R_HOP2: bnd_hop(o, 2, c, F, T); break;
+    case R_FUNNEL: bnd_funnel(o, c, F, T); break;
+    case R_FCORNERS: bnd_fcorners(o, c, F, T); break;
+    case R_WALLS: if (!removed) bnd_walls(o, c, F, T); break;
+    case R_FLUME: if (!removed) bnd_flume(o, c, F, T); break;
+  }
+}
+
+// One sphere-sphere contact of force_part.cu:139-252: own sphere s1 (clump centre rrl), partner
+// record m, partner sphere sm.  Returns 1 when the pair overlaps, 2 when it also exerts a force.
+__device__ __forceinline__ int part_pair(const V3 &rrl, const V3 &vvl, const V3 &wwl, const V3 &s1,
+                                         double rad_1, double massl, const NbrRec &m, int sm,
+                                         const Consts &c, bool xi0, V3 &F, V3 &T) {
+  const double rad_2 = m.rad;
+  const double sep = rad_1 + rad_2;
+  const double sep2 = sep * sep;
+  V3 d;
+  d.x = m.s[3 * sm] - s1.x;
+  double dist2 = d.x * d.x;
+  if (!(dist2 < sep2)) return 0;
+  d.y = m.s[3 * sm + 1] - s1.y;
+  dist2 += d.y * d.y;
+  if (!(dist2 < sep2)) return 0;
+  d.z = m.s[3 * sm + 2] - s1.z;
+  dist2 += d.z * d.z;
+  if (!(dist2 < sep2)) return 0;
+  const double meff = 0.5 * (m.msph + massl);
+  const double km = 0.5 * c.kappa_pp * meff;
+  const double gm = 0.5 * c.gamma_pp * meff;
+  const double dist = sqrt(dist2);
+  V3 n = mk(d.x / dist, d.y / dist, d.z / dist);
+  V3 rrc = mk(s1.x + rad_1 * n.x, s1.y + rad_1 * n.y, s1.z + rad_1 * n.z);
+  V3 vl = point_velocity(vvl, wwl, rrc, rrl);
+  V3 vm = point_velocity(mk(m.vx, m.vy, m.vz), mk(m.wx, m.wy, m.wz), rrc, mk(m.rx, m.ry, m.rz));
+  V3 dvvc = mk(vm.x - vl.x, vm.y - vl.y, vm.z - vl.z);
+  V3 fs;
+  if (!contact_law(dvvc, n, sep - dist, km, gm, massl, c.mu_pp, c.cns_pp, c.dt, xi0, false, fs))
+    return 1;
+  accumulate(F, T, fs, rrc, rrl);
+  return 2;
+}
+
+// get_accel.cu:21-75 for one clump; R rows Rx, Ry, Rz.
+__device__ __forceinline__ void get_accel_one(V3 f, V3 t, V3 v, V3 w, V3 Rx, V3 Ry, V3 Rz, double m,
+                                              double rad, V3 I, V3 &a, V3 &al) {
+  double Cxy = (I.x - I.y) / I.z;
+  double Cyz = (I.y - I.z) / I.x;
+  double Czx = (I.z - I.x) / I.y;
+  double adrag = kDRAG * rad * rad / m;
+  double vmag = sqrt(v.x * v.x + v.y * v.y + v.z * v.z);
+  adrag *= vmag;
+  a.x = f.x / m - adrag * v.x;
+  a.y = f.y / m - adrag * v.y;
+  a.z = f.z / m - adrag * v.z - kGRAV;
+  V3 wb, tb, ab;
+  wb.x = w.x * Rx.x + w.y * Ry.x + w.z * Rz.x;
+  wb.y = w.x * Rx.y + w.y * Ry.y + w.z * Rz.y;
+  wb.z = w.x * Rx.z + w.y * Ry.z + w.z * Rz.z;
+  tb.x = t.x * Rx.x + t.y * Ry.x + t.z * Rz.x;
+  tb.y = t.x * Rx.y + t.y * Ry.y + t.z * Rz.y;
+  tb.z = t.x * Rx.z + t.y * Ry.z + t.z * Rz.z;
+  ab.x = tb.x / I.x + Cyz * wb.y * wb.z;
+  ab.y = tb.y / I.y + Czx * wb.z * wb.x;
+  ab.z = tb.z / I.z + Cxy * wb.x * wb.y;
+  al.x = ab.x * Rx.x + ab.y * Rx.y + ab.z * Rx.z;
+  al.y = ab.x * Ry.x + ab.y * Ry.y + ab.z * Ry.z;
+  al.z = ab.x * Rz.x + ab.y * Rz.y + ab.z * Rz.z;
+}
+
+}  // namespace af3d

@@ -1,0 +1,271 @@
+"""Host-side mirror of the reference's step interface over the C ABI (include/af3d.h).
+
+``Engine`` holds one device-resident context.  Its methods are named after the reference's
+routines and keep their argument meaning (system_par / Funnel / particle / cell_par as numpy
+structured scalars and arrays with the reference's binary layout); the step loop of
+avalanche_hst.cu:668-710 reads::
+
+    eng.init_verlet(); eng.advance_time(); eng.rotate_vectors(); eng.clear_forces()
+    eng.cell_build()
+    for nw in range(3): eng.force_hop(nw)
+    eng.force_funnel(); eng.force_fcorners(); eng.force_walls()
+    eng.force_part(0)            # all sixteen sph_id passes in one call
+    eng.force_flume(); eng.get_accel(); eng.finish_verlet(); eng.swap_accel()
+
+or, fused and graph-captured, ``eng.step(k)``.  Errors raise :class:`EngineError` with the
+AF3D_ERR_* code; there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from ._lib import (CELL_PAR, FRICTION_HST, FUNNEL, INPUTS, PARTICLE, PHASE_AVALANCHE, RNG,
+                   SYSTEM_PAR, EngineError, Vec3, check, lib, ptr)
+
+
+def _vec3(n: int) -> np.ndarray:
+    return np.zeros((n, 3), dtype=np.float64)
+
+
+class Engine:
+    """One simulation context on the current CUDA device."""
+
+    def __init__(self, sys: np.ndarray, fun: np.ndarray, ntags: int = 9, phase: int = PHASE_AVALANCHE,
+                 friction: int = FRICTION_HST, stream: int | None = None):
+        L = lib()
+        self._L = L
+        self.sys = np.array(sys, dtype=SYSTEM_PAR).copy()
+        self.fun = np.array(fun, dtype=FUNNEL).copy()
+        self.n = int(self.sys["npart"])
+        h = C.c_void_p()
+        check(L.af3d_create(ptr(self.sys.reshape(1)), ptr(self.fun.reshape(1)), int(ntags), int(phase),
+                            C.byref(h)), "af3d_create")
+        self._h = h
+        if friction != FRICTION_HST:
+            self.set_friction(friction)
+        if stream:
+            check(L.af3d_set_stream(h, C.c_void_p(stream)), "af3d_set_stream")
+
+    # ---- lifetime ----
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._L.af3d_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _call(self, name: str, *args) -> None:
+        check(getattr(self._L, name)(self._h, *args), name)
+
+    # ---- state in/out ----
+    def import_particles(self, pp: np.ndarray, acc: np.ndarray | None = None,
+                         anga: np.ndarray | None = None) -> None:
+        pp = np.ascontiguousarray(pp, dtype=PARTICLE)
+        assert pp.shape == (self.n,)
+        a = None if acc is None else np.ascontiguousarray(acc, dtype=np.float64)
+        al = None if anga is None else np.ascontiguousarray(anga, dtype=np.float64)
+        self._call("af3d_import_particles", ptr(pp), ptr(a), ptr(al))
+
+    def export_particles(self, with_accel: bool = True):
+        pp = np.zeros(self.n, dtype=PARTICLE)
+        a = _vec3(self.n) if with_accel else None
+        al = _vec3(self.n) if with_accel else None
+        self._call("af3d_export_particles", ptr(pp), ptr(a), ptr(al))
+        return (pp, a, al) if with_accel else pp
+
+    def set_system(self, sys: np.ndarray) -> None:
+        self.sys = np.array(sys, dtype=SYSTEM_PAR).copy()
+        self._call("af3d_set_system", ptr(self.sys.reshape(1)))
+
+    def get_system(self) -> np.ndarray:
+        s = np.zeros(1, dtype=SYSTEM_PAR)
+        self._call("af3d_get_system", ptr(s))
+        self.sys = s[0].copy()
+        return self.sys
+
+    def set_grid(self, cell: np.ndarray) -> None:
+        c = np.array(cell, dtype=CELL_PAR).reshape(1).copy()
+        self._call("af3d_set_grid", ptr(c))
+
+    def get_grid(self) -> np.ndarray:
+        c = np.zeros(1, dtype=CELL_PAR)
+        self._call("af3d_get_grid", ptr(c))
+        return c[0].copy()
+
+    def set_friction(self, variant: int) -> None:
+        self._call("af3d_set_friction", int(variant))
+
+    def set_phase(self, phase: int) -> None:
+        self._call("af3d_set_phase", int(phase))
+
+    def regrid(self) -> None:
+        self._call("af3d_regrid")
+
+    def open_door(self) -> None:
+        self._call("af3d_open_door")
+
+    # ---- one call per reference routine ----
+    def init_verlet(self): self._call("af3d_init_verlet")
+    def advance_time(self): self._call("af3d_advance_time")
+    def rotate_vectors(self): self._call("af3d_rotate_vectors")
+    def clear_forces(self): self._call("af3d_clear_forces")
+    def cell_build(self): self._call("af3d_cell_build")
+    def force_hop(self, nw: int): self._call("af3d_force_hop", int(nw))
+    def force_funnel(self): self._call("af3d_force_funnel")
+    def force_fcorners(self): self._call("af3d_force_fcorners")
+    def force_walls(self): self._call("af3d_force_walls")
+    def force_part(self, sph_id: int = 0): self._call("af3d_force_part", int(sph_id))
+    def force_flume(self): self._call("af3d_force_flume")
+    def get_accel(self): self._call("af3d_get_accel")
+    def finish_verlet(self): self._call("af3d_finish_verlet")
+    def swap_accel(self): self._call("af3d_swap_accel")
+
+    # ---- fused paths ----
+    def forces(self) -> None:
+        """clear_forces + cells + every force routine of the phase + get_accel (into a_f)."""
+        self._call("af3d_forces")
+
+    def step(self, k: int = 1) -> None:
+        """k fused steps of the current phase (CUDA-graph replay, re-grid every 2000 steps)."""
+        self._call("af3d_step", int(k))
+
+    # ---- diagnostics (indexed by clump id) ----
+    def status(self) -> int:
+        f = C.c_int()
+        self._call("af3d_get_status", C.byref(f))
+        return f.value
+
+    def get_forces(self):
+        F, T = _vec3(self.n), _vec3(self.n)
+        self._call("af3d_get_forces", ptr(F), ptr(T))
+        return F, T
+
+    def get_accels(self):
+        a, al = _vec3(self.n), _vec3(self.n)
+        self._call("af3d_get_accels", ptr(a), ptr(al))
+        return a, al
+
+    def get_cells(self):
+        """(cell of every clump or -1, (cell, id)-sorted ids of the binned clumps)."""
+        cell = np.zeros(self.n, dtype=np.int64)
+        ids = np.zeros(self.n, dtype=np.int64)
+        nb = C.c_long()
+        self._call("af3d_get_cells", ptr(cell), ptr(ids), C.byref(nb))
+        return cell, ids[:nb.value].copy()
+
+    def contact_pairs(self, active: bool = False) -> np.ndarray:
+        cap = max(1024, 64 * self.n)
+        while True:
+            out = np.zeros((cap, 3), dtype=np.int64)
+            cnt = C.c_long()
+            self._call("af3d_contact_pairs", ptr(out), cap, C.byref(cnt), int(bool(active)))
+            if cnt.value <= cap:
+                return out[:cnt.value].copy()
+            cap = cnt.value
+
+    def contact_count(self) -> int:
+        c = C.c_long()
+        self._call("af3d_contact_count", C.byref(c))
+        return c.value
+
+
+# ---- host I/O and generators (no GPU) ----
+
+def load_datainput(path: str) -> np.ndarray:
+    v = np.zeros(1, dtype=INPUTS)
+    check(lib().af3d_load_datainput(path.encode(), ptr(v)), "af3d_load_datainput")
+    return v[0].copy()
+
+
+def derive_system(inputs: np.ndarray):
+    s = np.zeros(1, dtype=SYSTEM_PAR)
+    f = np.zeros(1, dtype=FUNNEL)
+    v = np.array(inputs, dtype=INPUTS).reshape(1)
+    check(lib().af3d_derive_system(ptr(v), ptr(s), ptr(f)), "af3d_derive_system")
+    return s[0].copy(), f[0].copy()
+
+
+def error_check(sys: np.ndarray) -> tuple[int, str]:
+    buf = C.create_string_buffer(512)
+    s = np.array(sys, dtype=SYSTEM_PAR).reshape(1)
+    n = lib().af3d_error_check(ptr(s), buf, 512)
+    return n, buf.value.decode()
+
+
+def write_last_config(path: str, pp: np.ndarray, aval_start: int, time: float, cc: int, jj: int):
+    pp = np.ascontiguousarray(pp, dtype=PARTICLE)
+    check(lib().af3d_write_last_config(path.encode(), int(aval_start), float(time), int(cc), int(jj),
+                                       ptr(pp), len(pp)), "af3d_write_last_config")
+
+
+def read_last_config(path: str, pp: np.ndarray):
+    """Fill rr, R, vv, ww (and the sphere centres) of ``pp`` in place; returns the header."""
+    a, cc, jj = C.c_int(), C.c_long(), C.c_long()
+    t = C.c_double()
+    check(lib().af3d_read_last_config(path.encode(), C.byref(a), C.byref(t), C.byref(cc), C.byref(jj),
+                                      ptr(pp), len(pp)), "af3d_read_last_config")
+    return a.value, t.value, cc.value, jj.value
+
+
+class Rannew64:
+    """The reference's rannew64 generator (rannew64.cu:55) with explicit state."""
+
+    def __init__(self, idum: int):
+        self._s = RNG()
+        lib().af3d_rng_seed(C.byref(self._s), int(idum))
+
+    def __call__(self) -> float:
+        return lib().af3d_rng_next(C.byref(self._s))
+
+    @property
+    def ref(self):
+        return C.byref(self._s)
+
+
+def generate_particles(sys: np.ndarray) -> np.ndarray:
+    n = int(sys["npart"])
+    pp = np.zeros(n, dtype=PARTICLE)
+    s = np.array(sys, dtype=SYSTEM_PAR).reshape(1)
+    lib().af3d_generate_particles(ptr(pp), ptr(s))
+    return pp
+
+
+def calculate_particle_parameters(pp: np.ndarray) -> None:
+    lib().af3d_calculate_particle_parameters(ptr(pp), len(pp))
+
+
+def place_particles(sys: np.ndarray, pp: np.ndarray) -> None:
+    s = np.array(sys, dtype=SYSTEM_PAR).reshape(1)
+    check(lib().af3d_place_particles(ptr(s), ptr(pp)), "af3d_place_particles")
+
+
+def set_initial_velocity(sys: np.ndarray, pp: np.ndarray) -> None:
+    s = np.array(sys, dtype=SYSTEM_PAR).reshape(1)
+    lib().af3d_set_initial_velocity(ptr(s), ptr(pp))
+
+
+def sphere_centres(pp: np.ndarray) -> None:
+    lib().af3d_sphere_centres(ptr(pp), len(pp))
+
+
+def lattice_block(pp: np.ndarray, lo, hi, pitch: float, rng: Rannew64, max_tries: int = 64) -> int:
+    return int(lib().af3d_lattice_block(ptr(pp), len(pp), Vec3(*lo), Vec3(*hi), float(pitch), rng.ref,
+                                        int(max_tries)))
+
+
+__all__ = ["Engine", "EngineError", "load_datainput", "derive_system", "error_check",
+           "write_last_config", "read_last_config", "Rannew64", "generate_particles",
+           "calculate_particle_parameters", "place_particles", "set_initial_velocity",
+           "sphere_centres", "lattice_block"]

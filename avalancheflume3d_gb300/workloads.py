@@ -1,0 +1,103 @@
+"""Synthetic flume workloads in the reference's cgs units.
+
+The benchmark configurations are stated in SI with a linear spring constant kn; the reference
+parameterises its contact law by a collision time t_coll instead (avalanche_hst.cu:187-193,
+stiffness per sphere contact 0.5*kappa*m_eff, force_part.cu:121).  The mapping used here:
+
+    m_s     = (4/3) pi rho r^3                       sphere mass
+    kappa   = 2 kn / m_s                             so that 0.5*kappa*m_s = kn
+    t_coll  = sqrt((pi^2 + ln(e)^2) / kappa)         DataInput.dat line 12
+
+One t_coll serves particle-particle and particle-wall contacts, as in the reference.  Clumps are
+the reference's tetrahedral 4-sphere clumps (edge 2r, init_Verlet.cu:130-142).
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass
+
+import numpy as np
+
+from ._lib import INPUTS, PARTICLE
+from .engine import Rannew64, calculate_particle_parameters, derive_system, lattice_block, set_initial_velocity
+
+HOP_WIDTH, HOP_HEIGHT, YHOP_L, YHOP_R = 15.0, 25.0, 7.5, 22.5
+
+
+@dataclass
+class FlumeConfig:
+    """One flume run: geometry, material and the lattice release block (cgs units)."""
+    n: int
+    tilt_deg: float = 35.0
+    width: float = 20.0          # flume width side.y [cm]
+    Lflume: float = 200.0        # flume length [cm]
+    radius: float = 0.1          # sphere radius [cm]
+    density: float = 2.5         # [g/cm^3]
+    kn: float = 1.0e7            # linear spring constant [dyn/cm] (1e4 N/m)
+    restitution: float = 0.5
+    mu_pp: float = 0.5
+    mu_pw: float = 0.4
+    dt: float = 2.0e-6
+    pitch: float = 0.4           # lattice pitch of the release block [cm]
+    v0: float = 0.0              # initial speed in the reference's random directions
+    seed: int = 20240613         # rannew64 seed of the orientations
+    hopper_height: float | None = None
+
+    @property
+    def t_coll(self) -> float:
+        m_s = 4.0 / 3.0 * math.pi * self.radius ** 3 * self.density
+        kappa = 2.0 * self.kn / m_s
+        return math.sqrt((math.pi ** 2 + math.log(self.restitution) ** 2) / kappa)
+
+
+def flume_inputs(cfg: FlumeConfig) -> np.ndarray:
+    """The 16 DataInput.dat values of a configuration."""
+    per_layer = int(HOP_WIDTH // cfg.pitch) ** 2
+    layers = -(-cfg.n // per_layer)
+    height = cfg.hopper_height if cfg.hopper_height is not None else layers * cfg.pitch + 1.0
+    v = np.zeros((), dtype=INPUTS)
+    v["npart"] = cfg.n
+    v["width"], v["hopper_height"] = cfg.width, height
+    v["rmin"] = v["rmax"] = cfg.radius
+    v["v0"], v["dt"] = cfg.v0, cfg.dt
+    v["eps_pw"] = v["eps_pp"] = cfg.restitution
+    v["mu_pw"], v["mu_pp"] = cfg.mu_pw, cfg.mu_pp
+    v["t_coll"], v["Lflume"], v["tilt_deg"] = cfg.t_coll, cfg.Lflume, cfg.tilt_deg
+    v["ntags"], v["print_flag"] = 9, 0
+    return v
+
+
+def flume_state(cfg: FlumeConfig):
+    """(system_par, Funnel, particle array) of a lattice block released in the open hopper at
+    time 0 (avalanche phase: side.x = xfinal, avalanche_hst.cu:607-613).
+
+    Clumps sit on a cubic lattice of the given pitch inside the hopper box x in [0, 15],
+    y in [7.5, 22.5], z > 25, each with a uniformly random orientation (Shoemake quaternion from
+    rannew64); orientations that would overlap a placed neighbour or a hopper wall are redrawn.
+    With v0 > 0 the velocities follow the reference's set_initial_velocity (seed 26752658)."""
+    sys, fun = derive_system(flume_inputs(cfg))
+    sys["time"] = 0.0
+    sys["side"][0] = (70.0 + cfg.Lflume) * float(sys["cost"])
+    pp = np.zeros(cfg.n, dtype=PARTICLE)
+    pp["radius"] = cfg.radius
+    pp["density"] = cfg.density
+    calculate_particle_parameters(pp)
+    rng = Rannew64(cfg.seed)
+    top = HOP_HEIGHT + float(sys["side"][2])
+    placed = lattice_block(pp, (0.0, YHOP_L, HOP_HEIGHT), (HOP_WIDTH, YHOP_R, top), cfg.pitch, rng)
+    if placed != cfg.n:
+        raise ValueError("lattice block holds %d of %d clumps" % (placed, cfg.n))
+    if cfg.v0 > 0:
+        set_initial_velocity(sys, pp)
+    sys["tot_mass"] = float(pp["mass"].sum())
+    return sys, fun, pp
+
+
+# The benchmark configurations (cgs).  FLUME_2K: 2,048 clumps, 30 deg, 40 cm x 4 cm flume;
+# FLUME_262K: 262,144 clumps, 35 deg, 200 cm x 20 cm flume.
+def flume_2k(**kw) -> FlumeConfig:
+    return FlumeConfig(n=2048, tilt_deg=30.0, width=4.0, Lflume=40.0, **kw)
+
+
+def flume_262k(**kw) -> FlumeConfig:
+    return FlumeConfig(n=262144, tilt_deg=35.0, width=20.0, Lflume=200.0, **kw)

@@ -1,0 +1,362 @@
+#!/usr/bin/env python3
+"""Benchmark: clump-steps/s of the fused clump-DEM step on one GB300 (or N replicas).
+
+Workload ``flume262k`` (the 262,144-clump configuration): tetrahedral 4-sphere clumps, sphere
+radius 1 mm, density 2.5 g/cm^3, kn = 1e4 N/m (t_coll from the reference's law), restitution 0.5,
+mu_pp = 0.5, mu_wall = 0.4, flume 2.0 m x 0.2 m at 35 deg, dt = 2e-6 s, FP64.  The clumps start on
+a 4 mm cubic lattice in the open hopper with uniformly random orientations and the reference's
+random initial velocities (v0 = 10 cm/s, set_initial_velocity.cu), and are released for a pre-roll
+of P steps (untimed, part of the input) so that the timed window sees a colliding granular state
+rather than a lattice at rest.  Synthetic data; the state (~400 MB) is larger than L2.
+
+Timed: exactly K fused steps (graph replays, af3d_step) after W warm-up steps, CUDA events on
+the engine's stream, barrier + synchronize on both sides, max over ranks.  Then, outside the
+timed region: a profiled pass (CUDA events between the kernels) for the roofline of the dominant
+kernel, the end-to-end figure through the C ABI with host buffers, and the CPU baseline.
+
+``--impl reference`` times the reference's CPU implementation of the step (the oracle port of
+the reference's host routines, all host threads) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "clump-steps/s"
+# Algorithmic HBM bytes of one step: 448 B per clump (state read 192 + constants 32 + state
+# write 192 + cell-list traffic 32) plus 8 B per cell.
+BYTES_PER_CLUMP = 448
+BYTES_PER_CELL = 8
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", choices=["engine", "reference"], default="engine")
+    p.add_argument("--n", type=int, default=262144, help="clumps (262144 = the benchmark config)")
+    p.add_argument("--preroll", type=int, default=1000, help="untimed release steps of the input")
+    p.add_argument("--v0", type=float, default=10.0)
+    p.add_argument("--profile-steps", type=int, default=10)
+    p.add_argument("--e2e-steps", type=int, default=5)
+    p.add_argument("--cpu-sample", type=int, default=16384, help="clumps in the CPU baseline sample")
+    p.add_argument("--cpu-seconds", type=float, default=10.0)
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--trace-contacts", type=int, default=0,
+                   help="print active contacts every this many pre-roll steps (diagnostic)")
+    return p.parse_args()
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def workload(args):
+    from avalancheflume3d_gb300.workloads import flume_262k, flume_state
+    cfg = flume_262k(n=args.n, v0=args.v0)
+    return cfg, flume_state(cfg)
+
+
+def config_dict(args, cfg, extra=None):
+    d = {"workload": "flume262k" if args.n == 262144 else "flume%d" % args.n,
+         "clumps": args.n, "spheres": 4 * args.n, "tilt_deg": cfg.tilt_deg, "flume_m": cfg.Lflume / 100,
+         "width_m": cfg.width / 100, "dt_s": cfg.dt, "lattice_mm": cfg.pitch * 10, "v0_cm_s": args.v0,
+         "preroll_steps": args.preroll, "friction": "host (force_part.cu:224)",
+         "l2": "state larger than L2 (no flush needed)"}
+    if extra:
+        d.update(extra)
+    return d
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    def __init__(self, index: int):
+        self.fn = tempfile.NamedTemporaryFile(prefix="af3d_clocks_", suffix=".csv", delete=False).name
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(index), "--query-gpu=" + q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=open(self.fn, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        rows = []
+        for line in open(self.fn):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9 and f[1].replace(".", "").isdigit():
+                rows.append(f)
+        os.unlink(self.fn)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(float(r[1]) for r in rows),
+                "sm_max_mhz": max(float(r[2]) for r in rows), "reasons": reasons,
+                "samples": len(rows)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def traffic_from_profile():
+    """DRAM bytes per launch of the fused force kernel from the committed ncu summary, if any."""
+    fn = os.path.join(ROOT, "profiles", "fused_forces_flume262k.txt")
+    try:
+        for line in open(fn):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+def cpu_sample_state(cfg, sys_, fun, pp, m):
+    """The first m clumps of the workload (the bottom layers of the block) as their own system."""
+    from oracle.pyoracle import SYSTEM_PAR
+    s = np.array(sys_, dtype=SYSTEM_PAR).copy()
+    s["npart"] = m
+    return s, fun, np.ascontiguousarray(pp[:m]).copy()
+
+
+def time_cpu(sys_, fun, pp, threads, seconds, acc=None, anga=None, min_steps=2, max_steps=10 ** 6):
+    """Steps of the oracle port (the reference's host routines restated in C) timed on the host."""
+    from oracle.pyoracle import Oracle, OracleRun
+    o = Oracle()
+    o.set_threads(threads)
+    run = OracleRun(o, sys_, fun, pp, acc=acc, anga=anga)
+    if acc is None:
+        run.seed_accel()
+    t0 = time.perf_counter()
+    k = 0
+    while k < max_steps and (k < min_steps or time.perf_counter() - t0 < seconds):
+        st = run.step(1, cc0=k)
+        if st:
+            raise RuntimeError("oracle step failed with status %d" % st)
+        k += 1
+    dt = time.perf_counter() - t0
+    return len(pp) * k / dt, k, dt
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    cfg, (sys_, fun, pp) = workload(args)
+    m = min(args.n, max(args.cpu_sample, 65536))
+    s, f, q = cpu_sample_state(cfg, sys_, fun, pp, m)
+    from oracle.pyoracle import Oracle, OracleRun
+    o = Oracle()
+    o.set_threads(threads)
+    run = OracleRun(o, s, f, q)
+    run.seed_accel()
+    pre = min(args.preroll, 200)
+    run.step(pre, cc0=0)
+    run.step(args.warmup, cc0=pre)
+    t0 = time.perf_counter()
+    run.step(args.steps, cc0=pre + args.warmup)
+    dt = time.perf_counter() - t0
+    value = m * args.steps / dt
+    sample = ("first %d clumps of the workload (bottom lattice layers) as their own system, %d release "
+              "steps, then %d timed steps" % (m, pre, args.steps))
+    line = {"metric": METRIC, "value": value, "unit": "clump-steps/s", "impl": "reference",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 * dt / args.steps * (args.n / m), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config_dict(args, cfg, {"cpu_threads": threads}),
+            "cpu_baseline": {"value": value, "unit": "clump-steps/s", "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "clump-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_engine(args):
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from avalancheflume3d_gb300 import Engine, PARTICLE, lib
+    import ctypes as C
+
+    cfg, (sys_, fun, pp) = workload(args)
+    stream = torch.cuda.current_stream()
+    eng = Engine(sys_, fun, stream=stream.cuda_stream)
+    eng.import_particles(pp)
+    eng.forces()          # start-up force pass into a_i (avalanche_hst.cu:366-384)
+    eng.swap_accel()
+    trace = []
+    if args.preroll:
+        if args.trace_contacts:
+            eng.contact_count()
+            done = 0
+            while done < args.preroll:
+                k = min(args.trace_contacts, args.preroll - done)
+                eng.step(k)
+                done += k
+                trace.append((done, eng.contact_count() / k))
+            if rank == 0:
+                print("contacts per step during the pre-roll:", trace, file=sys.stderr, flush=True)
+        else:
+            eng.step(args.preroll)
+    eng.step(args.warmup)
+    grid = eng.get_grid()
+    ncell3 = int(grid["ncell3"])
+    eng.contact_count()   # restart the counter
+    launches0 = C.c_long()
+    lib().af3d_kernel_launches(eng._h, C.byref(launches0))
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    clocks = ClockSampler(local)
+    barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    eng.step(args.steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    ms = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    contacts = eng.contact_count()
+    launches1 = C.c_long()
+    lib().af3d_kernel_launches(eng._h, C.byref(launches1))
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    value = world * args.n * args.steps / (ms / 1e3)
+
+    # Roofline of the dominant kernel from CUDA events between the kernels (profiled steps after
+    # the timed region, same stream).
+    prof = np.zeros(6)
+    lib().af3d_step_profile(eng._h, args.profile_steps, prof.ctypes.data_as(C.c_void_p))
+    prof /= args.profile_steps
+    names = ["time_advance", "predict_keys", "cell_sort", "permute_records", "fused_forces", "regrid"]
+    peaks, peak_kind = measured_peaks()
+    t_forces = prof[4] / 1e3
+    alg = BYTES_PER_CLUMP * args.n + BYTES_PER_CELL * ncell3
+    achieved = alg / t_forces / 1e9 if t_forces > 0 else None
+    fp64 = C.c_double()
+    lib().af3d_fp64_peak(C.byref(fp64))
+
+    # End to end through the C ABI with pinned host buffers: import (H2D), one step, export (D2H).
+    e2e = None
+    if args.e2e_steps > 0:
+        h_pp = torch.empty(args.n * PARTICLE.itemsize, dtype=torch.uint8, pin_memory=True)
+        h_acc = torch.empty(args.n * 3, dtype=torch.float64, pin_memory=True)
+        h_anga = torch.empty(args.n * 3, dtype=torch.float64, pin_memory=True)
+        npp = h_pp.numpy().view(PARTICLE)
+        na, nal = h_acc.numpy().reshape(-1, 3), h_anga.numpy().reshape(-1, 3)
+        p_, a_, al_ = eng.export_particles()
+        npp[:] = p_
+        na[:] = a_
+        nal[:] = al_
+        barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            eng.import_particles(npp, na, nal)
+            eng.step(1)
+            lib().af3d_export_particles(eng._h, npp.ctypes.data_as(C.c_void_p), na.ctypes.data_as(C.c_void_p),
+                                        nal.ctypes.data_as(C.c_void_p))
+        torch.cuda.synchronize()
+        barrier()
+        dt = time.perf_counter() - t0
+        if world > 1:
+            import torch.distributed as dist
+            t = torch.tensor([dt], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            dt = float(t.item())
+        nbytes = args.n * (PARTICLE.itemsize + 48)
+        e2e = {"value": world * args.n * args.e2e_steps / dt, "unit": "clump-steps/s",
+               "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+               "what": "per step: import_particles (AoS + a_i from pinned host), af3d_step(1), "
+                       "export_particles (AoS + a_i to pinned host)"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        p_, a_, al_ = eng.export_particles()
+        m = min(args.cpu_sample, args.n)
+        s, f, q = cpu_sample_state(cfg, eng.get_system(), fun, p_, m)
+        val, k, dt = time_cpu(s, f, q, 1, args.cpu_seconds, acc=a_[:m].copy(), anga=al_[:m].copy())
+        cpu = {"value": val, "unit": "clump-steps/s", "cores": 1, "kind": "port",
+               "sample": "first %d clumps of the timed state (bottom lattice layers) as their own "
+                         "system, %d steps in %.1f s, 1 thread" % (m, k, dt)}
+
+    eng.close()
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "clump-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": config_dict(args, cfg, {"parallelism": "replicas" if world > 1 else "single",
+                                              "cells": ncell3}),
+            "contacts_per_s": world * contacts / (ms / 1e3),
+            "contacts_per_step": contacts / args.steps,
+            "e2e": e2e,
+            "gpu_launches": int(launches1.value - launches0.value),
+            "roofline": {"bound": "hbm", "kernel": "k_fused_forces", "achieved": achieved,
+                         "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                         "frac": (achieved / peaks["hbm_gbs"]) if achieved else None,
+                         "peak_source": peak_kind, "traffic": traffic_from_profile(),
+                         "algorithmic_bytes_per_launch": alg,
+                         "kernel_ms": prof[4], "note": "FP64-issue bound; see fp64"},
+            "fp64": {"peak_tflops": fp64.value, "peak_source": "measured DFMA microbenchmark"},
+            "phase_ms": {k: float(v) for k, v in zip(names, prof)},
+            "cpu_baseline": cpu,
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_engine(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,222 @@
+/*
+ * af3d.h -- C ABI of the GB300 clump-DEM engine (drop-in for the step loop of
+ * AvalancheFlume3D).
+ *
+ * The reference's step loop launches one routine per call on the default
+ * stream and keeps every array in caller-owned memory.  Here the state is
+ * device-resident inside an opaque context: the caller imports the reference's
+ * `particle` array once (host memory), calls one entry point per reference
+ * routine -- or af3d_step() for K fused, graph-captured steps -- and exports
+ * the state whenever it wants host copies.  Every entry point returns an
+ * af3d_status; nothing calls exit().
+ *
+ * Structs are binary-identical to the reference's (cabecera.hu:34-112), so a
+ * reference driver can pass its own `system_par`, `Funnel`, `particle` and
+ * `cell_par` objects.  All arithmetic is FP64 in cgs units.
+ */
+#ifndef AF3D_H
+#define AF3D_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AF3D_ABI_VERSION 1
+
+typedef struct { double x, y, z; } af3d_vec3;
+typedef struct { long x, y, z; } af3d_lvec3;
+
+/* system_par, cabecera.hu:34-66 (256 bytes). */
+typedef struct {
+  long      npart;
+  double    dt, hdt, rmin, rmax, v0, time, eps_pp, eps_pw, kappa_pp, kappa_pw, gamma_pp, gamma_pw,
+            mu_pp, mu_pw, t_coll, tot_mass, tilt, xhopper, Lflume, gyr_max, fr_fact_pp, fr_fact_pw,
+            sint, cost, sintg, costg, xfunnel, dy2;
+  af3d_vec3 side;
+} af3d_system_par;
+
+/* Funnel, cabecera.hu:69-74. */
+typedef struct { double sinfi, cosfi, tanfi; } af3d_funnel;
+
+/* particle, cabecera.hu:77-98 (408 bytes); rr_s[k] = rr_a..rr_d, rrot_s[k] = rrot_a..rrot_d. */
+typedef struct {
+  double    radius, mass, density;
+  af3d_vec3 moment_of_inertia;
+  af3d_vec3 rr_s[4];
+  af3d_vec3 rrot_s[4];
+  af3d_vec3 rr, rrot, vv, ww, Rmatx, Rmaty, Rmatz;
+} af3d_particle;
+
+/* cell_par, cabecera.hu:101-112 (168 bytes). */
+typedef struct {
+  long       ntags, ncell3;
+  af3d_lvec3 ncell;
+  long       ntot;
+  af3d_vec3  cell_side, cs_inv, rr_max, rr_min, length;
+} af3d_cell_par;
+
+/* The 16 positional lines of DataInput.dat (avalanche_hst.cu:34-81). */
+typedef struct {
+  long   npart;
+  double width, hopper_height, rmin, rmax, v0, dt, eps_pw, mu_pw, eps_pp, mu_pp, t_coll, Lflume,
+         tilt_deg;
+  long   ntags;
+  int    print_flag;
+} af3d_inputs;
+
+typedef int af3d_status;
+enum {
+  AF3D_OK = 0,
+  AF3D_ERR_ARG = 1,            /* bad argument or call order                                   */
+  AF3D_ERR_CUDA = 2,           /* a CUDA runtime call failed (af3d_last_error() has the text)  */
+  AF3D_ERR_NOMEM = 3,
+  AF3D_ERR_GRID_ESCAPE = 4,    /* a clump left the cell grid between re-grids (reference: UB)  */
+  AF3D_ERR_NEGATIVE_CELL = 5,  /* negative cell index (reference: exit(1), cells.cu:79-88)     */
+  AF3D_ERR_CELL_CAPACITY = 6,  /* a cell holds >= ntags clumps (reference: exit(1), :96-102)   */
+  AF3D_ERR_NAN = 7,            /* non-finite force or acceleration                             */
+  AF3D_ERR_IO = 8,             /* file missing or malformed                                    */
+  AF3D_ERR_INPUT = 9           /* DataInput values rejected by error_check (error_check.cu:3)  */
+};
+
+/* Friction variant of the particle-particle tangential law: the host routine omits the
+   `|| xi == 0` clause of the Coulomb test (force_part.cu:224), the device one has it (:487). */
+enum { AF3D_FRICTION_HST = 0, AF3D_FRICTION_DEV = 1 };
+
+/* Phase of the reference loop: hopper filling (avalanche_hst.cu:401-601) or avalanche (:618-856). */
+enum { AF3D_PHASE_FILL = 0, AF3D_PHASE_AVALANCHE = 1 };
+
+typedef struct af3d_ctx af3d_ctx;
+
+/* ---- context ---------------------------------------------------------------------------- */
+
+/* Create a context for sys->npart clumps on the current CUDA device.  ntags > 0 enforces the
+   reference's cell capacity (at most ntags-1 clumps per cell, cells.cu:96); ntags <= 0 lifts it.
+   Replaces the cudaMalloc block of avalanche_dev.cu:140-158. */
+af3d_status af3d_create (const af3d_system_par *sys, const af3d_funnel *fun, long ntags, int phase,
+                         af3d_ctx **out);
+af3d_status af3d_destroy (af3d_ctx *ctx);
+af3d_status af3d_set_stream (af3d_ctx *ctx, void *cuda_stream);      /* cudaStream_t, 0 = own */
+af3d_status af3d_set_friction (af3d_ctx *ctx, int variant);          /* AF3D_FRICTION_*       */
+const char *af3d_last_error (void);
+int         af3d_abi_version (void);
+
+/* Copy the reference particle array (host memory) and the current accelerations a_i, alpha_i
+   in/out (avalanche_dev.cu:347 / :716).  acc/anga may be NULL (import: zeros; export: skipped).
+   Export writes the slope-frame copies rrot from the current positions. */
+af3d_status af3d_import_particles (af3d_ctx *ctx, const af3d_particle *pp, const af3d_vec3 *acc,
+                                   const af3d_vec3 *anga);
+af3d_status af3d_export_particles (af3d_ctx *ctx, af3d_particle *pp, af3d_vec3 *acc,
+                                   af3d_vec3 *anga);
+
+/* system_par / cell_par passed by value in the reference become context state. */
+af3d_status af3d_set_system (af3d_ctx *ctx, const af3d_system_par *sys);
+af3d_status af3d_get_system (af3d_ctx *ctx, af3d_system_par *sys);
+af3d_status af3d_set_grid (af3d_ctx *ctx, const af3d_cell_par *cell);
+af3d_status af3d_get_grid (af3d_ctx *ctx, af3d_cell_par *cell);
+af3d_status af3d_set_phase (af3d_ctx *ctx, int phase);
+/* cell_dim (cell_dim.cu:7) + grid derivation (avalanche_hst.cu:314-333), on the device. */
+af3d_status af3d_regrid (af3d_ctx *ctx);
+/* Door opening: side.x = (LFUNNEL + Lflume) cos(tilt), time = 0, avalanche phase
+   (avalanche_hst.cu:607-613). */
+af3d_status af3d_open_door (af3d_ctx *ctx);
+
+/* ---- one entry point per reference routine (avalanche_hst.cu:668-710 order) ---------------- */
+af3d_status af3d_init_verlet (af3d_ctx *ctx);         /* init_Verlet.cu:11 with a_i, alpha_i     */
+af3d_status af3d_advance_time (af3d_ctx *ctx);        /* sys_par.time += dt, avalanche_hst.cu:672*/
+af3d_status af3d_rotate_vectors (af3d_ctx *ctx);      /* rotate_vectors.cu:7 (slope frame)       */
+af3d_status af3d_clear_forces (af3d_ctx *ctx);        /* clear_forces.cu:8                        */
+af3d_status af3d_cell_build (af3d_ctx *ctx);          /* clear_cell + clear_ocup + cell_locate,
+                                                         cells.cu:11,26,40                        */
+af3d_status af3d_force_hop (af3d_ctx *ctx, int nw);   /* force_hop.cu:9                           */
+af3d_status af3d_force_funnel (af3d_ctx *ctx);        /* force_funnel.cu:9                        */
+af3d_status af3d_force_fcorners (af3d_ctx *ctx);      /* force_funnel.cu:216                      */
+af3d_status af3d_force_walls (af3d_ctx *ctx);         /* force_walls.cu:9                         */
+af3d_status af3d_force_part (af3d_ctx *ctx, int sph_id); /* force_part.cu:11; sph_id 1..16, or 0
+                                                         for all sixteen in one call              */
+af3d_status af3d_force_flume (af3d_ctx *ctx);         /* force_flume.cu:10                        */
+af3d_status af3d_get_accel (af3d_ctx *ctx);           /* get_accel.cu:9 -> a_f, alpha_f           */
+af3d_status af3d_finish_verlet (af3d_ctx *ctx);       /* finish_Verlet.cu:10 with a_i and a_f     */
+af3d_status af3d_swap_accel (af3d_ctx *ctx);          /* avalanche_hst.cu:845-850                 */
+
+/* Fused force pass of the current phase: clear_forces, cell build, every force routine in the
+   reference's order, get_accel into a_f (avalanche_hst.cu:678-707; fill :445-464). */
+af3d_status af3d_forces (af3d_ctx *ctx);
+
+/* k steps of the current phase, fused and replayed from CUDA graphs, with the reference's
+   re-grid every 2000 steps (avalanche_hst.cu:713-748).  Returns the first error status raised
+   by the device checks during those steps. */
+af3d_status af3d_step (af3d_ctx *ctx, long k);
+
+/* Same steps as af3d_step, enqueued without graphs and with CUDA events between the kernels on
+   the context stream; adds the milliseconds of each phase to ms[AF3D_NPROF]:
+   0 time advance, 1 init_Verlet + cell keys, 2 cell sort, 3 permutation + neighbour records,
+   4 fused force kernel (walls, contacts, bed, get_accel, finish_Verlet), 5 re-grid. */
+enum { AF3D_NPROF = 6 };
+af3d_status af3d_step_profile (af3d_ctx *ctx, long k, double *ms);
+/* Kernels executed on the device by this context so far (graph replays included). */
+af3d_status af3d_kernel_launches (af3d_ctx *ctx, long *count);
+/* Measured FP64 fused-multiply-add throughput of the current device in TFLOP/s (2 flops per
+   DFMA), from a bounded ~0.1 s microbenchmark: the denominator of the FP64 roofline. */
+af3d_status af3d_fp64_peak (double *tflops);
+
+/* Status bits raised on the device since the last call (bitmask of 1 << AF3D_ERR_*); clears. */
+af3d_status af3d_get_status (af3d_ctx *ctx, int *flags);
+
+/* ---- diagnostics, indexed by clump id -------------------------------------------------- */
+af3d_status af3d_get_forces (af3d_ctx *ctx, af3d_vec3 *force, af3d_vec3 *torque);
+af3d_status af3d_get_accels (af3d_ctx *ctx, af3d_vec3 *acc_f, af3d_vec3 *anga_f);
+/* Cell of every clump (-1 if not binned) and the (cell, id)-sorted id list of the last build. */
+af3d_status af3d_get_cells (af3d_ctx *ctx, long *cell_of_id, long *sorted_ids, long *nbinned);
+/* Overlapping sphere pairs (ll, mm, sph_id) of the last cell build, in no particular order;
+   active = 1 keeps only pairs with a repulsive normal force.  *count may exceed cap. */
+af3d_status af3d_contact_pairs (af3d_ctx *ctx, long *out, long cap, long *count, int active);
+/* Active sphere-sphere contacts summed over the fused force passes (af3d_step, af3d_forces)
+   since the previous call; the counter restarts at zero. */
+af3d_status af3d_contact_count (af3d_ctx *ctx, long *count);
+
+/* ---- host I/O (no GPU) ----------------------------------------------------------------- */
+/* Parse DataInput.dat: first token of each of the 16 lines (avalanche_hst.cu:34-81). */
+af3d_status af3d_load_datainput (const char *path, af3d_inputs *in);
+/* Derived parameters of avalanche_hst.cu:84-102 and :187-195 (time = -1, side.x = HOP_WIDTH). */
+af3d_status af3d_derive_system (const af3d_inputs *in, af3d_system_par *sys, af3d_funnel *fun);
+/* error_check.cu:3; returns the reference's error number (0 = accepted). */
+int         af3d_error_check (const af3d_system_par *sys, char *msg, size_t msglen);
+/* last_config.dat writer/reader (avalanche_hst.cu:519-548 / :218-250); %lf text, lossy. */
+af3d_status af3d_write_last_config (const char *path, int aval_start, double time, long cc,
+                                    long jj, const af3d_particle *pp, long n);
+af3d_status af3d_read_last_config (const char *path, int *aval_start, double *time, long *cc,
+                                   long *jj, af3d_particle *pp, long n);
+
+/* ---- initial-state generators (host; generate_particles.cu, place_particles.cu,
+   set_initial_velocity.cu, rannew64.cu, calculate_particle_parameters.cu) ------------------- */
+typedef struct { uint64_t seed[250], uy; int np, nq, init; } af3d_rng;
+/* rannew64.cu:55-126 with its state in *rng instead of statics: the first draw after seeding
+   returns the reference's first draw for that idum. */
+void   af3d_rng_seed (af3d_rng *rng, long idum);
+double af3d_rng_next (af3d_rng *rng);
+/* generate_particles.cu:7-32: density 2.6, every 20th clump rmax, the others rmin. */
+void   af3d_generate_particles (af3d_particle *pp, const af3d_system_par *sys);
+/* calculate_particle_parameters.cu:10-41 (host version): m = 4 (4/3 pi) rho r^3, I = 112/15 pi rho r^5. */
+void   af3d_calculate_particle_parameters (af3d_particle *pp, long n);
+/* place_particles.cu:8-90: cubic lattice in the hopper, identity orientation.  Returns
+   AF3D_ERR_INPUT when the clumps do not fit (the reference exits). */
+af3d_status af3d_place_particles (const af3d_system_par *sys, af3d_particle *pp);
+/* set_initial_velocity.cu:7-42 with seed 26752658 on a fresh generator. */
+void   af3d_set_initial_velocity (const af3d_system_par *sys, af3d_particle *pp);
+/* Sphere centres from rr, R and radius (avalanche_hst.cu:265-293 / init_Verlet.cu:130-142). */
+void   af3d_sphere_centres (af3d_particle *pp, long n);
+/* Workload generator: clumps on a cubic lattice of the given pitch filling the box
+   [lo, hi] (x fastest), each with a uniformly random orientation drawn from rng (Shoemake unit
+   quaternion); an orientation whose spheres would overlap an already placed clump or leave the
+   box is redrawn (up to max_tries, then the last draw is kept).  Radius, density and mass must
+   already be set.  Returns the number of clumps placed (< n when the box is too small). */
+long   af3d_lattice_block (af3d_particle *pp, long n, af3d_vec3 lo, af3d_vec3 hi, double pitch,
+                           af3d_rng *rng, int max_tries);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

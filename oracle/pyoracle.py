@@ -85,8 +85,8 @@ class Oracle:
             getattr(L, name).argtypes = [C.c_void_p] * 4 + [C.c_int]
         L.orc_force_part.argtypes = [C.c_void_p] * 7 + [C.c_int, C.c_int]
         L.orc_set_threads.argtypes = [C.c_int]
-        L.orc_step.argtypes = [C.c_void_p] * 5 + [C.c_int, C.c_int]
-        L.orc_forces.argtypes = [C.c_void_p] * 5 + [C.c_int, C.c_int]
+        L.orc_step.argtypes = [C.c_void_p] * 4 + [C.POINTER(_Work), C.c_int, C.c_int]
+        L.orc_forces.argtypes = [C.c_void_p] * 4 + [C.POINTER(_Work), C.c_int, C.c_int]
 
     def set_threads(self, n: int) -> None:
         self.lib.orc_set_threads(int(n))
@@ -386,3 +386,86 @@ def dense_state(n: int, seed: int, sys, pitch_factor: float = 0.85, box=(0.0, 7.
     sphere_centres(pp)
     rotate_slope(pp, sys)
     return pp
+
+
+class OracleRun:
+    """A whole CPU run driven in C by orc_forces / orc_step (the reference's step sequence,
+    including time += dt and the acceleration swap), with the cell grid of cell_dim."""
+
+    def __init__(self, oracle: Oracle, sys, fun, pp, ntags=9, cp=None, acc=None, anga=None):
+        self.o = oracle
+        self.sys = np.array(sys, dtype=SYSTEM_PAR).copy()
+        self.fun = np.array(fun, dtype=FUNNEL).copy()
+        self.pp = np.ascontiguousarray(pp, dtype=PARTICLE).copy()
+        n = len(self.pp)
+        self.bufs = {k: np.zeros((n, 3)) for k in ("F", "T", "a0", "al0", "a1", "al1")}
+        if acc is not None:
+            self.bufs["a0"][:] = acc
+        if anga is not None:
+            self.bufs["al0"][:] = anga
+        self.w = _Work()
+        for f, k in (("force", "F"), ("torque", "T"), ("acc_i", "a0"), ("anga_i", "al0"),
+                     ("acc_f", "a1"), ("anga_f", "al1")):
+            setattr(self.w, f, self.bufs[k].ctypes.data)
+        self.ntags = ntags
+        if cp is None:
+            cp = np.zeros((), dtype=CELL_PAR)
+            cp["ntags"] = ntags
+            hi, lo = oracle.cell_dim(self.pp, self.sys)
+            cp["rr_max"], cp["rr_min"] = hi, lo
+            oracle.grid_from_bbox(cp, self.sys)
+        self.set_grid(cp)
+
+    def set_grid(self, cp):
+        self.cp = np.array(cp, dtype=CELL_PAR).copy()
+        self.cell_vec = np.full(max(1, int(self.cp["ntot"])), -1, dtype=np.int64)
+        self.nocup = np.zeros(max(1, int(self.cp["ncell3"])), dtype=np.int32)
+        self.w.cell_vec = self.cell_vec.ctypes.data
+        self.w.nocup_vec = self.nocup.ctypes.data
+        self.w.cell_vec_cap = len(self.cell_vec)
+        self.w.nocup_cap = len(self.nocup)
+
+    def regrid(self):
+        cp = np.zeros((), dtype=CELL_PAR)
+        cp["ntags"] = self.ntags
+        hi, lo = self.o.cell_dim(self.pp, self.sys)
+        cp["rr_max"], cp["rr_min"] = hi, lo
+        self.o.grid_from_bbox(cp, self.sys)
+        self.set_grid(cp)
+
+    def _arr(self, addr):
+        for v in self.bufs.values():
+            if v.ctypes.data == addr:
+                return v
+        raise KeyError(addr)
+
+    @property
+    def acc_i(self):
+        return self._arr(self.w.acc_i), self._arr(self.w.anga_i)
+
+    @property
+    def acc_f(self):
+        return self._arr(self.w.acc_f), self._arr(self.w.anga_f)
+
+    def forces(self, phase=PHASE_AVALANCHE, variant=FRICTION_HST) -> int:
+        return self.o.lib.orc_forces(_p(self.sys), _p(self.fun), _p(self.cp), _p(self.pp),
+                                     C.byref(self.w), int(phase), int(variant))
+
+    def seed_accel(self, phase=PHASE_AVALANCHE, variant=FRICTION_HST) -> int:
+        """Start-up force pass into a_i (avalanche_hst.cu:366-384)."""
+        st = self.forces(phase, variant)
+        self.w.acc_i, self.w.acc_f = self.w.acc_f, self.w.acc_i
+        self.w.anga_i, self.w.anga_f = self.w.anga_f, self.w.anga_i
+        return st
+
+    def step(self, k=1, phase=PHASE_AVALANCHE, variant=FRICTION_HST, cc0=None, regrid_every=2000) -> int:
+        for _ in range(k):
+            st = self.o.lib.orc_step(_p(self.sys), _p(self.fun), _p(self.cp), _p(self.pp),
+                                     C.byref(self.w), int(phase), int(variant))
+            if st:
+                return st
+            if cc0 is not None:
+                if cc0 % regrid_every == 0:
+                    self.regrid()
+                cc0 += 1
+        return 0
