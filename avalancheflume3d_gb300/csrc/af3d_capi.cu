@@ -146,6 +146,7 @@ af3d_status set_grid_device(af3d_ctx *c, const af3d_cell_par &g) {
 
 // Device re-grid, then adopt the result on the host (grow the bucket buffers if needed).
 af3d_status regrid(af3d_ctx *c) {
+  if (c->n == 0) return AF3D_OK;   // no clump to bound (cell_dim reads pp[0]): keep the grid
   launch_regrid(c->L(), c->cur, c->d, c->cells.cap);
   c->launches += kKernelsPerRegrid;
   long long pending = 0;
@@ -269,7 +270,7 @@ int af3d_abi_version(void) { return AF3D_ABI_VERSION; }
 af3d_status af3d_create(const af3d_system_par *sys, const af3d_funnel *fun, long ntags, int phase,
                         af3d_ctx **out) {
   if (!sys || !fun || !out) return fail(AF3D_ERR_ARG, "null argument");
-  if (sys->npart < 0 || sys->npart > (1L << 30)) return fail(AF3D_ERR_ARG, "npart out of range");
+  if (sys->npart < 0 || sys->npart > (1L << 28)) return fail(AF3D_ERR_ARG, "npart out of range (0..2^28)");
   *out = nullptr;
   af3d_ctx *c = new af3d_ctx();
   c->n = sys->npart;

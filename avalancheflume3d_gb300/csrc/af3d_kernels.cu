@@ -335,8 +335,14 @@ __device__ __forceinline__ void for_neighbour_slots(const Search &q, const af3d_
 
 // All sixteen sph_id passes of force_part for clump s, accumulated in the reference order:
 // sph_id outer, then cells, then slots.  Phase 1 walks the neighbour cells once and keeps the
-// FP32-surviving partners with their 16-bit pair masks; phase 2 runs the exact FP64 test and
-// contact law per sph_id over that list.  Returns the number of active contacts.
+// FP32-surviving partners with their 16-bit pair masks.  Phase 2 flattens them into one item
+// list per clump in that order (sph_id-major), and phase 3 runs the exact FP64 test and contact
+// law item by item.  Looping over the item index keeps the lanes of a warp busy with their own
+// clump's next pair (utilisation = mean/max items per lane) instead of idling at every (sph_id,
+// partner) slot where only one lane has work, and it leaves each clump's summation order
+// untouched.  Returns the number of active contacts.
+constexpr int kItemCap = 96;
+
 __device__ __forceinline__ int particle_contacts(long s, const Own &o, const Consts &c,
                                                  const af3d_cell_par &g, const NbrRec *__restrict__ nbr,
                                                  const CullRec *__restrict__ cull,
@@ -362,20 +368,32 @@ __device__ __forceinline__ int particle_contacts(long s, const Own &o, const Con
       overflow = true;
     }
   });
-  int active = 0;
+  unsigned items[kItemCap];   // (partner slot << 4) | (sph_id - 1)
+  int nitems = 0;
   if (!overflow) {
 #pragma unroll 1
-    for (int p = 0; p < 16; p++) {
+    for (int p = 0; p < 16 && !overflow; p++) {
       if (!((want >> p) & 1u)) continue;
-      const int sl = p & 3, sm = p >> 2;
 #pragma unroll 1
       for (int k = 0; k < ncand; k++) {
         if (!((cand_m[k] >> p) & 1u)) continue;
-        active += part_pair(o.r, o.v, o.w, o.s[sl], o.rad, o.msph, nbr[cand_t[k]], sm, c, xi0, F, T) == 2;
+        if (nitems == kItemCap) {
+          overflow = true;
+          break;
+        }
+        items[nitems++] = ((unsigned)cand_t[k] << 4) | (unsigned)p;
       }
     }
+  }
+  int active = 0;
+  if (!overflow) {
+#pragma unroll 1
+    for (int i = 0; i < nitems; i++) {
+      const int t = (int)(items[i] >> 4), p = (int)(items[i] & 15u);
+      active += part_pair(o.r, o.v, o.w, o.s[p & 3], o.rad, o.msph, nbr[t], p >> 2, c, xi0, F, T) == 2;
+    }
   } else {
-    // More partners than the list holds: walk the cells once per sph_id (same order).
+    // More partners than the lists hold: walk the cells once per sph_id (same order).
 #pragma unroll 1
     for (int p = 0; p < 16; p++) {
       if (!((want >> p) & 1u)) continue;

@@ -96,8 +96,10 @@ def flume_state(cfg: FlumeConfig):
 # The benchmark configurations (cgs).  FLUME_2K: 2,048 clumps, 30 deg, 40 cm x 4 cm flume;
 # FLUME_262K: 262,144 clumps, 35 deg, 200 cm x 20 cm flume.
 def flume_2k(**kw) -> FlumeConfig:
-    return FlumeConfig(n=2048, tilt_deg=30.0, width=4.0, Lflume=40.0, **kw)
+    kw = {"n": 2048, "tilt_deg": 30.0, "width": 4.0, "Lflume": 40.0, **kw}
+    return FlumeConfig(**kw)
 
 
 def flume_262k(**kw) -> FlumeConfig:
-    return FlumeConfig(n=262144, tilt_deg=35.0, width=20.0, Lflume=200.0, **kw)
+    kw = {"n": 262144, "tilt_deg": 35.0, "width": 20.0, "Lflume": 200.0, **kw}
+    return FlumeConfig(**kw)
