@@ -453,16 +453,19 @@ __global__ void __launch_bounds__(kBlock) k_fused_forces(Planes P, Planes out, D
     const af3d_cell_par g = d->grid;
     const Own o = own_from_record(nbr[s], P.p[MWALL][s]);
     const bool removed = is_removed(c.time, o.r.x, c.side_x);
+    const double B = (double)cull[s].c.w;   // sphere offsets + radius, rounded up
     V3 F = mk(0.0, 0.0, 0.0), T = mk(0.0, 0.0, 0.0);
     if (c.phase == AF3D_PHASE_AVALANCHE) {
       // hop x3, funnel, fcorners, walls (avalanche_hst.cu:688-696)
-      for (int rt = R_HOP0; rt <= R_WALLS; rt++) bnd_routine(rt, o, removed, c, F, T);
+      for (int rt = R_HOP0; rt <= R_WALLS; rt++)
+        if (bnd_may_touch(rt, o.r, B, c)) bnd_routine(rt, o, removed, c, F, T);
       if (!removed) active = particle_contacts(s, o, c, g, nbr, cull, start, -1, F, T);
-      bnd_routine(R_FLUME, o, removed, c, F, T);
+      if (bnd_may_touch(R_FLUME, o.r, B, c)) bnd_routine(R_FLUME, o, removed, c, F, T);
     } else {
       // part x16 then hop x3 (avalanche_hst.cu:455-461)
       if (!removed) active = particle_contacts(s, o, c, g, nbr, cull, start, -1, F, T);
-      for (int rt = R_HOP0; rt <= R_HOP2; rt++) bnd_routine(rt, o, removed, c, F, T);
+      for (int rt = R_HOP0; rt <= R_HOP2; rt++)
+        if (bnd_may_touch(rt, o.r, B, c)) bnd_routine(rt, o, removed, c, F, T);
     }
     if (WRITE_FT) {
       store3(P, FX, s, F);

@@ -287,6 +287,44 @@ __device__ __forceinline__ void bnd_routine(int routine, const Own &o, bool remo
   }
 }
 
+// Whether a boundary routine can touch any sphere of a clump whose spheres lie within distance
+// B of its centre r (B >= max sphere offset + radius, rounded up).  Every distance a boundary
+// routine tests is a 1-Lipschitz function of the sphere centre (plane distances, coordinates in
+// the rotated frame), so if the centre's value misses the routine's threshold by more than B no
+// sphere can pass the test and the routine adds nothing.  The margin `eps` covers the FP64
+// rounding of these centre expressions.  Used to skip routines, never to change their result.
+__device__ __forceinline__ bool bnd_may_touch(int routine, V3 r, double B, const Consts &c) {
+  const double eps = 1e-12 * (1.0 + fabs(r.x) + fabs(r.y) + fabs(r.z));
+  const double Bm = B + eps;
+  switch (routine) {
+    case R_HOP0: case R_HOP1: case R_HOP2: {
+      if (r.z + Bm < kHOP_HEIGHT || r.x - Bm > kHOP_WIDTH) return false;   // force_hop.cu:67
+      if (routine == R_HOP0) return r.x <= Bm || r.x >= kHOP_WIDTH - Bm;
+      if (routine == R_HOP1) return r.y - kYHOP_L <= Bm || kYHOP_R - r.y <= Bm;
+      return c.time < 0.0 && r.z - kHOP_HEIGHT <= Bm;
+    }
+    case R_FUNNEL: {
+      const double xr = r.x * c.cost - r.z * c.sint, yr = r.y;
+      if (xr - Bm > kLFUNNEL) return false;
+      return fabs(yr - xr * c.tanfi) * c.cosfi <= Bm || fabs(kYFUNNEL - yr - xr * c.tanfi) * c.cosfi <= Bm;
+    }
+    case R_FCORNERS: {
+      const double xr = r.x * c.cost - r.z * c.sint;
+      return fabs(xr - kLFUNNEL) <= 2.0 * Bm;
+    }
+    case R_WALLS: {
+      const double xr = r.x * c.cost - r.z * c.sint;
+      if (xr + Bm <= kLFUNNEL) return false;
+      return r.y - c.dy2 <= Bm || c.side_y + c.dy2 - r.y <= Bm;
+    }
+    case R_FLUME: {
+      const double zr = r.x * c.sint + r.z * c.cost;
+      return fabs(zr) <= Bm;
+    }
+  }
+  return true;
+}
+
 // One sphere-sphere contact of force_part.cu:139-252: own sphere s1 (clump centre rrl), partner
 // record m, partner sphere sm.  Returns 1 when the pair overlaps, 2 when it also exerts a force.
 __device__ __forceinline__ int part_pair(const V3 &rrl, const V3 &vvl, const V3 &wwl, const V3 &s1,

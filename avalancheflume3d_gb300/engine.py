@@ -92,7 +92,7 @@ class Engine:
     def get_system(self) -> np.ndarray:
         s = np.zeros(1, dtype=SYSTEM_PAR)
         self._call("af3d_get_system", ptr(s))
-        self.sys = s[0].copy()
+        self.sys = s.reshape(()).copy()
         return self.sys
 
     def set_grid(self, cell: np.ndarray) -> None:
@@ -102,7 +102,7 @@ class Engine:
     def get_grid(self) -> np.ndarray:
         c = np.zeros(1, dtype=CELL_PAR)
         self._call("af3d_get_grid", ptr(c))
-        return c[0].copy()
+        return c.reshape(()).copy()
 
     def set_friction(self, variant: int) -> None:
         self._call("af3d_set_friction", int(variant))
@@ -186,7 +186,7 @@ class Engine:
 def load_datainput(path: str) -> np.ndarray:
     v = np.zeros(1, dtype=INPUTS)
     check(lib().af3d_load_datainput(path.encode(), ptr(v)), "af3d_load_datainput")
-    return v[0].copy()
+    return v.reshape(()).copy()
 
 
 def derive_system(inputs: np.ndarray):
@@ -194,7 +194,7 @@ def derive_system(inputs: np.ndarray):
     f = np.zeros(1, dtype=FUNNEL)
     v = np.array(inputs, dtype=INPUTS).reshape(1)
     check(lib().af3d_derive_system(ptr(v), ptr(s), ptr(f)), "af3d_derive_system")
-    return s[0].copy(), f[0].copy()
+    return s.reshape(()).copy(), f.reshape(()).copy()
 
 
 def error_check(sys: np.ndarray) -> tuple[int, str]:

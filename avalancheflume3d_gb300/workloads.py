@@ -89,8 +89,22 @@ def flume_state(cfg: FlumeConfig):
         raise ValueError("lattice block holds %d of %d clumps" % (placed, cfg.n))
     if cfg.v0 > 0:
         set_initial_velocity(sys, pp)
+    slope_frame(pp, sys)
     sys["tot_mass"] = float(pp["mass"].sum())
     return sys, fun, pp
+
+
+def slope_frame(pp: np.ndarray, sys: np.ndarray) -> None:
+    """Fill the slope-frame copies rrot, rrot_a..d from the lab-frame positions with the arithmetic
+    of rotate_vectors.cu:28-46 (x' = x cos - z sin, y' = y, z' = x sin + z cos)."""
+    c, s = float(sys["cost"]), float(sys["sint"])
+    for src, dst in (("rr", "rrot"), ("rr_s", "rrot_s")):
+        v = pp[src]
+        out = np.empty_like(v)
+        out[..., 0] = v[..., 0] * c - v[..., 2] * s
+        out[..., 1] = v[..., 1]
+        out[..., 2] = v[..., 0] * s + v[..., 2] * c
+        pp[dst] = out
 
 
 # The benchmark configurations (cgs).  FLUME_2K: 2,048 clumps, 30 deg, 40 cm x 4 cm flume;
