@@ -108,6 +108,7 @@ SIGNATURES = [
     ("af3d_set_initial_velocity", [_P, _P], None),
     ("af3d_sphere_centres", [_P, C.c_long], None),
     ("af3d_lattice_block", [_P, C.c_long, Vec3, Vec3, C.c_double, _P, C.c_int], C.c_long),
+    ("af3d_lattice_pile", [_P, C.c_long, Vec3, Vec3, C.c_double, C.c_double, _P, C.c_int], C.c_long),
 ]
 
 _lib = None

@@ -23,6 +23,8 @@ OBJ = os.path.join(PKG, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC]
+# Extra nvcc flags for tuning sweeps (e.g. AF3D_NVCC_FLAGS="-DAF3D_FORCES_MINB=4").
+COMMON += os.environ.get("AF3D_NVCC_FLAGS", "").split()
 
 # (source, extra flags)
 UNITS = [

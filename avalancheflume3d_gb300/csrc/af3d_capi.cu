@@ -165,10 +165,10 @@ af3d_status regrid(af3d_ctx *c) {
 
 // clear_cell + clear_ocup + cell_locate: keys (optionally fused with the predictor), counting
 // sort, permutation of every plane into the new order, neighbour records.
-void enqueue_cell_build(af3d_ctx *c, bool predict, bool t_prev) {
+void enqueue_cell_build(af3d_ctx *c, bool predict, bool t_prev, bool ft = true) {
   launch_predict(c->L(), c->cur, c->d, predict, true, t_prev, c->cells, c->id_cur);
   launch_sort(c->L(), c->d, c->cells, c->id_cur, c->ntags);
-  launch_permute_records(c->L(), c->cur, c->alt, c->cells.perm, c->id_cur, c->id_alt, c->nbr, c->cull);
+  launch_permute_records(c->L(), c->cur, c->alt, c->cells.perm, c->id_cur, c->id_alt, c->nbr, c->cull, ft);
   std::swap(c->cur, c->alt);
   std::swap(c->id_cur, c->id_alt);
 }
@@ -177,7 +177,7 @@ void enqueue_cell_build(af3d_ctx *c, bool predict, bool t_prev) {
 // finish_Verlet, and the acceleration swap.
 void enqueue_fused_step(af3d_ctx *c) {
   launch_advance_time(c->st, c->d);
-  enqueue_cell_build(c, true, true);
+  enqueue_cell_build(c, true, true, false);   // F, T are not read by the fused force kernel
   launch_fused_forces(c->L(), c->cur, c->alt, c->d, c->nbr, c->cull, c->cells.start, false);
   swap_velocity_planes(c->cur, c->alt);
   swap_accel_planes(c->cur);
@@ -623,7 +623,8 @@ af3d_status af3d_step_profile(af3d_ctx *c, long k, double *ms) {
     AF3D_CUDA(cudaEventRecord(ev[2], c->st));
     launch_sort(c->L(), c->d, c->cells, c->id_cur, c->ntags);
     AF3D_CUDA(cudaEventRecord(ev[3], c->st));
-    launch_permute_records(c->L(), c->cur, c->alt, c->cells.perm, c->id_cur, c->id_alt, c->nbr, c->cull);
+    launch_permute_records(c->L(), c->cur, c->alt, c->cells.perm, c->id_cur, c->id_alt, c->nbr, c->cull,
+                           false);
     std::swap(c->cur, c->alt);
     std::swap(c->id_cur, c->id_alt);
     AF3D_CUDA(cudaEventRecord(ev[4], c->st));

@@ -8,6 +8,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "../../include/af3d.h"
 
@@ -352,6 +353,68 @@ long af3d_lattice_block(af3d_particle *pp, long n, af3d_vec3 lo, af3d_vec3 hi, d
     p.ww = {0.0, 0.0, 0.0};
   }
   return m;
+}
+
+long af3d_lattice_pile(af3d_particle *pp, long n, af3d_vec3 lo, af3d_vec3 hi, double pitch,
+                       double overlap, af3d_rng *rng, int max_tries) {
+  // Columns of a square lattice in x-y; clumps are dropped layer by layer.  Each clump gets a
+  // random orientation that keeps its spheres inside the box walls (redrawn up to max_tries),
+  // and is then lowered straight down until one of its spheres touches a sphere already placed
+  // in its own or a neighbouring column (or the floor z = lo.z), and pressed `overlap` further.
+  const long nx = (long)floor((hi.x - lo.x) / pitch), ny = (long)floor((hi.y - lo.y) / pitch);
+  if (nx <= 0 || ny <= 0 || n <= 0) return 0;
+  const long ncol = nx * ny;
+  // the last two clumps dropped into every column (obstacles for the next ones)
+  std::vector<long> top(2 * ncol, -1);
+  for (long a = 0; a < n; a++) {
+    const long col = a % ncol, i = col % nx, j = col / nx;
+    af3d_particle &p = pp[a];
+    const double cx = lo.x + (i + 0.5) * pitch, cy = lo.y + (j + 0.5) * pitch;
+    p.rr = {cx, cy, 0.0};
+    for (int t = 0; t < (max_tries > 0 ? max_tries : 1); t++) {
+      const double u1 = af3d_rng_next(rng), u2 = af3d_rng_next(rng), u3 = af3d_rng_next(rng);
+      const double s1 = sqrt(1.0 - u1), s2 = sqrt(u1);
+      const double w = s1 * sin(2 * kPI * u2), x = s1 * cos(2 * kPI * u2);
+      const double y = s2 * sin(2 * kPI * u3), z = s2 * cos(2 * kPI * u3);
+      p.Rmatx = {1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)};
+      p.Rmaty = {2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)};
+      p.Rmatz = {2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)};
+      af3d_sphere_centres(&p, 1);
+      bool bad = false;
+      for (int k = 0; k < 4 && !bad; k++)
+        bad = p.rr_s[k].x - p.radius < lo.x || p.rr_s[k].x + p.radius > hi.x ||
+              p.rr_s[k].y - p.radius < lo.y || p.rr_s[k].y + p.radius > hi.y;
+      if (!bad) break;
+    }
+    // lowest centre height at which no sphere is below the floor or inside a placed sphere
+    double zc = -1e300;
+    for (int k = 0; k < 4; k++) zc = fmax(zc, lo.z + p.radius - (p.rr_s[k].z - p.rr.z));
+    for (long di = -1; di <= 1; di++)
+      for (long dj = -1; dj <= 1; dj++) {
+        const long ii = i + di, jj = j + dj;
+        if (ii < 0 || jj < 0 || ii >= nx || jj >= ny) continue;
+        for (int h = 0; h < 2; h++) {
+          const long b = top[2 * (ii + nx * jj) + h];
+          if (b < 0) continue;
+          const af3d_particle &q = pp[b];
+          for (int k = 0; k < 4; k++)
+            for (int u = 0; u < 4; u++) {
+              const double dx = (p.rr_s[k].x) - q.rr_s[u].x, dy = (p.rr_s[k].y) - q.rr_s[u].y;
+              const double sep = p.radius + q.radius, h2 = sep * sep - dx * dx - dy * dy;
+              if (h2 <= 0.0) continue;
+              zc = fmax(zc, q.rr_s[u].z + sqrt(h2) - (p.rr_s[k].z - p.rr.z));
+            }
+        }
+      }
+    p.rr.z = zc - overlap;
+    af3d_sphere_centres(&p, 1);
+    top[2 * col + 1] = top[2 * col];
+    top[2 * col] = a;
+    p.vv = {0.0, 0.0, 0.0};
+    p.ww = {0.0, 0.0, 0.0};
+    if (p.rr.z > hi.z) return a;
+  }
+  return n;
 }
 
 }  // extern "C"

@@ -26,6 +26,7 @@ enum Plane : int {
   RAD, DEN, MASS, IXX, IYY, IZZ,                 // radius, density, clump mass, inertia
   MSPH,                                          // SPH_FACT*density*r^3 (force_part.cu:58 order)
   MWALL,                                         // SPH_FACT*r^3*density (force_walls.cu:47 order)
+  ADRAG,                                         // DRAG*r*r/mass (get_accel.cu:47 order)
   NPLANES
 };
 
@@ -99,8 +100,9 @@ void launch_sort (const Launch &L, DevScalars *d, Cells cells, const long long *
 long scan_tiles (long bucket_cap);
 void launch_permute (const Launch &L, Planes src, Planes dst, const int *perm, long long *id_src,
                      long long *id_dst);
+// `ft`: also carry the force/torque accumulators (the fused step does not need them).
 void launch_permute_records (const Launch &L, Planes src, Planes dst, const int *perm,
-                             long long *id_src, long long *id_dst, NbrRec *nbr, CullRec *cull);
+                             long long *id_src, long long *id_dst, NbrRec *nbr, CullRec *cull, bool ft);
 void launch_build_records (const Launch &L, Planes cur, NbrRec *nbr, CullRec *cull);
 void launch_fused_forces (const Launch &L, Planes cur, Planes out, DevScalars *d, const NbrRec *nbr,
                           const CullRec *cull, const int *start, bool write_ft);

@@ -17,6 +17,10 @@ namespace af3d {
 namespace {
 
 constexpr int kBlock = 128;
+// Resident blocks per SM requested for the fused force kernel (register budget 65536 / (128 x n)).
+#ifndef AF3D_FORCES_MINB
+#define AF3D_FORCES_MINB 3
+#endif
 
 inline unsigned grid_for(long n, int block = kBlock) {
   return (unsigned)((n + block - 1) / block);
@@ -64,6 +68,7 @@ __global__ void k_aos_to_planes(const af3d_particle *__restrict__ aos, const dou
   store3(P, IXX, s, mk(q.moment_of_inertia.x, q.moment_of_inertia.y, q.moment_of_inertia.z));
   P.p[MSPH][s] = kSPH_FACT * rho * r * r * r;   // force_part.cu:58
   P.p[MWALL][s] = kSPH_FACT * r * r * r * rho;  // force_walls.cu:47
+  P.p[ADRAG][s] = drag_factor(r, q.mass);       // get_accel.cu:47
   id[s] = s;
 }
 
@@ -222,10 +227,9 @@ __global__ void k_predict(Planes P, DevScalars *d, bool t_prev, Cells cells,
 
 __device__ __forceinline__ float f_up(double x) { return __double2float_ru(x); }
 
-// Packed FP64 neighbour record and conservative FP32 culling record of slot s.
-__device__ __forceinline__ void write_records(long s, V3 r, V3 v, V3 w, const V3 *sp, double rad,
-                                              double msph, NbrRec *nbr, CullRec *cull) {
-  NbrRec &q = nbr[s];
+// Packed FP64 neighbour record and conservative FP32 culling record of one clump.
+__device__ __forceinline__ void make_records(V3 r, V3 v, V3 w, const V3 *sp, double rad, double msph,
+                                             NbrRec &q, CullRec &c) {
   q.rx = r.x; q.ry = r.y; q.rz = r.z;
   q.vx = v.x; q.vy = v.y; q.vz = v.z;
   q.wx = w.x; q.wy = w.y; q.wz = w.z;
@@ -241,30 +245,59 @@ __device__ __forceinline__ void write_records(long s, V3 r, V3 v, V3 w, const V3
   // 2^-21 * max|coordinate| bounds 4x the FP32 rounding of a coordinate difference.
   const double mu = fmax(M, rad) * 4.76837158203125e-07 + 1e-30;
   const float radf = f_up(rad + mu);
-  CullRec c;
   c.c = make_float4((float)r.x, (float)r.y, (float)r.z, f_up(ext * (1.0 + 1e-12) + rad + mu));
   for (int k = 0; k < 4; k++) c.s[k] = make_float4((float)sp[k].x, (float)sp[k].y, (float)sp[k].z, radf);
-  cull[s] = c;
 }
 
-// dst[p][s] = src[p][perm[s]] for every plane, plus the records of the new slot.
-__global__ void k_permute(Planes src, Planes dst, const int *__restrict__ perm,
-                          const long long *__restrict__ id_src, long long *id_dst, NbrRec *nbr,
-                          CullRec *cull, long n) {
-  long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (s >= n) return;
-  const long o = perm ? perm[s] : s;
-  if (perm) {
+constexpr int kPermBlock = 128;
+// Records are staged in shared memory with an odd stride (25 doubles) so that the per-thread
+// writes of a 24-double record hit distinct banks.
+constexpr int kRecWords = (int)(sizeof(NbrRec) / 8);   // 24
+constexpr int kRecStride = kRecWords + 1;
+
+// dst[p][s] = src[p][perm[s]] for every plane (the force/torque accumulators and a_f only with
+// `ft`: the fused step rewrites them before reading), plus the packed records of the new slot,
+// assembled in shared memory and written out as contiguous 16-byte stores.
+__global__ void __launch_bounds__(kPermBlock) k_permute(Planes src, Planes dst, const int *__restrict__ perm,
+                                                        const long long *__restrict__ id_src,
+                                                        long long *id_dst, NbrRec *nbr, CullRec *cull,
+                                                        bool ft, long n) {
+  __shared__ double s_nbr[kPermBlock * kRecStride];
+  __shared__ CullRec s_cull[kPermBlock];
+  const long base = blockIdx.x * (long)kPermBlock;
+  const long s = base + threadIdx.x;
+  if (s < n) {
+    if (perm) {
+      const long o = perm[s];
 #pragma unroll 8
-    for (int p = 0; p < NPLANES; p++) dst.p[p][s] = src.p[p][o];
-    id_dst[s] = id_src[o];
+      for (int p = 0; p < NPLANES; p++)
+        if (ft || ((p < FX || p > TZ) && (p < AFX || p > ALFZ))) dst.p[p][s] = src.p[p][o];
+      id_dst[s] = id_src[o];
+    }
+    if (nbr) {
+      V3 sp[4];
+      for (int k = 0; k < 4; k++) sp[k] = load3(dst, S0X + 3 * k, s);
+      NbrRec q;
+      make_records(load3(dst, RX, s), load3(dst, VX, s), load3(dst, WX, s), sp, dst.p[RAD][s],
+                   dst.p[MSPH][s], q, s_cull[threadIdx.x]);
+      const double *qw = reinterpret_cast<const double *>(&q);
+#pragma unroll
+      for (int k = 0; k < kRecWords; k++) s_nbr[threadIdx.x * kRecStride + k] = qw[k];
+    }
   }
-  if (nbr) {
-    V3 sp[4];
-    for (int k = 0; k < 4; k++) sp[k] = load3(dst, S0X + 3 * k, s);
-    write_records(s, load3(dst, RX, s), load3(dst, VX, s), load3(dst, WX, s), sp, dst.p[RAD][s],
-                  dst.p[MSPH][s], nbr, cull);
+  if (!nbr) return;
+  __syncthreads();
+  const long cnt = n - base < kPermBlock ? n - base : kPermBlock;
+  const int nw = (int)(cnt * kRecWords) / 2;   // double2 words of the block's records
+  double2 *b = reinterpret_cast<double2 *>(nbr + base);
+  for (int i = threadIdx.x; i < nw; i += kPermBlock) {
+    const int w0 = 2 * i, r0 = w0 / kRecWords, k0 = w0 - r0 * kRecWords;   // k0 even, k0 + 1 < 24
+    b[i] = make_double2(s_nbr[r0 * kRecStride + k0], s_nbr[r0 * kRecStride + k0 + 1]);
   }
+  const int m16 = (int)(cnt * (long)(sizeof(CullRec) / 16));
+  const float4 *c = reinterpret_cast<const float4 *>(s_cull);
+  float4 *e = reinterpret_cast<float4 *>(cull + base);
+  for (int i = threadIdx.x; i < m16; i += kPermBlock) e[i] = c[i];
 }
 
 // ------------------------------------------------------------------ particle contacts
@@ -297,18 +330,29 @@ struct Search {
   long ci, cj, ck;
 };
 
-// Search-centre cell of force_part.cu:77-85 (division by cell_side).
-__device__ __forceinline__ long search_axis(double x, double xmin, double side, long n) {
-  long i = (long)((x - xmin) / side);
+// Search-centre cell of force_part.cu:77-85: (long)((x - xmin)/side).  The quotient is first
+// estimated with the reciprocal cs_inv = 1/side.  For |q| < 1e6 the estimate is within
+// 4.4e-16 |Q| < 1e-9 of the true quotient Q, so when it is more than 1e-9 away from an integer,
+// Q and its correctly rounded value lie in the same open unit interval and truncate to the same
+// index; the division is only carried out near a cell boundary.  Same index as the reference.
+__device__ __forceinline__ long search_axis(double x, double xmin, double side, double inv, long n) {
+  const double dx = x - xmin;
+  const double q = dx * inv;
+  const double fl = floor(q);
+  long i;
+  if (q - fl > 1e-9 && q - fl < 1.0 - 1e-9 && fabs(q) < 1.0e6)   // |q - Q| <= 4.4e-16 |Q| < 1e-9
+    i = (long)q;
+  else
+    i = (long)(dx / side);
   if (i == n) i--;
   return i;
 }
 
 __device__ __forceinline__ Search search_centre(V3 r, const af3d_cell_par &g) {
   Search q;
-  q.ci = search_axis(r.x, g.rr_min.x, g.cell_side.x, g.ncell.x);
-  q.cj = search_axis(r.y, g.rr_min.y, g.cell_side.y, g.ncell.y);
-  q.ck = search_axis(r.z, g.rr_min.z, g.cell_side.z, g.ncell.z);
+  q.ci = search_axis(r.x, g.rr_min.x, g.cell_side.x, g.cs_inv.x, g.ncell.x);
+  q.cj = search_axis(r.y, g.rr_min.y, g.cell_side.y, g.cs_inv.y, g.ncell.y);
+  q.ck = search_axis(r.z, g.rr_min.z, g.cell_side.z, g.cs_inv.z, g.ncell.z);
   return q;
 }
 
@@ -333,30 +377,56 @@ __device__ __forceinline__ void for_neighbour_slots(const Search &q, const af3d_
       }
 }
 
-// All sixteen sph_id passes of force_part for clump s, accumulated in the reference order:
-// sph_id outer, then cells, then slots.  Phase 1 walks the neighbour cells once and keeps the
-// FP32-surviving partners with their 16-bit pair masks.  Phase 2 flattens them into one item
-// list per clump in that order (sph_id-major), and phase 3 runs the exact FP64 test and contact
-// law item by item.  Looping over the item index keeps the lanes of a warp busy with their own
-// clump's next pair (utilisation = mean/max items per lane) instead of idling at every (sph_id,
-// partner) slot where only one lane has work, and it leaves each clump's summation order
-// untouched.  Returns the number of active contacts.
+// The same visit with every cell boundary loaded up front.  The three cells of one (jdel, kdel)
+// row are consecutive in the linear cell index, so their members form one slot range split by
+// four start[] values; the 9 rows x 4 boundaries are issued as independent loads before the walk
+// (instead of 27 dependent round trips), then the cells are walked in the reference's order.
+template <typename F>
+__device__ __forceinline__ void for_neighbour_slots_pre(const Search &q, const af3d_cell_par &g,
+                                                        const int *__restrict__ start, F &&f) {
+  int bnd[9][4];
+  const long x0 = q.ci - 1;
+#pragma unroll
+  for (int r = 0; r < 9; r++) {
+    const long jn = q.cj + (r / 3 - 1), kn = q.ck + (r % 3 - 1);
+    const bool row_ok = jn >= 0 && kn >= 0 && jn < g.ncell.y && kn < g.ncell.z;
+    const long rb = g.ncell.x * (jn + g.ncell.y * kn);
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+      // boundary e of the row: start of cell x0 + e, clamped into the row (empty cells outside)
+      long x = x0 + e;
+      x = x < 0 ? 0 : (x > g.ncell.x ? g.ncell.x : x);
+      bnd[r][e] = row_ok ? __ldg(&start[rb + x]) : 0;
+    }
+  }
+#pragma unroll 1
+  for (int di = 0; di < 3; di++)
+#pragma unroll 1
+    for (int r = 0; r < 9; r++) {
+      const int t0 = bnd[r][di], t1 = bnd[r][di + 1];
+#pragma unroll 1
+      for (int t = t0; t < t1; t++) f(t);
+    }
+}
+
+// The sixteen sph_id passes of force_part for one clump are summed in the reference order:
+// sph_id outer, then cells, then slots.  Phase 1 walks the 27 neighbour cells once and keeps the
+// FP32-surviving partners with their 16-bit pair masks; phase 2 flattens them into one item list
+// per clump in that order (sph_id-major); the items are then run through the exact FP64 test and
+// contact law one by one and added in list order.  Returns false when a list would overflow.
 constexpr int kItemCap = 96;
 
-__device__ __forceinline__ int particle_contacts(long s, const Own &o, const Consts &c,
-                                                 const af3d_cell_par &g, const NbrRec *__restrict__ nbr,
-                                                 const CullRec *__restrict__ cull,
-                                                 const int *__restrict__ start, int only_p, V3 &F,
-                                                 V3 &T) {
-  const bool xi0 = c.variant == AF3D_FRICTION_DEV;
+__device__ __forceinline__ bool gather_items(long s, const Own &o, const af3d_cell_par &g,
+                                             const CullRec *__restrict__ cull,
+                                             const int *__restrict__ start, unsigned want,
+                                             unsigned *items, int cap, int &nitems) {
   const CullRec me = cull[s];
   const Search q = search_centre(o.r, g);
   int cand_t[kCandCap];
   unsigned short cand_m[kCandCap];
   int ncand = 0;
   bool overflow = false;
-  const unsigned want = only_p < 0 ? 0xffffu : (1u << only_p);
-  for_neighbour_slots(q, g, start, [&](int t) {
+  for_neighbour_slots_pre(q, g, start, [&](int t) {
     if (t == s) return;
     const unsigned m = pair_mask(me, cull[t]) & want;
     if (!m) return;
@@ -368,43 +438,141 @@ __device__ __forceinline__ int particle_contacts(long s, const Own &o, const Con
       overflow = true;
     }
   });
-  unsigned items[kItemCap];   // (partner slot << 4) | (sph_id - 1)
+  nitems = 0;
+  if (overflow) return false;
+#pragma unroll 1
+  for (int p = 0; p < 16; p++) {
+    if (!((want >> p) & 1u)) continue;
+#pragma unroll 1
+    for (int k = 0; k < ncand; k++) {
+      if (!((cand_m[k] >> p) & 1u)) continue;
+      if (nitems == cap) return false;
+      items[nitems++] = ((unsigned)cand_t[k] << 4) | (unsigned)p;   // (partner slot, sph_id - 1)
+    }
+  }
+  return true;
+}
+
+// Every pair of clump s walked cell by cell once per sph_id (the order of sixteen force_part
+// launches); used when a clump has more partners than the item lists hold.
+__device__ __forceinline__ int contacts_by_pass(long s, const Own &o, const Consts &c,
+                                                const af3d_cell_par &g, const NbrRec *__restrict__ nbr,
+                                                const CullRec *__restrict__ cull,
+                                                const int *__restrict__ start, unsigned want, V3 &F,
+                                                V3 &T) {
+  const bool xi0 = c.variant == AF3D_FRICTION_DEV;
+  const CullRec me = cull[s];
+  const Search q = search_centre(o.r, g);
+  int active = 0;
+#pragma unroll 1
+  for (int p = 0; p < 16; p++) {
+    if (!((want >> p) & 1u)) continue;
+    const int sl = p & 3, sm = p >> 2;
+    for_neighbour_slots(q, g, start, [&](int t) {
+      if (t == s) return;
+      if (!((pair_mask(me, cull[t]) >> p) & 1u)) return;
+      active += part_pair(o.r, o.v, o.w, o.s[sl], o.rad, o.msph, nbr[t], sm, c, xi0, F, T) == 2;
+    });
+  }
+  return active;
+}
+
+// Per-clump contact pass (one thread, its own item list): the per-routine force_part entry.
+__device__ __forceinline__ int particle_contacts(long s, const Own &o, const Consts &c,
+                                                 const af3d_cell_par &g, const NbrRec *__restrict__ nbr,
+                                                 const CullRec *__restrict__ cull,
+                                                 const int *__restrict__ start, int only_p, V3 &F,
+                                                 V3 &T) {
+  const bool xi0 = c.variant == AF3D_FRICTION_DEV;
+  const unsigned want = only_p < 0 ? 0xffffu : (1u << only_p);
+  unsigned items[kItemCap];
   int nitems = 0;
-  if (!overflow) {
+  if (!gather_items(s, o, g, cull, start, want, items, kItemCap, nitems))
+    return contacts_by_pass(s, o, c, g, nbr, cull, start, want, F, T);
+  int active = 0;
 #pragma unroll 1
-    for (int p = 0; p < 16 && !overflow; p++) {
-      if (!((want >> p) & 1u)) continue;
-#pragma unroll 1
-      for (int k = 0; k < ncand; k++) {
-        if (!((cand_m[k] >> p) & 1u)) continue;
-        if (nitems == kItemCap) {
-          overflow = true;
-          break;
-        }
-        items[nitems++] = ((unsigned)cand_t[k] << 4) | (unsigned)p;
+  for (int i = 0; i < nitems; i++) {
+    const int t = (int)(items[i] >> 4), p = (int)(items[i] & 15u);
+    active += part_pair(o.r, o.v, o.w, o.s[p & 3], o.rad, o.msph, nbr[t], p >> 2, c, xi0, F, T) == 2;
+  }
+  return active;
+}
+
+// Warp-cooperative contact pass of the fused kernel.  Every lane publishes its clump's item list
+// (sph_id-major, as above) in shared memory; the warp then works through the concatenated lists
+// 32 items per round, one item per lane, reading the owner clump from its record, and after each
+// round every owner adds its items' force and torque terms to its own sums in list order.  The
+// FP64 contact law thus runs with all lanes busy whatever the spread of contacts per clump, and
+// each clump's summation order stays the reference's.  All 32 lanes of the warp must call this;
+// `act` is false for lanes without a clump to process; `wbase` is the slot of the warp's lane 0.
+constexpr int kLaneItems = 32;
+
+struct WarpQueue {
+  unsigned items[32][kLaneItems];
+  double res[32][6];
+  int flag[32];
+  int base[33];
+};
+
+__device__ __forceinline__ int warp_contacts(WarpQueue &wq, long wbase, long s, bool act, const Own &o,
+                                             const Consts &c, const af3d_cell_par &g,
+                                             const NbrRec *__restrict__ nbr,
+                                             const CullRec *__restrict__ cull,
+                                             const int *__restrict__ start, V3 &F, V3 &T) {
+  const int lane = threadIdx.x & 31;
+  const bool xi0 = c.variant == AF3D_FRICTION_DEV;
+  int nitems = 0;
+  bool slow = false;
+  if (act) slow = !gather_items(s, o, g, cull, start, 0xffffu, wq.items[lane], kLaneItems, nitems);
+  if (slow) nitems = 0;
+  int incl = nitems;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const int u = __shfl_up_sync(0xffffffffu, incl, off);
+    if (lane >= off) incl += u;
+  }
+  const int base = incl - nitems;
+  const int total = __shfl_sync(0xffffffffu, incl, 31);
+  wq.base[lane] = base;
+  if (lane == 31) wq.base[32] = total;
+  __syncwarp();
+  int active = 0;
+  for (int j0 = 0; j0 < total; j0 += 32) {
+    const int j = j0 + lane;
+    if (j < total) {
+      int lo = 0, hi = 31;   // owner: the last lane whose list starts at or before j
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (wq.base[mid] <= j) lo = mid; else hi = mid - 1;
+      }
+      const unsigned it = wq.items[lo][j - wq.base[lo]];
+      const int t = (int)(it >> 4), p = (int)(it & 15u);
+      const NbrRec &me = nbr[wbase + lo];   // owner lanes hold clumps, so wbase + lo < n
+      const V3 rl = mk(me.rx, me.ry, me.rz), vl = mk(me.vx, me.vy, me.vz), wl = mk(me.wx, me.wy, me.wz);
+      const int k = p & 3;
+      const V3 s1 = mk(me.s[3 * k], me.s[3 * k + 1], me.s[3 * k + 2]);
+      V3 fs, tq;
+      const int r = part_pair_contrib(rl, vl, wl, s1, me.rad, me.msph, nbr[t], p >> 2, c, xi0, fs, tq);
+      wq.flag[lane] = r;
+      if (r == 2) {
+        wq.res[lane][0] = fs.x; wq.res[lane][1] = fs.y; wq.res[lane][2] = fs.z;
+        wq.res[lane][3] = tq.x; wq.res[lane][4] = tq.y; wq.res[lane][5] = tq.z;
       }
     }
-  }
-  int active = 0;
-  if (!overflow) {
-#pragma unroll 1
-    for (int i = 0; i < nitems; i++) {
-      const int t = (int)(items[i] >> 4), p = (int)(items[i] & 15u);
-      active += part_pair(o.r, o.v, o.w, o.s[p & 3], o.rad, o.msph, nbr[t], p >> 2, c, xi0, F, T) == 2;
+    __syncwarp();
+    if (nitems > 0) {
+      const int a = base > j0 ? base : j0;
+      const int b = base + nitems < j0 + 32 ? base + nitems : j0 + 32;
+      for (int e = a - j0; e < b - j0; e++) {
+        if (wq.flag[e] != 2) continue;
+        T.x += wq.res[e][3]; T.y += wq.res[e][4]; T.z += wq.res[e][5];
+        F.x += wq.res[e][0]; F.y += wq.res[e][1]; F.z += wq.res[e][2];
+        active++;
+      }
     }
-  } else {
-    // More partners than the lists hold: walk the cells once per sph_id (same order).
-#pragma unroll 1
-    for (int p = 0; p < 16; p++) {
-      if (!((want >> p) & 1u)) continue;
-      const int sl = p & 3, sm = p >> 2;
-      for_neighbour_slots(q, g, start, [&](int t) {
-        if (t == s) return;
-        if (!((pair_mask(me, cull[t]) >> p) & 1u)) return;
-        active += part_pair(o.r, o.v, o.w, o.s[sl], o.rad, o.msph, nbr[t], sm, c, xi0, F, T) == 2;
-      });
-    }
+    __syncwarp();
   }
+  if (slow) active += contacts_by_pass(s, o, c, g, nbr, cull, start, 0xffffu, F, T);
   return active;
 }
 
@@ -440,31 +608,47 @@ __device__ __forceinline__ void warp_count(DevScalars *d, int active) {
 
 // The whole force pass of one step for clump s, in the reference's call order, then get_accel
 // and finish_Verlet.  Velocities after the corrector go to `out` (the other plane set), because
-// neighbours still read this step's predicted velocities from the records.
+// neighbours still read this step's predicted velocities from the records.  Every lane of a
+// launched warp reaches the warp-cooperative contact pass (lanes past n take no clump).
+#ifndef AF3D_COOP
+#define AF3D_COOP 1
+#endif
 template <bool WRITE_FT>
-__global__ void __launch_bounds__(kBlock) k_fused_forces(Planes P, Planes out, DevScalars *d,
+__global__ void __launch_bounds__(kBlock, AF3D_FORCES_MINB) k_fused_forces(Planes P, Planes out, DevScalars *d,
                                                          const NbrRec *__restrict__ nbr,
                                                          const CullRec *__restrict__ cull,
                                                          const int *__restrict__ start, long n) {
+#if AF3D_COOP
+  __shared__ WarpQueue wq[kBlock / 32];
+#endif
   const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  int active = 0;
-  if (s < n) {
-    const Consts c = load_consts(d);
-    const af3d_cell_par g = d->grid;
-    const Own o = own_from_record(nbr[s], P.p[MWALL][s]);
-    const bool removed = is_removed(c.time, o.r.x, c.side_x);
-    const double B = (double)cull[s].c.w;   // sphere offsets + radius, rounded up
-    V3 F = mk(0.0, 0.0, 0.0), T = mk(0.0, 0.0, 0.0);
-    if (c.phase == AF3D_PHASE_AVALANCHE) {
-      // hop x3, funnel, fcorners, walls (avalanche_hst.cu:688-696)
-      for (int rt = R_HOP0; rt <= R_WALLS; rt++)
-        if (bnd_may_touch(rt, o.r, B, c)) bnd_routine(rt, o, removed, c, F, T);
-      if (!removed) active = particle_contacts(s, o, c, g, nbr, cull, start, -1, F, T);
-      if (bnd_may_touch(R_FLUME, o.r, B, c)) bnd_routine(R_FLUME, o, removed, c, F, T);
+  const bool valid = s < n;
+  const long sv = valid ? s : n - 1;   // in-range slot for lanes past n (nothing is written for them)
+  const Consts c = load_consts(d);
+  const af3d_cell_par g = d->grid;
+  const Own o = own_from_record(nbr[sv], P.p[MWALL][sv]);
+  const bool removed = is_removed(c.time, o.r.x, c.side_x);
+  const double B = (double)cull[sv].c.w;   // sphere offsets + radius, rounded up
+  V3 F = mk(0.0, 0.0, 0.0), T = mk(0.0, 0.0, 0.0);
+  const bool aval = c.phase == AF3D_PHASE_AVALANCHE;
+  if (valid && aval) {
+    // hop x3, funnel, fcorners, walls (avalanche_hst.cu:688-696)
+    for (int rt = R_HOP0; rt <= R_WALLS; rt++)
+      if (bnd_may_touch(rt, o.r, B, c)) bnd_routine(rt, o, removed, c, F, T);
+  }
+  // part x16 (avalanche_hst.cu:699-701, fill :455-457)
+#if AF3D_COOP
+  const long wbase = blockIdx.x * (long)blockDim.x + (threadIdx.x & ~31u);
+  const int active = warp_contacts(wq[threadIdx.x >> 5], wbase, sv, valid && !removed, o, c, g, nbr, cull,
+                                   start, F, T);
+#else
+  const int active = (valid && !removed) ? particle_contacts(s, o, c, g, nbr, cull, start, -1, F, T) : 0;
+#endif
+  if (valid) {
+    if (aval) {
+      if (bnd_may_touch(R_FLUME, o.r, B, c)) bnd_routine(R_FLUME, o, removed, c, F, T);   // :704
     } else {
-      // part x16 then hop x3 (avalanche_hst.cu:455-461)
-      if (!removed) active = particle_contacts(s, o, c, g, nbr, cull, start, -1, F, T);
-      for (int rt = R_HOP0; rt <= R_HOP2; rt++)
+      for (int rt = R_HOP0; rt <= R_HOP2; rt++)   // hop x3 after the particles (:460-461)
         if (bnd_may_touch(rt, o.r, B, c)) bnd_routine(rt, o, removed, c, F, T);
     }
     if (WRITE_FT) {
@@ -474,7 +658,7 @@ __global__ void __launch_bounds__(kBlock) k_fused_forces(Planes P, Planes out, D
     if (!removed) {
       V3 a, al;
       get_accel_one(F, T, o.v, o.w, load3(P, R00, s), load3(P, R10, s), load3(P, R20, s),
-                    P.p[MASS][s], o.rad, load3(P, IXX, s), a, al);
+                    P.p[MASS][s], P.p[ADRAG][s], load3(P, IXX, s), a, al);
       store3(P, AFX, s, a);
       store3(P, ALFX, s, al);
       const V3 ai = load3(P, AIX, s), ali = load3(P, ALIX, s);
@@ -489,6 +673,8 @@ __global__ void __launch_bounds__(kBlock) k_fused_forces(Planes P, Planes out, D
     } else {
       store3(out, VX, s, mk(0.0, 0.0, 0.0));  // finish_Verlet.cu:28-32
       store3(out, WX, s, o.w);
+      store3(P, AFX, s, mk(0.0, 0.0, 0.0));   // the reference leaves stale values here
+      store3(P, ALFX, s, mk(0.0, 0.0, 0.0));
     }
   }
   warp_count(d, active);
@@ -529,7 +715,7 @@ __global__ void k_get_accel(Planes P, DevScalars *d, long n) {
   if (is_removed(d->sys.time, P.p[RX][s], d->sys.side.x)) return;
   V3 a, al;
   get_accel_one(load3(P, FX, s), load3(P, TX, s), load3(P, VX, s), load3(P, WX, s), load3(P, R00, s),
-                load3(P, R10, s), load3(P, R20, s), P.p[MASS][s], P.p[RAD][s], load3(P, IXX, s), a, al);
+                load3(P, R10, s), load3(P, R20, s), P.p[MASS][s], P.p[ADRAG][s], load3(P, IXX, s), a, al);
   store3(P, AFX, s, a);
   store3(P, ALFX, s, al);
 }
@@ -718,18 +904,21 @@ void launch_predict(const Launch &L, Planes cur, DevScalars *d, bool predict, bo
 void launch_permute(const Launch &L, Planes src, Planes dst, const int *perm, long long *id_src,
                     long long *id_dst) {
   if (L.n <= 0) return;
-  k_permute<<<grid_for(L.n), kBlock, 0, L.st>>>(src, dst, perm, id_src, id_dst, nullptr, nullptr, L.n);
+  k_permute<<<grid_for(L.n, kPermBlock), kPermBlock, 0, L.st>>>(src, dst, perm, id_src, id_dst, nullptr,
+                                                                nullptr, true, L.n);
 }
 
 void launch_permute_records(const Launch &L, Planes src, Planes dst, const int *perm,
-                            long long *id_src, long long *id_dst, NbrRec *nbr, CullRec *cull) {
+                            long long *id_src, long long *id_dst, NbrRec *nbr, CullRec *cull, bool ft) {
   if (L.n <= 0) return;
-  k_permute<<<grid_for(L.n), kBlock, 0, L.st>>>(src, dst, perm, id_src, id_dst, nbr, cull, L.n);
+  k_permute<<<grid_for(L.n, kPermBlock), kPermBlock, 0, L.st>>>(src, dst, perm, id_src, id_dst, nbr, cull,
+                                                                ft, L.n);
 }
 
 void launch_build_records(const Launch &L, Planes cur, NbrRec *nbr, CullRec *cull) {
   if (L.n <= 0) return;
-  k_permute<<<grid_for(L.n), kBlock, 0, L.st>>>(cur, cur, nullptr, nullptr, nullptr, nbr, cull, L.n);
+  k_permute<<<grid_for(L.n, kPermBlock), kPermBlock, 0, L.st>>>(cur, cur, nullptr, nullptr, nullptr, nbr,
+                                                                cull, true, L.n);
 }
 
 void launch_fused_forces(const Launch &L, Planes cur, Planes out, DevScalars *d, const NbrRec *nbr,

@@ -326,10 +326,12 @@ __device__ __forceinline__ bool bnd_may_touch(int routine, V3 r, double B, const
 }
 
 // One sphere-sphere contact of force_part.cu:139-252: own sphere s1 (clump centre rrl), partner
-// record m, partner sphere sm.  Returns 1 when the pair overlaps, 2 when it also exerts a force.
-__device__ __forceinline__ int part_pair(const V3 &rrl, const V3 &vvl, const V3 &wwl, const V3 &s1,
-                                         double rad_1, double massl, const NbrRec &m, int sm,
-                                         const Consts &c, bool xi0, V3 &F, V3 &T) {
+// record m, partner sphere sm.  Returns 0 (no overlap), 1 (overlap, no force) or 2 (force); with
+// 2, fs is the contact force and tq its torque about rrl, the terms force_part.cu:245-251 adds.
+__device__ __forceinline__ int part_pair_contrib(const V3 &rrl, const V3 &vvl, const V3 &wwl,
+                                                 const V3 &s1, double rad_1, double massl,
+                                                 const NbrRec &m, int sm, const Consts &c, bool xi0,
+                                                 V3 &fs, V3 &tq) {
   const double rad_2 = m.rad;
   const double sep = rad_1 + rad_2;
   const double sep2 = sep * sep;
@@ -352,22 +354,44 @@ __device__ __forceinline__ int part_pair(const V3 &rrl, const V3 &vvl, const V3 
   V3 vl = point_velocity(vvl, wwl, rrc, rrl);
   V3 vm = point_velocity(mk(m.vx, m.vy, m.vz), mk(m.wx, m.wy, m.wz), rrc, mk(m.rx, m.ry, m.rz));
   V3 dvvc = mk(vm.x - vl.x, vm.y - vl.y, vm.z - vl.z);
-  V3 fs;
   if (!contact_law(dvvc, n, sep - dist, km, gm, massl, c.mu_pp, c.cns_pp, c.dt, xi0, false, fs))
     return 1;
-  accumulate(F, T, fs, rrc, rrl);
+  tq.x = (rrc.y - rrl.y) * fs.z - (rrc.z - rrl.z) * fs.y;
+  tq.y = (rrc.z - rrl.z) * fs.x - (rrc.x - rrl.x) * fs.z;
+  tq.z = (rrc.x - rrl.x) * fs.y - (rrc.y - rrl.y) * fs.x;
   return 2;
 }
 
-// get_accel.cu:21-75 for one clump; R rows Rx, Ry, Rz.
+// The same contact accumulated into (F, T) in place.
+__device__ __forceinline__ int part_pair(const V3 &rrl, const V3 &vvl, const V3 &wwl, const V3 &s1,
+                                         double rad_1, double massl, const NbrRec &m, int sm,
+                                         const Consts &c, bool xi0, V3 &F, V3 &T) {
+  V3 fs, tq;
+  const int r = part_pair_contrib(rrl, vvl, wwl, s1, rad_1, massl, m, sm, c, xi0, fs, tq);
+  if (r == 2) {
+    T.x += tq.x; T.y += tq.y; T.z += tq.z;
+    F.x += fs.x; F.y += fs.y; F.z += fs.z;
+  }
+  return r;
+}
+
+// (+0 * a) * b as IEEE arithmetic evaluates it for finite a and b: a zero whose sign is the
+// exclusive-or of the signs of a and b.
+__device__ __forceinline__ double signed_zero_product(double a, double b) {
+  const unsigned long long sa = (unsigned long long)__double_as_longlong(a);
+  const unsigned long long sb = (unsigned long long)__double_as_longlong(b);
+  return __longlong_as_double((long long)((sa ^ sb) & 0x8000000000000000ull));
+}
+
+// get_accel.cu:21-75 for one clump; R rows Rx, Ry, Rz.  `adrag0` = DRAG*rad*rad/m (the same
+// expression, precomputed per clump).  For isotropic inertia (Ix == Iy == Iz, the reference's
+// clumps, calculate_particle_parameters.cu:33) the Euler coupling terms C*wb*wb are (+0*wb)*wb,
+// i.e. signed zeros; they are formed from the sign bits instead of two divisions-by-I and four
+// multiplications, which gives the same bits for finite angular velocities.
 __device__ __forceinline__ void get_accel_one(V3 f, V3 t, V3 v, V3 w, V3 Rx, V3 Ry, V3 Rz, double m,
-                                              double rad, V3 I, V3 &a, V3 &al) {
-  double Cxy = (I.x - I.y) / I.z;
-  double Cyz = (I.y - I.z) / I.x;
-  double Czx = (I.z - I.x) / I.y;
-  double adrag = kDRAG * rad * rad / m;
+                                              double adrag0, V3 I, V3 &a, V3 &al) {
   double vmag = sqrt(v.x * v.x + v.y * v.y + v.z * v.z);
-  adrag *= vmag;
+  double adrag = adrag0 * vmag;
   a.x = f.x / m - adrag * v.x;
   a.y = f.y / m - adrag * v.y;
   a.z = f.z / m - adrag * v.z - kGRAV;
@@ -378,12 +402,25 @@ __device__ __forceinline__ void get_accel_one(V3 f, V3 t, V3 v, V3 w, V3 Rx, V3 
   tb.x = t.x * Rx.x + t.y * Ry.x + t.z * Rz.x;
   tb.y = t.x * Rx.y + t.y * Ry.y + t.z * Rz.y;
   tb.z = t.x * Rx.z + t.y * Ry.z + t.z * Rz.z;
-  ab.x = tb.x / I.x + Cyz * wb.y * wb.z;
-  ab.y = tb.y / I.y + Czx * wb.z * wb.x;
-  ab.z = tb.z / I.z + Cxy * wb.x * wb.y;
+  if (I.x == I.y && I.y == I.z && isfinite(wb.x) && isfinite(wb.y) && isfinite(wb.z) && I.x > 0.0 &&
+      isfinite(I.x)) {
+    ab.x = tb.x / I.x + signed_zero_product(wb.y, wb.z);
+    ab.y = tb.y / I.y + signed_zero_product(wb.z, wb.x);
+    ab.z = tb.z / I.z + signed_zero_product(wb.x, wb.y);
+  } else {
+    double Cxy = (I.x - I.y) / I.z;
+    double Cyz = (I.y - I.z) / I.x;
+    double Czx = (I.z - I.x) / I.y;
+    ab.x = tb.x / I.x + Cyz * wb.y * wb.z;
+    ab.y = tb.y / I.y + Czx * wb.z * wb.x;
+    ab.z = tb.z / I.z + Cxy * wb.x * wb.y;
+  }
   al.x = ab.x * Rx.x + ab.y * Rx.y + ab.z * Rx.z;
   al.y = ab.x * Ry.x + ab.y * Ry.y + ab.z * Ry.z;
   al.z = ab.x * Rz.x + ab.y * Rz.y + ab.z * Rz.z;
 }
+
+// DRAG*rad*rad/m in get_accel.cu:47's operand order.
+__device__ __forceinline__ double drag_factor(double rad, double m) { return kDRAG * rad * rad / m; }
 
 }  // namespace af3d

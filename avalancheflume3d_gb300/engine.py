@@ -265,7 +265,13 @@ def lattice_block(pp: np.ndarray, lo, hi, pitch: float, rng: Rannew64, max_tries
                                         int(max_tries)))
 
 
+def lattice_pile(pp: np.ndarray, lo, hi, pitch: float, overlap: float, rng: Rannew64,
+                 max_tries: int = 64) -> int:
+    return int(lib().af3d_lattice_pile(ptr(pp), len(pp), Vec3(*lo), Vec3(*hi), float(pitch),
+                                       float(overlap), rng.ref, int(max_tries)))
+
+
 __all__ = ["Engine", "EngineError", "load_datainput", "derive_system", "error_check",
            "write_last_config", "read_last_config", "Rannew64", "generate_particles",
            "calculate_particle_parameters", "place_particles", "set_initial_velocity",
-           "sphere_centres", "lattice_block"]
+           "sphere_centres", "lattice_block", "lattice_pile"]

@@ -19,7 +19,8 @@ from dataclasses import dataclass
 import numpy as np
 
 from ._lib import INPUTS, PARTICLE
-from .engine import Rannew64, calculate_particle_parameters, derive_system, lattice_block, set_initial_velocity
+from .engine import (Rannew64, calculate_particle_parameters, derive_system, lattice_block, lattice_pile,
+                     set_initial_velocity)
 
 HOP_WIDTH, HOP_HEIGHT, YHOP_L, YHOP_R = 15.0, 25.0, 7.5, 22.5
 
@@ -42,6 +43,8 @@ class FlumeConfig:
     v0: float = 0.0              # initial speed in the reference's random directions
     seed: int = 20240613         # rannew64 seed of the orientations
     hopper_height: float | None = None
+    layout: str = "lattice"      # "lattice": clumps on the lattice; "pile": dropped into a pile
+    overlap: float = 2.0e-5      # pile: how far each clump is pressed into its support [cm]
 
     @property
     def t_coll(self) -> float:
@@ -54,7 +57,7 @@ def flume_inputs(cfg: FlumeConfig) -> np.ndarray:
     """The 16 DataInput.dat values of a configuration."""
     per_layer = int(HOP_WIDTH // cfg.pitch) ** 2
     layers = -(-cfg.n // per_layer)
-    height = cfg.hopper_height if cfg.hopper_height is not None else layers * cfg.pitch + 1.0
+    height = cfg.hopper_height if cfg.hopper_height is not None else layers * cfg.pitch * 1.25 + 1.0
     v = np.zeros((), dtype=INPUTS)
     v["npart"] = cfg.n
     v["width"], v["hopper_height"] = cfg.width, height
@@ -68,12 +71,16 @@ def flume_inputs(cfg: FlumeConfig) -> np.ndarray:
 
 
 def flume_state(cfg: FlumeConfig):
-    """(system_par, Funnel, particle array) of a lattice block released in the open hopper at
-    time 0 (avalanche phase: side.x = xfinal, avalanche_hst.cu:607-613).
+    """(system_par, Funnel, particle array) of a clump block in the hopper at the moment the door
+    opens (time 0, avalanche phase: side.x = xfinal, avalanche_hst.cu:607-613).
 
-    Clumps sit on a cubic lattice of the given pitch inside the hopper box x in [0, 15],
-    y in [7.5, 22.5], z > 25, each with a uniformly random orientation (Shoemake quaternion from
-    rannew64); orientations that would overlap a placed neighbour or a hopper wall are redrawn.
+    layout "lattice": clumps on a cubic lattice of the given pitch inside the hopper box x in
+    [0, 15], y in [7.5, 22.5], z > 25, each with a uniformly random orientation (Shoemake
+    quaternion from rannew64); orientations that would overlap a placed neighbour or a hopper
+    wall are redrawn.
+    layout "pile": the same lattice columns and random orientations, each clump dropped onto the
+    closed door (z = 25) or the clumps already placed and pressed `overlap` into its support: the
+    packed pile the hopper-fill phase ends with, every resting contact carrying load.
     With v0 > 0 the velocities follow the reference's set_initial_velocity (seed 26752658)."""
     sys, fun = derive_system(flume_inputs(cfg))
     sys["time"] = 0.0
@@ -84,7 +91,11 @@ def flume_state(cfg: FlumeConfig):
     calculate_particle_parameters(pp)
     rng = Rannew64(cfg.seed)
     top = HOP_HEIGHT + float(sys["side"][2])
-    placed = lattice_block(pp, (0.0, YHOP_L, HOP_HEIGHT), (HOP_WIDTH, YHOP_R, top), cfg.pitch, rng)
+    if cfg.layout == "pile":
+        placed = lattice_pile(pp, (0.0, YHOP_L, HOP_HEIGHT), (HOP_WIDTH, YHOP_R, top), cfg.pitch,
+                              cfg.overlap, rng)
+    else:
+        placed = lattice_block(pp, (0.0, YHOP_L, HOP_HEIGHT), (HOP_WIDTH, YHOP_R, top), cfg.pitch, rng)
     if placed != cfg.n:
         raise ValueError("lattice block holds %d of %d clumps" % (placed, cfg.n))
     if cfg.v0 > 0:

@@ -3,11 +3,14 @@
 
 Workload ``flume262k`` (the 262,144-clump configuration): tetrahedral 4-sphere clumps, sphere
 radius 1 mm, density 2.5 g/cm^3, kn = 1e4 N/m (t_coll from the reference's law), restitution 0.5,
-mu_pp = 0.5, mu_wall = 0.4, flume 2.0 m x 0.2 m at 35 deg, dt = 2e-6 s, FP64.  The clumps start on
-a 4 mm cubic lattice in the open hopper with uniformly random orientations and the reference's
-random initial velocities (v0 = 10 cm/s, set_initial_velocity.cu), and are released for a pre-roll
-of P steps (untimed, part of the input) so that the timed window sees a colliding granular state
-rather than a lattice at rest.  Synthetic data; the state (~400 MB) is larger than L2.
+mu_pp = 0.5, mu_wall = 0.4, flume 2.0 m x 0.2 m at 35 deg, dt = 2e-6 s, FP64.  The block stands in
+the hopper on the columns of a 4 mm lattice, each clump with a uniformly random orientation and
+zero velocity, dropped onto the clumps below it and pressed 2e-5 cm into its support (``--layout
+pile``): the packed block the hopper-fill phase ends with.  The door opens at time 0 and the timed
+steps follow the W warm-up steps of the release.  At dt = 2 us a timed window is a near-frozen
+snapshot, so its contact density is that of the input; ``--layout lattice`` (the bare lattice,
+optionally with the reference's random initial velocities ``--v0`` and a release ``--preroll``)
+has almost no contacts.  Synthetic data; the state (~400 MB) is larger than L2.
 
 Timed: exactly K fused steps (graph replays, af3d_step) after W warm-up steps, CUDA events on
 the engine's stream, barrier + synchronize on both sides, max over ranks.  Then, outside the
@@ -47,8 +50,9 @@ def parse_args():
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", choices=["engine", "reference"], default="engine")
     p.add_argument("--n", type=int, default=262144, help="clumps (262144 = the benchmark config)")
-    p.add_argument("--preroll", type=int, default=1000, help="untimed release steps of the input")
-    p.add_argument("--v0", type=float, default=10.0)
+    p.add_argument("--layout", choices=["pile", "lattice"], default="pile")
+    p.add_argument("--preroll", type=int, default=0, help="untimed release steps of the input")
+    p.add_argument("--v0", type=float, default=0.0)
     p.add_argument("--profile-steps", type=int, default=10)
     p.add_argument("--e2e-steps", type=int, default=5)
     p.add_argument("--cpu-sample", type=int, default=16384, help="clumps in the CPU baseline sample")
@@ -59,14 +63,9 @@ def parse_args():
     return p.parse_args()
 
 
-def dist_env():
-    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
-            int(os.environ.get("LOCAL_RANK", "0")))
-
-
 def workload(args):
     from avalancheflume3d_gb300.workloads import flume_262k, flume_state
-    cfg = flume_262k(n=args.n, v0=args.v0)
+    cfg = flume_262k(n=args.n, v0=args.v0, layout=args.layout)
     return cfg, flume_state(cfg)
 
 
@@ -74,7 +73,7 @@ def config_dict(args, cfg, extra=None):
     d = {"workload": "flume262k" if args.n == 262144 else "flume%d" % args.n,
          "clumps": args.n, "spheres": 4 * args.n, "tilt_deg": cfg.tilt_deg, "flume_m": cfg.Lflume / 100,
          "width_m": cfg.width / 100, "dt_s": cfg.dt, "lattice_mm": cfg.pitch * 10, "v0_cm_s": args.v0,
-         "preroll_steps": args.preroll, "friction": "host (force_part.cu:224)",
+         "layout": args.layout, "preroll_steps": args.preroll, "friction": "host (force_part.cu:224)",
          "l2": "state larger than L2 (no flush needed)"}
     if extra:
         d.update(extra)
@@ -167,8 +166,8 @@ def time_cpu(sys_, fun, pp, threads, seconds, acc=None, anga=None, min_steps=2, 
 
 
 def run_reference(args):
-    rank, world, _ = dist_env()
-    if rank != 0:
+    from avalancheflume3d_gb300 import replicas
+    if replicas.from_env().rank != 0:
         return
     threads = os.cpu_count() or 1
     cfg, (sys_, fun, pp) = workload(args)
@@ -201,11 +200,12 @@ def run_reference(args):
 
 def run_engine(args):
     import torch
-    rank, world, local = dist_env()
+    from avalancheflume3d_gb300 import replicas
+    R = replicas.from_env()
+    rank, world, local = R.rank, R.world, R.local
     torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    dev = torch.device("cuda", local)
+    replicas.init(R, "nccl", dev)
     from avalancheflume3d_gb300 import Engine, PARTICLE, lib
     import ctypes as C
 
@@ -240,9 +240,7 @@ def run_engine(args):
     lib().af3d_kernel_launches(eng._h, C.byref(launches0))
 
     def barrier():
-        if world > 1:
-            import torch.distributed as dist
-            dist.barrier()
+        replicas.barrier(R)
 
     barrier()
     torch.cuda.synchronize()
@@ -257,11 +255,7 @@ def run_engine(args):
     contacts = eng.contact_count()
     launches1 = C.c_long()
     lib().af3d_kernel_launches(eng._h, C.byref(launches1))
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = replicas.max_over_ranks(R, ms, dev)
     ms_step = ms / args.steps
     value = world * args.n * args.steps / (ms / 1e3)
 
@@ -300,12 +294,7 @@ def run_engine(args):
                                         nal.ctypes.data_as(C.c_void_p))
         torch.cuda.synchronize()
         barrier()
-        dt = time.perf_counter() - t0
-        if world > 1:
-            import torch.distributed as dist
-            t = torch.tensor([dt], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            dt = float(t.item())
+        dt = replicas.max_over_ranks(R, time.perf_counter() - t0, dev)
         nbytes = args.n * (PARTICLE.itemsize + 48)
         e2e = {"value": world * args.n * args.e2e_steps / dt, "unit": "clump-steps/s",
                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
@@ -347,9 +336,7 @@ def run_engine(args):
             "clocks": clk,
         }
         print(json.dumps(line), flush=True)
-    if world > 1:
-        import torch.distributed as dist
-        dist.destroy_process_group()
+    replicas.finalize(R)
 
 
 def main():

@@ -215,6 +215,14 @@ void   af3d_sphere_centres (af3d_particle *pp, long n);
    already be set.  Returns the number of clumps placed (< n when the box is too small). */
 long   af3d_lattice_block (af3d_particle *pp, long n, af3d_vec3 lo, af3d_vec3 hi, double pitch,
                            af3d_rng *rng, int max_tries);
+/* Workload generator: a pile settled in the box.  Clumps stand in the columns of a square
+   lattice of the given pitch (x, y), each with a random orientation from rng (redrawn while a
+   sphere would cross a side wall), and are dropped layer by layer: each is lowered until a sphere
+   touches the floor z = lo.z or a sphere already placed in its own or a neighbouring column, then
+   pressed `overlap` further so its resting contacts carry load.  Radius, density and mass must
+   already be set.  Returns the number placed (< n when a clump rises above hi.z). */
+long   af3d_lattice_pile (af3d_particle *pp, long n, af3d_vec3 lo, af3d_vec3 hi, double pitch,
+                          double overlap, af3d_rng *rng, int max_tries);
 
 #ifdef __cplusplus
 }
