@@ -67,6 +67,12 @@ SIGNATURES = [
     ("af3d_get_system", [_P, _P], C.c_int),
     ("af3d_set_grid", [_P, _P], C.c_int),
     ("af3d_get_grid", [_P, _P], C.c_int),
+    ("af3d_create_ensemble", [C.c_int, _P, _P, C.c_long, C.c_int, _P], C.c_int),
+    ("af3d_flume_count", [_P], C.c_int),
+    ("af3d_set_flume_system", [_P, C.c_int, _P, _P], C.c_int),
+    ("af3d_get_flume_system", [_P, C.c_int, _P], C.c_int),
+    ("af3d_set_flume_grid", [_P, C.c_int, _P], C.c_int),
+    ("af3d_get_flume_grid", [_P, C.c_int, _P], C.c_int),
     ("af3d_set_phase", [_P, C.c_int], C.c_int),
     ("af3d_regrid", [_P], C.c_int),
     ("af3d_open_door", [_P], C.c_int),

@@ -1,14 +1,16 @@
 // af3d_capi.cu -- host side of the C ABI declared in include/af3d.h.
 //
 // The context owns every device buffer; the reference's caller-owned arrays become planes of a
-// structure-of-arrays state kept in cell-sorted order.  The per-routine entry points enqueue one
-// kernel (or the cell build) each on the context stream and return; af3d_step() enqueues whole
-// fused steps and replays them from CUDA graphs.  Device-side checks raise bits in a status word
-// that af3d_step() and af3d_get_status() read back; nothing calls exit().
+// structure-of-arrays state kept in cell-sorted order.  A context holds one flume (the plain
+// drop-in) or many independent flumes (a batched ensemble) that share dt and the clock; every
+// flume has its own system_par, Funnel and cell grid, and the cell list is segmented by flume.
+// The per-routine entry points enqueue one kernel (or the cell build) each on the context stream
+// and return; af3d_step() enqueues whole fused steps and replays them from CUDA graphs.
+// Device-side checks raise bits in a status word that af3d_step() and af3d_get_status() read
+// back; nothing calls exit().
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
-#include <mutex>
 #include <string>
 #include <utility>
 #include <vector>
@@ -36,11 +38,14 @@ af3d_status fail(af3d_status code, const std::string &msg) {
 constexpr long kRegridEvery = 2000;   // avalanche_hst.cu:470 and :713 (cc % 2000 == 0)
 constexpr long kKernelsPerCellBuild = 7;   // predict/keys, 3 scan, scatter, rank, permute
 constexpr long kKernelsPerStep = kKernelsPerCellBuild + 2;   // + time advance, fused forces
-constexpr long kKernelsPerRegrid = 3;
+constexpr long kKernelsPerRegrid = 4;
+
+constexpr long kGraphSteps = 64;   // steps per long graph (a multiple of the pointer period 2)
 
 struct StepGraph {
   Planes cur, alt;
   long long *id_cur = nullptr;
+  long steps = 0;
   cudaGraphExec_t exec = nullptr;
 };
 
@@ -49,25 +54,31 @@ struct StepGraph {
 struct af3d_ctx {
   int device = 0;
   long n = 0;
+  int nflumes = 1;
   cudaStream_t st = nullptr;
   bool own_stream = false;
-  af3d_system_par sys{};     // host mirror (time advanced in step with the device)
-  af3d_funnel fun{};
-  af3d_cell_par grid{};      // host mirror, refreshed from the device after a device re-grid
+  std::vector<af3d_system_par> sys;   // host mirrors, one per flume (time: see `time`)
+  std::vector<af3d_funnel> fun;
+  std::vector<af3d_cell_par> grid;    // refreshed from the device after device re-grids
+  std::vector<long> first_id;         // ids of flume f: [first_id[f], first_id[f+1])
+  double time = 0.0;                  // the shared clock, mirrored
   bool have_grid = false;
   long ntags = 9;
   int phase = AF3D_PHASE_AVALANCHE;
   int variant = AF3D_FRICTION_HST;
-  long cc = 0;               // steps done in the current phase
+  long cc = 0;                        // steps done in the current phase
   bool imported = false;
 
   double *plane_mem[2] = {nullptr, nullptr};
   Planes cur{}, alt{};
   long long *id_cur = nullptr, *id_alt = nullptr;
+  int *fl_cur = nullptr, *fl_alt = nullptr;   // flume of every slot
+  int *flume_of_id = nullptr;                  // flume of every clump id
   NbrRec *nbr = nullptr;
   CullRec *cull = nullptr;
   Cells cells{};
   DevScalars *d = nullptr;
+  DevFlume *flumes = nullptr;
   bool records_valid = false;   // records reflect the current planes
   bool cells_valid = false;     // start[] describes the current layout
 
@@ -76,7 +87,7 @@ struct af3d_ctx {
   long long *d_tmp = nullptr;
   unsigned long long *d_count = nullptr;
 
-  StepGraph graphs[2];
+  StepGraph graphs[4];
   int graph_next = 0;
   long launches = 0;          // kernels executed (graph replays included)
 
@@ -104,20 +115,39 @@ void drop_graphs(af3d_ctx *c) {
   }
 }
 
-af3d_status push_scalars(af3d_ctx *c) {
-  // Host-side system/grid edits go to the device on the context stream (ordered with kernels).
-  AF3D_CUDA(cudaMemcpyAsync(&c->d->sys, &c->sys, sizeof(af3d_system_par), cudaMemcpyHostToDevice, c->st));
-  AF3D_CUDA(cudaMemcpyAsync(&c->d->fun, &c->fun, sizeof(af3d_funnel), cudaMemcpyHostToDevice, c->st));
+// Host-side parameter edits (system_par, Funnel, clock, phase, friction) to the device; the
+// device-derived grids are read back first so that they are not overwritten.
+af3d_status push_params(af3d_ctx *c) {
+  std::vector<DevFlume> fl(c->nflumes);
+  AF3D_CUDA(cudaMemcpyAsync(fl.data(), c->flumes, sizeof(DevFlume) * c->nflumes, cudaMemcpyDeviceToHost, c->st));
+  AF3D_CUDA(cudaStreamSynchronize(c->st));
+  for (int f = 0; f < c->nflumes; f++) {
+    fl[f].sys = c->sys[f];
+    fl[f].sys.time = c->time;
+    fl[f].fun = c->fun[f];
+  }
+  AF3D_CUDA(cudaMemcpyAsync(c->flumes, fl.data(), sizeof(DevFlume) * c->nflumes, cudaMemcpyHostToDevice, c->st));
+  AF3D_CUDA(cudaMemcpyAsync(&c->d->time, &c->time, sizeof(double), cudaMemcpyHostToDevice, c->st));
   AF3D_CUDA(cudaMemcpyAsync(&c->d->phase, &c->phase, sizeof(int), cudaMemcpyHostToDevice, c->st));
   AF3D_CUDA(cudaMemcpyAsync(&c->d->variant, &c->variant, sizeof(int), cudaMemcpyHostToDevice, c->st));
   AF3D_CUDA(cudaStreamSynchronize(c->st));
   return AF3D_OK;
 }
 
-af3d_status ensure_buckets(af3d_ctx *c, long ncell3) {
-  const long need = ncell3 + c->n + 1;
+af3d_status pull_params(af3d_ctx *c) {
+  std::vector<DevFlume> fl(c->nflumes);
+  AF3D_CUDA(cudaMemcpyAsync(fl.data(), c->flumes, sizeof(DevFlume) * c->nflumes, cudaMemcpyDeviceToHost, c->st));
+  AF3D_CUDA(cudaMemcpyAsync(&c->time, &c->d->time, sizeof(double), cudaMemcpyDeviceToHost, c->st));
+  AF3D_CUDA(cudaStreamSynchronize(c->st));
+  for (int f = 0; f < c->nflumes; f++) c->grid[f] = fl[f].grid;
+  return AF3D_OK;
+}
+
+af3d_status ensure_buckets(af3d_ctx *c, long ncell_total) {
+  const long need = ncell_total + c->n + 1;
   if (need <= c->cells.cap && c->cells.count) return AF3D_OK;
   const long cap = std::max<long>(need + need / 2, 1024);
+  if (cap > (1L << 31) - 2) return fail(AF3D_ERR_NOMEM, "cell grid too large for 32-bit bucket indices");
   AF3D_CUDA(cudaStreamSynchronize(c->st));
   cudaFree(c->cells.count);
   cudaFree(c->cells.start);
@@ -133,78 +163,98 @@ af3d_status ensure_buckets(af3d_ctx *c, long ncell3) {
   return AF3D_OK;
 }
 
-af3d_status set_grid_device(af3d_ctx *c, const af3d_cell_par &g) {
-  af3d_status s = ensure_buckets(c, g.ncell3);
+// Install host grids for every flume (cell offsets in flume order).
+af3d_status set_grids_device(af3d_ctx *c) {
+  long long total = 0;
+  for (int f = 0; f < c->nflumes; f++) total += c->grid[f].ncell3;
+  af3d_status s = ensure_buckets(c, total);
   if (s) return s;
-  c->grid = g;
-  c->have_grid = true;
-  AF3D_CUDA(cudaMemcpyAsync(&c->d->grid, &c->grid, sizeof(af3d_cell_par), cudaMemcpyHostToDevice, c->st));
+  std::vector<DevFlume> fl(c->nflumes);
+  AF3D_CUDA(cudaMemcpyAsync(fl.data(), c->flumes, sizeof(DevFlume) * c->nflumes, cudaMemcpyDeviceToHost, c->st));
   AF3D_CUDA(cudaStreamSynchronize(c->st));
+  long long off = 0;
+  for (int f = 0; f < c->nflumes; f++) {
+    fl[f].grid = c->grid[f];
+    fl[f].cell_off = off;
+    off += c->grid[f].ncell3;
+  }
+  AF3D_CUDA(cudaMemcpyAsync(c->flumes, fl.data(), sizeof(DevFlume) * c->nflumes, cudaMemcpyHostToDevice, c->st));
+  AF3D_CUDA(cudaMemcpyAsync(&c->d->ncell_total, &total, sizeof(long long), cudaMemcpyHostToDevice, c->st));
+  AF3D_CUDA(cudaStreamSynchronize(c->st));
+  c->have_grid = true;
   c->cells_valid = false;
   return AF3D_OK;
 }
 
-// Device re-grid, then adopt the result on the host (grow the bucket buffers if needed).
+// Device re-grid of every flume, then adopt the result on the host (grow the bucket buffers and
+// commit again if the new grids did not fit).
 af3d_status regrid(af3d_ctx *c) {
-  if (c->n == 0) return AF3D_OK;   // no clump to bound (cell_dim reads pp[0]): keep the grid
-  launch_regrid(c->L(), c->cur, c->d, c->cells.cap);
+  if (c->n == 0) return AF3D_OK;   // no clump to bound (cell_dim reads pp[0]): keep the grids
+  launch_regrid(c->L(), c->cur, c->d, c->fl_cur, c->nflumes, c->cells.cap);
   c->launches += kKernelsPerRegrid;
   long long pending = 0;
-  AF3D_CUDA(cudaMemcpyAsync(&pending, &c->d->pending_ncell3, sizeof(long long), cudaMemcpyDeviceToHost, c->st));
+  AF3D_CUDA(cudaMemcpyAsync(&pending, &c->d->pending, sizeof(long long), cudaMemcpyDeviceToHost, c->st));
   AF3D_CUDA(cudaStreamSynchronize(c->st));
   if (pending < 0) return fail(AF3D_ERR_GRID_ESCAPE, "re-grid produced an empty grid");
   if (pending > 0) {
-    af3d_cell_par g;
-    AF3D_CUDA(cudaMemcpy(&g, &c->d->pending, sizeof(g), cudaMemcpyDeviceToHost));
-    return set_grid_device(c, g);
+    af3d_status s = ensure_buckets(c, pending);
+    if (s) return s;
+    launch_commit_grids(c->st, c->d, c->nflumes, c->n, c->cells.cap);
+    AF3D_CUDA(cudaMemcpyAsync(&pending, &c->d->pending, sizeof(long long), cudaMemcpyDeviceToHost, c->st));
+    AF3D_CUDA(cudaStreamSynchronize(c->st));
+    if (pending != 0) return fail(AF3D_ERR_NOMEM, "re-grid does not fit after growing the buckets");
   }
-  AF3D_CUDA(cudaMemcpy(&c->grid, &c->d->grid, sizeof(af3d_cell_par), cudaMemcpyDeviceToHost));
   c->have_grid = true;
-  return AF3D_OK;
+  c->cells_valid = false;
+  return pull_params(c);
 }
 
 // clear_cell + clear_ocup + cell_locate: keys (optionally fused with the predictor), counting
 // sort, permutation of every plane into the new order, neighbour records.
 void enqueue_cell_build(af3d_ctx *c, bool predict, bool t_prev, bool ft = true) {
-  launch_predict(c->L(), c->cur, c->d, predict, true, t_prev, c->cells, c->id_cur);
+  launch_predict(c->L(), c->cur, c->d, predict, true, t_prev, c->cells, c->id_cur, c->fl_cur);
   launch_sort(c->L(), c->d, c->cells, c->id_cur, c->ntags);
-  launch_permute_records(c->L(), c->cur, c->alt, c->cells.perm, c->id_cur, c->id_alt, c->nbr, c->cull, ft);
+  launch_permute_records(c->L(), c->cur, c->alt, c->cells.perm, c->id_cur, c->id_alt, c->fl_cur, c->fl_alt,
+                         c->nbr, c->cull, ft);
   std::swap(c->cur, c->alt);
   std::swap(c->id_cur, c->id_alt);
+  std::swap(c->fl_cur, c->fl_alt);
 }
 
 // One fused step: time += dt, init_Verlet + cell build, every force of the phase, get_accel,
 // finish_Verlet, and the acceleration swap.
 void enqueue_fused_step(af3d_ctx *c) {
   launch_advance_time(c->st, c->d);
-  enqueue_cell_build(c, true, true, false);   // F, T are not read by the fused force kernel
-  launch_fused_forces(c->L(), c->cur, c->alt, c->d, c->nbr, c->cull, c->cells.start, false);
+  enqueue_cell_build(c, true, true, false);   // F, T and a_f are rewritten before being read
+  launch_fused_forces(c->L(), c->cur, c->alt, c->d, c->fl_cur, c->nbr, c->cull, c->cells.start, false);
   swap_velocity_planes(c->cur, c->alt);
   swap_accel_planes(c->cur);
   swap_accel_planes(c->alt);
 }
 
 af3d_status run_steps(af3d_ctx *c, long m) {
-  // Pairs of steps return the plane pointers to where they started, so a captured two-step
-  // graph can be replayed; an odd step is enqueued directly.
+  // Every pair of steps returns the plane pointers to where they started, so captured graphs of
+  // an even number of steps can be replayed: 64-step graphs while at least 64 steps remain,
+  // then two-step graphs; an odd last step is enqueued directly.
   while (m >= 2) {
+    const long len = m >= kGraphSteps ? kGraphSteps : 2;
     StepGraph *g = nullptr;
     for (auto &cand : c->graphs)
-      if (cand.exec && cand.id_cur == c->id_cur && same_planes(cand.cur, c->cur) &&
+      if (cand.exec && cand.steps == len && cand.id_cur == c->id_cur && same_planes(cand.cur, c->cur) &&
           same_planes(cand.alt, c->alt))
         g = &cand;
     if (!g) {
       g = &c->graphs[c->graph_next];
-      c->graph_next ^= 1;
+      c->graph_next = (c->graph_next + 1) % 4;
       if (g->exec) cudaGraphExecDestroy(g->exec);
       *g = StepGraph{};
       g->cur = c->cur;
       g->alt = c->alt;
       g->id_cur = c->id_cur;
+      g->steps = len;
       cudaGraph_t graph;
       AF3D_CUDA(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
-      enqueue_fused_step(c);
-      enqueue_fused_step(c);
+      for (long i = 0; i < len; i++) enqueue_fused_step(c);
       AF3D_CUDA(cudaStreamEndCapture(c->st, &graph));
       cudaError_t e = cudaGraphInstantiate(&g->exec, graph, 0);
       cudaGraphDestroy(graph);
@@ -214,8 +264,8 @@ af3d_status run_steps(af3d_ctx *c, long m) {
       }
     }
     AF3D_CUDA(cudaGraphLaunch(g->exec, c->st));
-    c->launches += 2 * kKernelsPerStep;
-    m -= 2;
+    c->launches += len * kKernelsPerStep;
+    m -= len;
   }
   if (m == 1) {
     enqueue_fused_step(c);
@@ -250,6 +300,24 @@ af3d_status ensure_records(af3d_ctx *c) {
   return AF3D_OK;
 }
 
+// Plane-resident per-clump vectors back to clump-id order on the host.
+af3d_status gather_by_id(af3d_ctx *c, int plane0, af3d_vec3 *a, af3d_vec3 *b) {
+  if (c->n == 0) return AF3D_OK;
+  std::vector<double> hp(6 * (size_t)c->n);
+  std::vector<long long> ids((size_t)c->n);
+  for (int k = 0; k < 6; k++)
+    AF3D_CUDA(cudaMemcpyAsync(hp.data() + (size_t)k * c->n, c->cur.p[plane0 + k], sizeof(double) * c->n,
+                              cudaMemcpyDeviceToHost, c->st));
+  AF3D_CUDA(cudaMemcpyAsync(ids.data(), c->id_cur, sizeof(long long) * c->n, cudaMemcpyDeviceToHost, c->st));
+  AF3D_CUDA(cudaStreamSynchronize(c->st));
+  for (long s = 0; s < c->n; s++) {
+    const long long i = ids[s];
+    if (a) a[i] = {hp[s], hp[c->n + s], hp[2 * c->n + s]};
+    if (b) b[i] = {hp[3 * c->n + s], hp[4 * c->n + s], hp[5 * c->n + s]};
+  }
+  return AF3D_OK;
+}
+
 #define CHECK_CTX(c)                                                                            \
   do {                                                                                          \
     if (!(c)) return fail(AF3D_ERR_ARG, "null context");                                       \
@@ -259,6 +327,10 @@ af3d_status ensure_records(af3d_ctx *c) {
     CHECK_CTX(c);                                                                               \
     if (!(c)->imported) return fail(AF3D_ERR_ARG, "no particles imported");                    \
   } while (0)
+#define CHECK_FLUME(c, f)                                                                       \
+  do {                                                                                          \
+    if ((f) < 0 || (f) >= (c)->nflumes) return fail(AF3D_ERR_ARG, "flume index out of range");  \
+  } while (0)
 
 }  // namespace
 
@@ -267,15 +339,28 @@ extern "C" {
 const char *af3d_last_error(void) { return g_last_error.c_str(); }
 int af3d_abi_version(void) { return AF3D_ABI_VERSION; }
 
-af3d_status af3d_create(const af3d_system_par *sys, const af3d_funnel *fun, long ntags, int phase,
-                        af3d_ctx **out) {
-  if (!sys || !fun || !out) return fail(AF3D_ERR_ARG, "null argument");
-  if (sys->npart < 0 || sys->npart > (1L << 28)) return fail(AF3D_ERR_ARG, "npart out of range (0..2^28)");
+af3d_status af3d_create_ensemble(int nflumes, const af3d_system_par *sys, const af3d_funnel *fun,
+                                 long ntags, int phase, af3d_ctx **out) {
+  if (!sys || !fun || !out || nflumes < 1) return fail(AF3D_ERR_ARG, "bad argument");
   *out = nullptr;
+  long total = 0;
+  for (int f = 0; f < nflumes; f++) {
+    if (sys[f].npart < 0) return fail(AF3D_ERR_ARG, "negative npart");
+    if (sys[f].dt != sys[0].dt || sys[f].hdt != sys[0].hdt)
+      return fail(AF3D_ERR_ARG, "the flumes of an ensemble share dt");
+    total += sys[f].npart;
+  }
+  if (total > (1L << 28)) return fail(AF3D_ERR_ARG, "too many clumps (at most 2^28)");
   af3d_ctx *c = new af3d_ctx();
-  c->n = sys->npart;
-  c->sys = *sys;
-  c->fun = *fun;
+  c->n = total;
+  c->nflumes = nflumes;
+  c->sys.assign(sys, sys + nflumes);
+  c->fun.assign(fun, fun + nflumes);
+  c->grid.assign(nflumes, af3d_cell_par{});
+  for (auto &g : c->grid) g.ntags = ntags;
+  c->first_id.resize(nflumes + 1, 0);
+  for (int f = 0; f < nflumes; f++) c->first_id[f + 1] = c->first_id[f] + sys[f].npart;
+  c->time = sys[0].time;
   c->ntags = ntags;
   c->phase = phase;
   cudaError_t e = cudaGetDevice(&c->device);
@@ -285,21 +370,24 @@ af3d_status af3d_create(const af3d_system_par *sys, const af3d_funnel *fun, long
     return fail(AF3D_ERR_CUDA, std::string("CUDA unavailable: ") + cudaGetErrorString(e));
   }
   c->own_stream = true;
-  c->grid.ntags = ntags;
   const long n = std::max<long>(c->n, 1);
-  auto alloc = [&](void **p, size_t bytes) { return cudaMalloc(p, bytes); };
   bool ok = true;
-  for (int b = 0; b < 2 && ok; b++) ok = alloc((void **)&c->plane_mem[b], sizeof(double) * n * NPLANES) == cudaSuccess;
-  ok = ok && alloc((void **)&c->id_cur, sizeof(long long) * n) == cudaSuccess;
-  ok = ok && alloc((void **)&c->id_alt, sizeof(long long) * n) == cudaSuccess;
-  ok = ok && alloc((void **)&c->nbr, sizeof(NbrRec) * n) == cudaSuccess;
-  ok = ok && alloc((void **)&c->cull, sizeof(CullRec) * n) == cudaSuccess;
-  ok = ok && alloc((void **)&c->cells.key, sizeof(int) * n) == cudaSuccess;
-  ok = ok && alloc((void **)&c->cells.rank_tmp, sizeof(int) * n) == cudaSuccess;
-  ok = ok && alloc((void **)&c->cells.tmp_slot, sizeof(int) * n) == cudaSuccess;
-  ok = ok && alloc((void **)&c->cells.perm, sizeof(int) * n) == cudaSuccess;
-  ok = ok && alloc((void **)&c->d, sizeof(DevScalars)) == cudaSuccess;
-  ok = ok && alloc((void **)&c->d_count, sizeof(unsigned long long)) == cudaSuccess;
+  for (int b = 0; b < 2 && ok; b++)
+    ok = cudaMalloc((void **)&c->plane_mem[b], sizeof(double) * n * NPLANES) == cudaSuccess;
+  ok = ok && cudaMalloc((void **)&c->id_cur, sizeof(long long) * n) == cudaSuccess;
+  ok = ok && cudaMalloc((void **)&c->id_alt, sizeof(long long) * n) == cudaSuccess;
+  ok = ok && cudaMalloc((void **)&c->fl_cur, sizeof(int) * n) == cudaSuccess;
+  ok = ok && cudaMalloc((void **)&c->fl_alt, sizeof(int) * n) == cudaSuccess;
+  ok = ok && cudaMalloc((void **)&c->flume_of_id, sizeof(int) * n) == cudaSuccess;
+  ok = ok && cudaMalloc((void **)&c->nbr, sizeof(NbrRec) * n) == cudaSuccess;
+  ok = ok && cudaMalloc((void **)&c->cull, sizeof(CullRec) * n) == cudaSuccess;
+  ok = ok && cudaMalloc((void **)&c->cells.key, sizeof(int) * n) == cudaSuccess;
+  ok = ok && cudaMalloc((void **)&c->cells.rank_tmp, sizeof(int) * n) == cudaSuccess;
+  ok = ok && cudaMalloc((void **)&c->cells.tmp_slot, sizeof(int) * n) == cudaSuccess;
+  ok = ok && cudaMalloc((void **)&c->cells.perm, sizeof(int) * n) == cudaSuccess;
+  ok = ok && cudaMalloc((void **)&c->d, sizeof(DevScalars)) == cudaSuccess;
+  ok = ok && cudaMalloc((void **)&c->flumes, sizeof(DevFlume) * nflumes) == cudaSuccess;
+  ok = ok && cudaMalloc((void **)&c->d_count, sizeof(unsigned long long)) == cudaSuccess;
   if (!ok) {
     af3d_destroy(c);
     return fail(AF3D_ERR_NOMEM, "device allocation failed");
@@ -308,17 +396,42 @@ af3d_status af3d_create(const af3d_system_par *sys, const af3d_funnel *fun, long
     c->cur.p[k] = c->plane_mem[0] + (size_t)k * n;
     c->alt.p[k] = c->plane_mem[1] + (size_t)k * n;
   }
+  std::vector<int> fid((size_t)n, 0);
+  for (int f = 0; f < nflumes; f++)
+    for (long i = c->first_id[f]; i < c->first_id[f + 1]; i++) fid[i] = f;
+  std::vector<DevFlume> fl(nflumes);
+  std::memset(fl.data(), 0, sizeof(DevFlume) * nflumes);
+  for (int f = 0; f < nflumes; f++) {
+    fl[f].sys = c->sys[f];
+    fl[f].fun = c->fun[f];
+    fl[f].grid = c->grid[f];
+    fl[f].pending = c->grid[f];
+  }
+  DevScalars ds;
+  std::memset(&ds, 0, sizeof ds);
+  ds.time = c->time;
+  ds.time_prev = c->time;
+  ds.phase = phase;
+  ds.variant = c->variant;
+  ds.nflumes = nflumes;
+  ds.flumes = c->flumes;
   cudaMemsetAsync(c->plane_mem[0], 0, sizeof(double) * n * NPLANES, c->st);
   cudaMemsetAsync(c->plane_mem[1], 0, sizeof(double) * n * NPLANES, c->st);
-  cudaMemsetAsync(c->d, 0, sizeof(DevScalars), c->st);
-  cudaMemcpyAsync(&c->d->grid, &c->grid, sizeof(af3d_cell_par), cudaMemcpyHostToDevice, c->st);
-  af3d_status s = push_scalars(c);
-  if (s) {
+  cudaMemcpyAsync(c->flume_of_id, fid.data(), sizeof(int) * n, cudaMemcpyHostToDevice, c->st);
+  cudaMemcpyAsync(c->flumes, fl.data(), sizeof(DevFlume) * nflumes, cudaMemcpyHostToDevice, c->st);
+  cudaMemcpyAsync(c->d, &ds, sizeof ds, cudaMemcpyHostToDevice, c->st);
+  e = cudaStreamSynchronize(c->st);
+  if (e != cudaSuccess) {
     af3d_destroy(c);
-    return s;
+    return fail(AF3D_ERR_CUDA, std::string("context set-up: ") + cudaGetErrorString(e));
   }
   *out = c;
   return AF3D_OK;
+}
+
+af3d_status af3d_create(const af3d_system_par *sys, const af3d_funnel *fun, long ntags, int phase,
+                        af3d_ctx **out) {
+  return af3d_create_ensemble(1, sys, fun, ntags, phase, out);
 }
 
 af3d_status af3d_destroy(af3d_ctx *c) {
@@ -326,9 +439,10 @@ af3d_status af3d_destroy(af3d_ctx *c) {
   if (c->st) cudaStreamSynchronize(c->st);
   drop_graphs(c);
   for (void *p : {(void *)c->plane_mem[0], (void *)c->plane_mem[1], (void *)c->id_cur, (void *)c->id_alt,
-                  (void *)c->nbr, (void *)c->cull, (void *)c->cells.key, (void *)c->cells.rank_tmp,
-                  (void *)c->cells.tmp_slot, (void *)c->cells.perm, (void *)c->cells.count,
-                  (void *)c->cells.start, (void *)c->cells.block_sums, (void *)c->d, (void *)c->d_aos,
+                  (void *)c->fl_cur, (void *)c->fl_alt, (void *)c->flume_of_id, (void *)c->nbr,
+                  (void *)c->cull, (void *)c->cells.key, (void *)c->cells.rank_tmp, (void *)c->cells.tmp_slot,
+                  (void *)c->cells.perm, (void *)c->cells.count, (void *)c->cells.start,
+                  (void *)c->cells.block_sums, (void *)c->d, (void *)c->flumes, (void *)c->d_aos,
                   (void *)c->d_acc, (void *)c->d_anga, (void *)c->d_tmp, (void *)c->d_count})
     if (p) cudaFree(p);
   if (c->own_stream && c->st) cudaStreamDestroy(c->st);
@@ -356,7 +470,7 @@ af3d_status af3d_set_friction(af3d_ctx *c, int variant) {
   if (variant != AF3D_FRICTION_HST && variant != AF3D_FRICTION_DEV)
     return fail(AF3D_ERR_ARG, "unknown friction variant");
   c->variant = variant;
-  return push_scalars(c);
+  return push_params(c);
 }
 
 af3d_status af3d_import_particles(af3d_ctx *c, const af3d_particle *pp, const af3d_vec3 *acc,
@@ -372,8 +486,8 @@ af3d_status af3d_import_particles(af3d_ctx *c, const af3d_particle *pp, const af
     if (acc) AF3D_CUDA(cudaMemcpyAsync(c->d_acc, acc, sizeof(double) * 3 * c->n, cudaMemcpyHostToDevice, c->st));
     if (anga) AF3D_CUDA(cudaMemcpyAsync(c->d_anga, anga, sizeof(double) * 3 * c->n, cudaMemcpyHostToDevice, c->st));
   }
-  launch_aos_to_planes(c->L(), c->d_aos, acc ? c->d_acc : nullptr, anga ? c->d_anga : nullptr, c->cur,
-                       c->id_cur);
+  launch_aos_to_planes(c->L(), c->d_aos, acc ? c->d_acc : nullptr, anga ? c->d_anga : nullptr, c->flume_of_id,
+                       c->cur, c->id_cur, c->fl_cur);
   AF3D_CUDA(cudaStreamSynchronize(c->st));
   AF3D_CUDA(cudaGetLastError());
   c->imported = true;
@@ -387,7 +501,7 @@ af3d_status af3d_import_particles(af3d_ctx *c, const af3d_particle *pp, const af
 af3d_status af3d_export_particles(af3d_ctx *c, af3d_particle *pp, af3d_vec3 *acc, af3d_vec3 *anga) {
   CHECK_STATE(c);
   if (!pp && c->n > 0) return fail(AF3D_ERR_ARG, "null particle array");
-  launch_planes_to_aos(c->L(), c->cur, c->id_cur, c->d_aos, acc ? c->d_acc : nullptr,
+  launch_planes_to_aos(c->L(), c->cur, c->id_cur, c->fl_cur, c->d_aos, acc ? c->d_acc : nullptr,
                        anga ? c->d_anga : nullptr, c->d);
   if (c->n > 0) {
     AF3D_CUDA(cudaMemcpyAsync(pp, c->d_aos, sizeof(af3d_particle) * c->n, cudaMemcpyDeviceToHost, c->st));
@@ -399,80 +513,105 @@ af3d_status af3d_export_particles(af3d_ctx *c, af3d_particle *pp, af3d_vec3 *acc
   return AF3D_OK;
 }
 
-af3d_status af3d_set_system(af3d_ctx *c, const af3d_system_par *sys) {
+af3d_status af3d_set_flume_system(af3d_ctx *c, int f, const af3d_system_par *sys, const af3d_funnel *fun) {
   CHECK_CTX(c);
-  if (!sys || sys->npart != c->n) return fail(AF3D_ERR_ARG, "system_par npart differs from the context");
-  c->sys = *sys;
-  return push_scalars(c);
+  CHECK_FLUME(c, f);
+  if (!sys || sys->npart != c->first_id[f + 1] - c->first_id[f])
+    return fail(AF3D_ERR_ARG, "system_par npart differs from the flume's");
+  if (sys->dt != c->sys[0].dt && c->nflumes > 1) return fail(AF3D_ERR_ARG, "the flumes share dt");
+  af3d_status s = pull_params(c);
+  if (s) return s;
+  c->sys[f] = *sys;
+  if (fun) c->fun[f] = *fun;
+  c->time = sys->time;
+  return push_params(c);
 }
 
-af3d_status af3d_get_system(af3d_ctx *c, af3d_system_par *sys) {
+af3d_status af3d_set_system(af3d_ctx *c, const af3d_system_par *sys) {
   CHECK_CTX(c);
+  return af3d_set_flume_system(c, 0, sys, nullptr);
+}
+
+af3d_status af3d_get_flume_system(af3d_ctx *c, int f, af3d_system_par *sys) {
+  CHECK_CTX(c);
+  CHECK_FLUME(c, f);
   if (!sys) return fail(AF3D_ERR_ARG, "null argument");
-  AF3D_CUDA(cudaMemcpyAsync(&c->sys, &c->d->sys, sizeof(af3d_system_par), cudaMemcpyDeviceToHost, c->st));
-  AF3D_CUDA(cudaStreamSynchronize(c->st));
-  *sys = c->sys;
+  af3d_status s = pull_params(c);
+  if (s) return s;
+  *sys = c->sys[f];
+  sys->time = c->time;
   return AF3D_OK;
 }
 
-af3d_status af3d_set_grid(af3d_ctx *c, const af3d_cell_par *g) {
+af3d_status af3d_get_system(af3d_ctx *c, af3d_system_par *sys) { return af3d_get_flume_system(c, 0, sys); }
+
+af3d_status af3d_set_flume_grid(af3d_ctx *c, int f, const af3d_cell_par *g) {
   CHECK_CTX(c);
+  CHECK_FLUME(c, f);
   if (!g || g->ncell.x <= 0 || g->ncell.y <= 0 || g->ncell.z <= 0 ||
       g->ncell3 != g->ncell.x * g->ncell.y * g->ncell.z)
     return fail(AF3D_ERR_ARG, "inconsistent cell_par");
-  af3d_cell_par gg = *g;
-  gg.ntags = c->ntags;
-  return set_grid_device(c, gg);
+  if (c->have_grid) {
+    af3d_status s = pull_params(c);
+    if (s) return s;
+  } else {
+    for (auto &gg : c->grid)   // other flumes get a copy until they are set or re-gridded
+      if (gg.ncell3 <= 0) gg = *g;
+  }
+  c->grid[f] = *g;
+  c->grid[f].ntags = c->ntags;
+  c->grid[f].ntot = c->grid[f].ncell3 * c->ntags;
+  return set_grids_device(c);
 }
 
-af3d_status af3d_get_grid(af3d_ctx *c, af3d_cell_par *g) {
+af3d_status af3d_set_grid(af3d_ctx *c, const af3d_cell_par *g) { return af3d_set_flume_grid(c, 0, g); }
+
+af3d_status af3d_get_flume_grid(af3d_ctx *c, int f, af3d_cell_par *g) {
   CHECK_CTX(c);
+  CHECK_FLUME(c, f);
   if (!g) return fail(AF3D_ERR_ARG, "null argument");
-  AF3D_CUDA(cudaMemcpyAsync(&c->grid, &c->d->grid, sizeof(af3d_cell_par), cudaMemcpyDeviceToHost, c->st));
-  AF3D_CUDA(cudaStreamSynchronize(c->st));
-  *g = c->grid;
+  af3d_status s = pull_params(c);
+  if (s) return s;
+  *g = c->grid[f];
   return AF3D_OK;
 }
+
+af3d_status af3d_get_grid(af3d_ctx *c, af3d_cell_par *g) { return af3d_get_flume_grid(c, 0, g); }
+
+int af3d_flume_count(af3d_ctx *c) { return c ? c->nflumes : 0; }
 
 af3d_status af3d_set_phase(af3d_ctx *c, int phase) {
   CHECK_CTX(c);
   if (phase != AF3D_PHASE_FILL && phase != AF3D_PHASE_AVALANCHE) return fail(AF3D_ERR_ARG, "bad phase");
-  af3d_status s = af3d_get_system(c, &c->sys);
+  af3d_status s = pull_params(c);
   if (s) return s;
   c->phase = phase;
   c->cc = 0;
-  return push_scalars(c);
+  return push_params(c);
 }
 
 af3d_status af3d_regrid(af3d_ctx *c) {
   CHECK_STATE(c);
-  c->grid.ntags = c->ntags;
-  if (!c->have_grid) {
-    af3d_cell_par g{};
-    g.ntags = c->ntags;
-    AF3D_CUDA(cudaMemcpyAsync(&c->d->grid, &g, sizeof(g), cudaMemcpyHostToDevice, c->st));
-  }
-  af3d_status s = regrid(c);
-  c->cells_valid = false;
-  return s;
+  return regrid(c);
 }
 
 af3d_status af3d_open_door(af3d_ctx *c) {
   CHECK_CTX(c);
-  af3d_status s = af3d_get_system(c, &c->sys);
+  af3d_status s = pull_params(c);
   if (s) return s;
-  c->sys.side.x = (70.0 + c->sys.Lflume) * c->sys.cost;   // xfinal, avalanche_hst.cu:116
-  c->sys.time = 0.0;
+  for (auto &sy : c->sys) sy.side.x = (70.0 + sy.Lflume) * sy.cost;   // xfinal, avalanche_hst.cu:116
+  c->time = 0.0;
   c->phase = AF3D_PHASE_AVALANCHE;
   c->cc = 0;
-  return push_scalars(c);
+  return push_params(c);
 }
 
 // ---- per-routine entry points ----
 
 af3d_status af3d_init_verlet(af3d_ctx *c) {
   CHECK_STATE(c);
-  launch_predict(c->L(), c->cur, c->d, true, false, false, c->cells, c->id_cur);
+  launch_predict(c->L(), c->cur, c->d, true, false, false, c->cells, c->id_cur, c->fl_cur);
+  c->launches++;
   c->records_valid = false;
   return AF3D_OK;
 }
@@ -480,7 +619,8 @@ af3d_status af3d_init_verlet(af3d_ctx *c) {
 af3d_status af3d_advance_time(af3d_ctx *c) {
   CHECK_CTX(c);
   launch_advance_time(c->st, c->d);
-  c->sys.time = c->sys.time + c->sys.dt;
+  c->launches++;
+  c->time = c->time + c->sys[0].dt;
   return AF3D_OK;
 }
 
@@ -494,6 +634,7 @@ af3d_status af3d_rotate_vectors(af3d_ctx *c) {
 af3d_status af3d_clear_forces(af3d_ctx *c) {
   CHECK_STATE(c);
   launch_clear_forces(c->L(), c->cur);
+  c->launches++;
   return AF3D_OK;
 }
 
@@ -501,60 +642,50 @@ af3d_status af3d_cell_build(af3d_ctx *c) {
   CHECK_STATE(c);
   if (!c->have_grid) return fail(AF3D_ERR_ARG, "no grid");
   enqueue_cell_build(c, false, false);
+  c->launches += kKernelsPerCellBuild;
   c->records_valid = true;
   c->cells_valid = true;
   return AF3D_OK;
 }
 
+static af3d_status boundary(af3d_ctx *c, int routine) {
+  CHECK_STATE(c);
+  launch_boundary(c->L(), c->cur, c->d, c->fl_cur, routine);
+  c->launches++;
+  return AF3D_OK;
+}
+
 af3d_status af3d_force_hop(af3d_ctx *c, int nw) {
-  CHECK_STATE(c);
+  CHECK_CTX(c);
   if (nw < 0 || nw > 2) return fail(AF3D_ERR_ARG, "nw must be 0, 1 or 2");
-  launch_boundary(c->L(), c->cur, c->d, R_HOP0 + nw);
-  return AF3D_OK;
+  return boundary(c, R_HOP0 + nw);
 }
-
-af3d_status af3d_force_funnel(af3d_ctx *c) {
-  CHECK_STATE(c);
-  launch_boundary(c->L(), c->cur, c->d, R_FUNNEL);
-  return AF3D_OK;
-}
-
-af3d_status af3d_force_fcorners(af3d_ctx *c) {
-  CHECK_STATE(c);
-  launch_boundary(c->L(), c->cur, c->d, R_FCORNERS);
-  return AF3D_OK;
-}
-
-af3d_status af3d_force_walls(af3d_ctx *c) {
-  CHECK_STATE(c);
-  launch_boundary(c->L(), c->cur, c->d, R_WALLS);
-  return AF3D_OK;
-}
-
-af3d_status af3d_force_flume(af3d_ctx *c) {
-  CHECK_STATE(c);
-  launch_boundary(c->L(), c->cur, c->d, R_FLUME);
-  return AF3D_OK;
-}
+af3d_status af3d_force_funnel(af3d_ctx *c) { return boundary(c, R_FUNNEL); }
+af3d_status af3d_force_fcorners(af3d_ctx *c) { return boundary(c, R_FCORNERS); }
+af3d_status af3d_force_walls(af3d_ctx *c) { return boundary(c, R_WALLS); }
+af3d_status af3d_force_flume(af3d_ctx *c) { return boundary(c, R_FLUME); }
 
 af3d_status af3d_force_part(af3d_ctx *c, int sph_id) {
   CHECK_STATE(c);
   if (sph_id < 0 || sph_id > 16) return fail(AF3D_ERR_ARG, "sph_id must be 0..16");
   af3d_status s = ensure_records(c);
   if (s) return s;
-  launch_part(c->L(), c->cur, c->d, c->nbr, c->cull, c->cells.start, sph_id);
+  launch_part(c->L(), c->cur, c->d, c->fl_cur, c->nbr, c->cull, c->cells.start, sph_id);
+  c->launches++;
   return AF3D_OK;
 }
 
 af3d_status af3d_get_accel(af3d_ctx *c) {
   CHECK_STATE(c);
-  launch_get_accel(c->L(), c->cur, c->d);
+  launch_get_accel(c->L(), c->cur, c->d, c->fl_cur);
+  c->launches++;
   return AF3D_OK;
 }
 
 af3d_status af3d_finish_verlet(af3d_ctx *c) {
   CHECK_STATE(c);
-  launch_finish_verlet(c->L(), c->cur, c->d);
+  launch_finish_verlet(c->L(), c->cur, c->d, c->fl_cur);
+  c->launches++;
   c->records_valid = false;
   return AF3D_OK;
 }
@@ -573,7 +704,8 @@ af3d_status af3d_forces(af3d_ctx *c) {
   enqueue_cell_build(c, false, false);
   c->cells_valid = true;
   // Corrected velocities go to the dead plane set and are dropped: this pass stops at get_accel.
-  launch_fused_forces(c->L(), c->cur, c->alt, c->d, c->nbr, c->cull, c->cells.start, true);
+  launch_fused_forces(c->L(), c->cur, c->alt, c->d, c->fl_cur, c->nbr, c->cull, c->cells.start, true);
+  c->launches += kKernelsPerCellBuild + 1;
   c->records_valid = true;
   int flags = 0;
   af3d_status s = read_status(c, &flags);
@@ -591,7 +723,7 @@ af3d_status af3d_step(af3d_ctx *c, long k) {
     const long m = std::min(k, to_regrid + 1);
     af3d_status s = run_steps(c, m);
     if (s) return s;
-    for (long i = 0; i < m; i++) c->sys.time = c->sys.time + c->sys.dt;
+    for (long i = 0; i < m; i++) c->time = c->time + c->sys[0].dt;
     const bool do_regrid = (c->cc + m - 1) % kRegridEvery == 0;
     c->cc += m;
     k -= m;
@@ -600,7 +732,6 @@ af3d_status af3d_step(af3d_ctx *c, long k) {
     if (do_regrid) {
       s = regrid(c);
       if (s) return s;
-      c->cells_valid = false;   // the next step rebuilds the cells on the new grid
     }
   }
   int flags = 0;
@@ -619,22 +750,23 @@ af3d_status af3d_step_profile(af3d_ctx *c, long k, double *ms) {
     AF3D_CUDA(cudaEventRecord(ev[0], c->st));
     launch_advance_time(c->st, c->d);
     AF3D_CUDA(cudaEventRecord(ev[1], c->st));
-    launch_predict(c->L(), c->cur, c->d, true, true, true, c->cells, c->id_cur);
+    launch_predict(c->L(), c->cur, c->d, true, true, true, c->cells, c->id_cur, c->fl_cur);
     AF3D_CUDA(cudaEventRecord(ev[2], c->st));
     launch_sort(c->L(), c->d, c->cells, c->id_cur, c->ntags);
     AF3D_CUDA(cudaEventRecord(ev[3], c->st));
-    launch_permute_records(c->L(), c->cur, c->alt, c->cells.perm, c->id_cur, c->id_alt, c->nbr, c->cull,
-                           false);
+    launch_permute_records(c->L(), c->cur, c->alt, c->cells.perm, c->id_cur, c->id_alt, c->fl_cur, c->fl_alt,
+                           c->nbr, c->cull, false);
     std::swap(c->cur, c->alt);
     std::swap(c->id_cur, c->id_alt);
+    std::swap(c->fl_cur, c->fl_alt);
     AF3D_CUDA(cudaEventRecord(ev[4], c->st));
-    launch_fused_forces(c->L(), c->cur, c->alt, c->d, c->nbr, c->cull, c->cells.start, false);
+    launch_fused_forces(c->L(), c->cur, c->alt, c->d, c->fl_cur, c->nbr, c->cull, c->cells.start, false);
     swap_velocity_planes(c->cur, c->alt);
     swap_accel_planes(c->cur);
     swap_accel_planes(c->alt);
     AF3D_CUDA(cudaEventRecord(ev[5], c->st));
     c->launches += kKernelsPerStep;
-    c->sys.time = c->sys.time + c->sys.dt;
+    c->time = c->time + c->sys[0].dt;
     const bool do_regrid = c->cc % kRegridEvery == 0;
     c->cc++;
     if (do_regrid) {
@@ -648,9 +780,9 @@ af3d_status af3d_step_profile(af3d_ctx *c, long k, double *ms) {
       AF3D_CUDA(cudaEventElapsedTime(&t, ev[p], ev[p + 1]));
       ms[p] += t;
     }
+    c->cells_valid = !do_regrid;
   }
   for (auto &e : ev) cudaEventDestroy(e);
-  c->cells_valid = c->cc % kRegridEvery != 1;
   c->records_valid = false;
   int flags = 0;
   af3d_status s = read_status(c, &flags);
@@ -688,39 +820,12 @@ af3d_status af3d_get_status(af3d_ctx *c, int *flags) {
 
 af3d_status af3d_get_forces(af3d_ctx *c, af3d_vec3 *force, af3d_vec3 *torque) {
   CHECK_STATE(c);
-  // Reuse the export path's id scatter through a temporary AoS-free copy.
-  std::vector<double> hp(6 * (size_t)c->n);
-  std::vector<long long> ids((size_t)c->n);
-  if (c->n == 0) return AF3D_OK;
-  for (int k = 0; k < 6; k++)
-    AF3D_CUDA(cudaMemcpyAsync(hp.data() + (size_t)k * c->n, c->cur.p[FX + k], sizeof(double) * c->n,
-                              cudaMemcpyDeviceToHost, c->st));
-  AF3D_CUDA(cudaMemcpyAsync(ids.data(), c->id_cur, sizeof(long long) * c->n, cudaMemcpyDeviceToHost, c->st));
-  AF3D_CUDA(cudaStreamSynchronize(c->st));
-  for (long s = 0; s < c->n; s++) {
-    const long long i = ids[s];
-    if (force) force[i] = {hp[s], hp[c->n + s], hp[2 * c->n + s]};
-    if (torque) torque[i] = {hp[3 * c->n + s], hp[4 * c->n + s], hp[5 * c->n + s]};
-  }
-  return AF3D_OK;
+  return gather_by_id(c, FX, force, torque);
 }
 
 af3d_status af3d_get_accels(af3d_ctx *c, af3d_vec3 *acc_f, af3d_vec3 *anga_f) {
   CHECK_STATE(c);
-  std::vector<double> hp(6 * (size_t)c->n);
-  std::vector<long long> ids((size_t)c->n);
-  if (c->n == 0) return AF3D_OK;
-  for (int k = 0; k < 6; k++)
-    AF3D_CUDA(cudaMemcpyAsync(hp.data() + (size_t)k * c->n, c->cur.p[AFX + k], sizeof(double) * c->n,
-                              cudaMemcpyDeviceToHost, c->st));
-  AF3D_CUDA(cudaMemcpyAsync(ids.data(), c->id_cur, sizeof(long long) * c->n, cudaMemcpyDeviceToHost, c->st));
-  AF3D_CUDA(cudaStreamSynchronize(c->st));
-  for (long s = 0; s < c->n; s++) {
-    const long long i = ids[s];
-    if (acc_f) acc_f[i] = {hp[s], hp[c->n + s], hp[2 * c->n + s]};
-    if (anga_f) anga_f[i] = {hp[3 * c->n + s], hp[4 * c->n + s], hp[5 * c->n + s]};
-  }
-  return AF3D_OK;
+  return gather_by_id(c, AFX, acc_f, anga_f);
 }
 
 af3d_status af3d_get_cells(af3d_ctx *c, long *cell_of_id, long *sorted_ids, long *nbinned) {
@@ -731,15 +836,15 @@ af3d_status af3d_get_cells(af3d_ctx *c, long *cell_of_id, long *sorted_ids, long
     return AF3D_OK;
   }
   if (!c->d_tmp) AF3D_CUDA(cudaMalloc(&c->d_tmp, sizeof(long long) * c->n));
-  af3d_cell_par g;
-  AF3D_CUDA(cudaMemcpyAsync(&g, &c->d->grid, sizeof(g), cudaMemcpyDeviceToHost, c->st));
+  long long total = 0;
+  AF3D_CUDA(cudaMemcpyAsync(&total, &c->d->ncell_total, sizeof(total), cudaMemcpyDeviceToHost, c->st));
   AF3D_CUDA(cudaStreamSynchronize(c->st));
   int nb = 0;
-  AF3D_CUDA(cudaMemcpy(&nb, c->cells.start + g.ncell3, sizeof(int), cudaMemcpyDeviceToHost));
+  AF3D_CUDA(cudaMemcpy(&nb, c->cells.start + total, sizeof(int), cudaMemcpyDeviceToHost));
   if (nbinned) *nbinned = nb;
   if (cell_of_id) {
     // keys belong to the layout before the last permutation, whose ids are now in id_alt
-    launch_cells_by_id(c->L(), c->cells.key, c->id_alt, g.ncell3, c->d_tmp);
+    launch_cells_by_id(c->L(), c->cells.key, c->id_alt, c->d, c->d_tmp);
     AF3D_CUDA(cudaMemcpyAsync(cell_of_id, c->d_tmp, sizeof(long long) * c->n, cudaMemcpyDeviceToHost, c->st));
   }
   if (sorted_ids && nb > 0)
@@ -755,8 +860,8 @@ af3d_status af3d_contact_pairs(af3d_ctx *c, long *out, long cap, long *count, in
   long long *d_out = nullptr;
   if (cap > 0) AF3D_CUDA(cudaMalloc(&d_out, sizeof(long long) * 3 * cap));
   AF3D_CUDA(cudaMemsetAsync(c->d_count, 0, sizeof(unsigned long long), c->st));
-  launch_contact_pairs(c->L(), c->cur, c->d, c->nbr, c->cull, c->cells.start, c->id_cur, d_out, c->d_count,
-                       cap, active);
+  launch_contact_pairs(c->L(), c->cur, c->d, c->fl_cur, c->nbr, c->cull, c->cells.start, c->id_cur, d_out,
+                       c->d_count, cap, active);
   unsigned long long cnt = 0;
   AF3D_CUDA(cudaMemcpyAsync(&cnt, c->d_count, sizeof(cnt), cudaMemcpyDeviceToHost, c->st));
   AF3D_CUDA(cudaStreamSynchronize(c->st));

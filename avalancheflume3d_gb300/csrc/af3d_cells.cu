@@ -48,8 +48,8 @@ __device__ __forceinline__ int block_excl_scan(int v, int *total) {
   return r;
 }
 
-// Buckets in use: ncell3 cells plus one private bucket per clump for the clumps not binned.
-__device__ __forceinline__ long n_buckets(const DevScalars *d, long n) { return d->grid.ncell3 + n; }
+// Buckets in use: every flume's cells plus one private bucket per clump for the clumps not binned.
+__device__ __forceinline__ long n_buckets(const DevScalars *d, long n) { return d->ncell_total + n; }
 
 __global__ void k_scan_partials(const int *__restrict__ count, int *block_sums, const DevScalars *d,
                                 long n) {
@@ -114,7 +114,7 @@ __global__ void k_rank(const int *__restrict__ key, const int *__restrict__ star
                        int *count, DevScalars *d, long ntags, long n) {
   const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (s >= n) return;
-  const long ncell3 = d->grid.ncell3;
+  const long ncell3 = d->ncell_total;
   const int k = key[s];
   count[k] = 0;
   const int b = start[k], e = start[k + 1];

@@ -50,9 +50,10 @@ struct __align__(16) CullRec {
   float4 s[4];
 };
 
-// Cell-list buffers.  Keys: cell index in [0, ncell3) for binned clumps, ncell3 + id for clumps
-// that are not binned (removed), so every bucket holds its clumps in id order after the rank
-// pass and no bucket is large.
+// Cell-list buffers.  Keys: flume cell offset + cell index for binned clumps (the flumes' grids
+// are concatenated, so the sort keeps every flume contiguous), ncell_total + id for clumps that
+// are not binned (removed), so every bucket holds its clumps in id order after the rank pass and
+// no bucket is large.
 struct Cells {
   int *key;         // [N]   key of old slot
   int *rank_tmp;    // [N]   atomic arrival rank inside the bucket (nondeterministic)
@@ -61,23 +62,34 @@ struct Cells {
   int *count;       // [cap] bucket sizes (all zero between builds)
   int *start;       // [cap+1] exclusive scan of count
   int *block_sums;  // [scan_tiles(cap)] scan scratch
-  long cap;         // buckets available (ncell3 + N must fit)
+  long cap;         // buckets available (ncell_total + N must fit)
+};
+
+// One flume of the context (a plain drop-in run has one; a batched ensemble has many).  Every
+// flume has its own system_par (friction, restitution, slope, ...), Funnel and cell grid; all
+// flumes share dt and advance in lockstep.
+struct DevFlume {
+  af3d_system_par sys;        // sys.time is unused: the shared clock is DevScalars::time
+  af3d_funnel     fun;
+  af3d_cell_par   grid;
+  long long       cell_off;   // first bucket of this flume's cells
+  long long       pad;
+  unsigned long long bbox[8]; // re-grid scratch: ordered-int min/max of x, y, z, max vx, min vz
+  af3d_cell_par   pending;    // grid derived by the last re-grid, committed when it fits
 };
 
 // Per-context device scalars (one struct in global memory).
 struct DevScalars {
-  af3d_system_par sys;      // time here is the CURRENT time (after the last advance)
-  af3d_funnel     fun;
-  af3d_cell_par   grid;
+  double          time;       // current time (after the last advance)
   double          time_prev;  // time before the last advance (init_Verlet's removal test)
   int             phase;      // AF3D_PHASE_*
   int             variant;    // AF3D_FRICTION_*
   int             status;     // bitmask of 1 << AF3D_ERR_*
-  int             pad;
-  unsigned long long bbox[8];  // regrid scratch: ordered-int min/max of x, y, z, max vx, min vz
-  unsigned long long contacts; // active sphere-sphere contacts of the last fused force pass
-  long long       pending_ncell3;  // grid derived on the device that did not fit the buffers
-  af3d_cell_par   pending;
+  int             nflumes;
+  unsigned long long contacts; // active sphere-sphere contacts summed over fused force passes
+  long long       ncell_total; // sum of the flumes' ncell3: the first removed-clump bucket
+  long long       pending;     // > 0: a re-grid derived grids needing this many cell buckets
+  DevFlume       *flumes;      // [nflumes]
 };
 
 // Which force routines a boundary kernel applies, in the reference's call order.
@@ -92,36 +104,43 @@ struct Launch {
 };
 
 void launch_predict (const Launch &L, Planes cur, DevScalars *d, bool predict, bool keys, bool t_prev,
-                     Cells cells, const long long *id);
+                     Cells cells, const long long *id, const int *flume);
 // Exclusive scan of the bucket counts, scatter by arrival, then the deterministic (bucket, id)
 // rank: fills cells.start[0..nbuckets] and cells.perm, checks the ntags capacity and leaves the
-// count array zeroed.  nbuckets = grid.ncell3 + N is read on the device.
+// count array zeroed.  nbuckets = ncell_total + N is read on the device.
 void launch_sort (const Launch &L, DevScalars *d, Cells cells, const long long *id, long ntags);
 long scan_tiles (long bucket_cap);
-void launch_permute (const Launch &L, Planes src, Planes dst, const int *perm, long long *id_src,
-                     long long *id_dst);
-// `ft`: also carry the force/torque accumulators (the fused step does not need them).
+// Moves every plane (and the id and flume arrays) into the new order and builds the records.
+// `ft`: also carry the force/torque accumulators and a_f (the fused step rewrites them first).
 void launch_permute_records (const Launch &L, Planes src, Planes dst, const int *perm,
-                             long long *id_src, long long *id_dst, NbrRec *nbr, CullRec *cull, bool ft);
+                             const long long *id_src, long long *id_dst, const int *fl_src,
+                             int *fl_dst, NbrRec *nbr, CullRec *cull, bool ft);
 void launch_build_records (const Launch &L, Planes cur, NbrRec *nbr, CullRec *cull);
-void launch_fused_forces (const Launch &L, Planes cur, Planes out, DevScalars *d, const NbrRec *nbr,
-                          const CullRec *cull, const int *start, bool write_ft);
-void launch_boundary (const Launch &L, Planes cur, DevScalars *d, int routine);
-void launch_part (const Launch &L, Planes cur, DevScalars *d, const NbrRec *nbr, const CullRec *cull,
-                  const int *start, int sph_id);
-void launch_get_accel (const Launch &L, Planes cur, DevScalars *d);
-void launch_finish_verlet (const Launch &L, Planes cur, DevScalars *d);
+void launch_fused_forces (const Launch &L, Planes cur, Planes out, DevScalars *d, const int *flume,
+                          const NbrRec *nbr, const CullRec *cull, const int *start, bool write_ft);
+void launch_boundary (const Launch &L, Planes cur, DevScalars *d, const int *flume, int routine);
+void launch_part (const Launch &L, Planes cur, DevScalars *d, const int *flume, const NbrRec *nbr,
+                  const CullRec *cull, const int *start, int sph_id);
+void launch_get_accel (const Launch &L, Planes cur, DevScalars *d, const int *flume);
+void launch_finish_verlet (const Launch &L, Planes cur, DevScalars *d, const int *flume);
 void launch_clear_forces (const Launch &L, Planes cur);
 void launch_advance_time (cudaStream_t st, DevScalars *d);
-void launch_regrid (const Launch &L, Planes cur, DevScalars *d, long bucket_cap);
+// Per-flume cell_dim + grid derivation; commits the grids (and bucket offsets) when they fit
+// bucket_cap, else leaves them pending (DevScalars::pending = buckets needed).
+void launch_regrid (const Launch &L, Planes cur, DevScalars *d, const int *flume, int nflumes,
+                    long bucket_cap);
+// Re-commit pending grids after the host grew the bucket buffers.
+void launch_commit_grids (cudaStream_t st, DevScalars *d, int nflumes, long n, long bucket_cap);
 void launch_aos_to_planes (const Launch &L, const af3d_particle *aos, const double *acc,
-                           const double *anga, Planes cur, long long *id);
-void launch_planes_to_aos (const Launch &L, Planes cur, const long long *id, af3d_particle *aos,
-                           double *acc, double *anga, DevScalars *d);
-void launch_contact_pairs (const Launch &L, Planes cur, DevScalars *d, const NbrRec *nbr,
-                           const CullRec *cull, const int *start, const long long *id,
-                           long long *out, unsigned long long *count, long cap, int active);
-void launch_cells_by_id (const Launch &L, const int *key, const long long *id, long ncell3,
+                           const double *anga, const int *flume_of_id, Planes cur, long long *id,
+                           int *flume);
+void launch_planes_to_aos (const Launch &L, Planes cur, const long long *id, const int *flume,
+                           af3d_particle *aos, double *acc, double *anga, DevScalars *d);
+void launch_contact_pairs (const Launch &L, Planes cur, DevScalars *d, const int *flume,
+                           const NbrRec *nbr, const CullRec *cull, const int *start,
+                           const long long *id, long long *out, unsigned long long *count, long cap,
+                           int active);
+void launch_cells_by_id (const Launch &L, const int *key, const long long *id, DevScalars *d,
                          long long *cell_of_id);
 // DFMA throughput microbenchmark (TFLOP/s, 2 flops per DFMA), bounded to ~0.1 s.
 cudaError_t measure_dfma (int sms, double *tflops);

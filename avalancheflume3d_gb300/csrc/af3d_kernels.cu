@@ -42,7 +42,8 @@ __device__ __forceinline__ void raise_status(DevScalars *d, int err) {
 // ------------------------------------------------------------------ import / export
 
 __global__ void k_aos_to_planes(const af3d_particle *__restrict__ aos, const double *__restrict__ acc,
-                                const double *__restrict__ anga, Planes P, long long *id, long n) {
+                                const double *__restrict__ anga, const int *__restrict__ flume_of_id,
+                                Planes P, long long *id, int *flume, long n) {
   long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (s >= n) return;
   const af3d_particle &q = aos[s];
@@ -70,13 +71,16 @@ __global__ void k_aos_to_planes(const af3d_particle *__restrict__ aos, const dou
   P.p[MWALL][s] = kSPH_FACT * r * r * r * rho;  // force_walls.cu:47
   P.p[ADRAG][s] = drag_factor(r, q.mass);       // get_accel.cu:47
   id[s] = s;
+  flume[s] = flume_of_id[s];
 }
 
-__global__ void k_planes_to_aos(Planes P, const long long *__restrict__ id, af3d_particle *aos,
-                                double *acc, double *anga, const DevScalars *d, long n) {
+__global__ void k_planes_to_aos(Planes P, const long long *__restrict__ id, const int *__restrict__ flume,
+                                af3d_particle *aos, double *acc, double *anga, const DevScalars *d,
+                                long n) {
   long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (s >= n) return;
-  const double cost = d->sys.cost, sint = d->sys.sint;
+  const af3d_system_par &sy = d->flumes[flume[s]].sys;
+  const double cost = sy.cost, sint = sy.sint;
   af3d_particle &q = aos[id[s]];
   q.radius = P.p[RAD][s];
   q.mass = P.p[MASS][s];
@@ -121,19 +125,20 @@ __device__ __forceinline__ long bin_axis(double x, double xmin, double inv, long
 
 // init_Verlet.cu:25-148 for one clump (PREDICT), and/or cell_locate's binning (cells.cu:60-92)
 // with the current time (KEYS): the bucket key, the bucket count and the clump's arrival rank.
-// Clumps that are not binned (removed, or non-finite) get the unique bucket ncell3 + id, so every
+// Clumps that are not binned (removed, or non-finite) get the unique bucket ncell_total + id, so every
 // bucket holds its clumps in id order after the rank pass.  `t_prev`: init_Verlet's removal test
 // uses the time before the advance (the fused step advances time first).
 template <bool PREDICT, bool KEYS>
 __global__ void k_predict(Planes P, DevScalars *d, bool t_prev, Cells cells,
-                          const long long *__restrict__ id, long n) {
+                          const long long *__restrict__ id, const int *__restrict__ flume, long n) {
   long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (s >= n) return;
-  const double side_x = d->sys.side.x;
+  const DevFlume &fl = d->flumes[flume[s]];
+  const double side_x = fl.sys.side.x;
   V3 r = load3(P, RX, s);
   if (PREDICT) {
-    const double dt = d->sys.dt, hdt = d->sys.hdt;
-    const double t_init = t_prev ? d->time_prev : d->sys.time;
+    const double dt = fl.sys.dt, hdt = fl.sys.hdt;
+    const double t_init = t_prev ? d->time_prev : d->time;
     if (is_removed(t_init, r.x, side_x)) {
       P.p[RAD][s] = 0.0;
     } else {
@@ -195,14 +200,13 @@ __global__ void k_predict(Planes P, DevScalars *d, bool t_prev, Cells cells,
     }
   }
   if (!KEYS) return;
-  const af3d_cell_par &g = d->grid;
-  const long ncell3 = g.ncell3;
+  const af3d_cell_par &g = fl.grid;
   long key;
-  if (is_removed(d->sys.time, r.x, side_x)) {
-    key = ncell3 + id[s];
+  if (is_removed(d->time, r.x, side_x)) {
+    key = d->ncell_total + id[s];
   } else if (!(isfinite(r.x) && isfinite(r.y) && isfinite(r.z))) {
     raise_status(d, AF3D_ERR_NAN);
-    key = ncell3 + id[s];
+    key = d->ncell_total + id[s];
   } else {
     long i = bin_axis(r.x, g.rr_min.x, g.cs_inv.x, g.ncell.x);
     long j = bin_axis(r.y, g.rr_min.y, g.cs_inv.y, g.ncell.y);
@@ -217,7 +221,7 @@ __global__ void k_predict(Planes P, DevScalars *d, bool t_prev, Cells cells,
       j = j < g.ncell.y ? j : g.ncell.y - 1;
       k = k < g.ncell.z ? k : g.ncell.z - 1;
     }
-    key = i + g.ncell.x * (j + k * g.ncell.y);
+    key = fl.cell_off + i + g.ncell.x * (j + k * g.ncell.y);
   }
   cells.key[s] = (int)key;
   cells.rank_tmp[s] = atomicAdd(&cells.count[key], 1);
@@ -260,7 +264,8 @@ constexpr int kRecStride = kRecWords + 1;
 // assembled in shared memory and written out as contiguous 16-byte stores.
 __global__ void __launch_bounds__(kPermBlock) k_permute(Planes src, Planes dst, const int *__restrict__ perm,
                                                         const long long *__restrict__ id_src,
-                                                        long long *id_dst, NbrRec *nbr, CullRec *cull,
+                                                        long long *id_dst, const int *__restrict__ fl_src,
+                                                        int *fl_dst, NbrRec *nbr, CullRec *cull,
                                                         bool ft, long n) {
   __shared__ double s_nbr[kPermBlock * kRecStride];
   __shared__ CullRec s_cull[kPermBlock];
@@ -273,6 +278,7 @@ __global__ void __launch_bounds__(kPermBlock) k_permute(Planes src, Planes dst, 
       for (int p = 0; p < NPLANES; p++)
         if (ft || ((p < FX || p > TZ) && (p < AFX || p > ALFZ))) dst.p[p][s] = src.p[p][o];
       id_dst[s] = id_src[o];
+      fl_dst[s] = fl_src[o];
     }
     if (nbr) {
       V3 sp[4];
@@ -328,6 +334,7 @@ __device__ __forceinline__ unsigned pair_mask(const CullRec &me, const CullRec &
 
 struct Search {
   long ci, cj, ck;
+  long long off;   // the flume's first cell bucket
 };
 
 // Search-centre cell of force_part.cu:77-85: (long)((x - xmin)/side).  The quotient is first
@@ -348,8 +355,9 @@ __device__ __forceinline__ long search_axis(double x, double xmin, double side, 
   return i;
 }
 
-__device__ __forceinline__ Search search_centre(V3 r, const af3d_cell_par &g) {
+__device__ __forceinline__ Search search_centre(V3 r, const af3d_cell_par &g, long long off) {
   Search q;
+  q.off = off;
   q.ci = search_axis(r.x, g.rr_min.x, g.cell_side.x, g.cs_inv.x, g.ncell.x);
   q.cj = search_axis(r.y, g.rr_min.y, g.cell_side.y, g.cs_inv.y, g.ncell.y);
   q.ck = search_axis(r.z, g.rr_min.z, g.cell_side.z, g.cs_inv.z, g.ncell.z);
@@ -370,7 +378,7 @@ __device__ __forceinline__ void for_neighbour_slots(const Search &q, const af3d_
         const long in = q.ci + di, jn = q.cj + dj, kn = q.ck + dk;
         if (in < 0 || jn < 0 || kn < 0 || in >= g.ncell.x || jn >= g.ncell.y || kn >= g.ncell.z)
           continue;
-        const long c = in + g.ncell.x * (jn + g.ncell.y * kn);
+        const long c = q.off + in + g.ncell.x * (jn + g.ncell.y * kn);
         const int t0 = __ldg(&start[c]), t1 = __ldg(&start[c + 1]);
 #pragma unroll 1
         for (int t = t0; t < t1; t++) f(t);
@@ -390,7 +398,7 @@ __device__ __forceinline__ void for_neighbour_slots_pre(const Search &q, const a
   for (int r = 0; r < 9; r++) {
     const long jn = q.cj + (r / 3 - 1), kn = q.ck + (r % 3 - 1);
     const bool row_ok = jn >= 0 && kn >= 0 && jn < g.ncell.y && kn < g.ncell.z;
-    const long rb = g.ncell.x * (jn + g.ncell.y * kn);
+    const long rb = q.off + g.ncell.x * (jn + g.ncell.y * kn);
 #pragma unroll
     for (int e = 0; e < 4; e++) {
       // boundary e of the row: start of cell x0 + e, clamped into the row (empty cells outside)
@@ -417,11 +425,11 @@ __device__ __forceinline__ void for_neighbour_slots_pre(const Search &q, const a
 constexpr int kItemCap = 96;
 
 __device__ __forceinline__ bool gather_items(long s, const Own &o, const af3d_cell_par &g,
-                                             const CullRec *__restrict__ cull,
+                                             long long off, const CullRec *__restrict__ cull,
                                              const int *__restrict__ start, unsigned want,
                                              unsigned *items, int cap, int &nitems) {
   const CullRec me = cull[s];
-  const Search q = search_centre(o.r, g);
+  const Search q = search_centre(o.r, g, off);
   int cand_t[kCandCap];
   unsigned short cand_m[kCandCap];
   int ncand = 0;
@@ -456,13 +464,14 @@ __device__ __forceinline__ bool gather_items(long s, const Own &o, const af3d_ce
 // Every pair of clump s walked cell by cell once per sph_id (the order of sixteen force_part
 // launches); used when a clump has more partners than the item lists hold.
 __device__ __forceinline__ int contacts_by_pass(long s, const Own &o, const Consts &c,
-                                                const af3d_cell_par &g, const NbrRec *__restrict__ nbr,
+                                                const af3d_cell_par &g, long long off,
+                                                const NbrRec *__restrict__ nbr,
                                                 const CullRec *__restrict__ cull,
                                                 const int *__restrict__ start, unsigned want, V3 &F,
                                                 V3 &T) {
   const bool xi0 = c.variant == AF3D_FRICTION_DEV;
   const CullRec me = cull[s];
-  const Search q = search_centre(o.r, g);
+  const Search q = search_centre(o.r, g, off);
   int active = 0;
 #pragma unroll 1
   for (int p = 0; p < 16; p++) {
@@ -479,7 +488,8 @@ __device__ __forceinline__ int contacts_by_pass(long s, const Own &o, const Cons
 
 // Per-clump contact pass (one thread, its own item list): the per-routine force_part entry.
 __device__ __forceinline__ int particle_contacts(long s, const Own &o, const Consts &c,
-                                                 const af3d_cell_par &g, const NbrRec *__restrict__ nbr,
+                                                 const af3d_cell_par &g, long long off,
+                                                 const NbrRec *__restrict__ nbr,
                                                  const CullRec *__restrict__ cull,
                                                  const int *__restrict__ start, int only_p, V3 &F,
                                                  V3 &T) {
@@ -487,8 +497,8 @@ __device__ __forceinline__ int particle_contacts(long s, const Own &o, const Con
   const unsigned want = only_p < 0 ? 0xffffu : (1u << only_p);
   unsigned items[kItemCap];
   int nitems = 0;
-  if (!gather_items(s, o, g, cull, start, want, items, kItemCap, nitems))
-    return contacts_by_pass(s, o, c, g, nbr, cull, start, want, F, T);
+  if (!gather_items(s, o, g, off, cull, start, want, items, kItemCap, nitems))
+    return contacts_by_pass(s, o, c, g, off, nbr, cull, start, want, F, T);
   int active = 0;
 #pragma unroll 1
   for (int i = 0; i < nitems; i++) {
@@ -515,15 +525,16 @@ struct WarpQueue {
 };
 
 __device__ __forceinline__ int warp_contacts(WarpQueue &wq, long wbase, long s, bool act, const Own &o,
-                                             const Consts &c, const af3d_cell_par &g,
+                                             const Consts &c, const af3d_cell_par &g, long long off,
+                                             const DevScalars *d, const int *__restrict__ flume,
                                              const NbrRec *__restrict__ nbr,
                                              const CullRec *__restrict__ cull,
                                              const int *__restrict__ start, V3 &F, V3 &T) {
   const int lane = threadIdx.x & 31;
-  const bool xi0 = c.variant == AF3D_FRICTION_DEV;
+  const int my_flume = flume[s];
   int nitems = 0;
   bool slow = false;
-  if (act) slow = !gather_items(s, o, g, cull, start, 0xffffu, wq.items[lane], kLaneItems, nitems);
+  if (act) slow = !gather_items(s, o, g, off, cull, start, 0xffffu, wq.items[lane], kLaneItems, nitems);
   if (slow) nitems = 0;
   int incl = nitems;
 #pragma unroll
@@ -551,8 +562,12 @@ __device__ __forceinline__ int warp_contacts(WarpQueue &wq, long wbase, long s, 
       const V3 rl = mk(me.rx, me.ry, me.rz), vl = mk(me.vx, me.vy, me.vz), wl = mk(me.wx, me.wy, me.wz);
       const int k = p & 3;
       const V3 s1 = mk(me.s[3 * k], me.s[3 * k + 1], me.s[3 * k + 2]);
+      // the owner's flume may differ from this lane's at a flume boundary of an ensemble
+      const int of = flume[wbase + lo];
+      const Consts co = of == my_flume ? c : load_consts(d, of);
       V3 fs, tq;
-      const int r = part_pair_contrib(rl, vl, wl, s1, me.rad, me.msph, nbr[t], p >> 2, c, xi0, fs, tq);
+      const int r = part_pair_contrib(rl, vl, wl, s1, me.rad, me.msph, nbr[t], p >> 2, co,
+                                      co.variant == AF3D_FRICTION_DEV, fs, tq);
       wq.flag[lane] = r;
       if (r == 2) {
         wq.res[lane][0] = fs.x; wq.res[lane][1] = fs.y; wq.res[lane][2] = fs.z;
@@ -572,7 +587,7 @@ __device__ __forceinline__ int warp_contacts(WarpQueue &wq, long wbase, long s, 
     }
     __syncwarp();
   }
-  if (slow) active += contacts_by_pass(s, o, c, g, nbr, cull, start, 0xffffu, F, T);
+  if (slow) active += contacts_by_pass(s, o, c, g, off, nbr, cull, start, 0xffffu, F, T);
   return active;
 }
 
@@ -615,6 +630,7 @@ __device__ __forceinline__ void warp_count(DevScalars *d, int active) {
 #endif
 template <bool WRITE_FT>
 __global__ void __launch_bounds__(kBlock, AF3D_FORCES_MINB) k_fused_forces(Planes P, Planes out, DevScalars *d,
+                                                         const int *__restrict__ flume,
                                                          const NbrRec *__restrict__ nbr,
                                                          const CullRec *__restrict__ cull,
                                                          const int *__restrict__ start, long n) {
@@ -624,8 +640,10 @@ __global__ void __launch_bounds__(kBlock, AF3D_FORCES_MINB) k_fused_forces(Plane
   const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
   const bool valid = s < n;
   const long sv = valid ? s : n - 1;   // in-range slot for lanes past n (nothing is written for them)
-  const Consts c = load_consts(d);
-  const af3d_cell_par g = d->grid;
+  const int f = flume[sv];
+  const Consts c = load_consts(d, f);
+  const af3d_cell_par g = d->flumes[f].grid;
+  const long long off = d->flumes[f].cell_off;
   const Own o = own_from_record(nbr[sv], P.p[MWALL][sv]);
   const bool removed = is_removed(c.time, o.r.x, c.side_x);
   const double B = (double)cull[sv].c.w;   // sphere offsets + radius, rounded up
@@ -639,10 +657,10 @@ __global__ void __launch_bounds__(kBlock, AF3D_FORCES_MINB) k_fused_forces(Plane
   // part x16 (avalanche_hst.cu:699-701, fill :455-457)
 #if AF3D_COOP
   const long wbase = blockIdx.x * (long)blockDim.x + (threadIdx.x & ~31u);
-  const int active = warp_contacts(wq[threadIdx.x >> 5], wbase, sv, valid && !removed, o, c, g, nbr, cull,
-                                   start, F, T);
+  const int active = warp_contacts(wq[threadIdx.x >> 5], wbase, sv, valid && !removed, o, c, g, off, d,
+                                   flume, nbr, cull, start, F, T);
 #else
-  const int active = (valid && !removed) ? particle_contacts(s, o, c, g, nbr, cull, start, -1, F, T) : 0;
+  const int active = (valid && !removed) ? particle_contacts(s, o, c, g, off, nbr, cull, start, -1, F, T) : 0;
 #endif
   if (valid) {
     if (aval) {
@@ -681,10 +699,10 @@ __global__ void __launch_bounds__(kBlock, AF3D_FORCES_MINB) k_fused_forces(Plane
 }
 
 // One boundary routine added to the F, T planes (per-routine entry points).
-__global__ void k_boundary(Planes P, DevScalars *d, int routine, long n) {
+__global__ void k_boundary(Planes P, DevScalars *d, const int *__restrict__ flume, int routine, long n) {
   const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (s >= n) return;
-  const Consts c = load_consts(d);
+  const Consts c = load_consts(d, flume[s]);
   const Own o = own_from_planes(P, s);
   const bool removed = is_removed(c.time, o.r.x, c.side_x);
   V3 F = load3(P, FX, s), T = load3(P, TX, s);
@@ -694,25 +712,27 @@ __global__ void k_boundary(Planes P, DevScalars *d, int routine, long n) {
 }
 
 // force_part for one sph_id (1..16) or all sixteen (0), added to the F, T planes.
-__global__ void __launch_bounds__(kBlock) k_part(Planes P, DevScalars *d, const NbrRec *__restrict__ nbr,
+__global__ void __launch_bounds__(kBlock) k_part(Planes P, DevScalars *d, const int *__restrict__ flume,
+                                                 const NbrRec *__restrict__ nbr,
                                                  const CullRec *__restrict__ cull,
                                                  const int *__restrict__ start, int sph_id, long n) {
   const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (s >= n) return;
-  const Consts c = load_consts(d);
-  const af3d_cell_par g = d->grid;
+  const int f = flume[s];
+  const Consts c = load_consts(d, f);
+  const af3d_cell_par g = d->flumes[f].grid;
   const Own o = own_from_planes(P, s);
   if (is_removed(c.time, o.r.x, c.side_x)) return;
   V3 F = load3(P, FX, s), T = load3(P, TX, s);
-  particle_contacts(s, o, c, g, nbr, cull, start, sph_id - 1, F, T);
+  particle_contacts(s, o, c, g, d->flumes[f].cell_off, nbr, cull, start, sph_id - 1, F, T);
   store3(P, FX, s, F);
   store3(P, TX, s, T);
 }
 
-__global__ void k_get_accel(Planes P, DevScalars *d, long n) {
+__global__ void k_get_accel(Planes P, DevScalars *d, const int *__restrict__ flume, long n) {
   const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (s >= n) return;
-  if (is_removed(d->sys.time, P.p[RX][s], d->sys.side.x)) return;
+  if (is_removed(d->time, P.p[RX][s], d->flumes[flume[s]].sys.side.x)) return;
   V3 a, al;
   get_accel_one(load3(P, FX, s), load3(P, TX, s), load3(P, VX, s), load3(P, WX, s), load3(P, R00, s),
                 load3(P, R10, s), load3(P, R20, s), P.p[MASS][s], P.p[ADRAG][s], load3(P, IXX, s), a, al);
@@ -720,11 +740,12 @@ __global__ void k_get_accel(Planes P, DevScalars *d, long n) {
   store3(P, ALFX, s, al);
 }
 
-__global__ void k_finish_verlet(Planes P, DevScalars *d, long n) {
+__global__ void k_finish_verlet(Planes P, DevScalars *d, const int *__restrict__ flume, long n) {
   const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (s >= n) return;
-  const double hdt = d->sys.hdt;
-  if (is_removed(d->sys.time, P.p[RX][s], d->sys.side.x)) {
+  const af3d_system_par &sy = d->flumes[flume[s]].sys;
+  const double hdt = sy.hdt;
+  if (is_removed(d->time, P.p[RX][s], sy.side.x)) {
     store3(P, VX, s, mk(0.0, 0.0, 0.0));
     return;
   }
@@ -747,10 +768,11 @@ __global__ void k_clear_forces(Planes P, long n) {
   store3(P, TX, s, mk(0.0, 0.0, 0.0));
 }
 
-// sys_par.time += dt (avalanche_hst.cu:672), keeping the previous value for init_Verlet.
+// sys_par.time += dt (avalanche_hst.cu:672), keeping the previous value for init_Verlet.  The
+// flumes of an ensemble share dt and the clock.
 __global__ void k_advance_time(DevScalars *d) {
-  d->time_prev = d->sys.time;
-  d->sys.time = d->sys.time + d->sys.dt;
+  d->time_prev = d->time;
+  d->time = d->time + d->flumes[0].sys.dt;
 }
 
 // ------------------------------------------------------------------ re-grid (cell_dim)
@@ -764,61 +786,83 @@ __device__ __forceinline__ double unord(unsigned long long k) {
   return __longlong_as_double((long long)u);
 }
 
-__global__ void k_bbox_init(DevScalars *d) {
+__global__ void k_bbox_init(DevScalars *d, int nflumes) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nflumes) return;
+  unsigned long long *b = d->flumes[f].bbox;
   for (int i = 0; i < 3; i++) {
-    d->bbox[i] = ~0ull;    // min x, y, z
-    d->bbox[3 + i] = 0ull; // max x, y, z
+    b[i] = ~0ull;    // min x, y, z
+    b[3 + i] = 0ull; // max x, y, z
   }
-  d->bbox[6] = 0ull;       // max vx
-  d->bbox[7] = ~0ull;      // min vz
+  b[6] = 0ull;       // max vx
+  b[7] = ~0ull;      // min vz
 }
 
-// Min/max of clump centres, max vx and min vz over every clump (cell_dim.cu:21-54).
-__global__ void k_bbox_reduce(Planes P, DevScalars *d, long n) {
+// Min/max of clump centres, max vx and min vz over every clump of each flume (cell_dim.cu:21-54),
+// warp-reduced when a warp's clumps belong to one flume.
+__global__ void k_bbox_reduce(Planes P, DevScalars *d, const int *__restrict__ flume, long n) {
   const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const long sv = s < n ? s : n - 1;
+  const int f = flume[sv];
   unsigned long long mn[3], mx[3], vx, vz;
-  if (s < n) {
-    for (int i = 0; i < 3; i++) mn[i] = mx[i] = ord(P.p[RX + i][s]);
-    vx = ord(P.p[VX][s]);
-    vz = ord(P.p[VZ][s]);
-  } else {
-    for (int i = 0; i < 3; i++) { mn[i] = ~0ull; mx[i] = 0ull; }
-    vx = 0ull;
-    vz = ~0ull;
-  }
-  for (int off = 16; off; off >>= 1) {
-    for (int i = 0; i < 3; i++) {
-      mn[i] = min(mn[i], __shfl_xor_sync(0xffffffffu, mn[i], off));
-      mx[i] = max(mx[i], __shfl_xor_sync(0xffffffffu, mx[i], off));
+  for (int i = 0; i < 3; i++) mn[i] = mx[i] = ord(P.p[RX + i][sv]);
+  vx = ord(P.p[VX][sv]);
+  vz = ord(P.p[VZ][sv]);
+  const int f0 = __shfl_sync(0xffffffffu, f, 0);
+  const bool uniform = __all_sync(0xffffffffu, f == f0);
+  if (uniform) {
+    for (int off = 16; off; off >>= 1) {
+      for (int i = 0; i < 3; i++) {
+        mn[i] = min(mn[i], __shfl_xor_sync(0xffffffffu, mn[i], off));
+        mx[i] = max(mx[i], __shfl_xor_sync(0xffffffffu, mx[i], off));
+      }
+      vx = max(vx, __shfl_xor_sync(0xffffffffu, vx, off));
+      vz = min(vz, __shfl_xor_sync(0xffffffffu, vz, off));
     }
-    vx = max(vx, __shfl_xor_sync(0xffffffffu, vx, off));
-    vz = min(vz, __shfl_xor_sync(0xffffffffu, vz, off));
   }
-  if ((threadIdx.x & 31) == 0) {
+  if (!uniform || (threadIdx.x & 31) == 0) {
+    unsigned long long *b = d->flumes[f].bbox;
     for (int i = 0; i < 3; i++) {
-      atomicMin(&d->bbox[i], mn[i]);
-      atomicMax(&d->bbox[3 + i], mx[i]);
+      atomicMin(&b[i], mn[i]);
+      atomicMax(&b[3 + i], mx[i]);
     }
-    atomicMax(&d->bbox[6], vx);
-    atomicMin(&d->bbox[7], vz);
+    atomicMax(&b[6], vx);
+    atomicMin(&b[7], vz);
   }
 }
 
-// cell_dim.cu:56-66 padding and the grid derivation of avalanche_hst.cu:314-333.  A grid whose
-// bucket count does not fit the cell buffers is parked in `pending` for the host to grow them.
-__global__ void k_grid_derive(DevScalars *d, long n, long bucket_cap) {
-  const af3d_system_par &sy = d->sys;
+// cell_dim.cu:56-66 padding and the grid derivation of avalanche_hst.cu:314-333, per flume, into
+// the flume's pending grid.
+__global__ void k_grid_derive(DevScalars *d, int nflumes) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nflumes) return;
+  DevFlume &fl = d->flumes[f];
+  if (fl.bbox[0] == ~0ull) {
+    // A flume without clumps keeps its grid (a one-cell grid if it never had one): nothing is
+    // binned there, and cell_dim would read a clump that does not exist.
+    af3d_cell_par g = fl.grid;
+    if (g.ncell3 <= 0) {
+      g.rr_min = {0.0, 0.0, 0.0};
+      g.rr_max = g.length = g.cell_side = g.cs_inv = {1.0, 1.0, 1.0};
+      g.ncell = {1, 1, 1};
+      g.ncell3 = 1;
+      g.ntot = g.ntags;
+    }
+    fl.pending = g;
+    return;
+  }
+  const af3d_system_par &sy = fl.sys;
   const double rgyr = 0.5 * sy.gyr_max, ddt = 2000.0 * sy.dt;
-  const double vxmax = unord(d->bbox[6]), vzmin = unord(d->bbox[7]);
-  V3 hi = mk(unord(d->bbox[3]), unord(d->bbox[4]), unord(d->bbox[5]));
-  V3 lo = mk(unord(d->bbox[0]), unord(d->bbox[1]), unord(d->bbox[2]));
+  const double vxmax = unord(fl.bbox[6]), vzmin = unord(fl.bbox[7]);
+  V3 hi = mk(unord(fl.bbox[3]), unord(fl.bbox[4]), unord(fl.bbox[5]));
+  V3 lo = mk(unord(fl.bbox[0]), unord(fl.bbox[1]), unord(fl.bbox[2]));
   hi.x += 1.05 * rgyr + vxmax * ddt;
   lo.x -= 1.05 * rgyr;
   hi.y += 1.05 * rgyr;
   lo.y -= 1.05 * rgyr;
   hi.z += 1.05 * rgyr;
   lo.z -= 1.05 * rgyr - vzmin * ddt;
-  af3d_cell_par g = d->grid;
+  af3d_cell_par g = fl.grid;
   const double dist = kGYR + (double)0.05f;   // avalanche_hst.cu:115 adds a float literal
   g.rr_max = {hi.x, hi.y, hi.z};
   g.rr_min = {lo.x, lo.y, lo.z};
@@ -834,29 +878,53 @@ __global__ void k_grid_derive(DevScalars *d, long n, long bucket_cap) {
   g.cs_inv.z = 1.0 / g.cell_side.z;
   g.ncell3 = g.ncell.x * g.ncell.y * g.ncell.z;
   g.ntot = g.ncell3 * g.ntags;
-  if (g.ncell3 + n + 1 <= bucket_cap && g.ncell3 > 0) {
-    d->grid = g;
-    d->pending_ncell3 = 0;
-  } else {
-    d->pending = g;
-    d->pending_ncell3 = g.ncell3 > 0 ? g.ncell3 : -1;
+  fl.pending = g;
+}
+
+// Commit the pending grids with their bucket offsets when every grid is non-empty and the
+// buckets fit; otherwise record the buckets needed (-1: an empty grid) and keep the old grids.
+__global__ void k_grid_commit(DevScalars *d, int nflumes, long n, long bucket_cap) {
+  long long total = 0;
+  bool ok = true;
+  for (int f = 0; f < nflumes; f++) {
+    const long long c = d->flumes[f].pending.ncell3;
+    ok = ok && c > 0;
+    total += c > 0 ? c : 0;
   }
+  if (!ok) {
+    d->pending = -1;
+    return;
+  }
+  if (total + n + 1 > bucket_cap) {
+    d->pending = total;
+    return;
+  }
+  long long off = 0;
+  for (int f = 0; f < nflumes; f++) {
+    d->flumes[f].grid = d->flumes[f].pending;
+    d->flumes[f].cell_off = off;
+    off += d->flumes[f].grid.ncell3;
+  }
+  d->ncell_total = total;
+  d->pending = 0;
 }
 
 // ------------------------------------------------------------------ diagnostics
 
-__global__ void k_contact_pairs(Planes P, DevScalars *d, const NbrRec *__restrict__ nbr,
-                                const CullRec *__restrict__ cull, const int *__restrict__ start,
-                                const long long *__restrict__ id, long long *out,
-                                unsigned long long *count, long cap, int active_only, long n) {
+__global__ void k_contact_pairs(Planes P, DevScalars *d, const int *__restrict__ flume,
+                                const NbrRec *__restrict__ nbr, const CullRec *__restrict__ cull,
+                                const int *__restrict__ start, const long long *__restrict__ id,
+                                long long *out, unsigned long long *count, long cap, int active_only,
+                                long n) {
   const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (s >= n) return;
-  const Consts c = load_consts(d);
-  const af3d_cell_par g = d->grid;
+  const int f = flume[s];
+  const Consts c = load_consts(d, f);
+  const af3d_cell_par g = d->flumes[f].grid;
   const Own o = own_from_planes(P, s);
   if (is_removed(c.time, o.r.x, c.side_x)) return;
   const CullRec me = cull[s];
-  const Search q = search_centre(o.r, g);
+  const Search q = search_centre(o.r, g, d->flumes[f].cell_off);
   for_neighbour_slots(q, g, start, [&](int t) {
     if (t == s) return;
     unsigned m = pair_mask(me, cull[t]);
@@ -877,12 +945,13 @@ __global__ void k_contact_pairs(Planes P, DevScalars *d, const NbrRec *__restric
   });
 }
 
-__global__ void k_cells_by_id(const int *__restrict__ key, const long long *__restrict__ id, long ncell3,
-                              long long *cell_of_id, long n) {
+// Bucket of every clump by id (-1 when not binned): the flume's cell offset plus the cell index.
+__global__ void k_cells_by_id(const int *__restrict__ key, const long long *__restrict__ id,
+                              const DevScalars *d, long long *cell_of_id, long n) {
   const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (s >= n) return;
   const int k = key[s];
-  cell_of_id[id[s]] = k < ncell3 ? k : -1;
+  cell_of_id[id[s]] = k < d->ncell_total ? k : -1;
 }
 
 }  // namespace
@@ -890,65 +959,59 @@ __global__ void k_cells_by_id(const int *__restrict__ key, const long long *__re
 // ------------------------------------------------------------------ launchers
 
 void launch_predict(const Launch &L, Planes cur, DevScalars *d, bool predict, bool keys, bool t_prev,
-                    Cells cells, const long long *id) {
+                    Cells cells, const long long *id, const int *flume) {
   if (L.n <= 0) return;
   const unsigned g = grid_for(L.n);
   if (predict && keys)
-    k_predict<true, true><<<g, kBlock, 0, L.st>>>(cur, d, t_prev, cells, id, L.n);
+    k_predict<true, true><<<g, kBlock, 0, L.st>>>(cur, d, t_prev, cells, id, flume, L.n);
   else if (predict)
-    k_predict<true, false><<<g, kBlock, 0, L.st>>>(cur, d, t_prev, cells, id, L.n);
+    k_predict<true, false><<<g, kBlock, 0, L.st>>>(cur, d, t_prev, cells, id, flume, L.n);
   else if (keys)
-    k_predict<false, true><<<g, kBlock, 0, L.st>>>(cur, d, t_prev, cells, id, L.n);
-}
-
-void launch_permute(const Launch &L, Planes src, Planes dst, const int *perm, long long *id_src,
-                    long long *id_dst) {
-  if (L.n <= 0) return;
-  k_permute<<<grid_for(L.n, kPermBlock), kPermBlock, 0, L.st>>>(src, dst, perm, id_src, id_dst, nullptr,
-                                                                nullptr, true, L.n);
+    k_predict<false, true><<<g, kBlock, 0, L.st>>>(cur, d, t_prev, cells, id, flume, L.n);
 }
 
 void launch_permute_records(const Launch &L, Planes src, Planes dst, const int *perm,
-                            long long *id_src, long long *id_dst, NbrRec *nbr, CullRec *cull, bool ft) {
+                            const long long *id_src, long long *id_dst, const int *fl_src, int *fl_dst,
+                            NbrRec *nbr, CullRec *cull, bool ft) {
   if (L.n <= 0) return;
-  k_permute<<<grid_for(L.n, kPermBlock), kPermBlock, 0, L.st>>>(src, dst, perm, id_src, id_dst, nbr, cull,
-                                                                ft, L.n);
+  k_permute<<<grid_for(L.n, kPermBlock), kPermBlock, 0, L.st>>>(src, dst, perm, id_src, id_dst, fl_src,
+                                                                fl_dst, nbr, cull, ft, L.n);
 }
 
 void launch_build_records(const Launch &L, Planes cur, NbrRec *nbr, CullRec *cull) {
   if (L.n <= 0) return;
-  k_permute<<<grid_for(L.n, kPermBlock), kPermBlock, 0, L.st>>>(cur, cur, nullptr, nullptr, nullptr, nbr,
-                                                                cull, true, L.n);
+  k_permute<<<grid_for(L.n, kPermBlock), kPermBlock, 0, L.st>>>(cur, cur, nullptr, nullptr, nullptr,
+                                                                nullptr, nullptr, nbr, cull, true, L.n);
 }
 
-void launch_fused_forces(const Launch &L, Planes cur, Planes out, DevScalars *d, const NbrRec *nbr,
-                         const CullRec *cull, const int *start, bool write_ft) {
+void launch_fused_forces(const Launch &L, Planes cur, Planes out, DevScalars *d, const int *flume,
+                         const NbrRec *nbr, const CullRec *cull, const int *start, bool write_ft) {
   if (L.n <= 0) return;
   if (write_ft)
-    k_fused_forces<true><<<grid_for(L.n), kBlock, 0, L.st>>>(cur, out, d, nbr, cull, start, L.n);
+    k_fused_forces<true><<<grid_for(L.n), kBlock, 0, L.st>>>(cur, out, d, flume, nbr, cull, start, L.n);
   else
-    k_fused_forces<false><<<grid_for(L.n), kBlock, 0, L.st>>>(cur, out, d, nbr, cull, start, L.n);
+    k_fused_forces<false><<<grid_for(L.n), kBlock, 0, L.st>>>(cur, out, d, flume, nbr, cull, start, L.n);
 }
 
-void launch_boundary(const Launch &L, Planes cur, DevScalars *d, int routine) {
+void launch_boundary(const Launch &L, Planes cur, DevScalars *d, const int *flume, int routine) {
   if (L.n <= 0) return;
-  k_boundary<<<grid_for(L.n), kBlock, 0, L.st>>>(cur, d, routine, L.n);
+  k_boundary<<<grid_for(L.n), kBlock, 0, L.st>>>(cur, d, flume, routine, L.n);
 }
 
-void launch_part(const Launch &L, Planes cur, DevScalars *d, const NbrRec *nbr, const CullRec *cull,
-                 const int *start, int sph_id) {
+void launch_part(const Launch &L, Planes cur, DevScalars *d, const int *flume, const NbrRec *nbr,
+                 const CullRec *cull, const int *start, int sph_id) {
   if (L.n <= 0) return;
-  k_part<<<grid_for(L.n), kBlock, 0, L.st>>>(cur, d, nbr, cull, start, sph_id, L.n);
+  k_part<<<grid_for(L.n), kBlock, 0, L.st>>>(cur, d, flume, nbr, cull, start, sph_id, L.n);
 }
 
-void launch_get_accel(const Launch &L, Planes cur, DevScalars *d) {
+void launch_get_accel(const Launch &L, Planes cur, DevScalars *d, const int *flume) {
   if (L.n <= 0) return;
-  k_get_accel<<<grid_for(L.n), kBlock, 0, L.st>>>(cur, d, L.n);
+  k_get_accel<<<grid_for(L.n), kBlock, 0, L.st>>>(cur, d, flume, L.n);
 }
 
-void launch_finish_verlet(const Launch &L, Planes cur, DevScalars *d) {
+void launch_finish_verlet(const Launch &L, Planes cur, DevScalars *d, const int *flume) {
   if (L.n <= 0) return;
-  k_finish_verlet<<<grid_for(L.n), kBlock, 0, L.st>>>(cur, d, L.n);
+  k_finish_verlet<<<grid_for(L.n), kBlock, 0, L.st>>>(cur, d, flume, L.n);
 }
 
 void launch_clear_forces(const Launch &L, Planes cur) {
@@ -958,36 +1021,45 @@ void launch_clear_forces(const Launch &L, Planes cur) {
 
 void launch_advance_time(cudaStream_t st, DevScalars *d) { k_advance_time<<<1, 1, 0, st>>>(d); }
 
-void launch_regrid(const Launch &L, Planes cur, DevScalars *d, long bucket_cap) {
-  k_bbox_init<<<1, 1, 0, L.st>>>(d);
-  if (L.n > 0) k_bbox_reduce<<<grid_for(L.n, 256), 256, 0, L.st>>>(cur, d, L.n);
-  k_grid_derive<<<1, 1, 0, L.st>>>(d, L.n, bucket_cap);
+void launch_regrid(const Launch &L, Planes cur, DevScalars *d, const int *flume, int nflumes,
+                   long bucket_cap) {
+  const unsigned gf = (unsigned)((nflumes + 127) / 128);
+  k_bbox_init<<<gf, 128, 0, L.st>>>(d, nflumes);
+  if (L.n > 0) k_bbox_reduce<<<grid_for(L.n, 256), 256, 0, L.st>>>(cur, d, flume, L.n);
+  k_grid_derive<<<gf, 128, 0, L.st>>>(d, nflumes);
+  k_grid_commit<<<1, 1, 0, L.st>>>(d, nflumes, L.n, bucket_cap);
+}
+
+void launch_commit_grids(cudaStream_t st, DevScalars *d, int nflumes, long n, long bucket_cap) {
+  k_grid_commit<<<1, 1, 0, st>>>(d, nflumes, n, bucket_cap);
 }
 
 void launch_aos_to_planes(const Launch &L, const af3d_particle *aos, const double *acc,
-                          const double *anga, Planes cur, long long *id) {
+                          const double *anga, const int *flume_of_id, Planes cur, long long *id,
+                          int *flume) {
   if (L.n <= 0) return;
-  k_aos_to_planes<<<grid_for(L.n), kBlock, 0, L.st>>>(aos, acc, anga, cur, id, L.n);
+  k_aos_to_planes<<<grid_for(L.n), kBlock, 0, L.st>>>(aos, acc, anga, flume_of_id, cur, id, flume, L.n);
 }
 
-void launch_planes_to_aos(const Launch &L, Planes cur, const long long *id, af3d_particle *aos,
-                          double *acc, double *anga, DevScalars *d) {
+void launch_planes_to_aos(const Launch &L, Planes cur, const long long *id, const int *flume,
+                          af3d_particle *aos, double *acc, double *anga, DevScalars *d) {
   if (L.n <= 0) return;
-  k_planes_to_aos<<<grid_for(L.n), kBlock, 0, L.st>>>(cur, id, aos, acc, anga, d, L.n);
+  k_planes_to_aos<<<grid_for(L.n), kBlock, 0, L.st>>>(cur, id, flume, aos, acc, anga, d, L.n);
 }
 
-void launch_contact_pairs(const Launch &L, Planes cur, DevScalars *d, const NbrRec *nbr,
-                          const CullRec *cull, const int *start, const long long *id,
-                          long long *out, unsigned long long *count, long cap, int active) {
+void launch_contact_pairs(const Launch &L, Planes cur, DevScalars *d, const int *flume,
+                          const NbrRec *nbr, const CullRec *cull, const int *start,
+                          const long long *id, long long *out, unsigned long long *count, long cap,
+                          int active) {
   if (L.n <= 0) return;
-  k_contact_pairs<<<grid_for(L.n), kBlock, 0, L.st>>>(cur, d, nbr, cull, start, id, out, count, cap,
+  k_contact_pairs<<<grid_for(L.n), kBlock, 0, L.st>>>(cur, d, flume, nbr, cull, start, id, out, count, cap,
                                                       active, L.n);
 }
 
-void launch_cells_by_id(const Launch &L, const int *key, const long long *id, long ncell3,
+void launch_cells_by_id(const Launch &L, const int *key, const long long *id, DevScalars *d,
                         long long *cell_of_id) {
   if (L.n <= 0) return;
-  k_cells_by_id<<<grid_for(L.n), kBlock, 0, L.st>>>(key, id, ncell3, cell_of_id, L.n);
+  k_cells_by_id<<<grid_for(L.n), kBlock, 0, L.st>>>(key, id, d, cell_of_id, L.n);
 }
 
 }  // namespace af3d

@@ -35,7 +35,7 @@ __device__ __forceinline__ V3 mk(double x, double y, double z) {
   return r;
 }
 
-// Scalars of system_par / Funnel used by the force routines, loaded once per thread.
+// Scalars of one flume's system_par / Funnel used by the force routines, loaded once per thread.
 struct Consts {
   double dt, hdt, time, time_prev;
   double mu_pp, kappa_pp, gamma_pp, cns_pp;
@@ -45,14 +45,15 @@ struct Consts {
   int phase, variant;
 };
 
-__device__ __forceinline__ Consts load_consts(const DevScalars *d) {
+__device__ __forceinline__ Consts load_consts(const DevScalars *d, int f) {
   Consts c;
-  const af3d_system_par &s = d->sys;
-  c.dt = s.dt; c.hdt = s.hdt; c.time = s.time; c.time_prev = d->time_prev;
+  const DevFlume &fl = d->flumes[f];
+  const af3d_system_par &s = fl.sys;
+  c.dt = s.dt; c.hdt = s.hdt; c.time = d->time; c.time_prev = d->time_prev;
   c.mu_pp = s.mu_pp; c.kappa_pp = s.kappa_pp; c.gamma_pp = s.gamma_pp; c.cns_pp = s.fr_fact_pp;
   c.mu_pw = s.mu_pw; c.kappa_pw = s.kappa_pw; c.gamma_pw = s.gamma_pw; c.cns_pw = s.fr_fact_pw;
   c.sint = s.sint; c.cost = s.cost; c.dy2 = s.dy2; c.side_x = s.side.x; c.side_y = s.side.y;
-  c.sinfi = d->fun.sinfi; c.cosfi = d->fun.cosfi; c.tanfi = d->fun.tanfi;
+  c.sinfi = fl.fun.sinfi; c.cosfi = fl.fun.cosfi; c.tanfi = fl.fun.tanfi;
   c.phase = d->phase; c.variant = d->variant;
   return c;
 }

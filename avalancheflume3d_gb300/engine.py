@@ -30,18 +30,32 @@ def _vec3(n: int) -> np.ndarray:
 
 
 class Engine:
-    """One simulation context on the current CUDA device."""
+    """One simulation context on the current CUDA device.
+
+    ``sys``/``fun`` as structured scalars give the reference's single flume; as 1-d arrays of
+    length F they give a batched ensemble of F independent flumes (clump ids flume after flume,
+    shared dt and clock; see ``af3d_create_ensemble``)."""
 
     def __init__(self, sys: np.ndarray, fun: np.ndarray, ntags: int = 9, phase: int = PHASE_AVALANCHE,
                  friction: int = FRICTION_HST, stream: int | None = None):
         L = lib()
         self._L = L
-        self.sys = np.array(sys, dtype=SYSTEM_PAR).copy()
-        self.fun = np.array(fun, dtype=FUNNEL).copy()
-        self.n = int(self.sys["npart"])
+        sys_a = np.array(sys, dtype=SYSTEM_PAR)
+        fun_a = np.array(fun, dtype=FUNNEL)
+        self.ensemble = sys_a.ndim == 1
+        sys_a = np.ascontiguousarray(sys_a.reshape(-1)).copy()
+        fun_a = np.ascontiguousarray(fun_a.reshape(-1)).copy()
+        if len(fun_a) != len(sys_a):
+            raise ValueError("one Funnel per flume")
+        self.nflumes = len(sys_a)
+        self.flume_sizes = [int(s["npart"]) for s in sys_a]
+        self.first_id = np.concatenate([[0], np.cumsum(self.flume_sizes)]).astype(np.int64)
+        self.n = int(self.first_id[-1])
+        self.sys = sys_a if self.ensemble else sys_a.reshape(()).copy()
+        self.fun = fun_a if self.ensemble else fun_a.reshape(()).copy()
         h = C.c_void_p()
-        check(L.af3d_create(ptr(self.sys.reshape(1)), ptr(self.fun.reshape(1)), int(ntags), int(phase),
-                            C.byref(h)), "af3d_create")
+        check(L.af3d_create_ensemble(self.nflumes, ptr(sys_a), ptr(fun_a), int(ntags), int(phase),
+                                     C.byref(h)), "af3d_create_ensemble")
         self._h = h
         if friction != FRICTION_HST:
             self.set_friction(friction)
@@ -86,14 +100,19 @@ class Engine:
         return (pp, a, al) if with_accel else pp
 
     def set_system(self, sys: np.ndarray) -> None:
-        self.sys = np.array(sys, dtype=SYSTEM_PAR).copy()
-        self._call("af3d_set_system", ptr(self.sys.reshape(1)))
+        """system_par of flume 0 (the only flume of a plain context)."""
+        s = np.array(sys, dtype=SYSTEM_PAR).reshape(1).copy()
+        self._call("af3d_set_system", ptr(s))
+        if not self.ensemble:
+            self.sys = s.reshape(()).copy()
 
     def get_system(self) -> np.ndarray:
         s = np.zeros(1, dtype=SYSTEM_PAR)
         self._call("af3d_get_system", ptr(s))
-        self.sys = s.reshape(()).copy()
-        return self.sys
+        s = s.reshape(()).copy()
+        if not self.ensemble:
+            self.sys = s
+        return s
 
     def set_grid(self, cell: np.ndarray) -> None:
         c = np.array(cell, dtype=CELL_PAR).reshape(1).copy()
@@ -103,6 +122,33 @@ class Engine:
         c = np.zeros(1, dtype=CELL_PAR)
         self._call("af3d_get_grid", ptr(c))
         return c.reshape(()).copy()
+
+    # ---- per flume of an ensemble ----
+    def flume_slice(self, f: int) -> slice:
+        """Clump ids of flume f."""
+        return slice(int(self.first_id[f]), int(self.first_id[f + 1]))
+
+    def set_flume_system(self, f: int, sys: np.ndarray, fun: np.ndarray | None = None) -> None:
+        s = np.array(sys, dtype=SYSTEM_PAR).reshape(1).copy()
+        u = None if fun is None else np.array(fun, dtype=FUNNEL).reshape(1).copy()
+        self._call("af3d_set_flume_system", int(f), ptr(s), ptr(u))
+
+    def get_flume_system(self, f: int) -> np.ndarray:
+        s = np.zeros(1, dtype=SYSTEM_PAR)
+        self._call("af3d_get_flume_system", int(f), ptr(s))
+        return s.reshape(()).copy()
+
+    def set_flume_grid(self, f: int, cell: np.ndarray) -> None:
+        c = np.array(cell, dtype=CELL_PAR).reshape(1).copy()
+        self._call("af3d_set_flume_grid", int(f), ptr(c))
+
+    def get_flume_grid(self, f: int) -> np.ndarray:
+        c = np.zeros(1, dtype=CELL_PAR)
+        self._call("af3d_get_flume_grid", int(f), ptr(c))
+        return c.reshape(()).copy()
+
+    def flume_count(self) -> int:
+        return int(self._L.af3d_flume_count(self._h))
 
     def set_friction(self, variant: int) -> None:
         self._call("af3d_set_friction", int(variant))

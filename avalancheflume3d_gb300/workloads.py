@@ -20,9 +20,10 @@ import numpy as np
 
 from ._lib import INPUTS, PARTICLE
 from .engine import (Rannew64, calculate_particle_parameters, derive_system, lattice_block, lattice_pile,
-                     set_initial_velocity)
+                     set_initial_velocity, sphere_centres)
 
 HOP_WIDTH, HOP_HEIGHT, YHOP_L, YHOP_R = 15.0, 25.0, 7.5, 22.5
+LFUNNEL = 70.0
 
 
 @dataclass
@@ -43,8 +44,9 @@ class FlumeConfig:
     v0: float = 0.0              # initial speed in the reference's random directions
     seed: int = 20240613         # rannew64 seed of the orientations
     hopper_height: float | None = None
-    layout: str = "lattice"      # "lattice": clumps on the lattice; "pile": dropped into a pile
-    overlap: float = 2.0e-5      # pile: how far each clump is pressed into its support [cm]
+    layout: str = "lattice"      # "lattice" | "pile" | "bed" (see flume_state)
+    overlap: float | None = None  # how far each clump is pressed into its support [cm]:
+                                  # pile 2e-5 (default), bed 0 (default; gravity loads the layer)
 
     @property
     def t_coll(self) -> float:
@@ -80,7 +82,12 @@ def flume_state(cfg: FlumeConfig):
     wall are redrawn.
     layout "pile": the same lattice columns and random orientations, each clump dropped onto the
     closed door (z = 25) or the clumps already placed and pressed `overlap` into its support: the
-    packed pile the hopper-fill phase ends with, every resting contact carrying load.
+    packed pile the hopper-fill phase ends with, every resting contact carrying load.  Once the
+    door is open the pile falls freely, so its contacts relax within a few tens of steps.
+    layout "bed": the same packing built on the flume bed instead, in the slope frame (floor
+    z' = 0, side walls y = dy2 and dy2 + width, 1 cm clear of the funnel exit and the flume end)
+    and turned rigidly into the lab frame: a dense layer that gravity keeps pressed on the bed
+    while it slides, the state of an avalanche in full flow.
     With v0 > 0 the velocities follow the reference's set_initial_velocity (seed 26752658)."""
     sys, fun = derive_system(flume_inputs(cfg))
     sys["time"] = 0.0
@@ -93,7 +100,12 @@ def flume_state(cfg: FlumeConfig):
     top = HOP_HEIGHT + float(sys["side"][2])
     if cfg.layout == "pile":
         placed = lattice_pile(pp, (0.0, YHOP_L, HOP_HEIGHT), (HOP_WIDTH, YHOP_R, top), cfg.pitch,
-                              cfg.overlap, rng)
+                              2.0e-5 if cfg.overlap is None else cfg.overlap, rng)
+    elif cfg.layout == "bed":
+        dy2 = float(sys["dy2"])
+        placed = lattice_pile(pp, (LFUNNEL + 1.0, dy2, 0.0), (LFUNNEL + cfg.Lflume - 1.0, dy2 + cfg.width, 1e9),
+                              cfg.pitch, 0.0 if cfg.overlap is None else cfg.overlap, rng)
+        slope_to_lab(pp, sys)
     else:
         placed = lattice_block(pp, (0.0, YHOP_L, HOP_HEIGHT), (HOP_WIDTH, YHOP_R, top), cfg.pitch, rng)
     if placed != cfg.n:
@@ -103,6 +115,20 @@ def flume_state(cfg: FlumeConfig):
     slope_frame(pp, sys)
     sys["tot_mass"] = float(pp["mass"].sum())
     return sys, fun, pp
+
+
+def slope_to_lab(pp: np.ndarray, sys: np.ndarray) -> None:
+    """Turn clumps built in slope-frame coordinates into the lab frame (the inverse of
+    rotate_vectors.cu:28-46: x = x' cos + z' sin, y = y', z = z' cos - x' sin), centres and
+    orientation matrices alike; the sphere centres are then recomputed from them."""
+    c, s = float(sys["cost"]), float(sys["sint"])
+    r = pp["rr"].copy()
+    pp["rr"][:, 0] = r[:, 0] * c + r[:, 2] * s
+    pp["rr"][:, 2] = r[:, 2] * c - r[:, 0] * s
+    mx, mz = pp["Rmatx"].copy(), pp["Rmatz"].copy()
+    pp["Rmatx"] = mx * c + mz * s
+    pp["Rmatz"] = mz * c - mx * s
+    sphere_centres(pp)
 
 
 def slope_frame(pp: np.ndarray, sys: np.ndarray) -> None:
@@ -128,3 +154,42 @@ def flume_2k(**kw) -> FlumeConfig:
 def flume_262k(**kw) -> FlumeConfig:
     kw = {"n": 262144, "tilt_deg": 35.0, "width": 20.0, "Lflume": 200.0, **kw}
     return FlumeConfig(**kw)
+
+
+# Batched ensemble: independent flumes of the 2,048-clump geometry (40 cm x 4 cm flume) with
+# uneven clump counts and their own friction, restitution and slope.
+ENSEMBLE_SEED = 7340033
+
+
+def ensemble_configs(nflumes: int = 256, nmin: int = 1024, nmax: int = 16384, seed: int = ENSEMBLE_SEED,
+                     **kw) -> list[FlumeConfig]:
+    """Per flume, five rannew64 draws in this order: clump count ~ U{nmin..nmax}, mu_pp ~
+    U[0.2, 0.8], mu_pw ~ U[0.2, 0.6], restitution ~ U[0.2, 0.8], inclination ~ U[25, 40] deg.
+    Flume f's orientations use seed + 1 + f.  Some draws fail the reference's admission test
+    tan(tilt) >= 1.25 mu_pw (error_check.cu:58); they are kept (see `ensemble_flagged`)."""
+    rng = Rannew64(seed)
+    out = []
+    for f in range(nflumes):
+        n = nmin + min(int(rng() * (nmax - nmin + 1)), nmax - nmin)
+        mu_pp = 0.2 + 0.6 * rng()
+        mu_pw = 0.2 + 0.4 * rng()
+        e = 0.2 + 0.6 * rng()
+        tilt = 25.0 + 15.0 * rng()
+        out.append(flume_2k(**{"n": n, "mu_pp": mu_pp, "mu_pw": mu_pw, "restitution": e, "tilt_deg": tilt,
+                               "seed": seed + 1 + f, **kw}))
+    return out
+
+
+def ensemble_flagged(cfgs: list[FlumeConfig]) -> list[int]:
+    """Flumes the reference's error_check would refuse (tan(tilt) < 1.25 mu_pw)."""
+    return [f for f, c in enumerate(cfgs) if math.tan(math.radians(c.tilt_deg)) < 1.25 * c.mu_pw]
+
+
+def ensemble_state(cfgs: list[FlumeConfig]):
+    """(system_par[F], Funnel[F], particle array of every flume back to back) for an ensemble
+    context; flume f's clumps carry ids [sum of earlier counts, + cfgs[f].n)."""
+    states = [flume_state(c) for c in cfgs]
+    sys = np.stack([s for s, _, _ in states])
+    fun = np.stack([u for _, u, _ in states])
+    pp = np.concatenate([p for _, _, p in states])
+    return sys, fun, pp

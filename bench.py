@@ -3,14 +3,17 @@
 
 Workload ``flume262k`` (the 262,144-clump configuration): tetrahedral 4-sphere clumps, sphere
 radius 1 mm, density 2.5 g/cm^3, kn = 1e4 N/m (t_coll from the reference's law), restitution 0.5,
-mu_pp = 0.5, mu_wall = 0.4, flume 2.0 m x 0.2 m at 35 deg, dt = 2e-6 s, FP64.  The block stands in
-the hopper on the columns of a 4 mm lattice, each clump with a uniformly random orientation and
-zero velocity, dropped onto the clumps below it and pressed 2e-5 cm into its support (``--layout
-pile``): the packed block the hopper-fill phase ends with.  The door opens at time 0 and the timed
-steps follow the W warm-up steps of the release.  At dt = 2 us a timed window is a near-frozen
-snapshot, so its contact density is that of the input; ``--layout lattice`` (the bare lattice,
-optionally with the reference's random initial velocities ``--v0`` and a release ``--preroll``)
-has almost no contacts.  Synthetic data; the state (~400 MB) is larger than L2.
+mu_pp = 0.5, mu_wall = 0.4, flume 2.0 m x 0.2 m at 35 deg, dt = 2e-6 s, FP64.  Default input
+(``--layout bed``): the clumps, each with a uniformly random orientation and zero velocity, are
+dropped column by column on a 4 mm lattice onto the flume bed (in the slope frame, between the
+side walls, from 1 cm past the funnel exit to 1 cm before the flume end) and onto each other,
+then the layer is turned rigidly into the lab frame: a dense avalanche in full flow (~11 clump
+layers deep), which gravity keeps loaded on the bed, so the contact density holds over any
+timed window.  ``--layout pile`` builds the same packing in the hopper (it falls freely once the
+door opens, and its contacts relax within a few tens of steps); ``--layout lattice`` is the
+bare release block of the configuration (optionally with the reference's random initial
+velocities ``--v0`` and a release ``--preroll``), which has almost no contacts.  Synthetic data;
+the state (~400 MB) is larger than L2.
 
 Timed: exactly K fused steps (graph replays, af3d_step) after W warm-up steps, CUDA events on
 the engine's stream, barrier + synchronize on both sides, max over ranks.  Then, outside the
@@ -50,7 +53,7 @@ def parse_args():
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", choices=["engine", "reference"], default="engine")
     p.add_argument("--n", type=int, default=262144, help="clumps (262144 = the benchmark config)")
-    p.add_argument("--layout", choices=["pile", "lattice"], default="pile")
+    p.add_argument("--layout", choices=["bed", "pile", "lattice"], default="bed")
     p.add_argument("--preroll", type=int, default=0, help="untimed release steps of the input")
     p.add_argument("--v0", type=float, default=0.0)
     p.add_argument("--profile-steps", type=int, default=10)
@@ -58,6 +61,11 @@ def parse_args():
     p.add_argument("--cpu-sample", type=int, default=16384, help="clumps in the CPU baseline sample")
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--ensemble-flumes", type=int, default=256,
+                   help="flumes of the batched-ensemble measurement (0 skips it)")
+    p.add_argument("--ensemble-steps", type=int, default=64)
+    p.add_argument("--ensemble-seq-flumes", type=int, default=64,
+                   help="flumes timed one after another as plain runs (every k-th of the ensemble)")
     p.add_argument("--trace-contacts", type=int, default=0,
                    help="print active contacts every this many pre-roll steps (diagnostic)")
     return p.parse_args()
@@ -138,12 +146,19 @@ def traffic_from_profile():
     return None
 
 
-def cpu_sample_state(cfg, sys_, fun, pp, m):
-    """The first m clumps of the workload (the bottom layers of the block) as their own system."""
+def cpu_sample_state(cfg, sys_, fun, pp, m, acc=None, anga=None):
+    """The m clumps furthest upslope (smallest slope-frame x), a full-depth section of the layer,
+    as their own system (with their accelerations, when given)."""
     from oracle.pyoracle import SYSTEM_PAR
     s = np.array(sys_, dtype=SYSTEM_PAR).copy()
     s["npart"] = m
-    return s, fun, np.ascontiguousarray(pp[:m]).copy()
+    c, si = float(s["cost"]), float(s["sint"])
+    xrot = pp["rr"][:, 0] * c - pp["rr"][:, 2] * si
+    idx = np.sort(np.argsort(xrot, kind="stable")[:m])
+    out = [s, fun, np.ascontiguousarray(pp[idx]).copy()]
+    if acc is not None:
+        out += [np.ascontiguousarray(acc[idx]), np.ascontiguousarray(anga[idx])]
+    return out
 
 
 def time_cpu(sys_, fun, pp, threads, seconds, acc=None, anga=None, min_steps=2, max_steps=10 ** 6):
@@ -172,7 +187,7 @@ def run_reference(args):
     threads = os.cpu_count() or 1
     cfg, (sys_, fun, pp) = workload(args)
     m = min(args.n, max(args.cpu_sample, 65536))
-    s, f, q = cpu_sample_state(cfg, sys_, fun, pp, m)
+    s, f, q = cpu_sample_state(cfg, sys_, fun, pp, m)[:3]
     from oracle.pyoracle import Oracle, OracleRun
     o = Oracle()
     o.set_threads(threads)
@@ -185,8 +200,8 @@ def run_reference(args):
     run.step(args.steps, cc0=pre + args.warmup)
     dt = time.perf_counter() - t0
     value = m * args.steps / dt
-    sample = ("first %d clumps of the workload (bottom lattice layers) as their own system, %d release "
-              "steps, then %d timed steps" % (m, pre, args.steps))
+    sample = ("the %d clumps furthest upslope (a full-depth section of the input) as their own system, "
+              "%d release steps, then %d timed steps" % (m, pre, args.steps))
     line = {"metric": METRIC, "value": value, "unit": "clump-steps/s", "impl": "reference",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1000.0 * dt / args.steps * (args.n / m), "higher_is_better": True,
@@ -196,6 +211,72 @@ def run_reference(args):
                              "sample": sample},
             "e2e": {"value": value, "unit": "clump-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def measure_ensemble(args, stream):
+    """Batched ensemble against sequential plain runs, both through af3d_step on this stream.
+
+    Ensemble: ``--ensemble-flumes`` independent flumes of the 2,048-clump geometry with clump
+    counts ~ U{1024..16384} and per-flume mu_pp, mu_wall, restitution and slope from a seeded
+    rannew64, in one context with a segmented cell list; after a warm-up (which includes the
+    device re-grid after the first step and the capture of a 64-step graph) K steps are timed.
+    Sequential: every k-th flume of the same ensemble alone in a plain context, the same warm-up
+    and K timed steps each, one after another; throughput = their clump-steps / their summed
+    times.  Each flume evolves bit-identically in both (the ensemble tests check this)."""
+    import torch
+    from avalancheflume3d_gb300 import Engine
+    from avalancheflume3d_gb300.workloads import ensemble_configs, ensemble_flagged, ensemble_state
+    cfgs = ensemble_configs(args.ensemble_flumes, layout=args.layout)
+    sys_, fun, pp = ensemble_state(cfgs)
+    K = args.ensemble_steps
+    warm = K + 1
+
+    def timed(eng):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        eng.step(K)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1e3
+
+    eng = Engine(sys_, fun, stream=stream.cuda_stream)
+    eng.import_particles(pp)
+    eng.forces()
+    eng.swap_accel()
+    eng.step(warm)
+    eng.contact_count()
+    t_ens = timed(eng)
+    contacts = eng.contact_count()
+    n_total = len(pp)
+    first = eng.first_id.copy()
+    eng.close()
+    del eng
+    value = n_total * K / t_ens
+
+    stride = max(1, len(cfgs) // max(1, args.ensemble_seq_flumes))
+    seq_units, seq_t = 0, 0.0
+    for f in range(0, len(cfgs), stride):
+        pp_f = pp[first[f]:first[f + 1]]
+        with Engine(sys_[f], fun[f], stream=stream.cuda_stream) as one:
+            one.import_particles(pp_f)
+            one.forces()
+            one.swap_accel()
+            one.step(warm)
+            seq_t += timed(one)
+        seq_units += len(pp_f) * K
+    seq = seq_units / seq_t
+    return {"flumes": len(cfgs), "clumps": n_total, "steps": K, "warmup": warm,
+            "value": value, "unit": "clump-steps/s", "ms_per_step": 1e3 * t_ens / K,
+            "contacts_per_step": contacts / K,
+            "sequential_plain": {"value": seq, "unit": "clump-steps/s",
+                                 "flumes_timed": len(range(0, len(cfgs), stride)),
+                                 "what": "every %d-th flume alone in a plain context, one after another"
+                                         % stride},
+            "speedup_vs_sequential": value / seq,
+            "flagged_by_error_check": len(ensemble_flagged(cfgs)),
+            "graph_steps": 64, "layout": args.layout + " in each hopper, door open at t = 0",
+            "geometry": "40 cm x 4 cm flume, reference hopper and funnel; per-flume slope 25-40 deg"}
 
 
 def run_engine(args):
@@ -301,15 +382,19 @@ def run_engine(args):
                "what": "per step: import_particles (AoS + a_i from pinned host), af3d_step(1), "
                        "export_particles (AoS + a_i to pinned host)"}
 
+    ens = None
+    if world == 1 and args.ensemble_flumes > 0:
+        ens = measure_ensemble(args, stream)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         p_, a_, al_ = eng.export_particles()
         m = min(args.cpu_sample, args.n)
-        s, f, q = cpu_sample_state(cfg, eng.get_system(), fun, p_, m)
-        val, k, dt = time_cpu(s, f, q, 1, args.cpu_seconds, acc=a_[:m].copy(), anga=al_[:m].copy())
+        s, f, q, qa, qal = cpu_sample_state(cfg, eng.get_system(), fun, p_, m, a_, al_)
+        val, k, dt = time_cpu(s, f, q, 1, args.cpu_seconds, acc=qa, anga=qal)
         cpu = {"value": val, "unit": "clump-steps/s", "cores": 1, "kind": "port",
-               "sample": "first %d clumps of the timed state (bottom lattice layers) as their own "
-                         "system, %d steps in %.1f s, 1 thread" % (m, k, dt)}
+               "sample": "the %d clumps furthest upslope in the timed state (a full-depth section) as "
+                         "their own system, %d steps in %.1f s, 1 thread" % (m, k, dt)}
 
     eng.close()
     if rank == 0:
@@ -332,6 +417,7 @@ def run_engine(args):
                          "kernel_ms": prof[4], "note": "FP64-issue bound; see fp64"},
             "fp64": {"peak_tflops": fp64.value, "peak_source": "measured DFMA microbenchmark"},
             "phase_ms": {k: float(v) for k, v in zip(names, prof)},
+            "ensemble": ens,
             "cpu_baseline": cpu,
             "clocks": clk,
         }

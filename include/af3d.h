@@ -117,7 +117,28 @@ af3d_status af3d_get_system (af3d_ctx *ctx, af3d_system_par *sys);
 af3d_status af3d_set_grid (af3d_ctx *ctx, const af3d_cell_par *cell);
 af3d_status af3d_get_grid (af3d_ctx *ctx, af3d_cell_par *cell);
 af3d_status af3d_set_phase (af3d_ctx *ctx, int phase);
-/* cell_dim (cell_dim.cu:7) + grid derivation (avalanche_hst.cu:314-333), on the device. */
+
+/* ---- batched ensemble: many independent flumes in one context ---------------------------
+   The reference runs one flume per process (avalanche_dev.cu:140-158 sizes every array for one
+   system).  An ensemble context holds nflumes flumes back to back in clump-id order (flume f
+   owns ids [sum npart of flumes < f, + sys[f].npart)), each with its own system_par, Funnel
+   and cell grid, stepped together by af3d_step on one stream.  Clumps of different flumes
+   never interact.  The flumes share dt and the clock (time); material, geometry and tilt may
+   differ.  af3d_create is af3d_create_ensemble with nflumes = 1, and the single-flume calls
+   above (set/get_system, set/get_grid) address flume 0. */
+af3d_status af3d_create_ensemble (int nflumes, const af3d_system_par *sys, const af3d_funnel *fun,
+                                  long ntags, int phase, af3d_ctx **out);
+int         af3d_flume_count (af3d_ctx *ctx);
+/* fun may be NULL (keep the flume's Funnel).  sys->time sets the shared clock. */
+af3d_status af3d_set_flume_system (af3d_ctx *ctx, int flume, const af3d_system_par *sys,
+                                   const af3d_funnel *fun);
+af3d_status af3d_get_flume_system (af3d_ctx *ctx, int flume, af3d_system_par *sys);
+/* Setting the first grid of a context copies it to every flume that has none yet. */
+af3d_status af3d_set_flume_grid (af3d_ctx *ctx, int flume, const af3d_cell_par *cell);
+af3d_status af3d_get_flume_grid (af3d_ctx *ctx, int flume, af3d_cell_par *cell);
+
+/* cell_dim (cell_dim.cu:7) + grid derivation (avalanche_hst.cu:314-333), on the device, for
+   every flume of the context. */
 af3d_status af3d_regrid (af3d_ctx *ctx);
 /* Door opening: side.x = (LFUNNEL + Lflume) cos(tilt), time = 0, avalanche phase
    (avalanche_hst.cu:607-613). */

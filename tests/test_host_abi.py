@@ -183,3 +183,44 @@ def test_lattice_block_workload(af3d):
     assert np.allclose(np.einsum("nij,nkj->nik", R, R), np.eye(3), atol=1e-12)
     again = flume_state(flume_2k())[2]
     assert again.tobytes() == pp.tobytes()
+
+
+def test_bed_layer_workload(af3d):
+    """The dense layer on the flume bed: every sphere above the bed plane and between the side
+    walls (slope frame), rotations orthonormal, and resting contacts only (overlaps at rounding
+    level, no interpenetration)."""
+    from avalancheflume3d_gb300.workloads import flume_2k, flume_state
+    sys, fun, pp = flume_state(flume_2k(n=3000, layout="bed"))
+    r = float(pp["radius"][0])
+    q = pp["rrot_s"].reshape(-1, 3)
+    dy2, width = float(sys["dy2"]), float(sys["side"][1])
+    assert q[:, 2].min() >= r - 1e-9                      # on or above the bed z' = 0
+    assert q[:, 1].min() >= dy2 + r - 1e-9 and q[:, 1].max() <= dy2 + width - r + 1e-9
+    assert q[:, 0].min() >= 71.0 + r - 1e-9 and q[:, 0].max() <= 109.0 - r + 1e-9
+    R = np.stack([pp["Rmatx"], pp["Rmaty"], pp["Rmatz"]], 1)
+    assert np.allclose(np.einsum("nij,nkj->nik", R, R), np.eye(3), atol=1e-12)
+    # sphere pairs of different clumps: separation >= 2r up to rounding
+    from scipy.spatial import cKDTree
+    owner = np.repeat(np.arange(len(pp)), 4)
+    pairs = cKDTree(q).query_pairs(2 * r - 1e-9, output_type="ndarray")
+    pairs = pairs[owner[pairs[:, 0]] != owner[pairs[:, 1]]]
+    assert len(pairs) == 0
+    touching = cKDTree(q).query_pairs(2 * r + 1e-9, output_type="ndarray")
+    assert len(touching) > len(pp) // 2                    # a packed layer, not a loose lattice
+
+
+def test_ensemble_configs_draws(af3d):
+    from avalancheflume3d_gb300.workloads import ensemble_configs, ensemble_flagged, ensemble_state
+    cfgs = ensemble_configs(256)
+    n = np.array([c.n for c in cfgs])
+    assert n.min() >= 1024 and n.max() <= 16384 and len(set(n.tolist())) > 200
+    for name, lo, hi in (("mu_pp", 0.2, 0.8), ("mu_pw", 0.2, 0.6), ("restitution", 0.2, 0.8),
+                         ("tilt_deg", 25.0, 40.0)):
+        v = np.array([getattr(c, name) for c in cfgs])
+        assert v.min() >= lo and v.max() <= hi and v.max() - v.min() > 0.8 * (hi - lo), name
+    flagged = ensemble_flagged(cfgs)
+    assert 0 < len(flagged) < len(cfgs)
+    assert [c.n for c in ensemble_configs(256)] == n.tolist()          # seeded, repeatable
+    sys, fun, pp = ensemble_state(cfgs[:3])
+    assert sys.shape == (3,) and len(pp) == sum(c.n for c in cfgs[:3])
+    assert np.all(sys["dt"] == sys["dt"][0]) and len(set(sys["mu_pp"].tolist())) == 3
