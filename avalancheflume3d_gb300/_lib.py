@@ -101,6 +101,7 @@ SIGNATURES = [
     ("af3d_get_cells", [_P, _P, _P, _P], C.c_int),
     ("af3d_contact_pairs", [_P, _P, C.c_long, _P, C.c_int], C.c_int),
     ("af3d_contact_count", [_P, _P], C.c_int),
+    ("af3d_contact_pairs_noalloc", [_P, _P, C.c_long, _P, C.c_int], C.c_int),
     ("af3d_load_datainput", [C.c_char_p, _P], C.c_int),
     ("af3d_derive_system", [_P, _P, _P], C.c_int),
     ("af3d_error_check", [_P, C.c_char_p, C.c_size_t], C.c_int),

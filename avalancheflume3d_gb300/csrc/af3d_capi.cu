@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <utility>
 #include <vector>
@@ -885,3 +886,80 @@ af3d_status af3d_contact_count(af3d_ctx *c, long *count) {
 }
 
 }  // extern "C"
+
+// ---- allocation-free contact-pair readout ----------------------------------------------------
+//
+// af3d_contact_pairs stages the pairs in a device buffer it allocates and frees on every call.
+// Some callers cannot allow that: a host framework that reserved the GPU's memory for its own
+// caching pool at start-up would see the allocation fail mid-run, and cudaMalloc/cudaFree
+// around a diagnostic synchronise the whole device, stalling every other stream of a running
+// simulation.  af3d_contact_pairs_noalloc runs the same contact-pair kernel on a fixed staging
+// array that is part of this library's device image, so a call allocates no device memory.
+//
+// Set-up: the first call on a device, made with that device current, looks up the array's
+// device address once (cudaGetSymbolAddress; this also loads the library's device image on that
+// device if nothing else has).  Make that first call before any stream capture begins.
+// Sharing: every context on a device uses the same array, so calls that overlap in time (from
+// two host threads, or on two streams) race on it; callers serialise them per device.
+namespace {
+
+constexpr long kNoAllocMaxPairs = 262144;   // at most 262,144 (ll, mm, sph_id) triples: 6 MiB
+constexpr size_t kNoAllocHead = 256;        // the pair counter, padded to the array alignment
+constexpr int kNoAllocMaxDevices = 64;
+
+// [0, 8): pair counter, zeroed on the stream before each launch; [256, ...): the triples.
+static __device__ __align__(256) unsigned char
+    g_noalloc_scratch[kNoAllocHead + sizeof(long long) * 3 * kNoAllocMaxPairs];
+
+std::mutex g_noalloc_mutex;
+unsigned char *g_noalloc_addr[kNoAllocMaxDevices] = {};
+
+af3d_status noalloc_scratch(int device, unsigned char **addr) {
+  if (device < 0 || device >= kNoAllocMaxDevices)
+    return fail(AF3D_ERR_ARG, "device index beyond the " + std::to_string(kNoAllocMaxDevices) +
+                                  " devices the staging table covers");
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_addr[device]) {
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+      return fail(AF3D_ERR_CUDA, std::string("cudaGetSymbolAddress(staging array): ") + cudaGetErrorString(e));
+    g_noalloc_addr[device] = static_cast<unsigned char *>(p);
+  }
+  *addr = g_noalloc_addr[device];
+  return AF3D_OK;
+}
+
+}  // namespace
+
+extern "C" af3d_status af3d_contact_pairs_noalloc(af3d_ctx *c, long *out, long cap, long *count, int active) {
+  CHECK_STATE(c);
+  if (cap < 0 || cap > kNoAllocMaxPairs)
+    return fail(AF3D_ERR_ARG, "cap " + std::to_string(cap) + " is outside [0, " +
+                                  std::to_string(kNoAllocMaxPairs) + "], the staging array's size in pairs");
+  if (cap > 0 && !out) return fail(AF3D_ERR_ARG, "null output array");
+  int device = -1;
+  AF3D_CUDA(cudaGetDevice(&device));
+  if (device != c->device) return fail(AF3D_ERR_ARG, "the context's device must be the current device");
+  unsigned char *scratch = nullptr;
+  af3d_status s = noalloc_scratch(device, &scratch);
+  if (s) return s;
+  s = ensure_records(c);
+  if (s) return s;
+  unsigned long long *d_count = reinterpret_cast<unsigned long long *>(scratch);
+  long long *d_out = reinterpret_cast<long long *>(scratch + kNoAllocHead);
+  AF3D_CUDA(cudaMemsetAsync(d_count, 0, sizeof(unsigned long long), c->st));   // counter starts at 0
+  launch_contact_pairs(c->L(), c->cur, c->d, c->fl_cur, c->nbr, c->cull, c->cells.start, c->id_cur, d_out,
+                       d_count, cap, active);
+  unsigned long long cnt = 0;
+  AF3D_CUDA(cudaMemcpyAsync(&cnt, d_count, sizeof(cnt), cudaMemcpyDeviceToHost, c->st));
+  AF3D_CUDA(cudaStreamSynchronize(c->st));
+  const long kept = std::min<long>(cap, (long)cnt);
+  if (kept > 0) {
+    AF3D_CUDA(cudaMemcpyAsync(out, d_out, sizeof(long long) * 3 * kept, cudaMemcpyDeviceToHost, c->st));
+    AF3D_CUDA(cudaStreamSynchronize(c->st));
+  }
+  AF3D_CUDA(cudaGetLastError());
+  if (count) *count = (long)cnt;
+  return AF3D_OK;
+}

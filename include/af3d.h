@@ -194,6 +194,16 @@ af3d_status af3d_get_cells (af3d_ctx *ctx, long *cell_of_id, long *sorted_ids, l
 /* Overlapping sphere pairs (ll, mm, sph_id) of the last cell build, in no particular order;
    active = 1 keeps only pairs with a repulsive normal force.  *count may exceed cap. */
 af3d_status af3d_contact_pairs (af3d_ctx *ctx, long *out, long cap, long *count, int active);
+/* No counterpart in the reference.  af3d_contact_pairs without any device allocation, for
+   callers that must not allocate device memory mid-run (a host whose caching pool already holds
+   the GPU's memory; a running simulation that cannot afford the device-wide synchronisation of
+   cudaMalloc/cudaFree).  Pairs are staged in a fixed array inside the library's device image:
+   cap must lie in [0, 262144] (larger caps are refused with AF3D_ERR_ARG); *count is the total,
+   which may exceed cap.  The context's device must be current.  The first call on a device
+   looks up the array (set-up): make it before any stream capture.  The staging counter is
+   zeroed by each call on the context stream.  All contexts of a device share the array, so
+   calls that overlap in time race: serialise them per device. */
+af3d_status af3d_contact_pairs_noalloc (af3d_ctx *ctx, long *out, long cap, long *count, int active);
 /* Active sphere-sphere contacts summed over the fused force passes (af3d_step, af3d_forces)
    since the previous call; the counter restarts at zero. */
 af3d_status af3d_contact_count (af3d_ctx *ctx, long *count);
