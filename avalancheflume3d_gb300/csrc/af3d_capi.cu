@@ -351,7 +351,9 @@ af3d_status af3d_create_ensemble(int nflumes, const af3d_system_par *sys, const 
       return fail(AF3D_ERR_ARG, "the flumes of an ensemble share dt");
     total += sys[f].npart;
   }
-  if (total > (1L << 28)) return fail(AF3D_ERR_ARG, "too many clumps (at most 2^28)");
+  // Slots are packed with a 4-bit sphere-pair index into 32-bit work items, and the top 256
+  // codes are reserved for boundary items: at most 2^28 - 16 clumps.
+  if (total > (1L << 28) - 16) return fail(AF3D_ERR_ARG, "too many clumps (at most 2^28 - 16)");
   af3d_ctx *c = new af3d_ctx();
   c->n = total;
   c->nflumes = nflumes;

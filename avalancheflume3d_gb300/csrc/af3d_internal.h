@@ -38,7 +38,7 @@ struct Planes {
 struct __align__(64) NbrRec {
   double rx, ry, rz, vx, vy, vz, wx, wy, wz;
   double s[12];          // sphere k: s[3k], s[3k+1], s[3k+2]
-  double rad, msph, pad;
+  double rad, msph, mwall;   // sphere radius, sphere mass, wall-contact mass
 };
 
 // FP32 culling record.  c = (centre, bound), sk = (sphere centre, inflated radius).  The bounds

@@ -233,7 +233,7 @@ __device__ __forceinline__ float f_up(double x) { return __double2float_ru(x); }
 
 // Packed FP64 neighbour record and conservative FP32 culling record of one clump.
 __device__ __forceinline__ void make_records(V3 r, V3 v, V3 w, const V3 *sp, double rad, double msph,
-                                             NbrRec &q, CullRec &c) {
+                                             double mwall, NbrRec &q, CullRec &c) {
   q.rx = r.x; q.ry = r.y; q.rz = r.z;
   q.vx = v.x; q.vy = v.y; q.vz = v.z;
   q.wx = w.x; q.wy = w.y; q.wz = w.z;
@@ -245,7 +245,7 @@ __device__ __forceinline__ void make_records(V3 r, V3 v, V3 w, const V3 *sp, dou
     double dx = sp[k].x - r.x, dy = sp[k].y - r.y, dz = sp[k].z - r.z;
     ext = fmax(ext, sqrt(dx * dx + dy * dy + dz * dz));
   }
-  q.rad = rad; q.msph = msph; q.pad = 0.0;
+  q.rad = rad; q.msph = msph; q.mwall = mwall;
   // 2^-21 * max|coordinate| bounds 4x the FP32 rounding of a coordinate difference.
   const double mu = fmax(M, rad) * 4.76837158203125e-07 + 1e-30;
   const float radf = f_up(rad + mu);
@@ -285,7 +285,7 @@ __global__ void __launch_bounds__(kPermBlock) k_permute(Planes src, Planes dst, 
       for (int k = 0; k < 4; k++) sp[k] = load3(dst, S0X + 3 * k, s);
       NbrRec q;
       make_records(load3(dst, RX, s), load3(dst, VX, s), load3(dst, WX, s), sp, dst.p[RAD][s],
-                   dst.p[MSPH][s], q, s_cull[threadIdx.x]);
+                   dst.p[MSPH][s], dst.p[MWALL][s], q, s_cull[threadIdx.x]);
       const double *qw = reinterpret_cast<const double *>(&q);
 #pragma unroll
       for (int k = 0; k < kRecWords; k++) s_nbr[threadIdx.x * kRecStride + k] = qw[k];
@@ -311,9 +311,11 @@ __global__ void __launch_bounds__(kPermBlock) k_permute(Planes src, Planes dst, 
 constexpr int kCandCap = 48;
 constexpr float kCullSlack = 1.0f + 3.814697265625e-06f;  // 1 + 2^-18
 
+// Squared distance for the conservative FP32 culling tests (fused multiply-adds: their rounding
+// error is below the unfused one, and the tests' 2^-18 slack covers either).
 __device__ __forceinline__ float d2f(float4 a, float4 b) {
-  float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
-  return dx * dx + dy * dy + dz * dz;
+  const float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+  return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
 }
 
 // 16-bit mask of the sphere pairs of own clump (cull record me) and partner m that the FP32
@@ -508,14 +510,21 @@ __device__ __forceinline__ int particle_contacts(long s, const Own &o, const Con
   return active;
 }
 
-// Warp-cooperative contact pass of the fused kernel.  Every lane publishes its clump's item list
-// (sph_id-major, as above) in shared memory; the warp then works through the concatenated lists
-// 32 items per round, one item per lane, reading the owner clump from its record, and after each
-// round every owner adds its items' force and torque terms to its own sums in list order.  The
-// FP64 contact law thus runs with all lanes busy whatever the spread of contacts per clump, and
-// each clump's summation order stays the reference's.  All 32 lanes of the warp must call this;
-// `act` is false for lanes without a clump to process; `wbase` is the slot of the warp's lane 0.
+// Warp-cooperative pass of the fused kernel over every contact of a clump: the boundary routines
+// that run before the particle contacts, the sixteen sph_id passes, and the routines that run
+// after them (avalanche: hop x3, funnel, fcorners, walls | part x16 | flume; fill: part x16 |
+// hop x3).  Every lane publishes its clump's item list in that order in shared memory: boundary
+// items (routine, sphere) for the spheres the routine's 1-Lipschitz gate cannot rule out, and
+// particle items (partner slot, sph_id) in sph_id-major order.  The warp then works through the
+// concatenated lists 32 items per round, one item per lane, reading the owner clump from its
+// record; after each round every owner adds its items' force and torque terms to its own sums in
+// list order.  The FP64 contact laws thus run with all lanes busy whatever the spread of
+// contacts and walls over the clumps, and each clump's summation order stays the reference's.
+// All 32 lanes of the warp must call this; `act` is false for lanes without a clump to process
+// (and for removed clumps); `wbase` is the slot of the warp's lane 0.  A lane whose list would
+// overflow runs its own clump alone afterwards, in the same order.
 constexpr int kLaneItems = 32;
+constexpr unsigned kBndItem = 0xFFFFFF00u;   // boundary item: kBndItem | routine << 2 | sphere
 
 struct WarpQueue {
   unsigned items[32][kLaneItems];
@@ -524,17 +533,43 @@ struct WarpQueue {
   int base[33];
 };
 
-__device__ __forceinline__ int warp_contacts(WarpQueue &wq, long wbase, long s, bool act, const Own &o,
-                                             const Consts &c, const af3d_cell_par &g, long long off,
+// Boundary items of the routines [r0, r1] for one clump; false if the list would overflow.
+__device__ __forceinline__ bool push_boundary(int r0, int r1, const Own &o, double B, const Consts &c,
+                                              unsigned *items, int &nitems) {
+  for (int rt = r0; rt <= r1; rt++) {
+    if (!bnd_may_touch(rt, o.r, B, c)) continue;
+    for (int ns = 0; ns < 4; ns++) {
+      if (!bnd_may_touch(rt, o.s[ns], o.rad, c)) continue;   // the gate applied to one sphere
+      if (nitems == kLaneItems) return false;
+      items[nitems++] = kBndItem | (unsigned)(rt << 2) | (unsigned)ns;
+    }
+  }
+  return true;
+}
+
+__device__ __forceinline__ int warp_contacts(WarpQueue &wq, long wbase, long s, bool act, bool aval,
+                                             double B, const Own &o, const Consts &c,
+                                             const af3d_cell_par &g, long long off,
                                              const DevScalars *d, const int *__restrict__ flume,
                                              const NbrRec *__restrict__ nbr,
                                              const CullRec *__restrict__ cull,
                                              const int *__restrict__ start, V3 &F, V3 &T) {
   const int lane = threadIdx.x & 31;
   const int my_flume = flume[s];
+  const int pre0 = aval ? R_HOP0 : 1, pre1 = aval ? R_WALLS : 0;         // fill: none before
+  const int post0 = aval ? R_FLUME : R_HOP0, post1 = aval ? R_FLUME : R_HOP2;
   int nitems = 0;
   bool slow = false;
-  if (act) slow = !gather_items(s, o, g, off, cull, start, 0xffffu, wq.items[lane], kLaneItems, nitems);
+  if (act) {
+    unsigned *L = wq.items[lane];
+    slow = !push_boundary(pre0, pre1, o, B, c, L, nitems);
+    if (!slow) {
+      int np = 0;
+      slow = !gather_items(s, o, g, off, cull, start, 0xffffu, L + nitems, kLaneItems - nitems, np);
+      nitems += np;
+    }
+    if (!slow) slow = !push_boundary(post0, post1, o, B, c, L, nitems);
+  }
   if (slow) nitems = 0;
   int incl = nitems;
 #pragma unroll
@@ -557,19 +592,38 @@ __device__ __forceinline__ int warp_contacts(WarpQueue &wq, long wbase, long s, 
         if (wq.base[mid] <= j) lo = mid; else hi = mid - 1;
       }
       const unsigned it = wq.items[lo][j - wq.base[lo]];
-      const int t = (int)(it >> 4), p = (int)(it & 15u);
       const NbrRec &me = nbr[wbase + lo];   // owner lanes hold clumps, so wbase + lo < n
-      const V3 rl = mk(me.rx, me.ry, me.rz), vl = mk(me.vx, me.vy, me.vz), wl = mk(me.wx, me.wy, me.wz);
-      const int k = p & 3;
-      const V3 s1 = mk(me.s[3 * k], me.s[3 * k + 1], me.s[3 * k + 2]);
       // the owner's flume may differ from this lane's at a flume boundary of an ensemble
       const int of = flume[wbase + lo];
       const Consts co = of == my_flume ? c : load_consts(d, of);
+      // Prepare the item's contact (type-specific, short), then run the contact law once for
+      // every lane that has a contact, whatever its type.
+      ContactIn ci;
+      V3 rl = mk(me.rx, me.ry, me.rz);
+      int kind;   // 0 nothing, 1 sphere pair, 2 wall
+      if (it >= kBndItem) {
+        const int rt = (int)((it >> 2) & 7u), ns = (int)(it & 3u);
+        Sph q;
+        q.r = rl;
+        q.v = mk(me.vx, me.vy, me.vz);
+        q.w = mk(me.wx, me.wy, me.wz);
+        q.s = mk(me.s[3 * ns], me.s[3 * ns + 1], me.s[3 * ns + 2]);
+        q.rad = me.rad;
+        q.mwall = me.mwall;
+        kind = bnd_input(rt, q, co, ci) ? 2 : 0;
+      } else {
+        const int t = (int)(it >> 4), p = (int)(it & 15u);
+        const V3 vl = mk(me.vx, me.vy, me.vz), wl = mk(me.wx, me.wy, me.wz);
+        const int k = p & 3;
+        const V3 s1 = mk(me.s[3 * k], me.s[3 * k + 1], me.s[3 * k + 2]);
+        kind = pair_input(rl, vl, wl, s1, me.rad, me.msph, nbr[t], p >> 2, co,
+                          co.variant == AF3D_FRICTION_DEV, ci) ? 1 : 0;
+      }
       V3 fs, tq;
-      const int r = part_pair_contrib(rl, vl, wl, s1, me.rad, me.msph, nbr[t], p >> 2, co,
-                                      co.variant == AF3D_FRICTION_DEV, fs, tq);
+      int r = kind == 1 ? 1 : 0;
+      if (kind && apply_law(ci, rl, co.dt, fs, tq)) r = kind == 1 ? 2 : 3;
       wq.flag[lane] = r;
-      if (r == 2) {
+      if (r >= 2) {
         wq.res[lane][0] = fs.x; wq.res[lane][1] = fs.y; wq.res[lane][2] = fs.z;
         wq.res[lane][3] = tq.x; wq.res[lane][4] = tq.y; wq.res[lane][5] = tq.z;
       }
@@ -579,19 +633,26 @@ __device__ __forceinline__ int warp_contacts(WarpQueue &wq, long wbase, long s, 
       const int a = base > j0 ? base : j0;
       const int b = base + nitems < j0 + 32 ? base + nitems : j0 + 32;
       for (int e = a - j0; e < b - j0; e++) {
-        if (wq.flag[e] != 2) continue;
+        const int fl = wq.flag[e];
+        if (fl < 2) continue;
         T.x += wq.res[e][3]; T.y += wq.res[e][4]; T.z += wq.res[e][5];
         F.x += wq.res[e][0]; F.y += wq.res[e][1]; F.z += wq.res[e][2];
-        active++;
+        active += fl == 2;   // sphere-sphere contacts only
       }
     }
     __syncwarp();
   }
-  if (slow) active += contacts_by_pass(s, o, c, g, off, nbr, cull, start, 0xffffu, F, T);
+  if (slow) {
+    for (int rt = pre0; rt <= pre1; rt++)
+      if (bnd_may_touch(rt, o.r, B, c)) bnd_routine(rt, o, false, c, F, T);
+    active += contacts_by_pass(s, o, c, g, off, nbr, cull, start, 0xffffu, F, T);
+    for (int rt = post0; rt <= post1; rt++)
+      if (bnd_may_touch(rt, o.r, B, c)) bnd_routine(rt, o, false, c, F, T);
+  }
   return active;
 }
 
-__device__ __forceinline__ Own own_from_record(const NbrRec &q, double mwall) {
+__device__ __forceinline__ Own own_from_record(const NbrRec &q) {
   Own o;
   o.r = mk(q.rx, q.ry, q.rz);
   o.v = mk(q.vx, q.vy, q.vz);
@@ -599,7 +660,7 @@ __device__ __forceinline__ Own own_from_record(const NbrRec &q, double mwall) {
   for (int k = 0; k < 4; k++) o.s[k] = mk(q.s[3 * k], q.s[3 * k + 1], q.s[3 * k + 2]);
   o.rad = q.rad;
   o.msph = q.msph;
-  o.mwall = mwall;
+  o.mwall = q.mwall;
   return o;
 }
 
@@ -644,24 +705,27 @@ __global__ void __launch_bounds__(kBlock, AF3D_FORCES_MINB) k_fused_forces(Plane
   const Consts c = load_consts(d, f);
   const af3d_cell_par g = d->flumes[f].grid;
   const long long off = d->flumes[f].cell_off;
-  const Own o = own_from_record(nbr[sv], P.p[MWALL][sv]);
+  const Own o = own_from_record(nbr[sv]);
   const bool removed = is_removed(c.time, o.r.x, c.side_x);
   const double B = (double)cull[sv].c.w;   // sphere offsets + radius, rounded up
   V3 F = mk(0.0, 0.0, 0.0), T = mk(0.0, 0.0, 0.0);
   const bool aval = c.phase == AF3D_PHASE_AVALANCHE;
+#if AF3D_COOP
+  // Removed clumps get hop, funnel and fcorners only (walls, part and flume skip them).
+  if (valid && removed && aval)
+    for (int rt = R_HOP0; rt <= R_FCORNERS; rt++)
+      if (bnd_may_touch(rt, o.r, B, c)) bnd_routine(rt, o, true, c, F, T);
+  const long wbase = blockIdx.x * (long)blockDim.x + (threadIdx.x & ~31u);
+  const int active = warp_contacts(wq[threadIdx.x >> 5], wbase, sv, valid && !removed, aval, B, o, c, g, off,
+                                   d, flume, nbr, cull, start, F, T);
+#else
   if (valid && aval) {
     // hop x3, funnel, fcorners, walls (avalanche_hst.cu:688-696)
     for (int rt = R_HOP0; rt <= R_WALLS; rt++)
       if (bnd_may_touch(rt, o.r, B, c)) bnd_routine(rt, o, removed, c, F, T);
   }
   // part x16 (avalanche_hst.cu:699-701, fill :455-457)
-#if AF3D_COOP
-  const long wbase = blockIdx.x * (long)blockDim.x + (threadIdx.x & ~31u);
-  const int active = warp_contacts(wq[threadIdx.x >> 5], wbase, sv, valid && !removed, o, c, g, off, d,
-                                   flume, nbr, cull, start, F, T);
-#else
   const int active = (valid && !removed) ? particle_contacts(s, o, c, g, off, nbr, cull, start, -1, F, T) : 0;
-#endif
   if (valid) {
     if (aval) {
       if (bnd_may_touch(R_FLUME, o.r, B, c)) bnd_routine(R_FLUME, o, removed, c, F, T);   // :704
@@ -669,6 +733,9 @@ __global__ void __launch_bounds__(kBlock, AF3D_FORCES_MINB) k_fused_forces(Plane
       for (int rt = R_HOP0; rt <= R_HOP2; rt++)   // hop x3 after the particles (:460-461)
         if (bnd_may_touch(rt, o.r, B, c)) bnd_routine(rt, o, removed, c, F, T);
     }
+  }
+#endif
+  if (valid) {
     if (WRITE_FT) {
       store3(P, FX, s, F);
       store3(P, TX, s, T);

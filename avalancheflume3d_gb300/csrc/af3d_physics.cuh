@@ -91,17 +91,24 @@ __device__ __forceinline__ bool contact_law(V3 dvvc, V3 n, double comp, double k
   double xi_dot = xi / dt;
   double fsdt = 1.0e12 * mass_t * xi + 2.0e6 * mass_t * xi_dot;
   if (vt_mag > 0.0) {
-    if (fabs(fsdt) > mu * normal || (xi0 && xi == 0.0)) {
-      double af = 0.8 * mu * normal / vt_mag;
-      double t0 = mass_t / af;
-      af /= (1.0 + (dt / t0) * (dt / t0));
+    // Coulomb branch:  af = 0.8 mu N / |vt|; t0 = m / af; af /= 1 + (dt/t0)^2; f += af vt.
+    // Otherwise:       f_i += fsdt vt_i / |vt| where vt_i != 0.
+    // The two branches' first three divisions run as one sequence with per-lane operands, so
+    // a warp whose lanes take different branches executes three divisions, not seven; every
+    // lane still evaluates exactly its own branch's operations.
+    const bool coulomb = fabs(fsdt) > mu * normal || (xi0 && xi == 0.0);
+    const double q1 = (coulomb ? 0.8 * mu * normal : fsdt * vt.x) / vt_mag;   // af  | f_x term
+    const double q2 = (coulomb ? mass_t : fsdt * vt.y) / (coulomb ? q1 : vt_mag);   // t0 | f_y
+    const double q3 = (coulomb ? dt : fsdt * vt.z) / (coulomb ? q2 : vt_mag);   // dt/t0 | f_z
+    if (coulomb) {
+      const double af = q1 / (1.0 + q3 * q3);
       f.x += af * vt.x;
       f.y += af * vt.y;
       f.z += af * vt.z;
     } else {
-      if (vt.x != 0.0) f.x += fsdt * vt.x / vt_mag;
-      if (vt.y != 0.0) f.y += fsdt * vt.y / vt_mag;
-      if (vt.z != 0.0) f.z += fsdt * vt.z / vt_mag;
+      if (vt.x != 0.0) f.x += q1;
+      if (vt.y != 0.0) f.y += q2;
+      if (vt.z != 0.0) f.z += q3;
     }
   }
   return true;
@@ -116,16 +123,6 @@ __device__ __forceinline__ V3 point_velocity(V3 v, V3 w, V3 c, V3 r) {
   return u;
 }
 
-// T += (c - r) x fs; F += fs (force_part.cu:245-251).
-__device__ __forceinline__ void accumulate(V3 &F, V3 &T, V3 fs, V3 c, V3 r) {
-  T.x += (c.y - r.y) * fs.z - (c.z - r.z) * fs.y;
-  T.y += (c.z - r.z) * fs.x - (c.x - r.x) * fs.z;
-  T.z += (c.x - r.x) * fs.y - (c.y - r.y) * fs.x;
-  F.x += fs.x;
-  F.y += fs.y;
-  F.z += fs.z;
-}
-
 // The own clump as the force routines see it.
 struct Own {
   V3 r, v, w;
@@ -133,14 +130,63 @@ struct Own {
   double rad, mwall, msph;
 };
 
-__device__ __forceinline__ bool wall_contact(const Own &o, V3 rrc, V3 n, double comp, double km,
-                                             double gm, const Consts &c, bool gate, V3 &F, V3 &T) {
+// One sphere of a clump as a boundary routine sees it: clump centre, velocities, sphere
+// centre, radius and the wall-contact mass.
+struct Sph {
+  V3 r, v, w, s;
+  double rad, mwall;
+};
+
+__device__ __forceinline__ Sph sphere_of(const Own &o, int ns) {
+  Sph q;
+  q.r = o.r; q.v = o.v; q.w = o.w; q.s = o.s[ns]; q.rad = o.rad; q.mwall = o.mwall;
+  return q;
+}
+
+// The terms T += (c - r) x fs adds (force_part.cu:245-251), one component each.
+__device__ __forceinline__ V3 torque_term(V3 c, V3 r, V3 fs) {
+  return mk((c.y - r.y) * fs.z - (c.z - r.z) * fs.y, (c.z - r.z) * fs.x - (c.x - r.x) * fs.z,
+            (c.x - r.x) * fs.y - (c.y - r.y) * fs.x);
+}
+
+// T += tq; F += fs (force_part.cu:245-251 with tq = torque_term(c, r, fs)).
+__device__ __forceinline__ void add_terms(V3 &F, V3 &T, V3 fs, V3 tq) {
+  T.x += tq.x; T.y += tq.y; T.z += tq.z;
+  F.x += fs.x; F.y += fs.y; F.z += fs.z;
+}
+
+// Everything the contact law needs about one contact, from either a sphere pair or a sphere and
+// a wall: the relative velocity at the contact point, the normal, the compression, the spring
+// and dashpot coefficients, the tangential mass, friction and its cap, and the law's switches.
+struct ContactIn {
+  V3 dvvc, n, rrc;
+  double comp, km, gm, mass_t, mu, cns;
+  bool xi0, gate;
+};
+
+// Wall contact of one sphere at contact point rrc with outward normal n (force_walls.cu:106-177
+// and the same tail in every boundary routine).
+__device__ __forceinline__ void wall_input(const Sph &o, V3 rrc, V3 n, double comp, const Consts &c,
+                                           bool gate, ContactIn &ci) {
+  ci.km = 0.5 * c.kappa_pw * o.mwall;
+  ci.gm = 0.5 * c.gamma_pw * o.mwall;
   V3 vvc = point_velocity(o.v, o.w, rrc, o.r);
-  V3 dvvc = mk(-vvc.x, -vvc.y, -vvc.z);
-  V3 fs;
-  if (!contact_law(dvvc, n, comp, km, gm, o.mwall, c.mu_pw, c.cns_pw, c.dt, true, gate, fs))
+  ci.dvvc = mk(-vvc.x, -vvc.y, -vvc.z);
+  ci.n = n;
+  ci.rrc = rrc;
+  ci.comp = comp;
+  ci.mass_t = o.mwall;
+  ci.mu = c.mu_pw;
+  ci.cns = c.cns_pw;
+  ci.xi0 = true;
+  ci.gate = gate;
+}
+
+// The contact law on a prepared contact: force fs and its torque term about the clump centre r.
+__device__ __forceinline__ bool apply_law(const ContactIn &ci, V3 r, double dt, V3 &fs, V3 &tq) {
+  if (!contact_law(ci.dvvc, ci.n, ci.comp, ci.km, ci.gm, ci.mass_t, ci.mu, ci.cns, dt, ci.xi0, ci.gate, fs))
     return false;
-  accumulate(F, T, fs, rrc, o.r);
+  tq = torque_term(ci.rrc, r, fs);
   return true;
 }
 
@@ -152,139 +198,153 @@ __device__ __forceinline__ V3 to_lab(V3 q, double cost, double sint) {
   return mk(q.x * cost + q.z * sint, q.y, q.z * cost - q.x * sint);
 }
 
-// force_hop.cu:9-244 for one wall group nw.
-__device__ __forceinline__ void bnd_hop(const Own &o, int nw, const Consts &c, V3 &F, V3 &T) {
-  const double ri = o.rad, km = 0.5 * c.kappa_pw * o.mwall, gm = 0.5 * c.gamma_pw * o.mwall;
-#pragma unroll 1
-  for (int ns = 0; ns < 4; ns++) {
-    V3 s = o.s[ns], rrc, n;
-    double dist, comp = 0.0;
-    int touch = 0;
-    if (s.z < kHOP_HEIGHT || s.x > kHOP_WIDTH) continue;
-    if (nw == 0) {
-      dist = s.x - 0.0;
-      if (dist <= ri) { touch = 1; rrc = mk(0.0, s.y, s.z); n = mk(-1.0, 0.0, 0.0); comp = ri - dist; }
-      dist = kHOP_WIDTH - s.x;
-      if (dist <= ri) { touch = 2; rrc = mk(kHOP_WIDTH, s.y, s.z); n = mk(1.0, 0.0, 0.0); comp = ri - dist; }
-    } else if (nw == 1) {
-      dist = s.y - kYHOP_L;
-      if (dist <= ri) { touch = 3; rrc = mk(s.x, kYHOP_L, s.z); n = mk(0.0, -1.0, 0.0); comp = ri - dist; }
-      dist = kYHOP_R - s.y;
-      if (dist <= ri) { touch = 4; rrc = mk(s.x, kYHOP_R, s.z); n = mk(0.0, 1.0, 0.0); comp = ri - dist; }
-    } else {
-      dist = s.z - kHOP_HEIGHT;
-      if (dist <= ri) {
-        touch = c.time < 0.0 ? 5 : 0;   // the door is open once time >= 0 (force_hop.cu:140-143)
-        rrc = mk(s.x, s.y, kHOP_HEIGHT); n = mk(0.0, 0.0, -1.0); comp = ri - dist;
-      }
+// The per-sphere bodies of the boundary routines: the force of routine `routine` on one sphere
+// (false: no force).  Each routine adds its spheres' terms in sphere order a, b, c, d.
+
+// force_hop.cu:9-244, wall group nw, one sphere.
+__device__ __forceinline__ bool hop_sphere(const Sph &o, int nw, const Consts &c, ContactIn &ci) {
+  const double ri = o.rad;
+  const V3 s = o.s;
+  V3 rrc, n;
+  double dist, comp = 0.0;
+  int touch = 0;
+  if (s.z < kHOP_HEIGHT || s.x > kHOP_WIDTH) return false;
+  if (nw == 0) {
+    dist = s.x - 0.0;
+    if (dist <= ri) { touch = 1; rrc = mk(0.0, s.y, s.z); n = mk(-1.0, 0.0, 0.0); comp = ri - dist; }
+    dist = kHOP_WIDTH - s.x;
+    if (dist <= ri) { touch = 2; rrc = mk(kHOP_WIDTH, s.y, s.z); n = mk(1.0, 0.0, 0.0); comp = ri - dist; }
+  } else if (nw == 1) {
+    dist = s.y - kYHOP_L;
+    if (dist <= ri) { touch = 3; rrc = mk(s.x, kYHOP_L, s.z); n = mk(0.0, -1.0, 0.0); comp = ri - dist; }
+    dist = kYHOP_R - s.y;
+    if (dist <= ri) { touch = 4; rrc = mk(s.x, kYHOP_R, s.z); n = mk(0.0, 1.0, 0.0); comp = ri - dist; }
+  } else {
+    dist = s.z - kHOP_HEIGHT;
+    if (dist <= ri) {
+      touch = c.time < 0.0 ? 5 : 0;   // the door is open once time >= 0 (force_hop.cu:140-143)
+      rrc = mk(s.x, s.y, kHOP_HEIGHT); n = mk(0.0, 0.0, -1.0); comp = ri - dist;
     }
-    if (touch) wall_contact(o, rrc, n, comp, km, gm, c, false, F, T);
   }
+  if (!touch) return false;
+  wall_input(o, rrc, n, comp, c, false, ci);
+  return true;
 }
 
-// force_funnel.cu:9-213
-__device__ __forceinline__ void bnd_funnel(const Own &o, const Consts &c, V3 &F, V3 &T) {
-  const double ri = o.rad, km = 0.5 * c.kappa_pw * o.mwall, gm = 0.5 * c.gamma_pw * o.mwall;
-#pragma unroll 1
-  for (int ns = 0; ns < 4; ns++) {
-    V3 q = to_slope(o.s[ns], c.cost, c.sint), qc, nr, rrc, n;
-    double dist, comp = 0.0;
-    int touch = 0;
-    if (q.x > kLFUNNEL - ri * c.sinfi) continue;
-    dist = fabs(q.y - q.x * c.tanfi) * c.cosfi;
-    if (dist <= ri) {
-      touch = 1;
-      qc = mk(q.x + dist * c.sinfi, q.y - dist * c.cosfi, q.z);
-      nr = mk(c.sinfi, -c.cosfi, 0.0);
-      rrc = to_lab(qc, c.cost, c.sint);
-      n = to_lab(nr, c.cost, c.sint);
-      comp = ri - dist;
-    }
-    dist = fabs(kYFUNNEL - q.y - q.x * c.tanfi) * c.cosfi;
-    if (dist <= ri) {
-      touch = 2;
-      qc = mk(q.x + dist * c.sinfi, q.y + dist * c.cosfi, q.z);
-      nr = mk(c.sinfi, c.cosfi, 0.0);
-      rrc = to_lab(qc, c.cost, c.sint);
-      n = to_lab(nr, c.cost, c.sint);
-      comp = ri - dist;
-    }
-    if (touch) wall_contact(o, rrc, n, comp, km, gm, c, false, F, T);
+// force_funnel.cu:9-213, one sphere.
+__device__ __forceinline__ bool funnel_sphere(const Sph &o, const Consts &c, ContactIn &ci) {
+  const double ri = o.rad;
+  V3 q = to_slope(o.s, c.cost, c.sint), qc, nr, rrc, n;
+  double dist, comp = 0.0;
+  int touch = 0;
+  if (q.x > kLFUNNEL - ri * c.sinfi) return false;
+  dist = fabs(q.y - q.x * c.tanfi) * c.cosfi;
+  if (dist <= ri) {
+    touch = 1;
+    qc = mk(q.x + dist * c.sinfi, q.y - dist * c.cosfi, q.z);
+    nr = mk(c.sinfi, -c.cosfi, 0.0);
+    rrc = to_lab(qc, c.cost, c.sint);
+    n = to_lab(nr, c.cost, c.sint);
+    comp = ri - dist;
   }
+  dist = fabs(kYFUNNEL - q.y - q.x * c.tanfi) * c.cosfi;
+  if (dist <= ri) {
+    touch = 2;
+    qc = mk(q.x + dist * c.sinfi, q.y + dist * c.cosfi, q.z);
+    nr = mk(c.sinfi, c.cosfi, 0.0);
+    rrc = to_lab(qc, c.cost, c.sint);
+    n = to_lab(nr, c.cost, c.sint);
+    comp = ri - dist;
+  }
+  if (!touch) return false;
+  wall_input(o, rrc, n, comp, c, false, ci);
+  return true;
 }
 
-// force_funnel.cu:216-404
-__device__ __forceinline__ void bnd_fcorners(const Own &o, const Consts &c, V3 &F, V3 &T) {
-  const double ri = o.rad, km = 0.5 * c.kappa_pw * o.mwall, gm = 0.5 * c.gamma_pw * o.mwall;
+// force_funnel.cu:216-404, one sphere.
+__device__ __forceinline__ bool fcorners_sphere(const Sph &o, const Consts &c, ContactIn &ci) {
+  const double ri = o.rad;
   const double yfun_l = c.dy2, yfun_r = c.side_y + c.dy2, hsy = c.dy2 + c.side_y / 2.0;
-#pragma unroll 1
-  for (int ns = 0; ns < 4; ns++) {
-    V3 q = to_slope(o.s[ns], c.cost, c.sint);
-    if (q.x < kLFUNNEL - ri * c.sinfi || q.x > kLFUNNEL + ri) continue;
-    if (q.y > yfun_r || q.y < yfun_l) continue;
-    double yc = (q.y <= hsy) ? yfun_l : yfun_r;
-    double sep2 = ri * ri;
-    V3 d;
-    d.x = kLFUNNEL - q.x;
-    double dist2 = d.x * d.x;
-    if (dist2 > sep2) continue;
-    d.y = yc - q.y;
-    dist2 += d.y * d.y;
-    if (dist2 > sep2) continue;
-    double dist = sqrt(dist2);
-    V3 nr = mk(d.x / dist, d.y / dist, 0.0);
-    V3 qc = mk(q.x + ri * nr.x, q.y + ri * nr.y, q.z);
-    wall_contact(o, to_lab(qc, c.cost, c.sint), to_lab(nr, c.cost, c.sint), ri - dist, km, gm, c,
-                 true, F, T);
-  }
+  V3 q = to_slope(o.s, c.cost, c.sint);
+  if (q.x < kLFUNNEL - ri * c.sinfi || q.x > kLFUNNEL + ri) return false;
+  if (q.y > yfun_r || q.y < yfun_l) return false;
+  double yc = (q.y <= hsy) ? yfun_l : yfun_r;
+  double sep2 = ri * ri;
+  V3 d;
+  d.x = kLFUNNEL - q.x;
+  double dist2 = d.x * d.x;
+  if (dist2 > sep2) return false;
+  d.y = yc - q.y;
+  dist2 += d.y * d.y;
+  if (dist2 > sep2) return false;
+  double dist = sqrt(dist2);
+  V3 nr = mk(d.x / dist, d.y / dist, 0.0);
+  V3 qc = mk(q.x + ri * nr.x, q.y + ri * nr.y, q.z);
+  wall_input(o, to_lab(qc, c.cost, c.sint), to_lab(nr, c.cost, c.sint), ri - dist, c, true, ci);
+  return true;
 }
 
-// force_walls.cu:9-199 (caller skips removed clumps)
-__device__ __forceinline__ void bnd_walls(const Own &o, const Consts &c, V3 &F, V3 &T) {
-  const double ri = o.rad, km = 0.5 * c.kappa_pw * o.mwall, gm = 0.5 * c.gamma_pw * o.mwall;
+// force_walls.cu:9-199, one sphere (callers skip removed clumps).
+__device__ __forceinline__ bool walls_sphere(const Sph &o, const Consts &c, ContactIn &ci) {
+  const double ri = o.rad;
   const double yleft = c.dy2, yright = c.side_y + c.dy2;
-#pragma unroll 1
-  for (int ns = 0; ns < 4; ns++) {
-    V3 s = o.s[ns], rrc, n;
-    if (to_slope(s, c.cost, c.sint).x <= kLFUNNEL) continue;
-    double dist, comp = 0.0;
-    int touch = 0;
-    dist = s.y - yleft;
-    if (dist <= ri) { touch = 1; rrc = mk(s.x, yleft, s.z); n = mk(0.0, -1.0, 0.0); comp = ri - dist; }
-    dist = yright - s.y;
-    if (dist <= ri) { touch = 2; rrc = mk(s.x, yright, s.z); n = mk(0.0, 1.0, 0.0); comp = ri - dist; }
-    if (touch) wall_contact(o, rrc, n, comp, km, gm, c, false, F, T);
-  }
+  const V3 s = o.s;
+  V3 rrc, n;
+  if (to_slope(s, c.cost, c.sint).x <= kLFUNNEL) return false;
+  double dist, comp = 0.0;
+  int touch = 0;
+  dist = s.y - yleft;
+  if (dist <= ri) { touch = 1; rrc = mk(s.x, yleft, s.z); n = mk(0.0, -1.0, 0.0); comp = ri - dist; }
+  dist = yright - s.y;
+  if (dist <= ri) { touch = 2; rrc = mk(s.x, yright, s.z); n = mk(0.0, 1.0, 0.0); comp = ri - dist; }
+  if (!touch) return false;
+  wall_input(o, rrc, n, comp, c, false, ci);
+  return true;
 }
 
-// force_flume.cu:10-182 (caller skips removed clumps)
-__device__ __forceinline__ void bnd_flume(const Own &o, const Consts &c, V3 &F, V3 &T) {
-  const double ri = o.rad, km = 0.5 * c.kappa_pw * o.mwall, gm = 0.5 * c.gamma_pw * o.mwall;
+// force_flume.cu:10-182, one sphere (callers skip removed clumps).
+__device__ __forceinline__ bool flume_sphere(const Sph &o, const Consts &c, ContactIn &ci) {
+  const double ri = o.rad;
   const double tant = c.sint / c.cost;
+  const V3 s = o.s;
+  double rect = -tant * s.x - s.z;
+  double dist = fabs(c.cost * rect);
+  if (!(dist <= ri)) return false;
   const V3 n = mk(-c.sint, 0.0, -c.cost);
-#pragma unroll 1
-  for (int ns = 0; ns < 4; ns++) {
-    V3 s = o.s[ns];
-    double rect = -tant * s.x - s.z;
-    double dist = fabs(c.cost * rect);
-    if (dist <= ri) {
-      V3 rrc = mk(s.x - dist * c.sint, s.y, s.z - dist * c.cost);
-      wall_contact(o, rrc, n, ri - dist, km, gm, c, false, F, T);
-    }
-  }
+  V3 rrc = mk(s.x - dist * c.sint, s.y, s.z - dist * c.cost);
+  wall_input(o, rrc, n, ri - dist, c, false, ci);
+  return true;
 }
 
-// Apply one boundary routine with the reference's removed-clump rule for that routine.
+// The contact of routine `routine` with one sphere, prepared for the law (false: no contact).
+__device__ __forceinline__ bool bnd_input(int routine, const Sph &o, const Consts &c, ContactIn &ci) {
+  switch (routine) {
+    case R_HOP0: return hop_sphere(o, 0, c, ci);
+    case R_HOP1: return hop_sphere(o, 1, c, ci);
+    case R_HOP2: return hop_sphere(o, 2, c, ci);
+    case R_FUNNEL: return funnel_sphere(o, c, ci);
+    case R_FCORNERS: return fcorners_sphere(o, c, ci);
+    case R_WALLS: return walls_sphere(o, c, ci);
+    case R_FLUME: return flume_sphere(o, c, ci);
+  }
+  return false;
+}
+
+// The force of routine `routine` on one sphere and its torque term (false: no force).
+__device__ __forceinline__ bool bnd_sphere(int routine, const Sph &o, const Consts &c, V3 &fs, V3 &tq) {
+  ContactIn ci;
+  return bnd_input(routine, o, c, ci) && apply_law(ci, o.r, c.dt, fs, tq);
+}
+
+// One boundary routine over the four spheres of a clump, with the reference's removed-clump
+// rule for that routine (walls and flume skip removed clumps; hop, funnel, fcorners do not).
 __device__ __forceinline__ void bnd_routine(int routine, const Own &o, bool removed, const Consts &c,
                                             V3 &F, V3 &T) {
-  switch (routine) {
-    case R_HOP0: bnd_hop(o, 0, c, F, T); break;
-    case R_HOP1: bnd_hop(o, 1, c, F, T); break;
-    case R_HOP2: bnd_hop(o, 2, c, F, T); break;
-    case R_FUNNEL: bnd_funnel(o, c, F, T); break;
-    case R_FCORNERS: bnd_fcorners(o, c, F, T); break;
-    case R_WALLS: if (!removed) bnd_walls(o, c, F, T); break;
-    case R_FLUME: if (!removed) bnd_flume(o, c, F, T); break;
+  if (removed && (routine == R_WALLS || routine == R_FLUME)) return;
+#pragma unroll 1
+  for (int ns = 0; ns < 4; ns++) {
+    V3 fs, tq;
+    if (bnd_sphere(routine, sphere_of(o, ns), c, fs, tq)) add_terms(F, T, fs, tq);
   }
 }
 
@@ -326,41 +386,52 @@ __device__ __forceinline__ bool bnd_may_touch(int routine, V3 r, double B, const
   return true;
 }
 
-// One sphere-sphere contact of force_part.cu:139-252: own sphere s1 (clump centre rrl), partner
-// record m, partner sphere sm.  Returns 0 (no overlap), 1 (overlap, no force) or 2 (force); with
-// 2, fs is the contact force and tq its torque about rrl, the terms force_part.cu:245-251 adds.
-__device__ __forceinline__ int part_pair_contrib(const V3 &rrl, const V3 &vvl, const V3 &wwl,
-                                                 const V3 &s1, double rad_1, double massl,
-                                                 const NbrRec &m, int sm, const Consts &c, bool xi0,
-                                                 V3 &fs, V3 &tq) {
+// One sphere-sphere contact of force_part.cu:139-241: own sphere s1 (clump centre rrl), partner
+// record m, partner sphere sm.  Returns false when the staged test finds no overlap; otherwise
+// the contact is prepared for the law.
+__device__ __forceinline__ bool pair_input(const V3 &rrl, const V3 &vvl, const V3 &wwl, const V3 &s1,
+                                           double rad_1, double massl, const NbrRec &m, int sm,
+                                           const Consts &c, bool xi0, ContactIn &ci) {
   const double rad_2 = m.rad;
   const double sep = rad_1 + rad_2;
   const double sep2 = sep * sep;
   V3 d;
   d.x = m.s[3 * sm] - s1.x;
   double dist2 = d.x * d.x;
-  if (!(dist2 < sep2)) return 0;
+  if (!(dist2 < sep2)) return false;
   d.y = m.s[3 * sm + 1] - s1.y;
   dist2 += d.y * d.y;
-  if (!(dist2 < sep2)) return 0;
+  if (!(dist2 < sep2)) return false;
   d.z = m.s[3 * sm + 2] - s1.z;
   dist2 += d.z * d.z;
-  if (!(dist2 < sep2)) return 0;
+  if (!(dist2 < sep2)) return false;
   const double meff = 0.5 * (m.msph + massl);
-  const double km = 0.5 * c.kappa_pp * meff;
-  const double gm = 0.5 * c.gamma_pp * meff;
+  ci.km = 0.5 * c.kappa_pp * meff;
+  ci.gm = 0.5 * c.gamma_pp * meff;
   const double dist = sqrt(dist2);
-  V3 n = mk(d.x / dist, d.y / dist, d.z / dist);
-  V3 rrc = mk(s1.x + rad_1 * n.x, s1.y + rad_1 * n.y, s1.z + rad_1 * n.z);
-  V3 vl = point_velocity(vvl, wwl, rrc, rrl);
-  V3 vm = point_velocity(mk(m.vx, m.vy, m.vz), mk(m.wx, m.wy, m.wz), rrc, mk(m.rx, m.ry, m.rz));
-  V3 dvvc = mk(vm.x - vl.x, vm.y - vl.y, vm.z - vl.z);
-  if (!contact_law(dvvc, n, sep - dist, km, gm, massl, c.mu_pp, c.cns_pp, c.dt, xi0, false, fs))
-    return 1;
-  tq.x = (rrc.y - rrl.y) * fs.z - (rrc.z - rrl.z) * fs.y;
-  tq.y = (rrc.z - rrl.z) * fs.x - (rrc.x - rrl.x) * fs.z;
-  tq.z = (rrc.x - rrl.x) * fs.y - (rrc.y - rrl.y) * fs.x;
-  return 2;
+  ci.n = mk(d.x / dist, d.y / dist, d.z / dist);
+  ci.rrc = mk(s1.x + rad_1 * ci.n.x, s1.y + rad_1 * ci.n.y, s1.z + rad_1 * ci.n.z);
+  V3 vl = point_velocity(vvl, wwl, ci.rrc, rrl);
+  V3 vm = point_velocity(mk(m.vx, m.vy, m.vz), mk(m.wx, m.wy, m.wz), ci.rrc, mk(m.rx, m.ry, m.rz));
+  ci.dvvc = mk(vm.x - vl.x, vm.y - vl.y, vm.z - vl.z);
+  ci.comp = sep - dist;
+  ci.mass_t = massl;
+  ci.mu = c.mu_pp;
+  ci.cns = c.cns_pp;
+  ci.xi0 = xi0;
+  ci.gate = false;
+  return true;
+}
+
+// The whole sphere-sphere contact: 0 (no overlap), 1 (overlap, no force) or 2 (force); with 2,
+// fs is the contact force and tq its torque about rrl, the terms force_part.cu:245-251 adds.
+__device__ __forceinline__ int part_pair_contrib(const V3 &rrl, const V3 &vvl, const V3 &wwl,
+                                                 const V3 &s1, double rad_1, double massl,
+                                                 const NbrRec &m, int sm, const Consts &c, bool xi0,
+                                                 V3 &fs, V3 &tq) {
+  ContactIn ci;
+  if (!pair_input(rrl, vvl, wwl, s1, rad_1, massl, m, sm, c, xi0, ci)) return 0;
+  return apply_law(ci, rrl, c.dt, fs, tq) ? 2 : 1;
 }
 
 // The same contact accumulated into (F, T) in place.
