@@ -51,6 +51,7 @@ ERRORS = {1: "ARG", 2: "CUDA", 3: "NOMEM", 4: "GRID_ESCAPE", 5: "NEGATIVE_CELL",
           6: "CELL_CAPACITY", 7: "NAN", 8: "IO", 9: "INPUT"}
 FRICTION_HST, FRICTION_DEV = 0, 1
 PHASE_FILL, PHASE_AVALANCHE = 0, 1
+FP_EXACT, FP_FAST = 0, 1
 
 # (name, argtypes, restype) of every exported entry point of include/af3d.h.
 _P = C.c_void_p
@@ -59,6 +60,7 @@ SIGNATURES = [
     ("af3d_destroy", [_P], C.c_int),
     ("af3d_set_stream", [_P, _P], C.c_int),
     ("af3d_set_friction", [_P, C.c_int], C.c_int),
+    ("af3d_set_fp_mode", [_P, C.c_int], C.c_int),
     ("af3d_last_error", [], C.c_char_p),
     ("af3d_abi_version", [], C.c_int),
     ("af3d_import_particles", [_P, _P, _P, _P], C.c_int),

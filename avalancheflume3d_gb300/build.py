@@ -26,14 +26,16 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE
 # Extra nvcc flags for tuning sweeps (e.g. AF3D_NVCC_FLAGS="-DAF3D_FORCES_MINB=4").
 COMMON += os.environ.get("AF3D_NVCC_FLAGS", "").split()
 
-# (source, extra flags)
+# (source, object name, extra flags).  The step kernels are built twice: exact (no contraction,
+# the reference's operation order) and the fast FP64 mode (-DAF3D_FAST, contracted multiply-adds).
 UNITS = [
-    ("af3d_kernels.cu", ["-fmad=false", "-Xptxas", "-v"]),
-    ("af3d_cells.cu", []),
-    ("af3d_capi.cu", []),
-    ("af3d_peaks.cu", []),
+    ("af3d_kernels.cu", "af3d_kernels", ["-fmad=false", "-Xptxas", "-v"]),
+    ("af3d_kernels.cu", "af3d_kernels_fast", ["-fmad=true", "-DAF3D_FAST", "-Xptxas", "-v"]),
+    ("af3d_cells.cu", "af3d_cells", []),
+    ("af3d_capi.cu", "af3d_capi", []),
+    ("af3d_peaks.cu", "af3d_peaks", []),
 ]
-HOST_UNITS = [("af3d_hostio.cpp", ["-O2", "-ffp-contract=off"])]
+HOST_UNITS = [("af3d_hostio.cpp", "af3d_hostio", ["-O2", "-ffp-contract=off"])]
 
 HEADERS = ["af3d_internal.h", "af3d_physics.cuh"]
 
@@ -56,21 +58,21 @@ def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(OBJ, exist_ok=True)
     hdrs = [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(INCLUDE, "af3d.h"), __file__]
     jobs = []
-    for src, extra in UNITS:
+    for src, obj, extra in UNITS:
         s = os.path.join(CSRC, src)
-        o = os.path.join(OBJ, src + ".o")
+        o = os.path.join(OBJ, obj + ".o")
         if force or _stale(o, [s] + hdrs):
             jobs.append([NVCC, "-c"] + ARCH + COMMON + extra + ["-o", o, s])
-    for src, extra in HOST_UNITS:
+    for src, obj, extra in HOST_UNITS:
         s = os.path.join(CSRC, src)
-        o = os.path.join(OBJ, src + ".o")
+        o = os.path.join(OBJ, obj + ".o")
         if force or _stale(o, [s] + hdrs):
             jobs.append(["g++", "-c", "-std=c++17", "-fPIC", "-I", INCLUDE] + extra + ["-o", o, s])
     logs = []
     if jobs:
         with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 2))) as ex:
             logs = list(ex.map(_run, jobs))
-    objs = [os.path.join(OBJ, u + ".o") for u, _ in UNITS + HOST_UNITS]
+    objs = [os.path.join(OBJ, obj + ".o") for _, obj, _ in UNITS + HOST_UNITS]
     if force or jobs or _stale(LIB, objs):
         tmp = LIB + ".tmp%d" % os.getpid()
         _run([NVCC, "-shared"] + ARCH + ["-o", tmp] + objs)

@@ -67,6 +67,7 @@ struct af3d_ctx {
   long ntags = 9;
   int phase = AF3D_PHASE_AVALANCHE;
   int variant = AF3D_FRICTION_HST;
+  int fp_mode = AF3D_FP_EXACT;
   long cc = 0;                        // steps done in the current phase
   bool imported = false;
 
@@ -212,8 +213,23 @@ af3d_status regrid(af3d_ctx *c) {
 
 // clear_cell + clear_ocup + cell_locate: keys (optionally fused with the predictor), counting
 // sort, permutation of every plane into the new order, neighbour records.
+// The predictor and force launchers of the context's FP64 mode (the other kernels have one form).
+void predict_for(af3d_ctx *c, bool predict, bool keys, bool t_prev) {
+  if (c->fp_mode == AF3D_FP_FAST)
+    fast::launch_predict(c->L(), c->cur, c->d, predict, keys, t_prev, c->cells, c->id_cur, c->fl_cur);
+  else
+    launch_predict(c->L(), c->cur, c->d, predict, keys, t_prev, c->cells, c->id_cur, c->fl_cur);
+}
+
+void forces_for(af3d_ctx *c, bool write_ft) {
+  if (c->fp_mode == AF3D_FP_FAST)
+    fast::launch_fused_forces(c->L(), c->cur, c->alt, c->d, c->fl_cur, c->nbr, c->cull, c->cells.start, write_ft);
+  else
+    launch_fused_forces(c->L(), c->cur, c->alt, c->d, c->fl_cur, c->nbr, c->cull, c->cells.start, write_ft);
+}
+
 void enqueue_cell_build(af3d_ctx *c, bool predict, bool t_prev, bool ft = true) {
-  launch_predict(c->L(), c->cur, c->d, predict, true, t_prev, c->cells, c->id_cur, c->fl_cur);
+  predict_for(c, predict, true, t_prev);
   launch_sort(c->L(), c->d, c->cells, c->id_cur, c->ntags);
   launch_permute_records(c->L(), c->cur, c->alt, c->cells.perm, c->id_cur, c->id_alt, c->fl_cur, c->fl_alt,
                          c->nbr, c->cull, ft);
@@ -227,7 +243,7 @@ void enqueue_cell_build(af3d_ctx *c, bool predict, bool t_prev, bool ft = true) 
 void enqueue_fused_step(af3d_ctx *c) {
   launch_advance_time(c->st, c->d);
   enqueue_cell_build(c, true, true, false);   // F, T and a_f are rewritten before being read
-  launch_fused_forces(c->L(), c->cur, c->alt, c->d, c->fl_cur, c->nbr, c->cull, c->cells.start, false);
+  forces_for(c, false);
   swap_velocity_planes(c->cur, c->alt);
   swap_accel_planes(c->cur);
   swap_accel_planes(c->alt);
@@ -476,6 +492,15 @@ af3d_status af3d_set_friction(af3d_ctx *c, int variant) {
   return push_params(c);
 }
 
+af3d_status af3d_set_fp_mode(af3d_ctx *c, int mode) {
+  CHECK_CTX(c);
+  if (mode != AF3D_FP_EXACT && mode != AF3D_FP_FAST) return fail(AF3D_ERR_ARG, "unknown FP64 mode");
+  AF3D_CUDA(cudaStreamSynchronize(c->st));
+  if (mode != c->fp_mode) drop_graphs(c);
+  c->fp_mode = mode;
+  return AF3D_OK;
+}
+
 af3d_status af3d_import_particles(af3d_ctx *c, const af3d_particle *pp, const af3d_vec3 *acc,
                                   const af3d_vec3 *anga) {
   CHECK_CTX(c);
@@ -707,7 +732,7 @@ af3d_status af3d_forces(af3d_ctx *c) {
   enqueue_cell_build(c, false, false);
   c->cells_valid = true;
   // Corrected velocities go to the dead plane set and are dropped: this pass stops at get_accel.
-  launch_fused_forces(c->L(), c->cur, c->alt, c->d, c->fl_cur, c->nbr, c->cull, c->cells.start, true);
+  forces_for(c, true);
   c->launches += kKernelsPerCellBuild + 1;
   c->records_valid = true;
   int flags = 0;
@@ -753,7 +778,7 @@ af3d_status af3d_step_profile(af3d_ctx *c, long k, double *ms) {
     AF3D_CUDA(cudaEventRecord(ev[0], c->st));
     launch_advance_time(c->st, c->d);
     AF3D_CUDA(cudaEventRecord(ev[1], c->st));
-    launch_predict(c->L(), c->cur, c->d, true, true, true, c->cells, c->id_cur, c->fl_cur);
+    predict_for(c, true, true, true);
     AF3D_CUDA(cudaEventRecord(ev[2], c->st));
     launch_sort(c->L(), c->d, c->cells, c->id_cur, c->ntags);
     AF3D_CUDA(cudaEventRecord(ev[3], c->st));
@@ -763,7 +788,7 @@ af3d_status af3d_step_profile(af3d_ctx *c, long k, double *ms) {
     std::swap(c->id_cur, c->id_alt);
     std::swap(c->fl_cur, c->fl_alt);
     AF3D_CUDA(cudaEventRecord(ev[4], c->st));
-    launch_fused_forces(c->L(), c->cur, c->alt, c->d, c->fl_cur, c->nbr, c->cull, c->cells.start, false);
+    forces_for(c, false);
     swap_velocity_planes(c->cur, c->alt);
     swap_accel_planes(c->cur);
     swap_accel_planes(c->alt);

@@ -145,4 +145,13 @@ void launch_cells_by_id (const Launch &L, const int *key, const long long *id, D
 // DFMA throughput microbenchmark (TFLOP/s, 2 flops per DFMA), bounded to ~0.1 s.
 cudaError_t measure_dfma (int sms, double *tflops);
 
+// The predictor and the fused force pass of the fast FP64 mode (af3d_kernels.cu compiled with
+// -DAF3D_FAST -fmad=true; same arguments as above).
+namespace fast {
+void launch_predict (const Launch &L, Planes cur, DevScalars *d, bool predict, bool keys, bool t_prev,
+                     Cells cells, const long long *id, const int *flume);
+void launch_fused_forces (const Launch &L, Planes cur, Planes out, DevScalars *d, const int *flume,
+                          const NbrRec *nbr, const CullRec *cull, const int *start, bool write_ft);
+}  // namespace fast
+
 }  // namespace af3d

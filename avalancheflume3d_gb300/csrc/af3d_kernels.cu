@@ -151,12 +151,28 @@ __global__ void k_predict(Planes P, DevScalars *d, bool t_prev, Cells cells,
       v.y += dt * a.y;
       v.z += dt * a.z;
       V3 dO = mk(dt * (w.x + hdt * al.x), dt * (w.y + hdt * al.y), dt * (w.z + hdt * al.z));
-      double mag = sqrt(dO.x * dO.x + dO.y * dO.y + dO.z * dO.z);
+      const double mag2 = dO.x * dO.x + dO.y * dO.y + dO.z * dO.z;
+      double mag, imag = 0.0;
+      if (kFast) {
+        imag = rsqrt(mag2);
+        mag = mag2 * imag;
+      } else {
+        mag = sqrt(mag2);
+      }
       V3 dRx, dRy, dRz;
       if (mag > 0.0) {
         // Rodrigues rotation about dO/|dO| by |dO| (init_Verlet.cu:63-83)
-        V3 u = mk(dO.x / mag, dO.y / mag, dO.z / mag);
-        double c = cos(mag), sn = sin(mag), omc = 1.0 - c;
+        V3 u;
+        double c, sn;
+        if (kFast) {
+          u = mk(dO.x * imag, dO.y * imag, dO.z * imag);
+          sincos(mag, &sn, &c);
+        } else {
+          u = mk(dO.x / mag, dO.y / mag, dO.z / mag);
+          c = cos(mag);
+          sn = sin(mag);
+        }
+        const double omc = 1.0 - c;
         dRx = mk(omc * u.x * u.x + c, omc * u.x * u.y - sn * u.z, omc * u.x * u.z + sn * u.y);
         dRy = mk(omc * u.y * u.x + sn * u.z, omc * u.y * u.y + c, omc * u.y * u.z - sn * u.x);
         dRz = mk(omc * u.z * u.x - sn * u.y, omc * u.z * u.y + sn * u.x, omc * u.z * u.z + c);
@@ -172,12 +188,21 @@ __global__ void k_predict(Planes P, DevScalars *d, bool t_prev, Cells cells,
                  dRy.x * Rx.z + dRy.y * Ry.z + dRy.z * Rz.z);
       V3 Tz = mk(dRz.x * Rx.x + dRz.y * Ry.x + dRz.z * Rz.x, dRz.x * Rx.y + dRz.y * Ry.y + dRz.z * Rz.y,
                  dRz.x * Rx.z + dRz.y * Ry.z + dRz.z * Rz.z);
-      double nrm = sqrt(Tx.x * Tx.x + Ty.x * Ty.x + Tz.x * Tz.x);
-      Rx.x = Tx.x / nrm; Ry.x = Ty.x / nrm; Rz.x = Tz.x / nrm;
-      nrm = sqrt(Tx.y * Tx.y + Ty.y * Ty.y + Tz.y * Tz.y);
-      Rx.y = Tx.y / nrm; Ry.y = Ty.y / nrm; Rz.y = Tz.y / nrm;
-      nrm = sqrt(Tx.z * Tx.z + Ty.z * Ty.z + Tz.z * Tz.z);
-      Rx.z = Tx.z / nrm; Ry.z = Ty.z / nrm; Rz.z = Tz.z / nrm;
+      if (kFast) {
+        double in = rsqrt(Tx.x * Tx.x + Ty.x * Ty.x + Tz.x * Tz.x);
+        Rx.x = Tx.x * in; Ry.x = Ty.x * in; Rz.x = Tz.x * in;
+        in = rsqrt(Tx.y * Tx.y + Ty.y * Ty.y + Tz.y * Tz.y);
+        Rx.y = Tx.y * in; Ry.y = Ty.y * in; Rz.y = Tz.y * in;
+        in = rsqrt(Tx.z * Tx.z + Ty.z * Ty.z + Tz.z * Tz.z);
+        Rx.z = Tx.z * in; Ry.z = Ty.z * in; Rz.z = Tz.z * in;
+      } else {
+        double nrm = sqrt(Tx.x * Tx.x + Ty.x * Ty.x + Tz.x * Tz.x);
+        Rx.x = Tx.x / nrm; Ry.x = Ty.x / nrm; Rz.x = Tz.x / nrm;
+        nrm = sqrt(Tx.y * Tx.y + Ty.y * Ty.y + Tz.y * Tz.y);
+        Rx.y = Tx.y / nrm; Ry.y = Ty.y / nrm; Rz.y = Tz.y / nrm;
+        nrm = sqrt(Tx.z * Tx.z + Ty.z * Ty.z + Tz.z * Tz.z);
+        Rx.z = Tx.z / nrm; Ry.z = Ty.z / nrm; Rz.z = Tz.z / nrm;
+      }
       w.x += dt * al.x;
       w.y += dt * al.y;
       w.z += dt * al.z;
@@ -188,7 +213,7 @@ __global__ void k_predict(Planes P, DevScalars *d, bool t_prev, Cells cells,
       store3(P, R10, s, Ry);
       store3(P, R20, s, Rz);
       // sphere centres r + (radius/sqrt2) R (+-1,+-1,+-1) (init_Verlet.cu:130-142)
-      const double pos = P.p[RAD][s] / kROOT2;
+      const double pos = kFast ? P.p[RAD][s] * (1.0 / kROOT2) : P.p[RAD][s] / kROOT2;
       store3(P, S0X, s, mk(r.x + pos * (Rx.x + Rx.y + Rx.z), r.y + pos * (Ry.x + Ry.y + Ry.z),
                            r.z + pos * (Rz.x + Rz.y + Rz.z)));
       store3(P, S1X, s, mk(r.x + pos * (Rx.x - Rx.y - Rx.z), r.y + pos * (Ry.x - Ry.y - Ry.z),
@@ -323,6 +348,19 @@ __device__ __forceinline__ float d2f(float4 a, float4 b) {
 __device__ __forceinline__ unsigned pair_mask(const CullRec &me, const CullRec &m) {
   const float lim = me.c.w + m.c.w;
   if (d2f(me.c, m.c) > lim * lim * kCullSlack) return 0u;
+  const float rl = me.s[0].w + m.s[0].w;
+  const float r2 = rl * rl * kCullSlack;
+  unsigned mask = 0u;
+#pragma unroll
+  for (int j = 0; j < 4; j++)
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+      if (d2f(me.s[k], m.s[j]) <= r2) mask |= 1u << (4 * j + k);
+  return mask;
+}
+
+// The sixteen sphere tests of pair_mask alone (for partners whose centre test passed).
+__device__ __forceinline__ unsigned sphere_mask(const CullRec &me, const CullRec &m) {
   const float rl = me.s[0].w + m.s[0].w;
   const float r2 = rl * rl * kCullSlack;
   unsigned mask = 0u;
@@ -526,12 +564,43 @@ __device__ __forceinline__ int particle_contacts(long s, const Own &o, const Con
 constexpr int kLaneItems = 32;
 constexpr unsigned kBndItem = 0xFFFFFF00u;   // boundary item: kBndItem | routine << 2 | sphere
 
+constexpr int kPassCap = 32;   // partners per clump that pass the centre test
+
 struct WarpQueue {
   unsigned items[32][kLaneItems];
   double res[32][6];
   int flag[32];
   int base[33];
+  int pass_t[32][kPassCap];              // partner slots in walk order, per lane
+  unsigned short pass_m[32][kPassCap];   // their 16-bit sphere-pair masks
+  int pbase[33];
 };
+
+// Exclusive prefix of `v` over the warp into sh[0..32]; returns the total.
+__device__ __forceinline__ int warp_prefix(int v, int *sh) {
+  const int lane = threadIdx.x & 31;
+  int incl = v;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const int u = __shfl_up_sync(0xffffffffu, incl, off);
+    if (lane >= off) incl += u;
+  }
+  sh[lane] = incl - v;
+  const int total = __shfl_sync(0xffffffffu, incl, 31);
+  if (lane == 31) sh[32] = total;
+  __syncwarp();
+  return total;
+}
+
+// The lane whose range [sh[l], sh[l+1]) holds position j (sh: exclusive prefix of 32 counts).
+__device__ __forceinline__ int owner_of(const int *sh, int j) {
+  int lo = 0, hi = 31;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (sh[mid] <= j) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
 
 // Boundary items of the routines [r0, r1] for one clump; false if the list would overflow.
 __device__ __forceinline__ bool push_boundary(int r0, int r1, const Own &o, double B, const Consts &c,
@@ -560,37 +629,60 @@ __device__ __forceinline__ int warp_contacts(WarpQueue &wq, long wbase, long s, 
   const int post0 = aval ? R_FLUME : R_HOP0, post1 = aval ? R_FLUME : R_HOP2;
   int nitems = 0;
   bool slow = false;
-  if (act) {
-    unsigned *L = wq.items[lane];
-    slow = !push_boundary(pre0, pre1, o, B, c, L, nitems);
-    if (!slow) {
-      int np = 0;
-      slow = !gather_items(s, o, g, off, cull, start, 0xffffu, L + nitems, kLaneItems - nitems, np);
-      nitems += np;
+  unsigned *L = wq.items[lane];
+  if (act) slow = !push_boundary(pre0, pre1, o, B, c, L, nitems);
+  // Particle partners, stage 1 (per lane): walk the 27 neighbour cells in the reference's order
+  // and keep the partners whose bounding spheres can touch (FP32 centre test).
+  int npass = 0;
+  if (act && !slow) {
+    const float4 mc = cull[s].c;
+    const Search q = search_centre(o.r, g, off);
+    for_neighbour_slots_pre(q, g, start, [&](int t) {
+      if (t == s) return;
+      const float4 pc = cull[t].c;
+      const float lim = mc.w + pc.w;
+      if (d2f(mc, pc) > lim * lim * kCullSlack) return;
+      if (npass < kPassCap) wq.pass_t[lane][npass] = t;
+      npass++;
+    });
+    if (npass > kPassCap) {
+      slow = true;
+      npass = 0;
     }
+  }
+  // Stage 2 (whole warp): the sixteen sphere tests of every kept partner, 32 partners a round.
+  const int total_pass = warp_prefix(npass, wq.pbase);
+  for (int j0 = 0; j0 < total_pass; j0 += 32) {
+    const int j = j0 + lane;
+    if (j < total_pass) {
+      const int ow = owner_of(wq.pbase, j), k = j - wq.pbase[ow];
+      wq.pass_m[ow][k] = (unsigned short)sphere_mask(cull[wbase + ow], cull[wq.pass_t[ow][k]]);
+    }
+  }
+  __syncwarp();
+  // Each lane's particle items, sph_id-major (the order of the sixteen force_part launches).
+  if (act && !slow) {
+#pragma unroll 1
+    for (int p = 0; p < 16 && !slow; p++)
+#pragma unroll 1
+      for (int k = 0; k < npass; k++) {
+        if (!((wq.pass_m[lane][k] >> p) & 1u)) continue;
+        if (nitems == kLaneItems) {
+          slow = true;
+          break;
+        }
+        L[nitems++] = ((unsigned)wq.pass_t[lane][k] << 4) | (unsigned)p;   // (partner slot, sph_id-1)
+      }
     if (!slow) slow = !push_boundary(post0, post1, o, B, c, L, nitems);
   }
   if (slow) nitems = 0;
-  int incl = nitems;
-#pragma unroll
-  for (int off = 1; off < 32; off <<= 1) {
-    const int u = __shfl_up_sync(0xffffffffu, incl, off);
-    if (lane >= off) incl += u;
-  }
-  const int base = incl - nitems;
-  const int total = __shfl_sync(0xffffffffu, incl, 31);
-  wq.base[lane] = base;
-  if (lane == 31) wq.base[32] = total;
-  __syncwarp();
+  const int total = warp_prefix(nitems, wq.base);
+  const int base = wq.base[lane];
   int active = 0;
   for (int j0 = 0; j0 < total; j0 += 32) {
     const int j = j0 + lane;
     if (j < total) {
-      int lo = 0, hi = 31;   // owner: the last lane whose list starts at or before j
-      while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (wq.base[mid] <= j) lo = mid; else hi = mid - 1;
-      }
+      const int lo = owner_of(wq.base, j);   // the lane whose list holds item j
       const unsigned it = wq.items[lo][j - wq.base[lo]];
       const NbrRec &me = nbr[wbase + lo];   // owner lanes hold clumps, so wbase + lo < n
       // the owner's flume may differ from this lane's at a flume boundary of an ensemble
@@ -621,7 +713,7 @@ __device__ __forceinline__ int warp_contacts(WarpQueue &wq, long wbase, long s, 
       }
       V3 fs, tq;
       int r = kind == 1 ? 1 : 0;
-      if (kind && apply_law(ci, rl, co.dt, fs, tq)) r = kind == 1 ? 2 : 3;
+      if (kind && apply_law(ci, rl, co, fs, tq)) r = kind == 1 ? 2 : 3;
       wq.flag[lane] = r;
       if (r >= 2) {
         wq.res[lane][0] = fs.x; wq.res[lane][1] = fs.y; wq.res[lane][2] = fs.z;
@@ -1025,6 +1117,12 @@ __global__ void k_cells_by_id(const int *__restrict__ key, const long long *__re
 
 // ------------------------------------------------------------------ launchers
 
+// Built twice: the exact launchers in namespace af3d, and (with -DAF3D_FAST) the fast-mode
+// build of the same kernels, whose predictor and force launchers the context uses in fast mode.
+#ifdef AF3D_FAST
+namespace fast {
+#endif
+
 void launch_predict(const Launch &L, Planes cur, DevScalars *d, bool predict, bool keys, bool t_prev,
                     Cells cells, const long long *id, const int *flume) {
   if (L.n <= 0) return;
@@ -1128,5 +1226,9 @@ void launch_cells_by_id(const Launch &L, const int *key, const long long *id, De
   if (L.n <= 0) return;
   k_cells_by_id<<<grid_for(L.n), kBlock, 0, L.st>>>(key, id, d, cell_of_id, L.n);
 }
+
+#ifdef AF3D_FAST
+}  // namespace fast
+#endif
 
 }  // namespace af3d

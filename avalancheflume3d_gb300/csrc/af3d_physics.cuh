@@ -1,15 +1,27 @@
 // af3d_physics.cuh -- per-clump FP64 physics of the reference step, as device functions.
 //
-// Every expression keeps the reference's FP64 evaluation order, and the translation units that
-// include this header are compiled with -fmad=false, so a force, torque or acceleration computed
-// here is bit-identical to the reference host routine on the same input (+, -, *, / and sqrt are
-// correctly rounded on both sides).  Only init_Verlet's sin/cos come from CUDA's libm, which may
-// differ from the host libm in the last bit.
+// Exact mode (the default build): every expression keeps the reference's FP64 evaluation order,
+// and the translation units that include this header are compiled with -fmad=false, so a force,
+// torque or acceleration computed here is bit-identical to the reference host routine on the
+// same input (+, -, *, / and sqrt are correctly rounded on both sides).  Only init_Verlet's
+// sin/cos come from CUDA's libm, which may differ from the host libm in the last bit.
+//
+// Fast mode (built with -DAF3D_FAST -fmad=true): the same FP64 physics with multiply-adds
+// contracted, normals and tangents from a reciprocal square root instead of sqrt and three
+// divisions, and quotients by a shared divisor taken as products with one reciprocal.  Each of
+// these changes a result by a few units in the last place, so forces agree with the reference
+// to ~1e-14 relative rather than bit for bit.
 #pragma once
 
 #include "af3d_internal.h"
 
 namespace af3d {
+
+#ifdef AF3D_FAST
+constexpr bool kFast = true;
+#else
+constexpr bool kFast = false;
+#endif
 
 // cabecera.hu:5-19
 constexpr double kPI = 3.1415926535897932;
@@ -42,6 +54,7 @@ struct Consts {
   double mu_pw, kappa_pw, gamma_pw, cns_pw;
   double sint, cost, dy2, side_x, side_y;
   double sinfi, cosfi, tanfi;
+  double inv_dt;   // fast mode only: 1/dt
   int phase, variant;
 };
 
@@ -55,6 +68,7 @@ __device__ __forceinline__ Consts load_consts(const DevScalars *d, int f) {
   c.sint = s.sint; c.cost = s.cost; c.dy2 = s.dy2; c.side_x = s.side.x; c.side_y = s.side.y;
   c.sinfi = fl.fun.sinfi; c.cosfi = fl.fun.cosfi; c.tanfi = fl.fun.tanfi;
   c.phase = d->phase; c.variant = d->variant;
+  c.inv_dt = kFast ? 1.0 / s.dt : 0.0;
   return c;
 }
 
@@ -67,6 +81,40 @@ __device__ __forceinline__ bool is_removed(double time, double x, double side_x)
 // tail of every contact type (force_part.cu:189-241, force_walls.cu:123-177, ...).
 //   xi0:  Coulomb branch also when xi was zeroed (walls; DEV particle variant)
 //   gate: false -> proceed when normal > 0; true -> proceed unless normal <= 0 (fcorners)
+__device__ __forceinline__ bool contact_law_fast(V3 dvvc, V3 n, double comp, double km, double gm,
+                                                 double mass_t, double mu, double cns_1, double dt,
+                                                 double inv_dt, bool xi0, bool gate, V3 &f) {
+  const double vn = dvvc.x * n.x + dvvc.y * n.y + dvvc.z * n.z;
+  const V3 vt = mk(dvvc.x - vn * n.x, dvvc.y - vn * n.y, dvvc.z - vn * n.z);
+  const double vt2 = vt.x * vt.x + vt.y * vt.y + vt.z * vt.z;
+  const double inv_vt = rsqrt(vt2);          // +inf for vt = 0: the tangential part is then NaN
+  const double vt_mag = vt2 * inv_vt;        // and skipped, as in the exact law
+  const double vt_sig = (dvvc.x * vt.x + dvvc.y * vt.y + dvvc.z * vt.z) * inv_vt;
+  const double normal = km * comp + gm * (-vn);
+  if (gate ? (normal <= 0.0) : !(normal > 0.0)) return false;
+  f = mk(-normal * n.x, -normal * n.y, -normal * n.z);
+  double xi = dt * vt_sig;
+  if (cns_1 * normal < fabs(xi)) xi = 0.0;
+  const double fsdt = 1.0e12 * mass_t * xi + 2.0e6 * mass_t * (xi * inv_dt);
+  if (vt_mag > 0.0) {
+    if (fabs(fsdt) > mu * normal || (xi0 && xi == 0.0)) {
+      // af = 0.8 mu N / |vt|, t0 = m / af, af / (1 + (dt / t0)^2) = af m^2 / (m^2 + (dt af)^2)
+      const double af = 0.8 * mu * normal * inv_vt;
+      const double dta = dt * af;
+      const double a = af * (mass_t * mass_t) / (mass_t * mass_t + dta * dta);
+      f.x += a * vt.x;
+      f.y += a * vt.y;
+      f.z += a * vt.z;
+    } else {
+      const double q = fsdt * inv_vt;
+      if (vt.x != 0.0) f.x += q * vt.x;
+      if (vt.y != 0.0) f.y += q * vt.y;
+      if (vt.z != 0.0) f.z += q * vt.z;
+    }
+  }
+  return true;
+}
+
 __device__ __forceinline__ bool contact_law(V3 dvvc, V3 n, double comp, double km, double gm,
                                             double mass_t, double mu, double cns_1, double dt,
                                             bool xi0, bool gate, V3 &f) {
@@ -183,9 +231,12 @@ __device__ __forceinline__ void wall_input(const Sph &o, V3 rrc, V3 n, double co
 }
 
 // The contact law on a prepared contact: force fs and its torque term about the clump centre r.
-__device__ __forceinline__ bool apply_law(const ContactIn &ci, V3 r, double dt, V3 &fs, V3 &tq) {
-  if (!contact_law(ci.dvvc, ci.n, ci.comp, ci.km, ci.gm, ci.mass_t, ci.mu, ci.cns, dt, ci.xi0, ci.gate, fs))
-    return false;
+__device__ __forceinline__ bool apply_law(const ContactIn &ci, V3 r, const Consts &c, V3 &fs, V3 &tq) {
+  const bool on = kFast ? contact_law_fast(ci.dvvc, ci.n, ci.comp, ci.km, ci.gm, ci.mass_t, ci.mu, ci.cns, c.dt,
+                                           c.inv_dt, ci.xi0, ci.gate, fs)
+                        : contact_law(ci.dvvc, ci.n, ci.comp, ci.km, ci.gm, ci.mass_t, ci.mu, ci.cns, c.dt,
+                                      ci.xi0, ci.gate, fs);
+  if (!on) return false;
   tq = torque_term(ci.rrc, r, fs);
   return true;
 }
@@ -277,8 +328,16 @@ __device__ __forceinline__ bool fcorners_sphere(const Sph &o, const Consts &c, C
   d.y = yc - q.y;
   dist2 += d.y * d.y;
   if (dist2 > sep2) return false;
-  double dist = sqrt(dist2);
-  V3 nr = mk(d.x / dist, d.y / dist, 0.0);
+  double dist;
+  V3 nr;
+  if (kFast) {
+    const double inv = rsqrt(dist2);
+    dist = dist2 * inv;
+    nr = mk(d.x * inv, d.y * inv, 0.0);
+  } else {
+    dist = sqrt(dist2);
+    nr = mk(d.x / dist, d.y / dist, 0.0);
+  }
   V3 qc = mk(q.x + ri * nr.x, q.y + ri * nr.y, q.z);
   wall_input(o, to_lab(qc, c.cost, c.sint), to_lab(nr, c.cost, c.sint), ri - dist, c, true, ci);
   return true;
@@ -333,7 +392,7 @@ __device__ __forceinline__ bool bnd_input(int routine, const Sph &o, const Const
 // The force of routine `routine` on one sphere and its torque term (false: no force).
 __device__ __forceinline__ bool bnd_sphere(int routine, const Sph &o, const Consts &c, V3 &fs, V3 &tq) {
   ContactIn ci;
-  return bnd_input(routine, o, c, ci) && apply_law(ci, o.r, c.dt, fs, tq);
+  return bnd_input(routine, o, c, ci) && apply_law(ci, o.r, c, fs, tq);
 }
 
 // One boundary routine over the four spheres of a clump, with the reference's removed-clump
@@ -408,8 +467,15 @@ __device__ __forceinline__ bool pair_input(const V3 &rrl, const V3 &vvl, const V
   const double meff = 0.5 * (m.msph + massl);
   ci.km = 0.5 * c.kappa_pp * meff;
   ci.gm = 0.5 * c.gamma_pp * meff;
-  const double dist = sqrt(dist2);
-  ci.n = mk(d.x / dist, d.y / dist, d.z / dist);
+  double dist;
+  if (kFast) {
+    const double inv = rsqrt(dist2);
+    dist = dist2 * inv;
+    ci.n = mk(d.x * inv, d.y * inv, d.z * inv);
+  } else {
+    dist = sqrt(dist2);
+    ci.n = mk(d.x / dist, d.y / dist, d.z / dist);
+  }
   ci.rrc = mk(s1.x + rad_1 * ci.n.x, s1.y + rad_1 * ci.n.y, s1.z + rad_1 * ci.n.z);
   V3 vl = point_velocity(vvl, wwl, ci.rrc, rrl);
   V3 vm = point_velocity(mk(m.vx, m.vy, m.vz), mk(m.wx, m.wy, m.wz), ci.rrc, mk(m.rx, m.ry, m.rz));
@@ -431,7 +497,7 @@ __device__ __forceinline__ int part_pair_contrib(const V3 &rrl, const V3 &vvl, c
                                                  V3 &fs, V3 &tq) {
   ContactIn ci;
   if (!pair_input(rrl, vvl, wwl, s1, rad_1, massl, m, sm, c, xi0, ci)) return 0;
-  return apply_law(ci, rrl, c.dt, fs, tq) ? 2 : 1;
+  return apply_law(ci, rrl, c, fs, tq) ? 2 : 1;
 }
 
 // The same contact accumulated into (F, T) in place.
@@ -464,9 +530,16 @@ __device__ __forceinline__ void get_accel_one(V3 f, V3 t, V3 v, V3 w, V3 Rx, V3 
                                               double adrag0, V3 I, V3 &a, V3 &al) {
   double vmag = sqrt(v.x * v.x + v.y * v.y + v.z * v.z);
   double adrag = adrag0 * vmag;
-  a.x = f.x / m - adrag * v.x;
-  a.y = f.y / m - adrag * v.y;
-  a.z = f.z / m - adrag * v.z - kGRAV;
+  if (kFast) {
+    const double im = 1.0 / m;
+    a.x = f.x * im - adrag * v.x;
+    a.y = f.y * im - adrag * v.y;
+    a.z = f.z * im - adrag * v.z - kGRAV;
+  } else {
+    a.x = f.x / m - adrag * v.x;
+    a.y = f.y / m - adrag * v.y;
+    a.z = f.z / m - adrag * v.z - kGRAV;
+  }
   V3 wb, tb, ab;
   wb.x = w.x * Rx.x + w.y * Ry.x + w.z * Rz.x;
   wb.y = w.x * Rx.y + w.y * Ry.y + w.z * Rz.y;
@@ -476,9 +549,16 @@ __device__ __forceinline__ void get_accel_one(V3 f, V3 t, V3 v, V3 w, V3 Rx, V3 
   tb.z = t.x * Rx.z + t.y * Ry.z + t.z * Rz.z;
   if (I.x == I.y && I.y == I.z && isfinite(wb.x) && isfinite(wb.y) && isfinite(wb.z) && I.x > 0.0 &&
       isfinite(I.x)) {
-    ab.x = tb.x / I.x + signed_zero_product(wb.y, wb.z);
-    ab.y = tb.y / I.y + signed_zero_product(wb.z, wb.x);
-    ab.z = tb.z / I.z + signed_zero_product(wb.x, wb.y);
+    if (kFast) {
+      const double iI = 1.0 / I.x;
+      ab.x = tb.x * iI + signed_zero_product(wb.y, wb.z);
+      ab.y = tb.y * iI + signed_zero_product(wb.z, wb.x);
+      ab.z = tb.z * iI + signed_zero_product(wb.x, wb.y);
+    } else {
+      ab.x = tb.x / I.x + signed_zero_product(wb.y, wb.z);
+      ab.y = tb.y / I.y + signed_zero_product(wb.z, wb.x);
+      ab.z = tb.z / I.z + signed_zero_product(wb.x, wb.y);
+    }
   } else {
     double Cxy = (I.x - I.y) / I.z;
     double Cyz = (I.y - I.z) / I.x;

@@ -21,7 +21,7 @@ import ctypes as C
 
 import numpy as np
 
-from ._lib import (CELL_PAR, FRICTION_HST, FUNNEL, INPUTS, PARTICLE, PHASE_AVALANCHE, RNG,
+from ._lib import (CELL_PAR, FP_EXACT, FRICTION_HST, FUNNEL, INPUTS, PARTICLE, PHASE_AVALANCHE, RNG,
                    SYSTEM_PAR, EngineError, Vec3, check, lib, ptr)
 
 
@@ -37,7 +37,7 @@ class Engine:
     shared dt and clock; see ``af3d_create_ensemble``)."""
 
     def __init__(self, sys: np.ndarray, fun: np.ndarray, ntags: int = 9, phase: int = PHASE_AVALANCHE,
-                 friction: int = FRICTION_HST, stream: int | None = None):
+                 friction: int = FRICTION_HST, stream: int | None = None, fp_mode: int = FP_EXACT):
         L = lib()
         self._L = L
         sys_a = np.array(sys, dtype=SYSTEM_PAR)
@@ -61,6 +61,8 @@ class Engine:
             self.set_friction(friction)
         if stream:
             check(L.af3d_set_stream(h, C.c_void_p(stream)), "af3d_set_stream")
+        if fp_mode != FP_EXACT:
+            self.set_fp_mode(fp_mode)
 
     # ---- lifetime ----
     def close(self) -> None:
@@ -149,6 +151,10 @@ class Engine:
 
     def flume_count(self) -> int:
         return int(self._L.af3d_flume_count(self._h))
+
+    def set_fp_mode(self, mode: int) -> None:
+        """FP_EXACT (bit-identical to the reference) or FP_FAST (contracted FP64) for step/forces."""
+        self._call("af3d_set_fp_mode", int(mode))
 
     def set_friction(self, variant: int) -> None:
         self._call("af3d_set_friction", int(variant))

@@ -61,6 +61,8 @@ def parse_args():
     p.add_argument("--cpu-sample", type=int, default=16384, help="clumps in the CPU baseline sample")
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--fp-mode", choices=["exact", "fast"], default="fast",
+                   help="FP64 mode of the timed steps (the other mode is timed beside it)")
     p.add_argument("--ensemble-flumes", type=int, default=256,
                    help="flumes of the batched-ensemble measurement (0 skips it)")
     p.add_argument("--ensemble-steps", type=int, default=64)
@@ -240,7 +242,9 @@ def measure_ensemble(args, stream):
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / 1e3
 
-    eng = Engine(sys_, fun, stream=stream.cuda_stream)
+    from avalancheflume3d_gb300 import FP_EXACT, FP_FAST
+    mode = FP_FAST if args.fp_mode == "fast" else FP_EXACT
+    eng = Engine(sys_, fun, stream=stream.cuda_stream, fp_mode=mode)
     eng.import_particles(pp)
     eng.forces()
     eng.swap_accel()
@@ -258,7 +262,7 @@ def measure_ensemble(args, stream):
     seq_units, seq_t = 0, 0.0
     for f in range(0, len(cfgs), stride):
         pp_f = pp[first[f]:first[f + 1]]
-        with Engine(sys_[f], fun[f], stream=stream.cuda_stream) as one:
+        with Engine(sys_[f], fun[f], stream=stream.cuda_stream, fp_mode=mode) as one:
             one.import_particles(pp_f)
             one.forces()
             one.swap_accel()
@@ -292,7 +296,9 @@ def run_engine(args):
 
     cfg, (sys_, fun, pp) = workload(args)
     stream = torch.cuda.current_stream()
-    eng = Engine(sys_, fun, stream=stream.cuda_stream)
+    from avalancheflume3d_gb300 import FP_EXACT, FP_FAST
+    modes = {"exact": FP_EXACT, "fast": FP_FAST}
+    eng = Engine(sys_, fun, stream=stream.cuda_stream, fp_mode=modes[args.fp_mode])
     eng.import_particles(pp)
     eng.forces()          # start-up force pass into a_i (avalanche_hst.cu:366-384)
     eng.swap_accel()
@@ -339,6 +345,21 @@ def run_engine(args):
     ms = replicas.max_over_ranks(R, ms, dev)
     ms_step = ms / args.steps
     value = world * args.n * args.steps / (ms / 1e3)
+
+    # The other FP64 mode on the same state, same step count (outside the timed region).
+    other = "exact" if args.fp_mode == "fast" else "fast"
+    eng.set_fp_mode(modes[other])
+    eng.step(2)
+    torch.cuda.synchronize()
+    o0, o1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    o0.record(stream)
+    eng.step(args.steps)
+    o1.record(stream)
+    torch.cuda.synchronize()
+    ms_other = replicas.max_over_ranks(R, o0.elapsed_time(o1), dev)
+    eng.set_fp_mode(modes[args.fp_mode])
+    other_line = {"fp_mode": other, "value": world * args.n * args.steps / (ms_other / 1e3),
+                  "ms_per_step": ms_other / args.steps, "steps": args.steps}
 
     # Roofline of the dominant kernel from CUDA events between the kernels (profiled steps after
     # the timed region, same stream).
@@ -404,7 +425,8 @@ def run_engine(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic",
             "config": config_dict(args, cfg, {"parallelism": "replicas" if world > 1 else "single",
-                                              "cells": ncell3}),
+                                              "cells": ncell3, "fp_mode": args.fp_mode}),
+            "other_fp_mode": other_line,
             "contacts_per_s": world * contacts / (ms / 1e3),
             "contacts_per_step": contacts / args.steps,
             "e2e": e2e,

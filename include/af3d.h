@@ -85,6 +85,14 @@ enum {
    `|| xi == 0` clause of the Coulomb test (force_part.cu:224), the device one has it (:487). */
 enum { AF3D_FRICTION_HST = 0, AF3D_FRICTION_DEV = 1 };
 
+/* FP64 arithmetic of af3d_step and af3d_forces (the per-routine entry points are always exact).
+   EXACT: the reference's operations in its order, no contraction: forces, torques and
+   accelerations bit-identical to the reference host routines on the same input.  FAST: the same
+   FP64 physics with contracted multiply-adds and reciprocal-square-root normalisation (no
+   reference counterpart): forces within ~1e-14 relative of the reference, trajectories within
+   1e-8 relative over 100 steps. */
+enum { AF3D_FP_EXACT = 0, AF3D_FP_FAST = 1 };
+
 /* Phase of the reference loop: hopper filling (avalanche_hst.cu:401-601) or avalanche (:618-856). */
 enum { AF3D_PHASE_FILL = 0, AF3D_PHASE_AVALANCHE = 1 };
 
@@ -100,6 +108,7 @@ af3d_status af3d_create (const af3d_system_par *sys, const af3d_funnel *fun, lon
 af3d_status af3d_destroy (af3d_ctx *ctx);
 af3d_status af3d_set_stream (af3d_ctx *ctx, void *cuda_stream);      /* cudaStream_t, 0 = own */
 af3d_status af3d_set_friction (af3d_ctx *ctx, int variant);          /* AF3D_FRICTION_*       */
+af3d_status af3d_set_fp_mode (af3d_ctx *ctx, int mode);              /* AF3D_FP_*, default EXACT */
 const char *af3d_last_error (void);
 int         af3d_abi_version (void);
 
