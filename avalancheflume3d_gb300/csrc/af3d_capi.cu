@@ -39,14 +39,27 @@ af3d_status fail(af3d_status code, const std::string &msg) {
 constexpr long kRegridEvery = 2000;   // avalanche_hst.cu:470 and :713 (cc % 2000 == 0)
 constexpr long kKernelsPerCellBuild = 7;   // predict/keys, 3 scan, scatter, rank, permute
 constexpr long kKernelsPerStep = kKernelsPerCellBuild + 2;   // + time advance, fused forces
+constexpr long kKernelsPerKeptStep = kKernelsPerStep - 1;    // a step without the permutation
 constexpr long kKernelsPerRegrid = 4;
+// The clumps are moved into (cell, id) order by a permutation of every plane at most this many
+// steps apart; the steps in between keep the slot order and reach the sorted order through the
+// sort's index array.  Results do not depend on it (every sum runs in (sph_id, cell, id) order);
+// it bounds how far the slot order may drift from the spatial order.
+constexpr long kResortEvery = 64;
 
 constexpr long kGraphSteps = 64;   // steps per long graph (a multiple of the pointer period 2)
 
-struct StepGraph {
+// Pointer state of the context that a captured sequence of steps depends on and changes.
+struct PtrState {
   Planes cur, alt;
-  long long *id_cur = nullptr;
+  long long *id_cur, *id_alt;
+  int *fl_cur, *fl_alt;
+};
+
+struct StepGraph {
+  PtrState start{}, end{};      // before and after the captured steps
   long steps = 0;
+  bool resort_first = false;    // the first captured step permutes the planes
   cudaGraphExec_t exec = nullptr;
 };
 
@@ -83,6 +96,8 @@ struct af3d_ctx {
   DevFlume *flumes = nullptr;
   bool records_valid = false;   // records reflect the current planes
   bool cells_valid = false;     // start[] describes the current layout
+  bool sorted = false;          // the slots are in the (cell, id) order of the last sort
+  long since_sort = kResortEvery;   // steps since the planes were last permuted
 
   af3d_particle *d_aos = nullptr;
   double *d_acc = nullptr, *d_anga = nullptr;
@@ -108,6 +123,21 @@ void swap_velocity_planes(Planes &a, Planes &b) {
 
 bool same_planes(const Planes &a, const Planes &b) {
   return std::memcmp(&a, &b, sizeof(Planes)) == 0;
+}
+
+PtrState ptr_state(const af3d_ctx *c) {
+  return PtrState{c->cur, c->alt, c->id_cur, c->id_alt, c->fl_cur, c->fl_alt};
+}
+
+void set_ptr_state(af3d_ctx *c, const PtrState &p) {
+  c->cur = p.cur; c->alt = p.alt;
+  c->id_cur = p.id_cur; c->id_alt = p.id_alt;
+  c->fl_cur = p.fl_cur; c->fl_alt = p.fl_alt;
+}
+
+bool same_state(const PtrState &a, const PtrState &b) {
+  return same_planes(a.cur, b.cur) && same_planes(a.alt, b.alt) && a.id_cur == b.id_cur &&
+         a.id_alt == b.id_alt && a.fl_cur == b.fl_cur && a.fl_alt == b.fl_alt;
 }
 
 void drop_graphs(af3d_ctx *c) {
@@ -214,18 +244,25 @@ af3d_status regrid(af3d_ctx *c) {
 // clear_cell + clear_ocup + cell_locate: keys (optionally fused with the predictor), counting
 // sort, permutation of every plane into the new order, neighbour records.
 // The predictor and force launchers of the context's FP64 mode (the other kernels have one form).
-void predict_for(af3d_ctx *c, bool predict, bool keys, bool t_prev) {
+void predict_for(af3d_ctx *c, bool predict, bool keys, bool t_prev, bool records = false) {
+  NbrRec *nbr = records ? c->nbr : nullptr;
+  CullRec *cull = records ? c->cull : nullptr;
   if (c->fp_mode == AF3D_FP_FAST)
-    fast::launch_predict(c->L(), c->cur, c->d, predict, keys, t_prev, c->cells, c->id_cur, c->fl_cur);
+    fast::launch_predict(c->L(), c->cur, c->d, predict, keys, t_prev, c->cells, c->id_cur, c->fl_cur, nbr, cull);
   else
-    launch_predict(c->L(), c->cur, c->d, predict, keys, t_prev, c->cells, c->id_cur, c->fl_cur);
+    launch_predict(c->L(), c->cur, c->d, predict, keys, t_prev, c->cells, c->id_cur, c->fl_cur, nbr, cull);
 }
 
-void forces_for(af3d_ctx *c, bool write_ft) {
+// order: null when the slots were just permuted into (cell, id) order; out: where the corrected
+// velocities go.
+void forces_for(af3d_ctx *c, bool write_ft, const int *order, Planes out) {
+  const float4 *csort = order ? c->cells.csort : nullptr;
   if (c->fp_mode == AF3D_FP_FAST)
-    fast::launch_fused_forces(c->L(), c->cur, c->alt, c->d, c->fl_cur, c->nbr, c->cull, c->cells.start, write_ft);
+    fast::launch_fused_forces(c->L(), c->cur, out, c->d, c->fl_cur, c->nbr, c->cull, c->cells.start, order,
+                              csort, write_ft);
   else
-    launch_fused_forces(c->L(), c->cur, c->alt, c->d, c->fl_cur, c->nbr, c->cull, c->cells.start, write_ft);
+    launch_fused_forces(c->L(), c->cur, out, c->d, c->fl_cur, c->nbr, c->cull, c->cells.start, order, csort,
+                        write_ft);
 }
 
 void enqueue_cell_build(af3d_ctx *c, bool predict, bool t_prev, bool ft = true) {
@@ -236,43 +273,61 @@ void enqueue_cell_build(af3d_ctx *c, bool predict, bool t_prev, bool ft = true) 
   std::swap(c->cur, c->alt);
   std::swap(c->id_cur, c->id_alt);
   std::swap(c->fl_cur, c->fl_alt);
+  c->sorted = true;
+  c->since_sort = 0;
 }
 
 // One fused step: time += dt, init_Verlet + cell build, every force of the phase, get_accel,
-// finish_Verlet, and the acceleration swap.
-void enqueue_fused_step(af3d_ctx *c) {
+// finish_Verlet, and the acceleration swap.  With `resort` the planes are permuted into the new
+// (cell, id) order; otherwise the predictor writes the records at the clumps' own slots, the
+// force pass reaches the sorted order through cells.perm and corrects the velocities in place.
+void enqueue_fused_step(af3d_ctx *c, bool resort) {
   launch_advance_time(c->st, c->d);
-  enqueue_cell_build(c, true, true, false);   // F, T and a_f are rewritten before being read
-  forces_for(c, false);
-  swap_velocity_planes(c->cur, c->alt);
+  if (resort) {
+    enqueue_cell_build(c, true, true, false);   // F, T and a_f are rewritten before being read
+    forces_for(c, false, nullptr, c->alt);
+    swap_velocity_planes(c->cur, c->alt);
+  } else {
+    predict_for(c, true, true, true, true);
+    launch_sort(c->L(), c->d, c->cells, c->id_cur, c->ntags, c->cull);
+    forces_for(c, false, c->cells.perm, c->cur);
+  }
   swap_accel_planes(c->cur);
   swap_accel_planes(c->alt);
+  c->sorted = resort;
+}
+
+long kernels_of(long len, bool resort_first) {
+  return len * kKernelsPerKeptStep + (resort_first ? 1 : 0);
 }
 
 af3d_status run_steps(af3d_ctx *c, long m) {
-  // Every pair of steps returns the plane pointers to where they started, so captured graphs of
-  // an even number of steps can be replayed: 64-step graphs while at least 64 steps remain,
-  // then two-step graphs; an odd last step is enqueued directly.
+  // Captured graphs of 64 steps (the first one permuting the planes) while at least 64 steps
+  // remain, then of two steps (permuting first only when the last permutation is due); an odd
+  // last step is enqueued directly.  A graph is replayed when the context is in the pointer
+  // state it was captured from, and leaves the context in the state it ended in.
   while (m >= 2) {
     const long len = m >= kGraphSteps ? kGraphSteps : 2;
+    const bool resort_first = len == kGraphSteps || c->since_sort + len > kResortEvery;
+    const PtrState now = ptr_state(c);
     StepGraph *g = nullptr;
     for (auto &cand : c->graphs)
-      if (cand.exec && cand.steps == len && cand.id_cur == c->id_cur && same_planes(cand.cur, c->cur) &&
-          same_planes(cand.alt, c->alt))
+      if (cand.exec && cand.steps == len && cand.resort_first == resort_first && same_state(cand.start, now))
         g = &cand;
     if (!g) {
       g = &c->graphs[c->graph_next];
       c->graph_next = (c->graph_next + 1) % 4;
       if (g->exec) cudaGraphExecDestroy(g->exec);
       *g = StepGraph{};
-      g->cur = c->cur;
-      g->alt = c->alt;
-      g->id_cur = c->id_cur;
+      g->start = now;
       g->steps = len;
+      g->resort_first = resort_first;
       cudaGraph_t graph;
       AF3D_CUDA(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
-      for (long i = 0; i < len; i++) enqueue_fused_step(c);
+      for (long i = 0; i < len; i++) enqueue_fused_step(c, i == 0 && resort_first);
       AF3D_CUDA(cudaStreamEndCapture(c->st, &graph));
+      g->end = ptr_state(c);
+      set_ptr_state(c, now);
       cudaError_t e = cudaGraphInstantiate(&g->exec, graph, 0);
       cudaGraphDestroy(graph);
       if (e != cudaSuccess) {
@@ -281,12 +336,17 @@ af3d_status run_steps(af3d_ctx *c, long m) {
       }
     }
     AF3D_CUDA(cudaGraphLaunch(g->exec, c->st));
-    c->launches += len * kKernelsPerStep;
+    set_ptr_state(c, g->end);
+    c->sorted = false;   // the last captured step keeps the slot order
+    c->since_sort = resort_first ? len - 1 : c->since_sort + len;
+    c->launches += kernels_of(len, resort_first);
     m -= len;
   }
   if (m == 1) {
-    enqueue_fused_step(c);
-    c->launches += kKernelsPerStep;
+    const bool resort = c->since_sort + 1 > kResortEvery;
+    enqueue_fused_step(c, resort);
+    c->since_sort = resort ? 0 : c->since_sort + 1;
+    c->launches += kernels_of(1, resort);
   }
   return AF3D_OK;
 }
@@ -310,6 +370,7 @@ af3d_status first_error(int flags) {
 af3d_status ensure_records(af3d_ctx *c) {
   if (!c->imported) return fail(AF3D_ERR_ARG, "no particles imported");
   if (!c->cells_valid) return fail(AF3D_ERR_ARG, "no cell build since the last grid change");
+  if (!c->sorted) return fail(AF3D_ERR_ARG, "af3d_step left the slots out of cell order: call af3d_cell_build");
   if (!c->records_valid) {
     launch_build_records(c->L(), c->cur, c->nbr, c->cull);
     c->records_valid = true;
@@ -404,6 +465,7 @@ af3d_status af3d_create_ensemble(int nflumes, const af3d_system_par *sys, const 
   ok = ok && cudaMalloc((void **)&c->cells.rank_tmp, sizeof(int) * n) == cudaSuccess;
   ok = ok && cudaMalloc((void **)&c->cells.tmp_slot, sizeof(int) * n) == cudaSuccess;
   ok = ok && cudaMalloc((void **)&c->cells.perm, sizeof(int) * n) == cudaSuccess;
+  ok = ok && cudaMalloc((void **)&c->cells.csort, sizeof(float4) * n) == cudaSuccess;
   ok = ok && cudaMalloc((void **)&c->d, sizeof(DevScalars)) == cudaSuccess;
   ok = ok && cudaMalloc((void **)&c->flumes, sizeof(DevFlume) * nflumes) == cudaSuccess;
   ok = ok && cudaMalloc((void **)&c->d_count, sizeof(unsigned long long)) == cudaSuccess;
@@ -460,7 +522,7 @@ af3d_status af3d_destroy(af3d_ctx *c) {
   for (void *p : {(void *)c->plane_mem[0], (void *)c->plane_mem[1], (void *)c->id_cur, (void *)c->id_alt,
                   (void *)c->fl_cur, (void *)c->fl_alt, (void *)c->flume_of_id, (void *)c->nbr,
                   (void *)c->cull, (void *)c->cells.key, (void *)c->cells.rank_tmp, (void *)c->cells.tmp_slot,
-                  (void *)c->cells.perm, (void *)c->cells.count, (void *)c->cells.start,
+                  (void *)c->cells.perm, (void *)c->cells.csort, (void *)c->cells.count, (void *)c->cells.start,
                   (void *)c->cells.block_sums, (void *)c->d, (void *)c->flumes, (void *)c->d_aos,
                   (void *)c->d_acc, (void *)c->d_anga, (void *)c->d_tmp, (void *)c->d_count})
     if (p) cudaFree(p);
@@ -521,6 +583,8 @@ af3d_status af3d_import_particles(af3d_ctx *c, const af3d_particle *pp, const af
   c->imported = true;
   c->records_valid = false;
   c->cells_valid = false;
+  c->sorted = false;
+  c->since_sort = kResortEvery;
   drop_graphs(c);
   if (!c->have_grid && c->n > 0) return regrid(c);
   return AF3D_OK;
@@ -732,7 +796,7 @@ af3d_status af3d_forces(af3d_ctx *c) {
   enqueue_cell_build(c, false, false);
   c->cells_valid = true;
   // Corrected velocities go to the dead plane set and are dropped: this pass stops at get_accel.
-  forces_for(c, true);
+  forces_for(c, true, nullptr, c->alt);
   c->launches += kKernelsPerCellBuild + 1;
   c->records_valid = true;
   int flags = 0;
@@ -775,25 +839,35 @@ af3d_status af3d_step_profile(af3d_ctx *c, long k, double *ms) {
   cudaEvent_t ev[AF3D_NPROF + 1];
   for (auto &e : ev) AF3D_CUDA(cudaEventCreate(&e));
   for (long i = 0; i < k; i++) {
+    // The steps af3d_step runs, one at a time (the planes are permuted when that is due).
+    const bool resort = c->since_sort + 1 > kResortEvery;
     AF3D_CUDA(cudaEventRecord(ev[0], c->st));
     launch_advance_time(c->st, c->d);
     AF3D_CUDA(cudaEventRecord(ev[1], c->st));
-    predict_for(c, true, true, true);
+    predict_for(c, true, true, true, !resort);
     AF3D_CUDA(cudaEventRecord(ev[2], c->st));
-    launch_sort(c->L(), c->d, c->cells, c->id_cur, c->ntags);
+    launch_sort(c->L(), c->d, c->cells, c->id_cur, c->ntags, resort ? nullptr : c->cull);
     AF3D_CUDA(cudaEventRecord(ev[3], c->st));
-    launch_permute_records(c->L(), c->cur, c->alt, c->cells.perm, c->id_cur, c->id_alt, c->fl_cur, c->fl_alt,
-                           c->nbr, c->cull, false);
-    std::swap(c->cur, c->alt);
-    std::swap(c->id_cur, c->id_alt);
-    std::swap(c->fl_cur, c->fl_alt);
+    if (resort) {
+      launch_permute_records(c->L(), c->cur, c->alt, c->cells.perm, c->id_cur, c->id_alt, c->fl_cur,
+                             c->fl_alt, c->nbr, c->cull, false);
+      std::swap(c->cur, c->alt);
+      std::swap(c->id_cur, c->id_alt);
+      std::swap(c->fl_cur, c->fl_alt);
+    }
     AF3D_CUDA(cudaEventRecord(ev[4], c->st));
-    forces_for(c, false);
-    swap_velocity_planes(c->cur, c->alt);
+    if (resort) {
+      forces_for(c, false, nullptr, c->alt);
+      swap_velocity_planes(c->cur, c->alt);
+    } else {
+      forces_for(c, false, c->cells.perm, c->cur);
+    }
     swap_accel_planes(c->cur);
     swap_accel_planes(c->alt);
     AF3D_CUDA(cudaEventRecord(ev[5], c->st));
-    c->launches += kKernelsPerStep;
+    c->sorted = resort;
+    c->since_sort = resort ? 0 : c->since_sort + 1;
+    c->launches += kernels_of(1, resort);
     c->time = c->time + c->sys[0].dt;
     const bool do_regrid = c->cc % kRegridEvery == 0;
     c->cc++;
@@ -859,6 +933,7 @@ af3d_status af3d_get_accels(af3d_ctx *c, af3d_vec3 *acc_f, af3d_vec3 *anga_f) {
 af3d_status af3d_get_cells(af3d_ctx *c, long *cell_of_id, long *sorted_ids, long *nbinned) {
   CHECK_STATE(c);
   if (!c->cells_valid) return fail(AF3D_ERR_ARG, "no cell build since the last grid change");
+  if (!c->sorted) return fail(AF3D_ERR_ARG, "af3d_step left the slots out of cell order: call af3d_cell_build");
   if (c->n == 0) {
     if (nbinned) *nbinned = 0;
     return AF3D_OK;

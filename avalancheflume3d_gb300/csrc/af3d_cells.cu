@@ -64,17 +64,46 @@ __global__ void k_scan_partials(const int *__restrict__ count, int *block_sums, 
   if (threadIdx.x == 0) block_sums[blockIdx.x] = tot;
 }
 
-// One block scans the per-tile sums in place (exclusive), chunk by chunk.
-__global__ void k_scan_top(int *block_sums, long ntiles, int *start, const DevScalars *d, long n) {
+// One block of kTopThreads threads scans the per-tile sums in place (exclusive): each thread
+// takes kTopItems consecutive tiles, so one block-wide scan covers kTopThreads * kTopItems tiles.
+constexpr int kTopThreads = 1024;
+constexpr int kTopItems = 8;
+
+__global__ void __launch_bounds__(kTopThreads) k_scan_top(int *block_sums, long ntiles, int *start,
+                                                          const DevScalars *d, long n) {
+  __shared__ int warp_tot[kTopThreads / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const long nb = n_buckets(d, n);
-  __shared__ int tot;
   int carry = 0;
-  for (long b0 = 0; b0 < ntiles; b0 += kScanThreads) {
-    const long i = b0 + threadIdx.x;
-    int v = i < ntiles ? block_sums[i] : 0;
-    int e = block_excl_scan(v, &tot);
-    if (i < ntiles) block_sums[i] = e + carry;
-    carry += tot;
+  for (long b0 = 0; b0 < ntiles; b0 += (long)kTopThreads * kTopItems) {
+    const long i0 = b0 + (long)threadIdx.x * kTopItems;
+    int v[kTopItems];
+    int sum = 0;
+#pragma unroll
+    for (int i = 0; i < kTopItems; i++) {
+      v[i] = i0 + i < ntiles ? block_sums[i0 + i] : 0;
+      sum += v[i];
+    }
+    const int incl = warp_incl_scan(sum);
+    if (lane == 31) warp_tot[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+      const int t = warp_tot[lane];
+      const int ti = warp_incl_scan(t);
+      warp_tot[lane] = ti - t;
+    }
+    __syncthreads();
+    int e = carry + warp_tot[wid] + incl - sum;
+#pragma unroll
+    for (int i = 0; i < kTopItems; i++) {
+      if (i0 + i < ntiles) block_sums[i0 + i] = e;
+      e += v[i];
+    }
+    // the chunk total: the last thread's running value
+    __shared__ int chunk_total;
+    if (threadIdx.x == kTopThreads - 1) chunk_total = e - carry;
+    __syncthreads();
+    carry += chunk_total;
     __syncthreads();
   }
   if (threadIdx.x == 0) start[nb] = (int)n;   // every clump has exactly one bucket
@@ -111,7 +140,8 @@ __global__ void k_scatter(const int *__restrict__ key, const int *__restrict__ r
 // whatever the grid then is (the scan has consumed it already).
 __global__ void k_rank(const int *__restrict__ key, const int *__restrict__ start,
                        const int *__restrict__ tmp_slot, const long long *__restrict__ id, int *perm,
-                       int *count, DevScalars *d, long ntags, long n) {
+                       const CullRec *__restrict__ cull, float4 *csort, int *count, DevScalars *d,
+                       long ntags, long n) {
   const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (s >= n) return;
   const long ncell3 = d->ncell_total;
@@ -122,6 +152,7 @@ __global__ void k_rank(const int *__restrict__ key, const int *__restrict__ star
   int r = 0;
   for (int j = b; j < e; j++) r += id[tmp_slot[j]] < me;
   perm[b + r] = (int)s;
+  if (cull) csort[b + r] = cull[s].c;
   // cells.cu:96-102: a cell may hold at most ntags - 1 clumps
   if (ntags > 0 && k < ncell3 && r == 0 && (e - b) >= ntags)
     atomicOr(&d->status, 1 << AF3D_ERR_CELL_CAPACITY);
@@ -131,17 +162,17 @@ __global__ void k_rank(const int *__restrict__ key, const int *__restrict__ star
 
 long scan_tiles(long bucket_cap) { return (bucket_cap + kTile - 1) / kTile; }
 
-void launch_sort(const Launch &L, DevScalars *d, Cells c, const long long *id, long ntags) {
+void launch_sort(const Launch &L, DevScalars *d, Cells c, const long long *id, long ntags, const CullRec *cull) {
   // Launch sizes follow the capacity; the kernels read the bucket count in use from the device,
   // so a captured graph stays valid across device-side re-grids.
   const long ntiles = scan_tiles(c.cap);
   k_scan_partials<<<(unsigned)ntiles, kScanThreads, 0, L.st>>>(c.count, c.block_sums, d, L.n);
-  k_scan_top<<<1, kScanThreads, 0, L.st>>>(c.block_sums, ntiles, c.start, d, L.n);
+  k_scan_top<<<1, kTopThreads, 0, L.st>>>(c.block_sums, ntiles, c.start, d, L.n);
   k_scan_final<<<(unsigned)ntiles, kScanThreads, 0, L.st>>>(c.count, c.block_sums, c.start, d, L.n);
   if (L.n <= 0) return;
   const unsigned g = (unsigned)((L.n + 127) / 128);
   k_scatter<<<g, 128, 0, L.st>>>(c.key, c.rank_tmp, c.start, c.tmp_slot, L.n);
-  k_rank<<<g, 128, 0, L.st>>>(c.key, c.start, c.tmp_slot, id, c.perm, c.count, d, ntags, L.n);
+  k_rank<<<g, 128, 0, L.st>>>(c.key, c.start, c.tmp_slot, id, c.perm, cull, c.csort, c.count, d, ntags, L.n);
 }
 
 }  // namespace af3d

@@ -59,6 +59,7 @@ struct Cells {
   int *rank_tmp;    // [N]   atomic arrival rank inside the bucket (nondeterministic)
   int *tmp_slot;    // [N]   old slots scattered by arrival order
   int *perm;        // [N]   new slot -> old slot, deterministic (cell, id) order
+  float4 *csort;    // [N]   FP32 culling centre of the clump at each position of that order
   int *count;       // [cap] bucket sizes (all zero between builds)
   int *start;       // [cap+1] exclusive scan of count
   int *block_sums;  // [scan_tiles(cap)] scan scratch
@@ -103,12 +104,17 @@ struct Launch {
   long n;
 };
 
+// init_Verlet and/or the cell keys; with nbr/cull (predict and keys only) also the neighbour
+// records of every clump at its own slot.
 void launch_predict (const Launch &L, Planes cur, DevScalars *d, bool predict, bool keys, bool t_prev,
-                     Cells cells, const long long *id, const int *flume);
+                     Cells cells, const long long *id, const int *flume, NbrRec *nbr = nullptr,
+                     CullRec *cull = nullptr);
 // Exclusive scan of the bucket counts, scatter by arrival, then the deterministic (bucket, id)
 // rank: fills cells.start[0..nbuckets] and cells.perm, checks the ntags capacity and leaves the
 // count array zeroed.  nbuckets = ncell_total + N is read on the device.
-void launch_sort (const Launch &L, DevScalars *d, Cells cells, const long long *id, long ntags);
+// With cull (records already written at the old slots) also fills cells.csort.
+void launch_sort (const Launch &L, DevScalars *d, Cells cells, const long long *id, long ntags,
+                  const CullRec *cull = nullptr);
 long scan_tiles (long bucket_cap);
 // Moves every plane (and the id and flume arrays) into the new order and builds the records.
 // `ft`: also carry the force/torque accumulators and a_f (the fused step rewrites them first).
@@ -116,8 +122,11 @@ void launch_permute_records (const Launch &L, Planes src, Planes dst, const int 
                              const long long *id_src, long long *id_dst, const int *fl_src,
                              int *fl_dst, NbrRec *nbr, CullRec *cull, bool ft);
 void launch_build_records (const Launch &L, Planes cur, NbrRec *nbr, CullRec *cull);
+// order: null when the slots are in (cell, id) order, else cells.perm of the last sort, with
+// csort the matching culling centres.
 void launch_fused_forces (const Launch &L, Planes cur, Planes out, DevScalars *d, const int *flume,
-                          const NbrRec *nbr, const CullRec *cull, const int *start, bool write_ft);
+                          const NbrRec *nbr, const CullRec *cull, const int *start, const int *order,
+                          const float4 *csort, bool write_ft);
 void launch_boundary (const Launch &L, Planes cur, DevScalars *d, const int *flume, int routine);
 void launch_part (const Launch &L, Planes cur, DevScalars *d, const int *flume, const NbrRec *nbr,
                   const CullRec *cull, const int *start, int sph_id);
@@ -149,9 +158,11 @@ cudaError_t measure_dfma (int sms, double *tflops);
 // -DAF3D_FAST -fmad=true; same arguments as above).
 namespace fast {
 void launch_predict (const Launch &L, Planes cur, DevScalars *d, bool predict, bool keys, bool t_prev,
-                     Cells cells, const long long *id, const int *flume);
+                     Cells cells, const long long *id, const int *flume, NbrRec *nbr = nullptr,
+                     CullRec *cull = nullptr);
 void launch_fused_forces (const Launch &L, Planes cur, Planes out, DevScalars *d, const int *flume,
-                          const NbrRec *nbr, const CullRec *cull, const int *start, bool write_ft);
+                          const NbrRec *nbr, const CullRec *cull, const int *start, const int *order,
+                          const float4 *csort, bool write_ft);
 }  // namespace fast
 
 }  // namespace af3d

@@ -114,6 +114,73 @@ __global__ void k_planes_to_aos(Planes P, const long long *__restrict__ id, cons
   }
 }
 
+// ------------------------------------------------------------------ neighbour records
+
+__device__ __forceinline__ float f_up(double x) { return __double2float_ru(x); }
+
+// Packed FP64 neighbour record and conservative FP32 culling record of one clump.
+// The culling bounds are formed in FP32 from the FP32-rounded coordinates.  M32 = max |coordinate|
+// in FP32 is within 2^-24 of the FP64 maximum M, so mu = 2^-21 * M32 * (1 + 2^-20) still bounds
+// 4x the rounding of any FP32 coordinate (and of a coordinate difference); the sphere extent
+// ext32 = max_k |s_k - r| from the FP32 coordinates is within 2 mu + a few 2^-24 ext of the
+// exact one, which the factor (1 + 2^-20) and the added 2 mu cover.
+__device__ __forceinline__ void make_records(V3 r, V3 v, V3 w, const V3 *sp, double rad, double msph,
+                                             double mwall, NbrRec &q, CullRec &c) {
+  q.rx = r.x; q.ry = r.y; q.rz = r.z;
+  q.vx = v.x; q.vy = v.y; q.vz = v.z;
+  q.wx = w.x; q.wy = w.y; q.wz = w.z;
+  for (int k = 0; k < 4; k++) {
+    q.s[3 * k] = sp[k].x; q.s[3 * k + 1] = sp[k].y; q.s[3 * k + 2] = sp[k].z;
+  }
+  q.rad = rad; q.msph = msph; q.mwall = mwall;
+  const float cx = (float)r.x, cy = (float)r.y, cz = (float)r.z;
+  float M = fmaxf(fmaxf(fabsf(cx), fabsf(cy)), fabsf(cz));
+  float ext = 0.0f;
+  float4 sf[4];
+  for (int k = 0; k < 4; k++) {
+    sf[k] = make_float4((float)sp[k].x, (float)sp[k].y, (float)sp[k].z, 0.0f);
+    M = fmaxf(M, fmaxf(fmaxf(fabsf(sf[k].x), fabsf(sf[k].y)), fabsf(sf[k].z)));
+    const float dx = sf[k].x - cx, dy = sf[k].y - cy, dz = sf[k].z - cz;
+    ext = fmaxf(ext, sqrtf(__fmaf_rn(dz, dz, __fmaf_rn(dy, dy, dx * dx))));
+  }
+  const float radf = f_up(rad);
+  // 2^-21 * max|coordinate| bounds 4x the FP32 rounding of a coordinate difference.
+  const float mu = fmaxf(M, radf) * 4.76837158203125e-07f * (1.0f + 9.5367431640625e-07f) + 1e-30f;
+  const float sph = radf * (1.0f + 9.5367431640625e-07f) + mu;
+  c.c = make_float4(cx, cy, cz, (ext * (1.0f + 9.5367431640625e-07f) + 2.0f * mu) + sph);
+  for (int k = 0; k < 4; k++) c.s[k] = make_float4(sf[k].x, sf[k].y, sf[k].z, sph);
+}
+
+constexpr int kPermBlock = 128;
+// Records are staged in shared memory with an odd stride (25 doubles) so that the per-thread
+// writes of a 24-double record hit distinct banks.
+constexpr int kRecWords = (int)(sizeof(NbrRec) / 8);   // 24
+constexpr int kRecStride = kRecWords + 1;
+
+// The block's records, staged in shared memory and written out as contiguous 16-byte stores.
+// Every thread of a kPermBlock-thread block calls this (slots past n contribute nothing).
+__device__ __forceinline__ void store_records(bool valid, long base, long n, const NbrRec &q, const CullRec &cr,
+                                              NbrRec *nbr, CullRec *cull, double *s_nbr, CullRec *s_cull) {
+  if (valid) {
+    const double *qw = reinterpret_cast<const double *>(&q);
+#pragma unroll
+    for (int k = 0; k < kRecWords; k++) s_nbr[threadIdx.x * kRecStride + k] = qw[k];
+    s_cull[threadIdx.x] = cr;
+  }
+  __syncthreads();
+  const long cnt = n - base < kPermBlock ? n - base : kPermBlock;
+  const int nw = (int)(cnt * kRecWords) / 2;   // double2 words of the block's records
+  double2 *b = reinterpret_cast<double2 *>(nbr + base);
+  for (int i = threadIdx.x; i < nw; i += kPermBlock) {
+    const int w0 = 2 * i, r0 = w0 / kRecWords, k0 = w0 - r0 * kRecWords;   // k0 even, k0 + 1 < 24
+    b[i] = make_double2(s_nbr[r0 * kRecStride + k0], s_nbr[r0 * kRecStride + k0 + 1]);
+  }
+  const int m16 = (int)(cnt * (long)(sizeof(CullRec) / 16));
+  const float4 *c = reinterpret_cast<const float4 *>(s_cull);
+  float4 *e = reinterpret_cast<float4 *>(cull + base);
+  for (int i = threadIdx.x; i < m16; i += kPermBlock) e[i] = c[i];
+}
+
 // ------------------------------------------------------------------ init_Verlet (+ cell keys)
 
 // Cell coordinate of cells.cu:69-77 (multiplication by cs_inv, then `== ncell -> ncell-1`).
@@ -127,162 +194,159 @@ __device__ __forceinline__ long bin_axis(double x, double xmin, double inv, long
 // with the current time (KEYS): the bucket key, the bucket count and the clump's arrival rank.
 // Clumps that are not binned (removed, or non-finite) get the unique bucket ncell_total + id, so every
 // bucket holds its clumps in id order after the rank pass.  `t_prev`: init_Verlet's removal test
-// uses the time before the advance (the fused step advances time first).
-template <bool PREDICT, bool KEYS>
-__global__ void k_predict(Planes P, DevScalars *d, bool t_prev, Cells cells,
-                          const long long *__restrict__ id, const int *__restrict__ flume, long n) {
-  long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (s >= n) return;
-  const DevFlume &fl = d->flumes[flume[s]];
-  const double side_x = fl.sys.side.x;
-  V3 r = load3(P, RX, s);
-  if (PREDICT) {
-    const double dt = fl.sys.dt, hdt = fl.sys.hdt;
-    const double t_init = t_prev ? d->time_prev : d->time;
-    if (is_removed(t_init, r.x, side_x)) {
-      P.p[RAD][s] = 0.0;
-    } else {
-      V3 v = load3(P, VX, s), a = load3(P, AIX, s), w = load3(P, WX, s), al = load3(P, ALIX, s);
-      V3 Rx = load3(P, R00, s), Ry = load3(P, R10, s), Rz = load3(P, R20, s);
-      r.x += dt * (v.x + hdt * a.x);
-      r.y += dt * (v.y + hdt * a.y);
-      r.z += dt * (v.z + hdt * a.z);
-      v.x += dt * a.x;
-      v.y += dt * a.y;
-      v.z += dt * a.z;
-      V3 dO = mk(dt * (w.x + hdt * al.x), dt * (w.y + hdt * al.y), dt * (w.z + hdt * al.z));
-      const double mag2 = dO.x * dO.x + dO.y * dO.y + dO.z * dO.z;
-      double mag, imag = 0.0;
-      if (kFast) {
-        imag = rsqrt(mag2);
-        mag = mag2 * imag;
+// uses the time before the advance (the fused step advances time first).  RECORDS: also write
+// the clump's neighbour records at its own slot (steps that keep the slot order).
+template <bool PREDICT, bool KEYS, bool RECORDS>
+__global__ void __launch_bounds__(kBlock) k_predict(Planes P, DevScalars *d, bool t_prev, Cells cells,
+                                                    const long long *__restrict__ id,
+                                                    const int *__restrict__ flume, NbrRec *nbr,
+                                                    CullRec *cull, long n) {
+  __shared__ double s_nbr[RECORDS ? kPermBlock * kRecStride : 1];
+  __shared__ CullRec s_cull[RECORDS ? kPermBlock : 1];
+  const long base = blockIdx.x * (long)blockDim.x;
+  const long s = base + threadIdx.x;
+  const bool valid = s < n;
+  if (!RECORDS && !valid) return;
+  NbrRec q;
+  CullRec cr;
+  if (valid) {
+    const DevFlume &fl = d->flumes[flume[s]];
+    const double side_x = fl.sys.side.x;
+    V3 r = load3(P, RX, s);
+    V3 v, w, sp[4];
+    bool have = false;   // v, w, sp hold the clump's current values
+    if (PREDICT) {
+      const double dt = fl.sys.dt, hdt = fl.sys.hdt;
+      const double t_init = t_prev ? d->time_prev : d->time;
+      if (is_removed(t_init, r.x, side_x)) {
+        P.p[RAD][s] = 0.0;
       } else {
-        mag = sqrt(mag2);
-      }
-      V3 dRx, dRy, dRz;
-      if (mag > 0.0) {
-        // Rodrigues rotation about dO/|dO| by |dO| (init_Verlet.cu:63-83)
-        V3 u;
-        double c, sn;
+        v = load3(P, VX, s);
+        w = load3(P, WX, s);
+        V3 a = load3(P, AIX, s), al = load3(P, ALIX, s);
+        V3 Rx = load3(P, R00, s), Ry = load3(P, R10, s), Rz = load3(P, R20, s);
+        r.x += dt * (v.x + hdt * a.x);
+        r.y += dt * (v.y + hdt * a.y);
+        r.z += dt * (v.z + hdt * a.z);
+        v.x += dt * a.x;
+        v.y += dt * a.y;
+        v.z += dt * a.z;
+        V3 dO = mk(dt * (w.x + hdt * al.x), dt * (w.y + hdt * al.y), dt * (w.z + hdt * al.z));
+        const double mag2 = dO.x * dO.x + dO.y * dO.y + dO.z * dO.z;
+        double mag, imag = 0.0;
         if (kFast) {
-          u = mk(dO.x * imag, dO.y * imag, dO.z * imag);
-          sincos(mag, &sn, &c);
+          imag = rsqrt(mag2);
+          mag = mag2 * imag;
         } else {
-          u = mk(dO.x / mag, dO.y / mag, dO.z / mag);
-          c = cos(mag);
-          sn = sin(mag);
+          mag = sqrt(mag2);
         }
-        const double omc = 1.0 - c;
-        dRx = mk(omc * u.x * u.x + c, omc * u.x * u.y - sn * u.z, omc * u.x * u.z + sn * u.y);
-        dRy = mk(omc * u.y * u.x + sn * u.z, omc * u.y * u.y + c, omc * u.y * u.z - sn * u.x);
-        dRz = mk(omc * u.z * u.x - sn * u.y, omc * u.z * u.y + sn * u.x, omc * u.z * u.z + c);
-      } else {
-        dRx = mk(1.0, 0.0, 0.0);
-        dRy = mk(0.0, 1.0, 0.0);
-        dRz = mk(0.0, 0.0, 1.0);
+        V3 dRx, dRy, dRz;
+        if (mag > 0.0) {
+          // Rodrigues rotation about dO/|dO| by |dO| (init_Verlet.cu:63-83)
+          V3 u;
+          double c, sn;
+          if (kFast) {
+            u = mk(dO.x * imag, dO.y * imag, dO.z * imag);
+            sincos(mag, &sn, &c);
+          } else {
+            u = mk(dO.x / mag, dO.y / mag, dO.z / mag);
+            c = cos(mag);
+            sn = sin(mag);
+          }
+          const double omc = 1.0 - c;
+          dRx = mk(omc * u.x * u.x + c, omc * u.x * u.y - sn * u.z, omc * u.x * u.z + sn * u.y);
+          dRy = mk(omc * u.y * u.x + sn * u.z, omc * u.y * u.y + c, omc * u.y * u.z - sn * u.x);
+          dRz = mk(omc * u.z * u.x - sn * u.y, omc * u.z * u.y + sn * u.x, omc * u.z * u.z + c);
+        } else {
+          dRx = mk(1.0, 0.0, 0.0);
+          dRy = mk(0.0, 1.0, 0.0);
+          dRz = mk(0.0, 0.0, 1.0);
+        }
+        // R <- dR R (rows), then each column renormalised (init_Verlet.cu:92-114)
+        V3 Tx = mk(dRx.x * Rx.x + dRx.y * Ry.x + dRx.z * Rz.x, dRx.x * Rx.y + dRx.y * Ry.y + dRx.z * Rz.y,
+                   dRx.x * Rx.z + dRx.y * Ry.z + dRx.z * Rz.z);
+        V3 Ty = mk(dRy.x * Rx.x + dRy.y * Ry.x + dRy.z * Rz.x, dRy.x * Rx.y + dRy.y * Ry.y + dRy.z * Rz.y,
+                   dRy.x * Rx.z + dRy.y * Ry.z + dRy.z * Rz.z);
+        V3 Tz = mk(dRz.x * Rx.x + dRz.y * Ry.x + dRz.z * Rz.x, dRz.x * Rx.y + dRz.y * Ry.y + dRz.z * Rz.y,
+                   dRz.x * Rx.z + dRz.y * Ry.z + dRz.z * Rz.z);
+        if (kFast) {
+          double in = rsqrt(Tx.x * Tx.x + Ty.x * Ty.x + Tz.x * Tz.x);
+          Rx.x = Tx.x * in; Ry.x = Ty.x * in; Rz.x = Tz.x * in;
+          in = rsqrt(Tx.y * Tx.y + Ty.y * Ty.y + Tz.y * Tz.y);
+          Rx.y = Tx.y * in; Ry.y = Ty.y * in; Rz.y = Tz.y * in;
+          in = rsqrt(Tx.z * Tx.z + Ty.z * Ty.z + Tz.z * Tz.z);
+          Rx.z = Tx.z * in; Ry.z = Ty.z * in; Rz.z = Tz.z * in;
+        } else {
+          double nrm = sqrt(Tx.x * Tx.x + Ty.x * Ty.x + Tz.x * Tz.x);
+          Rx.x = Tx.x / nrm; Ry.x = Ty.x / nrm; Rz.x = Tz.x / nrm;
+          nrm = sqrt(Tx.y * Tx.y + Ty.y * Ty.y + Tz.y * Tz.y);
+          Rx.y = Tx.y / nrm; Ry.y = Ty.y / nrm; Rz.y = Tz.y / nrm;
+          nrm = sqrt(Tx.z * Tx.z + Ty.z * Ty.z + Tz.z * Tz.z);
+          Rx.z = Tx.z / nrm; Ry.z = Ty.z / nrm; Rz.z = Tz.z / nrm;
+        }
+        w.x += dt * al.x;
+        w.y += dt * al.y;
+        w.z += dt * al.z;
+        store3(P, RX, s, r);
+        store3(P, VX, s, v);
+        store3(P, WX, s, w);
+        store3(P, R00, s, Rx);
+        store3(P, R10, s, Ry);
+        store3(P, R20, s, Rz);
+        // sphere centres r + (radius/sqrt2) R (+-1,+-1,+-1) (init_Verlet.cu:130-142)
+        const double pos = kFast ? P.p[RAD][s] * (1.0 / kROOT2) : P.p[RAD][s] / kROOT2;
+        sp[0] = mk(r.x + pos * (Rx.x + Rx.y + Rx.z), r.y + pos * (Ry.x + Ry.y + Ry.z),
+                   r.z + pos * (Rz.x + Rz.y + Rz.z));
+        sp[1] = mk(r.x + pos * (Rx.x - Rx.y - Rx.z), r.y + pos * (Ry.x - Ry.y - Ry.z),
+                   r.z + pos * (Rz.x - Rz.y - Rz.z));
+        sp[2] = mk(r.x + pos * (-Rx.x - Rx.y + Rx.z), r.y + pos * (-Ry.x - Ry.y + Ry.z),
+                   r.z + pos * (-Rz.x - Rz.y + Rz.z));
+        sp[3] = mk(r.x + pos * (-Rx.x + Rx.y - Rx.z), r.y + pos * (-Ry.x + Ry.y - Ry.z),
+                   r.z + pos * (-Rz.x + Rz.y - Rz.z));
+        for (int k = 0; k < 4; k++) store3(P, S0X + 3 * k, s, sp[k]);
+        have = true;
       }
-      // R <- dR R (rows), then each column renormalised (init_Verlet.cu:92-114)
-      V3 Tx = mk(dRx.x * Rx.x + dRx.y * Ry.x + dRx.z * Rz.x, dRx.x * Rx.y + dRx.y * Ry.y + dRx.z * Rz.y,
-                 dRx.x * Rx.z + dRx.y * Ry.z + dRx.z * Rz.z);
-      V3 Ty = mk(dRy.x * Rx.x + dRy.y * Ry.x + dRy.z * Rz.x, dRy.x * Rx.y + dRy.y * Ry.y + dRy.z * Rz.y,
-                 dRy.x * Rx.z + dRy.y * Ry.z + dRy.z * Rz.z);
-      V3 Tz = mk(dRz.x * Rx.x + dRz.y * Ry.x + dRz.z * Rz.x, dRz.x * Rx.y + dRz.y * Ry.y + dRz.z * Rz.y,
-                 dRz.x * Rx.z + dRz.y * Ry.z + dRz.z * Rz.z);
-      if (kFast) {
-        double in = rsqrt(Tx.x * Tx.x + Ty.x * Ty.x + Tz.x * Tz.x);
-        Rx.x = Tx.x * in; Ry.x = Ty.x * in; Rz.x = Tz.x * in;
-        in = rsqrt(Tx.y * Tx.y + Ty.y * Ty.y + Tz.y * Tz.y);
-        Rx.y = Tx.y * in; Ry.y = Ty.y * in; Rz.y = Tz.y * in;
-        in = rsqrt(Tx.z * Tx.z + Ty.z * Ty.z + Tz.z * Tz.z);
-        Rx.z = Tx.z * in; Ry.z = Ty.z * in; Rz.z = Tz.z * in;
-      } else {
-        double nrm = sqrt(Tx.x * Tx.x + Ty.x * Ty.x + Tz.x * Tz.x);
-        Rx.x = Tx.x / nrm; Ry.x = Ty.x / nrm; Rz.x = Tz.x / nrm;
-        nrm = sqrt(Tx.y * Tx.y + Ty.y * Ty.y + Tz.y * Tz.y);
-        Rx.y = Tx.y / nrm; Ry.y = Ty.y / nrm; Rz.y = Tz.y / nrm;
-        nrm = sqrt(Tx.z * Tx.z + Ty.z * Ty.z + Tz.z * Tz.z);
-        Rx.z = Tx.z / nrm; Ry.z = Ty.z / nrm; Rz.z = Tz.z / nrm;
+    }
+    if (RECORDS) {
+      if (!have) {
+        v = load3(P, VX, s);
+        w = load3(P, WX, s);
+        for (int k = 0; k < 4; k++) sp[k] = load3(P, S0X + 3 * k, s);
       }
-      w.x += dt * al.x;
-      w.y += dt * al.y;
-      w.z += dt * al.z;
-      store3(P, RX, s, r);
-      store3(P, VX, s, v);
-      store3(P, WX, s, w);
-      store3(P, R00, s, Rx);
-      store3(P, R10, s, Ry);
-      store3(P, R20, s, Rz);
-      // sphere centres r + (radius/sqrt2) R (+-1,+-1,+-1) (init_Verlet.cu:130-142)
-      const double pos = kFast ? P.p[RAD][s] * (1.0 / kROOT2) : P.p[RAD][s] / kROOT2;
-      store3(P, S0X, s, mk(r.x + pos * (Rx.x + Rx.y + Rx.z), r.y + pos * (Ry.x + Ry.y + Ry.z),
-                           r.z + pos * (Rz.x + Rz.y + Rz.z)));
-      store3(P, S1X, s, mk(r.x + pos * (Rx.x - Rx.y - Rx.z), r.y + pos * (Ry.x - Ry.y - Ry.z),
-                           r.z + pos * (Rz.x - Rz.y - Rz.z)));
-      store3(P, S2X, s, mk(r.x + pos * (-Rx.x - Rx.y + Rx.z), r.y + pos * (-Ry.x - Ry.y + Ry.z),
-                           r.z + pos * (-Rz.x - Rz.y + Rz.z)));
-      store3(P, S3X, s, mk(r.x + pos * (-Rx.x + Rx.y - Rx.z), r.y + pos * (-Ry.x + Ry.y - Ry.z),
-                           r.z + pos * (-Rz.x + Rz.y - Rz.z)));
+      make_records(r, v, w, sp, P.p[RAD][s], P.p[MSPH][s], P.p[MWALL][s], q, cr);
+    }
+    if (KEYS) {
+      const af3d_cell_par &g = fl.grid;
+      long key;
+      if (is_removed(d->time, r.x, side_x)) {
+        key = d->ncell_total + id[s];
+      } else if (!(isfinite(r.x) && isfinite(r.y) && isfinite(r.z))) {
+        raise_status(d, AF3D_ERR_NAN);
+        key = d->ncell_total + id[s];
+      } else {
+        long i = bin_axis(r.x, g.rr_min.x, g.cs_inv.x, g.ncell.x);
+        long j = bin_axis(r.y, g.rr_min.y, g.cs_inv.y, g.ncell.y);
+        long k = bin_axis(r.z, g.rr_min.z, g.cs_inv.z, g.ncell.z);
+        if (i < 0 || j < 0 || k < 0) {
+          raise_status(d, AF3D_ERR_NEGATIVE_CELL);
+          i = i < 0 ? 0 : i; j = j < 0 ? 0 : j; k = k < 0 ? 0 : k;
+        }
+        if (i >= g.ncell.x || j >= g.ncell.y || k >= g.ncell.z) {
+          raise_status(d, AF3D_ERR_GRID_ESCAPE);
+          i = i < g.ncell.x ? i : g.ncell.x - 1;
+          j = j < g.ncell.y ? j : g.ncell.y - 1;
+          k = k < g.ncell.z ? k : g.ncell.z - 1;
+        }
+        key = fl.cell_off + i + g.ncell.x * (j + k * g.ncell.y);
+      }
+      cells.key[s] = (int)key;
+      cells.rank_tmp[s] = atomicAdd(&cells.count[key], 1);
     }
   }
-  if (!KEYS) return;
-  const af3d_cell_par &g = fl.grid;
-  long key;
-  if (is_removed(d->time, r.x, side_x)) {
-    key = d->ncell_total + id[s];
-  } else if (!(isfinite(r.x) && isfinite(r.y) && isfinite(r.z))) {
-    raise_status(d, AF3D_ERR_NAN);
-    key = d->ncell_total + id[s];
-  } else {
-    long i = bin_axis(r.x, g.rr_min.x, g.cs_inv.x, g.ncell.x);
-    long j = bin_axis(r.y, g.rr_min.y, g.cs_inv.y, g.ncell.y);
-    long k = bin_axis(r.z, g.rr_min.z, g.cs_inv.z, g.ncell.z);
-    if (i < 0 || j < 0 || k < 0) {
-      raise_status(d, AF3D_ERR_NEGATIVE_CELL);
-      i = i < 0 ? 0 : i; j = j < 0 ? 0 : j; k = k < 0 ? 0 : k;
-    }
-    if (i >= g.ncell.x || j >= g.ncell.y || k >= g.ncell.z) {
-      raise_status(d, AF3D_ERR_GRID_ESCAPE);
-      i = i < g.ncell.x ? i : g.ncell.x - 1;
-      j = j < g.ncell.y ? j : g.ncell.y - 1;
-      k = k < g.ncell.z ? k : g.ncell.z - 1;
-    }
-    key = fl.cell_off + i + g.ncell.x * (j + k * g.ncell.y);
-  }
-  cells.key[s] = (int)key;
-  cells.rank_tmp[s] = atomicAdd(&cells.count[key], 1);
+  if (RECORDS) store_records(valid, base, n, q, cr, nbr, cull, s_nbr, s_cull);
 }
 
 // ------------------------------------------------------------------ permutation + records
-
-__device__ __forceinline__ float f_up(double x) { return __double2float_ru(x); }
-
-// Packed FP64 neighbour record and conservative FP32 culling record of one clump.
-__device__ __forceinline__ void make_records(V3 r, V3 v, V3 w, const V3 *sp, double rad, double msph,
-                                             double mwall, NbrRec &q, CullRec &c) {
-  q.rx = r.x; q.ry = r.y; q.rz = r.z;
-  q.vx = v.x; q.vy = v.y; q.vz = v.z;
-  q.wx = w.x; q.wy = w.y; q.wz = w.z;
-  double M = fmax(fmax(fabs(r.x), fabs(r.y)), fabs(r.z));
-  double ext = 0.0;
-  for (int k = 0; k < 4; k++) {
-    q.s[3 * k] = sp[k].x; q.s[3 * k + 1] = sp[k].y; q.s[3 * k + 2] = sp[k].z;
-    M = fmax(M, fmax(fmax(fabs(sp[k].x), fabs(sp[k].y)), fabs(sp[k].z)));
-    double dx = sp[k].x - r.x, dy = sp[k].y - r.y, dz = sp[k].z - r.z;
-    ext = fmax(ext, sqrt(dx * dx + dy * dy + dz * dz));
-  }
-  q.rad = rad; q.msph = msph; q.mwall = mwall;
-  // 2^-21 * max|coordinate| bounds 4x the FP32 rounding of a coordinate difference.
-  const double mu = fmax(M, rad) * 4.76837158203125e-07 + 1e-30;
-  const float radf = f_up(rad + mu);
-  c.c = make_float4((float)r.x, (float)r.y, (float)r.z, f_up(ext * (1.0 + 1e-12) + rad + mu));
-  for (int k = 0; k < 4; k++) c.s[k] = make_float4((float)sp[k].x, (float)sp[k].y, (float)sp[k].z, radf);
-}
-
-constexpr int kPermBlock = 128;
-// Records are staged in shared memory with an odd stride (25 doubles) so that the per-thread
-// writes of a 24-double record hit distinct banks.
-constexpr int kRecWords = (int)(sizeof(NbrRec) / 8);   // 24
-constexpr int kRecStride = kRecWords + 1;
 
 // dst[p][s] = src[p][perm[s]] for every plane (the force/torque accumulators and a_f only with
 // `ft`: the fused step rewrites them before reading), plus the packed records of the new slot,
@@ -305,30 +369,17 @@ __global__ void __launch_bounds__(kPermBlock) k_permute(Planes src, Planes dst, 
       id_dst[s] = id_src[o];
       fl_dst[s] = fl_src[o];
     }
-    if (nbr) {
-      V3 sp[4];
-      for (int k = 0; k < 4; k++) sp[k] = load3(dst, S0X + 3 * k, s);
-      NbrRec q;
-      make_records(load3(dst, RX, s), load3(dst, VX, s), load3(dst, WX, s), sp, dst.p[RAD][s],
-                   dst.p[MSPH][s], dst.p[MWALL][s], q, s_cull[threadIdx.x]);
-      const double *qw = reinterpret_cast<const double *>(&q);
-#pragma unroll
-      for (int k = 0; k < kRecWords; k++) s_nbr[threadIdx.x * kRecStride + k] = qw[k];
-    }
   }
   if (!nbr) return;
-  __syncthreads();
-  const long cnt = n - base < kPermBlock ? n - base : kPermBlock;
-  const int nw = (int)(cnt * kRecWords) / 2;   // double2 words of the block's records
-  double2 *b = reinterpret_cast<double2 *>(nbr + base);
-  for (int i = threadIdx.x; i < nw; i += kPermBlock) {
-    const int w0 = 2 * i, r0 = w0 / kRecWords, k0 = w0 - r0 * kRecWords;   // k0 even, k0 + 1 < 24
-    b[i] = make_double2(s_nbr[r0 * kRecStride + k0], s_nbr[r0 * kRecStride + k0 + 1]);
+  NbrRec q;
+  CullRec cr;
+  if (s < n) {
+    V3 sp[4];
+    for (int k = 0; k < 4; k++) sp[k] = load3(dst, S0X + 3 * k, s);
+    make_records(load3(dst, RX, s), load3(dst, VX, s), load3(dst, WX, s), sp, dst.p[RAD][s], dst.p[MSPH][s],
+                 dst.p[MWALL][s], q, cr);
   }
-  const int m16 = (int)(cnt * (long)(sizeof(CullRec) / 16));
-  const float4 *c = reinterpret_cast<const float4 *>(s_cull);
-  float4 *e = reinterpret_cast<float4 *>(cull + base);
-  for (int i = threadIdx.x; i < m16; i += kPermBlock) e[i] = c[i];
+  store_records(s < n, base, n, q, cr, nbr, cull, s_nbr, s_cull);
 }
 
 // ------------------------------------------------------------------ particle contacts
@@ -406,9 +457,12 @@ __device__ __forceinline__ Search search_centre(V3 r, const af3d_cell_par &g, lo
 
 // Visit the occupied slots of the 27 neighbour cells in the reference's order
 // (idel, jdel, kdel from -1 to 1; force_part.cu:88-106); slots inside a cell are in id order.
+// `order` (may be null): the slot of the clump at each position of the (cell, id) order, for
+// steps that do not move the clumps into that order.
 template <typename F>
 __device__ __forceinline__ void for_neighbour_slots(const Search &q, const af3d_cell_par &g,
-                                                    const int *__restrict__ start, F &&f) {
+                                                    const int *__restrict__ start,
+                                                    const int *__restrict__ order, F &&f) {
 #pragma unroll 1
   for (int di = -1; di <= 1; di++)
 #pragma unroll 1
@@ -421,8 +475,37 @@ __device__ __forceinline__ void for_neighbour_slots(const Search &q, const af3d_
         const long c = q.off + in + g.ncell.x * (jn + g.ncell.y * kn);
         const int t0 = __ldg(&start[c]), t1 = __ldg(&start[c + 1]);
 #pragma unroll 1
-        for (int t = t0; t < t1; t++) f(t);
+        for (int t = t0; t < t1; t++) f(order ? __ldg(&order[t]) : t);
       }
+}
+
+// The positions (in the (cell, id) order) of the 27 neighbour cells' clumps, in the reference's
+// order, with every cell boundary loaded up front (as below).
+template <typename F>
+__device__ __forceinline__ void for_neighbour_positions_pre(const Search &q, const af3d_cell_par &g,
+                                                            const int *__restrict__ start, F &&f) {
+  int bnd[9][4];
+  const long x0 = q.ci - 1;
+#pragma unroll
+  for (int r = 0; r < 9; r++) {
+    const long jn = q.cj + (r / 3 - 1), kn = q.ck + (r % 3 - 1);
+    const bool row_ok = jn >= 0 && kn >= 0 && jn < g.ncell.y && kn < g.ncell.z;
+    const long rb = q.off + g.ncell.x * (jn + g.ncell.y * kn);
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+      long x = x0 + e;
+      x = x < 0 ? 0 : (x > g.ncell.x ? g.ncell.x : x);
+      bnd[r][e] = row_ok ? __ldg(&start[rb + x]) : 0;
+    }
+  }
+#pragma unroll 1
+  for (int di = 0; di < 3; di++)
+#pragma unroll 1
+    for (int r = 0; r < 9; r++) {
+      const int k0 = bnd[r][di], k1 = bnd[r][di + 1];
+#pragma unroll 1
+      for (int k = k0; k < k1; k++) f(k);
+    }
 }
 
 // The same visit with every cell boundary loaded up front.  The three cells of one (jdel, kdel)
@@ -431,7 +514,8 @@ __device__ __forceinline__ void for_neighbour_slots(const Search &q, const af3d_
 // (instead of 27 dependent round trips), then the cells are walked in the reference's order.
 template <typename F>
 __device__ __forceinline__ void for_neighbour_slots_pre(const Search &q, const af3d_cell_par &g,
-                                                        const int *__restrict__ start, F &&f) {
+                                                        const int *__restrict__ start,
+                                                        const int *__restrict__ order, F &&f) {
   int bnd[9][4];
   const long x0 = q.ci - 1;
 #pragma unroll
@@ -453,7 +537,7 @@ __device__ __forceinline__ void for_neighbour_slots_pre(const Search &q, const a
     for (int r = 0; r < 9; r++) {
       const int t0 = bnd[r][di], t1 = bnd[r][di + 1];
 #pragma unroll 1
-      for (int t = t0; t < t1; t++) f(t);
+      for (int t = t0; t < t1; t++) f(order ? __ldg(&order[t]) : t);
     }
 }
 
@@ -466,15 +550,15 @@ constexpr int kItemCap = 96;
 
 __device__ __forceinline__ bool gather_items(long s, const Own &o, const af3d_cell_par &g,
                                              long long off, const CullRec *__restrict__ cull,
-                                             const int *__restrict__ start, unsigned want,
-                                             unsigned *items, int cap, int &nitems) {
+                                             const int *__restrict__ start, const int *__restrict__ order,
+                                             unsigned want, unsigned *items, int cap, int &nitems) {
   const CullRec me = cull[s];
   const Search q = search_centre(o.r, g, off);
   int cand_t[kCandCap];
   unsigned short cand_m[kCandCap];
   int ncand = 0;
   bool overflow = false;
-  for_neighbour_slots_pre(q, g, start, [&](int t) {
+  for_neighbour_slots_pre(q, g, start, order, [&](int t) {
     if (t == s) return;
     const unsigned m = pair_mask(me, cull[t]) & want;
     if (!m) return;
@@ -507,7 +591,8 @@ __device__ __forceinline__ int contacts_by_pass(long s, const Own &o, const Cons
                                                 const af3d_cell_par &g, long long off,
                                                 const NbrRec *__restrict__ nbr,
                                                 const CullRec *__restrict__ cull,
-                                                const int *__restrict__ start, unsigned want, V3 &F,
+                                                const int *__restrict__ start,
+                                                const int *__restrict__ order, unsigned want, V3 &F,
                                                 V3 &T) {
   const bool xi0 = c.variant == AF3D_FRICTION_DEV;
   const CullRec me = cull[s];
@@ -517,7 +602,7 @@ __device__ __forceinline__ int contacts_by_pass(long s, const Own &o, const Cons
   for (int p = 0; p < 16; p++) {
     if (!((want >> p) & 1u)) continue;
     const int sl = p & 3, sm = p >> 2;
-    for_neighbour_slots(q, g, start, [&](int t) {
+    for_neighbour_slots(q, g, start, order, [&](int t) {
       if (t == s) return;
       if (!((pair_mask(me, cull[t]) >> p) & 1u)) return;
       active += part_pair(o.r, o.v, o.w, o.s[sl], o.rad, o.msph, nbr[t], sm, c, xi0, F, T) == 2;
@@ -531,14 +616,15 @@ __device__ __forceinline__ int particle_contacts(long s, const Own &o, const Con
                                                  const af3d_cell_par &g, long long off,
                                                  const NbrRec *__restrict__ nbr,
                                                  const CullRec *__restrict__ cull,
-                                                 const int *__restrict__ start, int only_p, V3 &F,
+                                                 const int *__restrict__ start,
+                                                 const int *__restrict__ order, int only_p, V3 &F,
                                                  V3 &T) {
   const bool xi0 = c.variant == AF3D_FRICTION_DEV;
   const unsigned want = only_p < 0 ? 0xffffu : (1u << only_p);
   unsigned items[kItemCap];
   int nitems = 0;
-  if (!gather_items(s, o, g, off, cull, start, want, items, kItemCap, nitems))
-    return contacts_by_pass(s, o, c, g, off, nbr, cull, start, want, F, T);
+  if (!gather_items(s, o, g, off, cull, start, order, want, items, kItemCap, nitems))
+    return contacts_by_pass(s, o, c, g, off, nbr, cull, start, order, want, F, T);
   int active = 0;
 #pragma unroll 1
   for (int i = 0; i < nitems; i++) {
@@ -622,7 +708,9 @@ __device__ __forceinline__ int warp_contacts(WarpQueue &wq, long wbase, long s, 
                                              const DevScalars *d, const int *__restrict__ flume,
                                              const NbrRec *__restrict__ nbr,
                                              const CullRec *__restrict__ cull,
-                                             const int *__restrict__ start, V3 &F, V3 &T) {
+                                             const int *__restrict__ start,
+                                             const int *__restrict__ order,
+                                             const float4 *__restrict__ csort, V3 &F, V3 &T) {
   const int lane = threadIdx.x & 31;
   const int my_flume = flume[s];
   const int pre0 = aval ? R_HOP0 : 1, pre1 = aval ? R_WALLS : 0;         // fill: none before
@@ -637,11 +725,13 @@ __device__ __forceinline__ int warp_contacts(WarpQueue &wq, long wbase, long s, 
   if (act && !slow) {
     const float4 mc = cull[s].c;
     const Search q = search_centre(o.r, g, off);
-    for_neighbour_slots_pre(q, g, start, [&](int t) {
-      if (t == s) return;
-      const float4 pc = cull[t].c;
+    for_neighbour_positions_pre(q, g, start, [&](int k) {
+      // the culling centre at position k: contiguous along a cell row in either layout
+      const float4 pc = order ? __ldg(&csort[k]) : cull[k].c;
       const float lim = mc.w + pc.w;
       if (d2f(mc, pc) > lim * lim * kCullSlack) return;
+      const int t = order ? __ldg(&order[k]) : k;
+      if (t == s) return;
       if (npass < kPassCap) wq.pass_t[lane][npass] = t;
       npass++;
     });
@@ -737,7 +827,7 @@ __device__ __forceinline__ int warp_contacts(WarpQueue &wq, long wbase, long s, 
   if (slow) {
     for (int rt = pre0; rt <= pre1; rt++)
       if (bnd_may_touch(rt, o.r, B, c)) bnd_routine(rt, o, false, c, F, T);
-    active += contacts_by_pass(s, o, c, g, off, nbr, cull, start, 0xffffu, F, T);
+    active += contacts_by_pass(s, o, c, g, off, nbr, cull, start, order, 0xffffu, F, T);
     for (int rt = post0; rt <= post1; rt++)
       if (bnd_may_touch(rt, o.r, B, c)) bnd_routine(rt, o, false, c, F, T);
   }
@@ -786,7 +876,9 @@ __global__ void __launch_bounds__(kBlock, AF3D_FORCES_MINB) k_fused_forces(Plane
                                                          const int *__restrict__ flume,
                                                          const NbrRec *__restrict__ nbr,
                                                          const CullRec *__restrict__ cull,
-                                                         const int *__restrict__ start, long n) {
+                                                         const int *__restrict__ start,
+                                                         const int *__restrict__ order,
+                                                         const float4 *__restrict__ csort, long n) {
 #if AF3D_COOP
   __shared__ WarpQueue wq[kBlock / 32];
 #endif
@@ -809,7 +901,7 @@ __global__ void __launch_bounds__(kBlock, AF3D_FORCES_MINB) k_fused_forces(Plane
       if (bnd_may_touch(rt, o.r, B, c)) bnd_routine(rt, o, true, c, F, T);
   const long wbase = blockIdx.x * (long)blockDim.x + (threadIdx.x & ~31u);
   const int active = warp_contacts(wq[threadIdx.x >> 5], wbase, sv, valid && !removed, aval, B, o, c, g, off,
-                                   d, flume, nbr, cull, start, F, T);
+                                   d, flume, nbr, cull, start, order, csort, F, T);
 #else
   if (valid && aval) {
     // hop x3, funnel, fcorners, walls (avalanche_hst.cu:688-696)
@@ -817,7 +909,8 @@ __global__ void __launch_bounds__(kBlock, AF3D_FORCES_MINB) k_fused_forces(Plane
       if (bnd_may_touch(rt, o.r, B, c)) bnd_routine(rt, o, removed, c, F, T);
   }
   // part x16 (avalanche_hst.cu:699-701, fill :455-457)
-  const int active = (valid && !removed) ? particle_contacts(s, o, c, g, off, nbr, cull, start, -1, F, T) : 0;
+  const int active =
+      (valid && !removed) ? particle_contacts(s, o, c, g, off, nbr, cull, start, order, -1, F, T) : 0;
   if (valid) {
     if (aval) {
       if (bnd_may_touch(R_FLUME, o.r, B, c)) bnd_routine(R_FLUME, o, removed, c, F, T);   // :704
@@ -883,7 +976,7 @@ __global__ void __launch_bounds__(kBlock) k_part(Planes P, DevScalars *d, const 
   const Own o = own_from_planes(P, s);
   if (is_removed(c.time, o.r.x, c.side_x)) return;
   V3 F = load3(P, FX, s), T = load3(P, TX, s);
-  particle_contacts(s, o, c, g, d->flumes[f].cell_off, nbr, cull, start, sph_id - 1, F, T);
+  particle_contacts(s, o, c, g, d->flumes[f].cell_off, nbr, cull, start, nullptr, sph_id - 1, F, T);
   store3(P, FX, s, F);
   store3(P, TX, s, T);
 }
@@ -1084,7 +1177,7 @@ __global__ void k_contact_pairs(Planes P, DevScalars *d, const int *__restrict__
   if (is_removed(c.time, o.r.x, c.side_x)) return;
   const CullRec me = cull[s];
   const Search q = search_centre(o.r, g, d->flumes[f].cell_off);
-  for_neighbour_slots(q, g, start, [&](int t) {
+  for_neighbour_slots(q, g, start, nullptr, [&](int t) {
     if (t == s) return;
     unsigned m = pair_mask(me, cull[t]);
     while (m) {
@@ -1124,15 +1217,17 @@ namespace fast {
 #endif
 
 void launch_predict(const Launch &L, Planes cur, DevScalars *d, bool predict, bool keys, bool t_prev,
-                    Cells cells, const long long *id, const int *flume) {
+                    Cells cells, const long long *id, const int *flume, NbrRec *nbr, CullRec *cull) {
   if (L.n <= 0) return;
   const unsigned g = grid_for(L.n);
-  if (predict && keys)
-    k_predict<true, true><<<g, kBlock, 0, L.st>>>(cur, d, t_prev, cells, id, flume, L.n);
+  if (predict && keys && nbr)
+    k_predict<true, true, true><<<g, kBlock, 0, L.st>>>(cur, d, t_prev, cells, id, flume, nbr, cull, L.n);
+  else if (predict && keys)
+    k_predict<true, true, false><<<g, kBlock, 0, L.st>>>(cur, d, t_prev, cells, id, flume, nbr, cull, L.n);
   else if (predict)
-    k_predict<true, false><<<g, kBlock, 0, L.st>>>(cur, d, t_prev, cells, id, flume, L.n);
+    k_predict<true, false, false><<<g, kBlock, 0, L.st>>>(cur, d, t_prev, cells, id, flume, nbr, cull, L.n);
   else if (keys)
-    k_predict<false, true><<<g, kBlock, 0, L.st>>>(cur, d, t_prev, cells, id, flume, L.n);
+    k_predict<false, true, false><<<g, kBlock, 0, L.st>>>(cur, d, t_prev, cells, id, flume, nbr, cull, L.n);
 }
 
 void launch_permute_records(const Launch &L, Planes src, Planes dst, const int *perm,
@@ -1150,12 +1245,15 @@ void launch_build_records(const Launch &L, Planes cur, NbrRec *nbr, CullRec *cul
 }
 
 void launch_fused_forces(const Launch &L, Planes cur, Planes out, DevScalars *d, const int *flume,
-                         const NbrRec *nbr, const CullRec *cull, const int *start, bool write_ft) {
+                         const NbrRec *nbr, const CullRec *cull, const int *start, const int *order,
+                         const float4 *csort, bool write_ft) {
   if (L.n <= 0) return;
   if (write_ft)
-    k_fused_forces<true><<<grid_for(L.n), kBlock, 0, L.st>>>(cur, out, d, flume, nbr, cull, start, L.n);
+    k_fused_forces<true><<<grid_for(L.n), kBlock, 0, L.st>>>(cur, out, d, flume, nbr, cull, start, order, csort,
+                                                             L.n);
   else
-    k_fused_forces<false><<<grid_for(L.n), kBlock, 0, L.st>>>(cur, out, d, flume, nbr, cull, start, L.n);
+    k_fused_forces<false><<<grid_for(L.n), kBlock, 0, L.st>>>(cur, out, d, flume, nbr, cull, start, order, csort,
+                                                              L.n);
 }
 
 void launch_boundary(const Launch &L, Planes cur, DevScalars *d, const int *flume, int routine) {
