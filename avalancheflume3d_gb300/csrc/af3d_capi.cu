@@ -157,6 +157,7 @@ af3d_status push_params(af3d_ctx *c) {
     fl[f].sys = c->sys[f];
     fl[f].sys.time = c->time;
     fl[f].fun = c->fun[f];
+    fl[f].tant = c->sys[f].sint / c->sys[f].cost;
   }
   AF3D_CUDA(cudaMemcpyAsync(c->flumes, fl.data(), sizeof(DevFlume) * c->nflumes, cudaMemcpyHostToDevice, c->st));
   AF3D_CUDA(cudaMemcpyAsync(&c->d->time, &c->time, sizeof(double), cudaMemcpyHostToDevice, c->st));
@@ -487,6 +488,7 @@ af3d_status af3d_create_ensemble(int nflumes, const af3d_system_par *sys, const 
     fl[f].fun = c->fun[f];
     fl[f].grid = c->grid[f];
     fl[f].pending = c->grid[f];
+    fl[f].tant = c->sys[f].sint / c->sys[f].cost;
   }
   DevScalars ds;
   std::memset(&ds, 0, sizeof ds);

@@ -74,7 +74,7 @@ struct DevFlume {
   af3d_funnel     fun;
   af3d_cell_par   grid;
   long long       cell_off;   // first bucket of this flume's cells
-  long long       pad;
+  double          tant;       // sys.sint / sys.cost (force_flume.cu's tangent), set by the host
   unsigned long long bbox[8]; // re-grid scratch: ordered-int min/max of x, y, z, max vx, min vz
   af3d_cell_par   pending;    // grid derived by the last re-grid, committed when it fits
 };

@@ -19,7 +19,11 @@ namespace {
 constexpr int kBlock = 128;
 // Resident blocks per SM requested for the fused force kernel (register budget 65536 / (128 x n)).
 #ifndef AF3D_FORCES_MINB
+#ifdef AF3D_FAST
+#define AF3D_FORCES_MINB 4
+#else
 #define AF3D_FORCES_MINB 3
+#endif
 #endif
 
 inline unsigned grid_for(long n, int block = kBlock) {

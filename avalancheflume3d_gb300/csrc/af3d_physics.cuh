@@ -54,6 +54,7 @@ struct Consts {
   double mu_pw, kappa_pw, gamma_pw, cns_pw;
   double sint, cost, dy2, side_x, side_y;
   double sinfi, cosfi, tanfi;
+  double tant;     // sint / cost
   double inv_dt;   // fast mode only: 1/dt
   int phase, variant;
 };
@@ -67,6 +68,7 @@ __device__ __forceinline__ Consts load_consts(const DevScalars *d, int f) {
   c.mu_pw = s.mu_pw; c.kappa_pw = s.kappa_pw; c.gamma_pw = s.gamma_pw; c.cns_pw = s.fr_fact_pw;
   c.sint = s.sint; c.cost = s.cost; c.dy2 = s.dy2; c.side_x = s.side.x; c.side_y = s.side.y;
   c.sinfi = fl.fun.sinfi; c.cosfi = fl.fun.cosfi; c.tanfi = fl.fun.tanfi;
+  c.tant = fl.tant;
   c.phase = d->phase; c.variant = d->variant;
   c.inv_dt = kFast ? 1.0 / s.dt : 0.0;
   return c;
@@ -364,7 +366,7 @@ __device__ __forceinline__ bool walls_sphere(const Sph &o, const Consts &c, Cont
 // force_flume.cu:10-182, one sphere (callers skip removed clumps).
 __device__ __forceinline__ bool flume_sphere(const Sph &o, const Consts &c, ContactIn &ci) {
   const double ri = o.rad;
-  const double tant = c.sint / c.cost;
+  const double tant = c.tant;   // c.sint / c.cost, formed once per flume by the host
   const V3 s = o.s;
   double rect = -tant * s.x - s.z;
   double dist = fabs(c.cost * rect);
