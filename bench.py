@@ -13,7 +13,7 @@ timed window.  ``--layout pile`` builds the same packing in the hopper (it falls
 door opens, and its contacts relax within a few tens of steps); ``--layout lattice`` is the
 bare release block of the configuration (optionally with the reference's random initial
 velocities ``--v0`` and a release ``--preroll``), which has almost no contacts.  Synthetic data;
-the state (~400 MB) is larger than L2.
+the state (~350 MB) is larger than L2.
 
 Timed: exactly K fused steps (graph replays, af3d_step) after W warm-up steps, CUDA events on
 the engine's stream, barrier + synchronize on both sides, max over ranks.  Then, outside the
@@ -56,6 +56,9 @@ def parse_args():
     p.add_argument("--layout", choices=["bed", "pile", "lattice"], default="bed")
     p.add_argument("--preroll", type=int, default=0, help="untimed release steps of the input")
     p.add_argument("--v0", type=float, default=0.0)
+    p.add_argument("--clock-window", type=float, default=1.0,
+                   help="seconds of untimed steps before the warm-up, so that the clock samples "
+                        "cover the GPU under sustained load (0: none)")
     p.add_argument("--profile-steps", type=int, default=10)
     p.add_argument("--e2e-steps", type=int, default=5)
     p.add_argument("--cpu-sample", type=int, default=16384, help="clumps in the CPU baseline sample")
@@ -63,6 +66,7 @@ def parse_args():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--fp-mode", choices=["exact", "fast"], default="fast",
                    help="FP64 mode of the timed steps (the other mode is timed beside it)")
+    p.add_argument("--no-other-mode", action="store_true", help="do not time the other FP64 mode")
     p.add_argument("--ensemble-flumes", type=int, default=256,
                    help="flumes of the batched-ensemble measurement (0 skips it)")
     p.add_argument("--ensemble-steps", type=int, default=64)
@@ -83,7 +87,8 @@ def config_dict(args, cfg, extra=None):
     d = {"workload": "flume262k" if args.n == 262144 else "flume%d" % args.n,
          "clumps": args.n, "spheres": 4 * args.n, "tilt_deg": cfg.tilt_deg, "flume_m": cfg.Lflume / 100,
          "width_m": cfg.width / 100, "dt_s": cfg.dt, "lattice_mm": cfg.pitch * 10, "v0_cm_s": args.v0,
-         "layout": args.layout, "preroll_steps": args.preroll, "friction": "host (force_part.cu:224)",
+         "layout": args.layout, "preroll_steps": args.preroll, "load_window_s": args.clock_window,
+         "friction": "host (force_part.cu:224)",
          "l2": "state larger than L2 (no flush needed)"}
     if extra:
         d.update(extra)
@@ -125,7 +130,7 @@ class ClockSampler:
         reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
         return {"sm_mhz": statistics.median(float(r[1]) for r in rows),
                 "sm_max_mhz": max(float(r[2]) for r in rows), "reasons": reasons,
-                "samples": len(rows), "window": "pre-roll start to end of the timed region"}
+                "samples": len(rows), "window": "untimed load window, warm-up and timed steps"}
 
 
 def measured_peaks():
@@ -283,6 +288,23 @@ def measure_ensemble(args, stream):
             "geometry": "40 cm x 4 cm flume, reference hopper and funnel; per-flume slope 25-40 deg"}
 
 
+def time_other_mode(eng, modes, other, args, stream, R, dev, world):
+    """K steps of the other FP64 mode on the same state (after the timed region)."""
+    import torch
+    from avalancheflume3d_gb300 import replicas
+    eng.set_fp_mode(modes[other])
+    eng.step(2)
+    torch.cuda.synchronize()
+    o0, o1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    o0.record(stream)
+    eng.step(args.steps)
+    o1.record(stream)
+    torch.cuda.synchronize()
+    ms_other = replicas.max_over_ranks(R, o0.elapsed_time(o1), dev)
+    return {"fp_mode": other, "value": world * args.n * args.steps / (ms_other / 1e3),
+            "ms_per_step": ms_other / args.steps, "steps": args.steps}
+
+
 def run_engine(args):
     import torch
     from avalancheflume3d_gb300 import replicas
@@ -302,8 +324,9 @@ def run_engine(args):
     eng.import_particles(pp)
     eng.forces()          # start-up force pass into a_i (avalanche_hst.cu:366-384)
     eng.swap_accel()
-    # Clocks are sampled every 200 ms from the start of the pre-roll to the end of the timed
-    # region (all under load): the timed window alone is shorter than one sampling period.
+    # Clocks are sampled every 200 ms from the start of the pre-roll through an untimed load
+    # window (--clock-window) to the end of the timed region, all under load: the timed window
+    # alone is shorter than one sampling period.
     clocks = ClockSampler(local)
     trace = []
     if args.preroll:
@@ -319,6 +342,11 @@ def run_engine(args):
                 print("contacts per step during the pre-roll:", trace, file=sys.stderr, flush=True)
         else:
             eng.step(args.preroll)
+    if args.clock_window > 0:
+        t_end = time.perf_counter() + args.clock_window
+        while time.perf_counter() < t_end:
+            eng.step(64)
+            torch.cuda.synchronize()
     eng.step(args.warmup)
     grid = eng.get_grid()
     ncell3 = int(grid["ncell3"])
@@ -348,18 +376,10 @@ def run_engine(args):
 
     # The other FP64 mode on the same state, same step count (outside the timed region).
     other = "exact" if args.fp_mode == "fast" else "fast"
-    eng.set_fp_mode(modes[other])
-    eng.step(2)
-    torch.cuda.synchronize()
-    o0, o1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    o0.record(stream)
-    eng.step(args.steps)
-    o1.record(stream)
-    torch.cuda.synchronize()
-    ms_other = replicas.max_over_ranks(R, o0.elapsed_time(o1), dev)
+    other_line = None
+    if not args.no_other_mode:
+        other_line = time_other_mode(eng, modes, other, args, stream, R, dev, world)
     eng.set_fp_mode(modes[args.fp_mode])
-    other_line = {"fp_mode": other, "value": world * args.n * args.steps / (ms_other / 1e3),
-                  "ms_per_step": ms_other / args.steps, "steps": args.steps}
 
     # Roofline of the dominant kernel from CUDA events between the kernels (profiled steps after
     # the timed region, same stream).
