@@ -95,6 +95,7 @@ SIGNATURES = [
     ("af3d_forces", [_P], C.c_int),
     ("af3d_step", [_P, C.c_long], C.c_int),
     ("af3d_get_status", [_P, _P], C.c_int),
+    ("af3d_adjoint", [_P, C.c_long, C.c_long, _P, _P, _P, _P, _P, _P], C.c_int),
     ("af3d_step_profile", [_P, C.c_long, _P], C.c_int),
     ("af3d_kernel_launches", [_P, _P], C.c_int),
     ("af3d_fp64_peak", [_P], C.c_int),

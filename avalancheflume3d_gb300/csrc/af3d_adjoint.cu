@@ -1,0 +1,834 @@
+// af3d_adjoint.cu -- reverse-mode derivative (adjoint) of the exact-mode step.
+//
+// The forward step, with its discrete structure held fixed (cells, contact sets, which branch of
+// the contact law and which wall each sphere touches):
+//   predict    r1 = r + dt (v + dt/2 a_i),  v1 = v + dt a_i,  w1 = w + dt alpha_i,
+//              R1 = colnorm(dR(dO) R) with dO = dt (w + dt/2 alpha_i),  s_k = r1 + pos R1 p_k
+//   forces     F, T = sum over contacts and walls (each a function of the two clumps' r1, v1,
+//              w1 and sphere centres, and of kappa, gamma, mu)
+//   get_accel  a_f = F/m - drag |v1| v1 - g z,  alpha_f = R1 (R1^T T) / I
+//   finish     v2 = v1 + dt/2 (a_f - a_i),  w2 = w1 + dt/2 (alpha_f - alpha_i)
+// and the next state is (r1, v2, w2, R1, a_f, alpha_f).  The kernels here run that step
+// backwards: given the adjoint of the next state they form the adjoint of this one, and add the
+// step's contributions to the adjoints of kappa, gamma and mu (particle and wall).  Every
+// contact is re-evaluated from the step's recomputed state; the derivative of the contact law
+// is its exact piecewise derivative, including the Coulomb-capped sliding branch.  A contact's
+// derivative with respect to the partner clump is scattered with FP64 atomics: derivatives of a
+// sum do not depend on the order of its terms.
+//
+// Compiled with -fmad=false like the exact step kernels (the forward re-evaluation must take
+// the forward's branches).
+#include "af3d_cellwalk.cuh"
+
+namespace af3d {
+
+namespace {
+
+constexpr int kAdjBlock = 128;
+
+__device__ __forceinline__ V3 ld3(const Planes &P, int x, long s) { return mk(P.p[x][s], P.p[x + 1][s], P.p[x + 2][s]); }
+__device__ __forceinline__ void st3(const Planes &P, int x, long s, V3 v) {
+  P.p[x][s] = v.x;
+  P.p[x + 1][s] = v.y;
+  P.p[x + 2][s] = v.z;
+}
+__device__ __forceinline__ V3 operator+(V3 a, V3 b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ V3 operator-(V3 a, V3 b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ V3 operator*(double k, V3 a) { return mk(k * a.x, k * a.y, k * a.z); }
+__device__ __forceinline__ V3 &operator+=(V3 &a, V3 b) {
+  a.x += b.x; a.y += b.y; a.z += b.z;
+  return a;
+}
+__device__ __forceinline__ V3 &operator-=(V3 &a, V3 b) {
+  a.x -= b.x; a.y -= b.y; a.z -= b.z;
+  return a;
+}
+__device__ __forceinline__ double dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ V3 cross(V3 a, V3 b) {
+  return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ void atomic_add3(const Planes &P, int x, long s, V3 v) {
+  atomicAdd(&P.p[x][s], v.x);
+  atomicAdd(&P.p[x + 1][s], v.y);
+  atomicAdd(&P.p[x + 2][s], v.z);
+}
+
+// Adjoints of the law's inputs.
+struct LawBar {
+  V3 dv, n;
+  double comp, km, gm, mu;
+};
+
+// Reverse of contact_law (af3d_physics.cuh) for a contact that produced a force, given the
+// adjoint fb of that force.  The law is re-evaluated in the same operations to take the same
+// branches.
+__device__ __forceinline__ void contact_law_rev(const ContactIn &ci, double dt, V3 fb, LawBar &lb) {
+  const V3 dv = ci.dvvc, n = ci.n;
+  const double vn = dv.x * n.x + dv.y * n.y + dv.z * n.z;
+  V3 vt;
+  vt.x = dv.x - vn * n.x;
+  vt.y = dv.y - vn * n.y;
+  vt.z = dv.z - vn * n.z;
+  const double vt_mag = sqrt(vt.x * vt.x + vt.y * vt.y + vt.z * vt.z);
+  V3 tv;
+  tv.x = vt.x / vt_mag;
+  tv.y = vt.y / vt_mag;
+  tv.z = vt.z / vt_mag;
+  const double vt_sig = dv.x * tv.x + dv.y * tv.y + dv.z * tv.z;
+  const double normal = ci.km * ci.comp + ci.gm * (-vn);
+  double xi = dt * vt_sig;
+  const bool zeroed = ci.cns * normal < fabs(xi);
+  if (zeroed) xi = 0.0;
+  const double xi_dot = xi / dt;
+  const double m = ci.mass_t;
+  const double fsdt = 1.0e12 * m * xi + 2.0e6 * m * xi_dot;
+  const bool tang = vt_mag > 0.0;
+  const bool coul = tang && (fabs(fsdt) > ci.mu * normal || (ci.xi0 && xi == 0.0));
+
+  double normal_b = -dot(fb, n);
+  V3 n_b = (-normal) * fb;
+  V3 dv_b = mk(0.0, 0.0, 0.0), vt_b = mk(0.0, 0.0, 0.0);
+  double vtmag_b = 0.0, mu_b = 0.0;
+  if (tang) {
+    if (coul) {
+      // af = 0.8 mu N / |vt|;  t0 = m / af;  r = dt / t0;  f += af / (1 + r^2) vt
+      const double af = 0.8 * ci.mu * normal / vt_mag;
+      const double r = dt / (m / af);
+      const double den = 1.0 + r * r;
+      const double af2 = af / den;
+      const double af2_b = dot(fb, vt);
+      vt_b += af2 * fb;
+      const double af_b = af2_b * (1.0 - r * r) / (den * den);
+      mu_b += af_b * 0.8 * normal / vt_mag;
+      normal_b += af_b * 0.8 * ci.mu / vt_mag;
+      vtmag_b -= af_b * af / vt_mag;
+    } else {
+      // f_i += fsdt vt_i / |vt| for every component with vt_i != 0
+      const double g = fsdt / vt_mag;
+      double g_b = 0.0;
+      if (vt.x != 0.0) { vt_b.x += g * fb.x; g_b += fb.x * vt.x; }
+      if (vt.y != 0.0) { vt_b.y += g * fb.y; g_b += fb.y * vt.y; }
+      if (vt.z != 0.0) { vt_b.z += g * fb.z; g_b += fb.z * vt.z; }
+      const double fsdt_b = g_b / vt_mag;
+      vtmag_b -= g_b * g / vt_mag;
+      if (!zeroed) {
+        // fsdt = m xi (1e12 + 2e6 / dt), xi = dt vt_sig, vt_sig = dv . vt / |vt|
+        const double xi_b = fsdt_b * (1.0e12 * m + 2.0e6 * m / dt);
+        const double vtsig_b = dt * xi_b;
+        dv_b += vtsig_b * tv;
+        const V3 tv_b = vtsig_b * dv;
+        vt_b += (1.0 / vt_mag) * tv_b;
+        vtmag_b -= dot(tv_b, vt) / (vt_mag * vt_mag);
+      }
+    }
+    vt_b += vtmag_b * tv;   // |vt| = sqrt(vt . vt)
+  }
+  // normal = km comp - gm vn
+  lb.km = normal_b * ci.comp;
+  lb.comp = normal_b * ci.km;
+  lb.gm = -normal_b * vn;
+  double vn_b = -normal_b * ci.gm;
+  // vt = dv - vn n
+  dv_b += vt_b;
+  vn_b -= dot(vt_b, n);
+  n_b -= vn * vt_b;
+  // vn = dv . n
+  dv_b += vn_b * n;
+  n_b += vn_b * dv;
+  lb.dv = dv_b;
+  lb.n = n_b;
+  lb.mu = mu_b;
+}
+
+// Adjoint accumulators of one clump's contact inputs.
+struct ClumpBar {
+  V3 r, v, w;
+  V3 s[4];
+};
+
+// The owner's adjoints from one contact item: centre, velocities and the item's own sphere.
+struct ItemBar {
+  V3 r, v, w, s;
+};
+
+__device__ __forceinline__ ItemBar zero_item() {
+  ItemBar b;
+  b.r = b.v = b.w = b.s = mk(0.0, 0.0, 0.0);
+  return b;
+}
+
+__device__ __forceinline__ void add_item(ClumpBar &ob, const ItemBar &ib, int k) {
+  ob.r += ib.r;
+  ob.v += ib.v;
+  ob.w += ib.w;
+  ob.s[k] += ib.s;
+}
+
+struct ParamBar {
+  double kappa_pp, gamma_pp, mu_pp, kappa_pw, gamma_pw, mu_pw;
+};
+
+// Reverse of one sphere-sphere contact (pair_input + contact law + torque term) of the owner
+// (centre rl, velocities vl, wl, sphere s1 = own sphere k) with partner record m, sphere sm.
+// fb_tot / tb_tot: adjoints of the owner's force and torque sums.  Returns the partner's
+// adjoints in pb (centre, velocities, sphere sm).
+__device__ __forceinline__ void pair_rev(V3 rl, V3 vl, V3 wl, V3 s1, double rad1, double massl, const NbrRec &m,
+                                         int sm, const Consts &c, bool xi0, V3 fb_tot, V3 tb_tot, ItemBar &ob,
+                                         V3 &pr_b, V3 &pv_b, V3 &pw_b, V3 &ps_b, ParamBar &par, bool &any) {
+  any = false;
+  ContactIn ci;
+  if (!pair_input(rl, vl, wl, s1, rad1, massl, m, sm, c, xi0, ci)) return;
+  V3 f;
+  if (!contact_law(ci.dvvc, ci.n, ci.comp, ci.km, ci.gm, ci.mass_t, ci.mu, ci.cns, c.dt, ci.xi0, ci.gate, f))
+    return;
+  any = true;
+  const V3 sp = mk(m.s[3 * sm], m.s[3 * sm + 1], m.s[3 * sm + 2]);
+  const V3 rm = mk(m.rx, m.ry, m.rz), vm_lin = mk(m.vx, m.vy, m.vz), wm = mk(m.wx, m.wy, m.wz);
+  const V3 d = sp - s1;
+  const double dist = sqrt(d.x * d.x + d.y * d.y + d.z * d.z);
+  const V3 n = ci.n, rrc = ci.rrc;
+  const V3 e_l = rrc - rl, e_m = rrc - rm;
+  // F += f; T += e_l x f
+  const V3 f_b = fb_tot + cross(tb_tot, e_l);
+  V3 e_l_b = cross(f, tb_tot);
+  LawBar lb;
+  contact_law_rev(ci, c.dt, f_b, lb);
+  const double meff = 0.5 * (m.msph + massl);
+  par.kappa_pp += lb.km * 0.5 * meff;
+  par.gamma_pp += lb.gm * 0.5 * meff;
+  par.mu_pp += lb.mu;
+  // dv = vm - vl;  vm = vm_lin + wm x e_m;  vl = vl_lin + wl x e_l
+  const V3 vm_b = lb.dv, vl_b = (-1.0) * lb.dv;
+  pv_b = vm_b;
+  pw_b = cross(e_m, vm_b);
+  V3 e_m_b = cross(vm_b, wm);
+  ob.v += vl_b;
+  ob.w += cross(e_l, vl_b);
+  e_l_b += cross(vl_b, wl);
+  // e_l = rrc - rl;  e_m = rrc - rm
+  const V3 rrc_b = e_l_b + e_m_b;
+  ob.r -= e_l_b;
+  pr_b = (-1.0) * e_m_b;
+  // rrc = s1 + rad1 n;  comp = sep - dist;  n = d / dist;  d = sp - s1
+  V3 n_b = lb.n + rad1 * rrc_b;
+  const double dist_b = -lb.comp;
+  const V3 d_b = (1.0 / dist) * (n_b - dot(n, n_b) * n) + dist_b * n;
+  ob.s += rrc_b;
+  ob.s -= d_b;
+  ps_b = d_b;
+}
+
+// Geometry of one wall contact as its routine forms it (the touch the routine keeps), and the
+// map from the adjoints of (contact point, normal, compression) back to the sphere centre.
+__device__ __forceinline__ bool wall_geom(int rt, const Sph &o, const Consts &c, V3 &rrc, V3 &n, double &comp,
+                                          bool &gate, int &touch, double &aux) {
+  const double ri = o.rad;
+  const V3 s = o.s;
+  touch = 0;
+  gate = false;
+  aux = 0.0;
+  double dist;
+  switch (rt) {
+    case R_HOP0: case R_HOP1: case R_HOP2: {
+      if (s.z < kHOP_HEIGHT || s.x > kHOP_WIDTH) return false;
+      const int nw = rt - R_HOP0;
+      if (nw == 0) {
+        dist = s.x - 0.0;
+        if (dist <= ri) { touch = 1; rrc = mk(0.0, s.y, s.z); n = mk(-1.0, 0.0, 0.0); comp = ri - dist; }
+        dist = kHOP_WIDTH - s.x;
+        if (dist <= ri) { touch = 2; rrc = mk(kHOP_WIDTH, s.y, s.z); n = mk(1.0, 0.0, 0.0); comp = ri - dist; }
+      } else if (nw == 1) {
+        dist = s.y - kYHOP_L;
+        if (dist <= ri) { touch = 3; rrc = mk(s.x, kYHOP_L, s.z); n = mk(0.0, -1.0, 0.0); comp = ri - dist; }
+        dist = kYHOP_R - s.y;
+        if (dist <= ri) { touch = 4; rrc = mk(s.x, kYHOP_R, s.z); n = mk(0.0, 1.0, 0.0); comp = ri - dist; }
+      } else {
+        dist = s.z - kHOP_HEIGHT;
+        if (dist <= ri && c.time < 0.0) {
+          touch = 5; rrc = mk(s.x, s.y, kHOP_HEIGHT); n = mk(0.0, 0.0, -1.0); comp = ri - dist;
+        }
+      }
+      return touch != 0;
+    }
+    case R_FUNNEL: {
+      const V3 q = to_slope(s, c.cost, c.sint);
+      if (q.x > kLFUNNEL - ri * c.sinfi) return false;
+      double e = q.y - q.x * c.tanfi;
+      dist = fabs(e) * c.cosfi;
+      if (dist <= ri) {
+        touch = 1; aux = e;
+        rrc = to_lab(mk(q.x + dist * c.sinfi, q.y - dist * c.cosfi, q.z), c.cost, c.sint);
+        n = to_lab(mk(c.sinfi, -c.cosfi, 0.0), c.cost, c.sint);
+        comp = ri - dist;
+      }
+      e = kYFUNNEL - q.y - q.x * c.tanfi;
+      dist = fabs(e) * c.cosfi;
+      if (dist <= ri) {
+        touch = 2; aux = e;
+        rrc = to_lab(mk(q.x + dist * c.sinfi, q.y + dist * c.cosfi, q.z), c.cost, c.sint);
+        n = to_lab(mk(c.sinfi, c.cosfi, 0.0), c.cost, c.sint);
+        comp = ri - dist;
+      }
+      return touch != 0;
+    }
+    case R_FCORNERS: {
+      const double yfun_l = c.dy2, yfun_r = c.side_y + c.dy2, hsy = c.dy2 + c.side_y / 2.0;
+      const V3 q = to_slope(s, c.cost, c.sint);
+      if (q.x < kLFUNNEL - ri * c.sinfi || q.x > kLFUNNEL + ri) return false;
+      if (q.y > yfun_r || q.y < yfun_l) return false;
+      const double yc = (q.y <= hsy) ? yfun_l : yfun_r;
+      const double sep2 = ri * ri;
+      V3 d;
+      d.x = kLFUNNEL - q.x;
+      double dist2 = d.x * d.x;
+      if (dist2 > sep2) return false;
+      d.y = yc - q.y;
+      dist2 += d.y * d.y;
+      if (dist2 > sep2) return false;
+      dist = sqrt(dist2);
+      const V3 nr = mk(d.x / dist, d.y / dist, 0.0);
+      rrc = to_lab(mk(q.x + ri * nr.x, q.y + ri * nr.y, q.z), c.cost, c.sint);
+      n = to_lab(nr, c.cost, c.sint);
+      comp = ri - dist;
+      gate = true;
+      touch = 1;
+      aux = yc;
+      return true;
+    }
+    case R_WALLS: {
+      const double yleft = c.dy2, yright = c.side_y + c.dy2;
+      if (to_slope(s, c.cost, c.sint).x <= kLFUNNEL) return false;
+      dist = s.y - yleft;
+      if (dist <= ri) { touch = 1; rrc = mk(s.x, yleft, s.z); n = mk(0.0, -1.0, 0.0); comp = ri - dist; }
+      dist = yright - s.y;
+      if (dist <= ri) { touch = 2; rrc = mk(s.x, yright, s.z); n = mk(0.0, 1.0, 0.0); comp = ri - dist; }
+      return touch != 0;
+    }
+    case R_FLUME: {
+      const double rect = -c.tant * s.x - s.z;
+      dist = fabs(c.cost * rect);
+      if (!(dist <= ri)) return false;
+      touch = 1;
+      aux = c.cost * rect;
+      rrc = mk(s.x - dist * c.sint, s.y, s.z - dist * c.cost);
+      n = mk(-c.sint, 0.0, -c.cost);
+      comp = ri - dist;
+      return true;
+    }
+  }
+  return false;
+}
+
+__device__ __forceinline__ double sgn(double x) { return x > 0.0 ? 1.0 : (x < 0.0 ? -1.0 : 0.0); }
+
+// Sphere-centre adjoint from the adjoints of the wall contact's point, normal and compression.
+__device__ __forceinline__ V3 wall_geom_rev(int rt, const Sph &o, const Consts &c, int touch, double aux, V3 rrc_b,
+                                           V3 n_b, double comp_b) {
+  const double ri = o.rad;
+  switch (rt) {
+    case R_HOP0: return mk(touch == 1 ? -comp_b : comp_b, rrc_b.y, rrc_b.z);
+    case R_HOP1: return mk(rrc_b.x, touch == 3 ? -comp_b : comp_b, rrc_b.z);
+    case R_HOP2: return mk(rrc_b.x, rrc_b.y, -comp_b);
+    case R_WALLS: return mk(rrc_b.x, touch == 1 ? -comp_b : comp_b, rrc_b.z);
+    case R_FUNNEL: {
+      // q = S s; dist = |e| cosfi; qc = (q.x + dist sinfi, q.y -+ dist cosfi, q.z); rrc = L qc
+      const V3 qc_b = to_slope(rrc_b, c.cost, c.sint);   // L^T = S
+      const double side = touch == 1 ? -1.0 : 1.0;
+      const double dist_b = -comp_b + qc_b.x * c.sinfi + side * qc_b.y * c.cosfi;
+      const double ge = sgn(aux) * c.cosfi;   // d dist / d e
+      // e = q.y - q.x tanfi (touch 1) or 30 - q.y - q.x tanfi (touch 2)
+      const V3 q_b = mk(qc_b.x - dist_b * ge * c.tanfi, qc_b.y + (touch == 1 ? 1.0 : -1.0) * dist_b * ge, qc_b.z);
+      return to_lab(q_b, c.cost, c.sint);   // S^T = L
+    }
+    case R_FCORNERS: {
+      const V3 q = to_slope(o.s, c.cost, c.sint);
+      const double dx = kLFUNNEL - q.x, dy = aux - q.y;
+      const double dist = sqrt(dx * dx + dy * dy);
+      const double nx = dx / dist, ny = dy / dist;
+      const V3 qc_b = to_slope(rrc_b, c.cost, c.sint);
+      const V3 nr_b3 = to_slope(n_b, c.cost, c.sint);
+      const double nrx_b = nr_b3.x + ri * qc_b.x, nry_b = nr_b3.y + ri * qc_b.y;
+      const double dist_b = -comp_b;
+      const double proj = nx * nrx_b + ny * nry_b;
+      const double ddx = (nrx_b - nx * proj) / dist + dist_b * nx;
+      const double ddy = (nry_b - ny * proj) / dist + dist_b * ny;
+      const V3 q_b = mk(qc_b.x - ddx, qc_b.y - ddy, qc_b.z);
+      return to_lab(q_b, c.cost, c.sint);
+    }
+    case R_FLUME: {
+      // rect = -tant s.x - s.z; dist = |cost rect|; rrc = (s.x - dist sint, s.y, s.z - dist cost)
+      const double dist_b = -comp_b - rrc_b.x * c.sint - rrc_b.z * c.cost;
+      const double g = sgn(aux) * c.cost;
+      return mk(rrc_b.x - dist_b * g * c.tant, rrc_b.y, rrc_b.z - dist_b * g);
+    }
+  }
+  return mk(0.0, 0.0, 0.0);
+}
+
+// Reverse of one wall contact of sphere k.
+__device__ __forceinline__ void wall_rev(int rt, const Sph &o, const Consts &c, V3 fb_tot, V3 tb_tot, ItemBar &ob,
+                                         ParamBar &par) {
+  V3 rrc, n;
+  double comp, aux;
+  bool gate;
+  int touch;
+  if (!wall_geom(rt, o, c, rrc, n, comp, gate, touch, aux)) return;
+  ContactIn ci;
+  wall_input(o, rrc, n, comp, c, gate, ci);
+  V3 f;
+  if (!contact_law(ci.dvvc, ci.n, ci.comp, ci.km, ci.gm, ci.mass_t, ci.mu, ci.cns, c.dt, ci.xi0, ci.gate, f)) return;
+  const V3 e = rrc - o.r;
+  const V3 f_b = fb_tot + cross(tb_tot, e);
+  V3 e_b = cross(f, tb_tot);
+  LawBar lb;
+  contact_law_rev(ci, c.dt, f_b, lb);
+  par.kappa_pw += lb.km * 0.5 * o.mwall;
+  par.gamma_pw += lb.gm * 0.5 * o.mwall;
+  par.mu_pw += lb.mu;
+  // dv = -(v + w x e)
+  const V3 vvc_b = (-1.0) * lb.dv;
+  ob.v += vvc_b;
+  ob.w += cross(e, vvc_b);
+  e_b += cross(vvc_b, o.w);
+  // e = rrc - r
+  ob.r -= e_b;
+  ob.s += wall_geom_rev(rt, o, c, touch, aux, e_b, lb.n, lb.comp);
+}
+
+// Adjoint planes (one FP64 plane per scalar).
+enum AdjPlane : int { AR = 0, AV = 3, AW = 6, ARM = 9, AA = 18, AAL = 21, NADJ = 24 };   // state adjoint
+enum AccPlane : int { CR = 0, CV = 3, CW = 6, CS = 9, NACC = 21 };                          // scattered parts
+
+__device__ __forceinline__ void warp_reduce_add(double *dst, double v) {
+  for (int off = 16; off; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  if ((threadIdx.x & 31) == 0 && v != 0.0) atomicAdd(dst, v);
+}
+
+// Every contact of one clump reversed by its own lane (the path of a clump whose item lists
+// would overflow): walls of the phase, then every partner in the neighbour cells.
+__device__ __forceinline__ void adj_contacts_lane(long s, const Own &o, const Consts &c, const af3d_cell_par &g,
+                                                  long long off, double B, V3 Fb, V3 Tb, Planes acc,
+                                                  const NbrRec *__restrict__ nbr, const CullRec *__restrict__ cull,
+                                                  const int *__restrict__ start, const int *__restrict__ order,
+                                                  ClumpBar &ob, ParamBar &par) {
+  const bool aval = c.phase == AF3D_PHASE_AVALANCHE;
+  for (int rt = R_HOP0; rt <= R_FLUME; rt++) {
+    if (!aval && rt > R_HOP2) break;
+    if (!bnd_may_touch(rt, o.r, B, c)) continue;
+    for (int k = 0; k < 4; k++) {
+      ItemBar ib = zero_item();
+      wall_rev(rt, sphere_of(o, k), c, Fb, Tb, ib, par);
+      add_item(ob, ib, k);
+    }
+  }
+  const bool xi0 = c.variant == AF3D_FRICTION_DEV;
+  const CullRec mine = cull[s];
+  const Search q = search_centre(o.r, g, off);
+  for_neighbour_slots(q, g, start, order, [&](int t) {
+    if (t == s) return;
+    unsigned mask = pair_mask(mine, cull[t]);
+    while (mask) {
+      const int p = __ffs(mask) - 1;
+      mask &= mask - 1;
+      const int k = p & 3, sm = p >> 2;
+      V3 pr_b, pv_b, pw_b, ps_b;
+      bool any;
+      ItemBar ib = zero_item();
+      pair_rev(o.r, o.v, o.w, o.s[k], o.rad, o.msph, nbr[t], sm, c, xi0, Fb, Tb, ib, pr_b, pv_b, pw_b, ps_b, par,
+               any);
+      add_item(ob, ib, k);
+      if (any) {
+        atomic_add3(acc, CR, t, pr_b);
+        atomic_add3(acc, CV, t, pv_b);
+        atomic_add3(acc, CW, t, pw_b);
+        atomic_add3(acc, CS + 3 * sm, t, ps_b);
+      }
+    }
+  });
+}
+
+constexpr int kAdjCoopBlock = 64;
+
+// Per-warp shared state of the cooperative reverse: the item lists, every owner's force and
+// torque adjoints, and every owner's contact adjoints (centre, v, w, four spheres) accumulated
+// with shared-memory atomics (a reverse needs no order).
+struct AdjQueue {
+  ItemLists il;
+  double fb[32][6];
+  double own[32][21];
+};
+
+__device__ __forceinline__ void shared_add3(double *p, V3 v) {
+  atomicAdd(p, v.x);
+  atomicAdd(p + 1, v.y);
+  atomicAdd(p + 2, v.z);
+}
+
+// Reverse of finish_Verlet, get_accel and every contact of one clump (startup: the start-up
+// force pass, which has no finish and whose accelerations become a_i of the first step).
+// in: adjoint of the next state; out.a/out.al receive the finish terms of this step's a_i and
+// alpha_i; acc receives (atomically) the adjoints of every clump's r1, v1, w1 and spheres;
+// rb receives this clump's own R1 adjoint.  The contacts run warp-cooperatively: the item lists
+// of the forward pass, 32 items a round, each lane reversing one contact for its owner.
+__global__ void __launch_bounds__(kAdjCoopBlock) k_adj_forces(Planes P, Planes in, Planes out, Planes acc,
+                                                              Planes rb, DevScalars *d, const int *__restrict__ flume,
+                                                              const NbrRec *__restrict__ nbr,
+                                                              const CullRec *__restrict__ cull,
+                                                              const int *__restrict__ start,
+                                                              const int *__restrict__ order,
+                                                              const float4 *__restrict__ csort, double *param_b,
+                                                              int startup, long n) {
+  __shared__ AdjQueue queues[kAdjCoopBlock / 32];
+  AdjQueue &aq = queues[threadIdx.x >> 5];
+  const int lane = threadIdx.x & 31;
+  const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const bool valid = s < n;
+  const long sv = valid ? s : n - 1;
+  const long wbase = blockIdx.x * (long)blockDim.x + (threadIdx.x & ~31u);
+  ParamBar par = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  const int f = flume[sv];
+  const Consts c = load_consts(d, f);
+  const af3d_cell_par g = d->flumes[f].grid;
+  const long long off = d->flumes[f].cell_off;
+  const NbrRec &me = nbr[sv];
+  Own o;
+  o.r = mk(me.rx, me.ry, me.rz);
+  o.v = mk(me.vx, me.vy, me.vz);
+  o.w = mk(me.wx, me.wy, me.wz);
+  for (int k = 0; k < 4; k++) o.s[k] = mk(me.s[3 * k], me.s[3 * k + 1], me.s[3 * k + 2]);
+  o.rad = me.rad; o.msph = me.msph; o.mwall = me.mwall;
+  const bool removed = is_removed(c.time, o.r.x, c.side_x);
+  const bool act = valid && !removed;
+  ClumpBar ob;
+  ob.r = ob.v = ob.w = mk(0.0, 0.0, 0.0);
+  for (int k = 0; k < 4; k++) ob.s[k] = mk(0.0, 0.0, 0.0);
+  V3 Fb = mk(0.0, 0.0, 0.0), Tb = mk(0.0, 0.0, 0.0);
+  if (act) {
+    // finish: v2 = v1 + hdt (a_f - a_i), w2 likewise
+    const V3 v2_b = startup ? mk(0.0, 0.0, 0.0) : ld3(in, AV, s);
+    const V3 w2_b = startup ? mk(0.0, 0.0, 0.0) : ld3(in, AW, s);
+    const V3 af_b = ld3(in, AA, s) + c.hdt * v2_b;
+    const V3 alf_b = ld3(in, AAL, s) + c.hdt * w2_b;
+    if (!startup) {
+      st3(out, AA, s, (-c.hdt) * v2_b);
+      st3(out, AAL, s, (-c.hdt) * w2_b);
+    }
+    ob.v = v2_b;
+    ob.w = w2_b;
+    // get_accel: a_f = F/m - adrag0 |v1| v1 - g z;  alpha_f = R1 (R1^T T) / I (isotropic I)
+    const double m = P.p[MASS][s], I = P.p[IXX][s], adrag0 = P.p[ADRAG][s];
+    Fb = (1.0 / m) * af_b;
+    const double vmag = sqrt(dot(o.v, o.v));
+    if (vmag > 0.0) ob.v -= adrag0 * vmag * af_b + (adrag0 * dot(o.v, af_b) / vmag) * o.v;
+    const V3 Rx = ld3(P, R00, s), Ry = ld3(P, R10, s), Rz = ld3(P, R20, s);
+    const V3 T = ld3(P, TX, s);
+    const V3 tb = mk(T.x * Rx.x + T.y * Ry.x + T.z * Rz.x, T.x * Rx.y + T.y * Ry.y + T.z * Rz.y,
+                     T.x * Rx.z + T.y * Ry.z + T.z * Rz.z);
+    const V3 ab = (1.0 / I) * tb;
+    const V3 ab_b = mk(alf_b.x * Rx.x + alf_b.y * Ry.x + alf_b.z * Rz.x,
+                       alf_b.x * Rx.y + alf_b.y * Ry.y + alf_b.z * Rz.y,
+                       alf_b.x * Rx.z + alf_b.y * Ry.z + alf_b.z * Rz.z);
+    const V3 tb_b = (1.0 / I) * ab_b;
+    Tb = mk(dot(Rx, tb_b), dot(Ry, tb_b), dot(Rz, tb_b));
+    // R1 adjoint: alpha_i = sum_j R_ij ab_j and tb_j = sum_i R_ij T_i
+    V3 RbX = ld3(in, ARM, s), RbY = ld3(in, ARM + 3, s), RbZ = ld3(in, ARM + 6, s);
+    RbX += alf_b.x * ab + T.x * tb_b;
+    RbY += alf_b.y * ab + T.y * tb_b;
+    RbZ += alf_b.z * ab + T.z * tb_b;
+    st3(rb, 0, s, RbX);
+    st3(rb, 3, s, RbY);
+    st3(rb, 6, s, RbZ);
+  } else if (valid) {
+    for (int k = 0; k < 9; k++) rb.p[k][s] = 0.0;
+    if (!startup) {
+      st3(out, AA, s, mk(0.0, 0.0, 0.0));
+      st3(out, AAL, s, mk(0.0, 0.0, 0.0));
+    }
+  }
+  aq.fb[lane][0] = Fb.x; aq.fb[lane][1] = Fb.y; aq.fb[lane][2] = Fb.z;
+  aq.fb[lane][3] = Tb.x; aq.fb[lane][4] = Tb.y; aq.fb[lane][5] = Tb.z;
+  for (int k = 0; k < 21; k++) aq.own[lane][k] = 0.0;
+  // the contacts: the forward pass's item lists, reversed 32 a round
+  const bool aval = c.phase == AF3D_PHASE_AVALANCHE;
+  const double B = (double)cull[sv].c.w;
+  bool slow = false;
+  const int nitems = build_item_lists(aq.il, wbase, sv, act, aval, B, o, c, g, off, cull, start, order, csort, slow);
+  const int total = warp_prefix(nitems, aq.il.base);
+  for (int j0 = 0; j0 < total; j0 += 32) {
+    const int j = j0 + lane;
+    if (j < total) {
+      const int lo = owner_of(aq.il.base, j);
+      const unsigned it = aq.il.items[lo][j - aq.il.base[lo]];
+      const long os = wbase + lo;
+      const NbrRec &om = nbr[os];
+      const int of = flume[os];
+      const Consts co = of == f ? c : load_consts(d, of);
+      const V3 fb_o = mk(aq.fb[lo][0], aq.fb[lo][1], aq.fb[lo][2]);
+      const V3 tb_o = mk(aq.fb[lo][3], aq.fb[lo][4], aq.fb[lo][5]);
+      const V3 rl = mk(om.rx, om.ry, om.rz), vl = mk(om.vx, om.vy, om.vz), wl = mk(om.wx, om.wy, om.wz);
+      ItemBar ib = zero_item();
+      int k;
+      if (it >= kBndItem) {
+        const int rt = (int)((it >> 2) & 7u);
+        k = (int)(it & 3u);
+        Sph q;
+        q.r = rl; q.v = vl; q.w = wl;
+        q.s = mk(om.s[3 * k], om.s[3 * k + 1], om.s[3 * k + 2]);
+        q.rad = om.rad;
+        q.mwall = om.mwall;
+        wall_rev(rt, q, co, fb_o, tb_o, ib, par);
+      } else {
+        const int t = (int)(it >> 4), p = (int)(it & 15u);
+        k = p & 3;
+        const int sm = p >> 2;
+        const V3 s1 = mk(om.s[3 * k], om.s[3 * k + 1], om.s[3 * k + 2]);
+        V3 pr_b, pv_b, pw_b, ps_b;
+        bool any;
+        pair_rev(rl, vl, wl, s1, om.rad, om.msph, nbr[t], sm, co, co.variant == AF3D_FRICTION_DEV, fb_o, tb_o, ib,
+                 pr_b, pv_b, pw_b, ps_b, par, any);
+        if (any) {
+          atomic_add3(acc, CR, t, pr_b);
+          atomic_add3(acc, CV, t, pv_b);
+          atomic_add3(acc, CW, t, pw_b);
+          atomic_add3(acc, CS + 3 * sm, t, ps_b);
+        }
+      }
+      double *ow = aq.own[lo];
+      shared_add3(ow + CR, ib.r);
+      shared_add3(ow + CV, ib.v);
+      shared_add3(ow + CW, ib.w);
+      shared_add3(ow + CS + 3 * k, ib.s);
+    }
+  }
+  __syncwarp();
+  if (act) {
+    if (slow) adj_contacts_lane(s, o, c, g, off, B, Fb, Tb, acc, nbr, cull, start, order, ob, par);
+    const double *ow = aq.own[lane];
+    atomic_add3(acc, CR, s, ob.r + mk(ow[CR], ow[CR + 1], ow[CR + 2]));
+    atomic_add3(acc, CV, s, ob.v + mk(ow[CV], ow[CV + 1], ow[CV + 2]));
+    atomic_add3(acc, CW, s, ob.w + mk(ow[CW], ow[CW + 1], ow[CW + 2]));
+    for (int k = 0; k < 4; k++)
+      atomic_add3(acc, CS + 3 * k, s, ob.s[k] + mk(ow[CS + 3 * k], ow[CS + 3 * k + 1], ow[CS + 3 * k + 2]));
+  }
+  warp_reduce_add(param_b + 0, par.kappa_pp);
+  warp_reduce_add(param_b + 1, par.gamma_pp);
+  warp_reduce_add(param_b + 2, par.mu_pp);
+  warp_reduce_add(param_b + 3, par.kappa_pw);
+  warp_reduce_add(param_b + 4, par.gamma_pw);
+  warp_reduce_add(param_b + 5, par.mu_pw);
+}
+
+// Sphere patterns of init_Verlet.cu:130-142.
+__device__ __forceinline__ V3 pattern(int k) {
+  switch (k) {
+    case 0: return mk(1.0, 1.0, 1.0);
+    case 1: return mk(1.0, -1.0, -1.0);
+    case 2: return mk(-1.0, -1.0, 1.0);
+    default: return mk(-1.0, 1.0, -1.0);
+  }
+}
+
+// Folds the sphere-centre adjoints s_b[k] (s_k = r1 + pos R1 p_k) into r1_b and the rows of R1_b.
+__device__ __forceinline__ void fold_spheres(const Planes &acc, long s, double pos, V3 &r1_b, V3 *Rb) {
+  for (int k = 0; k < 4; k++) {
+    const V3 sb = ld3(acc, CS + 3 * k, s), p = pattern(k);
+    r1_b += sb;
+    Rb[0] += (pos * sb.x) * p;
+    Rb[1] += (pos * sb.y) * p;
+    Rb[2] += (pos * sb.z) * p;
+  }
+}
+
+// Reverse of init_Verlet for one clump: from the adjoints of r1, v1, w1, R1 and the sphere
+// centres (in + acc + rb) to the adjoint of this step's state (out; out.a/out.al already hold
+// the finish terms).  tape: this step's state before the predictor.
+__global__ void __launch_bounds__(kAdjBlock) k_adj_predict(Planes P, Planes tape, Planes in, Planes out, Planes acc,
+                                                           Planes rb, DevScalars *d, const int *__restrict__ flume,
+                                                           long n) {
+  const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const DevFlume &fl = d->flumes[flume[s]];
+  const double dt = fl.sys.dt, hdt = fl.sys.hdt;
+  const V3 r = ld3(tape, AR, s), w = ld3(tape, AW, s), al = ld3(tape, AAL, s);
+  if (is_removed(d->time_prev, r.x, fl.sys.side.x)) {
+    for (int k = 0; k < NADJ; k++) out.p[k][s] = 0.0;
+    return;
+  }
+  double R[3][3];
+  for (int i = 0; i < 3; i++) {
+    const V3 row = ld3(tape, ARM + 3 * i, s);
+    R[i][0] = row.x; R[i][1] = row.y; R[i][2] = row.z;
+  }
+  V3 r1_b = ld3(in, AR, s) + ld3(acc, CR, s);
+  const V3 v1_b = ld3(acc, CV, s), w1_b = ld3(acc, CW, s);
+  V3 Rb3[3] = {ld3(rb, 0, s), ld3(rb, 3, s), ld3(rb, 6, s)};
+  fold_spheres(acc, s, P.p[RAD][s] / kROOT2, r1_b, Rb3);
+  double R1b[3][3];
+  for (int i = 0; i < 3; i++) {
+    R1b[i][0] = Rb3[i].x; R1b[i][1] = Rb3[i].y; R1b[i][2] = Rb3[i].z;
+  }
+  // forward re-evaluation of the rotation update
+  const V3 dO = mk(dt * (w.x + hdt * al.x), dt * (w.y + hdt * al.y), dt * (w.z + hdt * al.z));
+  const double mag = sqrt(dO.x * dO.x + dO.y * dO.y + dO.z * dO.z);
+  double dR[3][3];
+  V3 u = mk(0.0, 0.0, 0.0);
+  double c = 1.0, sn = 0.0, omc = 0.0;
+  if (mag > 0.0) {
+    u = mk(dO.x / mag, dO.y / mag, dO.z / mag);
+    c = cos(mag);
+    sn = sin(mag);
+    omc = 1.0 - c;
+    const double uu[3] = {u.x, u.y, u.z};
+    const double ux[3][3] = {{0.0, -u.z, u.y}, {u.z, 0.0, -u.x}, {-u.y, u.x, 0.0}};
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) dR[i][j] = omc * uu[i] * uu[j] + (i == j ? c : 0.0) + sn * ux[i][j];
+  } else {
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) dR[i][j] = i == j ? 1.0 : 0.0;
+  }
+  double T[3][3], nrm[3];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) T[i][j] = dR[i][0] * R[0][j] + dR[i][1] * R[1][j] + dR[i][2] * R[2][j];
+  for (int j = 0; j < 3; j++) nrm[j] = sqrt(T[0][j] * T[0][j] + T[1][j] * T[1][j] + T[2][j] * T[2][j]);
+  // column normalisation R1_ij = T_ij / n_j
+  double Tb[3][3];
+  for (int j = 0; j < 3; j++) {
+    double sj = 0.0;
+    for (int i = 0; i < 3; i++) sj += R1b[i][j] * (T[i][j] / nrm[j]);
+    for (int i = 0; i < 3; i++) Tb[i][j] = (R1b[i][j] - (T[i][j] / nrm[j]) * sj) / nrm[j];
+  }
+  // T = dR R
+  double G[3][3], Rb0[3][3];
+  for (int i = 0; i < 3; i++)
+    for (int k = 0; k < 3; k++) {
+      G[i][k] = Tb[i][0] * R[k][0] + Tb[i][1] * R[k][1] + Tb[i][2] * R[k][2];
+      Rb0[i][k] = dR[0][i] * Tb[0][k] + dR[1][i] * Tb[1][k] + dR[2][i] * Tb[2][k];
+    }
+  // dR = c I + sn [u]x + (1 - c) u u^T,  u = dO / |dO|,  c = cos |dO|,  sn = sin |dO|
+  const V3 skew = mk(G[2][1] - G[1][2], G[0][2] - G[2][0], G[1][0] - G[0][1]);
+  V3 dO_b;
+  if (mag > 0.0) {
+    const double uu[3] = {u.x, u.y, u.z};
+    double c_b = G[0][0] + G[1][1] + G[2][2], ub[3];
+    for (int i = 0; i < 3; i++) {
+      double a2 = 0.0;
+      for (int j = 0; j < 3; j++) {
+        c_b -= G[i][j] * uu[i] * uu[j];
+        a2 += (G[i][j] + G[j][i]) * uu[j];
+      }
+      ub[i] = omc * a2;
+    }
+    const double sn_b = dot(u, skew);
+    ub[0] += sn * skew.x;
+    ub[1] += sn * skew.y;
+    ub[2] += sn * skew.z;
+    const double mag_b = -sn * c_b + c * sn_b;
+    const V3 u_b = mk(ub[0], ub[1], ub[2]);
+    dO_b = (1.0 / mag) * (u_b - dot(u, u_b) * u) + mag_b * u;
+  } else {
+    dO_b = skew;   // dR = I + [dO]x to first order
+  }
+  // r1 = r + dt (v + hdt a);  v1 = v + dt a;  w1 = w + dt al;  dO = dt (w + hdt al)
+  st3(out, AR, s, r1_b);
+  st3(out, AV, s, dt * r1_b + v1_b);
+  st3(out, AA, s, ld3(out, AA, s) + (dt * hdt) * r1_b + dt * v1_b);
+  st3(out, AW, s, w1_b + dt * dO_b);
+  st3(out, AAL, s, ld3(out, AAL, s) + dt * w1_b + (dt * hdt) * dO_b);
+  for (int i = 0; i < 3; i++) st3(out, ARM + 3 * i, s, mk(Rb0[i][0], Rb0[i][1], Rb0[i][2]));
+}
+
+// The start-up force pass (no predictor): the adjoint of the initial state is in + the pass's
+// contributions (acc, rb, sphere centres).
+__global__ void k_adj_startup(Planes P, Planes in, Planes out, Planes acc, Planes rb, long n) {
+  const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  V3 r_b = ld3(in, AR, s) + ld3(acc, CR, s);
+  V3 Rb3[3] = {ld3(rb, 0, s), ld3(rb, 3, s), ld3(rb, 6, s)};
+  fold_spheres(acc, s, P.p[RAD][s] / kROOT2, r_b, Rb3);
+  st3(out, AR, s, r_b);
+  st3(out, AV, s, ld3(in, AV, s) + ld3(acc, CV, s));
+  st3(out, AW, s, ld3(in, AW, s) + ld3(acc, CW, s));
+  for (int i = 0; i < 3; i++) st3(out, ARM + 3 * i, s, Rb3[i]);
+  st3(out, AA, s, mk(0.0, 0.0, 0.0));
+  st3(out, AAL, s, mk(0.0, 0.0, 0.0));
+}
+
+// Objective sums: mass-weighted downslope position sum_m x_rot and total mass.
+__global__ void k_adj_objective(Planes P, DevScalars *d, const int *__restrict__ flume, double *sums, long n) {
+  const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  double mx = 0.0, m = 0.0;
+  if (s < n) {
+    const af3d_system_par &sy = d->flumes[flume[s]].sys;
+    m = P.p[MASS][s];
+    mx = m * (P.p[RX][s] * sy.cost - P.p[RZ][s] * sy.sint);
+  }
+  warp_reduce_add(sums, mx);
+  warp_reduce_add(sums + 1, m);
+}
+
+// Seed: the adjoint of the final state for J = sum_m x_rot / sum_m.
+__global__ void k_adj_seed(Planes P, Planes adj, DevScalars *d, const int *__restrict__ flume, double mass_total,
+                           long n) {
+  const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const af3d_system_par &sy = d->flumes[flume[s]].sys;
+  const double w = P.p[MASS][s] / mass_total;
+  for (int k = 0; k < NADJ; k++) adj.p[k][s] = 0.0;
+  st3(adj, AR, s, mk(w * sy.cost, 0.0, -w * sy.sint));
+}
+
+// The state of a step (r, v, w, R, a_i, alpha_i; with spheres also the four sphere centres)
+// between the planes and a tape slot.  The steps recompute the sphere centres from r and R; the
+// start-up force pass reads them as they are.
+__global__ void k_state_copy(Planes P, Planes tape, int to_tape, int nplanes, long n) {
+  const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const int src[NADJ + 12] = {RX, RY, RZ, VX, VY, VZ, WX, WY, WZ, R00, R01, R02, R10, R11, R12, R20, R21, R22,
+                              AIX, AIY, AIZ, ALIX, ALIY, ALIZ, S0X, S0Y, S0Z, S1X, S1Y, S1Z, S2X, S2Y, S2Z,
+                              S3X, S3Y, S3Z};
+  for (int k = 0; k < nplanes; k++) {
+    if (to_tape) tape.p[k][s] = P.p[src[k]][s];
+    else P.p[src[k]][s] = tape.p[k][s];
+  }
+}
+
+inline unsigned blocks(long n) { return (unsigned)((n + kAdjBlock - 1) / kAdjBlock); }
+
+}  // namespace
+
+void launch_adj_forces(const Launch &L, Planes P, Planes in, Planes out, Planes acc, Planes rb, DevScalars *d,
+                       const int *flume, const NbrRec *nbr, const CullRec *cull, const int *start, const int *order,
+                       const float4 *csort, double *param_b, bool startup) {
+  if (L.n <= 0) return;
+  const unsigned nb = (unsigned)((L.n + kAdjCoopBlock - 1) / kAdjCoopBlock);
+  k_adj_forces<<<nb, kAdjCoopBlock, 0, L.st>>>(P, in, out, acc, rb, d, flume, nbr, cull, start, order, csort, param_b,
+                                               startup ? 1 : 0, L.n);
+}
+
+void launch_adj_predict(const Launch &L, Planes P, Planes tape, Planes in, Planes out, Planes acc, Planes rb,
+                        DevScalars *d, const int *flume) {
+  if (L.n <= 0) return;
+  k_adj_predict<<<blocks(L.n), kAdjBlock, 0, L.st>>>(P, tape, in, out, acc, rb, d, flume, L.n);
+}
+
+void launch_adj_startup(const Launch &L, Planes P, Planes in, Planes out, Planes acc, Planes rb) {
+  if (L.n <= 0) return;
+  k_adj_startup<<<blocks(L.n), kAdjBlock, 0, L.st>>>(P, in, out, acc, rb, L.n);
+}
+
+void launch_adj_objective(const Launch &L, Planes P, DevScalars *d, const int *flume, double *sums) {
+  if (L.n <= 0) return;
+  k_adj_objective<<<blocks(L.n), kAdjBlock, 0, L.st>>>(P, d, flume, sums, L.n);
+}
+
+void launch_adj_seed(const Launch &L, Planes P, Planes adj, DevScalars *d, const int *flume, double mass_total) {
+  if (L.n <= 0) return;
+  k_adj_seed<<<blocks(L.n), kAdjBlock, 0, L.st>>>(P, adj, d, flume, mass_total, L.n);
+}
+
+void launch_state_copy(const Launch &L, Planes P, Planes tape, bool to_tape, bool spheres) {
+  if (L.n <= 0) return;
+  k_state_copy<<<blocks(L.n), kAdjBlock, 0, L.st>>>(P, tape, to_tape ? 1 : 0, spheres ? NADJ + 12 : NADJ, L.n);
+}
+
+}  // namespace af3d

@@ -282,16 +282,16 @@ void enqueue_cell_build(af3d_ctx *c, bool predict, bool t_prev, bool ft = true) 
 // finish_Verlet, and the acceleration swap.  With `resort` the planes are permuted into the new
 // (cell, id) order; otherwise the predictor writes the records at the clumps' own slots, the
 // force pass reaches the sorted order through cells.perm and corrects the velocities in place.
-void enqueue_fused_step(af3d_ctx *c, bool resort) {
+void enqueue_fused_step(af3d_ctx *c, bool resort, bool write_ft = false) {
   launch_advance_time(c->st, c->d);
   if (resort) {
     enqueue_cell_build(c, true, true, false);   // F, T and a_f are rewritten before being read
-    forces_for(c, false, nullptr, c->alt);
+    forces_for(c, write_ft, nullptr, c->alt);
     swap_velocity_planes(c->cur, c->alt);
   } else {
     predict_for(c, true, true, true, true);
     launch_sort(c->L(), c->d, c->cells, c->id_cur, c->ntags, c->cull);
-    forces_for(c, false, c->cells.perm, c->cur);
+    forces_for(c, write_ft, c->cells.perm, c->cur);
   }
   swap_accel_planes(c->cur);
   swap_accel_planes(c->alt);
@@ -1066,4 +1066,193 @@ extern "C" af3d_status af3d_contact_pairs_noalloc(af3d_ctx *c, long *out, long c
   AF3D_CUDA(cudaGetLastError());
   if (count) *count = (long)cnt;
   return AF3D_OK;
+}
+
+// ---- adjoint of the exact step ----------------------------------------------------------------
+namespace {
+
+// Device buffers of the adjoint run, freed on every exit path.
+struct AdjBuffers {
+  std::vector<void *> owned;
+  ~AdjBuffers() {
+    for (void *p : owned) cudaFree(p);
+  }
+  cudaError_t planes(int k, long n, Planes &P) {
+    double *base = nullptr;
+    const cudaError_t e = cudaMalloc((void **)&base, sizeof(double) * (size_t)k * (size_t)n);
+    if (e != cudaSuccess) return e;
+    owned.push_back(base);
+    for (int i = 0; i < NPLANES; i++) P.p[i] = i < k ? base + (size_t)i * n : nullptr;
+    return cudaSuccess;
+  }
+};
+
+af3d_status set_device_time(af3d_ctx *c, double t) {
+  AF3D_CUDA(cudaMemcpyAsync(&c->d->time, &t, sizeof(double), cudaMemcpyHostToDevice, c->st));
+  return AF3D_OK;
+}
+
+// The start-up force pass without moving the slots: keys and records at the current positions,
+// the sort, and every force of the phase into F, T and a_f.
+void enqueue_startup_pass(af3d_ctx *c) {
+  predict_for(c, false, true, false, true);
+  launch_sort(c->L(), c->d, c->cells, c->id_cur, c->ntags, c->cull);
+  forces_for(c, true, c->cells.perm, c->alt);   // corrected velocities go to the dead set
+}
+
+// This step's cell structure at the recomputed predicted state (records, keys, sort).
+void enqueue_step_cells(af3d_ctx *c) {
+  launch_advance_time(c->st, c->d);
+  predict_for(c, true, true, true, true);
+  launch_sort(c->L(), c->d, c->cells, c->id_cur, c->ntags, c->cull);
+}
+
+// The torque sums of a step between the plane set and planes 24..26 of its tape slot.
+af3d_status copy_torque(af3d_ctx *c, Planes &tape, bool to_tape) {
+  for (int k = 0; k < 3; k++) {
+    double *a = tape.p[kAdjPlanes + k], *b = c->cur.p[TX + k];
+    AF3D_CUDA(cudaMemcpyAsync(to_tape ? a : b, to_tape ? b : a, sizeof(double) * c->n, cudaMemcpyDeviceToDevice,
+                              c->st));
+  }
+  return AF3D_OK;
+}
+
+}  // namespace
+
+extern "C" af3d_status af3d_adjoint(af3d_ctx *c, long steps, long ckpt_every, double *J, double *param_grad,
+                                    af3d_vec3 *dr0, double *dR0, af3d_vec3 *dv0, af3d_vec3 *dw0) {
+  CHECK_STATE(c);
+  if (steps < 0 || ckpt_every <= 0 || !J) return fail(AF3D_ERR_ARG, "bad argument");
+  if (c->nflumes != 1) return fail(AF3D_ERR_ARG, "the adjoint runs one flume per context");
+  if (!c->have_grid) return fail(AF3D_ERR_ARG, "no grid");
+  const long n = c->n;
+  const bool want_grad = param_grad || dr0 || dR0 || dv0 || dw0;
+  const int mode = c->fp_mode;
+  c->fp_mode = AF3D_FP_EXACT;   // the adjoint differentiates the exact step
+  struct ModeBack {
+    af3d_ctx *c;
+    int m;
+    ~ModeBack() { c->fp_mode = m; }
+  } mode_back{c, mode};
+  drop_graphs(c);
+  const long nck = steps / ckpt_every + 1;
+  AdjBuffers buf;
+  Planes state0{}, fin{}, adjA{}, adjB{}, acc{}, rb{};
+  std::vector<Planes> ckpt(nck), tape(want_grad ? std::min(ckpt_every, std::max<long>(steps, 1)) : 0);
+  cudaError_t e = buf.planes(kAdjPlanes + 12, n, state0);   // with the sphere centres
+  if (e == cudaSuccess) e = buf.planes(kAdjPlanes + 12, n, fin);
+  for (long k = 0; k < nck && e == cudaSuccess && want_grad; k++) e = buf.planes(kAdjPlanes, n, ckpt[k]);
+  for (size_t k = 0; k < tape.size() && e == cudaSuccess; k++) e = buf.planes(kAdjPlanes + 3, n, tape[k]);
+  if (want_grad && e == cudaSuccess) e = buf.planes(kAdjPlanes, n, adjA);
+  if (want_grad && e == cudaSuccess) e = buf.planes(kAdjPlanes, n, adjB);
+  if (want_grad && e == cudaSuccess) e = buf.planes(kAccPlanes, n, acc);
+  if (want_grad && e == cudaSuccess) e = buf.planes(kRbPlanes, n, rb);
+  double *dsc = nullptr;   // [0..1] objective sums, [2..7] parameter adjoints
+  if (e == cudaSuccess) e = cudaMalloc((void **)&dsc, sizeof(double) * 8);
+  if (e == cudaSuccess) buf.owned.push_back(dsc);
+  if (e != cudaSuccess) return fail(AF3D_ERR_NOMEM, std::string("adjoint buffers: ") + cudaGetErrorString(e));
+  AF3D_CUDA(cudaMemsetAsync(dsc, 0, sizeof(double) * 8, c->st));
+
+  // Forward: the start-up force pass (a_i of the first step), then `steps` steps keeping the
+  // slot order, the state saved every ckpt_every steps.
+  const double t_init = c->time, dt = c->sys[0].dt;
+  launch_state_copy(c->L(), c->cur, state0, true, true);
+  enqueue_startup_pass(c);
+  swap_accel_planes(c->cur);
+  swap_accel_planes(c->alt);
+  std::vector<double> t_start(steps + 1);
+  double t = t_init;
+  for (long k = 0; k < steps; k++) {
+    if (want_grad && k % ckpt_every == 0) launch_state_copy(c->L(), c->cur, ckpt[k / ckpt_every], true);
+    t_start[k] = t;
+    enqueue_fused_step(c, false);
+    t = t + dt;
+  }
+  t_start[steps] = t;
+  c->time = t;
+  launch_state_copy(c->L(), c->cur, fin, true, true);
+  launch_adj_objective(c->L(), c->cur, c->d, c->fl_cur, dsc);
+  double sums[2] = {0.0, 0.0};
+  AF3D_CUDA(cudaMemcpyAsync(sums, dsc, sizeof(sums), cudaMemcpyDeviceToHost, c->st));
+  int flags = 0;
+  af3d_status s = read_status(c, &flags);
+  if (s) return s;
+  s = first_error(flags);
+  if (s) return s;
+  *J = sums[1] > 0.0 ? sums[0] / sums[1] : 0.0;
+
+  if (want_grad && n > 0) {
+    launch_adj_seed(c->L(), c->cur, adjA, c->d, c->fl_cur, sums[1]);
+    for (long seg = (steps - 1) / ckpt_every; steps > 0 && seg >= 0; seg--) {
+      const long k0 = seg * ckpt_every, k1 = std::min(steps, k0 + ckpt_every);
+      // recompute the segment, keeping every step's starting state
+      launch_state_copy(c->L(), c->cur, ckpt[seg], false);
+      s = set_device_time(c, t_start[k0]);
+      if (s) return s;
+      for (long k = k0; k < k1; k++) {
+        launch_state_copy(c->L(), c->cur, tape[k - k0], true);
+        enqueue_fused_step(c, false, true);
+        s = copy_torque(c, tape[k - k0], true);
+        if (s) return s;
+      }
+      // then each step backwards: its cell structure again, its torques from the tape
+      for (long k = k1 - 1; k >= k0; k--) {
+        launch_state_copy(c->L(), c->cur, tape[k - k0], false);
+        s = copy_torque(c, tape[k - k0], false);
+        if (s) return s;
+        s = set_device_time(c, t_start[k]);
+        if (s) return s;
+        enqueue_step_cells(c);
+        AF3D_CUDA(cudaMemsetAsync(acc.p[0], 0, sizeof(double) * kAccPlanes * n, c->st));   // one block
+        launch_adj_forces(c->L(), c->cur, adjA, adjB, acc, rb, c->d, c->fl_cur, c->nbr, c->cull, c->cells.start,
+                          c->cells.perm, c->cells.csort, dsc + 2, false);
+        launch_adj_predict(c->L(), c->cur, tape[k - k0], adjA, adjB, acc, rb, c->d, c->fl_cur);
+        std::swap(adjA, adjB);
+      }
+    }
+    // the start-up pass backwards
+    launch_state_copy(c->L(), c->cur, state0, false, true);
+    s = set_device_time(c, t_init);
+    if (s) return s;
+    enqueue_startup_pass(c);
+    AF3D_CUDA(cudaMemsetAsync(acc.p[0], 0, sizeof(double) * kAccPlanes * n, c->st));
+    launch_adj_forces(c->L(), c->cur, adjA, adjB, acc, rb, c->d, c->fl_cur, c->nbr, c->cull, c->cells.start,
+                      c->cells.perm, c->cells.csort, dsc + 2, true);
+    launch_adj_startup(c->L(), c->cur, adjA, adjB, acc, rb);
+    // gradients by clump id
+    std::vector<double> h((size_t)kAdjPlanes * n);
+    std::vector<long long> ids(n);
+    for (int p = 0; p < kAdjPlanes; p++)
+      AF3D_CUDA(cudaMemcpyAsync(h.data() + (size_t)p * n, adjB.p[p], sizeof(double) * n, cudaMemcpyDeviceToHost,
+                                c->st));
+    AF3D_CUDA(cudaMemcpyAsync(ids.data(), c->id_cur, sizeof(long long) * n, cudaMemcpyDeviceToHost, c->st));
+    double pg[6];
+    AF3D_CUDA(cudaMemcpyAsync(pg, dsc + 2, sizeof(pg), cudaMemcpyDeviceToHost, c->st));
+    AF3D_CUDA(cudaStreamSynchronize(c->st));
+    if (param_grad)
+      for (int k = 0; k < 6; k++) param_grad[k] = pg[k];
+    for (long sl = 0; sl < n; sl++) {
+      const long long i = ids[sl];
+      auto at = [&](int p) { return h[(size_t)p * n + sl]; };
+      if (dr0) dr0[i] = {at(0), at(1), at(2)};
+      if (dv0) dv0[i] = {at(3), at(4), at(5)};
+      if (dw0) dw0[i] = {at(6), at(7), at(8)};
+      if (dR0)
+        for (int k = 0; k < 9; k++) dR0[9 * i + k] = at(9 + k);
+    }
+  }
+  // leave the context at the final state of the forward run
+  launch_state_copy(c->L(), c->cur, fin, false, true);
+  s = set_device_time(c, t);
+  if (s) return s;
+  AF3D_CUDA(cudaStreamSynchronize(c->st));
+  c->sorted = false;
+  c->records_valid = false;
+  c->cells_valid = false;
+  c->since_sort = kResortEvery;
+  c->cc += steps;
+  flags = 0;
+  s = read_status(c, &flags);
+  if (s) return s;
+  return first_error(flags);
 }

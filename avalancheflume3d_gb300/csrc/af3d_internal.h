@@ -154,6 +154,21 @@ void launch_cells_by_id (const Launch &L, const int *key, const long long *id, D
 // DFMA throughput microbenchmark (TFLOP/s, 2 flops per DFMA), bounded to ~0.1 s.
 cudaError_t measure_dfma (int sms, double *tflops);
 
+// Adjoint of the exact step (af3d_adjoint.cu).  Planes of 24 state adjoints (r, v, w, R rows,
+// a_i, alpha_i), 21 scattered parts (r1, v1, w1, sphere centres), 9 own R1 parts.
+constexpr int kAdjPlanes = 24, kAccPlanes = 21, kRbPlanes = 9;
+void launch_adj_forces (const Launch &L, Planes P, Planes in, Planes out, Planes acc, Planes rb, DevScalars *d,
+                        const int *flume, const NbrRec *nbr, const CullRec *cull, const int *start,
+                        const int *order, const float4 *csort, double *param_b, bool startup);
+void launch_adj_predict (const Launch &L, Planes P, Planes tape, Planes in, Planes out, Planes acc, Planes rb,
+                         DevScalars *d, const int *flume);
+void launch_adj_startup (const Launch &L, Planes P, Planes in, Planes out, Planes acc, Planes rb);
+void launch_adj_objective (const Launch &L, Planes P, DevScalars *d, const int *flume, double *sums);
+void launch_adj_seed (const Launch &L, Planes P, Planes adj, DevScalars *d, const int *flume, double mass_total);
+// The 24 state planes (with spheres: 36, the sphere centres too) between the plane set and a
+// tape slot (to_tape: planes -> tape).
+void launch_state_copy (const Launch &L, Planes P, Planes tape, bool to_tape, bool spheres = false);
+
 // The predictor and the fused force pass of the fast FP64 mode (af3d_kernels.cu compiled with
 // -DAF3D_FAST -fmad=true; same arguments as above).
 namespace fast {

@@ -193,6 +193,26 @@ class Engine:
         """k fused steps of the current phase (CUDA-graph replay, re-grid every 2000 steps)."""
         self._call("af3d_step", int(k))
 
+    # ---- adjoint ----
+    def adjoint(self, steps: int, ckpt_every: int = 500, gradients: bool = True) -> dict:
+        """Start-up force pass + `steps` exact steps from the imported state, J = mass-weighted
+        mean downslope position at the end and (gradients=True) dJ/d(parameters, initial state)
+        from the hand-written adjoint (af3d_adjoint).  Leaves the context at the final state."""
+        J = C.c_double()
+        out = {}
+        if gradients:
+            pg = np.zeros(6)
+            dr, dv, dw = _vec3(self.n), _vec3(self.n), _vec3(self.n)
+            dR = np.zeros((self.n, 9))
+            self._call("af3d_adjoint", int(steps), int(ckpt_every), C.byref(J), ptr(pg), ptr(dr), ptr(dR), ptr(dv),
+                       ptr(dw))
+            out.update(params=dict(zip(("kappa_pp", "gamma_pp", "mu_pp", "kappa_pw", "gamma_pw", "mu_pw"), pg)),
+                       r0=dr, v0=dv, w0=dw, R0=dR.reshape(-1, 3, 3))
+        else:
+            self._call("af3d_adjoint", int(steps), int(ckpt_every), C.byref(J), None, None, None, None, None)
+        out["J"] = J.value
+        return out
+
     # ---- diagnostics (indexed by clump id) ----
     def status(self) -> int:
         f = C.c_int()

@@ -72,6 +72,9 @@ def parse_args():
     p.add_argument("--ensemble-steps", type=int, default=64)
     p.add_argument("--ensemble-seq-flumes", type=int, default=64,
                    help="flumes timed one after another as plain runs (every k-th of the ensemble)")
+    p.add_argument("--adjoint-steps", type=int, default=1000,
+                   help="steps of the adjoint measurement (0 skips it)")
+    p.add_argument("--adjoint-ckpt", type=int, default=500)
     p.add_argument("--trace-contacts", type=int, default=0,
                    help="print active contacts every this many pre-roll steps (diagnostic)")
     return p.parse_args()
@@ -288,6 +291,51 @@ def measure_ensemble(args, stream):
             "geometry": "40 cm x 4 cm flume, reference hopper and funnel; per-flume slope 25-40 deg"}
 
 
+def measure_adjoint(args, stream):
+    """Adjoint/forward cost on the adjoint configuration: 32,768 clumps, 80 cm x 4 cm flume at 35
+    deg, dense bed layer, exact FP64 (the mode the adjoint differentiates).  Forward: K fused steps
+    (graph replay).  Adjoint: af3d_adjoint over the same K steps from the same state (start-up
+    pass, forward with checkpoints every C steps, segment recompute, reverse), timed end to end."""
+    import torch
+    from avalancheflume3d_gb300 import Engine, FP_EXACT
+    from avalancheflume3d_gb300.workloads import flume_2k, flume_state
+    cfg = flume_2k(n=32768, tilt_deg=35.0, Lflume=80.0, layout="bed")
+    sys_, fun, pp = flume_state(cfg)
+    K = args.adjoint_steps
+
+    def events():
+        return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    with Engine(sys_, fun, stream=stream.cuda_stream, fp_mode=FP_EXACT) as eng:
+        eng.import_particles(pp)
+        eng.forces()
+        eng.swap_accel()
+        eng.step(K)                      # warm-up (captures the graphs)
+        torch.cuda.synchronize()
+        e0, e1 = events()
+        e0.record(stream)
+        eng.step(K)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t_fwd = e0.elapsed_time(e1) / 1e3
+    with Engine(sys_, fun, stream=stream.cuda_stream) as eng:
+        eng.import_particles(pp)
+        eng.adjoint(min(K, 2 * args.adjoint_ckpt), args.adjoint_ckpt)   # warm-up
+    with Engine(sys_, fun, stream=stream.cuda_stream) as eng:
+        eng.import_particles(pp)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = eng.adjoint(K, args.adjoint_ckpt)
+        torch.cuda.synchronize()
+        t_adj = time.perf_counter() - t0
+    return {"workload": "flume 32,768 clumps, 80 cm x 4 cm at 35 deg, dense bed layer, exact FP64",
+            "steps": K, "ckpt_every": args.adjoint_ckpt, "ms_per_step_forward": 1e3 * t_fwd / K,
+            "ms_per_step_adjoint": 1e3 * t_adj / K, "adjoint_over_forward": t_adj / t_fwd,
+            "what": "adjoint = the whole af3d_adjoint call (forward with checkpoints, segment recompute, "
+                    "reverse, gradient gather) per step, over a graph-replayed exact forward step",
+            "J": out["J"], "dJ_dparams": out["params"]}
+
+
 def time_other_mode(eng, modes, other, args, stream, R, dev, world):
     """K steps of the other FP64 mode on the same state (after the timed region)."""
     import torch
@@ -426,6 +474,9 @@ def run_engine(args):
     ens = None
     if world == 1 and args.ensemble_flumes > 0:
         ens = measure_ensemble(args, stream)
+    adj = None
+    if world == 1 and args.adjoint_steps > 0:
+        adj = measure_adjoint(args, stream)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -460,6 +511,7 @@ def run_engine(args):
             "fp64": {"peak_tflops": fp64.value, "peak_source": "measured DFMA microbenchmark"},
             "phase_ms": {k: float(v) for k, v in zip(names, prof)},
             "ensemble": ens,
+            "adjoint": adj,
             "cpu_baseline": cpu,
             "clocks": clk,
         }
