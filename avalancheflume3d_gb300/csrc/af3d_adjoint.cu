@@ -404,6 +404,25 @@ __device__ __forceinline__ void warp_reduce_add(double *dst, double v) {
   if ((threadIdx.x & 31) == 0 && v != 0.0) atomicAdd(dst, v);
 }
 
+// Adds every lane's value into dst[6 f + k] for the lane's flume f: one warp reduction when the
+// warp's lanes share a flume, else one atomic per lane.  All 32 lanes call this.
+__device__ __forceinline__ void add_params(double *dst, int f, const ParamBar &p) {
+  const double v[6] = {p.kappa_pp, p.gamma_pp, p.mu_pp, p.kappa_pw, p.gamma_pw, p.mu_pw};
+  const int f0 = __shfl_sync(0xffffffffu, f, 0);
+  if (__all_sync(0xffffffffu, f == f0)) {
+    for (int k = 0; k < 6; k++) warp_reduce_add(dst + 6 * f0 + k, v[k]);
+  } else {
+    for (int k = 0; k < 6; k++)
+      if (v[k] != 0.0) atomicAdd(dst + 6 * f + k, v[k]);
+  }
+}
+
+__device__ __forceinline__ void flush_params(double *dst, int f, const ParamBar &p) {
+  const double v[6] = {p.kappa_pp, p.gamma_pp, p.mu_pp, p.kappa_pw, p.gamma_pw, p.mu_pw};
+  for (int k = 0; k < 6; k++)
+    if (v[k] != 0.0) atomicAdd(dst + 6 * f + k, v[k]);
+}
+
 // Every contact of one clump reversed by its own lane (the path of a clump whose item lists
 // would overflow): walls of the phase, then every partner in the neighbour cells.
 __device__ __forceinline__ void adj_contacts_lane(long s, const Own &o, const Consts &c, const af3d_cell_par &g,
@@ -567,6 +586,7 @@ __global__ void __launch_bounds__(kAdjCoopBlock) k_adj_forces(Planes P, Planes i
       const V3 tb_o = mk(aq.fb[lo][3], aq.fb[lo][4], aq.fb[lo][5]);
       const V3 rl = mk(om.rx, om.ry, om.rz), vl = mk(om.vx, om.vy, om.vz), wl = mk(om.wx, om.wy, om.wz);
       ItemBar ib = zero_item();
+      ParamBar ipar = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};   // this item's; the lane's flume or the owner's
       int k;
       if (it >= kBndItem) {
         const int rt = (int)((it >> 2) & 7u);
@@ -576,7 +596,7 @@ __global__ void __launch_bounds__(kAdjCoopBlock) k_adj_forces(Planes P, Planes i
         q.s = mk(om.s[3 * k], om.s[3 * k + 1], om.s[3 * k + 2]);
         q.rad = om.rad;
         q.mwall = om.mwall;
-        wall_rev(rt, q, co, fb_o, tb_o, ib, par);
+        wall_rev(rt, q, co, fb_o, tb_o, ib, ipar);
       } else {
         const int t = (int)(it >> 4), p = (int)(it & 15u);
         k = p & 3;
@@ -585,13 +605,19 @@ __global__ void __launch_bounds__(kAdjCoopBlock) k_adj_forces(Planes P, Planes i
         V3 pr_b, pv_b, pw_b, ps_b;
         bool any;
         pair_rev(rl, vl, wl, s1, om.rad, om.msph, nbr[t], sm, co, co.variant == AF3D_FRICTION_DEV, fb_o, tb_o, ib,
-                 pr_b, pv_b, pw_b, ps_b, par, any);
+                 pr_b, pv_b, pw_b, ps_b, ipar, any);
         if (any) {
           atomic_add3(acc, CR, t, pr_b);
           atomic_add3(acc, CV, t, pv_b);
           atomic_add3(acc, CW, t, pw_b);
           atomic_add3(acc, CS + 3 * sm, t, ps_b);
         }
+      }
+      if (of == f) {
+        par.kappa_pp += ipar.kappa_pp; par.gamma_pp += ipar.gamma_pp; par.mu_pp += ipar.mu_pp;
+        par.kappa_pw += ipar.kappa_pw; par.gamma_pw += ipar.gamma_pw; par.mu_pw += ipar.mu_pw;
+      } else {
+        flush_params(param_b, of, ipar);
       }
       double *ow = aq.own[lo];
       shared_add3(ow + CR, ib.r);
@@ -610,12 +636,7 @@ __global__ void __launch_bounds__(kAdjCoopBlock) k_adj_forces(Planes P, Planes i
     for (int k = 0; k < 4; k++)
       atomic_add3(acc, CS + 3 * k, s, ob.s[k] + mk(ow[CS + 3 * k], ow[CS + 3 * k + 1], ow[CS + 3 * k + 2]));
   }
-  warp_reduce_add(param_b + 0, par.kappa_pp);
-  warp_reduce_add(param_b + 1, par.gamma_pp);
-  warp_reduce_add(param_b + 2, par.mu_pp);
-  warp_reduce_add(param_b + 3, par.kappa_pw);
-  warp_reduce_add(param_b + 4, par.gamma_pw);
-  warp_reduce_add(param_b + 5, par.mu_pw);
+  add_params(param_b, f, par);
 }
 
 // Sphere patterns of init_Verlet.cu:130-142.
@@ -753,26 +774,36 @@ __global__ void k_adj_startup(Planes P, Planes in, Planes out, Planes acc, Plane
   st3(out, AAL, s, mk(0.0, 0.0, 0.0));
 }
 
-// Objective sums: mass-weighted downslope position sum_m x_rot and total mass.
+// Objective sums per flume: sums[2 f] = sum of m x_rot, sums[2 f + 1] = sum of m.
 __global__ void k_adj_objective(Planes P, DevScalars *d, const int *__restrict__ flume, double *sums, long n) {
   const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const long sv = s < n ? s : n - 1;
+  const int f = flume[sv];
   double mx = 0.0, m = 0.0;
   if (s < n) {
-    const af3d_system_par &sy = d->flumes[flume[s]].sys;
+    const af3d_system_par &sy = d->flumes[f].sys;
     m = P.p[MASS][s];
     mx = m * (P.p[RX][s] * sy.cost - P.p[RZ][s] * sy.sint);
   }
-  warp_reduce_add(sums, mx);
-  warp_reduce_add(sums + 1, m);
+  const int f0 = __shfl_sync(0xffffffffu, f, 0);
+  if (__all_sync(0xffffffffu, f == f0)) {
+    warp_reduce_add(sums + 2 * f0, mx);
+    warp_reduce_add(sums + 2 * f0 + 1, m);
+  } else if (s < n) {
+    atomicAdd(sums + 2 * f, mx);
+    atomicAdd(sums + 2 * f + 1, m);
+  }
 }
 
-// Seed: the adjoint of the final state for J = sum_m x_rot / sum_m.
-__global__ void k_adj_seed(Planes P, Planes adj, DevScalars *d, const int *__restrict__ flume, double mass_total,
+// Seed: the adjoint of the final state for the sum over flumes of J_f = sum_m x_rot / sum_m
+// (the flumes are independent, so each flume's gradients are those of its own J_f).
+__global__ void k_adj_seed(Planes P, Planes adj, DevScalars *d, const int *__restrict__ flume, const double *sums,
                            long n) {
   const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (s >= n) return;
-  const af3d_system_par &sy = d->flumes[flume[s]].sys;
-  const double w = P.p[MASS][s] / mass_total;
+  const int f = flume[s];
+  const af3d_system_par &sy = d->flumes[f].sys;
+  const double w = P.p[MASS][s] / sums[2 * f + 1];
   for (int k = 0; k < NADJ; k++) adj.p[k][s] = 0.0;
   st3(adj, AR, s, mk(w * sy.cost, 0.0, -w * sy.sint));
 }
@@ -821,9 +852,9 @@ void launch_adj_objective(const Launch &L, Planes P, DevScalars *d, const int *f
   k_adj_objective<<<blocks(L.n), kAdjBlock, 0, L.st>>>(P, d, flume, sums, L.n);
 }
 
-void launch_adj_seed(const Launch &L, Planes P, Planes adj, DevScalars *d, const int *flume, double mass_total) {
+void launch_adj_seed(const Launch &L, Planes P, Planes adj, DevScalars *d, const int *flume, const double *sums) {
   if (L.n <= 0) return;
-  k_adj_seed<<<blocks(L.n), kAdjBlock, 0, L.st>>>(P, adj, d, flume, mass_total, L.n);
+  k_adj_seed<<<blocks(L.n), kAdjBlock, 0, L.st>>>(P, adj, d, flume, sums, L.n);
 }
 
 void launch_state_copy(const Launch &L, Planes P, Planes tape, bool to_tape, bool spheres) {

@@ -1123,9 +1123,9 @@ extern "C" af3d_status af3d_adjoint(af3d_ctx *c, long steps, long ckpt_every, do
                                     af3d_vec3 *dr0, double *dR0, af3d_vec3 *dv0, af3d_vec3 *dw0) {
   CHECK_STATE(c);
   if (steps < 0 || ckpt_every <= 0 || !J) return fail(AF3D_ERR_ARG, "bad argument");
-  if (c->nflumes != 1) return fail(AF3D_ERR_ARG, "the adjoint runs one flume per context");
   if (!c->have_grid) return fail(AF3D_ERR_ARG, "no grid");
   const long n = c->n;
+  const int nf = c->nflumes;
   const bool want_grad = param_grad || dr0 || dR0 || dv0 || dw0;
   const int mode = c->fp_mode;
   c->fp_mode = AF3D_FP_EXACT;   // the adjoint differentiates the exact step
@@ -1147,11 +1147,14 @@ extern "C" af3d_status af3d_adjoint(af3d_ctx *c, long steps, long ckpt_every, do
   if (want_grad && e == cudaSuccess) e = buf.planes(kAdjPlanes, n, adjB);
   if (want_grad && e == cudaSuccess) e = buf.planes(kAccPlanes, n, acc);
   if (want_grad && e == cudaSuccess) e = buf.planes(kRbPlanes, n, rb);
-  double *dsc = nullptr;   // [0..1] objective sums, [2..7] parameter adjoints
-  if (e == cudaSuccess) e = cudaMalloc((void **)&dsc, sizeof(double) * 8);
+  // per flume f: dsc[2 f], dsc[2 f + 1] the objective sums, pgr[6 f .. 6 f + 5] the parameter adjoints
+  const size_t nsc = (size_t)8 * nf;
+  double *dsc = nullptr;
+  if (e == cudaSuccess) e = cudaMalloc((void **)&dsc, sizeof(double) * nsc);
   if (e == cudaSuccess) buf.owned.push_back(dsc);
   if (e != cudaSuccess) return fail(AF3D_ERR_NOMEM, std::string("adjoint buffers: ") + cudaGetErrorString(e));
-  AF3D_CUDA(cudaMemsetAsync(dsc, 0, sizeof(double) * 8, c->st));
+  double *pgr = dsc + 2 * nf;
+  AF3D_CUDA(cudaMemsetAsync(dsc, 0, sizeof(double) * nsc, c->st));
 
   // Forward: the start-up force pass (a_i of the first step), then `steps` steps keeping the
   // slot order, the state saved every ckpt_every steps.
@@ -1172,17 +1175,17 @@ extern "C" af3d_status af3d_adjoint(af3d_ctx *c, long steps, long ckpt_every, do
   c->time = t;
   launch_state_copy(c->L(), c->cur, fin, true, true);
   launch_adj_objective(c->L(), c->cur, c->d, c->fl_cur, dsc);
-  double sums[2] = {0.0, 0.0};
-  AF3D_CUDA(cudaMemcpyAsync(sums, dsc, sizeof(sums), cudaMemcpyDeviceToHost, c->st));
+  std::vector<double> sums((size_t)2 * nf);
+  AF3D_CUDA(cudaMemcpyAsync(sums.data(), dsc, sizeof(double) * 2 * nf, cudaMemcpyDeviceToHost, c->st));
   int flags = 0;
   af3d_status s = read_status(c, &flags);
   if (s) return s;
   s = first_error(flags);
   if (s) return s;
-  *J = sums[1] > 0.0 ? sums[0] / sums[1] : 0.0;
+  for (int f = 0; f < nf; f++) J[f] = sums[2 * f + 1] > 0.0 ? sums[2 * f] / sums[2 * f + 1] : 0.0;
 
   if (want_grad && n > 0) {
-    launch_adj_seed(c->L(), c->cur, adjA, c->d, c->fl_cur, sums[1]);
+    launch_adj_seed(c->L(), c->cur, adjA, c->d, c->fl_cur, dsc);
     for (long seg = (steps - 1) / ckpt_every; steps > 0 && seg >= 0; seg--) {
       const long k0 = seg * ckpt_every, k1 = std::min(steps, k0 + ckpt_every);
       // recompute the segment, keeping every step's starting state
@@ -1205,7 +1208,7 @@ extern "C" af3d_status af3d_adjoint(af3d_ctx *c, long steps, long ckpt_every, do
         enqueue_step_cells(c);
         AF3D_CUDA(cudaMemsetAsync(acc.p[0], 0, sizeof(double) * kAccPlanes * n, c->st));   // one block
         launch_adj_forces(c->L(), c->cur, adjA, adjB, acc, rb, c->d, c->fl_cur, c->nbr, c->cull, c->cells.start,
-                          c->cells.perm, c->cells.csort, dsc + 2, false);
+                          c->cells.perm, c->cells.csort, pgr, false);
         launch_adj_predict(c->L(), c->cur, tape[k - k0], adjA, adjB, acc, rb, c->d, c->fl_cur);
         std::swap(adjA, adjB);
       }
@@ -1217,7 +1220,7 @@ extern "C" af3d_status af3d_adjoint(af3d_ctx *c, long steps, long ckpt_every, do
     enqueue_startup_pass(c);
     AF3D_CUDA(cudaMemsetAsync(acc.p[0], 0, sizeof(double) * kAccPlanes * n, c->st));
     launch_adj_forces(c->L(), c->cur, adjA, adjB, acc, rb, c->d, c->fl_cur, c->nbr, c->cull, c->cells.start,
-                      c->cells.perm, c->cells.csort, dsc + 2, true);
+                      c->cells.perm, c->cells.csort, pgr, true);
     launch_adj_startup(c->L(), c->cur, adjA, adjB, acc, rb);
     // gradients by clump id
     std::vector<double> h((size_t)kAdjPlanes * n);
@@ -1226,11 +1229,9 @@ extern "C" af3d_status af3d_adjoint(af3d_ctx *c, long steps, long ckpt_every, do
       AF3D_CUDA(cudaMemcpyAsync(h.data() + (size_t)p * n, adjB.p[p], sizeof(double) * n, cudaMemcpyDeviceToHost,
                                 c->st));
     AF3D_CUDA(cudaMemcpyAsync(ids.data(), c->id_cur, sizeof(long long) * n, cudaMemcpyDeviceToHost, c->st));
-    double pg[6];
-    AF3D_CUDA(cudaMemcpyAsync(pg, dsc + 2, sizeof(pg), cudaMemcpyDeviceToHost, c->st));
-    AF3D_CUDA(cudaStreamSynchronize(c->st));
     if (param_grad)
-      for (int k = 0; k < 6; k++) param_grad[k] = pg[k];
+      AF3D_CUDA(cudaMemcpyAsync(param_grad, pgr, sizeof(double) * 6 * nf, cudaMemcpyDeviceToHost, c->st));
+    AF3D_CUDA(cudaStreamSynchronize(c->st));
     for (long sl = 0; sl < n; sl++) {
       const long long i = ids[sl];
       auto at = [&](int p) { return h[(size_t)p * n + sl]; };

@@ -164,7 +164,7 @@ void launch_adj_predict (const Launch &L, Planes P, Planes tape, Planes in, Plan
                          DevScalars *d, const int *flume);
 void launch_adj_startup (const Launch &L, Planes P, Planes in, Planes out, Planes acc, Planes rb);
 void launch_adj_objective (const Launch &L, Planes P, DevScalars *d, const int *flume, double *sums);
-void launch_adj_seed (const Launch &L, Planes P, Planes adj, DevScalars *d, const int *flume, double mass_total);
+void launch_adj_seed (const Launch &L, Planes P, Planes adj, DevScalars *d, const int *flume, const double *sums);
 // The 24 state planes (with spheres: 36, the sphere centres too) between the plane set and a
 // tape slot (to_tape: planes -> tape).
 void launch_state_copy (const Launch &L, Planes P, Planes tape, bool to_tape, bool spheres = false);

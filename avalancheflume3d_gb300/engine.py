@@ -197,20 +197,24 @@ class Engine:
     def adjoint(self, steps: int, ckpt_every: int = 500, gradients: bool = True) -> dict:
         """Start-up force pass + `steps` exact steps from the imported state, J = mass-weighted
         mean downslope position at the end and (gradients=True) dJ/d(parameters, initial state)
-        from the hand-written adjoint (af3d_adjoint).  Leaves the context at the final state."""
-        J = C.c_double()
+        from the hand-written adjoint (af3d_adjoint).  Leaves the context at the final state.
+
+        For an ensemble, ``J`` is an array over flumes and every ``params`` entry an array of
+        each flume's own derivative; the per-clump gradients are those of the clump's flume."""
+        names = ("kappa_pp", "gamma_pp", "mu_pp", "kappa_pw", "gamma_pw", "mu_pw")
+        J = np.zeros(self.nflumes)
         out = {}
         if gradients:
-            pg = np.zeros(6)
+            pg = np.zeros((self.nflumes, 6))
             dr, dv, dw = _vec3(self.n), _vec3(self.n), _vec3(self.n)
             dR = np.zeros((self.n, 9))
-            self._call("af3d_adjoint", int(steps), int(ckpt_every), C.byref(J), ptr(pg), ptr(dr), ptr(dR), ptr(dv),
+            self._call("af3d_adjoint", int(steps), int(ckpt_every), ptr(J), ptr(pg), ptr(dr), ptr(dR), ptr(dv),
                        ptr(dw))
-            out.update(params=dict(zip(("kappa_pp", "gamma_pp", "mu_pp", "kappa_pw", "gamma_pw", "mu_pw"), pg)),
-                       r0=dr, v0=dv, w0=dw, R0=dR.reshape(-1, 3, 3))
+            params = {k: (pg[:, i].copy() if self.ensemble else float(pg[0, i])) for i, k in enumerate(names)}
+            out.update(params=params, r0=dr, v0=dv, w0=dw, R0=dR.reshape(-1, 3, 3))
         else:
-            self._call("af3d_adjoint", int(steps), int(ckpt_every), C.byref(J), None, None, None, None, None)
-        out["J"] = J.value
+            self._call("af3d_adjoint", int(steps), int(ckpt_every), ptr(J), None, None, None, None, None)
+        out["J"] = J if self.ensemble else float(J[0])
         return out
 
     # ---- diagnostics (indexed by clump id) ----

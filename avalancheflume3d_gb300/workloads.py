@@ -14,6 +14,7 @@ the reference's tetrahedral 4-sphere clumps (edge 2r, init_Verlet.cu:130-142).
 from __future__ import annotations
 
 import math
+import dataclasses
 from dataclasses import dataclass
 
 import numpy as np
@@ -72,6 +73,15 @@ def flume_inputs(cfg: FlumeConfig) -> np.ndarray:
     return v
 
 
+def flume_system_of(cfg: FlumeConfig):
+    """(system_par, Funnel) of a configuration at the moment the door opens (time 0, avalanche
+    phase: side.x = xfinal, avalanche_hst.cu:607-613); tot_mass is left to the caller."""
+    sys, fun = derive_system(flume_inputs(cfg))
+    sys["time"] = 0.0
+    sys["side"][0] = (70.0 + cfg.Lflume) * float(sys["cost"])
+    return sys, fun
+
+
 def flume_state(cfg: FlumeConfig):
     """(system_par, Funnel, particle array) of a clump block in the hopper at the moment the door
     opens (time 0, avalanche phase: side.x = xfinal, avalanche_hst.cu:607-613).
@@ -89,9 +99,7 @@ def flume_state(cfg: FlumeConfig):
     and turned rigidly into the lab frame: a dense layer that gravity keeps pressed on the bed
     while it slides, the state of an avalanche in full flow.
     With v0 > 0 the velocities follow the reference's set_initial_velocity (seed 26752658)."""
-    sys, fun = derive_system(flume_inputs(cfg))
-    sys["time"] = 0.0
-    sys["side"][0] = (70.0 + cfg.Lflume) * float(sys["cost"])
+    sys, fun = flume_system_of(cfg)
     pp = np.zeros(cfg.n, dtype=PARTICLE)
     pp["radius"] = cfg.radius
     pp["density"] = cfg.density
@@ -193,3 +201,28 @@ def ensemble_state(cfgs: list[FlumeConfig]):
     fun = np.stack([u for _, u, _ in states])
     pp = np.concatenate([p for _, _, p in states])
     return sys, fun, pp
+
+
+ADJOINT_BATCH_SEED = 5242883
+
+
+def adjoint_batch(cfg: FlumeConfig, samples: int = 64, seed: int = ADJOINT_BATCH_SEED):
+    """A calibration batch: `samples` copies of the flume `cfg` (same clumps, same initial
+    state) whose material parameters are drawn per copy from rannew64 in this order: mu_pp ~
+    U[0.2, 0.8], mu_pw ~ U[0.2, 0.6], restitution ~ U[0.2, 0.8] (the ranges of the ensemble
+    workload).  Returns (configs, system_par[F], Funnel[F], particle array of all copies back to
+    back) for an ensemble context."""
+    sys0, fun0, pp = flume_state(cfg)
+    rng = Rannew64(seed)
+    cfgs, syss, funs = [], [], []
+    for _ in range(samples):
+        mu_pp = 0.2 + 0.6 * rng()
+        mu_pw = 0.2 + 0.4 * rng()
+        e = 0.2 + 0.6 * rng()
+        c = dataclasses.replace(cfg, mu_pp=mu_pp, mu_pw=mu_pw, restitution=e)
+        s, u = flume_system_of(c)
+        s["tot_mass"] = sys0["tot_mass"]
+        cfgs.append(c)
+        syss.append(s)
+        funs.append(u)
+    return cfgs, np.stack(syss), np.stack(funs), np.concatenate([pp] * samples)

@@ -75,6 +75,12 @@ def parse_args():
     p.add_argument("--adjoint-steps", type=int, default=1000,
                    help="steps of the adjoint measurement (0 skips it)")
     p.add_argument("--adjoint-ckpt", type=int, default=500)
+    p.add_argument("--adjoint-batch", type=int, default=64,
+                   help="parameter samples of the batched (calibration) adjoint (0 skips it)")
+    p.add_argument("--adjoint-batch-steps", type=int, default=200)
+    p.add_argument("--adjoint-batch-ckpt", type=int, default=50,
+                   help="checkpoint interval of the batched adjoint (its tape holds this many steps "
+                        "of all samples)")
     p.add_argument("--trace-contacts", type=int, default=0,
                    help="print active contacts every this many pre-roll steps (diagnostic)")
     return p.parse_args()
@@ -291,20 +297,11 @@ def measure_ensemble(args, stream):
             "geometry": "40 cm x 4 cm flume, reference hopper and funnel; per-flume slope 25-40 deg"}
 
 
-def measure_adjoint(args, stream):
-    """Adjoint/forward cost on the adjoint configuration: 32,768 clumps, 80 cm x 4 cm flume at 35
-    deg, dense bed layer, exact FP64 (the mode the adjoint differentiates).  Forward: K fused steps
-    (graph replay).  Adjoint: af3d_adjoint over the same K steps from the same state (start-up
-    pass, forward with checkpoints every C steps, segment recompute, reverse), timed end to end."""
+def _adjoint_cost(sys_, fun, pp, K, ckpt, stream):
+    """(forward seconds for K graph-replayed exact steps, adjoint seconds for af3d_adjoint over
+    the same K steps from the same state, the adjoint's output)."""
     import torch
     from avalancheflume3d_gb300 import Engine, FP_EXACT
-    from avalancheflume3d_gb300.workloads import flume_2k, flume_state
-    cfg = flume_2k(n=32768, tilt_deg=35.0, Lflume=80.0, layout="bed")
-    sys_, fun, pp = flume_state(cfg)
-    K = args.adjoint_steps
-
-    def events():
-        return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
     with Engine(sys_, fun, stream=stream.cuda_stream, fp_mode=FP_EXACT) as eng:
         eng.import_particles(pp)
@@ -312,7 +309,7 @@ def measure_adjoint(args, stream):
         eng.swap_accel()
         eng.step(K)                      # warm-up (captures the graphs)
         torch.cuda.synchronize()
-        e0, e1 = events()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         eng.step(K)
         e1.record(stream)
@@ -320,20 +317,52 @@ def measure_adjoint(args, stream):
         t_fwd = e0.elapsed_time(e1) / 1e3
     with Engine(sys_, fun, stream=stream.cuda_stream) as eng:
         eng.import_particles(pp)
-        eng.adjoint(min(K, 2 * args.adjoint_ckpt), args.adjoint_ckpt)   # warm-up
+        eng.adjoint(min(K, 2 * ckpt), ckpt)   # warm-up
     with Engine(sys_, fun, stream=stream.cuda_stream) as eng:
         eng.import_particles(pp)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        out = eng.adjoint(K, args.adjoint_ckpt)
+        out = eng.adjoint(K, ckpt)
         torch.cuda.synchronize()
         t_adj = time.perf_counter() - t0
-    return {"workload": "flume 32,768 clumps, 80 cm x 4 cm at 35 deg, dense bed layer, exact FP64",
-            "steps": K, "ckpt_every": args.adjoint_ckpt, "ms_per_step_forward": 1e3 * t_fwd / K,
-            "ms_per_step_adjoint": 1e3 * t_adj / K, "adjoint_over_forward": t_adj / t_fwd,
-            "what": "adjoint = the whole af3d_adjoint call (forward with checkpoints, segment recompute, "
-                    "reverse, gradient gather) per step, over a graph-replayed exact forward step",
-            "J": out["J"], "dJ_dparams": out["params"]}
+    return t_fwd, t_adj, out
+
+
+def measure_adjoint(args, stream):
+    """Adjoint/forward cost on the adjoint configuration: 32,768 clumps, 80 cm x 4 cm flume at 35
+    deg, dense bed layer, exact FP64 (the mode the adjoint differentiates).  Forward: K fused steps
+    (graph replay).  Adjoint: af3d_adjoint over the same K steps from the same state (start-up
+    pass, forward with checkpoints every C steps, segment recompute, reverse), timed end to end.
+    Then the same as a calibration batch: the flume in S copies with sampled (mu_pp, mu_pw,
+    restitution) in one ensemble context, every copy's gradients from one backward sweep."""
+    from avalancheflume3d_gb300.adjoint import config_gradients
+    from avalancheflume3d_gb300.workloads import adjoint_batch, flume_2k, flume_state
+    cfg = flume_2k(n=32768, tilt_deg=35.0, Lflume=80.0, layout="bed")
+    sys_, fun, pp = flume_state(cfg)
+    K = args.adjoint_steps
+    t_fwd, t_adj, out = _adjoint_cost(sys_, fun, pp, K, args.adjoint_ckpt, stream)
+    res = {"workload": "flume 32,768 clumps, 80 cm x 4 cm at 35 deg, dense bed layer, exact FP64",
+           "steps": K, "ckpt_every": args.adjoint_ckpt, "ms_per_step_forward": 1e3 * t_fwd / K,
+           "ms_per_step_adjoint": 1e3 * t_adj / K, "adjoint_over_forward": t_adj / t_fwd,
+           "what": "adjoint = the whole af3d_adjoint call (forward with checkpoints, segment recompute, "
+                   "reverse, gradient gather) per step, over a graph-replayed exact forward step",
+           "J": out["J"], "dJ_dparams": out["params"],
+           "dJ_dconfig": config_gradients(cfg, out["params"])}
+    S, Kb = args.adjoint_batch, args.adjoint_batch_steps
+    if S > 0 and Kb > 0:
+        cfgs, bsys, bfun, bpp = adjoint_batch(cfg, S)
+        tb_fwd, tb_adj, bout = _adjoint_cost(bsys, bfun, bpp, Kb, args.adjoint_batch_ckpt, stream)
+        g0 = config_gradients(cfgs[0], {k: float(v[0]) for k, v in bout["params"].items()})
+        res["batch"] = {
+            "samples": S, "clumps": int(len(bpp)), "steps": Kb, "ckpt_every": args.adjoint_batch_ckpt,
+            "sampled": "mu_pp ~ U[0.2, 0.8], mu_pw ~ U[0.2, 0.6], restitution ~ U[0.2, 0.8] per copy (rannew64)",
+            "ms_per_step_forward": 1e3 * tb_fwd / Kb, "ms_per_step_adjoint": 1e3 * tb_adj / Kb,
+            "adjoint_over_forward": tb_adj / tb_fwd,
+            "clump_steps_per_s_adjoint": len(bpp) * Kb / tb_adj,
+            "clump_steps_per_s_adjoint_single": cfg.n * K / t_adj,
+            "J_range": [float(bout["J"].min()), float(bout["J"].max())],
+            "dJ_dconfig_sample0": g0}
+    return res
 
 
 def time_other_mode(eng, modes, other, args, stream, R, dev, world):

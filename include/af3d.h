@@ -194,16 +194,20 @@ af3d_status af3d_fp64_peak (double *tflops);
 
 /* ---- adjoint (no counterpart in the reference) --------------------------------------------
    Runs, from the imported state (a_i = alpha_i = 0), the start-up force pass and `steps` exact
-   steps (fixed cell grid, no re-grid), and returns J = the mass-weighted mean downslope position
-   sum m (x cos(tilt) - z sin(tilt)) / sum m at the end.  With any gradient pointer non-NULL it
-   then runs the hand-written adjoint of those steps backwards, with the state checkpointed every
-   ckpt_every steps and each segment recomputed, and returns
-     param_grad[6]  dJ/d(kappa_pp, gamma_pp, mu_pp, kappa_pw, gamma_pw, mu_pw) of system_par
-     dr0, dv0, dw0  dJ/d(initial r, v, omega) per clump id (the sphere centres follow r and R)
-     dR0[9 n]       dJ/d(initial Rmatx, Rmaty, Rmatz) per clump id
-   Discrete events (cells, contact sets, Coulomb or elastic branch, which wall) are held at the
-   forward run's.  One flume per context; removed clumps carry no gradient.  The context is left
-   at the final state of the forward run. */
+   steps (fixed cell grid, no re-grid), and returns per flume f J[f] = the mass-weighted mean
+   downslope position sum m (x cos(tilt) - z sin(tilt)) / sum m of its clumps at the end.  With
+   any gradient pointer non-NULL it then runs the hand-written adjoint of those steps backwards,
+   with the state checkpointed every ckpt_every steps and each segment recomputed, and returns
+     param_grad[6 f + k]  dJ[f]/d(kappa_pp, gamma_pp, mu_pp, kappa_pw, gamma_pw, mu_pw)[k] of
+                          flume f's system_par
+     dr0, dv0, dw0        dJ[f]/d(initial r, v, omega) per clump id, f the clump's flume (the
+                          sphere centres follow r and R)
+     dR0[9 n]             dJ[f]/d(initial Rmatx, Rmaty, Rmatz) per clump id
+   J and param_grad hold af3d_flume_count entries (times 6); an ensemble differentiates all its
+   flumes in one backward sweep (they are independent, so the sweep of sum_f J[f] gives each
+   flume's own gradients).  Discrete events (cells, contact sets, Coulomb or elastic branch,
+   which wall) are held at the forward run's.  Removed clumps carry no gradient.  The context is
+   left at the final state of the forward run. */
 af3d_status af3d_adjoint (af3d_ctx *ctx, long steps, long ckpt_every, double *J, double *param_grad,
                           af3d_vec3 *dr0, double *dR0, af3d_vec3 *dv0, af3d_vec3 *dw0);
 

@@ -55,7 +55,7 @@ void orc_set_threads (int nthreads)
 #define ORC_PARALLEL_FOR
 #endif
 
-static inline int removed (const orc_system_par *sys, double x)
+static inline int removed (const orc_system_par *sys, orc_real x)
 {
   /* init_Verlet.cu:29, cells.cu:65, force_part.cu:47, ... */
   return sys->time > 0.0 && x > sys->side.x;
@@ -78,11 +78,11 @@ static inline int removed (const orc_system_par *sys, double x)
  *          (force_funnel.cu:354, only differs for a NaN normal)
  * Returns 1 and writes *fs when the contact exerts a force.
  */
-static inline int contact_law (orc_vec3 dvvc, orc_vec3 nvec, double comp, double km, double gm,
-                               double mass_t, double mu, double cns_1, double dt, int xi0, int gate,
+static inline int contact_law (orc_vec3 dvvc, orc_vec3 nvec, orc_real comp, orc_real km, orc_real gm,
+                               orc_real mass_t, orc_real mu, orc_real cns_1, orc_real dt, int xi0, int gate,
                                orc_vec3 *fs)
 {
-  double   vn, vt_mag, vt_sig, normal, xi, xi_dot, fsdt, af, t0;
+  orc_real   vn, vt_mag, vt_sig, normal, xi, xi_dot, fsdt, af, t0;
   orc_vec3 vt, tv, f;
 
   vn   = dvvc.x*nvec.x + dvvc.y*nvec.y + dvvc.z*nvec.z;
@@ -154,8 +154,8 @@ static inline void accumulate (orc_vec3 *ff, orc_vec3 *tq, orc_vec3 fs, orc_vec3
 
 /* Wall contact: relative velocity is minus the sphere's contact-point velocity
    (force_walls.cu:113-120).  Returns 1 when a force was added. */
-static inline int wall_contact (const orc_particle *p, orc_vec3 rrc, orc_vec3 nvec, double comp,
-                                double km, double gm, double mass, double mu, double cns_1, double dt,
+static inline int wall_contact (const orc_particle *p, orc_vec3 rrc, orc_vec3 nvec, orc_real comp,
+                                orc_real km, orc_real gm, orc_real mass, orc_real mu, orc_real cns_1, orc_real dt,
                                 int gate, orc_vec3 *ff, orc_vec3 *tq)
 {
   orc_vec3 vvc, dvvc, fs;
@@ -176,8 +176,8 @@ void orc_init_verlet (const orc_vec3 *accel, const orc_vec3 *ang_acc, const orc_
                       orc_particle *pp)
 {
   const long   n   = sys->npart;
-  const double dt  = sys->dt;
-  const double hdt = sys->hdt;
+  const orc_real dt  = sys->dt;
+  const orc_real hdt = sys->hdt;
   long ii;
 
   ORC_PARALLEL_FOR
@@ -185,7 +185,7 @@ void orc_init_verlet (const orc_vec3 *accel, const orc_vec3 *ang_acc, const orc_
   {
     orc_particle *p = &pp[ii];
     orc_vec3 rr = p->rr, vv, aa, Rx, Ry, Rz, ww, al, dO, u, dRx, dRy, dRz, Tx, Ty, Tz;
-    double   mag, c, s, omc, norm, pos;
+    orc_real   mag, c, s, omc, norm, pos;
 
     if (removed (sys, rr.x))
     {
@@ -268,7 +268,7 @@ void orc_init_verlet (const orc_vec3 *accel, const orc_vec3 *ang_acc, const orc_
 }
 
 /* rotate_vectors.cu:7-56: lab frame -> slope frame (rotation about y by the tilt). */
-static inline orc_vec3 to_slope (orc_vec3 r, double cost, double sint)
+static inline orc_vec3 to_slope (orc_vec3 r, orc_real cost, orc_real sint)
 {
   orc_vec3 q;
   q.x = r.x*cost - r.z*sint;
@@ -307,7 +307,7 @@ void orc_get_accel (const orc_vec3 *force, const orc_vec3 *torque, orc_vec3 *acc
   {
     const orc_particle *p = &pp[ii];
     orc_vec3 I, v, w, Rx, Ry, Rz, f, t, a, wb, tb, ab, al;
-    double   m, rad, Cxy, Cyz, Czx, adrag, vmag;
+    orc_real   m, rad, Cxy, Cyz, Czx, adrag, vmag;
 
     if (removed (sys, p->rr.x))
       continue;
@@ -352,7 +352,7 @@ void orc_finish_verlet (const orc_vec3 *accel_i, const orc_vec3 *ang_acc_i, cons
                         const orc_vec3 *ang_acc_f, const orc_system_par *sys, orc_particle *pp)
 {
   long ii, n = sys->npart;
-  const double hdt = sys->hdt;
+  const orc_real hdt = sys->hdt;
   ORC_PARALLEL_FOR
   for (ii = 0; ii < n; ii++)
   {
@@ -388,7 +388,7 @@ void orc_clear_ocup (const orc_cell_par *cc, int *nocup_vec)
 }
 
 /* Cell coordinate of one axis as binned by cells.cu:69-77 (multiplication by cs_inv). */
-static inline long bin_axis (double x, double xmin, double inv, long n)
+static inline long bin_axis (orc_real x, orc_real xmin, orc_real inv, long n)
 {
   long i = (long) (inv*(x - xmin));
   if (i == n)
@@ -433,7 +433,7 @@ void orc_cell_dim (orc_vec3 *rr_max, orc_vec3 *rr_min, const orc_particle *pp,
                    const orc_system_par *sys)
 {
   int      ii, n = (int) sys->npart;
-  double   rgyr = 0.5*sys->gyr_max, ddt = 2000.0*sys->dt, vxmax, vzmin;
+  orc_real   rgyr = 0.5*sys->gyr_max, ddt = 2000.0*sys->dt, vxmax, vzmin;
   orc_vec3 hi, lo;
 
   hi = lo = pp[0].rr;
@@ -464,16 +464,16 @@ void orc_cell_dim (orc_vec3 *rr_max, orc_vec3 *rr_min, const orc_particle *pp,
 /* avalanche_hst.cu:314-333 with the cell pitch factor of :115 (`GYR + 0.05f`, a float literal). */
 void orc_grid_from_bbox (orc_cell_par *cc, const orc_system_par *sys)
 {
-  const double dist = ORC_GYR + 0.05f;
+  const orc_real dist = ORC_GYR + 0.05f;
   cc->length.x = cc->rr_max.x - cc->rr_min.x;
   cc->length.y = cc->rr_max.y - cc->rr_min.y;
   cc->length.z = cc->rr_max.z - cc->rr_min.z;
   cc->ncell.x  = (long) (cc->length.x/(dist*sys->rmax));
   cc->ncell.y  = (long) (cc->length.y/(dist*sys->rmax));
   cc->ncell.z  = (long) (cc->length.z/(dist*sys->rmax));
-  cc->cell_side.x = cc->length.x/((double) cc->ncell.x);
-  cc->cell_side.y = cc->length.y/((double) cc->ncell.y);
-  cc->cell_side.z = cc->length.z/((double) cc->ncell.z);
+  cc->cell_side.x = cc->length.x/((orc_real) cc->ncell.x);
+  cc->cell_side.y = cc->length.y/((orc_real) cc->ncell.y);
+  cc->cell_side.z = cc->length.z/((orc_real) cc->ncell.z);
   cc->cs_inv.x = 1.0/cc->cell_side.x;
   cc->cs_inv.y = 1.0/cc->cell_side.y;
   cc->cs_inv.z = 1.0/cc->cell_side.z;
@@ -484,7 +484,7 @@ void orc_grid_from_bbox (orc_cell_par *cc, const orc_system_par *sys)
 /* ========================== particle-particle contacts ==================== */
 
 /* Search-centre cell of force_part.cu:77-85 (division by cell_side, not multiplication). */
-static inline long search_axis (double x, double xmin, double side, long n)
+static inline long search_axis (orc_real x, orc_real xmin, orc_real side, long n)
 {
   long i = (long) ((x - xmin)/side);
   if (i == n)
@@ -523,9 +523,9 @@ static inline long search_axis (double x, double xmin, double side, long n)
 
 /* Staged sphere-sphere overlap test of force_part.cu:140-157.  Returns 1 on overlap and leaves
    the separation vector in *d and its squared norm in *dist2. */
-static inline int sphere_overlap (orc_vec3 s1, orc_vec3 s2, double sep2, orc_vec3 *d, double *dist2)
+static inline int sphere_overlap (orc_vec3 s1, orc_vec3 s2, orc_real sep2, orc_vec3 *d, orc_real *dist2)
 {
-  double q;
+  orc_real q;
   d->x = s2.x - s1.x;
   q = d->x*d->x;
   if (!(q < sep2)) return 0;
@@ -546,8 +546,8 @@ void orc_force_part (orc_vec3 *force, orc_vec3 *torque, const long *cell_vec, co
                      int sph_id, int variant)
 {
   const int    sl = (sph_id - 1)%4, sm = (sph_id - 1)/4;
-  const double mu = sys->mu_pp, kappa = sys->kappa_pp, gamma = sys->gamma_pp, dt = sys->dt;
-  const double cns_1 = sys->fr_fact_pp;
+  const orc_real mu = sys->mu_pp, kappa = sys->kappa_pp, gamma = sys->gamma_pp, dt = sys->dt;
+  const orc_real cns_1 = sys->fr_fact_pp;
   long ll;
 
   ORC_PARALLEL_FOR
@@ -555,7 +555,7 @@ void orc_force_part (orc_vec3 *force, orc_vec3 *torque, const long *cell_vec, co
   {
     const orc_particle *pl = &pp[ll];
     orc_vec3 rrl = pl->rr, vvl, wwl, s1, ff, tq;
-    double   rad_1, massl;
+    orc_real   rad_1, massl;
 
     if (removed (sys, rrl.x))
       continue;
@@ -566,7 +566,7 @@ void orc_force_part (orc_vec3 *force, orc_vec3 *torque, const long *cell_vec, co
 
     ORC_FOR_NEIGHBOURS (cell, cell_vec, nocup_vec, rrl, ll, mm, {
       const orc_particle *pm = &pp[mm];
-      double   rad_2 = pm->radius, massm, meff, km, gm, sep, sep2, dist2, dist;
+      orc_real   rad_2 = pm->radius, massm, meff, km, gm, sep, sep2, dist2, dist;
       orc_vec3 d, nv, rrc, vl, vm, dvvc, fs;
 
       massm = ORC_SPH_FACT*pm->density*rad_2*rad_2*rad_2;
@@ -604,8 +604,8 @@ long orc_contact_pairs (long *out, long cap, const long *cell_vec, const int *no
                         const orc_particle *pp, const orc_system_par *sys, const orc_cell_par *cell,
                         int active)
 {
-  const double mu = sys->mu_pp, kappa = sys->kappa_pp, gamma = sys->gamma_pp, dt = sys->dt;
-  const double cns_1 = sys->fr_fact_pp;
+  const orc_real mu = sys->mu_pp, kappa = sys->kappa_pp, gamma = sys->gamma_pp, dt = sys->dt;
+  const orc_real cns_1 = sys->fr_fact_pp;
   long count = 0, ll;
   int  sph_id;
 
@@ -615,21 +615,21 @@ long orc_contact_pairs (long *out, long cap, const long *cell_vec, const int *no
     const orc_particle *pl = &pp[ll];
     const int sl = (sph_id - 1)%4, sm = (sph_id - 1)/4;
     orc_vec3 rrl = pl->rr;
-    double   rad_1 = pl->radius, massl;
+    orc_real   rad_1 = pl->radius, massl;
     if (removed (sys, rrl.x))
       continue;
     massl = ORC_SPH_FACT*pl->density*rad_1*rad_1*rad_1;
     ORC_FOR_NEIGHBOURS (cell, cell_vec, nocup_vec, rrl, ll, mm, {
       const orc_particle *pm = &pp[mm];
-      double   rad_2 = pm->radius, sep = rad_1 + rad_2, dist2;
+      orc_real   rad_2 = pm->radius, sep = rad_1 + rad_2, dist2;
       orc_vec3 d;
       if (sphere_overlap (pl->rr_s[sl], pm->rr_s[sm], sep*sep, &d, &dist2))
       {
         int keep = 1;
         if (active)
         {
-          double   massm = ORC_SPH_FACT*pm->density*rad_2*rad_2*rad_2, meff = 0.5*(massm + massl);
-          double   dist = sqrt (dist2);
+          orc_real   massm = ORC_SPH_FACT*pm->density*rad_2*rad_2*rad_2, meff = 0.5*(massm + massl);
+          orc_real   dist = sqrt (dist2);
           orc_vec3 nv, rrc, vl, vm, dvvc, fs;
           nv.x = d.x/dist;  nv.y = d.y/dist;  nv.z = d.z/dist;
           rrc.x = pl->rr_s[sl].x + rad_1*nv.x;
@@ -660,9 +660,9 @@ long orc_contact_pairs (long *out, long cap, const long *cell_vec, const int *no
 /* ================================ boundaries ============================== */
 
 /* Mass of one sphere in the wall routines' operand order (force_walls.cu:47). */
-static inline double wall_sphere_mass (const orc_particle *p)
+static inline orc_real wall_sphere_mass (const orc_particle *p)
 {
-  double ri = p->radius;
+  orc_real ri = p->radius;
   return ORC_SPH_FACT*ri*ri*ri*p->density;
 }
 
@@ -671,8 +671,8 @@ static inline double wall_sphere_mass (const orc_particle *p)
 void orc_force_hop (orc_vec3 *force, orc_vec3 *torque, const orc_system_par *sys,
                     const orc_particle *pp, int nw)
 {
-  const double mu = sys->mu_pw, kappa = sys->kappa_pw, gamma = sys->gamma_pw, dt = sys->dt;
-  const double cns_1 = sys->fr_fact_pw, time = sys->time;
+  const orc_real mu = sys->mu_pw, kappa = sys->kappa_pw, gamma = sys->gamma_pw, dt = sys->dt;
+  const orc_real cns_1 = sys->fr_fact_pw, time = sys->time;
   long ii;
 
   ORC_PARALLEL_FOR
@@ -680,13 +680,13 @@ void orc_force_hop (orc_vec3 *force, orc_vec3 *torque, const orc_system_par *sys
   {
     const orc_particle *p = &pp[ii];
     orc_vec3 ff = force[ii], tq = torque[ii];
-    double   ri = p->radius, mass = wall_sphere_mass (p), km = 0.5*kappa*mass, gm = 0.5*gamma*mass;
+    orc_real   ri = p->radius, mass = wall_sphere_mass (p), km = 0.5*kappa*mass, gm = 0.5*gamma*mass;
     int      ns;
 
     for (ns = 0; ns < 4; ns++)
     {
       orc_vec3 s = p->rr_s[ns], rrc, nv;
-      double   dist, comp = 0.0;
+      orc_real   dist, comp = 0.0;
       int      touch = 0;
       if (s.z < ORC_HOP_HEIGHT || s.x > ORC_HOP_WIDTH)
         continue;
@@ -739,7 +739,7 @@ void orc_force_hop (orc_vec3 *force, orc_vec3 *torque, const orc_system_par *sys
 }
 
 /* Slope frame -> lab frame (force_funnel.cu:88-93). */
-static inline orc_vec3 to_lab (orc_vec3 q, double cost, double sint)
+static inline orc_vec3 to_lab (orc_vec3 q, orc_real cost, orc_real sint)
 {
   orc_vec3 r;
   r.x = q.x*cost + q.z*sint;
@@ -752,9 +752,9 @@ static inline orc_vec3 to_lab (orc_vec3 q, double cost, double sint)
 void orc_force_funnel (orc_vec3 *force, orc_vec3 *torque, const orc_system_par *sys,
                        const orc_particle *pp, const orc_funnel *fun)
 {
-  const double mu = sys->mu_pw, kappa = sys->kappa_pw, gamma = sys->gamma_pw, dt = sys->dt;
-  const double cns_1 = sys->fr_fact_pw, cost = sys->cost, sint = sys->sint;
-  const double sinfi = fun->sinfi, cosfi = fun->cosfi, tanfi = fun->tanfi;
+  const orc_real mu = sys->mu_pw, kappa = sys->kappa_pw, gamma = sys->gamma_pw, dt = sys->dt;
+  const orc_real cns_1 = sys->fr_fact_pw, cost = sys->cost, sint = sys->sint;
+  const orc_real sinfi = fun->sinfi, cosfi = fun->cosfi, tanfi = fun->tanfi;
   long ii;
 
   ORC_PARALLEL_FOR
@@ -762,13 +762,13 @@ void orc_force_funnel (orc_vec3 *force, orc_vec3 *torque, const orc_system_par *
   {
     const orc_particle *p = &pp[ii];
     orc_vec3 ff = force[ii], tq = torque[ii];
-    double   ri = p->radius, mass = wall_sphere_mass (p), km = 0.5*kappa*mass, gm = 0.5*gamma*mass;
+    orc_real   ri = p->radius, mass = wall_sphere_mass (p), km = 0.5*kappa*mass, gm = 0.5*gamma*mass;
     int      ns;
 
     for (ns = 0; ns < 4; ns++)
     {
       orc_vec3 q = p->rrot_s[ns], qc, nr, rrc, nv;
-      double   dist, comp = 0.0;
+      orc_real   dist, comp = 0.0;
       int      touch = 0;
       if (q.x > ORC_LFUNNEL - ri*sinfi)
         continue;
@@ -804,9 +804,9 @@ void orc_force_funnel (orc_vec3 *force, orc_vec3 *torque, const orc_system_par *
 void orc_force_fcorners (orc_vec3 *force, orc_vec3 *torque, const orc_system_par *sys,
                          const orc_funnel *fun, const orc_particle *pp)
 {
-  const double mu = sys->mu_pw, kappa = sys->kappa_pw, gamma = sys->gamma_pw, dt = sys->dt;
-  const double cns_1 = sys->fr_fact_pw, sin_fa = fun->sinfi, cost = sys->cost, sint = sys->sint;
-  const double yfun_l = sys->dy2, yfun_r = sys->side.y + sys->dy2, hsy = sys->dy2 + sys->side.y/2.0;
+  const orc_real mu = sys->mu_pw, kappa = sys->kappa_pw, gamma = sys->gamma_pw, dt = sys->dt;
+  const orc_real cns_1 = sys->fr_fact_pw, sin_fa = fun->sinfi, cost = sys->cost, sint = sys->sint;
+  const orc_real yfun_l = sys->dy2, yfun_r = sys->side.y + sys->dy2, hsy = sys->dy2 + sys->side.y/2.0;
   long ii;
 
   ORC_PARALLEL_FOR
@@ -814,13 +814,13 @@ void orc_force_fcorners (orc_vec3 *force, orc_vec3 *torque, const orc_system_par
   {
     const orc_particle *p = &pp[ii];
     orc_vec3 ff = force[ii], tq = torque[ii];
-    double   ri = p->radius, mass = wall_sphere_mass (p), km = 0.5*kappa*mass, gm = 0.5*gamma*mass;
+    orc_real   ri = p->radius, mass = wall_sphere_mass (p), km = 0.5*kappa*mass, gm = 0.5*gamma*mass;
     int      ns;
 
     for (ns = 0; ns < 4; ns++)
     {
       orc_vec3 q = p->rrot_s[ns], d, nr, qc;
-      double   yc, sep2, dist2, dist;
+      orc_real   yc, sep2, dist2, dist;
       if (q.x < ORC_LFUNNEL - ri*sin_fa || q.x > ORC_LFUNNEL + ri)
         continue;
       if (q.y > yfun_r || q.y < yfun_l)
@@ -850,8 +850,8 @@ void orc_force_fcorners (orc_vec3 *force, orc_vec3 *torque, const orc_system_par
 void orc_force_walls (orc_vec3 *force, orc_vec3 *torque, const orc_system_par *sys,
                       const orc_particle *pp)
 {
-  const double mu = sys->mu_pw, kappa = sys->kappa_pw, gamma = sys->gamma_pw, dt = sys->dt;
-  const double cns_1 = sys->fr_fact_pw, yleft = sys->dy2, yright = sys->side.y + sys->dy2;
+  const orc_real mu = sys->mu_pw, kappa = sys->kappa_pw, gamma = sys->gamma_pw, dt = sys->dt;
+  const orc_real cns_1 = sys->fr_fact_pw, yleft = sys->dy2, yright = sys->side.y + sys->dy2;
   long ii;
 
   ORC_PARALLEL_FOR
@@ -859,7 +859,7 @@ void orc_force_walls (orc_vec3 *force, orc_vec3 *torque, const orc_system_par *s
   {
     const orc_particle *p = &pp[ii];
     orc_vec3 ff, tq;
-    double   ri, mass, km, gm;
+    orc_real   ri, mass, km, gm;
     int      ns;
 
     if (removed (sys, p->rr.x))
@@ -869,7 +869,7 @@ void orc_force_walls (orc_vec3 *force, orc_vec3 *torque, const orc_system_par *s
     for (ns = 0; ns < 4; ns++)
     {
       orc_vec3 s = p->rr_s[ns], rrc, nv;
-      double   dist, comp = 0.0;
+      orc_real   dist, comp = 0.0;
       int      touch = 0;
       if (p->rrot_s[ns].x <= ORC_LFUNNEL)
         continue;
@@ -897,8 +897,8 @@ void orc_force_walls (orc_vec3 *force, orc_vec3 *torque, const orc_system_par *s
 void orc_force_flume (orc_vec3 *force, orc_vec3 *torque, const orc_system_par *sys,
                       const orc_particle *pp)
 {
-  const double mu = sys->mu_pw, kappa = sys->kappa_pw, gamma = sys->gamma_pw, dt = sys->dt;
-  const double cns_1 = sys->fr_fact_pw, sint = sys->sint, cost = sys->cost, tant = sint/cost;
+  const orc_real mu = sys->mu_pw, kappa = sys->kappa_pw, gamma = sys->gamma_pw, dt = sys->dt;
+  const orc_real cns_1 = sys->fr_fact_pw, sint = sys->sint, cost = sys->cost, tant = sint/cost;
   long ii;
 
   ORC_PARALLEL_FOR
@@ -906,7 +906,7 @@ void orc_force_flume (orc_vec3 *force, orc_vec3 *torque, const orc_system_par *s
   {
     const orc_particle *p = &pp[ii];
     orc_vec3 ff, tq, nv;
-    double   ri, mass, km, gm;
+    orc_real   ri, mass, km, gm;
     int      ns;
 
     if (removed (sys, p->rr.x))
@@ -917,7 +917,7 @@ void orc_force_flume (orc_vec3 *force, orc_vec3 *torque, const orc_system_par *s
     for (ns = 0; ns < 4; ns++)
     {
       orc_vec3 s = p->rr_s[ns], rrc;
-      double   rect = -tant*s.x - s.z, dist = fabs (cost*rect);
+      orc_real   rect = -tant*s.x - s.z, dist = fabs (cost*rect);
       if (dist <= ri)
       {
         rrc.x = s.x - dist*sint;

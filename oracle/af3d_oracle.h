@@ -26,24 +26,32 @@
 extern "C" {
 #endif
 
-typedef struct { double x, y, z; } orc_vec3;
+/* The real type of the state and of every expression: double.  The tangent-linear model
+   (af3d_tangent.cpp) compiles af3d_oracle.c a second time, as C++, with ORC_REAL set to a
+   dual-number type carrying directional derivatives beside each value. */
+#ifndef ORC_REAL
+#define ORC_REAL double
+#endif
+typedef ORC_REAL orc_real;
+
+typedef struct { orc_real x, y, z; } orc_vec3;
 typedef struct { long x, y, z; } orc_lvec3;
 
 /* cabecera.hu:34-66 (256 bytes). */
 typedef struct {
   long     npart;
-  double   dt, hdt, rmin, rmax, v0, time, eps_pp, eps_pw, kappa_pp, kappa_pw, gamma_pp, gamma_pw,
+  orc_real   dt, hdt, rmin, rmax, v0, time, eps_pp, eps_pw, kappa_pp, kappa_pw, gamma_pp, gamma_pw,
            mu_pp, mu_pw, t_coll, tot_mass, tilt, xhopper, Lflume, gyr_max, fr_fact_pp, fr_fact_pw,
            sint, cost, sintg, costg, xfunnel, dy2;
   orc_vec3 side;
 } orc_system_par;
 
 /* cabecera.hu:69-74. */
-typedef struct { double sinfi, cosfi, tanfi; } orc_funnel;
+typedef struct { orc_real sinfi, cosfi, tanfi; } orc_funnel;
 
 /* cabecera.hu:77-98 (408 bytes).  rr_s[0..3] are rr_a..rr_d, rrot_s[0..3] are rrot_a..rrot_d. */
 typedef struct {
-  double   radius, mass, density;
+  orc_real   radius, mass, density;
   orc_vec3 moment_of_inertia;
   orc_vec3 rr_s[4];
   orc_vec3 rrot_s[4];

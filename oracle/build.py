@@ -1,10 +1,13 @@
 """Build recipe for the CPU oracle -- TEST INFRASTRUCTURE ONLY.
 
-Two libraries:
+Three libraries:
 
 * ``oracle/liboracle_af3d.so``: the plain-C restatement of the reference's
   host step routines (``af3d_oracle.c``).  Built everywhere, including the GPU
   box, because the GPU parity tests and the CPU baseline use it.
+* ``oracle/liboracle_tangent.so``: the FP64 tangent-linear model
+  (``af3d_tangent.cpp``: the same source compiled as C++ over a dual-number
+  type), the forward-mode reference for the engine's adjoint.  Built everywhere.
 * ``oracle/_ref/libaf3d_ref.so``: the reference's OWN routines, compiled from
   the unmodified sources where they lie in the read-only reference tree with
   the reference Makefile's flags (``nvcc -c -O2``, MakeAvalancheHst.mk:45-103)
@@ -24,6 +27,7 @@ from concurrent.futures import ThreadPoolExecutor
 HERE = os.path.dirname(os.path.abspath(__file__))
 REFERENCE_DIR = os.environ.get("AF3D_REFERENCE_DIR", "/root/reference")
 ORACLE_SO = os.path.join(HERE, "liboracle_af3d.so")
+TANGENT_SO = os.path.join(HERE, "liboracle_tangent.so")
 REF_DIR = os.path.join(HERE, "_ref")
 REF_SO = os.path.join(REF_DIR, "libaf3d_ref.so")
 
@@ -61,6 +65,17 @@ def build_oracle(force: bool = False) -> str:
     return ORACLE_SO
 
 
+def build_tangent(force: bool = False) -> str:
+    src = os.path.join(HERE, "af3d_tangent.cpp")
+    deps = [src, os.path.join(HERE, "af3d_oracle.c"), os.path.join(HERE, "af3d_oracle.h"), __file__]
+    if force or not _newer(TANGENT_SO, deps):
+        tmp = TANGENT_SO + ".tmp%d" % os.getpid()
+        _run(["g++", "-O2", "-fPIC", "-shared", "-std=c++17", "-ffp-contract=off", "-fvisibility=hidden",
+              "-o", tmp, src, "-lm"])
+        os.replace(tmp, TANGENT_SO)
+    return TANGENT_SO
+
+
 def reference_available() -> bool:
     return all(os.path.exists(os.path.join(REFERENCE_DIR, u + ".cu")) for u in REF_UNITS)
 
@@ -89,11 +104,15 @@ def build_ref(force: bool = False) -> str | None:
 
 
 def build(force: bool = False) -> None:
-    build_oracle(force)
+    with ThreadPoolExecutor(max_workers=2) as ex:
+        jobs = [ex.submit(build_oracle, force), ex.submit(build_tangent, force)]
+        for j in jobs:
+            j.result()
     build_ref(force)
 
 
 if __name__ == "__main__":
     build(force="--force" in sys.argv)
     print(ORACLE_SO)
+    print(TANGENT_SO)
     print(REF_SO if os.path.exists(REF_SO) else "(reference tree absent: _ref not built)")

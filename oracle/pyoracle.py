@@ -469,3 +469,75 @@ class OracleRun:
                     self.regrid()
                 cc0 += 1
         return 0
+
+
+class Tangent:
+    """The FP64 tangent-linear model (oracle/af3d_tangent.cpp): the oracle over dual numbers."""
+
+    def __init__(self, path: str | None = None):
+        if path is None:
+            from oracle import build as _b
+            path = _b.build_tangent()
+        self.lib = C.CDLL(path)
+        self.lib.tlm_directions.restype = C.c_int
+        self.lib.tlm_run.restype = C.c_int
+        self.lib.tlm_run.argtypes = [C.c_void_p] * 4 + [C.c_long, C.c_int, C.c_void_p, C.c_void_p, C.c_long,
+                                                        C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+        self.ndirs = int(self.lib.tlm_directions())
+
+    def run(self, sys, fun, cp, pp, steps, phase=PHASE_AVALANCHE, variant=FRICTION_HST, dsys=None, dpp=None):
+        """Start-up force pass + `steps` steps; returns (J, dJ[ndir], final state).  dsys: array
+        of SYSTEM_PAR (one per direction) holding the tangents of the system parameters; dpp:
+        array (ndir, n) of PARTICLE holding the tangents of the state."""
+        sys = np.ascontiguousarray(np.array(sys, dtype=SYSTEM_PAR))
+        fun = np.ascontiguousarray(np.array(fun, dtype=FUNNEL))
+        cp = np.ascontiguousarray(np.array(cp, dtype=CELL_PAR))
+        pp = np.ascontiguousarray(pp, dtype=PARTICLE)
+        n = len(pp)
+        ndir = len(dsys) if dsys is not None else (len(dpp) if dpp is not None else 0)
+        if ndir > self.ndirs:
+            raise ValueError("at most %d directions per run" % self.ndirs)
+        if dsys is not None:
+            dsys = np.ascontiguousarray(dsys, dtype=SYSTEM_PAR)
+            assert len(dsys) == ndir
+        if dpp is not None:
+            dpp = np.ascontiguousarray(dpp, dtype=PARTICLE)
+            assert dpp.shape == (ndir, n)
+        J = C.c_double()
+        dJ = np.zeros(max(ndir, 1))
+        out = np.zeros(n, dtype=PARTICLE)
+        st = self.lib.tlm_run(_p(sys), _p(fun), _p(cp), _p(pp) if n else None, n, ndir,
+                              _p(dsys) if dsys is not None else None, _p(dpp) if dpp is not None else None,
+                              int(steps), int(phase), int(variant), C.byref(J), _p(dJ), _p(out) if n else None)
+        if st != 0:
+            raise RuntimeError("tlm_run failed with status %d" % st)
+        return J.value, dJ[:ndir].copy(), out
+
+
+def state_tangent(pp: np.ndarray, sys, dr=None, dv=None, dw=None, dphi=None) -> np.ndarray:
+    """A PARTICLE-layout tangent of the state pp: position, velocity and angular-velocity
+    tangents (n, 3), and an orientation tangent dR = K(dphi) R (K the skew matrix of dphi, R's
+    rows Rmatx, Rmaty, Rmatz); the sphere centres follow r and R (init_Verlet.cu:130-142 is
+    linear in both) and the slope-frame copies rrot, rrot_s follow r and the sphere centres
+    (rotate_vectors.cu:28-46, linear; the wall routines of the start-up pass read them)."""
+    n = len(pp)
+    t = np.zeros(n, dtype=PARTICLE)
+    if dr is not None:
+        t["rr"] = dr
+    if dv is not None:
+        t["vv"] = dv
+    if dw is not None:
+        t["ww"] = dw
+    if dphi is not None:
+        R = np.stack([pp["Rmatx"], pp["Rmaty"], pp["Rmatz"]], 1)
+        k = np.asarray(dphi, dtype=np.float64)
+        K = np.zeros((n, 3, 3))
+        K[:, 0, 1], K[:, 0, 2], K[:, 1, 2] = -k[:, 2], k[:, 1], -k[:, 0]
+        K[:, 1, 0], K[:, 2, 0], K[:, 2, 1] = k[:, 2], -k[:, 1], k[:, 0]
+        dR = K @ R
+        t["Rmatx"], t["Rmaty"], t["Rmatz"] = dR[:, 0], dR[:, 1], dR[:, 2]
+    t["radius"] = pp["radius"]
+    sphere_centres(t)
+    t["radius"] = 0.0
+    rotate_slope(t, sys)
+    return t

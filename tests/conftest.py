@@ -25,3 +25,9 @@ def reference():
         pytest.skip("reference tree absent: the reference-built oracle is only available where it is")
     from oracle.pyoracle import Reference
     return Reference()
+
+
+@pytest.fixture(scope="session")
+def tangent():
+    from oracle.pyoracle import Tangent
+    return Tangent()

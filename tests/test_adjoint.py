@@ -164,6 +164,42 @@ def test_adjoint_orientations_vs_finite_differences(af3d, base):
     assert not bad, rows
 
 
+def test_adjoint_vs_tangent_linear_model(af3d, base, oracle, tangent):
+    """The adjoint against the FP64 CPU tangent-linear model (the oracle over dual numbers) on
+    the same run: eight directional derivatives -- each contact-law parameter, a random
+    perturbation of positions and orientations, and one of velocities and spins -- to 1e-7."""
+    from oracle.pyoracle import CELL_PAR, PARTICLE, SYSTEM_PAR, state_tangent
+    _, sys, fun, pp = base
+    out = _adjoint(af3d, sys, fun, pp)
+    rng = np.random.default_rng(17)
+    names = list(out["params"])
+    dsys = np.zeros(tangent.ndirs, dtype=SYSTEM_PAR)
+    for k, name in enumerate(names):
+        dsys[k][name] = float(sys[name])
+    dr, dphi = rng.standard_normal((N, 3)) * float(sys["rmax"]), rng.standard_normal((N, 3))
+    dv, dw = rng.standard_normal((N, 3)) * 10.0, rng.standard_normal((N, 3)) * 30.0
+    dpp = np.zeros((tangent.ndirs, N), dtype=PARTICLE)
+    dpp[6] = state_tangent(pp, sys, dr=dr, dphi=dphi)
+    dpp[7] = state_tangent(pp, sys, dv=dv, dw=dw)
+    # a coarse grid: the contacts found do not depend on the cell side
+    cp = np.zeros((), dtype=CELL_PAR)
+    cp["ntags"] = 128
+    cp["rr_max"], cp["rr_min"] = oracle.cell_dim(pp, sys)
+    s8 = sys.copy()
+    s8["rmax"] *= 8.0
+    oracle.grid_from_bbox(cp, s8)
+    J, dJ, _ = tangent.run(sys, fun, cp, pp, STEPS, dsys=dsys, dpp=dpp)
+    dR = np.stack([dpp[6]["Rmatx"], dpp[6]["Rmaty"], dpp[6]["Rmatz"]], 1)
+    adj =[out["params"][k] * float(sys[k]) for k in names]
+    adj.append(float(np.sum(out["r0"] * dr) + np.sum(out["R0"] * dR)))
+    adj.append(float(np.sum(out["v0"] * dv) + np.sum(out["w0"] * dw)))
+    adj = np.array(adj)
+    assert out["J"] == pytest.approx(J, rel=1e-12)
+    scale = float(np.abs(dJ).max())
+    bad = [(k, adj[k], dJ[k]) for k in range(8) if abs(adj[k] - dJ[k]) > 1e-7 * max(abs(dJ[k]), 1e-3 * scale)]
+    assert not bad, list(zip(adj, dJ))
+
+
 def test_adjoint_configuration_chain_vs_finite_differences(af3d, base):
     from avalancheflume3d_gb300.adjoint import config_gradients
     from avalancheflume3d_gb300.workloads import FlumeConfig
@@ -196,3 +232,31 @@ def test_adjoint_checkpoint_interval_does_not_matter(af3d, base):
     for k in a["params"]:
         assert a["params"][k] == pytest.approx(b["params"][k], rel=1e-9, abs=1e-12 * max(abs(a["params"][k]), 1e-300))
     assert np.allclose(a["r0"], b["r0"], rtol=1e-9, atol=1e-12 * float(np.abs(a["r0"]).max()))
+
+
+def test_ensemble_adjoint_equals_each_flume_alone(af3d):
+    """One backward sweep over an ensemble gives every flume's own J and gradients: those of the
+    flume run alone (up to the order of the FP64 atomic sums)."""
+    from tests.states import flume_system, wall_state
+    specs = [(300, 35.0, 0.5, 0.4, 0.5, 41), (180, 30.0, 0.3, 0.6, 0.7, 42), (240, 40.0, 0.8, 0.2, 0.3, 43)]
+    flumes = []
+    for n, tilt, mu_pp, mu_pw, eps, seed in specs:
+        sys, fun = flume_system(n, tilt=tilt, mu_pp=mu_pp, mu_pw=mu_pw, eps=eps)
+        flumes.append((sys, fun, wall_state(n, seed, sys)))
+    steps, ckpt = 60, 25
+    with af3d.Engine(np.stack([f[0] for f in flumes]), np.stack([f[1] for f in flumes])) as eng:
+        eng.import_particles(np.concatenate([f[2] for f in flumes]))
+        ens = eng.adjoint(steps, ckpt)
+    assert ens["J"].shape == (3,)
+    lo = 0
+    for f, (sys, fun, pp) in enumerate(flumes):
+        one = _adjoint(af3d, sys, fun, pp, steps=steps, ckpt=ckpt)
+        hi = lo + len(pp)
+        assert ens["J"][f] == pytest.approx(one["J"], rel=1e-13)
+        for k, v in one["params"].items():
+            assert ens["params"][k][f] == pytest.approx(v, rel=1e-9, abs=1e-12 * max(abs(v), 1e-300)), (f, k)
+        assert any(abs(v) > 0 for v in one["params"].values())
+        for key in ("r0", "v0", "w0", "R0"):
+            a, b = ens[key][lo:hi], one[key]
+            assert np.allclose(a, b, rtol=1e-9, atol=1e-12 * float(np.abs(b).max())), (f, key)
+        lo = hi
