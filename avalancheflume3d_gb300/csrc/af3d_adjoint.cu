@@ -473,14 +473,15 @@ constexpr int kAdjCoopBlock = 64;
 // with shared-memory atomics (a reverse needs no order).
 struct AdjQueue {
   ItemLists il;
-  double fb[32][6];
-  double own[32][21];
+  double fb[6][32];    // [component][lane]
+  double own[21][32];  // [component][lane]
 };
 
+// Adds v to three components of one lane's column (component stride 32).
 __device__ __forceinline__ void shared_add3(double *p, V3 v) {
   atomicAdd(p, v.x);
-  atomicAdd(p + 1, v.y);
-  atomicAdd(p + 2, v.z);
+  atomicAdd(p + 32, v.y);
+  atomicAdd(p + 64, v.z);
 }
 
 // Reverse of finish_Verlet, get_accel and every contact of one clump (startup: the start-up
@@ -564,9 +565,9 @@ __global__ void __launch_bounds__(kAdjCoopBlock) k_adj_forces(Planes P, Planes i
       st3(out, AAL, s, mk(0.0, 0.0, 0.0));
     }
   }
-  aq.fb[lane][0] = Fb.x; aq.fb[lane][1] = Fb.y; aq.fb[lane][2] = Fb.z;
-  aq.fb[lane][3] = Tb.x; aq.fb[lane][4] = Tb.y; aq.fb[lane][5] = Tb.z;
-  for (int k = 0; k < 21; k++) aq.own[lane][k] = 0.0;
+  aq.fb[0][lane] = Fb.x; aq.fb[1][lane] = Fb.y; aq.fb[2][lane] = Fb.z;
+  aq.fb[3][lane] = Tb.x; aq.fb[4][lane] = Tb.y; aq.fb[5][lane] = Tb.z;
+  for (int k = 0; k < 21; k++) aq.own[k][lane] = 0.0;
   // the contacts: the forward pass's item lists, reversed 32 a round
   const bool aval = c.phase == AF3D_PHASE_AVALANCHE;
   const double B = (double)cull[sv].c.w;
@@ -577,13 +578,13 @@ __global__ void __launch_bounds__(kAdjCoopBlock) k_adj_forces(Planes P, Planes i
     const int j = j0 + lane;
     if (j < total) {
       const int lo = owner_of(aq.il.base, j);
-      const unsigned it = aq.il.items[lo][j - aq.il.base[lo]];
+      const unsigned it = aq.il.items[j - aq.il.base[lo]][lo];
       const long os = wbase + lo;
       const NbrRec &om = nbr[os];
       const int of = flume[os];
       const Consts co = of == f ? c : load_consts(d, of);
-      const V3 fb_o = mk(aq.fb[lo][0], aq.fb[lo][1], aq.fb[lo][2]);
-      const V3 tb_o = mk(aq.fb[lo][3], aq.fb[lo][4], aq.fb[lo][5]);
+      const V3 fb_o = mk(aq.fb[0][lo], aq.fb[1][lo], aq.fb[2][lo]);
+      const V3 tb_o = mk(aq.fb[3][lo], aq.fb[4][lo], aq.fb[5][lo]);
       const V3 rl = mk(om.rx, om.ry, om.rz), vl = mk(om.vx, om.vy, om.vz), wl = mk(om.wx, om.wy, om.wz);
       ItemBar ib = zero_item();
       ParamBar ipar = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};   // this item's; the lane's flume or the owner's
@@ -619,22 +620,21 @@ __global__ void __launch_bounds__(kAdjCoopBlock) k_adj_forces(Planes P, Planes i
       } else {
         flush_params(param_b, of, ipar);
       }
-      double *ow = aq.own[lo];
-      shared_add3(ow + CR, ib.r);
-      shared_add3(ow + CV, ib.v);
-      shared_add3(ow + CW, ib.w);
-      shared_add3(ow + CS + 3 * k, ib.s);
+      double *ow = &aq.own[0][lo];
+      shared_add3(ow + 32 * CR, ib.r);
+      shared_add3(ow + 32 * CV, ib.v);
+      shared_add3(ow + 32 * CW, ib.w);
+      shared_add3(ow + 32 * (CS + 3 * k), ib.s);
     }
   }
   __syncwarp();
   if (act) {
     if (slow) adj_contacts_lane(s, o, c, g, off, B, Fb, Tb, acc, nbr, cull, start, order, ob, par);
-    const double *ow = aq.own[lane];
-    atomic_add3(acc, CR, s, ob.r + mk(ow[CR], ow[CR + 1], ow[CR + 2]));
-    atomic_add3(acc, CV, s, ob.v + mk(ow[CV], ow[CV + 1], ow[CV + 2]));
-    atomic_add3(acc, CW, s, ob.w + mk(ow[CW], ow[CW + 1], ow[CW + 2]));
-    for (int k = 0; k < 4; k++)
-      atomic_add3(acc, CS + 3 * k, s, ob.s[k] + mk(ow[CS + 3 * k], ow[CS + 3 * k + 1], ow[CS + 3 * k + 2]));
+    auto own3 = [&](int c0) { return mk(aq.own[c0][lane], aq.own[c0 + 1][lane], aq.own[c0 + 2][lane]); };
+    atomic_add3(acc, CR, s, ob.r + own3(CR));
+    atomic_add3(acc, CV, s, ob.v + own3(CV));
+    atomic_add3(acc, CW, s, ob.w + own3(CW));
+    for (int k = 0; k < 4; k++) atomic_add3(acc, CS + 3 * k, s, ob.s[k] + own3(CS + 3 * k));
   }
   add_params(param_b, f, par);
 }

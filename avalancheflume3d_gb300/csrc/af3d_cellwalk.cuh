@@ -170,12 +170,13 @@ constexpr unsigned kBndItem = 0xFFFFFF00u;   // boundary item: kBndItem | routin
 
 constexpr int kPassCap = 32;   // partners per clump that pass the centre test
 
-// Per-warp item lists in shared memory (one row per lane).
+// Per-warp item lists in shared memory, one column per lane ([entry][lane]): a lane's own
+// accesses always fall in its own bank, whatever entry each lane is at.
 struct ItemLists {
-  unsigned items[32][kLaneItems];
+  unsigned items[kLaneItems][32];
   int base[33];                          // exclusive prefix of the lanes' item counts
-  int pass_t[32][kPassCap];              // partner slots in walk order, per lane
-  unsigned short pass_m[32][kPassCap];   // their 16-bit sphere-pair masks
+  int pass_t[kPassCap][32];              // partner slots in walk order, per lane
+  unsigned short pass_m[kPassCap][32];   // their 16-bit sphere-pair masks
   int pbase[33];
 };
 
@@ -205,15 +206,16 @@ __device__ __forceinline__ int owner_of(const int *sh, int j) {
   return lo;
 }
 
-// Boundary items of the routines [r0, r1] for one clump; false if the list would overflow.
+// Boundary items of the routines [r0, r1] for one clump (appended to the lane's column `col`,
+// entry stride 32); false if the list would overflow.
 __device__ __forceinline__ bool push_boundary(int r0, int r1, const Own &o, double B, const Consts &c,
-                                              unsigned *items, int &nitems) {
+                                              unsigned *col, int &nitems) {
   for (int rt = r0; rt <= r1; rt++) {
     if (!bnd_may_touch(rt, o.r, B, c)) continue;
     for (int ns = 0; ns < 4; ns++) {
       if (!bnd_may_touch(rt, o.s[ns], o.rad, c)) continue;   // the gate applied to one sphere
       if (nitems == kLaneItems) return false;
-      items[nitems++] = kBndItem | (unsigned)(rt << 2) | (unsigned)ns;
+      col[32 * nitems++] = kBndItem | (unsigned)(rt << 2) | (unsigned)ns;
     }
   }
   return true;
@@ -237,7 +239,7 @@ __device__ __forceinline__ int build_item_lists(ItemLists &il, long wbase, long 
   const int post0 = aval ? R_FLUME : R_HOP0, post1 = aval ? R_FLUME : R_HOP2;
   int nitems = 0;
   slow = false;
-  unsigned *L = il.items[lane];
+  unsigned *L = &il.items[0][lane];   // the lane's column
   if (act) slow = !push_boundary(pre0, pre1, o, B, c, L, nitems);
   // Particle partners, stage 1 (per lane): walk the 27 neighbour cells in the reference's order
   // and keep the partners whose bounding spheres can touch (FP32 centre test).
@@ -252,7 +254,7 @@ __device__ __forceinline__ int build_item_lists(ItemLists &il, long wbase, long 
       if (d2f(mc, pc) > lim * lim * kCullSlack) return;
       const int t = order ? __ldg(&order[k]) : k;
       if (t == s) return;
-      if (npass < kPassCap) il.pass_t[lane][npass] = t;
+      if (npass < kPassCap) il.pass_t[npass][lane] = t;
       npass++;
     });
     if (npass > kPassCap) {
@@ -266,23 +268,39 @@ __device__ __forceinline__ int build_item_lists(ItemLists &il, long wbase, long 
     const int j = j0 + lane;
     if (j < total_pass) {
       const int ow = owner_of(il.pbase, j), k = j - il.pbase[ow];
-      il.pass_m[ow][k] = (unsigned short)sphere_mask(cull[wbase + ow], cull[il.pass_t[ow][k]]);
+      il.pass_m[k][ow] = (unsigned short)sphere_mask(cull[wbase + ow], cull[il.pass_t[k][ow]]);
     }
   }
   __syncwarp();
-  // Each lane's particle items, sph_id-major (the order of the sixteen force_part launches).
+  // Each lane's particle items, sph_id-major (the order of the sixteen force_part launches):
+  // the partners without a candidate sphere pair are dropped first (keeping the walk order), and
+  // only the sph_ids some partner has are visited.
   if (act && !slow) {
+    int m = 0;
+    unsigned any = 0u;
 #pragma unroll 1
-    for (int p = 0; p < 16 && !slow; p++)
+    for (int k = 0; k < npass; k++) {
+      const unsigned mk16 = il.pass_m[k][lane];
+      if (!mk16) continue;
+      il.pass_t[m][lane] = il.pass_t[k][lane];
+      il.pass_m[m][lane] = (unsigned short)mk16;
+      any |= mk16;
+      m++;
+    }
 #pragma unroll 1
-      for (int k = 0; k < npass; k++) {
-        if (!((il.pass_m[lane][k] >> p) & 1u)) continue;
+    while (any && !slow) {
+      const int p = __ffs(any) - 1;
+      any &= any - 1u;
+#pragma unroll 1
+      for (int k = 0; k < m; k++) {
+        if (!((il.pass_m[k][lane] >> p) & 1u)) continue;
         if (nitems == kLaneItems) {
           slow = true;
           break;
         }
-        L[nitems++] = ((unsigned)il.pass_t[lane][k] << 4) | (unsigned)p;   // (partner slot, sph_id-1)
+        L[32 * nitems++] = ((unsigned)il.pass_t[k][lane] << 4) | (unsigned)p;   // (partner slot, sph_id-1)
       }
+    }
     if (!slow) slow = !push_boundary(post0, post1, o, B, c, L, nitems);
   }
   return slow ? 0 : nitems;

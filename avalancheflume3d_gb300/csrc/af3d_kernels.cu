@@ -497,7 +497,7 @@ __device__ __forceinline__ int particle_contacts(long s, const Own &o, const Con
 // overflow runs its own clump alone afterwards, in the same order.
 struct WarpQueue {
   ItemLists il;
-  double res[32][6];
+  double res[6][32];   // [component][lane]
   int flag[32];
 };
 
@@ -523,7 +523,7 @@ __device__ __forceinline__ int warp_contacts(WarpQueue &wq, long wbase, long s, 
     const int j = j0 + lane;
     if (j < total) {
       const int lo = owner_of(wq.il.base, j);   // the lane whose list holds item j
-      const unsigned it = wq.il.items[lo][j - wq.il.base[lo]];
+      const unsigned it = wq.il.items[j - wq.il.base[lo]][lo];
       const NbrRec &me = nbr[wbase + lo];   // owner lanes hold clumps, so wbase + lo < n
       // the owner's flume may differ from this lane's at a flume boundary of an ensemble
       const int of = flume[wbase + lo];
@@ -556,8 +556,8 @@ __device__ __forceinline__ int warp_contacts(WarpQueue &wq, long wbase, long s, 
       if (kind && apply_law(ci, rl, co, fs, tq)) r = kind == 1 ? 2 : 3;
       wq.flag[lane] = r;
       if (r >= 2) {
-        wq.res[lane][0] = fs.x; wq.res[lane][1] = fs.y; wq.res[lane][2] = fs.z;
-        wq.res[lane][3] = tq.x; wq.res[lane][4] = tq.y; wq.res[lane][5] = tq.z;
+        wq.res[0][lane] = fs.x; wq.res[1][lane] = fs.y; wq.res[2][lane] = fs.z;
+        wq.res[3][lane] = tq.x; wq.res[4][lane] = tq.y; wq.res[5][lane] = tq.z;
       }
     }
     __syncwarp();
@@ -567,8 +567,8 @@ __device__ __forceinline__ int warp_contacts(WarpQueue &wq, long wbase, long s, 
       for (int e = a - j0; e < b - j0; e++) {
         const int fl = wq.flag[e];
         if (fl < 2) continue;
-        T.x += wq.res[e][3]; T.y += wq.res[e][4]; T.z += wq.res[e][5];
-        F.x += wq.res[e][0]; F.y += wq.res[e][1]; F.z += wq.res[e][2];
+        T.x += wq.res[3][e]; T.y += wq.res[4][e]; T.z += wq.res[5][e];
+        F.x += wq.res[0][e]; F.y += wq.res[1][e]; F.z += wq.res[2][e];
         active += fl == 2;   // sphere-sphere contacts only
       }
     }
