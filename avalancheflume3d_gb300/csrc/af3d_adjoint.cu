@@ -244,7 +244,7 @@ __device__ __forceinline__ bool wall_geom(int rt, const Sph &o, const Consts &c,
         if (dist <= ri) { touch = 4; rrc = mk(s.x, kYHOP_R, s.z); n = mk(0.0, 1.0, 0.0); comp = ri - dist; }
       } else {
         dist = s.z - kHOP_HEIGHT;
-        if (dist <= ri && c.time < 0.0) {
+        if (dist <= ri && *c.tp < 0.0) {
           touch = 5; rrc = mk(s.x, s.y, kHOP_HEIGHT); n = mk(0.0, 0.0, -1.0); comp = ri - dist;
         }
       }
@@ -517,7 +517,7 @@ __global__ void __launch_bounds__(kAdjCoopBlock) k_adj_forces(Planes P, Planes i
   o.w = mk(me.wx, me.wy, me.wz);
   for (int k = 0; k < 4; k++) o.s[k] = mk(me.s[3 * k], me.s[3 * k + 1], me.s[3 * k + 2]);
   o.rad = me.rad; o.msph = me.msph; o.mwall = me.mwall;
-  const bool removed = is_removed(c.time, o.r.x, c.side_x);
+  const bool removed = is_removed(*c.tp, o.r.x, c.side_x);
   const bool act = valid && !removed;
   ClumpBar ob;
   ob.r = ob.v = ob.w = mk(0.0, 0.0, 0.0);
@@ -572,7 +572,8 @@ __global__ void __launch_bounds__(kAdjCoopBlock) k_adj_forces(Planes P, Planes i
   const bool aval = c.phase == AF3D_PHASE_AVALANCHE;
   const double B = (double)cull[sv].c.w;
   bool slow = false;
-  const int nitems = build_item_lists(aq.il, wbase, sv, act, aval, B, o, c, g, off, cull, start, order, csort, slow);
+  const int nitems = build_item_lists(aq.il.pl, &aq.il.items[0][lane], 32, wbase, sv, act, aval, o.r, c, g,
+                                      d->flumes[f].gridf, off, cull, start, order, csort, slow);
   const int total = warp_prefix(nitems, aq.il.base);
   for (int j0 = 0; j0 < total; j0 += 32) {
     const int j = j0 + lane;

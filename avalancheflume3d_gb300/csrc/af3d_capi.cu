@@ -38,7 +38,8 @@ af3d_status fail(af3d_status code, const std::string &msg) {
 
 constexpr long kRegridEvery = 2000;   // avalanche_hst.cu:470 and :713 (cc % 2000 == 0)
 constexpr long kKernelsPerCellBuild = 7;   // predict/keys, 3 scan, scatter, rank, permute
-constexpr long kKernelsPerStep = kKernelsPerCellBuild + 2;   // + time advance, fused forces
+constexpr long kKernelsPerForcePass = 2;   // contact lists, fused forces
+constexpr long kKernelsPerStep = kKernelsPerCellBuild + 1 + kKernelsPerForcePass;   // + time advance
 constexpr long kKernelsPerKeptStep = kKernelsPerStep - 1;    // a step without the permutation
 constexpr long kKernelsPerRegrid = 4;
 // The clumps are moved into (cell, id) order by a permutation of every plane at most this many
@@ -91,6 +92,7 @@ struct af3d_ctx {
   int *flume_of_id = nullptr;                  // flume of every clump id
   NbrRec *nbr = nullptr;
   CullRec *cull = nullptr;
+  ContactLists lists{};   // the item lists of the current force pass
   Cells cells{};
   DevScalars *d = nullptr;
   DevFlume *flumes = nullptr;
@@ -150,6 +152,7 @@ void drop_graphs(af3d_ctx *c) {
 // Host-side parameter edits (system_par, Funnel, clock, phase, friction) to the device; the
 // device-derived grids are read back first so that they are not overwritten.
 af3d_status push_params(af3d_ctx *c) {
+  drop_graphs(c);   // graphs hold the constants of their force launches
   std::vector<DevFlume> fl(c->nflumes);
   AF3D_CUDA(cudaMemcpyAsync(fl.data(), c->flumes, sizeof(DevFlume) * c->nflumes, cudaMemcpyDeviceToHost, c->st));
   AF3D_CUDA(cudaStreamSynchronize(c->st));
@@ -208,6 +211,7 @@ af3d_status set_grids_device(af3d_ctx *c) {
   long long off = 0;
   for (int f = 0; f < c->nflumes; f++) {
     fl[f].grid = c->grid[f];
+    fl[f].gridf = grid_floats(c->grid[f]);
     fl[f].cell_off = off;
     off += c->grid[f].ncell3;
   }
@@ -256,14 +260,28 @@ void predict_for(af3d_ctx *c, bool predict, bool keys, bool t_prev, bool records
 
 // order: null when the slots were just permuted into (cell, id) order; out: where the corrected
 // velocities go.
-void forces_for(af3d_ctx *c, bool write_ft, const int *order, Planes out) {
+// A single-flume context passes its constants as a kernel parameter (from the host mirrors,
+// which push_params keeps equal to the device table; captured graphs are dropped whenever they
+// change).
+void forces_for(af3d_ctx *c, bool write_ft, const int *order, Planes out, cudaEvent_t between = nullptr) {
   const float4 *csort = order ? c->cells.csort : nullptr;
-  if (c->fp_mode == AF3D_FP_FAST)
+  Consts kc;
+  const Consts *uni = nullptr;
+  if (c->nflumes == 1) {
+    kc = make_consts(c->sys[0], c->fun[0], c->sys[0].sint / c->sys[0].cost, c->phase, c->variant, &c->d->time);
+    uni = &kc;
+  }
+  if (c->fp_mode == AF3D_FP_FAST) {
+    fast::launch_contact_lists(c->L(), c->d, c->fl_cur, c->nbr, c->cull, c->cells.start, order, csort, c->lists, uni);
+    if (between) cudaEventRecord(between, c->st);
     fast::launch_fused_forces(c->L(), c->cur, out, c->d, c->fl_cur, c->nbr, c->cull, c->cells.start, order,
-                              csort, write_ft);
-  else
-    launch_fused_forces(c->L(), c->cur, out, c->d, c->fl_cur, c->nbr, c->cull, c->cells.start, order, csort,
-                        write_ft);
+                              c->lists, write_ft, uni);
+  } else {
+    launch_contact_lists(c->L(), c->d, c->fl_cur, c->nbr, c->cull, c->cells.start, order, csort, c->lists, uni);
+    if (between) cudaEventRecord(between, c->st);
+    launch_fused_forces(c->L(), c->cur, out, c->d, c->fl_cur, c->nbr, c->cull, c->cells.start, order, c->lists,
+                        write_ft, uni);
+  }
 }
 
 void enqueue_cell_build(af3d_ctx *c, bool predict, bool t_prev, bool ft = true) {
@@ -462,6 +480,8 @@ af3d_status af3d_create_ensemble(int nflumes, const af3d_system_par *sys, const 
   ok = ok && cudaMalloc((void **)&c->flume_of_id, sizeof(int) * n) == cudaSuccess;
   ok = ok && cudaMalloc((void **)&c->nbr, sizeof(NbrRec) * n) == cudaSuccess;
   ok = ok && cudaMalloc((void **)&c->cull, sizeof(CullRec) * n) == cudaSuccess;
+  ok = ok && cudaMalloc((void **)&c->lists.items, sizeof(unsigned) * kListCap * n) == cudaSuccess;
+  ok = ok && cudaMalloc((void **)&c->lists.cnt, sizeof(int) * n) == cudaSuccess;
   ok = ok && cudaMalloc((void **)&c->cells.key, sizeof(int) * n) == cudaSuccess;
   ok = ok && cudaMalloc((void **)&c->cells.rank_tmp, sizeof(int) * n) == cudaSuccess;
   ok = ok && cudaMalloc((void **)&c->cells.tmp_slot, sizeof(int) * n) == cudaSuccess;
@@ -487,6 +507,7 @@ af3d_status af3d_create_ensemble(int nflumes, const af3d_system_par *sys, const 
     fl[f].sys = c->sys[f];
     fl[f].fun = c->fun[f];
     fl[f].grid = c->grid[f];
+    fl[f].gridf = grid_floats(c->grid[f]);
     fl[f].pending = c->grid[f];
     fl[f].tant = c->sys[f].sint / c->sys[f].cost;
   }
@@ -523,7 +544,7 @@ af3d_status af3d_destroy(af3d_ctx *c) {
   drop_graphs(c);
   for (void *p : {(void *)c->plane_mem[0], (void *)c->plane_mem[1], (void *)c->id_cur, (void *)c->id_alt,
                   (void *)c->fl_cur, (void *)c->fl_alt, (void *)c->flume_of_id, (void *)c->nbr,
-                  (void *)c->cull, (void *)c->cells.key, (void *)c->cells.rank_tmp, (void *)c->cells.tmp_slot,
+                  (void *)c->cull, (void *)c->lists.items, (void *)c->lists.cnt, (void *)c->cells.key, (void *)c->cells.rank_tmp, (void *)c->cells.tmp_slot,
                   (void *)c->cells.perm, (void *)c->cells.csort, (void *)c->cells.count, (void *)c->cells.start,
                   (void *)c->cells.block_sums, (void *)c->d, (void *)c->flumes, (void *)c->d_aos,
                   (void *)c->d_acc, (void *)c->d_anga, (void *)c->d_tmp, (void *)c->d_count})
@@ -799,7 +820,7 @@ af3d_status af3d_forces(af3d_ctx *c) {
   c->cells_valid = true;
   // Corrected velocities go to the dead plane set and are dropped: this pass stops at get_accel.
   forces_for(c, true, nullptr, c->alt);
-  c->launches += kKernelsPerCellBuild + 1;
+  c->launches += kKernelsPerCellBuild + kKernelsPerForcePass;
   c->records_valid = true;
   int flags = 0;
   af3d_status s = read_status(c, &flags);
@@ -859,14 +880,14 @@ af3d_status af3d_step_profile(af3d_ctx *c, long k, double *ms) {
     }
     AF3D_CUDA(cudaEventRecord(ev[4], c->st));
     if (resort) {
-      forces_for(c, false, nullptr, c->alt);
+      forces_for(c, false, nullptr, c->alt, ev[5]);
       swap_velocity_planes(c->cur, c->alt);
     } else {
-      forces_for(c, false, c->cells.perm, c->cur);
+      forces_for(c, false, c->cells.perm, c->cur, ev[5]);
     }
     swap_accel_planes(c->cur);
     swap_accel_planes(c->alt);
-    AF3D_CUDA(cudaEventRecord(ev[5], c->st));
+    AF3D_CUDA(cudaEventRecord(ev[6], c->st));
     c->sorted = resort;
     c->since_sort = resort ? 0 : c->since_sort + 1;
     c->launches += kernels_of(1, resort);
@@ -877,8 +898,8 @@ af3d_status af3d_step_profile(af3d_ctx *c, long k, double *ms) {
       af3d_status s = regrid(c);
       if (s) return s;
     }
-    AF3D_CUDA(cudaEventRecord(ev[6], c->st));
-    AF3D_CUDA(cudaEventSynchronize(ev[6]));
+    AF3D_CUDA(cudaEventRecord(ev[7], c->st));
+    AF3D_CUDA(cudaEventSynchronize(ev[7]));
     for (int p = 0; p < AF3D_NPROF; p++) {
       float t = 0.f;
       AF3D_CUDA(cudaEventElapsedTime(&t, ev[p], ev[p + 1]));

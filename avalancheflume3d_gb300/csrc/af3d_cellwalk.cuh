@@ -68,6 +68,37 @@ __device__ __forceinline__ long search_axis(double x, double xmin, double side, 
   return i;
 }
 
+// The same index from the FP32 culling coordinate xf and the FP32 grid copies: the estimate
+// q = (xf - xmin) * inv is within 2^-24 ((|x| + |xmin|) inv + 3 q) (1 + 2^-20) of the exact
+// quotient (four roundings), so when it is farther than eight times that bound from every
+// integer it truncates to the reference's index; otherwise (and for q near 0 or below) the FP64
+// path decides.
+__device__ __forceinline__ long search_axis_f(float xf, float xminf, float invf, double x, double xmin, double side,
+                                              double inv, long n) {
+  const float q = (xf - xminf) * invf;
+  const float E = 4.76837158203125e-07f * ((fabsf(xf) + fabsf(xminf)) * invf + 3.0f * q);   // 2^-21 (...)
+  if (q > E && q < 4.0e6f) {
+    const float tq = truncf(q);
+    const float fr = q - tq;   // exact: q and tq lie within a factor two of each other
+    if (fr > E && fr < 1.0f - E) {
+      long i = (long)tq;
+      if (i == n) i--;
+      return i;
+    }
+  }
+  return search_axis(x, xmin, side, inv, n);
+}
+
+__device__ __forceinline__ Search search_centre_f(float4 cf, V3 r, const af3d_cell_par &g, const GridF &gf,
+                                                  long long off) {
+  Search q;
+  q.off = off;
+  q.ci = search_axis_f(cf.x, gf.xmin, gf.ix, r.x, g.rr_min.x, g.cell_side.x, g.cs_inv.x, g.ncell.x);
+  q.cj = search_axis_f(cf.y, gf.ymin, gf.iy, r.y, g.rr_min.y, g.cell_side.y, g.cs_inv.y, g.ncell.y);
+  q.ck = search_axis_f(cf.z, gf.zmin, gf.iz, r.z, g.rr_min.z, g.cell_side.z, g.cs_inv.z, g.ncell.z);
+  return q;
+}
+
 __device__ __forceinline__ Search search_centre(V3 r, const af3d_cell_par &g, long long off) {
   Search q;
   q.off = off;
@@ -99,35 +130,6 @@ __device__ __forceinline__ void for_neighbour_slots(const Search &q, const af3d_
 #pragma unroll 1
         for (int t = t0; t < t1; t++) f(order ? __ldg(&order[t]) : t);
       }
-}
-
-// The positions (in the (cell, id) order) of the 27 neighbour cells' clumps, in the reference's
-// order, with every cell boundary loaded up front (as below).
-template <typename F>
-__device__ __forceinline__ void for_neighbour_positions_pre(const Search &q, const af3d_cell_par &g,
-                                                            const int *__restrict__ start, F &&f) {
-  int bnd[9][4];
-  const long x0 = q.ci - 1;
-#pragma unroll
-  for (int r = 0; r < 9; r++) {
-    const long jn = q.cj + (r / 3 - 1), kn = q.ck + (r % 3 - 1);
-    const bool row_ok = jn >= 0 && kn >= 0 && jn < g.ncell.y && kn < g.ncell.z;
-    const long rb = q.off + g.ncell.x * (jn + g.ncell.y * kn);
-#pragma unroll
-    for (int e = 0; e < 4; e++) {
-      long x = x0 + e;
-      x = x < 0 ? 0 : (x > g.ncell.x ? g.ncell.x : x);
-      bnd[r][e] = row_ok ? __ldg(&start[rb + x]) : 0;
-    }
-  }
-#pragma unroll 1
-  for (int di = 0; di < 3; di++)
-#pragma unroll 1
-    for (int r = 0; r < 9; r++) {
-      const int k0 = bnd[r][di], k1 = bnd[r][di + 1];
-#pragma unroll 1
-      for (int k = k0; k < k1; k++) f(k);
-    }
 }
 
 // The same visit with every cell boundary loaded up front.  The three cells of one (jdel, kdel)
@@ -165,19 +167,25 @@ __device__ __forceinline__ void for_neighbour_slots_pre(const Search &q, const a
 
 // ---- per-warp item lists (the warp-cooperative contact passes) -----------------------------
 
-constexpr int kLaneItems = 32;
+constexpr int kLaneItems = kListCap;
 constexpr unsigned kBndItem = 0xFFFFFF00u;   // boundary item: kBndItem | routine << 2 | sphere
 
 constexpr int kPassCap = 32;   // partners per clump that pass the centre test
+constexpr unsigned kSlotMask = 0x3FFFFFFFu;   // pass entry: slot | (x offset + 1) << 30
 
-// Per-warp item lists in shared memory, one column per lane ([entry][lane]): a lane's own
-// accesses always fall in its own bank, whatever entry each lane is at.
+// Per-warp partner lists of the two-stage gather in shared memory, one column per lane
+// ([entry][lane]): a lane's own accesses always fall in its own bank.
+struct PassLists {
+  unsigned pass_t[kPassCap][32];         // partner slot | (cell x offset + 1) << 30, per lane
+  unsigned short pass_m[kPassCap][32];   // their 16-bit sphere-pair masks
+  int pbase[33];
+};
+
+// Item lists held in shared memory (the adjoint's cooperative reverse).
 struct ItemLists {
   unsigned items[kLaneItems][32];
   int base[33];                          // exclusive prefix of the lanes' item counts
-  int pass_t[kPassCap][32];              // partner slots in walk order, per lane
-  unsigned short pass_m[kPassCap][32];   // their 16-bit sphere-pair masks
-  int pbase[33];
+  PassLists pl;
 };
 
 // Exclusive prefix of `v` over the warp into sh[0..32]; returns the total.
@@ -206,84 +214,125 @@ __device__ __forceinline__ int owner_of(const int *sh, int j) {
   return lo;
 }
 
-// Boundary items of the routines [r0, r1] for one clump (appended to the lane's column `col`,
-// entry stride 32); false if the list would overflow.
-__device__ __forceinline__ bool push_boundary(int r0, int r1, const Own &o, double B, const Consts &c,
-                                              unsigned *col, int &nitems) {
+// Boundary items of the routines [r0, r1] for one clump (culling record me), appended to the
+// lane's item column `col` (entries `stride` apart); false if the list would overflow.  The FP32
+// gates admit every sphere the routine can touch (and a few more, which the exact test of the
+// force pass then rejects).
+__device__ __forceinline__ bool push_boundary(int r0, int r1, const CullRec &me, const Consts &c, bool door_closed,
+                                              unsigned *col, long stride, int &nitems) {
   for (int rt = r0; rt <= r1; rt++) {
-    if (!bnd_may_touch(rt, o.r, B, c)) continue;
+    if (!bnd_may_touch_f(rt, me.c, me.c.w, c, door_closed)) continue;
     for (int ns = 0; ns < 4; ns++) {
-      if (!bnd_may_touch(rt, o.s[ns], o.rad, c)) continue;   // the gate applied to one sphere
+      if (!bnd_may_touch_f(rt, me.s[ns], me.s[ns].w, c, door_closed)) continue;   // one sphere
       if (nitems == kLaneItems) return false;
-      col[32 * nitems++] = kBndItem | (unsigned)(rt << 2) | (unsigned)ns;
+      col[stride * nitems++] = kBndItem | (unsigned)(rt << 2) | (unsigned)ns;
     }
   }
   return true;
+}
+
+// Stage 1 of the gather (per lane): the partners among the 27 neighbour cells whose bounding
+// spheres can touch the clump's (FP32 centre test).  The three cells of one (jdel, kdel) row are
+// consecutive in the linear cell index, so their members form one slot range split by four
+// start[] values; the nine ranges are walked one after another, two slots a turn with both
+// loads issued together.  Each kept partner is tagged with its cell's x offset (0..2) so that
+// the reference's visiting order (idel, then jdel, kdel, then slot) can be restored.  Returns
+// the number of partners found (which may exceed kPassCap).
+__device__ __forceinline__ int gather_partners(PassLists &pl, long s, float4 mc, const Search &q,
+                                               const af3d_cell_par &g, const int *__restrict__ start,
+                                               const int *__restrict__ order, const float4 *__restrict__ csort,
+                                               const CullRec *__restrict__ cull) {
+  const int lane = threadIdx.x & 31;
+  int npass = 0;
+  auto keep = [&](int k, unsigned tag, float4 pc) {
+    const float lim = mc.w + pc.w;
+    if (d2f(mc, pc) > lim * lim * kCullSlack) return;
+    const int t = order ? __ldg(&order[k]) : k;
+    if (t == s) return;
+    if (npass < kPassCap) pl.pass_t[npass][lane] = (unsigned)t | (tag << 30);
+    npass++;
+  };
+  const long x0 = q.ci - 1;
+#pragma unroll 1
+  for (int r = 0; r < 9; r++) {
+    const long jn = q.cj + (r / 3 - 1), kn = q.ck + (r % 3 - 1);
+    if (jn < 0 || kn < 0 || jn >= g.ncell.y || kn >= g.ncell.z) continue;
+    const long rb = q.off + g.ncell.x * (jn + g.ncell.y * kn);
+    // boundary e of the row: start of cell x0 + e, clamped into the row (empty cells outside)
+    int b[4];
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+      long x = x0 + e;
+      x = x < 0 ? 0 : (x > g.ncell.x ? g.ncell.x : x);
+      b[e] = __ldg(&start[rb + x]);
+    }
+    int k = b[0];
+#pragma unroll 1
+    for (; k + 1 < b[3]; k += 2) {
+      const float4 p0 = order ? __ldg(&csort[k]) : cull[k].c;
+      const float4 p1 = order ? __ldg(&csort[k + 1]) : cull[k + 1].c;
+      keep(k, 1u + (k >= b[1]) + (k >= b[2]), p0);
+      keep(k + 1, 1u + (k + 1 >= b[1]) + (k + 1 >= b[2]), p1);
+    }
+    if (k < b[3]) keep(k, 1u + (k >= b[1]) + (k >= b[2]), order ? __ldg(&csort[k]) : cull[k].c);
+  }
+  return npass;
 }
 
 // Every lane's item list of one contact pass, in the reference's order: the boundary routines
 // before the particles (avalanche: hop x3, funnel, fcorners, walls), the particle contacts
 // sph_id-major, the routines after them (avalanche: flume; fill: hop x3).  Boundary items
 // (routine, sphere) for the spheres the routine's 1-Lipschitz gate cannot rule out; particle
-// items (partner slot, sph_id) from a two-stage gather: stage 1 (per lane) walks the 27
-// neighbour cells keeping the partners whose bounding spheres can touch, stage 2 (whole warp)
-// runs the sixteen sphere tests of every kept partner, 32 a round.  All 32 lanes call this;
-// returns the lane's item count, 0 with `slow` set when the lane's lists would overflow.
-__device__ __forceinline__ int build_item_lists(ItemLists &il, long wbase, long s, bool act, bool aval, double B,
-                                                const Own &o, const Consts &c, const af3d_cell_par &g,
-                                                long long off, const CullRec *__restrict__ cull,
-                                                const int *__restrict__ start, const int *__restrict__ order,
-                                                const float4 *__restrict__ csort, bool &slow) {
+// items (partner slot, sph_id) from a two-stage gather: stage 1 (per lane, gather_partners)
+// keeps the partners whose bounding spheres can touch, stage 2 (whole warp) runs the sixteen
+// sphere tests of every kept partner, 32 a round.  Items go to the lane's column `col`, entries
+// `stride` apart.  All 32 lanes call this; returns the lane's item count, 0 with `slow` set
+// when the lane's lists would overflow.
+__device__ __forceinline__ int build_item_lists(PassLists &pl, unsigned *col, long stride, long wbase, long s,
+                                                bool act, bool aval, V3 r, const Consts &c,
+                                                const af3d_cell_par &g, const GridF &gf, long long off,
+                                                const CullRec *__restrict__ cull, const int *__restrict__ start,
+                                                const int *__restrict__ order, const float4 *__restrict__ csort,
+                                                bool &slow) {
   const int lane = threadIdx.x & 31;
   const int pre0 = aval ? R_HOP0 : 1, pre1 = aval ? R_WALLS : 0;         // fill: none before
   const int post0 = aval ? R_FLUME : R_HOP0, post1 = aval ? R_FLUME : R_HOP2;
   int nitems = 0;
   slow = false;
-  unsigned *L = &il.items[0][lane];   // the lane's column
-  if (act) slow = !push_boundary(pre0, pre1, o, B, c, L, nitems);
-  // Particle partners, stage 1 (per lane): walk the 27 neighbour cells in the reference's order
-  // and keep the partners whose bounding spheres can touch (FP32 centre test).
+  const CullRec me = cull[s];
+  const bool door_closed = *c.tp < 0.0;
+  if (act) slow = !push_boundary(pre0, pre1, me, c, door_closed, col, stride, nitems);
   int npass = 0;
   if (act && !slow) {
-    const float4 mc = cull[s].c;
-    const Search q = search_centre(o.r, g, off);
-    for_neighbour_positions_pre(q, g, start, [&](int k) {
-      // the culling centre at position k: contiguous along a cell row in either layout
-      const float4 pc = order ? __ldg(&csort[k]) : cull[k].c;
-      const float lim = mc.w + pc.w;
-      if (d2f(mc, pc) > lim * lim * kCullSlack) return;
-      const int t = order ? __ldg(&order[k]) : k;
-      if (t == s) return;
-      if (npass < kPassCap) il.pass_t[npass][lane] = t;
-      npass++;
-    });
+    npass = gather_partners(pl, s, me.c, search_centre_f(me.c, r, g, gf, off), g, start, order, csort, cull);
     if (npass > kPassCap) {
       slow = true;
       npass = 0;
     }
   }
   // Stage 2 (whole warp): the sixteen sphere tests of every kept partner, 32 partners a round.
-  const int total_pass = warp_prefix(npass, il.pbase);
+  const int total_pass = warp_prefix(npass, pl.pbase);
   for (int j0 = 0; j0 < total_pass; j0 += 32) {
     const int j = j0 + lane;
     if (j < total_pass) {
-      const int ow = owner_of(il.pbase, j), k = j - il.pbase[ow];
-      il.pass_m[k][ow] = (unsigned short)sphere_mask(cull[wbase + ow], cull[il.pass_t[k][ow]]);
+      const int ow = owner_of(pl.pbase, j), k = j - pl.pbase[ow];
+      pl.pass_m[k][ow] = (unsigned short)sphere_mask(cull[wbase + ow], cull[pl.pass_t[k][ow] & kSlotMask]);
     }
   }
   __syncwarp();
-  // Each lane's particle items, sph_id-major (the order of the sixteen force_part launches):
-  // the partners without a candidate sphere pair are dropped first (keeping the walk order), and
-  // only the sph_ids some partner has are visited.
+  // Each lane's particle items, sph_id-major (the order of the sixteen force_part launches), and
+  // within one sph_id in the reference's cell order: x offset, then row, then slot.  Partners
+  // without a candidate sphere pair are dropped first (keeping the walk order), and only the
+  // sph_ids some partner has are visited.
   if (act && !slow) {
     int m = 0;
     unsigned any = 0u;
 #pragma unroll 1
     for (int k = 0; k < npass; k++) {
-      const unsigned mk16 = il.pass_m[k][lane];
+      const unsigned mk16 = pl.pass_m[k][lane];
       if (!mk16) continue;
-      il.pass_t[m][lane] = il.pass_t[k][lane];
-      il.pass_m[m][lane] = (unsigned short)mk16;
+      pl.pass_t[m][lane] = pl.pass_t[k][lane];
+      pl.pass_m[m][lane] = (unsigned short)mk16;
       any |= mk16;
       m++;
     }
@@ -292,16 +341,19 @@ __device__ __forceinline__ int build_item_lists(ItemLists &il, long wbase, long 
       const int p = __ffs(any) - 1;
       any &= any - 1u;
 #pragma unroll 1
-      for (int k = 0; k < m; k++) {
-        if (!((il.pass_m[k][lane] >> p) & 1u)) continue;
-        if (nitems == kLaneItems) {
-          slow = true;
-          break;
+      for (unsigned tag = 1; tag <= 3 && !slow; tag++)
+#pragma unroll 1
+        for (int k = 0; k < m; k++) {
+          const unsigned e = pl.pass_t[k][lane];
+          if ((e >> 30) != tag || !((pl.pass_m[k][lane] >> p) & 1u)) continue;
+          if (nitems == kLaneItems) {
+            slow = true;
+            break;
+          }
+          col[stride * nitems++] = ((e & kSlotMask) << 4) | (unsigned)p;   // (partner slot, sph_id-1)
         }
-        L[32 * nitems++] = ((unsigned)il.pass_t[k][lane] << 4) | (unsigned)p;   // (partner slot, sph_id-1)
-      }
     }
-    if (!slow) slow = !push_boundary(post0, post1, o, B, c, L, nitems);
+    if (!slow) slow = !push_boundary(post0, post1, me, c, door_closed, col, stride, nitems);
   }
   return slow ? 0 : nitems;
 }

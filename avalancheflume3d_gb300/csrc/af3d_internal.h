@@ -69,10 +69,23 @@ struct Cells {
 // One flume of the context (a plain drop-in run has one; a batched ensemble has many).  Every
 // flume has its own system_par (friction, restitution, slope, ...), Funnel and cell grid; all
 // flumes share dt and advance in lockstep.
+// FP32 copies of a grid's origin and inverse cell sides (the search-cell estimate).
+struct GridF {
+  float xmin, ymin, zmin, ix, iy, iz;
+};
+
+__host__ __device__ inline GridF grid_floats(const af3d_cell_par &g) {
+  GridF q;
+  q.xmin = (float)g.rr_min.x; q.ymin = (float)g.rr_min.y; q.zmin = (float)g.rr_min.z;
+  q.ix = (float)g.cs_inv.x; q.iy = (float)g.cs_inv.y; q.iz = (float)g.cs_inv.z;
+  return q;
+}
+
 struct DevFlume {
   af3d_system_par sys;        // sys.time is unused: the shared clock is DevScalars::time
   af3d_funnel     fun;
   af3d_cell_par   grid;
+  GridF           gridf;      // grid_floats(grid), written with it
   long long       cell_off;   // first bucket of this flume's cells
   double          tant;       // sys.sint / sys.cost (force_flume.cu's tangent), set by the host
   unsigned long long bbox[8]; // re-grid scratch: ordered-int min/max of x, y, z, max vx, min vz
@@ -92,6 +105,50 @@ struct DevScalars {
   long long       pending;     // > 0: a re-grid derived grids needing this many cell buckets
   DevFlume       *flumes;      // [nflumes]
 };
+
+// Per-clump item lists of one force pass, from the list kernel to the force kernel: entry e of
+// slot s at items[e * n + s] (an item is a boundary (routine, sphere) or a particle (partner
+// slot, sph_id) contact), and the count at cnt[s] (-1: the clump's lists overflowed and the
+// force kernel walks its neighbours itself).
+constexpr int kListCap = 32;
+struct ContactLists {
+  unsigned *items;   // [kListCap][n]
+  int *cnt;          // [n]
+};
+
+// Scalars of one flume's system_par / Funnel used by the force routines.  A single-flume
+// context passes them to the fused force kernel as a __grid_constant__ parameter (constant-bank
+// operands, no registers held); the clock is read through `tp` (it advances on the device).
+struct Consts {
+  double dt, hdt;
+  double mu_pp, kappa_pp, gamma_pp, cns_pp;
+  double mu_pw, kappa_pw, gamma_pw, cns_pw;
+  double sint, cost, dy2, side_x, side_y;
+  double sinfi, cosfi, tanfi;
+  double tant;     // sint / cost
+  double inv_dt;   // 1 / dt (fast mode)
+  const double *tp;   // the device clock, DevScalars::time
+  float cost_f, sint_f, tanfi_f, cosfi_f, dy2_f, side_y_f;   // FP32 copies for the culling gates
+  int phase, variant;
+};
+
+// The constants of a flume from its parameters (the same values the device loads).
+__host__ __device__ inline Consts make_consts(const af3d_system_par &s, const af3d_funnel &fun, double tant, int phase, int variant,
+                          const double *tp) {
+  Consts c;
+  c.dt = s.dt; c.hdt = s.hdt;
+  c.mu_pp = s.mu_pp; c.kappa_pp = s.kappa_pp; c.gamma_pp = s.gamma_pp; c.cns_pp = s.fr_fact_pp;
+  c.mu_pw = s.mu_pw; c.kappa_pw = s.kappa_pw; c.gamma_pw = s.gamma_pw; c.cns_pw = s.fr_fact_pw;
+  c.sint = s.sint; c.cost = s.cost; c.dy2 = s.dy2; c.side_x = s.side.x; c.side_y = s.side.y;
+  c.sinfi = fun.sinfi; c.cosfi = fun.cosfi; c.tanfi = fun.tanfi;
+  c.tant = tant;
+  c.inv_dt = 1.0 / s.dt;
+  c.tp = tp;
+  c.cost_f = (float)s.cost; c.sint_f = (float)s.sint; c.tanfi_f = (float)fun.tanfi; c.cosfi_f = (float)fun.cosfi;
+  c.dy2_f = (float)s.dy2; c.side_y_f = (float)s.side.y;
+  c.phase = phase; c.variant = variant;
+  return c;
+}
 
 // Which force routines a boundary kernel applies, in the reference's call order.
 enum Routine : int {
@@ -122,11 +179,15 @@ void launch_permute_records (const Launch &L, Planes src, Planes dst, const int 
                              const long long *id_src, long long *id_dst, const int *fl_src,
                              int *fl_dst, NbrRec *nbr, CullRec *cull, bool ft);
 void launch_build_records (const Launch &L, Planes cur, NbrRec *nbr, CullRec *cull);
-// order: null when the slots are in (cell, id) order, else cells.perm of the last sort, with
-// csort the matching culling centres.
+// The force pass: the item lists (launch_contact_lists), then the force kernel.  order: null
+// when the slots are in (cell, id) order, else cells.perm of the last sort, with csort the
+// matching culling centres.
+void launch_contact_lists (const Launch &L, DevScalars *d, const int *flume, const NbrRec *nbr,
+                           const CullRec *cull, const int *start, const int *order, const float4 *csort,
+                           ContactLists lists, const Consts *uniform = nullptr);
 void launch_fused_forces (const Launch &L, Planes cur, Planes out, DevScalars *d, const int *flume,
                           const NbrRec *nbr, const CullRec *cull, const int *start, const int *order,
-                          const float4 *csort, bool write_ft);
+                          ContactLists lists, bool write_ft, const Consts *uniform = nullptr);
 void launch_boundary (const Launch &L, Planes cur, DevScalars *d, const int *flume, int routine);
 void launch_part (const Launch &L, Planes cur, DevScalars *d, const int *flume, const NbrRec *nbr,
                   const CullRec *cull, const int *start, int sph_id);
@@ -175,9 +236,12 @@ namespace fast {
 void launch_predict (const Launch &L, Planes cur, DevScalars *d, bool predict, bool keys, bool t_prev,
                      Cells cells, const long long *id, const int *flume, NbrRec *nbr = nullptr,
                      CullRec *cull = nullptr);
+void launch_contact_lists (const Launch &L, DevScalars *d, const int *flume, const NbrRec *nbr,
+                           const CullRec *cull, const int *start, const int *order, const float4 *csort,
+                           ContactLists lists, const Consts *uniform = nullptr);
 void launch_fused_forces (const Launch &L, Planes cur, Planes out, DevScalars *d, const int *flume,
                           const NbrRec *nbr, const CullRec *cull, const int *start, const int *order,
-                          const float4 *csort, bool write_ft);
+                          ContactLists lists, bool write_ft, const Consts *uniform = nullptr);
 }  // namespace fast
 
 }  // namespace af3d

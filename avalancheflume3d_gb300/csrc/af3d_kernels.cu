@@ -485,22 +485,25 @@ __device__ __forceinline__ int particle_contacts(long s, const Own &o, const Con
 // Warp-cooperative pass of the fused kernel over every contact of a clump: the boundary routines
 // that run before the particle contacts, the sixteen sph_id passes, and the routines that run
 // after them (avalanche: hop x3, funnel, fcorners, walls | part x16 | flume; fill: part x16 |
-// hop x3).  Every lane publishes its clump's item list in that order in shared memory: boundary
-// items (routine, sphere) for the spheres the routine's 1-Lipschitz gate cannot rule out, and
-// particle items (partner slot, sph_id) in sph_id-major order.  The warp then works through the
-// concatenated lists 32 items per round, one item per lane, reading the owner clump from its
-// record; after each round every owner adds its items' force and torque terms to its own sums in
-// list order.  The FP64 contact laws thus run with all lanes busy whatever the spread of
-// contacts and walls over the clumps, and each clump's summation order stays the reference's.
-// All 32 lanes of the warp must call this; `act` is false for lanes without a clump to process
-// (and for removed clumps); `wbase` is the slot of the warp's lane 0.  A lane whose list would
-// overflow runs its own clump alone afterwards, in the same order.
+// hop x3).  The list kernel (k_contact_lists) has published every clump's item list in that
+// order: boundary items (routine, sphere) for the spheres the routine's 1-Lipschitz gate cannot
+// rule out, and particle items (partner slot, sph_id) in sph_id-major order.  The warp works
+// through the concatenated lists of its 32 clumps 32 items per round, one item per lane, reading
+// the owner clump from its record; after each round every owner adds its items' force and
+// torque terms to its own sums in list order.  The FP64 contact laws thus run with all lanes
+// busy whatever the spread of contacts and walls over the clumps, and each clump's summation
+// order stays the reference's.  All 32 lanes of the warp must call this; `act` is false for
+// lanes without a clump to process (and for removed clumps); `wbase` is the slot of the warp's
+// lane 0.  A clump whose lists overflowed runs alone afterwards, in the same order.
 struct WarpQueue {
-  ItemLists il;
+  int base[33];        // exclusive prefix of the lanes' item counts
   double res[6][32];   // [component][lane]
   int flag[32];
 };
 
+// UNIFORM: every clump of the launch belongs to one flume, whose constants `c` are (a
+// reference to) a kernel parameter.
+template <bool UNIFORM>
 __device__ __forceinline__ int warp_contacts(WarpQueue &wq, long wbase, long s, bool act, bool aval,
                                              double B, const Own &o, const Consts &c,
                                              const af3d_cell_par &g, long long off,
@@ -509,51 +512,60 @@ __device__ __forceinline__ int warp_contacts(WarpQueue &wq, long wbase, long s, 
                                              const CullRec *__restrict__ cull,
                                              const int *__restrict__ start,
                                              const int *__restrict__ order,
-                                             const float4 *__restrict__ csort, V3 &F, V3 &T) {
+                                             const unsigned *__restrict__ items, int listed, long n,
+                                             V3 &F, V3 &T) {
   const int lane = threadIdx.x & 31;
-  const int my_flume = flume[s];
   const int pre0 = aval ? R_HOP0 : 1, pre1 = aval ? R_WALLS : 0;         // fill: none before
   const int post0 = aval ? R_FLUME : R_HOP0, post1 = aval ? R_FLUME : R_HOP2;
-  bool slow = false;
-  int nitems = build_item_lists(wq.il, wbase, s, act, aval, B, o, c, g, off, cull, start, order, csort, slow);
-  const int total = warp_prefix(nitems, wq.il.base);
-  const int base = wq.il.base[lane];
+  const bool slow = act && listed < 0;
+  const int nitems = act && listed > 0 ? listed : 0;
+  const int total = warp_prefix(nitems, wq.base);
+  const int base = wq.base[lane];
   int active = 0;
   for (int j0 = 0; j0 < total; j0 += 32) {
     const int j = j0 + lane;
     if (j < total) {
-      const int lo = owner_of(wq.il.base, j);   // the lane whose list holds item j
-      const unsigned it = wq.il.items[j - wq.il.base[lo]][lo];
+      const int lo = owner_of(wq.base, j);   // the lane whose list holds item j
+      const unsigned it = __ldg(&items[(long)(j - wq.base[lo]) * n + wbase + lo]);
       const NbrRec &me = nbr[wbase + lo];   // owner lanes hold clumps, so wbase + lo < n
-      // the owner's flume may differ from this lane's at a flume boundary of an ensemble
-      const int of = flume[wbase + lo];
-      const Consts co = of == my_flume ? c : load_consts(d, of);
       // Prepare the item's contact (type-specific, short), then run the contact law once for
       // every lane that has a contact, whatever its type.
-      ContactIn ci;
-      V3 rl = mk(me.rx, me.ry, me.rz);
-      int kind;   // 0 nothing, 1 sphere pair, 2 wall
-      if (it >= kBndItem) {
-        const int rt = (int)((it >> 2) & 7u), ns = (int)(it & 3u);
-        Sph q;
-        q.r = rl;
-        q.v = mk(me.vx, me.vy, me.vz);
-        q.w = mk(me.wx, me.wy, me.wz);
-        q.s = mk(me.s[3 * ns], me.s[3 * ns + 1], me.s[3 * ns + 2]);
-        q.rad = me.rad;
-        q.mwall = me.mwall;
-        kind = bnd_input(rt, q, co, ci) ? 2 : 0;
-      } else {
-        const int t = (int)(it >> 4), p = (int)(it & 15u);
-        const V3 vl = mk(me.vx, me.vy, me.vz), wl = mk(me.wx, me.wy, me.wz);
-        const int k = p & 3;
-        const V3 s1 = mk(me.s[3 * k], me.s[3 * k + 1], me.s[3 * k + 2]);
-        kind = pair_input(rl, vl, wl, s1, me.rad, me.msph, nbr[t], p >> 2, co,
-                          co.variant == AF3D_FRICTION_DEV, ci) ? 1 : 0;
-      }
+      auto contact = [&](const Consts &co, V3 &fs, V3 &tq) -> int {
+        ContactIn ci;
+        V3 rl = mk(me.rx, me.ry, me.rz);
+        int kind;   // 0 nothing, 1 sphere pair, 2 wall
+        if (it >= kBndItem) {
+          const int rt = (int)((it >> 2) & 7u), ns = (int)(it & 3u);
+          Sph q;
+          q.r = rl;
+          q.v = mk(me.vx, me.vy, me.vz);
+          q.w = mk(me.wx, me.wy, me.wz);
+          q.s = mk(me.s[3 * ns], me.s[3 * ns + 1], me.s[3 * ns + 2]);
+          q.rad = me.rad;
+          q.mwall = me.mwall;
+          kind = bnd_input(rt, q, co, ci) ? 2 : 0;
+        } else {
+          const int t = (int)(it >> 4), p = (int)(it & 15u);
+          const V3 vl = mk(me.vx, me.vy, me.vz), wl = mk(me.wx, me.wy, me.wz);
+          const int k = p & 3;
+          const V3 s1 = mk(me.s[3 * k], me.s[3 * k + 1], me.s[3 * k + 2]);
+          kind = pair_input(rl, vl, wl, s1, me.rad, me.msph, nbr[t], p >> 2, co,
+                            co.variant == AF3D_FRICTION_DEV, ci) ? 1 : 0;
+        }
+        int r = kind == 1 ? 1 : 0;
+        if (kind && apply_law(ci, rl, co, fs, tq)) r = kind == 1 ? 2 : 3;
+        return r;
+      };
       V3 fs, tq;
-      int r = kind == 1 ? 1 : 0;
-      if (kind && apply_law(ci, rl, co, fs, tq)) r = kind == 1 ? 2 : 3;
+      int r;
+      if constexpr (UNIFORM) {
+        r = contact(c, fs, tq);
+      } else {
+        // the owner's flume may differ from this lane's at a flume boundary of an ensemble
+        const int of = flume[wbase + lo];
+        const Consts co = of == flume[s] ? c : load_consts(d, of);
+        r = contact(co, fs, tq);
+      }
       wq.flag[lane] = r;
       if (r >= 2) {
         wq.res[0][lane] = fs.x; wq.res[1][lane] = fs.y; wq.res[2][lane] = fs.z;
@@ -614,90 +626,134 @@ __device__ __forceinline__ void warp_count(DevScalars *d, int active) {
   if ((threadIdx.x & 31) == 0 && v) atomicAdd(&d->contacts, (unsigned long long)v);
 }
 
-// The whole force pass of one step for clump s, in the reference's call order, then get_accel
-// and finish_Verlet.  Velocities after the corrector go to `out` (the other plane set), because
-// neighbours still read this step's predicted velocities from the records.  Every lane of a
-// launched warp reaches the warp-cooperative contact pass (lanes past n take no clump).
-#ifndef AF3D_COOP
-#define AF3D_COOP 1
+// k_contact_lists for one clump: its item lists (see warp_contacts) into `lists`.
+template <bool UNIFORM>
+__device__ __forceinline__ void lists_body(const Consts &c, const DevScalars *d, const int *__restrict__ flume,
+                                           const NbrRec *__restrict__ nbr, const CullRec *__restrict__ cull,
+                                           const int *__restrict__ start, const int *__restrict__ order,
+                                           const float4 *__restrict__ csort, ContactLists lists, long n,
+                                           PassLists &pl) {
+  const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const bool valid = s < n;
+  const long sv = valid ? s : n - 1;
+  const int f = flume[sv];
+  const DevFlume &fl = d->flumes[f];
+  const af3d_cell_par g = fl.grid;
+  const GridF gf = fl.gridf;
+  const long long off = fl.cell_off;
+  const NbrRec &me = nbr[sv];
+  const V3 r = mk(me.rx, me.ry, me.rz);
+  const bool act = valid && !is_removed(*c.tp, r.x, c.side_x);
+  bool slow = false;
+  const int k = build_item_lists(pl, lists.items + sv, n, blockIdx.x * (long)blockDim.x + (threadIdx.x & ~31u), sv,
+                                 act, c.phase == AF3D_PHASE_AVALANCHE, r, c, g, gf, off, cull, start, order, csort,
+                                 slow);
+  if (valid) lists.cnt[s] = slow ? -1 : k;
+}
+
+// The item lists of every clump of one force pass (the two-stage gather and the boundary gates),
+// ahead of the force kernel: a lean kernel, so that the neighbour walk runs with many warps
+// resident and most of the L1 free for the culling records.
+#ifndef AF3D_LISTS_MINB
+#define AF3D_LISTS_MINB 6
 #endif
-template <bool WRITE_FT>
-__global__ void __launch_bounds__(kBlock, AF3D_FORCES_MINB) k_fused_forces(Planes P, Planes out, DevScalars *d,
-                                                         const int *__restrict__ flume,
-                                                         const NbrRec *__restrict__ nbr,
-                                                         const CullRec *__restrict__ cull,
-                                                         const int *__restrict__ start,
-                                                         const int *__restrict__ order,
-                                                         const float4 *__restrict__ csort, long n) {
-#if AF3D_COOP
-  __shared__ WarpQueue wq[kBlock / 32];
-#endif
+template <bool UNIFORM>
+__global__ void __launch_bounds__(kBlock, AF3D_LISTS_MINB) k_contact_lists(const DevScalars *d,
+                                                          const int *__restrict__ flume,
+                                                          const NbrRec *__restrict__ nbr,
+                                                          const CullRec *__restrict__ cull,
+                                                          const int *__restrict__ start,
+                                                          const int *__restrict__ order,
+                                                          const float4 *__restrict__ csort, ContactLists lists,
+                                                          const __grid_constant__ Consts kc, long n) {
+  __shared__ PassLists pl[kBlock / 32];
+  if constexpr (UNIFORM) {
+    lists_body<true>(kc, d, flume, nbr, cull, start, order, csort, lists, n, pl[threadIdx.x >> 5]);
+  } else {
+    const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    const Consts c = load_consts(d, flume[s < n ? s : n - 1]);
+    lists_body<false>(c, d, flume, nbr, cull, start, order, csort, lists, n, pl[threadIdx.x >> 5]);
+  }
+}
+
+template <bool WRITE_FT, bool UNIFORM>
+__device__ __forceinline__ void fused_body(const Consts &c, Planes P, Planes out, DevScalars *d,
+                                           const int *__restrict__ flume, const NbrRec *__restrict__ nbr,
+                                           const CullRec *__restrict__ cull, const int *__restrict__ start,
+                                           const int *__restrict__ order, ContactLists lists, long n,
+                                           WarpQueue &wq) {
   const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
   const bool valid = s < n;
   const long sv = valid ? s : n - 1;   // in-range slot for lanes past n (nothing is written for them)
   const int f = flume[sv];
-  const Consts c = load_consts(d, f);
   const af3d_cell_par g = d->flumes[f].grid;
   const long long off = d->flumes[f].cell_off;
   const Own o = own_from_record(nbr[sv]);
-  const bool removed = is_removed(c.time, o.r.x, c.side_x);
+  const bool removed = is_removed(*c.tp, o.r.x, c.side_x);
   const double B = (double)cull[sv].c.w;   // sphere offsets + radius, rounded up
   V3 F = mk(0.0, 0.0, 0.0), T = mk(0.0, 0.0, 0.0);
   const bool aval = c.phase == AF3D_PHASE_AVALANCHE;
-#if AF3D_COOP
   // Removed clumps get hop, funnel and fcorners only (walls, part and flume skip them).
   if (valid && removed && aval)
     for (int rt = R_HOP0; rt <= R_FCORNERS; rt++)
       if (bnd_may_touch(rt, o.r, B, c)) bnd_routine(rt, o, true, c, F, T);
   const long wbase = blockIdx.x * (long)blockDim.x + (threadIdx.x & ~31u);
-  const int active = warp_contacts(wq[threadIdx.x >> 5], wbase, sv, valid && !removed, aval, B, o, c, g, off,
-                                   d, flume, nbr, cull, start, order, csort, F, T);
-#else
-  if (valid && aval) {
-    // hop x3, funnel, fcorners, walls (avalanche_hst.cu:688-696)
-    for (int rt = R_HOP0; rt <= R_WALLS; rt++)
-      if (bnd_may_touch(rt, o.r, B, c)) bnd_routine(rt, o, removed, c, F, T);
-  }
-  // part x16 (avalanche_hst.cu:699-701, fill :455-457)
-  const int active =
-      (valid && !removed) ? particle_contacts(s, o, c, g, off, nbr, cull, start, order, -1, F, T) : 0;
-  if (valid) {
-    if (aval) {
-      if (bnd_may_touch(R_FLUME, o.r, B, c)) bnd_routine(R_FLUME, o, removed, c, F, T);   // :704
-    } else {
-      for (int rt = R_HOP0; rt <= R_HOP2; rt++)   // hop x3 after the particles (:460-461)
-        if (bnd_may_touch(rt, o.r, B, c)) bnd_routine(rt, o, removed, c, F, T);
-    }
-  }
-#endif
+  const int listed = valid ? __ldg(&lists.cnt[s]) : 0;
+  const int active = warp_contacts<UNIFORM>(wq, wbase, sv, valid && !removed, aval, B, o, c, g, off, d, flume, nbr,
+                                            cull, start, order, lists.items, listed, n, F, T);
   if (valid) {
     if (WRITE_FT) {
       store3(P, FX, s, F);
       store3(P, TX, s, T);
     }
+    // this step's predicted velocities, read again from the record (not held across the contacts)
+    const NbrRec &me = nbr[s];
+    const V3 v = mk(me.vx, me.vy, me.vz), w = mk(me.wx, me.wy, me.wz);
     if (!removed) {
       V3 a, al;
-      get_accel_one(F, T, o.v, o.w, load3(P, R00, s), load3(P, R10, s), load3(P, R20, s),
-                    P.p[MASS][s], P.p[ADRAG][s], load3(P, IXX, s), a, al);
+      get_accel_one(F, T, v, w, load3(P, R00, s), load3(P, R10, s), load3(P, R20, s), P.p[MASS][s],
+                    P.p[ADRAG][s], load3(P, IXX, s), a, al);
       store3(P, AFX, s, a);
       store3(P, ALFX, s, al);
       const V3 ai = load3(P, AIX, s), ali = load3(P, ALIX, s);
       // finish_Verlet.cu:43-48
-      store3(out, VX, s, mk(o.v.x + c.hdt * (a.x - ai.x), o.v.y + c.hdt * (a.y - ai.y),
-                            o.v.z + c.hdt * (a.z - ai.z)));
-      store3(out, WX, s, mk(o.w.x + c.hdt * (al.x - ali.x), o.w.y + c.hdt * (al.y - ali.y),
-                            o.w.z + c.hdt * (al.z - ali.z)));
+      store3(out, VX, s, mk(v.x + c.hdt * (a.x - ai.x), v.y + c.hdt * (a.y - ai.y), v.z + c.hdt * (a.z - ai.z)));
+      store3(out, WX, s, mk(w.x + c.hdt * (al.x - ali.x), w.y + c.hdt * (al.y - ali.y), w.z + c.hdt * (al.z - ali.z)));
       if (!(isfinite(a.x) && isfinite(a.y) && isfinite(a.z) && isfinite(al.x) && isfinite(al.y) &&
             isfinite(al.z)))
         raise_status(d, AF3D_ERR_NAN);
     } else {
       store3(out, VX, s, mk(0.0, 0.0, 0.0));  // finish_Verlet.cu:28-32
-      store3(out, WX, s, o.w);
+      store3(out, WX, s, w);
       store3(P, AFX, s, mk(0.0, 0.0, 0.0));   // the reference leaves stale values here
       store3(P, ALFX, s, mk(0.0, 0.0, 0.0));
     }
   }
   warp_count(d, active);
+}
+
+// The whole force pass of one step for clump s, in the reference's call order, then get_accel
+// and finish_Verlet, from the item lists of k_contact_lists.  Velocities after the corrector go
+// to `out` (the other plane set), because neighbours still read this step's predicted
+// velocities from the records.  Every lane of a launched warp reaches the warp-cooperative
+// contact pass (lanes past n take no clump).  UNIFORM: one flume, whose constants are the
+// parameter kc; else each thread loads its flume's.
+template <bool WRITE_FT, bool UNIFORM>
+__global__ void __launch_bounds__(kBlock, AF3D_FORCES_MINB) k_fused_forces(Planes P, Planes out, DevScalars *d,
+                                                         const int *__restrict__ flume,
+                                                         const NbrRec *__restrict__ nbr,
+                                                         const CullRec *__restrict__ cull,
+                                                         const int *__restrict__ start,
+                                                         const int *__restrict__ order, ContactLists lists,
+                                                         const __grid_constant__ Consts kc, long n) {
+  __shared__ WarpQueue wq[kBlock / 32];
+  if constexpr (UNIFORM) {
+    fused_body<WRITE_FT, true>(kc, P, out, d, flume, nbr, cull, start, order, lists, n, wq[threadIdx.x >> 5]);
+  } else {
+    const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    const Consts c = load_consts(d, flume[s < n ? s : n - 1]);
+    fused_body<WRITE_FT, false>(c, P, out, d, flume, nbr, cull, start, order, lists, n, wq[threadIdx.x >> 5]);
+  }
 }
 
 // One boundary routine added to the F, T planes (per-routine entry points).
@@ -706,7 +762,7 @@ __global__ void k_boundary(Planes P, DevScalars *d, const int *__restrict__ flum
   if (s >= n) return;
   const Consts c = load_consts(d, flume[s]);
   const Own o = own_from_planes(P, s);
-  const bool removed = is_removed(c.time, o.r.x, c.side_x);
+  const bool removed = is_removed(*c.tp, o.r.x, c.side_x);
   V3 F = load3(P, FX, s), T = load3(P, TX, s);
   bnd_routine(routine, o, removed, c, F, T);
   store3(P, FX, s, F);
@@ -724,7 +780,7 @@ __global__ void __launch_bounds__(kBlock) k_part(Planes P, DevScalars *d, const 
   const Consts c = load_consts(d, f);
   const af3d_cell_par g = d->flumes[f].grid;
   const Own o = own_from_planes(P, s);
-  if (is_removed(c.time, o.r.x, c.side_x)) return;
+  if (is_removed(*c.tp, o.r.x, c.side_x)) return;
   V3 F = load3(P, FX, s), T = load3(P, TX, s);
   particle_contacts(s, o, c, g, d->flumes[f].cell_off, nbr, cull, start, nullptr, sph_id - 1, F, T);
   store3(P, FX, s, F);
@@ -904,6 +960,7 @@ __global__ void k_grid_commit(DevScalars *d, int nflumes, long n, long bucket_ca
   long long off = 0;
   for (int f = 0; f < nflumes; f++) {
     d->flumes[f].grid = d->flumes[f].pending;
+    d->flumes[f].gridf = grid_floats(d->flumes[f].grid);
     d->flumes[f].cell_off = off;
     off += d->flumes[f].grid.ncell3;
   }
@@ -924,7 +981,7 @@ __global__ void k_contact_pairs(Planes P, DevScalars *d, const int *__restrict__
   const Consts c = load_consts(d, f);
   const af3d_cell_par g = d->flumes[f].grid;
   const Own o = own_from_planes(P, s);
-  if (is_removed(c.time, o.r.x, c.side_x)) return;
+  if (is_removed(*c.tp, o.r.x, c.side_x)) return;
   const CullRec me = cull[s];
   const Search q = search_centre(o.r, g, d->flumes[f].cell_off);
   for_neighbour_slots(q, g, start, nullptr, [&](int t) {
@@ -996,16 +1053,36 @@ void launch_build_records(const Launch &L, Planes cur, NbrRec *nbr, CullRec *cul
                                                                 nullptr, nullptr, nbr, cull, true, L.n);
 }
 
+void launch_contact_lists(const Launch &L, DevScalars *d, const int *flume, const NbrRec *nbr, const CullRec *cull,
+                          const int *start, const int *order, const float4 *csort, ContactLists lists,
+                          const Consts *uniform) {
+  if (L.n <= 0) return;
+  const Consts kc = uniform ? *uniform : Consts{};
+  if (uniform)
+    k_contact_lists<true><<<grid_for(L.n), kBlock, 0, L.st>>>(d, flume, nbr, cull, start, order, csort, lists, kc, L.n);
+  else
+    k_contact_lists<false><<<grid_for(L.n), kBlock, 0, L.st>>>(d, flume, nbr, cull, start, order, csort, lists, kc,
+                                                              L.n);
+}
+
 void launch_fused_forces(const Launch &L, Planes cur, Planes out, DevScalars *d, const int *flume,
                          const NbrRec *nbr, const CullRec *cull, const int *start, const int *order,
-                         const float4 *csort, bool write_ft) {
+                         ContactLists lists, bool write_ft, const Consts *uniform) {
   if (L.n <= 0) return;
-  if (write_ft)
-    k_fused_forces<true><<<grid_for(L.n), kBlock, 0, L.st>>>(cur, out, d, flume, nbr, cull, start, order, csort,
-                                                             L.n);
-  else
-    k_fused_forces<false><<<grid_for(L.n), kBlock, 0, L.st>>>(cur, out, d, flume, nbr, cull, start, order, csort,
-                                                              L.n);
+  const Consts kc = uniform ? *uniform : Consts{};
+  const int g = grid_for(L.n);
+  if (uniform) {
+    if (write_ft)
+      k_fused_forces<true, true><<<g, kBlock, 0, L.st>>>(cur, out, d, flume, nbr, cull, start, order, lists, kc, L.n);
+    else
+      k_fused_forces<false, true><<<g, kBlock, 0, L.st>>>(cur, out, d, flume, nbr, cull, start, order, lists, kc, L.n);
+  } else {
+    if (write_ft)
+      k_fused_forces<true, false><<<g, kBlock, 0, L.st>>>(cur, out, d, flume, nbr, cull, start, order, lists, kc, L.n);
+    else
+      k_fused_forces<false, false><<<g, kBlock, 0, L.st>>>(cur, out, d, flume, nbr, cull, start, order, lists, kc,
+                                                            L.n);
+  }
 }
 
 void launch_boundary(const Launch &L, Planes cur, DevScalars *d, const int *flume, int routine) {

@@ -47,31 +47,10 @@ __device__ __forceinline__ V3 mk(double x, double y, double z) {
   return r;
 }
 
-// Scalars of one flume's system_par / Funnel used by the force routines, loaded once per thread.
-struct Consts {
-  double dt, hdt, time, time_prev;
-  double mu_pp, kappa_pp, gamma_pp, cns_pp;
-  double mu_pw, kappa_pw, gamma_pw, cns_pw;
-  double sint, cost, dy2, side_x, side_y;
-  double sinfi, cosfi, tanfi;
-  double tant;     // sint / cost
-  double inv_dt;   // fast mode only: 1/dt
-  int phase, variant;
-};
-
+// The constants of flume f, loaded per thread (contexts with several flumes).
 __device__ __forceinline__ Consts load_consts(const DevScalars *d, int f) {
-  Consts c;
   const DevFlume &fl = d->flumes[f];
-  const af3d_system_par &s = fl.sys;
-  c.dt = s.dt; c.hdt = s.hdt; c.time = d->time; c.time_prev = d->time_prev;
-  c.mu_pp = s.mu_pp; c.kappa_pp = s.kappa_pp; c.gamma_pp = s.gamma_pp; c.cns_pp = s.fr_fact_pp;
-  c.mu_pw = s.mu_pw; c.kappa_pw = s.kappa_pw; c.gamma_pw = s.gamma_pw; c.cns_pw = s.fr_fact_pw;
-  c.sint = s.sint; c.cost = s.cost; c.dy2 = s.dy2; c.side_x = s.side.x; c.side_y = s.side.y;
-  c.sinfi = fl.fun.sinfi; c.cosfi = fl.fun.cosfi; c.tanfi = fl.fun.tanfi;
-  c.tant = fl.tant;
-  c.phase = d->phase; c.variant = d->variant;
-  c.inv_dt = kFast ? 1.0 / s.dt : 0.0;
-  return c;
+  return make_consts(fl.sys, fl.fun, fl.tant, d->phase, d->variant, &d->time);
 }
 
 // time > 0 && x > side.x (init_Verlet.cu:29, cells.cu:65, force_part.cu:47, ...)
@@ -275,7 +254,7 @@ __device__ __forceinline__ bool hop_sphere(const Sph &o, int nw, const Consts &c
   } else {
     dist = s.z - kHOP_HEIGHT;
     if (dist <= ri) {
-      touch = c.time < 0.0 ? 5 : 0;   // the door is open once time >= 0 (force_hop.cu:140-143)
+      touch = *c.tp < 0.0 ? 5 : 0;   // the door is open once time >= 0 (force_hop.cu:140-143)
       rrc = mk(s.x, s.y, kHOP_HEIGHT); n = mk(0.0, 0.0, -1.0); comp = ri - dist;
     }
   }
@@ -423,7 +402,7 @@ __device__ __forceinline__ bool bnd_may_touch(int routine, V3 r, double B, const
       if (r.z + Bm < kHOP_HEIGHT || r.x - Bm > kHOP_WIDTH) return false;   // force_hop.cu:67
       if (routine == R_HOP0) return r.x <= Bm || r.x >= kHOP_WIDTH - Bm;
       if (routine == R_HOP1) return r.y - kYHOP_L <= Bm || kYHOP_R - r.y <= Bm;
-      return c.time < 0.0 && r.z - kHOP_HEIGHT <= Bm;
+      return *c.tp < 0.0 && r.z - kHOP_HEIGHT <= Bm;
     }
     case R_FUNNEL: {
       const double xr = r.x * c.cost - r.z * c.sint, yr = r.y;
@@ -442,6 +421,45 @@ __device__ __forceinline__ bool bnd_may_touch(int routine, V3 r, double B, const
     case R_FLUME: {
       const double zr = r.x * c.sint + r.z * c.cost;
       return fabs(zr) <= Bm;
+    }
+  }
+  return true;
+}
+
+// bnd_may_touch in FP32 on the culling record's coordinates p (each the FP32 rounding of the
+// FP64 value) and bound B (rounded up).  Each routine's expression is at most five FP32
+// operations on values below ~10^3 and constants rounded to FP32, so it lies within
+// ~10 * 2^-24 (|x| + |y| + |z| + 30) of the exact value; the slack S below is more than twice
+// that (and covers the FP64 rounding of the routine's own test), so every position the FP64
+// gate (and hence the routine) can pass also passes here.  door_closed: time < 0.
+__device__ __forceinline__ bool bnd_may_touch_f(int routine, float4 p, float B, const Consts &c, bool door_closed) {
+  const float S = 1e-5f * (101.0f + fabsf(p.x) + fabsf(p.y) + fabsf(p.z));
+  const float Bm = B + S;
+  switch (routine) {
+    case R_HOP0: case R_HOP1: case R_HOP2: {
+      if (p.z + Bm < (float)kHOP_HEIGHT || p.x - Bm > (float)kHOP_WIDTH) return false;
+      if (routine == R_HOP0) return p.x <= Bm || p.x >= (float)kHOP_WIDTH - Bm;
+      if (routine == R_HOP1) return p.y - (float)kYHOP_L <= Bm || (float)kYHOP_R - p.y <= Bm;
+      return door_closed && p.z - (float)kHOP_HEIGHT <= Bm;
+    }
+    case R_FUNNEL: {
+      const float xr = p.x * c.cost_f - p.z * c.sint_f, yr = p.y;
+      if (xr - Bm > (float)kLFUNNEL) return false;
+      return fabsf(yr - xr * c.tanfi_f) * c.cosfi_f <= Bm ||
+             fabsf((float)kYFUNNEL - yr - xr * c.tanfi_f) * c.cosfi_f <= Bm;
+    }
+    case R_FCORNERS: {
+      const float xr = p.x * c.cost_f - p.z * c.sint_f;
+      return fabsf(xr - (float)kLFUNNEL) <= 2.0f * Bm;
+    }
+    case R_WALLS: {
+      const float xr = p.x * c.cost_f - p.z * c.sint_f;
+      if (xr + Bm <= (float)kLFUNNEL) return false;
+      return p.y - c.dy2_f <= Bm || c.side_y_f + c.dy2_f - p.y <= Bm;
+    }
+    case R_FLUME: {
+      const float zr = p.x * c.sint_f + p.z * c.cost_f;
+      return fabsf(zr) <= Bm;
     }
   }
   return true;

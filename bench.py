@@ -460,12 +460,13 @@ def run_engine(args):
 
     # Roofline of the dominant kernel from CUDA events between the kernels (profiled steps after
     # the timed region, same stream).
-    prof = np.zeros(6)
+    names = ["time_advance", "predict_keys", "cell_sort", "permute_records", "contact_lists", "fused_forces",
+             "regrid"]
+    prof = np.zeros(len(names))
     lib().af3d_step_profile(eng._h, args.profile_steps, prof.ctypes.data_as(C.c_void_p))
     prof /= args.profile_steps
-    names = ["time_advance", "predict_keys", "cell_sort", "permute_records", "fused_forces", "regrid"]
     peaks, peak_kind = measured_peaks()
-    t_forces = prof[4] / 1e3
+    t_forces = prof[names.index("fused_forces")] / 1e3
     alg = BYTES_PER_CLUMP * args.n + BYTES_PER_CELL * ncell3
     achieved = alg / t_forces / 1e9 if t_forces > 0 else None
     fp64 = C.c_double()
@@ -536,7 +537,7 @@ def run_engine(args):
                          "frac": (achieved / peaks["hbm_gbs"]) if achieved else None,
                          "peak_source": peak_kind, "traffic": traffic_from_profile(),
                          "algorithmic_bytes_per_launch": alg,
-                         "kernel_ms": prof[4], "note": "FP64-issue bound; see fp64"},
+                         "kernel_ms": prof[names.index("fused_forces")], "note": "FP64-issue bound; see fp64"},
             "fp64": {"peak_tflops": fp64.value, "peak_source": "measured DFMA microbenchmark"},
             "phase_ms": {k: float(v) for k, v in zip(names, prof)},
             "ensemble": ens,
