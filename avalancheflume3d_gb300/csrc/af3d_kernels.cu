@@ -200,6 +200,8 @@ __device__ __forceinline__ long bin_axis(double x, double xmin, double inv, long
 // bucket holds its clumps in id order after the rank pass.  `t_prev`: init_Verlet's removal test
 // uses the time before the advance (the fused step advances time first).  RECORDS: also write
 // the clump's neighbour records at its own slot (steps that keep the slot order).
+constexpr double kSmallAngle2 = 9.765625e-04;   // (2^-5)^2
+
 template <bool PREDICT, bool KEYS, bool RECORDS>
 __global__ void __launch_bounds__(kBlock) k_predict(Planes P, DevScalars *d, bool t_prev, Cells cells,
                                                     const long long *__restrict__ id,
@@ -238,13 +240,30 @@ __global__ void __launch_bounds__(kBlock) k_predict(Planes P, DevScalars *d, boo
         V3 dO = mk(dt * (w.x + hdt * al.x), dt * (w.y + hdt * al.y), dt * (w.z + hdt * al.z));
         const double mag2 = dO.x * dO.x + dO.y * dO.y + dO.z * dO.z;
         double mag, imag = 0.0;
+        V3 dRx, dRy, dRz;
+        if (kFast && mag2 > 0.0 && mag2 < kSmallAngle2) {
+          // Fast mode, |dO| < 2^-5: the Rodrigues matrix c I + (sin/|dO|) [dO]x + ((1-c)/|dO|^2) dO dO^T
+          // from the Maclaurin series of sin(t)/t and (1 - cos t)/t^2 in t^2 = |dO|^2 (truncated
+          // after t^8 and t^10: the first omitted terms are below 2^-53 of the sums), no square
+          // root, sine or cosine.
+          const double t2 = mag2;
+          const double A = 1.0 - t2 * (1.0 / 6.0) * (1.0 - t2 * (1.0 / 20.0) * (1.0 - t2 * (1.0 / 42.0) *
+                                                                                  (1.0 - t2 * (1.0 / 72.0))));
+          const double Bq = 0.5 * (1.0 - t2 * (1.0 / 12.0) * (1.0 - t2 * (1.0 / 30.0) * (1.0 - t2 * (1.0 / 56.0) *
+                                                                                          (1.0 - t2 * (1.0 / 90.0)))));
+          const double cc = 1.0 - t2 * Bq;
+          const V3 sv = mk(A * dO.x, A * dO.y, A * dO.z);
+          const V3 bv = mk(Bq * dO.x, Bq * dO.y, Bq * dO.z);
+          dRx = mk(bv.x * dO.x + cc, bv.x * dO.y - sv.z, bv.x * dO.z + sv.y);
+          dRy = mk(bv.y * dO.x + sv.z, bv.y * dO.y + cc, bv.y * dO.z - sv.x);
+          dRz = mk(bv.z * dO.x - sv.y, bv.z * dO.y + sv.x, bv.z * dO.z + cc);
+        } else {
         if (kFast) {
           imag = rsqrt(mag2);
           mag = mag2 * imag;
         } else {
           mag = sqrt(mag2);
         }
-        V3 dRx, dRy, dRz;
         if (mag > 0.0) {
           // Rodrigues rotation about dO/|dO| by |dO| (init_Verlet.cu:63-83)
           V3 u;
@@ -266,6 +285,7 @@ __global__ void __launch_bounds__(kBlock) k_predict(Planes P, DevScalars *d, boo
           dRy = mk(0.0, 1.0, 0.0);
           dRz = mk(0.0, 0.0, 1.0);
         }
+        }
         // R <- dR R (rows), then each column renormalised (init_Verlet.cu:92-114)
         V3 Tx = mk(dRx.x * Rx.x + dRx.y * Ry.x + dRx.z * Rz.x, dRx.x * Rx.y + dRx.y * Ry.y + dRx.z * Rz.y,
                    dRx.x * Rx.z + dRx.y * Ry.z + dRx.z * Rz.z);
@@ -274,11 +294,14 @@ __global__ void __launch_bounds__(kBlock) k_predict(Planes P, DevScalars *d, boo
         V3 Tz = mk(dRz.x * Rx.x + dRz.y * Ry.x + dRz.z * Rz.x, dRz.x * Rx.y + dRz.y * Ry.y + dRz.z * Rz.y,
                    dRz.x * Rx.z + dRz.y * Ry.z + dRz.z * Rz.z);
         if (kFast) {
-          double in = rsqrt(Tx.x * Tx.x + Ty.x * Ty.x + Tz.x * Tz.x);
+          // 1/sqrt(n2) for a column norm n2 within 2^-26 of 1 (a rotation times a rotation):
+          // one Newton step from 1, 1.5 - n2/2, whose error 3/8 (n2 - 1)^2 is below 2^-54.
+          auto inv_norm = [](double n2) { return fabs(n2 - 1.0) < 1.4901161193847656e-08 ? 1.5 - 0.5 * n2 : rsqrt(n2); };
+          double in = inv_norm(Tx.x * Tx.x + Ty.x * Ty.x + Tz.x * Tz.x);
           Rx.x = Tx.x * in; Ry.x = Ty.x * in; Rz.x = Tz.x * in;
-          in = rsqrt(Tx.y * Tx.y + Ty.y * Ty.y + Tz.y * Tz.y);
+          in = inv_norm(Tx.y * Tx.y + Ty.y * Ty.y + Tz.y * Tz.y);
           Rx.y = Tx.y * in; Ry.y = Ty.y * in; Rz.y = Tz.y * in;
-          in = rsqrt(Tx.z * Tx.z + Ty.z * Ty.z + Tz.z * Tz.z);
+          in = inv_norm(Tx.z * Tx.z + Ty.z * Ty.z + Tz.z * Tz.z);
           Rx.z = Tx.z * in; Ry.z = Ty.z * in; Rz.z = Tz.z * in;
         } else {
           double nrm = sqrt(Tx.x * Tx.x + Ty.x * Ty.x + Tz.x * Tz.x);

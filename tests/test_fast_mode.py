@@ -145,3 +145,31 @@ def test_fast_mode_switch_and_determinism(af3d, oracle):
     with af3d.Engine(sys, fun) as eng:
         with pytest.raises(af3d.EngineError):
             eng.set_fp_mode(7)
+
+
+def test_fast_rotation_over_the_angle_range(af3d, oracle):
+    """init_Verlet's rotation in fast mode -- Maclaurin series of sin(t)/t and (1 - cos t)/t^2
+    below |dOmega| = 2^-5, rsqrt and sincos above -- against the oracle's sin/cos path, for
+    rotation angles per step from 1e-9 to 0.2 rad on either side of the switch.  Rotation
+    matrices and sphere centres within 1e-14 (absolute; entries are O(1)) per clump."""
+    n = 600
+    sys, fun, pp = _state("dense", n, 4, time=0.0)
+    rng = np.random.default_rng(6)
+    dt = float(sys["dt"])
+    theta = np.concatenate([10.0 ** rng.uniform(-9, -0.7, n - 8),
+                            2.0 ** -5 * np.array([0.999, 0.9999, 1.0, 1.0001, 1.001, 0.5, 2.0, 1e-3])])
+    axis = rng.standard_normal((n, 3))
+    axis /= np.linalg.norm(axis, axis=1, keepdims=True)
+    pp = pp.copy()
+    pp["ww"] = axis * (theta / dt)[:, None]
+    pp["vv"] = 0.0
+    zero = np.zeros((n, 3))
+    want = pp.copy()
+    oracle.init_verlet(zero, zero, sys, want)
+    with af3d.Engine(sys, fun, fp_mode=af3d.FP_FAST) as eng:
+        eng.import_particles(pp)
+        eng.init_verlet()
+        got = eng.export_particles(with_accel=False)
+    for f in ("Rmatx", "Rmaty", "Rmatz"):
+        assert float(np.max(np.abs(got[f] - want[f]))) <= 1e-14, f
+    assert float(np.max(np.abs(got["rr_s"] - want["rr_s"]))) <= 1e-14 * max(1.0, float(np.abs(want["rr_s"]).max()))
