@@ -179,6 +179,8 @@ struct PassLists {
   unsigned pass_t[kPassCap][32];         // partner slot | (cell x offset + 1) << 30, per lane
   unsigned short pass_m[kPassCap][32];   // their 16-bit sphere-pair masks
   int pbase[33];
+  unsigned cand[kLaneItems][32];         // candidate sphere pairs in item order: entry << 4 | sph_id-1
+  int cbase[33];
 };
 
 // Item lists held in shared memory (the adjoint's cooperative reverse).
@@ -283,14 +285,16 @@ __device__ __forceinline__ int gather_partners(PassLists &pl, long s, float4 mc,
 // before the particles (avalanche: hop x3, funnel, fcorners, walls), the particle contacts
 // sph_id-major, the routines after them (avalanche: flume; fill: hop x3).  Boundary items
 // (routine, sphere) for the spheres the routine's 1-Lipschitz gate cannot rule out; particle
-// items (partner slot, sph_id) from a two-stage gather: stage 1 (per lane, gather_partners)
+// items (partner slot, sph_id) from a three-stage gather: stage 1 (per lane, gather_partners)
 // keeps the partners whose bounding spheres can touch, stage 2 (whole warp) runs the sixteen
-// sphere tests of every kept partner, 32 a round.  Items go to the lane's column `col`, entries
+// FP32 sphere tests of every kept partner, 32 a round, and stage 3 (whole warp) the exact FP64
+// overlap test of every sphere pair the FP32 test could not rule out.  Items go to the lane's column `col`, entries
 // `stride` apart.  All 32 lanes call this; returns the lane's item count, 0 with `slow` set
 // when the lane's lists would overflow.
 __device__ __forceinline__ int build_item_lists(PassLists &pl, unsigned *col, long stride, long wbase, long s,
                                                 bool act, bool aval, V3 r, const Consts &c,
                                                 const af3d_cell_par &g, const GridF &gf, long long off,
+                                                const NbrRec *__restrict__ nbr,
                                                 const CullRec *__restrict__ cull, const int *__restrict__ start,
                                                 const int *__restrict__ order, const float4 *__restrict__ csort,
                                                 bool &slow) {
@@ -320,10 +324,11 @@ __device__ __forceinline__ int build_item_lists(PassLists &pl, unsigned *col, lo
     }
   }
   __syncwarp();
-  // Each lane's particle items, sph_id-major (the order of the sixteen force_part launches), and
-  // within one sph_id in the reference's cell order: x offset, then row, then slot.  Partners
-  // without a candidate sphere pair are dropped first (keeping the walk order), and only the
-  // sph_ids some partner has are visited.
+  // Each lane's candidate sphere pairs in item order: sph_id-major (the order of the sixteen
+  // force_part launches), and within one sph_id in the reference's cell order (x offset, then
+  // row, then slot).  Partners without a candidate sphere pair are dropped first (keeping the
+  // walk order), and only the sph_ids some partner has are visited.
+  int ncand = 0;
   if (act && !slow) {
     int m = 0;
     unsigned any = 0u;
@@ -344,16 +349,43 @@ __device__ __forceinline__ int build_item_lists(PassLists &pl, unsigned *col, lo
       for (unsigned tag = 1; tag <= 3 && !slow; tag++)
 #pragma unroll 1
         for (int k = 0; k < m; k++) {
-          const unsigned e = pl.pass_t[k][lane];
-          if ((e >> 30) != tag || !((pl.pass_m[k][lane] >> p) & 1u)) continue;
-          if (nitems == kLaneItems) {
+          if ((pl.pass_t[k][lane] >> 30) != tag || !((pl.pass_m[k][lane] >> p) & 1u)) continue;
+          if (nitems + ncand == kLaneItems) {
             slow = true;
             break;
           }
-          col[stride * nitems++] = ((e & kSlotMask) << 4) | (unsigned)p;   // (partner slot, sph_id-1)
+          pl.cand[ncand++][lane] = ((unsigned)k << 4) | (unsigned)p;
         }
     }
-    if (!slow) slow = !push_boundary(post0, post1, me, c, door_closed, col, stride, nitems);
+    if (slow) ncand = 0;
+  }
+  // Stage 3 (whole warp): the exact FP64 overlap test of every candidate (the test the force
+  // pass would make first), 32 a round, so that the force pass gets only overlapping pairs.
+  const int total_cand = warp_prefix(ncand, pl.cbase);
+  for (int j0 = 0; j0 < total_cand; j0 += 32) {
+    const int j = j0 + lane;
+    if (j < total_cand) {
+      const int ow = owner_of(pl.cbase, j), ci = j - pl.cbase[ow];
+      const unsigned e = pl.cand[ci][ow];
+      const int k = (int)(e >> 4), p = (int)(e & 15u);
+      const NbrRec &mo = nbr[wbase + ow];
+      const V3 s1 = mk(mo.s[3 * (p & 3)], mo.s[3 * (p & 3) + 1], mo.s[3 * (p & 3) + 2]);
+      V3 d;
+      double dist2, sep;
+      if (!spheres_overlap(s1, mo.rad, nbr[pl.pass_t[k][ow] & kSlotMask], p >> 2, d, dist2, sep))
+        pl.cand[ci][ow] = e | 0x80000000u;
+    }
+  }
+  __syncwarp();
+  if (act && !slow) {
+#pragma unroll 1
+    for (int i = 0; i < ncand; i++) {
+      const unsigned e = pl.cand[i][lane];
+      if (e & 0x80000000u) continue;
+      const unsigned t = pl.pass_t[e >> 4][lane] & kSlotMask;
+      col[stride * nitems++] = (t << 4) | (e & 15u);   // (partner slot, sph_id-1)
+    }
+    slow = !push_boundary(post0, post1, me, c, door_closed, col, stride, nitems);
   }
   return slow ? 0 : nitems;
 }

@@ -669,8 +669,8 @@ __device__ __forceinline__ void lists_body(const Consts &c, const DevScalars *d,
   const bool act = valid && !is_removed(*c.tp, r.x, c.side_x);
   bool slow = false;
   const int k = build_item_lists(pl, lists.items + sv, n, blockIdx.x * (long)blockDim.x + (threadIdx.x & ~31u), sv,
-                                 act, c.phase == AF3D_PHASE_AVALANCHE, r, c, g, gf, off, cull, start, order, csort,
-                                 slow);
+                                 act, c.phase == AF3D_PHASE_AVALANCHE, r, c, g, gf, off, nbr, cull, start, order,
+                                 csort, slow);
   if (valid) lists.cnt[s] = slow ? -1 : k;
 }
 

@@ -468,22 +468,31 @@ __device__ __forceinline__ bool bnd_may_touch_f(int routine, float4 p, float B, 
 // One sphere-sphere contact of force_part.cu:139-241: own sphere s1 (clump centre rrl), partner
 // record m, partner sphere sm.  Returns false when the staged test finds no overlap; otherwise
 // the contact is prepared for the law.
-__device__ __forceinline__ bool pair_input(const V3 &rrl, const V3 &vvl, const V3 &wwl, const V3 &s1,
-                                           double rad_1, double massl, const NbrRec &m, int sm,
-                                           const Consts &c, bool xi0, ContactIn &ci) {
+// The staged overlap test of force_part.cu:143-157 between own sphere s1 (radius rad_1) and
+// sphere sm of partner m: d = s2 - s1, dist2 = |d|^2 and sep = rad_1 + rad_2 on success.  The
+// list kernel and pair_input run this same function, so they take the same decision.
+__device__ __forceinline__ bool spheres_overlap(const V3 &s1, double rad_1, const NbrRec &m, int sm, V3 &d,
+                                                double &dist2, double &sep) {
   const double rad_2 = m.rad;
-  const double sep = rad_1 + rad_2;
+  sep = rad_1 + rad_2;
   const double sep2 = sep * sep;
-  V3 d;
   d.x = m.s[3 * sm] - s1.x;
-  double dist2 = d.x * d.x;
+  dist2 = d.x * d.x;
   if (!(dist2 < sep2)) return false;
   d.y = m.s[3 * sm + 1] - s1.y;
   dist2 += d.y * d.y;
   if (!(dist2 < sep2)) return false;
   d.z = m.s[3 * sm + 2] - s1.z;
   dist2 += d.z * d.z;
-  if (!(dist2 < sep2)) return false;
+  return dist2 < sep2;
+}
+
+__device__ __forceinline__ bool pair_input(const V3 &rrl, const V3 &vvl, const V3 &wwl, const V3 &s1,
+                                           double rad_1, double massl, const NbrRec &m, int sm,
+                                           const Consts &c, bool xi0, ContactIn &ci) {
+  V3 d;
+  double dist2, sep;
+  if (!spheres_overlap(s1, rad_1, m, sm, d, dist2, sep)) return false;
   const double meff = 0.5 * (m.msph + massl);
   ci.km = 0.5 * c.kappa_pp * meff;
   ci.gm = 0.5 * c.gamma_pp * meff;
