@@ -42,7 +42,7 @@ struct __align__(64) NbrRec {
 };
 
 // FP32 culling record.  c = (centre, bound), sk = (sphere centre, inflated radius).  The bounds
-// are rounded up and inflated by 2^-21 times the largest coordinate magnitude, which covers the
+// are rounded up and inflated by 2^-22 times the largest coordinate magnitude, which covers the
 // FP32 rounding of every coordinate; the tests multiply by (1 + 2^-18) on top, so a pair the
 // FP64 test could accept is never culled.
 struct __align__(16) CullRec {

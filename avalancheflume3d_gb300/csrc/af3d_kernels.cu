@@ -124,10 +124,13 @@ __device__ __forceinline__ float f_up(double x) { return __double2float_ru(x); }
 
 // Packed FP64 neighbour record and conservative FP32 culling record of one clump.
 // The culling bounds are formed in FP32 from the FP32-rounded coordinates.  M32 = max |coordinate|
-// in FP32 is within 2^-24 of the FP64 maximum M, so mu = 2^-21 * M32 * (1 + 2^-20) still bounds
-// 4x the rounding of any FP32 coordinate (and of a coordinate difference); the sphere extent
-// ext32 = max_k |s_k - r| from the FP32 coordinates is within 2 mu + a few 2^-24 ext of the
-// exact one, which the factor (1 + 2^-20) and the added 2 mu cover.
+// in FP32 is within 2^-24 of the FP64 maximum M, so mu = 2^-22 * M32 * (1 + 2^-20) is at least
+// 4 x 2^-24 M: the FP32 difference of a coordinate of this clump and one of a partner is within
+// 2^-24 (M + M') (the two roundings) + 2^-24 |difference| of the exact one, so a distance formed
+// from FP32 coordinates errs by at most sqrt(3) 2^-24 (M + M') + 2^-24 d < mu + mu' + 2^-24 d,
+// and the last term is covered by the tests' relative slack (1 + 2^-18) on squared bounds.  The
+// sphere extent ext32 = max_k |s_k - r| from the FP32 coordinates is within 2 sqrt(3) 2^-24 M + a
+// few 2^-24 ext of the exact one, which the added 2 mu and the factor (1 + 2^-20) cover.
 __device__ __forceinline__ void make_records(V3 r, V3 v, V3 w, const V3 *sp, double rad, double msph,
                                              double mwall, NbrRec &q, CullRec &c) {
   q.rx = r.x; q.ry = r.y; q.rz = r.z;
@@ -148,8 +151,8 @@ __device__ __forceinline__ void make_records(V3 r, V3 v, V3 w, const V3 *sp, dou
     ext = fmaxf(ext, sqrtf(__fmaf_rn(dz, dz, __fmaf_rn(dy, dy, dx * dx))));
   }
   const float radf = f_up(rad);
-  // 2^-21 * max|coordinate| bounds 4x the FP32 rounding of a coordinate difference.
-  const float mu = fmaxf(M, radf) * 4.76837158203125e-07f * (1.0f + 9.5367431640625e-07f) + 1e-30f;
+  // 2^-22 * max|coordinate|: see above.
+  const float mu = fmaxf(M, radf) * 2.384185791015625e-07f * (1.0f + 9.5367431640625e-07f) + 1e-30f;
   const float sph = radf * (1.0f + 9.5367431640625e-07f) + mu;
   c.c = make_float4(cx, cy, cz, (ext * (1.0f + 9.5367431640625e-07f) + 2.0f * mu) + sph);
   for (int k = 0; k < 4; k++) c.s[k] = make_float4(sf[k].x, sf[k].y, sf[k].z, sph);

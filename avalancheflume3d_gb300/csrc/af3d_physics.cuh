@@ -469,20 +469,20 @@ __device__ __forceinline__ bool bnd_may_touch_f(int routine, float4 p, float B, 
 // record m, partner sphere sm.  Returns false when the staged test finds no overlap; otherwise
 // the contact is prepared for the law.
 // The staged overlap test of force_part.cu:143-157 between own sphere s1 (radius rad_1) and
-// sphere sm of partner m: d = s2 - s1, dist2 = |d|^2 and sep = rad_1 + rad_2 on success.  The
-// list kernel and pair_input run this same function, so they take the same decision.
+// sphere sm of partner m: d = s2 - s1, dist2 = |d|^2 and sep = rad_1 + rad_2.  The reference
+// compares each partial sum of dist2 with sep^2; the partial sums never decrease (each adds a
+// square and rounding is monotone, fused or not), so the last comparison alone takes the same
+// decision, NaN included.  The list kernel and pair_input run this same function.
 __device__ __forceinline__ bool spheres_overlap(const V3 &s1, double rad_1, const NbrRec &m, int sm, V3 &d,
                                                 double &dist2, double &sep) {
   const double rad_2 = m.rad;
   sep = rad_1 + rad_2;
   const double sep2 = sep * sep;
   d.x = m.s[3 * sm] - s1.x;
-  dist2 = d.x * d.x;
-  if (!(dist2 < sep2)) return false;
   d.y = m.s[3 * sm + 1] - s1.y;
-  dist2 += d.y * d.y;
-  if (!(dist2 < sep2)) return false;
   d.z = m.s[3 * sm + 2] - s1.z;
+  dist2 = d.x * d.x;
+  dist2 += d.y * d.y;
   dist2 += d.z * d.z;
   return dist2 < sep2;
 }
