@@ -508,109 +508,144 @@ __device__ __forceinline__ int particle_contacts(long s, const Own &o, const Con
   return active;
 }
 
-// Warp-cooperative pass of the fused kernel over every contact of a clump: the boundary routines
+// Block-cooperative pass of the fused kernel over every contact of a clump: the boundary routines
 // that run before the particle contacts, the sixteen sph_id passes, and the routines that run
 // after them (avalanche: hop x3, funnel, fcorners, walls | part x16 | flume; fill: part x16 |
 // hop x3).  The list kernel (k_contact_lists) has published every clump's item list in that
 // order: boundary items (routine, sphere) for the spheres the routine's 1-Lipschitz gate cannot
-// rule out, and particle items (partner slot, sph_id) in sph_id-major order.  The warp works
-// through the concatenated lists of its 32 clumps 32 items per round, one item per lane, reading
-// the owner clump from its record; after each round every owner adds its items' force and
-// torque terms to its own sums in list order.  The FP64 contact laws thus run with all lanes
-// busy whatever the spread of contacts and walls over the clumps, and each clump's summation
-// order stays the reference's.  All 32 lanes of the warp must call this; `act` is false for
-// lanes without a clump to process (and for removed clumps); `wbase` is the slot of the warp's
-// lane 0.  A clump whose lists overflowed runs alone afterwards, in the same order.
-struct WarpQueue {
-  int base[33];        // exclusive prefix of the lanes' item counts
-  double res[6][32];   // [component][lane]
-  int flag[32];
+// rule out, and particle items (partner slot, sph_id) of overlapping sphere pairs in sph_id-major
+// order.  The block concatenates the lists of its clumps and works through them in batches of
+// kBatch items, 32 items a round per warp, one item per lane, reading the owner clump from its
+// record; after each batch every owner adds its items' force and torque terms to its own sums in
+// list order.  The FP64 contact laws thus run with nearly all lanes busy whatever the spread of
+// contacts and walls over the clumps, and each clump's summation order stays the reference's.
+// Every thread of the block must call this; `act` is false for threads without a clump to
+// process (and for removed clumps).  A clump whose lists overflowed runs alone afterwards, in
+// the same order.
+constexpr int kBatch = 256;
+struct BlockQueue {
+  int base[kBlock + 1];   // exclusive prefix of the clumps' item counts
+  int wsum[kBlock / 32];
+  double res[6][kBatch];  // [component][item in the batch]
+  unsigned char flag[kBatch];
 };
+
+// The thread whose range [base[t], base[t+1]) holds position j.
+__device__ __forceinline__ int block_owner_of(const int *base, int j) {
+  int lo = 0, hi = kBlock - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (base[mid] <= j) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
 
 // UNIFORM: every clump of the launch belongs to one flume, whose constants `c` are (a
 // reference to) a kernel parameter.
 template <bool UNIFORM>
-__device__ __forceinline__ int warp_contacts(WarpQueue &wq, long wbase, long s, bool act, bool aval,
-                                             double B, const Own &o, const Consts &c,
-                                             const af3d_cell_par &g, long long off,
-                                             const DevScalars *d, const int *__restrict__ flume,
-                                             const NbrRec *__restrict__ nbr,
-                                             const CullRec *__restrict__ cull,
-                                             const int *__restrict__ start,
-                                             const int *__restrict__ order,
-                                             const unsigned *__restrict__ items, int listed, long n,
-                                             V3 &F, V3 &T) {
-  const int lane = threadIdx.x & 31;
+__device__ __forceinline__ int block_contacts(BlockQueue &bq, long bbase, long s, bool act, bool aval,
+                                              double B, const Own &o, const Consts &c,
+                                              const af3d_cell_par &g, long long off,
+                                              const DevScalars *d, const int *__restrict__ flume,
+                                              const NbrRec *__restrict__ nbr,
+                                              const CullRec *__restrict__ cull,
+                                              const int *__restrict__ start,
+                                              const int *__restrict__ order,
+                                              const unsigned *__restrict__ items, int listed, long n,
+                                              V3 &F, V3 &T) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int pre0 = aval ? R_HOP0 : 1, pre1 = aval ? R_WALLS : 0;         // fill: none before
   const int post0 = aval ? R_FLUME : R_HOP0, post1 = aval ? R_FLUME : R_HOP2;
   const bool slow = act && listed < 0;
   const int nitems = act && listed > 0 ? listed : 0;
-  const int total = warp_prefix(nitems, wq.base);
-  const int base = wq.base[lane];
+  // block-wide exclusive prefix of the item counts
+  int incl = nitems;
+#pragma unroll
+  for (int k = 1; k < 32; k <<= 1) {
+    const int u = __shfl_up_sync(0xffffffffu, incl, k);
+    if (lane >= k) incl += u;
+  }
+  if (lane == 31) bq.wsum[warp] = incl;
+  __syncthreads();
+  int wofs = 0, total = 0;
+#pragma unroll
+  for (int w = 0; w < kBlock / 32; w++) {
+    const int t = bq.wsum[w];
+    wofs += w < warp ? t : 0;
+    total += t;
+  }
+  const int base = wofs + incl - nitems;
+  bq.base[tid] = base;
+  if (tid == kBlock - 1) bq.base[kBlock] = total;
+  __syncthreads();
   int active = 0;
-  for (int j0 = 0; j0 < total; j0 += 32) {
-    const int j = j0 + lane;
-    if (j < total) {
-      const int lo = owner_of(wq.base, j);   // the lane whose list holds item j
-      const unsigned it = __ldg(&items[(long)(j - wq.base[lo]) * n + wbase + lo]);
-      const NbrRec &me = nbr[wbase + lo];   // owner lanes hold clumps, so wbase + lo < n
-      // Prepare the item's contact (type-specific, short), then run the contact law once for
-      // every lane that has a contact, whatever its type.
-      auto contact = [&](const Consts &co, V3 &fs, V3 &tq) -> int {
-        ContactIn ci;
-        V3 rl = mk(me.rx, me.ry, me.rz);
-        int kind;   // 0 nothing, 1 sphere pair, 2 wall
-        if (it >= kBndItem) {
-          const int rt = (int)((it >> 2) & 7u), ns = (int)(it & 3u);
-          Sph q;
-          q.r = rl;
-          q.v = mk(me.vx, me.vy, me.vz);
-          q.w = mk(me.wx, me.wy, me.wz);
-          q.s = mk(me.s[3 * ns], me.s[3 * ns + 1], me.s[3 * ns + 2]);
-          q.rad = me.rad;
-          q.mwall = me.mwall;
-          kind = bnd_input(rt, q, co, ci) ? 2 : 0;
+  for (int b0 = 0; b0 < total; b0 += kBatch) {
+    const int bn = total - b0 < kBatch ? total - b0 : kBatch;
+    for (int r0 = warp * 32; r0 < bn; r0 += kBlock) {
+      const int jb = r0 + lane;
+      if (jb < bn) {
+        const int j = b0 + jb;
+        const int lo = block_owner_of(bq.base, j);   // the thread whose list holds item j
+        const unsigned it = __ldg(&items[(long)(j - bq.base[lo]) * n + bbase + lo]);
+        const NbrRec &me = nbr[bbase + lo];   // owners hold clumps, so bbase + lo < n
+        // Prepare the item's contact (type-specific, short), then run the contact law once for
+        // every lane that has a contact, whatever its type.
+        auto contact = [&](const Consts &co, V3 &fs, V3 &tq) -> int {
+          ContactIn ci;
+          V3 rl = mk(me.rx, me.ry, me.rz);
+          int kind;   // 0 nothing, 1 sphere pair, 2 wall
+          if (it >= kBndItem) {
+            const int rt = (int)((it >> 2) & 7u), ns = (int)(it & 3u);
+            Sph q;
+            q.r = rl;
+            q.v = mk(me.vx, me.vy, me.vz);
+            q.w = mk(me.wx, me.wy, me.wz);
+            q.s = mk(me.s[3 * ns], me.s[3 * ns + 1], me.s[3 * ns + 2]);
+            q.rad = me.rad;
+            q.mwall = me.mwall;
+            kind = bnd_input(rt, q, co, ci) ? 2 : 0;
+          } else {
+            const int t = (int)(it >> 4), p = (int)(it & 15u);
+            const V3 vl = mk(me.vx, me.vy, me.vz), wl = mk(me.wx, me.wy, me.wz);
+            const int k = p & 3;
+            const V3 s1 = mk(me.s[3 * k], me.s[3 * k + 1], me.s[3 * k + 2]);
+            kind = pair_input(rl, vl, wl, s1, me.rad, me.msph, nbr[t], p >> 2, co,
+                              co.variant == AF3D_FRICTION_DEV, ci) ? 1 : 0;
+          }
+          int r = kind == 1 ? 1 : 0;
+          if (kind && apply_law(ci, rl, co, fs, tq)) r = kind == 1 ? 2 : 3;
+          return r;
+        };
+        V3 fs, tq;
+        int r;
+        if constexpr (UNIFORM) {
+          r = contact(c, fs, tq);
         } else {
-          const int t = (int)(it >> 4), p = (int)(it & 15u);
-          const V3 vl = mk(me.vx, me.vy, me.vz), wl = mk(me.wx, me.wy, me.wz);
-          const int k = p & 3;
-          const V3 s1 = mk(me.s[3 * k], me.s[3 * k + 1], me.s[3 * k + 2]);
-          kind = pair_input(rl, vl, wl, s1, me.rad, me.msph, nbr[t], p >> 2, co,
-                            co.variant == AF3D_FRICTION_DEV, ci) ? 1 : 0;
+          // the owner's flume may differ from this thread's at a flume boundary of an ensemble
+          const int of = flume[bbase + lo];
+          const Consts co = of == flume[s] ? c : load_consts(d, of);
+          r = contact(co, fs, tq);
         }
-        int r = kind == 1 ? 1 : 0;
-        if (kind && apply_law(ci, rl, co, fs, tq)) r = kind == 1 ? 2 : 3;
-        return r;
-      };
-      V3 fs, tq;
-      int r;
-      if constexpr (UNIFORM) {
-        r = contact(c, fs, tq);
-      } else {
-        // the owner's flume may differ from this lane's at a flume boundary of an ensemble
-        const int of = flume[wbase + lo];
-        const Consts co = of == flume[s] ? c : load_consts(d, of);
-        r = contact(co, fs, tq);
-      }
-      wq.flag[lane] = r;
-      if (r >= 2) {
-        wq.res[0][lane] = fs.x; wq.res[1][lane] = fs.y; wq.res[2][lane] = fs.z;
-        wq.res[3][lane] = tq.x; wq.res[4][lane] = tq.y; wq.res[5][lane] = tq.z;
+        bq.flag[jb] = (unsigned char)r;
+        if (r >= 2) {
+          bq.res[0][jb] = fs.x; bq.res[1][jb] = fs.y; bq.res[2][jb] = fs.z;
+          bq.res[3][jb] = tq.x; bq.res[4][jb] = tq.y; bq.res[5][jb] = tq.z;
+        }
       }
     }
-    __syncwarp();
+    __syncthreads();
     if (nitems > 0) {
-      const int a = base > j0 ? base : j0;
-      const int b = base + nitems < j0 + 32 ? base + nitems : j0 + 32;
-      for (int e = a - j0; e < b - j0; e++) {
-        const int fl = wq.flag[e];
+      const int a = base > b0 ? base : b0;
+      const int b = base + nitems < b0 + bn ? base + nitems : b0 + bn;
+      for (int e = a - b0; e < b - b0; e++) {
+        const int fl = bq.flag[e];
         if (fl < 2) continue;
-        T.x += wq.res[3][e]; T.y += wq.res[4][e]; T.z += wq.res[5][e];
-        F.x += wq.res[0][e]; F.y += wq.res[1][e]; F.z += wq.res[2][e];
+        T.x += bq.res[3][e]; T.y += bq.res[4][e]; T.z += bq.res[5][e];
+        F.x += bq.res[0][e]; F.y += bq.res[1][e]; F.z += bq.res[2][e];
         active += fl == 2;   // sphere-sphere contacts only
       }
     }
-    __syncwarp();
+    __syncthreads();
   }
   if (slow) {
     for (int rt = pre0; rt <= pre1; rt++)
@@ -707,7 +742,7 @@ __device__ __forceinline__ void fused_body(const Consts &c, Planes P, Planes out
                                            const int *__restrict__ flume, const NbrRec *__restrict__ nbr,
                                            const CullRec *__restrict__ cull, const int *__restrict__ start,
                                            const int *__restrict__ order, ContactLists lists, long n,
-                                           WarpQueue &wq) {
+                                           BlockQueue &bq) {
   const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
   const bool valid = s < n;
   const long sv = valid ? s : n - 1;   // in-range slot for lanes past n (nothing is written for them)
@@ -723,10 +758,10 @@ __device__ __forceinline__ void fused_body(const Consts &c, Planes P, Planes out
   if (valid && removed && aval)
     for (int rt = R_HOP0; rt <= R_FCORNERS; rt++)
       if (bnd_may_touch(rt, o.r, B, c)) bnd_routine(rt, o, true, c, F, T);
-  const long wbase = blockIdx.x * (long)blockDim.x + (threadIdx.x & ~31u);
+  const long bbase = blockIdx.x * (long)blockDim.x;
   const int listed = valid ? __ldg(&lists.cnt[s]) : 0;
-  const int active = warp_contacts<UNIFORM>(wq, wbase, sv, valid && !removed, aval, B, o, c, g, off, d, flume, nbr,
-                                            cull, start, order, lists.items, listed, n, F, T);
+  const int active = block_contacts<UNIFORM>(bq, bbase, sv, valid && !removed, aval, B, o, c, g, off, d, flume, nbr,
+                                             cull, start, order, lists.items, listed, n, F, T);
   if (valid) {
     if (WRITE_FT) {
       store3(P, FX, s, F);
@@ -772,13 +807,13 @@ __global__ void __launch_bounds__(kBlock, AF3D_FORCES_MINB) k_fused_forces(Plane
                                                          const int *__restrict__ start,
                                                          const int *__restrict__ order, ContactLists lists,
                                                          const __grid_constant__ Consts kc, long n) {
-  __shared__ WarpQueue wq[kBlock / 32];
+  __shared__ BlockQueue bq;
   if constexpr (UNIFORM) {
-    fused_body<WRITE_FT, true>(kc, P, out, d, flume, nbr, cull, start, order, lists, n, wq[threadIdx.x >> 5]);
+    fused_body<WRITE_FT, true>(kc, P, out, d, flume, nbr, cull, start, order, lists, n, bq);
   } else {
     const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
     const Consts c = load_consts(d, flume[s < n ? s : n - 1]);
-    fused_body<WRITE_FT, false>(c, P, out, d, flume, nbr, cull, start, order, lists, n, wq[threadIdx.x >> 5]);
+    fused_body<WRITE_FT, false>(c, P, out, d, flume, nbr, cull, start, order, lists, n, bq);
   }
 }
 
