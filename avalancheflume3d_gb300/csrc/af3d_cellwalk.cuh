@@ -171,12 +171,12 @@ constexpr int kLaneItems = kListCap;
 constexpr unsigned kBndItem = 0xFFFFFF00u;   // boundary item: kBndItem | routine << 2 | sphere
 
 constexpr int kPassCap = 32;   // partners per clump that pass the centre test
-constexpr unsigned kSlotMask = 0x3FFFFFFFu;   // pass entry: slot | (x offset + 1) << 30
+constexpr unsigned kSlotMask = 0x3FFFFFFFu;   // pass entry: position or slot | (x offset + 1) << 30
 
 // Per-warp partner lists of the two-stage gather in shared memory, one column per lane
 // ([entry][lane]): a lane's own accesses always fall in its own bank.
 struct PassLists {
-  unsigned pass_t[kPassCap][32];         // partner slot | (cell x offset + 1) << 30, per lane
+  unsigned pass_t[kPassCap][32];         // partner position, then slot | (cell x offset + 1) << 30
   unsigned short pass_m[kPassCap][32];   // their 16-bit sphere-pair masks
   int pbase[33];
   unsigned cand[kLaneItems][32];         // candidate sphere pairs in item order: entry << 4 | sph_id-1
@@ -234,7 +234,7 @@ __device__ __forceinline__ bool push_boundary(int r0, int r1, const CullRec &me,
 }
 
 // Stage 1 of the gather (per lane): the partners among the 27 neighbour cells whose bounding
-// spheres can touch the clump's (FP32 centre test).  The three cells of one (jdel, kdel) row are
+// spheres can touch the clump's (FP32 centre test), the clump itself included.  The three cells of one (jdel, kdel) row are
 // consecutive in the linear cell index, so their members form one slot range split by four
 // start[] values; the nine ranges are walked one after another, two slots a turn with both
 // loads issued together.  Each kept partner is tagged with its cell's x offset (0..2) so that
@@ -246,12 +246,12 @@ __device__ __forceinline__ int gather_partners(PassLists &pl, long s, float4 mc,
                                                const CullRec *__restrict__ cull) {
   const int lane = threadIdx.x & 31;
   int npass = 0;
+  // Kept partners are recorded by their position k in the (cell, id) order; stage 2 looks up
+  // their slots (and drops the clump itself) with all lanes busy.
   auto keep = [&](int k, unsigned tag, float4 pc) {
     const float lim = mc.w + pc.w;
     if (d2f(mc, pc) > lim * lim * kCullSlack) return;
-    const int t = order ? __ldg(&order[k]) : k;
-    if (t == s) return;
-    if (npass < kPassCap) pl.pass_t[npass][lane] = (unsigned)t | (tag << 30);
+    if (npass < kPassCap) pl.pass_t[npass][lane] = (unsigned)k | (tag << 30);
     npass++;
   };
   const long x0 = q.ci - 1;
@@ -314,13 +314,18 @@ __device__ __forceinline__ int build_item_lists(PassLists &pl, unsigned *col, lo
       npass = 0;
     }
   }
-  // Stage 2 (whole warp): the sixteen sphere tests of every kept partner, 32 partners a round.
+  // Stage 2 (whole warp): each kept partner's slot, then its sixteen sphere tests, 32 partners a
+  // round (the clump itself gets an empty mask).
   const int total_pass = warp_prefix(npass, pl.pbase);
   for (int j0 = 0; j0 < total_pass; j0 += 32) {
     const int j = j0 + lane;
     if (j < total_pass) {
       const int ow = owner_of(pl.pbase, j), k = j - pl.pbase[ow];
-      pl.pass_m[k][ow] = (unsigned short)sphere_mask(cull[wbase + ow], cull[pl.pass_t[k][ow] & kSlotMask]);
+      const unsigned e = pl.pass_t[k][ow];
+      const int pos = (int)(e & kSlotMask);
+      const int t = order ? __ldg(&order[pos]) : pos;
+      pl.pass_t[k][ow] = (unsigned)t | (e & ~kSlotMask);
+      pl.pass_m[k][ow] = t == wbase + ow ? (unsigned short)0 : (unsigned short)sphere_mask(cull[wbase + ow], cull[t]);
     }
   }
   __syncwarp();
