@@ -38,7 +38,7 @@ af3d_status fail(af3d_status code, const std::string &msg) {
 
 constexpr long kRegridEvery = 2000;   // avalanche_hst.cu:470 and :713 (cc % 2000 == 0)
 constexpr long kKernelsPerCellBuild = 7;   // predict/keys, 3 scan, scatter, rank, permute
-constexpr long kKernelsPerForcePass = 2;   // contact lists, fused forces
+constexpr long kKernelsPerForcePass = 1;   // lists and forces in one kernel
 constexpr long kKernelsPerStep = kKernelsPerCellBuild + 1 + kKernelsPerForcePass;   // + time advance
 constexpr long kKernelsPerKeptStep = kKernelsPerStep - 1;    // a step without the permutation
 constexpr long kKernelsPerRegrid = 4;
@@ -263,7 +263,7 @@ void predict_for(af3d_ctx *c, bool predict, bool keys, bool t_prev, bool records
 // A single-flume context passes its constants as a kernel parameter (from the host mirrors,
 // which push_params keeps equal to the device table; captured graphs are dropped whenever they
 // change).
-void forces_for(af3d_ctx *c, bool write_ft, const int *order, Planes out, cudaEvent_t between = nullptr) {
+void forces_for(af3d_ctx *c, bool write_ft, const int *order, Planes out) {
   const float4 *csort = order ? c->cells.csort : nullptr;
   Consts kc;
   const Consts *uni = nullptr;
@@ -271,17 +271,12 @@ void forces_for(af3d_ctx *c, bool write_ft, const int *order, Planes out, cudaEv
     kc = make_consts(c->sys[0], c->fun[0], c->sys[0].sint / c->sys[0].cost, c->phase, c->variant, &c->d->time);
     uni = &kc;
   }
-  if (c->fp_mode == AF3D_FP_FAST) {
-    fast::launch_contact_lists(c->L(), c->d, c->fl_cur, c->nbr, c->cull, c->cells.start, order, csort, c->lists, uni);
-    if (between) cudaEventRecord(between, c->st);
-    fast::launch_fused_forces(c->L(), c->cur, out, c->d, c->fl_cur, c->nbr, c->cull, c->cells.start, order,
+  if (c->fp_mode == AF3D_FP_FAST)
+    fast::launch_lists_forces(c->L(), c->cur, out, c->d, c->fl_cur, c->nbr, c->cull, c->cells.start, order, csort,
                               c->lists, write_ft, uni);
-  } else {
-    launch_contact_lists(c->L(), c->d, c->fl_cur, c->nbr, c->cull, c->cells.start, order, csort, c->lists, uni);
-    if (between) cudaEventRecord(between, c->st);
-    launch_fused_forces(c->L(), c->cur, out, c->d, c->fl_cur, c->nbr, c->cull, c->cells.start, order, c->lists,
-                        write_ft, uni);
-  }
+  else
+    launch_lists_forces(c->L(), c->cur, out, c->d, c->fl_cur, c->nbr, c->cull, c->cells.start, order, csort,
+                        c->lists, write_ft, uni);
 }
 
 void enqueue_cell_build(af3d_ctx *c, bool predict, bool t_prev, bool ft = true) {
@@ -880,14 +875,14 @@ af3d_status af3d_step_profile(af3d_ctx *c, long k, double *ms) {
     }
     AF3D_CUDA(cudaEventRecord(ev[4], c->st));
     if (resort) {
-      forces_for(c, false, nullptr, c->alt, ev[5]);
+      forces_for(c, false, nullptr, c->alt);
       swap_velocity_planes(c->cur, c->alt);
     } else {
-      forces_for(c, false, c->cells.perm, c->cur, ev[5]);
+      forces_for(c, false, c->cells.perm, c->cur);
     }
     swap_accel_planes(c->cur);
     swap_accel_planes(c->alt);
-    AF3D_CUDA(cudaEventRecord(ev[6], c->st));
+    AF3D_CUDA(cudaEventRecord(ev[5], c->st));
     c->sorted = resort;
     c->since_sort = resort ? 0 : c->since_sort + 1;
     c->launches += kernels_of(1, resort);
@@ -898,8 +893,8 @@ af3d_status af3d_step_profile(af3d_ctx *c, long k, double *ms) {
       af3d_status s = regrid(c);
       if (s) return s;
     }
-    AF3D_CUDA(cudaEventRecord(ev[7], c->st));
-    AF3D_CUDA(cudaEventSynchronize(ev[7]));
+    AF3D_CUDA(cudaEventRecord(ev[6], c->st));
+    AF3D_CUDA(cudaEventSynchronize(ev[6]));
     for (int p = 0; p < AF3D_NPROF; p++) {
       float t = 0.f;
       AF3D_CUDA(cudaEventElapsedTime(&t, ev[p], ev[p + 1]));

@@ -179,15 +179,13 @@ void launch_permute_records (const Launch &L, Planes src, Planes dst, const int 
                              const long long *id_src, long long *id_dst, const int *fl_src,
                              int *fl_dst, NbrRec *nbr, CullRec *cull, bool ft);
 void launch_build_records (const Launch &L, Planes cur, NbrRec *nbr, CullRec *cull);
-// The force pass: the item lists (launch_contact_lists), then the force kernel.  order: null
-// when the slots are in (cell, id) order, else cells.perm of the last sort, with csort the
-// matching culling centres.
-void launch_contact_lists (const Launch &L, DevScalars *d, const int *flume, const NbrRec *nbr,
-                           const CullRec *cull, const int *start, const int *order, const float4 *csort,
-                           ContactLists lists, const Consts *uniform = nullptr);
-void launch_fused_forces (const Launch &L, Planes cur, Planes out, DevScalars *d, const int *flume,
+// The force pass: each block builds its clumps' item lists, then processes them (walls, contacts,
+// bed, get_accel, finish_Verlet).  order: null when the slots are in (cell, id) order, else
+// cells.perm of the last sort, with csort the matching culling centres.
+void launch_lists_forces (const Launch &L, Planes cur, Planes out, DevScalars *d, const int *flume,
                           const NbrRec *nbr, const CullRec *cull, const int *start, const int *order,
-                          ContactLists lists, bool write_ft, const Consts *uniform = nullptr);
+                          const float4 *csort, ContactLists lists, bool write_ft,
+                          const Consts *uniform = nullptr);
 void launch_boundary (const Launch &L, Planes cur, DevScalars *d, const int *flume, int routine);
 void launch_part (const Launch &L, Planes cur, DevScalars *d, const int *flume, const NbrRec *nbr,
                   const CullRec *cull, const int *start, int sph_id);
@@ -236,12 +234,10 @@ namespace fast {
 void launch_predict (const Launch &L, Planes cur, DevScalars *d, bool predict, bool keys, bool t_prev,
                      Cells cells, const long long *id, const int *flume, NbrRec *nbr = nullptr,
                      CullRec *cull = nullptr);
-void launch_contact_lists (const Launch &L, DevScalars *d, const int *flume, const NbrRec *nbr,
-                           const CullRec *cull, const int *start, const int *order, const float4 *csort,
-                           ContactLists lists, const Consts *uniform = nullptr);
-void launch_fused_forces (const Launch &L, Planes cur, Planes out, DevScalars *d, const int *flume,
+void launch_lists_forces (const Launch &L, Planes cur, Planes out, DevScalars *d, const int *flume,
                           const NbrRec *nbr, const CullRec *cull, const int *start, const int *order,
-                          ContactLists lists, bool write_ft, const Consts *uniform = nullptr);
+                          const float4 *csort, ContactLists lists, bool write_ft,
+                          const Consts *uniform = nullptr);
 }  // namespace fast
 
 }  // namespace af3d

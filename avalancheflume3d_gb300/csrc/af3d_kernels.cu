@@ -4,8 +4,10 @@
 //   k_predict      init_Verlet (+ cell key, bucket count)              one thread per clump
 //   (cells)        scan of bucket counts, scatter, deterministic rank  af3d_cells.cu
 //   k_permute      move every plane into (cell, id) order, build the packed neighbour records
-//   k_fused_forces boundaries + sphere contacts + bed + get_accel + finish_Verlet, per clump,
-//                  gathering (never scattering) contributions: no atomics on forces
+//   k_lists_forces each block builds its clumps' contact item lists (neighbour walk, FP32
+//                  culling, exact overlap tests, boundary gates), then runs boundaries + sphere
+//                  contacts + bed + get_accel + finish_Verlet for them, gathering (never
+//                  scattering) contributions: no atomics on forces
 // The per-routine C-ABI entry points use k_boundary / k_part / k_get_accel / k_finish_verlet,
 // which apply the same device functions to the F, T planes one routine at a time.
 #include <cfloat>
@@ -511,7 +513,7 @@ __device__ __forceinline__ int particle_contacts(long s, const Own &o, const Con
 // Block-cooperative pass of the fused kernel over every contact of a clump: the boundary routines
 // that run before the particle contacts, the sixteen sph_id passes, and the routines that run
 // after them (avalanche: hop x3, funnel, fcorners, walls | part x16 | flume; fill: part x16 |
-// hop x3).  The list kernel (k_contact_lists) has published every clump's item list in that
+// hop x3).  The list phase (lists_body) has published every clump's item list in that
 // order: boundary items (routine, sphere) for the spheres the routine's 1-Lipschitz gate cannot
 // rule out, and particle items (partner slot, sph_id) of overlapping sphere pairs in sph_id-major
 // order.  The block concatenates the lists of its clumps and works through them in batches of
@@ -551,7 +553,7 @@ __device__ __forceinline__ int block_contacts(BlockQueue &bq, long bbase, long s
                                               const CullRec *__restrict__ cull,
                                               const int *__restrict__ start,
                                               const int *__restrict__ order,
-                                              const unsigned *__restrict__ items, int listed, long n,
+                                              const unsigned *items, int listed, long n,
                                               V3 &F, V3 &T) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int pre0 = aval ? R_HOP0 : 1, pre1 = aval ? R_WALLS : 0;         // fill: none before
@@ -586,7 +588,7 @@ __device__ __forceinline__ int block_contacts(BlockQueue &bq, long bbase, long s
       if (jb < bn) {
         const int j = b0 + jb;
         const int lo = block_owner_of(bq.base, j);   // the thread whose list holds item j
-        const unsigned it = __ldg(&items[(long)(j - bq.base[lo]) * n + bbase + lo]);
+        const unsigned it = items[(long)(j - bq.base[lo]) * n + bbase + lo];   // written in this launch
         const NbrRec &me = nbr[bbase + lo];   // owners hold clumps, so bbase + lo < n
         // Prepare the item's contact (type-specific, short), then run the contact law once for
         // every lane that has a contact, whatever its type.
@@ -687,7 +689,7 @@ __device__ __forceinline__ void warp_count(DevScalars *d, int active) {
   if ((threadIdx.x & 31) == 0 && v) atomicAdd(&d->contacts, (unsigned long long)v);
 }
 
-// k_contact_lists for one clump: its item lists (see warp_contacts) into `lists`.
+// The list phase of k_lists_forces for one clump: its item lists (see block_contacts) into `lists`.
 template <bool UNIFORM>
 __device__ __forceinline__ void lists_body(const Consts &c, const DevScalars *d, const int *__restrict__ flume,
                                            const NbrRec *__restrict__ nbr, const CullRec *__restrict__ cull,
@@ -712,31 +714,6 @@ __device__ __forceinline__ void lists_body(const Consts &c, const DevScalars *d,
   if (valid) lists.cnt[s] = slow ? -1 : k;
 }
 
-// The item lists of every clump of one force pass (the two-stage gather and the boundary gates),
-// ahead of the force kernel: a lean kernel, so that the neighbour walk runs with many warps
-// resident and most of the L1 free for the culling records.
-#ifndef AF3D_LISTS_MINB
-#define AF3D_LISTS_MINB 6
-#endif
-template <bool UNIFORM>
-__global__ void __launch_bounds__(kBlock, AF3D_LISTS_MINB) k_contact_lists(const DevScalars *d,
-                                                          const int *__restrict__ flume,
-                                                          const NbrRec *__restrict__ nbr,
-                                                          const CullRec *__restrict__ cull,
-                                                          const int *__restrict__ start,
-                                                          const int *__restrict__ order,
-                                                          const float4 *__restrict__ csort, ContactLists lists,
-                                                          const __grid_constant__ Consts kc, long n) {
-  __shared__ PassLists pl[kBlock / 32];
-  if constexpr (UNIFORM) {
-    lists_body<true>(kc, d, flume, nbr, cull, start, order, csort, lists, n, pl[threadIdx.x >> 5]);
-  } else {
-    const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    const Consts c = load_consts(d, flume[s < n ? s : n - 1]);
-    lists_body<false>(c, d, flume, nbr, cull, start, order, csort, lists, n, pl[threadIdx.x >> 5]);
-  }
-}
-
 template <bool WRITE_FT, bool UNIFORM>
 __device__ __forceinline__ void fused_body(const Consts &c, Planes P, Planes out, DevScalars *d,
                                            const int *__restrict__ flume, const NbrRec *__restrict__ nbr,
@@ -759,7 +736,7 @@ __device__ __forceinline__ void fused_body(const Consts &c, Planes P, Planes out
     for (int rt = R_HOP0; rt <= R_FCORNERS; rt++)
       if (bnd_may_touch(rt, o.r, B, c)) bnd_routine(rt, o, true, c, F, T);
   const long bbase = blockIdx.x * (long)blockDim.x;
-  const int listed = valid ? __ldg(&lists.cnt[s]) : 0;
+  const int listed = valid ? lists.cnt[s] : 0;
   const int active = block_contacts<UNIFORM>(bq, bbase, sv, valid && !removed, aval, B, o, c, g, off, d, flume, nbr,
                                              cull, start, order, lists.items, listed, n, F, T);
   if (valid) {
@@ -791,30 +768,6 @@ __device__ __forceinline__ void fused_body(const Consts &c, Planes P, Planes out
     }
   }
   warp_count(d, active);
-}
-
-// The whole force pass of one step for clump s, in the reference's call order, then get_accel
-// and finish_Verlet, from the item lists of k_contact_lists.  Velocities after the corrector go
-// to `out` (the other plane set), because neighbours still read this step's predicted
-// velocities from the records.  Every lane of a launched warp reaches the warp-cooperative
-// contact pass (lanes past n take no clump).  UNIFORM: one flume, whose constants are the
-// parameter kc; else each thread loads its flume's.
-template <bool WRITE_FT, bool UNIFORM>
-__global__ void __launch_bounds__(kBlock, AF3D_FORCES_MINB) k_fused_forces(Planes P, Planes out, DevScalars *d,
-                                                         const int *__restrict__ flume,
-                                                         const NbrRec *__restrict__ nbr,
-                                                         const CullRec *__restrict__ cull,
-                                                         const int *__restrict__ start,
-                                                         const int *__restrict__ order, ContactLists lists,
-                                                         const __grid_constant__ Consts kc, long n) {
-  __shared__ BlockQueue bq;
-  if constexpr (UNIFORM) {
-    fused_body<WRITE_FT, true>(kc, P, out, d, flume, nbr, cull, start, order, lists, n, bq);
-  } else {
-    const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    const Consts c = load_consts(d, flume[s < n ? s : n - 1]);
-    fused_body<WRITE_FT, false>(c, P, out, d, flume, nbr, cull, start, order, lists, n, bq);
-  }
 }
 
 // One boundary routine added to the F, T planes (per-routine entry points).
@@ -1114,35 +1067,57 @@ void launch_build_records(const Launch &L, Planes cur, NbrRec *nbr, CullRec *cul
                                                                 nullptr, nullptr, nbr, cull, true, L.n);
 }
 
-void launch_contact_lists(const Launch &L, DevScalars *d, const int *flume, const NbrRec *nbr, const CullRec *cull,
-                          const int *start, const int *order, const float4 *csort, ContactLists lists,
-                          const Consts *uniform) {
-  if (L.n <= 0) return;
-  const Consts kc = uniform ? *uniform : Consts{};
-  if (uniform)
-    k_contact_lists<true><<<grid_for(L.n), kBlock, 0, L.st>>>(d, flume, nbr, cull, start, order, csort, lists, kc, L.n);
-  else
-    k_contact_lists<false><<<grid_for(L.n), kBlock, 0, L.st>>>(d, flume, nbr, cull, start, order, csort, lists, kc,
-                                                              L.n);
+// The lists and the force pass of one block's clumps in one launch: the block builds its clumps'
+// item lists (the list kernel's work), then processes them (the force kernel's work).  Blocks
+// resident on one SM are in different phases most of the time, so the latency-bound walk of
+// some overlaps the FP64-bound contact laws of others.  The lists pass through global memory
+// (the block's own entries, visible to its threads after the barrier).
+template <bool WRITE_FT, bool UNIFORM>
+__global__ void __launch_bounds__(kBlock, AF3D_FORCES_MINB) k_lists_forces(Planes P, Planes out, DevScalars *d,
+                                                         const int *__restrict__ flume,
+                                                         const NbrRec *__restrict__ nbr,
+                                                         const CullRec *__restrict__ cull,
+                                                         const int *__restrict__ start,
+                                                         const int *__restrict__ order,
+                                                         const float4 *__restrict__ csort, ContactLists lists,
+                                                         const __grid_constant__ Consts kc, long n) {
+  __shared__ union Shared {
+    PassLists pl[kBlock / 32];
+    BlockQueue bq;
+  } sh;
+  if constexpr (UNIFORM) {
+    lists_body<true>(kc, d, flume, nbr, cull, start, order, csort, lists, n, sh.pl[threadIdx.x >> 5]);
+    __syncthreads();
+    fused_body<WRITE_FT, true>(kc, P, out, d, flume, nbr, cull, start, order, lists, n, sh.bq);
+  } else {
+    const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    const Consts c = load_consts(d, flume[s < n ? s : n - 1]);
+    lists_body<false>(c, d, flume, nbr, cull, start, order, csort, lists, n, sh.pl[threadIdx.x >> 5]);
+    __syncthreads();
+    fused_body<WRITE_FT, false>(c, P, out, d, flume, nbr, cull, start, order, lists, n, sh.bq);
+  }
 }
 
-void launch_fused_forces(const Launch &L, Planes cur, Planes out, DevScalars *d, const int *flume,
+void launch_lists_forces(const Launch &L, Planes cur, Planes out, DevScalars *d, const int *flume,
                          const NbrRec *nbr, const CullRec *cull, const int *start, const int *order,
-                         ContactLists lists, bool write_ft, const Consts *uniform) {
+                         const float4 *csort, ContactLists lists, bool write_ft, const Consts *uniform) {
   if (L.n <= 0) return;
   const Consts kc = uniform ? *uniform : Consts{};
   const int g = grid_for(L.n);
   if (uniform) {
     if (write_ft)
-      k_fused_forces<true, true><<<g, kBlock, 0, L.st>>>(cur, out, d, flume, nbr, cull, start, order, lists, kc, L.n);
+      k_lists_forces<true, true><<<g, kBlock, 0, L.st>>>(cur, out, d, flume, nbr, cull, start, order, csort, lists, kc,
+                                                        L.n);
     else
-      k_fused_forces<false, true><<<g, kBlock, 0, L.st>>>(cur, out, d, flume, nbr, cull, start, order, lists, kc, L.n);
+      k_lists_forces<false, true><<<g, kBlock, 0, L.st>>>(cur, out, d, flume, nbr, cull, start, order, csort, lists,
+                                                         kc, L.n);
   } else {
     if (write_ft)
-      k_fused_forces<true, false><<<g, kBlock, 0, L.st>>>(cur, out, d, flume, nbr, cull, start, order, lists, kc, L.n);
+      k_lists_forces<true, false><<<g, kBlock, 0, L.st>>>(cur, out, d, flume, nbr, cull, start, order, csort, lists,
+                                                         kc, L.n);
     else
-      k_fused_forces<false, false><<<g, kBlock, 0, L.st>>>(cur, out, d, flume, nbr, cull, start, order, lists, kc,
-                                                            L.n);
+      k_lists_forces<false, false><<<g, kBlock, 0, L.st>>>(cur, out, d, flume, nbr, cull, start, order, csort, lists,
+                                                          kc, L.n);
   }
 }
 

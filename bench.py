@@ -151,8 +151,8 @@ def measured_peaks():
 
 
 def traffic_from_profile():
-    """DRAM bytes per launch of the fused force kernel from the committed ncu summary, if any."""
-    fn = os.path.join(ROOT, "profiles", "fused_forces_flume262k.txt")
+    """DRAM bytes per launch of the force kernel from the committed ncu summary, if any."""
+    fn = os.path.join(ROOT, "profiles", "lists_forces_flume262k.txt")
     try:
         for line in open(fn):
             if line.startswith("traffic_bytes_per_launch:"):
@@ -460,8 +460,7 @@ def run_engine(args):
 
     # Roofline of the dominant kernel from CUDA events between the kernels (profiled steps after
     # the timed region, same stream).
-    names = ["time_advance", "predict_keys", "cell_sort", "permute_records", "contact_lists", "fused_forces",
-             "regrid"]
+    names = ["time_advance", "predict_keys", "cell_sort", "permute_records", "fused_forces", "regrid"]
     prof = np.zeros(len(names))
     lib().af3d_step_profile(eng._h, args.profile_steps, prof.ctypes.data_as(C.c_void_p))
     prof /= args.profile_steps
@@ -532,7 +531,7 @@ def run_engine(args):
             "contacts_per_step": contacts / args.steps,
             "e2e": e2e,
             "gpu_launches": int(launches1.value - launches0.value),
-            "roofline": {"bound": "hbm", "kernel": "k_fused_forces", "achieved": achieved,
+            "roofline": {"bound": "hbm", "kernel": "k_lists_forces", "achieved": achieved,
                          "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
                          "frac": (achieved / peaks["hbm_gbs"]) if achieved else None,
                          "peak_source": peak_kind, "traffic": traffic_from_profile(),

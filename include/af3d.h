@@ -183,9 +183,8 @@ af3d_status af3d_step (af3d_ctx *ctx, long k);
 /* Same steps as af3d_step, enqueued without graphs and with CUDA events between the kernels on
    the context stream; adds the milliseconds of each phase to ms[AF3D_NPROF]:
    0 time advance, 1 init_Verlet + cell keys, 2 cell sort, 3 permutation + neighbour records,
-   4 contact lists (neighbour walk, culling, boundary gates), 5 fused force kernel (walls,
-   contacts, bed, get_accel, finish_Verlet), 6 re-grid. */
-enum { AF3D_NPROF = 7 };
+   4 force kernel (contact lists, walls, contacts, bed, get_accel, finish_Verlet), 5 re-grid. */
+enum { AF3D_NPROF = 6 };
 af3d_status af3d_step_profile (af3d_ctx *ctx, long k, double *ms);
 /* Kernels executed on the device by this context so far (graph replays included). */
 af3d_status af3d_kernel_launches (af3d_ctx *ctx, long *count);
