@@ -572,8 +572,9 @@ __global__ void __launch_bounds__(kAdjCoopBlock) k_adj_forces(Planes P, Planes i
   const bool aval = c.phase == AF3D_PHASE_AVALANCHE;
   const double B = (double)cull[sv].c.w;
   bool slow = false;
+  ListCounts lcounts;
   const int nitems = build_item_lists(aq.il.pl, &aq.il.items[0][lane], 32, wbase, sv, act, aval, o.r, c, g,
-                                      d->flumes[f].gridf, off, nbr, cull, start, order, csort, slow);
+                                      d->flumes[f].gridf, off, nbr, cull, start, order, csort, slow, lcounts);
   const int total = warp_prefix(nitems, aq.il.base);
   for (int j0 = 0; j0 < total; j0 += 32) {
     const int j = j0 + lane;

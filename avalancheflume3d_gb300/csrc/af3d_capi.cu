@@ -476,7 +476,6 @@ af3d_status af3d_create_ensemble(int nflumes, const af3d_system_par *sys, const 
   ok = ok && cudaMalloc((void **)&c->nbr, sizeof(NbrRec) * n) == cudaSuccess;
   ok = ok && cudaMalloc((void **)&c->cull, sizeof(CullRec) * n) == cudaSuccess;
   ok = ok && cudaMalloc((void **)&c->lists.items, sizeof(unsigned) * kListCap * n) == cudaSuccess;
-  ok = ok && cudaMalloc((void **)&c->lists.cnt, sizeof(int) * n) == cudaSuccess;
   ok = ok && cudaMalloc((void **)&c->cells.key, sizeof(int) * n) == cudaSuccess;
   ok = ok && cudaMalloc((void **)&c->cells.rank_tmp, sizeof(int) * n) == cudaSuccess;
   ok = ok && cudaMalloc((void **)&c->cells.tmp_slot, sizeof(int) * n) == cudaSuccess;
@@ -539,7 +538,7 @@ af3d_status af3d_destroy(af3d_ctx *c) {
   drop_graphs(c);
   for (void *p : {(void *)c->plane_mem[0], (void *)c->plane_mem[1], (void *)c->id_cur, (void *)c->id_alt,
                   (void *)c->fl_cur, (void *)c->fl_alt, (void *)c->flume_of_id, (void *)c->nbr,
-                  (void *)c->cull, (void *)c->lists.items, (void *)c->lists.cnt, (void *)c->cells.key, (void *)c->cells.rank_tmp, (void *)c->cells.tmp_slot,
+                  (void *)c->cull, (void *)c->lists.items, (void *)c->cells.key, (void *)c->cells.rank_tmp, (void *)c->cells.tmp_slot,
                   (void *)c->cells.perm, (void *)c->cells.csort, (void *)c->cells.count, (void *)c->cells.start,
                   (void *)c->cells.block_sums, (void *)c->d, (void *)c->flumes, (void *)c->d_aos,
                   (void *)c->d_acc, (void *)c->d_anga, (void *)c->d_tmp, (void *)c->d_count})

@@ -291,21 +291,28 @@ __device__ __forceinline__ int gather_partners(PassLists &pl, long s, float4 mc,
 // overlap test of every sphere pair the FP32 test could not rule out.  Items go to the lane's column `col`, entries
 // `stride` apart.  All 32 lanes call this; returns the lane's item count, 0 with `slow` set
 // when the lane's lists would overflow.
+// (the counts of a clump's list: `pre` boundary items, then `pair` particle items, then the rest)
+struct ListCounts {
+  int pre, pair;
+};
+
 __device__ __forceinline__ int build_item_lists(PassLists &pl, unsigned *col, long stride, long wbase, long s,
                                                 bool act, bool aval, V3 r, const Consts &c,
                                                 const af3d_cell_par &g, const GridF &gf, long long off,
                                                 const NbrRec *__restrict__ nbr,
                                                 const CullRec *__restrict__ cull, const int *__restrict__ start,
                                                 const int *__restrict__ order, const float4 *__restrict__ csort,
-                                                bool &slow) {
+                                                bool &slow, ListCounts &lc) {
   const int lane = threadIdx.x & 31;
   const int pre0 = aval ? R_HOP0 : 1, pre1 = aval ? R_WALLS : 0;         // fill: none before
   const int post0 = aval ? R_FLUME : R_HOP0, post1 = aval ? R_FLUME : R_HOP2;
   int nitems = 0;
   slow = false;
+  lc.pre = lc.pair = 0;
   const CullRec me = cull[s];
   const bool door_closed = *c.tp < 0.0;
   if (act) slow = !push_boundary(pre0, pre1, me, c, door_closed, col, stride, nitems);
+  lc.pre = nitems;
   int npass = 0;
   if (act && !slow) {
     npass = gather_partners(pl, s, me.c, search_centre_f(me.c, r, g, gf, off), g, start, order, csort, cull);
@@ -390,6 +397,7 @@ __device__ __forceinline__ int build_item_lists(PassLists &pl, unsigned *col, lo
       const unsigned t = pl.pass_t[e >> 4][lane] & kSlotMask;
       col[stride * nitems++] = (t << 4) | (e & 15u);   // (partner slot, sph_id-1)
     }
+    lc.pair = nitems - lc.pre;
     slow = !push_boundary(post0, post1, me, c, door_closed, col, stride, nitems);
   }
   return slow ? 0 : nitems;

@@ -106,14 +106,12 @@ struct DevScalars {
   DevFlume       *flumes;      // [nflumes]
 };
 
-// Per-clump item lists of one force pass, from the list kernel to the force kernel: entry e of
-// slot s at items[e * n + s] (an item is a boundary (routine, sphere) or a particle (partner
-// slot, sph_id) contact), and the count at cnt[s] (-1: the clump's lists overflowed and the
-// force kernel walks its neighbours itself).
+// Per-clump item lists of one force pass, from the list phase to the force phase of the force
+// kernel: entry e of slot s at items[e * n + s] (an item is a boundary (routine, sphere) or a
+// particle (partner slot, sph_id) contact).
 constexpr int kListCap = 32;
 struct ContactLists {
   unsigned *items;   // [kListCap][n]
-  int *cnt;          // [n]
 };
 
 // Scalars of one flume's system_par / Funnel used by the force routines.  A single-flume

@@ -527,7 +527,10 @@ __device__ __forceinline__ int particle_contacts(long s, const Own &o, const Con
 constexpr int kBatch = 256;
 struct BlockQueue {
   int base[kBlock + 1];   // exclusive prefix of the clumps' item counts
-  int wsum[kBlock / 32];
+  int pbase[kBlock + 1];  // ... of their particle item counts (kind-sorted pass)
+  int qbase[kBlock + 1];  // ... of their boundary item counts (kind-sorted pass)
+  int npre[kBlock];       // boundary items before the particle items, per clump
+  int wsum[3][kBlock / 32];
   double res[6][kBatch];  // [component][item in the batch]
   unsigned char flag[kBatch];
 };
@@ -542,8 +545,40 @@ __device__ __forceinline__ int block_owner_of(const int *base, int j) {
   return lo;
 }
 
+// Block-wide exclusive prefixes of three per-thread counts (all threads call this).
+__device__ __forceinline__ void block_prefix3(BlockQueue &bq, int a, int b, int c) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  int v[3] = {a, b, c};
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+#pragma unroll
+    for (int k = 1; k < 32; k <<= 1) {
+      const int u = __shfl_up_sync(0xffffffffu, v[q], k);
+      if (lane >= k) v[q] += u;
+    }
+    if (lane == 31) bq.wsum[q][warp] = v[q];
+  }
+  __syncthreads();
+  int *dst[3] = {bq.base, bq.pbase, bq.qbase};
+  const int own[3] = {a, b, c};
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+    int wofs = 0, total = 0;
+#pragma unroll
+    for (int w = 0; w < kBlock / 32; w++) {
+      const int t = bq.wsum[q][w];
+      wofs += w < warp ? t : 0;
+      total += t;
+    }
+    dst[q][tid] = wofs + v[q] - own[q];
+    if (tid == kBlock - 1) dst[q][kBlock] = total;
+  }
+  __syncthreads();
+}
+
 // UNIFORM: every clump of the launch belongs to one flume, whose constants `c` are (a
-// reference to) a kernel parameter.
+// reference to) a kernel parameter.  lc: the clump's list layout (pre boundary items, particle
+// items, the rest boundary items).
 template <bool UNIFORM>
 __device__ __forceinline__ int block_contacts(BlockQueue &bq, long bbase, long s, bool act, bool aval,
                                               double B, const Own &o, const Consts &c,
@@ -553,101 +588,117 @@ __device__ __forceinline__ int block_contacts(BlockQueue &bq, long bbase, long s
                                               const CullRec *__restrict__ cull,
                                               const int *__restrict__ start,
                                               const int *__restrict__ order,
-                                              const unsigned *items, int listed, long n,
+                                              const unsigned *items, int listed, ListCounts lc, long n,
                                               V3 &F, V3 &T) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int pre0 = aval ? R_HOP0 : 1, pre1 = aval ? R_WALLS : 0;         // fill: none before
   const int post0 = aval ? R_FLUME : R_HOP0, post1 = aval ? R_FLUME : R_HOP2;
   const bool slow = act && listed < 0;
   const int nitems = act && listed > 0 ? listed : 0;
-  // block-wide exclusive prefix of the item counts
-  int incl = nitems;
-#pragma unroll
-  for (int k = 1; k < 32; k <<= 1) {
-    const int u = __shfl_up_sync(0xffffffffu, incl, k);
-    if (lane >= k) incl += u;
-  }
-  if (lane == 31) bq.wsum[warp] = incl;
-  __syncthreads();
-  int wofs = 0, total = 0;
-#pragma unroll
-  for (int w = 0; w < kBlock / 32; w++) {
-    const int t = bq.wsum[w];
-    wofs += w < warp ? t : 0;
-    total += t;
-  }
-  const int base = wofs + incl - nitems;
-  bq.base[tid] = base;
-  if (tid == kBlock - 1) bq.base[kBlock] = total;
-  __syncthreads();
+  const int npair = nitems > 0 ? lc.pair : 0;
+  bq.npre[tid] = nitems > 0 ? lc.pre : 0;
+  block_prefix3(bq, nitems, npair, nitems - npair);
+  const int base = bq.base[tid], total = bq.base[kBlock];
+  const int ptotal = bq.pbase[kBlock];
+  // One item: its contact into the batch's result slot jb.
+  auto process = [&](int lo, int idx, int jb) {
+    const unsigned it = items[(long)idx * n + bbase + lo];   // written in this launch
+    const NbrRec &me = nbr[bbase + lo];   // owners hold clumps, so bbase + lo < n
+    // Prepare the item's contact (type-specific, short), then run the contact law.
+    auto contact = [&](const Consts &co, V3 &fs, V3 &tq) -> int {
+      ContactIn ci;
+      V3 rl = mk(me.rx, me.ry, me.rz);
+      int kind;   // 0 nothing, 1 sphere pair, 2 wall
+      if (it >= kBndItem) {
+        const int rt = (int)((it >> 2) & 7u), ns = (int)(it & 3u);
+        Sph q;
+        q.r = rl;
+        q.v = mk(me.vx, me.vy, me.vz);
+        q.w = mk(me.wx, me.wy, me.wz);
+        q.s = mk(me.s[3 * ns], me.s[3 * ns + 1], me.s[3 * ns + 2]);
+        q.rad = me.rad;
+        q.mwall = me.mwall;
+        kind = bnd_input(rt, q, co, ci) ? 2 : 0;
+      } else {
+        const int t = (int)(it >> 4), p = (int)(it & 15u);
+        const V3 vl = mk(me.vx, me.vy, me.vz), wl = mk(me.wx, me.wy, me.wz);
+        const int k = p & 3;
+        const V3 s1 = mk(me.s[3 * k], me.s[3 * k + 1], me.s[3 * k + 2]);
+        kind = pair_input(rl, vl, wl, s1, me.rad, me.msph, nbr[t], p >> 2, co,
+                          co.variant == AF3D_FRICTION_DEV, ci) ? 1 : 0;
+      }
+      int r = kind == 1 ? 1 : 0;
+      if (kind && apply_law(ci, rl, co, fs, tq)) r = kind == 1 ? 2 : 3;
+      return r;
+    };
+    V3 fs, tq;
+    int r;
+    if constexpr (UNIFORM) {
+      r = contact(c, fs, tq);
+    } else {
+      // the owner's flume may differ from this thread's at a flume boundary of an ensemble
+      const int of = flume[bbase + lo];
+      const Consts co = of == flume[s] ? c : load_consts(d, of);
+      r = contact(co, fs, tq);
+    }
+    bq.flag[jb] = (unsigned char)r;
+    if (r >= 2) {
+      bq.res[0][jb] = fs.x; bq.res[1][jb] = fs.y; bq.res[2][jb] = fs.z;
+      bq.res[3][jb] = tq.x; bq.res[4][jb] = tq.y; bq.res[5][jb] = tq.z;
+    }
+  };
   int active = 0;
-  for (int b0 = 0; b0 < total; b0 += kBatch) {
-    const int bn = total - b0 < kBatch ? total - b0 : kBatch;
-    for (int r0 = warp * 32; r0 < bn; r0 += kBlock) {
-      const int jb = r0 + lane;
-      if (jb < bn) {
-        const int j = b0 + jb;
-        const int lo = block_owner_of(bq.base, j);   // the thread whose list holds item j
-        const unsigned it = items[(long)(j - bq.base[lo]) * n + bbase + lo];   // written in this launch
-        const NbrRec &me = nbr[bbase + lo];   // owners hold clumps, so bbase + lo < n
-        // Prepare the item's contact (type-specific, short), then run the contact law once for
-        // every lane that has a contact, whatever its type.
-        auto contact = [&](const Consts &co, V3 &fs, V3 &tq) -> int {
-          ContactIn ci;
-          V3 rl = mk(me.rx, me.ry, me.rz);
-          int kind;   // 0 nothing, 1 sphere pair, 2 wall
-          if (it >= kBndItem) {
-            const int rt = (int)((it >> 2) & 7u), ns = (int)(it & 3u);
-            Sph q;
-            q.r = rl;
-            q.v = mk(me.vx, me.vy, me.vz);
-            q.w = mk(me.wx, me.wy, me.wz);
-            q.s = mk(me.s[3 * ns], me.s[3 * ns + 1], me.s[3 * ns + 2]);
-            q.rad = me.rad;
-            q.mwall = me.mwall;
-            kind = bnd_input(rt, q, co, ci) ? 2 : 0;
-          } else {
-            const int t = (int)(it >> 4), p = (int)(it & 15u);
-            const V3 vl = mk(me.vx, me.vy, me.vz), wl = mk(me.wx, me.wy, me.wz);
-            const int k = p & 3;
-            const V3 s1 = mk(me.s[3 * k], me.s[3 * k + 1], me.s[3 * k + 2]);
-            kind = pair_input(rl, vl, wl, s1, me.rad, me.msph, nbr[t], p >> 2, co,
-                              co.variant == AF3D_FRICTION_DEV, ci) ? 1 : 0;
-          }
-          int r = kind == 1 ? 1 : 0;
-          if (kind && apply_law(ci, rl, co, fs, tq)) r = kind == 1 ? 2 : 3;
-          return r;
-        };
-        V3 fs, tq;
-        int r;
-        if constexpr (UNIFORM) {
-          r = contact(c, fs, tq);
+  // Owners add their items' terms in list order.
+  auto gather = [&](int b0, int bn) {
+    if (nitems <= 0) return;
+    const int a = base > b0 ? base : b0;
+    const int b = base + nitems < b0 + bn ? base + nitems : b0 + bn;
+    for (int e = a - b0; e < b - b0; e++) {
+      const int fl = bq.flag[e];
+      if (fl < 2) continue;
+      T.x += bq.res[3][e]; T.y += bq.res[4][e]; T.z += bq.res[5][e];
+      F.x += bq.res[0][e]; F.y += bq.res[1][e]; F.z += bq.res[2][e];
+      active += fl == 2;   // sphere-sphere contacts only
+    }
+  };
+  if (total <= kBatch) {
+    // One batch, in kind order: every particle item of the block, then every boundary item, 32
+    // a round per warp, so that each round runs one input routine; results go to the items'
+    // places in the owners' lists.
+    for (int r0 = warp * 32; r0 < total; r0 += kBlock) {
+      const int i = r0 + lane;
+      if (i < total) {
+        int lo, idx;
+        if (i < ptotal) {
+          lo = block_owner_of(bq.pbase, i);
+          idx = bq.npre[lo] + (i - bq.pbase[lo]);
         } else {
-          // the owner's flume may differ from this thread's at a flume boundary of an ensemble
-          const int of = flume[bbase + lo];
-          const Consts co = of == flume[s] ? c : load_consts(d, of);
-          r = contact(co, fs, tq);
+          const int ib = i - ptotal;
+          lo = block_owner_of(bq.qbase, ib);
+          const int b = ib - bq.qbase[lo], np = bq.npre[lo];
+          idx = b < np ? b : b + (bq.pbase[lo + 1] - bq.pbase[lo]);
         }
-        bq.flag[jb] = (unsigned char)r;
-        if (r >= 2) {
-          bq.res[0][jb] = fs.x; bq.res[1][jb] = fs.y; bq.res[2][jb] = fs.z;
-          bq.res[3][jb] = tq.x; bq.res[4][jb] = tq.y; bq.res[5][jb] = tq.z;
-        }
+        process(lo, idx, bq.base[lo] + idx);
       }
     }
     __syncthreads();
-    if (nitems > 0) {
-      const int a = base > b0 ? base : b0;
-      const int b = base + nitems < b0 + bn ? base + nitems : b0 + bn;
-      for (int e = a - b0; e < b - b0; e++) {
-        const int fl = bq.flag[e];
-        if (fl < 2) continue;
-        T.x += bq.res[3][e]; T.y += bq.res[4][e]; T.z += bq.res[5][e];
-        F.x += bq.res[0][e]; F.y += bq.res[1][e]; F.z += bq.res[2][e];
-        active += fl == 2;   // sphere-sphere contacts only
+    gather(0, total);
+  } else {
+    // Batches of kBatch items in the owners' order.
+    for (int b0 = 0; b0 < total; b0 += kBatch) {
+      const int bn = total - b0 < kBatch ? total - b0 : kBatch;
+      for (int r0 = warp * 32; r0 < bn; r0 += kBlock) {
+        const int jb = r0 + lane;
+        if (jb < bn) {
+          const int j = b0 + jb;
+          const int lo = block_owner_of(bq.base, j);   // the thread whose list holds item j
+          process(lo, j - bq.base[lo], jb);
+        }
       }
+      __syncthreads();
+      gather(b0, bn);
+      __syncthreads();
     }
-    __syncthreads();
   }
   if (slow) {
     for (int rt = pre0; rt <= pre1; rt++)
@@ -689,13 +740,14 @@ __device__ __forceinline__ void warp_count(DevScalars *d, int active) {
   if ((threadIdx.x & 31) == 0 && v) atomicAdd(&d->contacts, (unsigned long long)v);
 }
 
-// The list phase of k_lists_forces for one clump: its item lists (see block_contacts) into `lists`.
+// The list phase of k_lists_forces for one clump: its item lists (see block_contacts) into
+// `lists`; returns the item count (-1: the lists overflowed) and their layout in lc.
 template <bool UNIFORM>
-__device__ __forceinline__ void lists_body(const Consts &c, const DevScalars *d, const int *__restrict__ flume,
+__device__ __forceinline__ int lists_body(const Consts &c, const DevScalars *d, const int *__restrict__ flume,
                                            const NbrRec *__restrict__ nbr, const CullRec *__restrict__ cull,
                                            const int *__restrict__ start, const int *__restrict__ order,
                                            const float4 *__restrict__ csort, ContactLists lists, long n,
-                                           PassLists &pl) {
+                                           PassLists &pl, ListCounts &lc) {
   const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
   const bool valid = s < n;
   const long sv = valid ? s : n - 1;
@@ -710,16 +762,16 @@ __device__ __forceinline__ void lists_body(const Consts &c, const DevScalars *d,
   bool slow = false;
   const int k = build_item_lists(pl, lists.items + sv, n, blockIdx.x * (long)blockDim.x + (threadIdx.x & ~31u), sv,
                                  act, c.phase == AF3D_PHASE_AVALANCHE, r, c, g, gf, off, nbr, cull, start, order,
-                                 csort, slow);
-  if (valid) lists.cnt[s] = slow ? -1 : k;
+                                 csort, slow, lc);
+  return slow ? -1 : k;
 }
 
 template <bool WRITE_FT, bool UNIFORM>
 __device__ __forceinline__ void fused_body(const Consts &c, Planes P, Planes out, DevScalars *d,
                                            const int *__restrict__ flume, const NbrRec *__restrict__ nbr,
                                            const CullRec *__restrict__ cull, const int *__restrict__ start,
-                                           const int *__restrict__ order, ContactLists lists, long n,
-                                           BlockQueue &bq) {
+                                           const int *__restrict__ order, ContactLists lists, int listed,
+                                           ListCounts lc, long n, BlockQueue &bq) {
   const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
   const bool valid = s < n;
   const long sv = valid ? s : n - 1;   // in-range slot for lanes past n (nothing is written for them)
@@ -736,9 +788,8 @@ __device__ __forceinline__ void fused_body(const Consts &c, Planes P, Planes out
     for (int rt = R_HOP0; rt <= R_FCORNERS; rt++)
       if (bnd_may_touch(rt, o.r, B, c)) bnd_routine(rt, o, true, c, F, T);
   const long bbase = blockIdx.x * (long)blockDim.x;
-  const int listed = valid ? lists.cnt[s] : 0;
   const int active = block_contacts<UNIFORM>(bq, bbase, sv, valid && !removed, aval, B, o, c, g, off, d, flume, nbr,
-                                             cull, start, order, lists.items, listed, n, F, T);
+                                             cull, start, order, lists.items, valid ? listed : 0, lc, n, F, T);
   if (valid) {
     if (WRITE_FT) {
       store3(P, FX, s, F);
@@ -1085,16 +1136,19 @@ __global__ void __launch_bounds__(kBlock, AF3D_FORCES_MINB) k_lists_forces(Plane
     PassLists pl[kBlock / 32];
     BlockQueue bq;
   } sh;
+  ListCounts lc;
   if constexpr (UNIFORM) {
-    lists_body<true>(kc, d, flume, nbr, cull, start, order, csort, lists, n, sh.pl[threadIdx.x >> 5]);
+    const int listed = lists_body<true>(kc, d, flume, nbr, cull, start, order, csort, lists, n,
+                                        sh.pl[threadIdx.x >> 5], lc);
     __syncthreads();
-    fused_body<WRITE_FT, true>(kc, P, out, d, flume, nbr, cull, start, order, lists, n, sh.bq);
+    fused_body<WRITE_FT, true>(kc, P, out, d, flume, nbr, cull, start, order, lists, listed, lc, n, sh.bq);
   } else {
     const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
     const Consts c = load_consts(d, flume[s < n ? s : n - 1]);
-    lists_body<false>(c, d, flume, nbr, cull, start, order, csort, lists, n, sh.pl[threadIdx.x >> 5]);
+    const int listed = lists_body<false>(c, d, flume, nbr, cull, start, order, csort, lists, n,
+                                         sh.pl[threadIdx.x >> 5], lc);
     __syncthreads();
-    fused_body<WRITE_FT, false>(c, P, out, d, flume, nbr, cull, start, order, lists, n, sh.bq);
+    fused_body<WRITE_FT, false>(c, P, out, d, flume, nbr, cull, start, order, lists, listed, lc, n, sh.bq);
   }
 }
 
