@@ -27,6 +27,7 @@ enum Plane : int {
   MSPH,                                          // SPH_FACT*density*r^3 (force_part.cu:58 order)
   MWALL,                                         // SPH_FACT*r^3*density (force_walls.cu:47 order)
   ADRAG,                                         // DRAG*r*r/mass (get_accel.cu:47 order)
+  IMASS, IINER,                                  // 1/mass, 1/inertia (fast FP64 mode)
   NPLANES
 };
 

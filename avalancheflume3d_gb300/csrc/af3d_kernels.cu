@@ -76,6 +76,8 @@ __global__ void k_aos_to_planes(const af3d_particle *__restrict__ aos, const dou
   P.p[MSPH][s] = kSPH_FACT * rho * r * r * r;   // force_part.cu:58
   P.p[MWALL][s] = kSPH_FACT * r * r * r * rho;  // force_walls.cu:47
   P.p[ADRAG][s] = drag_factor(r, q.mass);       // get_accel.cu:47
+  P.p[IMASS][s] = 1.0 / q.mass;
+  P.p[IINER][s] = 1.0 / q.moment_of_inertia.x;
   id[s] = s;
   flume[s] = flume_of_id[s];
 }
@@ -661,44 +663,35 @@ __device__ __forceinline__ int block_contacts(BlockQueue &bq, long bbase, long s
       active += fl == 2;   // sphere-sphere contacts only
     }
   };
-  if (total <= kBatch) {
-    // One batch, in kind order: every particle item of the block, then every boundary item, 32
-    // a round per warp, so that each round runs one input routine; results go to the items'
-    // places in the owners' lists.
-    for (int r0 = warp * 32; r0 < total; r0 += kBlock) {
+  // A block whose items fit one batch takes them in kind order: every particle item of the
+  // block, then every boundary item, 32 a round per warp, so that each round runs one input
+  // routine; results go to the items' places in the owners' lists.  Otherwise batches of kBatch
+  // items in the owners' order.
+  const bool kind_order = total <= kBatch;
+  for (int b0 = 0; b0 < total; b0 += kBatch) {
+    const int bn = total - b0 < kBatch ? total - b0 : kBatch;
+    for (int r0 = warp * 32; r0 < bn; r0 += kBlock) {
       const int i = r0 + lane;
-      if (i < total) {
+      if (i < bn) {
         int lo, idx;
-        if (i < ptotal) {
+        if (kind_order && i < ptotal) {
           lo = block_owner_of(bq.pbase, i);
           idx = bq.npre[lo] + (i - bq.pbase[lo]);
-        } else {
+        } else if (kind_order) {
           const int ib = i - ptotal;
           lo = block_owner_of(bq.qbase, ib);
           const int b = ib - bq.qbase[lo], np = bq.npre[lo];
           idx = b < np ? b : b + (bq.pbase[lo + 1] - bq.pbase[lo]);
+        } else {
+          lo = block_owner_of(bq.base, b0 + i);   // the thread whose list holds item b0 + i
+          idx = b0 + i - bq.base[lo];
         }
-        process(lo, idx, bq.base[lo] + idx);
+        process(lo, idx, kind_order ? bq.base[lo] + idx : i);
       }
     }
     __syncthreads();
-    gather(0, total);
-  } else {
-    // Batches of kBatch items in the owners' order.
-    for (int b0 = 0; b0 < total; b0 += kBatch) {
-      const int bn = total - b0 < kBatch ? total - b0 : kBatch;
-      for (int r0 = warp * 32; r0 < bn; r0 += kBlock) {
-        const int jb = r0 + lane;
-        if (jb < bn) {
-          const int j = b0 + jb;
-          const int lo = block_owner_of(bq.base, j);   // the thread whose list holds item j
-          process(lo, j - bq.base[lo], jb);
-        }
-      }
-      __syncthreads();
-      gather(b0, bn);
-      __syncthreads();
-    }
+    gather(b0, bn);
+    __syncthreads();
   }
   if (slow) {
     for (int rt = pre0; rt <= pre1; rt++)
@@ -801,7 +794,7 @@ __device__ __forceinline__ void fused_body(const Consts &c, Planes P, Planes out
     if (!removed) {
       V3 a, al;
       get_accel_one(F, T, v, w, load3(P, R00, s), load3(P, R10, s), load3(P, R20, s), P.p[MASS][s],
-                    P.p[ADRAG][s], load3(P, IXX, s), a, al);
+                    P.p[ADRAG][s], load3(P, IXX, s), a, al, P.p[IMASS][s], P.p[IINER][s]);
       store3(P, AFX, s, a);
       store3(P, ALFX, s, al);
       const V3 ai = load3(P, AIX, s), ali = load3(P, ALIX, s);
@@ -858,7 +851,7 @@ __global__ void k_get_accel(Planes P, DevScalars *d, const int *__restrict__ flu
   if (is_removed(d->time, P.p[RX][s], d->flumes[flume[s]].sys.side.x)) return;
   V3 a, al;
   get_accel_one(load3(P, FX, s), load3(P, TX, s), load3(P, VX, s), load3(P, WX, s), load3(P, R00, s),
-                load3(P, R10, s), load3(P, R20, s), P.p[MASS][s], P.p[ADRAG][s], load3(P, IXX, s), a, al);
+                load3(P, R10, s), load3(P, R20, s), P.p[MASS][s], P.p[ADRAG][s], load3(P, IXX, s), a, al, P.p[IMASS][s], P.p[IINER][s]);
   store3(P, AFX, s, a);
   store3(P, ALFX, s, al);
 }

@@ -555,12 +555,12 @@ __device__ __forceinline__ double signed_zero_product(double a, double b) {
 // clumps, calculate_particle_parameters.cu:33) the Euler coupling terms C*wb*wb are (+0*wb)*wb,
 // i.e. signed zeros; they are formed from the sign bits instead of two divisions-by-I and four
 // multiplications, which gives the same bits for finite angular velocities.
+// (fast mode: im = 1/m and iI = 1/I.x, formed once at import, replace the divisions)
 __device__ __forceinline__ void get_accel_one(V3 f, V3 t, V3 v, V3 w, V3 Rx, V3 Ry, V3 Rz, double m,
-                                              double adrag0, V3 I, V3 &a, V3 &al) {
+                                              double adrag0, V3 I, V3 &a, V3 &al, double im, double iI) {
   double vmag = sqrt(v.x * v.x + v.y * v.y + v.z * v.z);
   double adrag = adrag0 * vmag;
   if (kFast) {
-    const double im = 1.0 / m;
     a.x = f.x * im - adrag * v.x;
     a.y = f.y * im - adrag * v.y;
     a.z = f.z * im - adrag * v.z - kGRAV;
@@ -579,7 +579,6 @@ __device__ __forceinline__ void get_accel_one(V3 f, V3 t, V3 v, V3 w, V3 Rx, V3 
   if (I.x == I.y && I.y == I.z && isfinite(wb.x) && isfinite(wb.y) && isfinite(wb.z) && I.x > 0.0 &&
       isfinite(I.x)) {
     if (kFast) {
-      const double iI = 1.0 / I.x;
       ab.x = tb.x * iI + signed_zero_product(wb.y, wb.z);
       ab.y = tb.y * iI + signed_zero_product(wb.z, wb.x);
       ab.z = tb.z * iI + signed_zero_product(wb.x, wb.y);
