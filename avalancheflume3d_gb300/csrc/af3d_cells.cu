@@ -16,8 +16,24 @@ namespace af3d {
 namespace {
 
 constexpr int kScanThreads = 256;
-constexpr int kScanItems = 4;
+constexpr int kScanItems = 16;   // consecutive buckets per thread, moved as four int4
 constexpr int kTile = kScanThreads * kScanItems;
+
+// The kScanItems counts of one thread starting at bucket `base` (a multiple of kScanItems, so
+// the vector loads are 16-byte aligned); buckets at or past nb read as zero.
+__device__ __forceinline__ void load_counts(const int *__restrict__ count, long base, long nb, int *v) {
+  if (base + kScanItems <= nb) {
+    const int4 *q = reinterpret_cast<const int4 *>(count + base);
+#pragma unroll
+    for (int i = 0; i < kScanItems / 4; i++) {
+      const int4 x = q[i];
+      v[4 * i] = x.x; v[4 * i + 1] = x.y; v[4 * i + 2] = x.z; v[4 * i + 3] = x.w;
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < kScanItems; i++) v[i] = base + i < nb ? count[base + i] : 0;
+  }
+}
 
 __device__ __forceinline__ int warp_incl_scan(int v) {
   const int lane = threadIdx.x & 31;
@@ -55,11 +71,16 @@ __global__ void k_scan_partials(const int *__restrict__ count, int *block_sums, 
                                 long n) {
   const long nb = n_buckets(d, n);
   const long base = blockIdx.x * (long)kTile + threadIdx.x * (long)kScanItems;
+  __shared__ int tot;
+  if (blockIdx.x * (long)kTile >= nb) {   // a tile past the buckets in use
+    if (threadIdx.x == 0) block_sums[blockIdx.x] = 0;
+    return;
+  }
+  int c[kScanItems];
+  load_counts(count, base, nb, c);
   int v = 0;
 #pragma unroll
-  for (int i = 0; i < kScanItems; i++)
-    if (base + i < nb) v += count[base + i];
-  __shared__ int tot;
+  for (int i = 0; i < kScanItems; i++) v += c[i];
   block_excl_scan(v, &tot);
   if (threadIdx.x == 0) block_sums[blockIdx.x] = tot;
 }
@@ -112,20 +133,29 @@ __global__ void __launch_bounds__(kTopThreads) k_scan_top(int *block_sums, long 
 __global__ void k_scan_final(const int *__restrict__ count, const int *__restrict__ block_sums,
                              int *start, const DevScalars *d, long n) {
   const long nb = n_buckets(d, n);
+  if (blockIdx.x * (long)kTile >= nb) return;   // a tile past the buckets in use
   const long base = blockIdx.x * (long)kTile + threadIdx.x * (long)kScanItems;
   int v[kScanItems];
+  load_counts(count, base, nb, v);
   int sum = 0;
 #pragma unroll
-  for (int i = 0; i < kScanItems; i++) {
-    v[i] = base + i < nb ? count[base + i] : 0;
-    sum += v[i];
-  }
+  for (int i = 0; i < kScanItems; i++) sum += v[i];
   __shared__ int tot;
   int e = block_excl_scan(sum, &tot) + block_sums[blockIdx.x];
+  int o[kScanItems];
 #pragma unroll
   for (int i = 0; i < kScanItems; i++) {
-    if (base + i < nb) start[base + i] = e;
+    o[i] = e;
     e += v[i];
+  }
+  if (base + kScanItems <= nb) {
+    int4 *q = reinterpret_cast<int4 *>(start + base);
+#pragma unroll
+    for (int i = 0; i < kScanItems / 4; i++) q[i] = make_int4(o[4 * i], o[4 * i + 1], o[4 * i + 2], o[4 * i + 3]);
+  } else {
+#pragma unroll
+    for (int i = 0; i < kScanItems; i++)
+      if (base + i < nb) start[base + i] = o[i];
   }
 }
 
