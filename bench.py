@@ -397,33 +397,41 @@ def run_engine(args):
     stream = torch.cuda.current_stream()
     from avalancheflume3d_gb300 import FP_EXACT, FP_FAST
     modes = {"exact": FP_EXACT, "fast": FP_FAST}
-    eng = Engine(sys_, fun, stream=stream.cuda_stream, fp_mode=modes[args.fp_mode])
-    eng.import_particles(pp)
-    eng.forces()          # start-up force pass into a_i (avalanche_hst.cu:366-384)
-    eng.swap_accel()
-    # Clocks are sampled every 200 ms from the start of the pre-roll through an untimed load
-    # window (--clock-window) to the end of the timed region, all under load: the timed window
-    # alone is shorter than one sampling period.
+    def make_engine(trace_preroll=False):
+        """A context at the timed run's starting state: the input, the start-up force pass into
+        a_i (avalanche_hst.cu:366-384) and the pre-roll."""
+        e = Engine(sys_, fun, stream=stream.cuda_stream, fp_mode=modes[args.fp_mode])
+        e.import_particles(pp)
+        e.forces()
+        e.swap_accel()
+        if args.preroll:
+            if trace_preroll and args.trace_contacts:
+                trace = []
+                e.contact_count()
+                done = 0
+                while done < args.preroll:
+                    k = min(args.trace_contacts, args.preroll - done)
+                    e.step(k)
+                    done += k
+                    trace.append((done, e.contact_count() / k))
+                if rank == 0:
+                    print("contacts per step during the pre-roll:", trace, file=sys.stderr, flush=True)
+            else:
+                e.step(args.preroll)
+        return e
+
+    # Clocks are sampled every 200 ms from the start of an untimed load window (--clock-window)
+    # to the end of the timed region, all under load: the timed window alone is shorter than one
+    # sampling period.  The load window runs on its own context, so the timed steps start from
+    # the same state whatever the speed of the code.
     clocks = ClockSampler(local)
-    trace = []
-    if args.preroll:
-        if args.trace_contacts:
-            eng.contact_count()
-            done = 0
-            while done < args.preroll:
-                k = min(args.trace_contacts, args.preroll - done)
-                eng.step(k)
-                done += k
-                trace.append((done, eng.contact_count() / k))
-            if rank == 0:
-                print("contacts per step during the pre-roll:", trace, file=sys.stderr, flush=True)
-        else:
-            eng.step(args.preroll)
     if args.clock_window > 0:
-        t_end = time.perf_counter() + args.clock_window
-        while time.perf_counter() < t_end:
-            eng.step(64)
-            torch.cuda.synchronize()
+        with make_engine() as warm:
+            t_end = time.perf_counter() + args.clock_window
+            while time.perf_counter() < t_end:
+                warm.step(64)
+                torch.cuda.synchronize()
+    eng = make_engine(trace_preroll=True)
     eng.step(args.warmup)
     grid = eng.get_grid()
     ncell3 = int(grid["ncell3"])
