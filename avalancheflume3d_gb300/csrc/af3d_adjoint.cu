@@ -490,7 +490,10 @@ __device__ __forceinline__ void shared_add3(double *p, V3 v) {
 // alpha_i; acc receives (atomically) the adjoints of every clump's r1, v1, w1 and spheres;
 // rb receives this clump's own R1 adjoint.  The contacts run warp-cooperatively: the item lists
 // of the forward pass, 32 items a round, each lane reversing one contact for its owner.
-__global__ void __launch_bounds__(kAdjCoopBlock) k_adj_forces(Planes P, Planes in, Planes out, Planes acc,
+#ifndef AF3D_ADJ_MINB
+#define AF3D_ADJ_MINB 1
+#endif
+__global__ void __launch_bounds__(kAdjCoopBlock, AF3D_ADJ_MINB) k_adj_forces(Planes P, Planes in, Planes out, Planes acc,
                                                               Planes rb, DevScalars *d, const int *__restrict__ flume,
                                                               const NbrRec *__restrict__ nbr,
                                                               const CullRec *__restrict__ cull,
