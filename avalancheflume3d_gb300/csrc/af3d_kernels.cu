@@ -201,14 +201,136 @@ __device__ __forceinline__ long bin_axis(double x, double xmin, double inv, long
   return i;
 }
 
+constexpr double kSmallAngle2 = 9.765625e-04;   // (2^-5)^2
+
+// init_Verlet.cu:25-148 for one clump that is not removed: r, v, w and the rotation rows move
+// one step with a_i, alpha_i; sp receives the new sphere centres.
+__device__ __forceinline__ void predict_state(V3 &r, V3 &v, V3 &w, V3 a, V3 al, V3 &Rx, V3 &Ry, V3 &Rz, V3 *sp,
+                                              double rad, double dt, double hdt) {
+  r.x += dt * (v.x + hdt * a.x);
+  r.y += dt * (v.y + hdt * a.y);
+  r.z += dt * (v.z + hdt * a.z);
+  v.x += dt * a.x;
+  v.y += dt * a.y;
+  v.z += dt * a.z;
+  V3 dO = mk(dt * (w.x + hdt * al.x), dt * (w.y + hdt * al.y), dt * (w.z + hdt * al.z));
+  const double mag2 = dO.x * dO.x + dO.y * dO.y + dO.z * dO.z;
+  double mag, imag = 0.0;
+  V3 dRx, dRy, dRz;
+  if (kFast && mag2 > 0.0 && mag2 < kSmallAngle2) {
+    // Fast mode, |dO| < 2^-5: the Rodrigues matrix c I + (sin/|dO|) [dO]x + ((1-c)/|dO|^2) dO dO^T
+    // from the Maclaurin series of sin(t)/t and (1 - cos t)/t^2 in t^2 = |dO|^2 (truncated
+    // after t^8 and t^10: the first omitted terms are below 2^-53 of the sums), no square
+    // root, sine or cosine.
+    const double t2 = mag2;
+    const double A = 1.0 - t2 * (1.0 / 6.0) * (1.0 - t2 * (1.0 / 20.0) * (1.0 - t2 * (1.0 / 42.0) *
+                                                                            (1.0 - t2 * (1.0 / 72.0))));
+    const double Bq = 0.5 * (1.0 - t2 * (1.0 / 12.0) * (1.0 - t2 * (1.0 / 30.0) * (1.0 - t2 * (1.0 / 56.0) *
+                                                                                    (1.0 - t2 * (1.0 / 90.0)))));
+    const double cc = 1.0 - t2 * Bq;
+    const V3 sv = mk(A * dO.x, A * dO.y, A * dO.z);
+    const V3 bv = mk(Bq * dO.x, Bq * dO.y, Bq * dO.z);
+    dRx = mk(bv.x * dO.x + cc, bv.x * dO.y - sv.z, bv.x * dO.z + sv.y);
+    dRy = mk(bv.y * dO.x + sv.z, bv.y * dO.y + cc, bv.y * dO.z - sv.x);
+    dRz = mk(bv.z * dO.x - sv.y, bv.z * dO.y + sv.x, bv.z * dO.z + cc);
+  } else {
+    if (kFast) {
+      imag = rsqrt(mag2);
+      mag = mag2 * imag;
+    } else {
+      mag = sqrt(mag2);
+    }
+    if (mag > 0.0) {
+      // Rodrigues rotation about dO/|dO| by |dO| (init_Verlet.cu:63-83)
+      V3 u;
+      double c, sn;
+      if (kFast) {
+        u = mk(dO.x * imag, dO.y * imag, dO.z * imag);
+        sincos(mag, &sn, &c);
+      } else {
+        u = mk(dO.x / mag, dO.y / mag, dO.z / mag);
+        c = cos(mag);
+        sn = sin(mag);
+      }
+      const double omc = 1.0 - c;
+      dRx = mk(omc * u.x * u.x + c, omc * u.x * u.y - sn * u.z, omc * u.x * u.z + sn * u.y);
+      dRy = mk(omc * u.y * u.x + sn * u.z, omc * u.y * u.y + c, omc * u.y * u.z - sn * u.x);
+      dRz = mk(omc * u.z * u.x - sn * u.y, omc * u.z * u.y + sn * u.x, omc * u.z * u.z + c);
+    } else {
+      dRx = mk(1.0, 0.0, 0.0);
+      dRy = mk(0.0, 1.0, 0.0);
+      dRz = mk(0.0, 0.0, 1.0);
+    }
+  }
+  // R <- dR R (rows), then each column renormalised (init_Verlet.cu:92-114)
+  V3 Tx = mk(dRx.x * Rx.x + dRx.y * Ry.x + dRx.z * Rz.x, dRx.x * Rx.y + dRx.y * Ry.y + dRx.z * Rz.y,
+             dRx.x * Rx.z + dRx.y * Ry.z + dRx.z * Rz.z);
+  V3 Ty = mk(dRy.x * Rx.x + dRy.y * Ry.x + dRy.z * Rz.x, dRy.x * Rx.y + dRy.y * Ry.y + dRy.z * Rz.y,
+             dRy.x * Rx.z + dRy.y * Ry.z + dRy.z * Rz.z);
+  V3 Tz = mk(dRz.x * Rx.x + dRz.y * Ry.x + dRz.z * Rz.x, dRz.x * Rx.y + dRz.y * Ry.y + dRz.z * Rz.y,
+             dRz.x * Rx.z + dRz.y * Ry.z + dRz.z * Rz.z);
+  if (kFast) {
+    // 1/sqrt(n2) for a column norm n2 within 2^-26 of 1 (a rotation times a rotation):
+    // one Newton step from 1, 1.5 - n2/2, whose error 3/8 (n2 - 1)^2 is below 2^-54.
+    auto inv_norm = [](double n2) { return fabs(n2 - 1.0) < 1.4901161193847656e-08 ? 1.5 - 0.5 * n2 : rsqrt(n2); };
+    double in = inv_norm(Tx.x * Tx.x + Ty.x * Ty.x + Tz.x * Tz.x);
+    Rx.x = Tx.x * in; Ry.x = Ty.x * in; Rz.x = Tz.x * in;
+    in = inv_norm(Tx.y * Tx.y + Ty.y * Ty.y + Tz.y * Tz.y);
+    Rx.y = Tx.y * in; Ry.y = Ty.y * in; Rz.y = Tz.y * in;
+    in = inv_norm(Tx.z * Tx.z + Ty.z * Ty.z + Tz.z * Tz.z);
+    Rx.z = Tx.z * in; Ry.z = Ty.z * in; Rz.z = Tz.z * in;
+  } else {
+    double nrm = sqrt(Tx.x * Tx.x + Ty.x * Ty.x + Tz.x * Tz.x);
+    Rx.x = Tx.x / nrm; Ry.x = Ty.x / nrm; Rz.x = Tz.x / nrm;
+    nrm = sqrt(Tx.y * Tx.y + Ty.y * Ty.y + Tz.y * Tz.y);
+    Rx.y = Tx.y / nrm; Ry.y = Ty.y / nrm; Rz.y = Tz.y / nrm;
+    nrm = sqrt(Tx.z * Tx.z + Ty.z * Ty.z + Tz.z * Tz.z);
+    Rx.z = Tx.z / nrm; Ry.z = Ty.z / nrm; Rz.z = Tz.z / nrm;
+  }
+  w.x += dt * al.x;
+  w.y += dt * al.y;
+  w.z += dt * al.z;
+  // sphere centres r + (radius/sqrt2) R (+-1,+-1,+-1) (init_Verlet.cu:130-142)
+  const double pos = kFast ? rad * (1.0 / kROOT2) : rad / kROOT2;
+  sp[0] = mk(r.x + pos * (Rx.x + Rx.y + Rx.z), r.y + pos * (Ry.x + Ry.y + Ry.z), r.z + pos * (Rz.x + Rz.y + Rz.z));
+  sp[1] = mk(r.x + pos * (Rx.x - Rx.y - Rx.z), r.y + pos * (Ry.x - Ry.y - Ry.z), r.z + pos * (Rz.x - Rz.y - Rz.z));
+  sp[2] = mk(r.x + pos * (-Rx.x - Rx.y + Rx.z), r.y + pos * (-Ry.x - Ry.y + Ry.z),
+             r.z + pos * (-Rz.x - Rz.y + Rz.z));
+  sp[3] = mk(r.x + pos * (-Rx.x + Rx.y - Rx.z), r.y + pos * (-Ry.x + Ry.y - Ry.z),
+             r.z + pos * (-Rz.x + Rz.y - Rz.z));
+}
+
+// cell_locate's bucket of a clump at r (cells.cu:60-92) at time t: the flume's cell offset + cell
+// index, or ncell_total + id for a clump that is not binned (removed, or non-finite).
+__device__ __forceinline__ long bucket_key(V3 r, const DevFlume &fl, DevScalars *d, long long id, double t) {
+  const af3d_cell_par &g = fl.grid;
+  if (is_removed(t, r.x, fl.sys.side.x)) return d->ncell_total + id;
+  if (!(isfinite(r.x) && isfinite(r.y) && isfinite(r.z))) {
+    raise_status(d, AF3D_ERR_NAN);
+    return d->ncell_total + id;
+  }
+  long i = bin_axis(r.x, g.rr_min.x, g.cs_inv.x, g.ncell.x);
+  long j = bin_axis(r.y, g.rr_min.y, g.cs_inv.y, g.ncell.y);
+  long k = bin_axis(r.z, g.rr_min.z, g.cs_inv.z, g.ncell.z);
+  if (i < 0 || j < 0 || k < 0) {
+    raise_status(d, AF3D_ERR_NEGATIVE_CELL);
+    i = i < 0 ? 0 : i; j = j < 0 ? 0 : j; k = k < 0 ? 0 : k;
+  }
+  if (i >= g.ncell.x || j >= g.ncell.y || k >= g.ncell.z) {
+    raise_status(d, AF3D_ERR_GRID_ESCAPE);
+    i = i < g.ncell.x ? i : g.ncell.x - 1;
+    j = j < g.ncell.y ? j : g.ncell.y - 1;
+    k = k < g.ncell.z ? k : g.ncell.z - 1;
+  }
+  return fl.cell_off + i + g.ncell.x * (j + k * g.ncell.y);
+}
+
 // init_Verlet.cu:25-148 for one clump (PREDICT), and/or cell_locate's binning (cells.cu:60-92)
 // with the current time (KEYS): the bucket key, the bucket count and the clump's arrival rank.
 // Clumps that are not binned (removed, or non-finite) get the unique bucket ncell_total + id, so every
 // bucket holds its clumps in id order after the rank pass.  `t_prev`: init_Verlet's removal test
 // uses the time before the advance (the fused step advances time first).  RECORDS: also write
 // the clump's neighbour records at its own slot (steps that keep the slot order).
-constexpr double kSmallAngle2 = 9.765625e-04;   // (2^-5)^2
-
 template <bool PREDICT, bool KEYS, bool RECORDS>
 __global__ void __launch_bounds__(kBlock) k_predict(Planes P, DevScalars *d, bool t_prev, Cells cells,
                                                     const long long *__restrict__ id,
@@ -224,119 +346,25 @@ __global__ void __launch_bounds__(kBlock) k_predict(Planes P, DevScalars *d, boo
   CullRec cr;
   if (valid) {
     const DevFlume &fl = d->flumes[flume[s]];
-    const double side_x = fl.sys.side.x;
     V3 r = load3(P, RX, s);
     V3 v, w, sp[4];
     bool have = false;   // v, w, sp hold the clump's current values
     if (PREDICT) {
-      const double dt = fl.sys.dt, hdt = fl.sys.hdt;
       const double t_init = t_prev ? d->time_prev : d->time;
-      if (is_removed(t_init, r.x, side_x)) {
+      if (is_removed(t_init, r.x, fl.sys.side.x)) {
         P.p[RAD][s] = 0.0;
       } else {
         v = load3(P, VX, s);
         w = load3(P, WX, s);
-        V3 a = load3(P, AIX, s), al = load3(P, ALIX, s);
         V3 Rx = load3(P, R00, s), Ry = load3(P, R10, s), Rz = load3(P, R20, s);
-        r.x += dt * (v.x + hdt * a.x);
-        r.y += dt * (v.y + hdt * a.y);
-        r.z += dt * (v.z + hdt * a.z);
-        v.x += dt * a.x;
-        v.y += dt * a.y;
-        v.z += dt * a.z;
-        V3 dO = mk(dt * (w.x + hdt * al.x), dt * (w.y + hdt * al.y), dt * (w.z + hdt * al.z));
-        const double mag2 = dO.x * dO.x + dO.y * dO.y + dO.z * dO.z;
-        double mag, imag = 0.0;
-        V3 dRx, dRy, dRz;
-        if (kFast && mag2 > 0.0 && mag2 < kSmallAngle2) {
-          // Fast mode, |dO| < 2^-5: the Rodrigues matrix c I + (sin/|dO|) [dO]x + ((1-c)/|dO|^2) dO dO^T
-          // from the Maclaurin series of sin(t)/t and (1 - cos t)/t^2 in t^2 = |dO|^2 (truncated
-          // after t^8 and t^10: the first omitted terms are below 2^-53 of the sums), no square
-          // root, sine or cosine.
-          const double t2 = mag2;
-          const double A = 1.0 - t2 * (1.0 / 6.0) * (1.0 - t2 * (1.0 / 20.0) * (1.0 - t2 * (1.0 / 42.0) *
-                                                                                  (1.0 - t2 * (1.0 / 72.0))));
-          const double Bq = 0.5 * (1.0 - t2 * (1.0 / 12.0) * (1.0 - t2 * (1.0 / 30.0) * (1.0 - t2 * (1.0 / 56.0) *
-                                                                                          (1.0 - t2 * (1.0 / 90.0)))));
-          const double cc = 1.0 - t2 * Bq;
-          const V3 sv = mk(A * dO.x, A * dO.y, A * dO.z);
-          const V3 bv = mk(Bq * dO.x, Bq * dO.y, Bq * dO.z);
-          dRx = mk(bv.x * dO.x + cc, bv.x * dO.y - sv.z, bv.x * dO.z + sv.y);
-          dRy = mk(bv.y * dO.x + sv.z, bv.y * dO.y + cc, bv.y * dO.z - sv.x);
-          dRz = mk(bv.z * dO.x - sv.y, bv.z * dO.y + sv.x, bv.z * dO.z + cc);
-        } else {
-        if (kFast) {
-          imag = rsqrt(mag2);
-          mag = mag2 * imag;
-        } else {
-          mag = sqrt(mag2);
-        }
-        if (mag > 0.0) {
-          // Rodrigues rotation about dO/|dO| by |dO| (init_Verlet.cu:63-83)
-          V3 u;
-          double c, sn;
-          if (kFast) {
-            u = mk(dO.x * imag, dO.y * imag, dO.z * imag);
-            sincos(mag, &sn, &c);
-          } else {
-            u = mk(dO.x / mag, dO.y / mag, dO.z / mag);
-            c = cos(mag);
-            sn = sin(mag);
-          }
-          const double omc = 1.0 - c;
-          dRx = mk(omc * u.x * u.x + c, omc * u.x * u.y - sn * u.z, omc * u.x * u.z + sn * u.y);
-          dRy = mk(omc * u.y * u.x + sn * u.z, omc * u.y * u.y + c, omc * u.y * u.z - sn * u.x);
-          dRz = mk(omc * u.z * u.x - sn * u.y, omc * u.z * u.y + sn * u.x, omc * u.z * u.z + c);
-        } else {
-          dRx = mk(1.0, 0.0, 0.0);
-          dRy = mk(0.0, 1.0, 0.0);
-          dRz = mk(0.0, 0.0, 1.0);
-        }
-        }
-        // R <- dR R (rows), then each column renormalised (init_Verlet.cu:92-114)
-        V3 Tx = mk(dRx.x * Rx.x + dRx.y * Ry.x + dRx.z * Rz.x, dRx.x * Rx.y + dRx.y * Ry.y + dRx.z * Rz.y,
-                   dRx.x * Rx.z + dRx.y * Ry.z + dRx.z * Rz.z);
-        V3 Ty = mk(dRy.x * Rx.x + dRy.y * Ry.x + dRy.z * Rz.x, dRy.x * Rx.y + dRy.y * Ry.y + dRy.z * Rz.y,
-                   dRy.x * Rx.z + dRy.y * Ry.z + dRy.z * Rz.z);
-        V3 Tz = mk(dRz.x * Rx.x + dRz.y * Ry.x + dRz.z * Rz.x, dRz.x * Rx.y + dRz.y * Ry.y + dRz.z * Rz.y,
-                   dRz.x * Rx.z + dRz.y * Ry.z + dRz.z * Rz.z);
-        if (kFast) {
-          // 1/sqrt(n2) for a column norm n2 within 2^-26 of 1 (a rotation times a rotation):
-          // one Newton step from 1, 1.5 - n2/2, whose error 3/8 (n2 - 1)^2 is below 2^-54.
-          auto inv_norm = [](double n2) { return fabs(n2 - 1.0) < 1.4901161193847656e-08 ? 1.5 - 0.5 * n2 : rsqrt(n2); };
-          double in = inv_norm(Tx.x * Tx.x + Ty.x * Ty.x + Tz.x * Tz.x);
-          Rx.x = Tx.x * in; Ry.x = Ty.x * in; Rz.x = Tz.x * in;
-          in = inv_norm(Tx.y * Tx.y + Ty.y * Ty.y + Tz.y * Tz.y);
-          Rx.y = Tx.y * in; Ry.y = Ty.y * in; Rz.y = Tz.y * in;
-          in = inv_norm(Tx.z * Tx.z + Ty.z * Ty.z + Tz.z * Tz.z);
-          Rx.z = Tx.z * in; Ry.z = Ty.z * in; Rz.z = Tz.z * in;
-        } else {
-          double nrm = sqrt(Tx.x * Tx.x + Ty.x * Ty.x + Tz.x * Tz.x);
-          Rx.x = Tx.x / nrm; Ry.x = Ty.x / nrm; Rz.x = Tz.x / nrm;
-          nrm = sqrt(Tx.y * Tx.y + Ty.y * Ty.y + Tz.y * Tz.y);
-          Rx.y = Tx.y / nrm; Ry.y = Ty.y / nrm; Rz.y = Tz.y / nrm;
-          nrm = sqrt(Tx.z * Tx.z + Ty.z * Ty.z + Tz.z * Tz.z);
-          Rx.z = Tx.z / nrm; Ry.z = Ty.z / nrm; Rz.z = Tz.z / nrm;
-        }
-        w.x += dt * al.x;
-        w.y += dt * al.y;
-        w.z += dt * al.z;
+        predict_state(r, v, w, load3(P, AIX, s), load3(P, ALIX, s), Rx, Ry, Rz, sp, P.p[RAD][s], fl.sys.dt,
+                      fl.sys.hdt);
         store3(P, RX, s, r);
         store3(P, VX, s, v);
         store3(P, WX, s, w);
         store3(P, R00, s, Rx);
         store3(P, R10, s, Ry);
         store3(P, R20, s, Rz);
-        // sphere centres r + (radius/sqrt2) R (+-1,+-1,+-1) (init_Verlet.cu:130-142)
-        const double pos = kFast ? P.p[RAD][s] * (1.0 / kROOT2) : P.p[RAD][s] / kROOT2;
-        sp[0] = mk(r.x + pos * (Rx.x + Rx.y + Rx.z), r.y + pos * (Ry.x + Ry.y + Ry.z),
-                   r.z + pos * (Rz.x + Rz.y + Rz.z));
-        sp[1] = mk(r.x + pos * (Rx.x - Rx.y - Rx.z), r.y + pos * (Ry.x - Ry.y - Ry.z),
-                   r.z + pos * (Rz.x - Rz.y - Rz.z));
-        sp[2] = mk(r.x + pos * (-Rx.x - Rx.y + Rx.z), r.y + pos * (-Ry.x - Ry.y + Ry.z),
-                   r.z + pos * (-Rz.x - Rz.y + Rz.z));
-        sp[3] = mk(r.x + pos * (-Rx.x + Rx.y - Rx.z), r.y + pos * (-Ry.x + Ry.y - Ry.z),
-                   r.z + pos * (-Rz.x + Rz.y - Rz.z));
         for (int k = 0; k < 4; k++) store3(P, S0X + 3 * k, s, sp[k]);
         have = true;
       }
@@ -350,29 +378,7 @@ __global__ void __launch_bounds__(kBlock) k_predict(Planes P, DevScalars *d, boo
       make_records(r, v, w, sp, P.p[RAD][s], P.p[MSPH][s], P.p[MWALL][s], q, cr);
     }
     if (KEYS) {
-      const af3d_cell_par &g = fl.grid;
-      long key;
-      if (is_removed(d->time, r.x, side_x)) {
-        key = d->ncell_total + id[s];
-      } else if (!(isfinite(r.x) && isfinite(r.y) && isfinite(r.z))) {
-        raise_status(d, AF3D_ERR_NAN);
-        key = d->ncell_total + id[s];
-      } else {
-        long i = bin_axis(r.x, g.rr_min.x, g.cs_inv.x, g.ncell.x);
-        long j = bin_axis(r.y, g.rr_min.y, g.cs_inv.y, g.ncell.y);
-        long k = bin_axis(r.z, g.rr_min.z, g.cs_inv.z, g.ncell.z);
-        if (i < 0 || j < 0 || k < 0) {
-          raise_status(d, AF3D_ERR_NEGATIVE_CELL);
-          i = i < 0 ? 0 : i; j = j < 0 ? 0 : j; k = k < 0 ? 0 : k;
-        }
-        if (i >= g.ncell.x || j >= g.ncell.y || k >= g.ncell.z) {
-          raise_status(d, AF3D_ERR_GRID_ESCAPE);
-          i = i < g.ncell.x ? i : g.ncell.x - 1;
-          j = j < g.ncell.y ? j : g.ncell.y - 1;
-          k = k < g.ncell.z ? k : g.ncell.z - 1;
-        }
-        key = fl.cell_off + i + g.ncell.x * (j + k * g.ncell.y);
-      }
+      const long key = bucket_key(r, fl, d, id[s], d->time);
       cells.key[s] = (int)key;
       cells.rank_tmp[s] = atomicAdd(&cells.count[key], 1);
     }
