@@ -55,12 +55,16 @@ struct PtrState {
   Planes cur, alt;
   long long *id_cur, *id_alt;
   int *fl_cur, *fl_alt;
+  NbrRec *nbr, *nbr_next;
+  CullRec *cull, *cull_next;
+  bool look;
 };
 
 struct StepGraph {
   PtrState start{}, end{};      // before and after the captured steps
   long steps = 0;
   bool resort_first = false;    // the first captured step permutes the planes
+  bool look_last = false;       // the last captured force pass looks ahead
   cudaGraphExec_t exec = nullptr;
 };
 
@@ -92,6 +96,12 @@ struct af3d_ctx {
   int *flume_of_id = nullptr;                  // flume of every clump id
   NbrRec *nbr = nullptr;
   CullRec *cull = nullptr;
+  NbrRec *nbr_next = nullptr;     // the look-ahead's records of the next step
+  CullRec *cull_next = nullptr;
+  // The previous force pass ran this step's predictor (look-ahead): the step's predicted state is
+  // in nbr/cull (records), the RN planes (rotation rows) and the cell keys; the planes still hold
+  // the last step's corrected state.
+  bool look = false;
   ContactLists lists{};   // the item lists of the current force pass
   Cells cells{};
   DevScalars *d = nullptr;
@@ -128,18 +138,23 @@ bool same_planes(const Planes &a, const Planes &b) {
 }
 
 PtrState ptr_state(const af3d_ctx *c) {
-  return PtrState{c->cur, c->alt, c->id_cur, c->id_alt, c->fl_cur, c->fl_alt};
+  return PtrState{c->cur, c->alt, c->id_cur, c->id_alt, c->fl_cur, c->fl_alt, c->nbr, c->nbr_next, c->cull,
+                  c->cull_next, c->look};
 }
 
 void set_ptr_state(af3d_ctx *c, const PtrState &p) {
   c->cur = p.cur; c->alt = p.alt;
   c->id_cur = p.id_cur; c->id_alt = p.id_alt;
   c->fl_cur = p.fl_cur; c->fl_alt = p.fl_alt;
+  c->nbr = p.nbr; c->nbr_next = p.nbr_next;
+  c->cull = p.cull; c->cull_next = p.cull_next;
+  c->look = p.look;
 }
 
 bool same_state(const PtrState &a, const PtrState &b) {
   return same_planes(a.cur, b.cur) && same_planes(a.alt, b.alt) && a.id_cur == b.id_cur &&
-         a.id_alt == b.id_alt && a.fl_cur == b.fl_cur && a.fl_alt == b.fl_alt;
+         a.id_alt == b.id_alt && a.fl_cur == b.fl_cur && a.fl_alt == b.fl_alt && a.nbr == b.nbr &&
+         a.nbr_next == b.nbr_next && a.cull == b.cull && a.cull_next == b.cull_next && a.look == b.look;
 }
 
 void drop_graphs(af3d_ctx *c) {
@@ -263,7 +278,7 @@ void predict_for(af3d_ctx *c, bool predict, bool keys, bool t_prev, bool records
 // A single-flume context passes its constants as a kernel parameter (from the host mirrors,
 // which push_params keeps equal to the device table; captured graphs are dropped whenever they
 // change).
-void forces_for(af3d_ctx *c, bool write_ft, const int *order, Planes out) {
+void forces_for(af3d_ctx *c, bool write_ft, const int *order, Planes out, bool warm = false, bool look = false) {
   const float4 *csort = order ? c->cells.csort : nullptr;
   Consts kc;
   const Consts *uni = nullptr;
@@ -271,12 +286,14 @@ void forces_for(af3d_ctx *c, bool write_ft, const int *order, Planes out) {
     kc = make_consts(c->sys[0], c->fun[0], c->sys[0].sint / c->sys[0].cost, c->phase, c->variant, &c->d->time);
     uni = &kc;
   }
+  LookAhead la{};
+  if (look) la = LookAhead{c->nbr_next, c->cull_next, c->cells, c->id_cur};
   if (c->fp_mode == AF3D_FP_FAST)
     fast::launch_lists_forces(c->L(), c->cur, out, c->d, c->fl_cur, c->nbr, c->cull, c->cells.start, order, csort,
-                              c->lists, write_ft, uni);
+                              c->lists, write_ft, uni, warm, la);
   else
     launch_lists_forces(c->L(), c->cur, out, c->d, c->fl_cur, c->nbr, c->cull, c->cells.start, order, csort,
-                        c->lists, write_ft, uni);
+                        c->lists, write_ft, uni, warm, la);
 }
 
 void enqueue_cell_build(af3d_ctx *c, bool predict, bool t_prev, bool ft = true) {
@@ -295,38 +312,63 @@ void enqueue_cell_build(af3d_ctx *c, bool predict, bool t_prev, bool ft = true) 
 // finish_Verlet, and the acceleration swap.  With `resort` the planes are permuted into the new
 // (cell, id) order; otherwise the predictor writes the records at the clumps' own slots, the
 // force pass reaches the sorted order through cells.perm and corrects the velocities in place.
-void enqueue_fused_step(af3d_ctx *c, bool resort, bool write_ft = false) {
+// When the previous pass looked ahead (c->look), this step's predictor has already run and the
+// step is the sort and the force pass.  `look`: this step's force pass runs the next step's
+// predictor.
+void enqueue_fused_step(af3d_ctx *c, bool resort, bool write_ft = false, bool look = false) {
   launch_advance_time(c->st, c->d);
+  const bool warm = !resort && c->look;
   if (resort) {
     enqueue_cell_build(c, true, true, false);   // F, T and a_f are rewritten before being read
-    forces_for(c, write_ft, nullptr, c->alt);
+    forces_for(c, write_ft, nullptr, c->alt, false, look);
     swap_velocity_planes(c->cur, c->alt);
   } else {
-    predict_for(c, true, true, true, true);
+    if (!warm) predict_for(c, true, true, true, true);
     launch_sort(c->L(), c->d, c->cells, c->id_cur, c->ntags, c->cull);
-    forces_for(c, write_ft, c->cells.perm, c->cur);
+    forces_for(c, write_ft, c->cells.perm, c->cur, warm, look);
   }
+  if (look) {
+    std::swap(c->nbr, c->nbr_next);
+    std::swap(c->cull, c->cull_next);
+  }
+  c->look = look;
   swap_accel_planes(c->cur);
   swap_accel_planes(c->alt);
   c->sorted = resort;
 }
 
-long kernels_of(long len, bool resort_first) {
-  return len * kKernelsPerKeptStep + (resort_first ? 1 : 0);
+// Kernels of `len` fused steps, the first one permuting (resort_first) or, with look_first,
+// predicted by the previous pass; every later step is predicted by its previous pass.
+long kernels_of(long len, bool resort_first, bool look_first) {
+  const long first = resort_first ? kKernelsPerStep : (look_first ? kKernelsPerKeptStep - 1 : kKernelsPerKeptStep);
+  return first + (len - 1) * (kKernelsPerKeptStep - 1);
 }
 
 af3d_status run_steps(af3d_ctx *c, long m) {
   // Captured graphs of 64 steps (the first one permuting the planes) while at least 64 steps
   // remain, then of two steps (permuting first only when the last permutation is due); an odd
   // last step is enqueued directly.  A graph is replayed when the context is in the pointer
-  // state it was captured from, and leaves the context in the state it ended in.
+  // state it was captured from, and leaves the context in the state it ended in.  A force pass
+  // looks ahead (runs the next step's predictor) when the next step of the run keeps the slot
+  // order; a permuting step predicts from the planes itself.
+  auto resorts = [&](long since, long left) {   // does the next batch of `left` steps permute first?
+    if (left >= 2) {
+      const long l = left >= kGraphSteps ? kGraphSteps : 2;
+      return l == kGraphSteps || since + l > kResortEvery;
+    }
+    return since + 1 > kResortEvery;
+  };
   while (m >= 2) {
     const long len = m >= kGraphSteps ? kGraphSteps : 2;
     const bool resort_first = len == kGraphSteps || c->since_sort + len > kResortEvery;
+    const long since_after = resort_first ? len - 1 : c->since_sort + len;
+    const bool look_last = m > len && !resorts(since_after, m - len);
+    const bool look_first = c->look;
     const PtrState now = ptr_state(c);
     StepGraph *g = nullptr;
     for (auto &cand : c->graphs)
-      if (cand.exec && cand.steps == len && cand.resort_first == resort_first && same_state(cand.start, now))
+      if (cand.exec && cand.steps == len && cand.resort_first == resort_first && cand.look_last == look_last &&
+          same_state(cand.start, now))
         g = &cand;
     if (!g) {
       g = &c->graphs[c->graph_next];
@@ -336,9 +378,10 @@ af3d_status run_steps(af3d_ctx *c, long m) {
       g->start = now;
       g->steps = len;
       g->resort_first = resort_first;
+      g->look_last = look_last;
       cudaGraph_t graph;
       AF3D_CUDA(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
-      for (long i = 0; i < len; i++) enqueue_fused_step(c, i == 0 && resort_first);
+      for (long i = 0; i < len; i++) enqueue_fused_step(c, i == 0 && resort_first, false, i + 1 < len || look_last);
       AF3D_CUDA(cudaStreamEndCapture(c->st, &graph));
       g->end = ptr_state(c);
       set_ptr_state(c, now);
@@ -352,15 +395,16 @@ af3d_status run_steps(af3d_ctx *c, long m) {
     AF3D_CUDA(cudaGraphLaunch(g->exec, c->st));
     set_ptr_state(c, g->end);
     c->sorted = false;   // the last captured step keeps the slot order
-    c->since_sort = resort_first ? len - 1 : c->since_sort + len;
-    c->launches += kernels_of(len, resort_first);
+    c->since_sort = since_after;
+    c->launches += kernels_of(len, resort_first, look_first);
     m -= len;
   }
   if (m == 1) {
     const bool resort = c->since_sort + 1 > kResortEvery;
+    const bool look_first = c->look;
     enqueue_fused_step(c, resort);
     c->since_sort = resort ? 0 : c->since_sort + 1;
-    c->launches += kernels_of(1, resort);
+    c->launches += kernels_of(1, resort, look_first);
   }
   return AF3D_OK;
 }
@@ -475,6 +519,8 @@ af3d_status af3d_create_ensemble(int nflumes, const af3d_system_par *sys, const 
   ok = ok && cudaMalloc((void **)&c->flume_of_id, sizeof(int) * n) == cudaSuccess;
   ok = ok && cudaMalloc((void **)&c->nbr, sizeof(NbrRec) * n) == cudaSuccess;
   ok = ok && cudaMalloc((void **)&c->cull, sizeof(CullRec) * n) == cudaSuccess;
+  ok = ok && cudaMalloc((void **)&c->nbr_next, sizeof(NbrRec) * n) == cudaSuccess;
+  ok = ok && cudaMalloc((void **)&c->cull_next, sizeof(CullRec) * n) == cudaSuccess;
   ok = ok && cudaMalloc((void **)&c->lists.items, sizeof(unsigned) * kListCap * n) == cudaSuccess;
   ok = ok && cudaMalloc((void **)&c->cells.key, sizeof(int) * n) == cudaSuccess;
   ok = ok && cudaMalloc((void **)&c->cells.rank_tmp, sizeof(int) * n) == cudaSuccess;
@@ -538,7 +584,7 @@ af3d_status af3d_destroy(af3d_ctx *c) {
   drop_graphs(c);
   for (void *p : {(void *)c->plane_mem[0], (void *)c->plane_mem[1], (void *)c->id_cur, (void *)c->id_alt,
                   (void *)c->fl_cur, (void *)c->fl_alt, (void *)c->flume_of_id, (void *)c->nbr,
-                  (void *)c->cull, (void *)c->lists.items, (void *)c->cells.key, (void *)c->cells.rank_tmp, (void *)c->cells.tmp_slot,
+                  (void *)c->cull, (void *)c->lists.items, (void *)c->nbr_next, (void *)c->cull_next, (void *)c->cells.key, (void *)c->cells.rank_tmp, (void *)c->cells.tmp_slot,
                   (void *)c->cells.perm, (void *)c->cells.csort, (void *)c->cells.count, (void *)c->cells.start,
                   (void *)c->cells.block_sums, (void *)c->d, (void *)c->flumes, (void *)c->d_aos,
                   (void *)c->d_acc, (void *)c->d_anga, (void *)c->d_tmp, (void *)c->d_count})
@@ -856,12 +902,16 @@ af3d_status af3d_step_profile(af3d_ctx *c, long k, double *ms) {
   cudaEvent_t ev[AF3D_NPROF + 1];
   for (auto &e : ev) AF3D_CUDA(cudaEventCreate(&e));
   for (long i = 0; i < k; i++) {
-    // The steps af3d_step runs, one at a time (the planes are permuted when that is due).
+    // The steps af3d_step runs, one at a time (the planes are permuted when that is due; a pass
+    // looks ahead when the next step keeps the slot order and no re-grid comes between).
     const bool resort = c->since_sort + 1 > kResortEvery;
+    const bool warm = !resort && c->look;
+    const bool regrid_after = c->cc % kRegridEvery == 0;
+    const bool look = i + 1 < k && !regrid_after && !((resort ? 0 : c->since_sort + 1) + 1 > kResortEvery);
     AF3D_CUDA(cudaEventRecord(ev[0], c->st));
     launch_advance_time(c->st, c->d);
     AF3D_CUDA(cudaEventRecord(ev[1], c->st));
-    predict_for(c, true, true, true, !resort);
+    if (!warm) predict_for(c, true, true, true, !resort);
     AF3D_CUDA(cudaEventRecord(ev[2], c->st));
     launch_sort(c->L(), c->d, c->cells, c->id_cur, c->ntags, resort ? nullptr : c->cull);
     AF3D_CUDA(cudaEventRecord(ev[3], c->st));
@@ -874,17 +924,22 @@ af3d_status af3d_step_profile(af3d_ctx *c, long k, double *ms) {
     }
     AF3D_CUDA(cudaEventRecord(ev[4], c->st));
     if (resort) {
-      forces_for(c, false, nullptr, c->alt);
+      forces_for(c, false, nullptr, c->alt, false, look);
       swap_velocity_planes(c->cur, c->alt);
     } else {
-      forces_for(c, false, c->cells.perm, c->cur);
+      forces_for(c, false, c->cells.perm, c->cur, warm, look);
     }
+    if (look) {
+      std::swap(c->nbr, c->nbr_next);
+      std::swap(c->cull, c->cull_next);
+    }
+    c->look = look;
     swap_accel_planes(c->cur);
     swap_accel_planes(c->alt);
     AF3D_CUDA(cudaEventRecord(ev[5], c->st));
     c->sorted = resort;
     c->since_sort = resort ? 0 : c->since_sort + 1;
-    c->launches += kernels_of(1, resort);
+    c->launches += kernels_of(1, resort, warm);
     c->time = c->time + c->sys[0].dt;
     const bool do_regrid = c->cc % kRegridEvery == 0;
     c->cc++;

@@ -28,6 +28,7 @@ enum Plane : int {
   MWALL,                                         // SPH_FACT*r^3*density (force_walls.cu:47 order)
   ADRAG,                                         // DRAG*r*r/mass (get_accel.cu:47 order)
   IMASS, IINER,                                  // 1/mass, 1/inertia (fast FP64 mode)
+  RN00, RN01, RN02, RN10, RN11, RN12, RN20, RN21, RN22,   // next step's rotation rows (look-ahead)
   NPLANES
 };
 
@@ -115,6 +116,16 @@ struct ContactLists {
   unsigned *items;   // [kListCap][n]
 };
 
+// The next step's predictor run at the end of a force pass (look-ahead): the corrected clump is
+// advanced at once, its records go to the next step's record buffers, its rotation rows to the
+// RN planes, its bucket key, arrival rank and bucket count to the cell list.  nbr == null: none.
+struct LookAhead {
+  NbrRec *nbr;
+  CullRec *cull;
+  Cells cells;
+  const long long *id;
+};
+
 // Scalars of one flume's system_par / Funnel used by the force routines.  A single-flume
 // context passes them to the fused force kernel as a __grid_constant__ parameter (constant-bank
 // operands, no registers held); the clock is read through `tp` (it advances on the device).
@@ -180,11 +191,14 @@ void launch_permute_records (const Launch &L, Planes src, Planes dst, const int 
 void launch_build_records (const Launch &L, Planes cur, NbrRec *nbr, CullRec *cull);
 // The force pass: each block builds its clumps' item lists, then processes them (walls, contacts,
 // bed, get_accel, finish_Verlet).  order: null when the slots are in (cell, id) order, else
-// cells.perm of the last sort, with csort the matching culling centres.
+// cells.perm of the last sort, with csort the matching culling centres.  warm: the step's
+// predicted state was made by the previous pass's look-ahead (records, RN planes) and is
+// committed to the planes here; look: this pass runs the next step's predictor.
 void launch_lists_forces (const Launch &L, Planes cur, Planes out, DevScalars *d, const int *flume,
                           const NbrRec *nbr, const CullRec *cull, const int *start, const int *order,
                           const float4 *csort, ContactLists lists, bool write_ft,
-                          const Consts *uniform = nullptr);
+                          const Consts *uniform = nullptr, bool warm = false,
+                          LookAhead look = LookAhead{});
 void launch_boundary (const Launch &L, Planes cur, DevScalars *d, const int *flume, int routine);
 void launch_part (const Launch &L, Planes cur, DevScalars *d, const int *flume, const NbrRec *nbr,
                   const CullRec *cull, const int *start, int sph_id);
@@ -236,7 +250,8 @@ void launch_predict (const Launch &L, Planes cur, DevScalars *d, bool predict, b
 void launch_lists_forces (const Launch &L, Planes cur, Planes out, DevScalars *d, const int *flume,
                           const NbrRec *nbr, const CullRec *cull, const int *start, const int *order,
                           const float4 *csort, ContactLists lists, bool write_ft,
-                          const Consts *uniform = nullptr);
+                          const Consts *uniform = nullptr, bool warm = false,
+                          LookAhead look = LookAhead{});
 }  // namespace fast
 
 }  // namespace af3d

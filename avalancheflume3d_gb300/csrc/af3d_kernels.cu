@@ -765,12 +765,25 @@ __device__ __forceinline__ int lists_body(const Consts &c, const DevScalars *d, 
   return slow ? -1 : k;
 }
 
+// Shared memory of the force kernel: the list phase, the force phase and the look-ahead's record
+// staging run one after another.
+union ForceShared {
+  PassLists pl[kBlock / 32];
+  BlockQueue bq;
+  struct {
+    double nbr[kPermBlock * kRecStride];
+    CullRec cull[kPermBlock];
+  } rec;
+};
+static_assert(kPermBlock == kBlock, "record staging covers one block");
+
 template <bool WRITE_FT, bool UNIFORM>
 __device__ __forceinline__ void fused_body(const Consts &c, Planes P, Planes out, DevScalars *d,
                                            const int *__restrict__ flume, const NbrRec *__restrict__ nbr,
                                            const CullRec *__restrict__ cull, const int *__restrict__ start,
                                            const int *__restrict__ order, ContactLists lists, int listed,
-                                           ListCounts lc, long n, BlockQueue &bq) {
+                                           ListCounts lc, long n, bool warm, const LookAhead &la,
+                                           ForceShared &sh) {
   const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
   const bool valid = s < n;
   const long sv = valid ? s : n - 1;   // in-range slot for lanes past n (nothing is written for them)
@@ -787,37 +800,81 @@ __device__ __forceinline__ void fused_body(const Consts &c, Planes P, Planes out
     for (int rt = R_HOP0; rt <= R_FCORNERS; rt++)
       if (bnd_may_touch(rt, o.r, B, c)) bnd_routine(rt, o, true, c, F, T);
   const long bbase = blockIdx.x * (long)blockDim.x;
-  const int active = block_contacts<UNIFORM>(bq, bbase, sv, valid && !removed, aval, B, o, c, g, off, d, flume, nbr,
-                                             cull, start, order, lists.items, valid ? listed : 0, lc, n, F, T);
+  const int active = block_contacts<UNIFORM>(sh.bq, bbase, sv, valid && !removed, aval, B, o, c, g, off, d, flume,
+                                             nbr, cull, start, order, lists.items, valid ? listed : 0, lc, n, F, T);
+  NbrRec q;
+  CullRec cr;
   if (valid) {
     if (WRITE_FT) {
       store3(P, FX, s, F);
       store3(P, TX, s, T);
     }
-    // this step's predicted velocities, read again from the record (not held across the contacts)
+    // this step's predicted state, read again from the record (not held across the contacts);
+    // its rotation rows from the RN planes when the previous pass predicted it
     const NbrRec &me = nbr[s];
+    const V3 r = mk(me.rx, me.ry, me.rz);
     const V3 v = mk(me.vx, me.vy, me.vz), w = mk(me.wx, me.wy, me.wz);
+    const int R0 = warm ? RN00 : R00;
+    V3 Rx = load3(P, R0, s), Ry = load3(P, R0 + 3, s), Rz = load3(P, R0 + 6, s);
+    if (warm) {   // commit the predicted state to the planes
+      store3(P, RX, s, r);
+      for (int k = 0; k < 4; k++) store3(P, S0X + 3 * k, s, mk(me.s[3 * k], me.s[3 * k + 1], me.s[3 * k + 2]));
+      store3(P, R00, s, Rx);
+      store3(P, R10, s, Ry);
+      store3(P, R20, s, Rz);
+    }
+    V3 v2, w2, a, al;
     if (!removed) {
-      V3 a, al;
-      get_accel_one(F, T, v, w, load3(P, R00, s), load3(P, R10, s), load3(P, R20, s), P.p[MASS][s],
-                    P.p[ADRAG][s], load3(P, IXX, s), a, al, P.p[IMASS][s], P.p[IINER][s]);
+      get_accel_one(F, T, v, w, Rx, Ry, Rz, P.p[MASS][s], P.p[ADRAG][s], load3(P, IXX, s), a, al, P.p[IMASS][s],
+                    P.p[IINER][s]);
       store3(P, AFX, s, a);
       store3(P, ALFX, s, al);
       const V3 ai = load3(P, AIX, s), ali = load3(P, ALIX, s);
       // finish_Verlet.cu:43-48
-      store3(out, VX, s, mk(v.x + c.hdt * (a.x - ai.x), v.y + c.hdt * (a.y - ai.y), v.z + c.hdt * (a.z - ai.z)));
-      store3(out, WX, s, mk(w.x + c.hdt * (al.x - ali.x), w.y + c.hdt * (al.y - ali.y), w.z + c.hdt * (al.z - ali.z)));
+      v2 = mk(v.x + c.hdt * (a.x - ai.x), v.y + c.hdt * (a.y - ai.y), v.z + c.hdt * (a.z - ai.z));
+      w2 = mk(w.x + c.hdt * (al.x - ali.x), w.y + c.hdt * (al.y - ali.y), w.z + c.hdt * (al.z - ali.z));
       if (!(isfinite(a.x) && isfinite(a.y) && isfinite(a.z) && isfinite(al.x) && isfinite(al.y) &&
             isfinite(al.z)))
         raise_status(d, AF3D_ERR_NAN);
     } else {
-      store3(out, VX, s, mk(0.0, 0.0, 0.0));  // finish_Verlet.cu:28-32
-      store3(out, WX, s, w);
-      store3(P, AFX, s, mk(0.0, 0.0, 0.0));   // the reference leaves stale values here
-      store3(P, ALFX, s, mk(0.0, 0.0, 0.0));
+      v2 = mk(0.0, 0.0, 0.0);                 // finish_Verlet.cu:28-32
+      w2 = w;
+      a = al = mk(0.0, 0.0, 0.0);             // the reference leaves stale values here
+      store3(P, AFX, s, a);
+      store3(P, ALFX, s, al);
+    }
+    store3(out, VX, s, v2);
+    store3(out, WX, s, w2);
+    if (la.nbr) {
+      // The next step's init_Verlet (removal test at this step's time, a_i = this a_f), cell key
+      // (at the next step's time) and records, exactly as k_predict<1,1,1> would make them
+      // after this step.
+      const DevFlume &fl = d->flumes[f];
+      const double t_next = *c.tp + d->flumes[0].sys.dt;   // k_advance_time's expression
+      V3 rn = r, vn = v2, wn = w2, sp[4];
+      if (is_removed(*c.tp, r.x, fl.sys.side.x)) {
+        P.p[RAD][s] = 0.0;
+        for (int k = 0; k < 4; k++) sp[k] = mk(me.s[3 * k], me.s[3 * k + 1], me.s[3 * k + 2]);
+        store3(P, RN00, s, Rx);
+        store3(P, RN10, s, Ry);
+        store3(P, RN20, s, Rz);
+      } else {
+        predict_state(rn, vn, wn, a, al, Rx, Ry, Rz, sp, P.p[RAD][s], fl.sys.dt, fl.sys.hdt);
+        store3(P, RN00, s, Rx);
+        store3(P, RN10, s, Ry);
+        store3(P, RN20, s, Rz);
+      }
+      make_records(rn, vn, wn, sp, P.p[RAD][s], P.p[MSPH][s], P.p[MWALL][s], q, cr);
+      const long key = bucket_key(rn, fl, d, la.id[s], t_next);
+      la.cells.key[s] = (int)key;
+      la.cells.rank_tmp[s] = atomicAdd(&la.cells.count[key], 1);
     }
   }
   warp_count(d, active);
+  if (la.nbr) {
+    __syncthreads();   // the force phase's shared memory is free again
+    store_records(valid, bbase, n, q, cr, la.nbr, la.cull, sh.rec.nbr, sh.rec.cull);
+  }
 }
 
 // One boundary routine added to the F, T planes (per-routine entry points).
@@ -1130,47 +1187,46 @@ __global__ void __launch_bounds__(kBlock, AF3D_FORCES_MINB) k_lists_forces(Plane
                                                          const int *__restrict__ start,
                                                          const int *__restrict__ order,
                                                          const float4 *__restrict__ csort, ContactLists lists,
-                                                         const __grid_constant__ Consts kc, long n) {
-  __shared__ union Shared {
-    PassLists pl[kBlock / 32];
-    BlockQueue bq;
-  } sh;
+                                                         const __grid_constant__ Consts kc, bool warm,
+                                                         const __grid_constant__ LookAhead la, long n) {
+  __shared__ ForceShared sh;
   ListCounts lc;
   if constexpr (UNIFORM) {
     const int listed = lists_body<true>(kc, d, flume, nbr, cull, start, order, csort, lists, n,
                                         sh.pl[threadIdx.x >> 5], lc);
     __syncthreads();
-    fused_body<WRITE_FT, true>(kc, P, out, d, flume, nbr, cull, start, order, lists, listed, lc, n, sh.bq);
+    fused_body<WRITE_FT, true>(kc, P, out, d, flume, nbr, cull, start, order, lists, listed, lc, n, warm, la, sh);
   } else {
     const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
     const Consts c = load_consts(d, flume[s < n ? s : n - 1]);
     const int listed = lists_body<false>(c, d, flume, nbr, cull, start, order, csort, lists, n,
                                          sh.pl[threadIdx.x >> 5], lc);
     __syncthreads();
-    fused_body<WRITE_FT, false>(c, P, out, d, flume, nbr, cull, start, order, lists, listed, lc, n, sh.bq);
+    fused_body<WRITE_FT, false>(c, P, out, d, flume, nbr, cull, start, order, lists, listed, lc, n, warm, la, sh);
   }
 }
 
 void launch_lists_forces(const Launch &L, Planes cur, Planes out, DevScalars *d, const int *flume,
                          const NbrRec *nbr, const CullRec *cull, const int *start, const int *order,
-                         const float4 *csort, ContactLists lists, bool write_ft, const Consts *uniform) {
+                         const float4 *csort, ContactLists lists, bool write_ft, const Consts *uniform, bool warm,
+                         LookAhead look) {
   if (L.n <= 0) return;
   const Consts kc = uniform ? *uniform : Consts{};
   const int g = grid_for(L.n);
   if (uniform) {
     if (write_ft)
       k_lists_forces<true, true><<<g, kBlock, 0, L.st>>>(cur, out, d, flume, nbr, cull, start, order, csort, lists, kc,
-                                                        L.n);
+                                                        warm, look, L.n);
     else
       k_lists_forces<false, true><<<g, kBlock, 0, L.st>>>(cur, out, d, flume, nbr, cull, start, order, csort, lists,
-                                                         kc, L.n);
+                                                         kc, warm, look, L.n);
   } else {
     if (write_ft)
       k_lists_forces<true, false><<<g, kBlock, 0, L.st>>>(cur, out, d, flume, nbr, cull, start, order, csort, lists,
-                                                         kc, L.n);
+                                                         kc, warm, look, L.n);
     else
       k_lists_forces<false, false><<<g, kBlock, 0, L.st>>>(cur, out, d, flume, nbr, cull, start, order, csort, lists,
-                                                          kc, L.n);
+                                                          kc, warm, look, L.n);
   }
 }
 
