@@ -19,13 +19,11 @@ namespace af3d {
 namespace {
 
 constexpr int kBlock = 128;
-// Resident blocks per SM requested for the fused force kernel (register budget 65536 / (128 x n)).
+// Resident blocks per SM requested for the force kernel (register budget 65536 / (128 x n)):
+// five (102 registers, some spilled) measured fastest in both FP64 modes on the 262,144-clump
+// bed, ahead of 3, 4, 6 and 8.
 #ifndef AF3D_FORCES_MINB
-#ifdef AF3D_FAST
-#define AF3D_FORCES_MINB 4
-#else
-#define AF3D_FORCES_MINB 3
-#endif
+#define AF3D_FORCES_MINB 5
 #endif
 
 inline unsigned grid_for(long n, int block = kBlock) {
