@@ -1238,7 +1238,7 @@ extern "C" af3d_status af3d_adjoint(af3d_ctx *c, long steps, long ckpt_every, do
   for (long k = 0; k < steps; k++) {
     if (want_grad && k % ckpt_every == 0) launch_state_copy(c->L(), c->cur, ckpt[k / ckpt_every], true);
     t_start[k] = t;
-    enqueue_fused_step(c, false);
+    enqueue_fused_step(c, false, false, k + 1 < steps);   // the last pass does not look ahead
     t = t + dt;
   }
   t_start[steps] = t;
@@ -1260,11 +1260,12 @@ extern "C" af3d_status af3d_adjoint(af3d_ctx *c, long steps, long ckpt_every, do
       const long k0 = seg * ckpt_every, k1 = std::min(steps, k0 + ckpt_every);
       // recompute the segment, keeping every step's starting state
       launch_state_copy(c->L(), c->cur, ckpt[seg], false);
+      c->look = false;   // the restored state has not been predicted
       s = set_device_time(c, t_start[k0]);
       if (s) return s;
       for (long k = k0; k < k1; k++) {
         launch_state_copy(c->L(), c->cur, tape[k - k0], true);
-        enqueue_fused_step(c, false, true);
+        enqueue_fused_step(c, false, true, k + 1 < k1);
         s = copy_torque(c, tape[k - k0], true);
         if (s) return s;
       }
