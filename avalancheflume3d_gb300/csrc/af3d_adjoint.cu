@@ -699,8 +699,9 @@ __global__ void __launch_bounds__(kAdjBlock) k_adj_predict(Planes P, Planes tape
   double dR[3][3];
   V3 u = mk(0.0, 0.0, 0.0);
   double c = 1.0, sn = 0.0, omc = 0.0;
+  const double imag = mag > 0.0 ? 1.0 / mag : 0.0;
   if (mag > 0.0) {
-    u = mk(dO.x / mag, dO.y / mag, dO.z / mag);
+    u = mk(dO.x * imag, dO.y * imag, dO.z * imag);
     c = cos(mag);
     sn = sin(mag);
     omc = 1.0 - c;
@@ -716,12 +717,17 @@ __global__ void __launch_bounds__(kAdjBlock) k_adj_predict(Planes P, Planes tape
   for (int i = 0; i < 3; i++)
     for (int j = 0; j < 3; j++) T[i][j] = dR[i][0] * R[0][j] + dR[i][1] * R[1][j] + dR[i][2] * R[2][j];
   for (int j = 0; j < 3; j++) nrm[j] = sqrt(T[0][j] * T[0][j] + T[1][j] * T[1][j] + T[2][j] * T[2][j]);
-  // column normalisation R1_ij = T_ij / n_j
+  // column normalisation R1_ij = T_ij / n_j (the derivative needs no bit-exact quotient: one
+  // reciprocal per column)
   double Tb[3][3];
   for (int j = 0; j < 3; j++) {
-    double sj = 0.0;
-    for (int i = 0; i < 3; i++) sj += R1b[i][j] * (T[i][j] / nrm[j]);
-    for (int i = 0; i < 3; i++) Tb[i][j] = (R1b[i][j] - (T[i][j] / nrm[j]) * sj) / nrm[j];
+    const double in = 1.0 / nrm[j];
+    double q[3], sj = 0.0;
+    for (int i = 0; i < 3; i++) {
+      q[i] = T[i][j] * in;
+      sj += R1b[i][j] * q[i];
+    }
+    for (int i = 0; i < 3; i++) Tb[i][j] = (R1b[i][j] - q[i] * sj) * in;
   }
   // T = dR R
   double G[3][3], Rb0[3][3];
@@ -750,7 +756,7 @@ __global__ void __launch_bounds__(kAdjBlock) k_adj_predict(Planes P, Planes tape
     ub[2] += sn * skew.z;
     const double mag_b = -sn * c_b + c * sn_b;
     const V3 u_b = mk(ub[0], ub[1], ub[2]);
-    dO_b = (1.0 / mag) * (u_b - dot(u, u_b) * u) + mag_b * u;
+    dO_b = imag * (u_b - dot(u, u_b) * u) + mag_b * u;
   } else {
     dO_b = skew;   // dR = I + [dO]x to first order
   }
@@ -816,15 +822,24 @@ __global__ void k_adj_seed(Planes P, Planes adj, DevScalars *d, const int *__res
 // The state of a step (r, v, w, R, a_i, alpha_i; with spheres also the four sphere centres)
 // between the planes and a tape slot.  The steps recompute the sphere centres from r and R; the
 // start-up force pass reads them as they are.
-__global__ void k_state_copy(Planes P, Planes tape, int to_tape, int nplanes, long n) {
+// The state planes r, v, w, R, a_i, alpha_i (consecutive in the plane order), then the sphere
+// centres (SPHERES), between the plane set and a tape slot; every load is issued before the stores.
+static_assert(RX == 0 && R22 == 17 && AIX == 18 && ALIZ == 23, "state planes 0..23 are consecutive");
+template <int NP>
+__global__ void k_state_copy(Planes P, Planes tape, int to_tape, long n) {
   const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (s >= n) return;
-  const int src[NADJ + 12] = {RX, RY, RZ, VX, VY, VZ, WX, WY, WZ, R00, R01, R02, R10, R11, R12, R20, R21, R22,
-                              AIX, AIY, AIZ, ALIX, ALIY, ALIZ, S0X, S0Y, S0Z, S1X, S1Y, S1Z, S2X, S2Y, S2Z,
-                              S3X, S3Y, S3Z};
-  for (int k = 0; k < nplanes; k++) {
-    if (to_tape) tape.p[k][s] = P.p[src[k]][s];
-    else P.p[src[k]][s] = tape.p[k][s];
+  double v[NP];
+#pragma unroll
+  for (int k = 0; k < NP; k++) {
+    const int p = k < NADJ ? k : S0X + (k - NADJ);
+    v[k] = to_tape ? P.p[p][s] : tape.p[k][s];
+  }
+#pragma unroll
+  for (int k = 0; k < NP; k++) {
+    const int p = k < NADJ ? k : S0X + (k - NADJ);
+    if (to_tape) tape.p[k][s] = v[k];
+    else P.p[p][s] = v[k];
   }
 }
 
@@ -864,7 +879,10 @@ void launch_adj_seed(const Launch &L, Planes P, Planes adj, DevScalars *d, const
 
 void launch_state_copy(const Launch &L, Planes P, Planes tape, bool to_tape, bool spheres) {
   if (L.n <= 0) return;
-  k_state_copy<<<blocks(L.n), kAdjBlock, 0, L.st>>>(P, tape, to_tape ? 1 : 0, spheres ? NADJ + 12 : NADJ, L.n);
+  if (spheres)
+    k_state_copy<NADJ + 12><<<blocks(L.n), kAdjBlock, 0, L.st>>>(P, tape, to_tape ? 1 : 0, L.n);
+  else
+    k_state_copy<NADJ><<<blocks(L.n), kAdjBlock, 0, L.st>>>(P, tape, to_tape ? 1 : 0, L.n);
 }
 
 }  // namespace af3d
