@@ -639,16 +639,22 @@ af3d_status af3d_import_particles(af3d_ctx *c, const af3d_particle *pp, const af
     if (acc) AF3D_CUDA(cudaMemcpyAsync(c->d_acc, acc, sizeof(double) * 3 * c->n, cudaMemcpyHostToDevice, c->st));
     if (anga) AF3D_CUDA(cudaMemcpyAsync(c->d_anga, anga, sizeof(double) * 3 * c->n, cudaMemcpyHostToDevice, c->st));
   }
+  // A re-import keeps the slot order of the last permutation (every clump stays in its slot),
+  // so the next step need not permute; the first import puts clump i in slot i.
+  const bool keep_order = c->imported;
   launch_aos_to_planes(c->L(), c->d_aos, acc ? c->d_acc : nullptr, anga ? c->d_anga : nullptr, c->flume_of_id,
-                       c->cur, c->id_cur, c->fl_cur);
+                       c->cur, c->id_cur, c->fl_cur, keep_order);
   AF3D_CUDA(cudaStreamSynchronize(c->st));
   AF3D_CUDA(cudaGetLastError());
   c->imported = true;
   c->records_valid = false;
   c->cells_valid = false;
   c->sorted = false;
-  c->since_sort = kResortEvery;
-  drop_graphs(c);
+  c->look = false;
+  if (!keep_order) {
+    c->since_sort = kResortEvery;
+    drop_graphs(c);
+  }
   if (!c->have_grid && c->n > 0) return regrid(c);
   return AF3D_OK;
 }

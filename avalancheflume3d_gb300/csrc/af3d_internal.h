@@ -212,9 +212,11 @@ void launch_regrid (const Launch &L, Planes cur, DevScalars *d, const int *flume
                     long bucket_cap);
 // Re-commit pending grids after the host grew the bucket buffers.
 void launch_commit_grids (cudaStream_t st, DevScalars *d, int nflumes, long n, long bucket_cap);
+// AoS particles (+ a_i, alpha_i) into the planes, clump id at slot id for the first import
+// (keep_order false), else at the slot the clump already holds (the slot order is kept).
 void launch_aos_to_planes (const Launch &L, const af3d_particle *aos, const double *acc,
                            const double *anga, const int *flume_of_id, Planes cur, long long *id,
-                           int *flume);
+                           int *flume, bool keep_order);
 void launch_planes_to_aos (const Launch &L, Planes cur, const long long *id, const int *flume,
                            af3d_particle *aos, double *acc, double *anga, DevScalars *d);
 void launch_contact_pairs (const Launch &L, Planes cur, DevScalars *d, const int *flume,

@@ -45,12 +45,14 @@ __device__ __forceinline__ void raise_status(DevScalars *d, int err) {
 
 // ------------------------------------------------------------------ import / export
 
+// keep_order: slot s keeps the clump it holds (id[s]); otherwise slot s receives clump s.
 __global__ void k_aos_to_planes(const af3d_particle *__restrict__ aos, const double *__restrict__ acc,
                                 const double *__restrict__ anga, const int *__restrict__ flume_of_id,
-                                Planes P, long long *id, int *flume, long n) {
+                                Planes P, long long *id, int *flume, bool keep_order, long n) {
   long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (s >= n) return;
-  const af3d_particle &q = aos[s];
+  const long long i = keep_order ? id[s] : s;
+  const af3d_particle &q = aos[i];
   store3(P, RX, s, mk(q.rr.x, q.rr.y, q.rr.z));
   store3(P, VX, s, mk(q.vv.x, q.vv.y, q.vv.z));
   store3(P, WX, s, mk(q.ww.x, q.ww.y, q.ww.z));
@@ -58,8 +60,8 @@ __global__ void k_aos_to_planes(const af3d_particle *__restrict__ aos, const dou
   store3(P, R10, s, mk(q.Rmaty.x, q.Rmaty.y, q.Rmaty.z));
   store3(P, R20, s, mk(q.Rmatz.x, q.Rmatz.y, q.Rmatz.z));
   for (int k = 0; k < 4; k++) store3(P, S0X + 3 * k, s, mk(q.rr_s[k].x, q.rr_s[k].y, q.rr_s[k].z));
-  V3 a = acc ? mk(acc[3 * s], acc[3 * s + 1], acc[3 * s + 2]) : mk(0.0, 0.0, 0.0);
-  V3 al = anga ? mk(anga[3 * s], anga[3 * s + 1], anga[3 * s + 2]) : mk(0.0, 0.0, 0.0);
+  V3 a = acc ? mk(acc[3 * i], acc[3 * i + 1], acc[3 * i + 2]) : mk(0.0, 0.0, 0.0);
+  V3 al = anga ? mk(anga[3 * i], anga[3 * i + 1], anga[3 * i + 2]) : mk(0.0, 0.0, 0.0);
   store3(P, AIX, s, a);
   store3(P, ALIX, s, al);
   store3(P, AFX, s, mk(0.0, 0.0, 0.0));
@@ -76,8 +78,8 @@ __global__ void k_aos_to_planes(const af3d_particle *__restrict__ aos, const dou
   P.p[ADRAG][s] = drag_factor(r, q.mass);       // get_accel.cu:47
   P.p[IMASS][s] = 1.0 / q.mass;
   P.p[IINER][s] = 1.0 / q.moment_of_inertia.x;
-  id[s] = s;
-  flume[s] = flume_of_id[s];
+  id[s] = i;
+  flume[s] = flume_of_id[i];
 }
 
 __global__ void k_planes_to_aos(Planes P, const long long *__restrict__ id, const int *__restrict__ flume,
@@ -1271,9 +1273,9 @@ void launch_commit_grids(cudaStream_t st, DevScalars *d, int nflumes, long n, lo
 
 void launch_aos_to_planes(const Launch &L, const af3d_particle *aos, const double *acc,
                           const double *anga, const int *flume_of_id, Planes cur, long long *id,
-                          int *flume) {
+                          int *flume, bool keep_order) {
   if (L.n <= 0) return;
-  k_aos_to_planes<<<grid_for(L.n), kBlock, 0, L.st>>>(aos, acc, anga, flume_of_id, cur, id, flume, L.n);
+  k_aos_to_planes<<<grid_for(L.n), kBlock, 0, L.st>>>(aos, acc, anga, flume_of_id, cur, id, flume, keep_order, L.n);
 }
 
 void launch_planes_to_aos(const Launch &L, Planes cur, const long long *id, const int *flume,
