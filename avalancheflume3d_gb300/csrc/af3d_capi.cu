@@ -316,15 +316,15 @@ void enqueue_cell_build(af3d_ctx *c, bool predict, bool t_prev, bool ft = true) 
 // step is the sort and the force pass.  `look`: this step's force pass runs the next step's
 // predictor.
 void enqueue_fused_step(af3d_ctx *c, bool resort, bool write_ft = false, bool look = false) {
-  launch_advance_time(c->st, c->d);
   const bool warm = !resort && c->look;
+  if (!warm) launch_advance_time(c->st, c->d);   // a warm step advances the clock in its sort
   if (resort) {
     enqueue_cell_build(c, true, true, false);   // F, T and a_f are rewritten before being read
     forces_for(c, write_ft, nullptr, c->alt, false, look);
     swap_velocity_planes(c->cur, c->alt);
   } else {
     if (!warm) predict_for(c, true, true, true, true);
-    launch_sort(c->L(), c->d, c->cells, c->id_cur, c->ntags, c->cull);
+    launch_sort(c->L(), c->d, c->cells, c->id_cur, c->ntags, c->cull, warm);
     forces_for(c, write_ft, c->cells.perm, c->cur, warm, look);
   }
   if (look) {
@@ -340,8 +340,10 @@ void enqueue_fused_step(af3d_ctx *c, bool resort, bool write_ft = false, bool lo
 // Kernels of `len` fused steps, the first one permuting (resort_first) or, with look_first,
 // predicted by the previous pass; every later step is predicted by its previous pass.
 long kernels_of(long len, bool resort_first, bool look_first) {
-  const long first = resort_first ? kKernelsPerStep : (look_first ? kKernelsPerKeptStep - 1 : kKernelsPerKeptStep);
-  return first + (len - 1) * (kKernelsPerKeptStep - 1);
+  // a predicted step skips the predictor and advances the clock inside its sort
+  const long warm = kKernelsPerKeptStep - 2;
+  const long first = resort_first ? kKernelsPerStep : (look_first ? warm : kKernelsPerKeptStep);
+  return first + (len - 1) * warm;
 }
 
 af3d_status run_steps(af3d_ctx *c, long m) {
@@ -915,11 +917,11 @@ af3d_status af3d_step_profile(af3d_ctx *c, long k, double *ms) {
     const bool regrid_after = c->cc % kRegridEvery == 0;
     const bool look = i + 1 < k && !regrid_after && !((resort ? 0 : c->since_sort + 1) + 1 > kResortEvery);
     AF3D_CUDA(cudaEventRecord(ev[0], c->st));
-    launch_advance_time(c->st, c->d);
+    if (!warm) launch_advance_time(c->st, c->d);
     AF3D_CUDA(cudaEventRecord(ev[1], c->st));
     if (!warm) predict_for(c, true, true, true, !resort);
     AF3D_CUDA(cudaEventRecord(ev[2], c->st));
-    launch_sort(c->L(), c->d, c->cells, c->id_cur, c->ntags, resort ? nullptr : c->cull);
+    launch_sort(c->L(), c->d, c->cells, c->id_cur, c->ntags, resort ? nullptr : c->cull, warm);
     AF3D_CUDA(cudaEventRecord(ev[3], c->st));
     if (resort) {
       launch_permute_records(c->L(), c->cur, c->alt, c->cells.perm, c->id_cur, c->id_alt, c->fl_cur,

@@ -67,8 +67,14 @@ __device__ __forceinline__ int block_excl_scan(int v, int *total) {
 // Buckets in use: every flume's cells plus one private bucket per clump for the clumps not binned.
 __device__ __forceinline__ long n_buckets(const DevScalars *d, long n) { return d->ncell_total + n; }
 
-__global__ void k_scan_partials(const int *__restrict__ count, int *block_sums, const DevScalars *d,
+// advance: block 0 also performs k_advance_time's time += dt (steps whose predictor ran in the
+// previous force pass start with the sort; nothing before the force pass reads the clock).
+__global__ void k_scan_partials(const int *__restrict__ count, int *block_sums, DevScalars *d, bool advance,
                                 long n) {
+  if (advance && blockIdx.x == 0 && threadIdx.x == 0) {
+    d->time_prev = d->time;
+    d->time = d->time + d->flumes[0].sys.dt;
+  }
   const long nb = n_buckets(d, n);
   const long base = blockIdx.x * (long)kTile + threadIdx.x * (long)kScanItems;
   __shared__ int tot;
@@ -192,11 +198,12 @@ __global__ void k_rank(const int *__restrict__ key, const int *__restrict__ star
 
 long scan_tiles(long bucket_cap) { return (bucket_cap + kTile - 1) / kTile; }
 
-void launch_sort(const Launch &L, DevScalars *d, Cells c, const long long *id, long ntags, const CullRec *cull) {
+void launch_sort(const Launch &L, DevScalars *d, Cells c, const long long *id, long ntags, const CullRec *cull,
+                 bool advance) {
   // Launch sizes follow the capacity; the kernels read the bucket count in use from the device,
   // so a captured graph stays valid across device-side re-grids.
   const long ntiles = scan_tiles(c.cap);
-  k_scan_partials<<<(unsigned)ntiles, kScanThreads, 0, L.st>>>(c.count, c.block_sums, d, L.n);
+  k_scan_partials<<<(unsigned)ntiles, kScanThreads, 0, L.st>>>(c.count, c.block_sums, d, advance, L.n);
   k_scan_top<<<1, kTopThreads, 0, L.st>>>(c.block_sums, ntiles, c.start, d, L.n);
   k_scan_final<<<(unsigned)ntiles, kScanThreads, 0, L.st>>>(c.count, c.block_sums, c.start, d, L.n);
   if (L.n <= 0) return;

@@ -181,7 +181,7 @@ void launch_predict (const Launch &L, Planes cur, DevScalars *d, bool predict, b
 // count array zeroed.  nbuckets = ncell_total + N is read on the device.
 // With cull (records already written at the old slots) also fills cells.csort.
 void launch_sort (const Launch &L, DevScalars *d, Cells cells, const long long *id, long ntags,
-                  const CullRec *cull = nullptr);
+                  const CullRec *cull = nullptr, bool advance = false);
 long scan_tiles (long bucket_cap);
 // Moves every plane (and the id and flume arrays) into the new order and builds the records.
 // `ft`: also carry the force/torque accumulators and a_f (the fused step rewrites them first).
