@@ -484,48 +484,17 @@ __device__ __forceinline__ void shared_add3(double *p, V3 v) {
   atomicAdd(p + 64, v.z);
 }
 
-// Reverse of finish_Verlet, get_accel and every contact of one clump (startup: the start-up
-// force pass, which has no finish and whose accelerations become a_i of the first step).
-// in: adjoint of the next state; out.a/out.al receive the finish terms of this step's a_i and
-// alpha_i; acc receives (atomically) the adjoints of every clump's r1, v1, w1 and spheres;
-// rb receives this clump's own R1 adjoint.  The contacts run warp-cooperatively: the item lists
-// of the forward pass, 32 items a round, each lane reversing one contact for its owner.
-#ifndef AF3D_ADJ_MINB
-#define AF3D_ADJ_MINB 1
-#endif
-__global__ void __launch_bounds__(kAdjCoopBlock, AF3D_ADJ_MINB) k_adj_forces(Planes P, Planes in, Planes out, Planes acc,
-                                                              Planes rb, DevScalars *d, const int *__restrict__ flume,
-                                                              const NbrRec *__restrict__ nbr,
-                                                              const CullRec *__restrict__ cull,
-                                                              const int *__restrict__ start,
-                                                              const int *__restrict__ order,
-                                                              const float4 *__restrict__ csort, double *param_b,
-                                                              int startup, long n) {
-  __shared__ AdjQueue queues[kAdjCoopBlock / 32];
-  AdjQueue &aq = queues[threadIdx.x >> 5];
-  const int lane = threadIdx.x & 31;
-  const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  const bool valid = s < n;
-  const long sv = valid ? s : n - 1;
-  const long wbase = blockIdx.x * (long)blockDim.x + (threadIdx.x & ~31u);
-  ParamBar par = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-  const int f = flume[sv];
-  const Consts c = load_consts(d, f);
-  const af3d_cell_par g = d->flumes[f].grid;
-  const long long off = d->flumes[f].cell_off;
-  const NbrRec &me = nbr[sv];
-  Own o;
-  o.r = mk(me.rx, me.ry, me.rz);
-  o.v = mk(me.vx, me.vy, me.vz);
-  o.w = mk(me.wx, me.wy, me.wz);
-  for (int k = 0; k < 4; k++) o.s[k] = mk(me.s[3 * k], me.s[3 * k + 1], me.s[3 * k + 2]);
-  o.rad = me.rad; o.msph = me.msph; o.mwall = me.mwall;
-  const bool removed = is_removed(*c.tp, o.r.x, c.side_x);
-  const bool act = valid && !removed;
-  ClumpBar ob;
+// Reverse of finish_Verlet and get_accel for clump s (startup: the start-up pass, which has no
+// finish): out.a/out.al receive the finish terms of this step's a_i, alpha_i, rb the clump's own
+// R1 adjoint; returns the adjoints of the force and torque sums (Fb, Tb) and of the predicted
+// velocities (ob.v, ob.w).
+__device__ __forceinline__ void adj_head(long s, bool act, bool valid, int startup, const Own &o, const Consts &c,
+                                         const Planes &P, const Planes &in, const Planes &out, const Planes &rb,
+                                         ClumpBar &ob, V3 &Fb, V3 &Tb) {
   ob.r = ob.v = ob.w = mk(0.0, 0.0, 0.0);
   for (int k = 0; k < 4; k++) ob.s[k] = mk(0.0, 0.0, 0.0);
-  V3 Fb = mk(0.0, 0.0, 0.0), Tb = mk(0.0, 0.0, 0.0);
+  Fb = mk(0.0, 0.0, 0.0);
+  Tb = mk(0.0, 0.0, 0.0);
   if (act) {
     // finish: v2 = v1 + hdt (a_f - a_i), w2 likewise
     const V3 v2_b = startup ? mk(0.0, 0.0, 0.0) : ld3(in, AV, s);
@@ -568,6 +537,91 @@ __global__ void __launch_bounds__(kAdjCoopBlock, AF3D_ADJ_MINB) k_adj_forces(Pla
       st3(out, AAL, s, mk(0.0, 0.0, 0.0));
     }
   }
+}
+
+// Reverse of one item of owner record om (force/torque adjoints fb_o, tb_o): the owner's adjoints
+// in ib (returns the owner's sphere), the partner's straight into acc, the parameters' in ipar.
+__device__ __forceinline__ int adj_item(const NbrRec &om, unsigned it, const Consts &co, V3 fb_o, V3 tb_o,
+                                        const NbrRec *__restrict__ nbr, const Planes &acc, ItemBar &ib,
+                                        ParamBar &ipar) {
+  const V3 rl = mk(om.rx, om.ry, om.rz), vl = mk(om.vx, om.vy, om.vz), wl = mk(om.wx, om.wy, om.wz);
+  ib = zero_item();
+  int k;
+  if (it >= kBndItem) {
+    const int rt = (int)((it >> 2) & 7u);
+    k = (int)(it & 3u);
+    Sph q;
+    q.r = rl; q.v = vl; q.w = wl;
+    q.s = mk(om.s[3 * k], om.s[3 * k + 1], om.s[3 * k + 2]);
+    q.rad = om.rad;
+    q.mwall = om.mwall;
+    wall_rev(rt, q, co, fb_o, tb_o, ib, ipar);
+  } else {
+    const int t = (int)(it >> 4), p = (int)(it & 15u);
+    k = p & 3;
+    const int sm = p >> 2;
+    const V3 s1 = mk(om.s[3 * k], om.s[3 * k + 1], om.s[3 * k + 2]);
+    V3 pr_b, pv_b, pw_b, ps_b;
+    bool any;
+    pair_rev(rl, vl, wl, s1, om.rad, om.msph, nbr[t], sm, co, co.variant == AF3D_FRICTION_DEV, fb_o, tb_o, ib,
+             pr_b, pv_b, pw_b, ps_b, ipar, any);
+    if (any) {
+      atomic_add3(acc, CR, t, pr_b);
+      atomic_add3(acc, CV, t, pv_b);
+      atomic_add3(acc, CW, t, pw_b);
+      atomic_add3(acc, CS + 3 * sm, t, ps_b);
+    }
+  }
+  return k;
+}
+
+__device__ __forceinline__ void add_par(ParamBar &par, const ParamBar &ipar) {
+  par.kappa_pp += ipar.kappa_pp; par.gamma_pp += ipar.gamma_pp; par.mu_pp += ipar.mu_pp;
+  par.kappa_pw += ipar.kappa_pw; par.gamma_pw += ipar.gamma_pw; par.mu_pw += ipar.mu_pw;
+}
+
+// Reverse of finish_Verlet, get_accel and every contact of one clump (startup: the start-up
+// force pass, which has no finish and whose accelerations become a_i of the first step).
+// in: adjoint of the next state; out.a/out.al receive the finish terms of this step's a_i and
+// alpha_i; acc receives (atomically) the adjoints of every clump's r1, v1, w1 and spheres;
+// rb receives this clump's own R1 adjoint.  The contacts run warp-cooperatively: the item lists
+// of the forward pass, rebuilt here, 32 items a round, each lane reversing one contact for its
+// owner.
+#ifndef AF3D_ADJ_MINB
+#define AF3D_ADJ_MINB 1
+#endif
+__global__ void __launch_bounds__(kAdjCoopBlock, AF3D_ADJ_MINB) k_adj_forces(Planes P, Planes in, Planes out, Planes acc,
+                                                              Planes rb, DevScalars *d, const int *__restrict__ flume,
+                                                              const NbrRec *__restrict__ nbr,
+                                                              const CullRec *__restrict__ cull,
+                                                              const int *__restrict__ start,
+                                                              const int *__restrict__ order,
+                                                              const float4 *__restrict__ csort, double *param_b,
+                                                              int startup, long n) {
+  __shared__ AdjQueue queues[kAdjCoopBlock / 32];
+  AdjQueue &aq = queues[threadIdx.x >> 5];
+  const int lane = threadIdx.x & 31;
+  const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const bool valid = s < n;
+  const long sv = valid ? s : n - 1;
+  const long wbase = blockIdx.x * (long)blockDim.x + (threadIdx.x & ~31u);
+  ParamBar par = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  const int f = flume[sv];
+  const Consts c = load_consts(d, f);
+  const af3d_cell_par g = d->flumes[f].grid;
+  const long long off = d->flumes[f].cell_off;
+  const NbrRec &me = nbr[sv];
+  Own o;
+  o.r = mk(me.rx, me.ry, me.rz);
+  o.v = mk(me.vx, me.vy, me.vz);
+  o.w = mk(me.wx, me.wy, me.wz);
+  for (int k = 0; k < 4; k++) o.s[k] = mk(me.s[3 * k], me.s[3 * k + 1], me.s[3 * k + 2]);
+  o.rad = me.rad; o.msph = me.msph; o.mwall = me.mwall;
+  const bool removed = is_removed(*c.tp, o.r.x, c.side_x);
+  const bool act = valid && !removed;
+  ClumpBar ob;
+  V3 Fb, Tb;
+  adj_head(s, act, valid, startup, o, c, P, in, out, rb, ob, Fb, Tb);
   aq.fb[0][lane] = Fb.x; aq.fb[1][lane] = Fb.y; aq.fb[2][lane] = Fb.z;
   aq.fb[3][lane] = Tb.x; aq.fb[4][lane] = Tb.y; aq.fb[5][lane] = Tb.z;
   for (int k = 0; k < 21; k++) aq.own[k][lane] = 0.0;
@@ -585,46 +639,14 @@ __global__ void __launch_bounds__(kAdjCoopBlock, AF3D_ADJ_MINB) k_adj_forces(Pla
       const int lo = owner_of(aq.il.base, j);
       const unsigned it = aq.il.items[j - aq.il.base[lo]][lo];
       const long os = wbase + lo;
-      const NbrRec &om = nbr[os];
       const int of = flume[os];
       const Consts co = of == f ? c : load_consts(d, of);
-      const V3 fb_o = mk(aq.fb[0][lo], aq.fb[1][lo], aq.fb[2][lo]);
-      const V3 tb_o = mk(aq.fb[3][lo], aq.fb[4][lo], aq.fb[5][lo]);
-      const V3 rl = mk(om.rx, om.ry, om.rz), vl = mk(om.vx, om.vy, om.vz), wl = mk(om.wx, om.wy, om.wz);
-      ItemBar ib = zero_item();
+      ItemBar ib;
       ParamBar ipar = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};   // this item's; the lane's flume or the owner's
-      int k;
-      if (it >= kBndItem) {
-        const int rt = (int)((it >> 2) & 7u);
-        k = (int)(it & 3u);
-        Sph q;
-        q.r = rl; q.v = vl; q.w = wl;
-        q.s = mk(om.s[3 * k], om.s[3 * k + 1], om.s[3 * k + 2]);
-        q.rad = om.rad;
-        q.mwall = om.mwall;
-        wall_rev(rt, q, co, fb_o, tb_o, ib, ipar);
-      } else {
-        const int t = (int)(it >> 4), p = (int)(it & 15u);
-        k = p & 3;
-        const int sm = p >> 2;
-        const V3 s1 = mk(om.s[3 * k], om.s[3 * k + 1], om.s[3 * k + 2]);
-        V3 pr_b, pv_b, pw_b, ps_b;
-        bool any;
-        pair_rev(rl, vl, wl, s1, om.rad, om.msph, nbr[t], sm, co, co.variant == AF3D_FRICTION_DEV, fb_o, tb_o, ib,
-                 pr_b, pv_b, pw_b, ps_b, ipar, any);
-        if (any) {
-          atomic_add3(acc, CR, t, pr_b);
-          atomic_add3(acc, CV, t, pv_b);
-          atomic_add3(acc, CW, t, pw_b);
-          atomic_add3(acc, CS + 3 * sm, t, ps_b);
-        }
-      }
-      if (of == f) {
-        par.kappa_pp += ipar.kappa_pp; par.gamma_pp += ipar.gamma_pp; par.mu_pp += ipar.mu_pp;
-        par.kappa_pw += ipar.kappa_pw; par.gamma_pw += ipar.gamma_pw; par.mu_pw += ipar.mu_pw;
-      } else {
-        flush_params(param_b, of, ipar);
-      }
+      const int k = adj_item(nbr[os], it, co, mk(aq.fb[0][lo], aq.fb[1][lo], aq.fb[2][lo]),
+                             mk(aq.fb[3][lo], aq.fb[4][lo], aq.fb[5][lo]), nbr, acc, ib, ipar);
+      if (of == f) add_par(par, ipar);
+      else flush_params(param_b, of, ipar);
       double *ow = &aq.own[0][lo];
       shared_add3(ow + 32 * CR, ib.r);
       shared_add3(ow + 32 * CV, ib.v);
@@ -636,6 +658,140 @@ __global__ void __launch_bounds__(kAdjCoopBlock, AF3D_ADJ_MINB) k_adj_forces(Pla
   if (act) {
     if (slow) adj_contacts_lane(s, o, c, g, off, B, Fb, Tb, acc, nbr, cull, start, order, ob, par);
     auto own3 = [&](int c0) { return mk(aq.own[c0][lane], aq.own[c0 + 1][lane], aq.own[c0 + 2][lane]); };
+    atomic_add3(acc, CR, s, ob.r + own3(CR));
+    atomic_add3(acc, CV, s, ob.v + own3(CV));
+    atomic_add3(acc, CW, s, ob.w + own3(CW));
+    for (int k = 0; k < 4; k++) atomic_add3(acc, CS + 3 * k, s, ob.s[k] + own3(CS + 3 * k));
+  }
+  add_params(param_b, f, par);
+}
+
+// The same reverse from the item lists the forward pass recorded (ContactLists with cnt), pooled
+// over a block of 128 clumps: the block's particle items, then its boundary items, 32 a round per
+// warp, owners' adjoints summed in shared memory (a reverse needs no order).
+constexpr int kAdjListBlock = 128;
+struct AdjBlock {
+  double fb[6][kAdjListBlock];
+  double own[21][kAdjListBlock];
+  int base[kAdjListBlock + 1], pbase[kAdjListBlock + 1], qbase[kAdjListBlock + 1];
+  int npre[kAdjListBlock];
+  int wsum[3][kAdjListBlock / 32];
+};
+
+__global__ void __launch_bounds__(kAdjListBlock) k_adj_forces_l(Planes P, Planes in, Planes out, Planes acc,
+                                                               Planes rb, DevScalars *d, const int *__restrict__ flume,
+                                                               const NbrRec *__restrict__ nbr,
+                                                               const CullRec *__restrict__ cull,
+                                                               const int *__restrict__ start,
+                                                               const int *__restrict__ order, ContactLists lists,
+                                                               double *param_b, long n) {
+  __shared__ AdjBlock ab;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const long bbase = blockIdx.x * (long)kAdjListBlock;
+  const long s = bbase + tid;
+  const bool valid = s < n;
+  const long sv = valid ? s : n - 1;
+  ParamBar par = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  const int f = flume[sv];
+  const Consts c = load_consts(d, f);
+  const NbrRec &me = nbr[sv];
+  Own o;
+  o.r = mk(me.rx, me.ry, me.rz);
+  o.v = mk(me.vx, me.vy, me.vz);
+  o.w = mk(me.wx, me.wy, me.wz);
+  for (int k = 0; k < 4; k++) o.s[k] = mk(me.s[3 * k], me.s[3 * k + 1], me.s[3 * k + 2]);
+  o.rad = me.rad; o.msph = me.msph; o.mwall = me.mwall;
+  const bool removed = is_removed(*c.tp, o.r.x, c.side_x);
+  const bool act = valid && !removed;
+  ClumpBar ob;
+  V3 Fb, Tb;
+  adj_head(s, act, valid, 0, o, c, P, in, out, rb, ob, Fb, Tb);
+  ab.fb[0][tid] = Fb.x; ab.fb[1][tid] = Fb.y; ab.fb[2][tid] = Fb.z;
+  ab.fb[3][tid] = Tb.x; ab.fb[4][tid] = Tb.y; ab.fb[5][tid] = Tb.z;
+  for (int k = 0; k < 21; k++) ab.own[k][tid] = 0.0;
+  // the clump's recorded list layout
+  const int packed = act ? lists.cnt[s] : 0;
+  const bool slow = act && packed < 0;
+  const int nitems = packed > 0 ? (packed & 0xff) : 0;
+  const int npre = packed > 0 ? ((packed >> 8) & 0xff) : 0;
+  const int npair = packed > 0 ? ((packed >> 16) & 0xff) : 0;
+  ab.npre[tid] = npre;
+  int v[3] = {nitems, npair, nitems - npair};
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+    for (int k = 1; k < 32; k <<= 1) {
+      const int u = __shfl_up_sync(0xffffffffu, v[q], k);
+      if (lane >= k) v[q] += u;
+    }
+    if (lane == 31) ab.wsum[q][warp] = v[q];
+  }
+  __syncthreads();
+  const int own_cnt[3] = {nitems, npair, nitems - npair};
+  int *dst[3] = {ab.base, ab.pbase, ab.qbase};
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+    int wofs = 0, tot = 0;
+    for (int w = 0; w < kAdjListBlock / 32; w++) {
+      const int t = ab.wsum[q][w];
+      wofs += w < warp ? t : 0;
+      tot += t;
+    }
+    dst[q][tid] = wofs + v[q] - own_cnt[q];
+    if (tid == kAdjListBlock - 1) dst[q][kAdjListBlock] = tot;
+  }
+  __syncthreads();
+  const int total = ab.base[kAdjListBlock], ptotal = ab.pbase[kAdjListBlock];
+  auto owner = [&](const int *b, int j) {
+    int lo = 0, hi = kAdjListBlock - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (b[mid] <= j) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+  };
+  for (int r0 = warp * 32; r0 < total; r0 += kAdjListBlock) {
+    const int i = r0 + lane;
+    if (i < total) {
+      int lo, idx;
+      if (i < ptotal) {
+        lo = owner(ab.pbase, i);
+        idx = ab.npre[lo] + (i - ab.pbase[lo]);
+      } else {
+        const int ib = i - ptotal;
+        lo = owner(ab.qbase, ib);
+        const int b = ib - ab.qbase[lo], np = ab.npre[lo];
+        idx = b < np ? b : b + (ab.pbase[lo + 1] - ab.pbase[lo]);
+      }
+      const unsigned it = lists.items[(long)idx * n + bbase + lo];
+      const long os = bbase + lo;
+      const int of = flume[os];
+      const Consts co = of == f ? c : load_consts(d, of);
+      ItemBar itb;
+      ParamBar ipar = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+      const int k = adj_item(nbr[os], it, co, mk(ab.fb[0][lo], ab.fb[1][lo], ab.fb[2][lo]),
+                             mk(ab.fb[3][lo], ab.fb[4][lo], ab.fb[5][lo]), nbr, acc, itb, ipar);
+      if (of == f) add_par(par, ipar);
+      else flush_params(param_b, of, ipar);
+      double *ow = &ab.own[0][lo];
+      atomicAdd(ow + kAdjListBlock * CR, itb.r.x); atomicAdd(ow + kAdjListBlock * (CR + 1), itb.r.y);
+      atomicAdd(ow + kAdjListBlock * (CR + 2), itb.r.z);
+      atomicAdd(ow + kAdjListBlock * CV, itb.v.x); atomicAdd(ow + kAdjListBlock * (CV + 1), itb.v.y);
+      atomicAdd(ow + kAdjListBlock * (CV + 2), itb.v.z);
+      atomicAdd(ow + kAdjListBlock * CW, itb.w.x); atomicAdd(ow + kAdjListBlock * (CW + 1), itb.w.y);
+      atomicAdd(ow + kAdjListBlock * (CW + 2), itb.w.z);
+      const int cs = CS + 3 * k;
+      atomicAdd(ow + kAdjListBlock * cs, itb.s.x); atomicAdd(ow + kAdjListBlock * (cs + 1), itb.s.y);
+      atomicAdd(ow + kAdjListBlock * (cs + 2), itb.s.z);
+    }
+  }
+  __syncthreads();
+  if (act) {
+    if (slow) {
+      const af3d_cell_par g = d->flumes[f].grid;
+      adj_contacts_lane(s, o, c, g, d->flumes[f].cell_off, (double)cull[sv].c.w, Fb, Tb, acc, nbr, cull, start,
+                        order, ob, par);
+    }
+    auto own3 = [&](int c0) { return mk(ab.own[c0][tid], ab.own[c0 + 1][tid], ab.own[c0 + 2][tid]); };
     atomic_add3(acc, CR, s, ob.r + own3(CR));
     atomic_add3(acc, CV, s, ob.v + own3(CV));
     atomic_add3(acc, CW, s, ob.w + own3(CW));
@@ -854,6 +1010,15 @@ void launch_adj_forces(const Launch &L, Planes P, Planes in, Planes out, Planes 
   const unsigned nb = (unsigned)((L.n + kAdjCoopBlock - 1) / kAdjCoopBlock);
   k_adj_forces<<<nb, kAdjCoopBlock, 0, L.st>>>(P, in, out, acc, rb, d, flume, nbr, cull, start, order, csort, param_b,
                                                startup ? 1 : 0, L.n);
+}
+
+void launch_adj_forces_lists(const Launch &L, Planes P, Planes in, Planes out, Planes acc, Planes rb, DevScalars *d,
+                             const int *flume, const NbrRec *nbr, const CullRec *cull, const int *start,
+                             const int *order, ContactLists lists, double *param_b) {
+  if (L.n <= 0) return;
+  const unsigned nb = (unsigned)((L.n + kAdjListBlock - 1) / kAdjListBlock);
+  k_adj_forces_l<<<nb, kAdjListBlock, 0, L.st>>>(P, in, out, acc, rb, d, flume, nbr, cull, start, order, lists,
+                                                 param_b, L.n);
 }
 
 void launch_adj_predict(const Launch &L, Planes P, Planes tape, Planes in, Planes out, Planes acc, Planes rb,

@@ -1225,6 +1225,17 @@ extern "C" af3d_status af3d_adjoint(af3d_ctx *c, long steps, long ckpt_every, do
   if (want_grad && e == cudaSuccess) e = buf.planes(kAdjPlanes, n, adjB);
   if (want_grad && e == cudaSuccess) e = buf.planes(kAccPlanes, n, acc);
   if (want_grad && e == cudaSuccess) e = buf.planes(kRbPlanes, n, rb);
+  // every recomputed step's item lists and counts, for the reverse of its contacts
+  std::vector<ContactLists> tape_lists(tape.size());
+  for (size_t k = 0; k < tape.size() && e == cudaSuccess; k++) {
+    void *p = nullptr;
+    e = cudaMalloc(&p, (sizeof(unsigned) * kListCap + sizeof(int)) * (size_t)std::max<long>(n, 1));
+    if (e == cudaSuccess) {
+      buf.owned.push_back(p);
+      tape_lists[k].items = static_cast<unsigned *>(p);
+      tape_lists[k].cnt = reinterpret_cast<int *>(tape_lists[k].items + (size_t)kListCap * n);
+    }
+  }
   // per flume f: dsc[2 f], dsc[2 f + 1] the objective sums, pgr[6 f .. 6 f + 5] the parameter adjoints
   const size_t nsc = (size_t)8 * nf;
   double *dsc = nullptr;
@@ -1271,9 +1282,12 @@ extern "C" af3d_status af3d_adjoint(af3d_ctx *c, long steps, long ckpt_every, do
       c->look = false;   // the restored state has not been predicted
       s = set_device_time(c, t_start[k0]);
       if (s) return s;
+      const ContactLists own_lists = c->lists;
       for (long k = k0; k < k1; k++) {
         launch_state_copy(c->L(), c->cur, tape[k - k0], true);
+        c->lists = tape_lists[k - k0];
         enqueue_fused_step(c, false, true, k + 1 < k1);
+        c->lists = own_lists;
         s = copy_torque(c, tape[k - k0], true);
         if (s) return s;
       }
@@ -1286,8 +1300,8 @@ extern "C" af3d_status af3d_adjoint(af3d_ctx *c, long steps, long ckpt_every, do
         if (s) return s;
         enqueue_step_cells(c);
         AF3D_CUDA(cudaMemsetAsync(acc.p[0], 0, sizeof(double) * kAccPlanes * n, c->st));   // one block
-        launch_adj_forces(c->L(), c->cur, adjA, adjB, acc, rb, c->d, c->fl_cur, c->nbr, c->cull, c->cells.start,
-                          c->cells.perm, c->cells.csort, pgr, false);
+        launch_adj_forces_lists(c->L(), c->cur, adjA, adjB, acc, rb, c->d, c->fl_cur, c->nbr, c->cull,
+                                c->cells.start, c->cells.perm, tape_lists[k - k0], pgr);
         launch_adj_predict(c->L(), c->cur, tape[k - k0], adjA, adjB, acc, rb, c->d, c->fl_cur);
         std::swap(adjA, adjB);
       }

@@ -110,11 +110,19 @@ struct DevScalars {
 
 // Per-clump item lists of one force pass, from the list phase to the force phase of the force
 // kernel: entry e of slot s at items[e * n + s] (an item is a boundary (routine, sphere) or a
-// particle (partner slot, sph_id) contact).
+// particle (partner slot, sph_id) contact).  With cnt, the pass also records each clump's list
+// layout there (pack_list_counts), which lets the adjoint reverse the pass from the same lists.
 constexpr int kListCap = 32;
 struct ContactLists {
   unsigned *items;   // [kListCap][n]
+  int *cnt;          // [n] or null
 };
+
+// A clump's list layout as one int: -1 when its lists overflowed, else the item count | the
+// boundary items before the particle items << 8 | the particle items << 16 (each at most 32).
+__host__ __device__ inline int pack_list_counts(int listed, int pre, int pair) {
+  return listed < 0 ? -1 : listed | pre << 8 | pair << 16;
+}
 
 // The next step's predictor run at the end of a force pass (look-ahead): the corrected clump is
 // advanced at once, its records go to the next step's record buffers, its rotation rows to the
@@ -234,6 +242,11 @@ constexpr int kAdjPlanes = 24, kAccPlanes = 21, kRbPlanes = 9;
 void launch_adj_forces (const Launch &L, Planes P, Planes in, Planes out, Planes acc, Planes rb, DevScalars *d,
                         const int *flume, const NbrRec *nbr, const CullRec *cull, const int *start,
                         const int *order, const float4 *csort, double *param_b, bool startup);
+// The same reverse (not the start-up pass) from the item lists and counts the forward force pass
+// of this step recorded.
+void launch_adj_forces_lists (const Launch &L, Planes P, Planes in, Planes out, Planes acc, Planes rb,
+                              DevScalars *d, const int *flume, const NbrRec *nbr, const CullRec *cull,
+                              const int *start, const int *order, ContactLists lists, double *param_b);
 void launch_adj_predict (const Launch &L, Planes P, Planes tape, Planes in, Planes out, Planes acc, Planes rb,
                          DevScalars *d, const int *flume);
 void launch_adj_startup (const Launch &L, Planes P, Planes in, Planes out, Planes acc, Planes rb);

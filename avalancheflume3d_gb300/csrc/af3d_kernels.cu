@@ -805,6 +805,7 @@ __device__ __forceinline__ void fused_body(const Consts &c, Planes P, Planes out
   NbrRec q;
   CullRec cr;
   if (valid) {
+    if (lists.cnt) lists.cnt[s] = pack_list_counts(listed, lc.pre, lc.pair);
     if (WRITE_FT) {
       store3(P, FX, s, F);
       store3(P, TX, s, T);
