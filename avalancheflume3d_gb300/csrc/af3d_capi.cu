@@ -1185,14 +1185,10 @@ void enqueue_step_cells(af3d_ctx *c) {
   launch_sort(c->L(), c->d, c->cells, c->id_cur, c->ntags, c->cull);
 }
 
-// The torque sums of a step between the plane set and planes 24..26 of its tape slot.
-af3d_status copy_torque(af3d_ctx *c, Planes &tape, bool to_tape) {
-  for (int k = 0; k < 3; k++) {
-    double *a = tape.p[kAdjPlanes + k], *b = c->cur.p[TX + k];
-    AF3D_CUDA(cudaMemcpyAsync(to_tape ? a : b, to_tape ? b : a, sizeof(double) * c->n, cudaMemcpyDeviceToDevice,
-                              c->st));
-  }
-  return AF3D_OK;
+// The plane set with its torque planes replaced by planes 24..26 of a tape slot.
+Planes with_tape_torque(Planes P, const Planes &tape) {
+  for (int k = 0; k < 3; k++) P.p[TX + k] = tape.p[kAdjPlanes + k];
+  return P;
 }
 
 }  // namespace
@@ -1213,29 +1209,36 @@ extern "C" af3d_status af3d_adjoint(af3d_ctx *c, long steps, long ckpt_every, do
     ~ModeBack() { c->fp_mode = m; }
   } mode_back{c, mode};
   drop_graphs(c);
-  const long nck = steps / ckpt_every + 1;
+  // checkpoints open every segment but the last, which the forward run tapes itself
+  const long nck = steps > 0 ? (steps - 1) / ckpt_every : 0;
   AdjBuffers buf;
   Planes state0{}, fin{}, adjA{}, adjB{}, acc{}, rb{};
   std::vector<Planes> ckpt(nck), tape(want_grad ? std::min(ckpt_every, std::max<long>(steps, 1)) : 0);
+  std::vector<ContactLists> tape_lists(tape.size());
   cudaError_t e = buf.planes(kAdjPlanes + 12, n, state0);   // with the sphere centres
   if (e == cudaSuccess) e = buf.planes(kAdjPlanes + 12, n, fin);
   for (long k = 0; k < nck && e == cudaSuccess && want_grad; k++) e = buf.planes(kAdjPlanes, n, ckpt[k]);
-  for (size_t k = 0; k < tape.size() && e == cudaSuccess; k++) e = buf.planes(kAdjPlanes + 3, n, tape[k]);
+  if (!tape.empty() && e == cudaSuccess) {
+    // one block for the tape: per step its state, torque sums, item lists and list counts
+    const size_t m = (size_t)std::max<long>(n, 1);
+    const size_t slot =
+        (sizeof(double) * (kAdjPlanes + 3) * m + (sizeof(unsigned) * kListCap + sizeof(int)) * m + 255) & ~(size_t)255;
+    char *base = nullptr;
+    e = cudaMalloc((void **)&base, slot * tape.size());
+    if (e == cudaSuccess) {
+      buf.owned.push_back(base);
+      for (size_t k = 0; k < tape.size(); k++) {
+        double *pl = reinterpret_cast<double *>(base + slot * k);
+        for (int i = 0; i < NPLANES; i++) tape[k].p[i] = i < kAdjPlanes + 3 ? pl + (size_t)i * m : nullptr;
+        tape_lists[k].items = reinterpret_cast<unsigned *>(pl + (size_t)(kAdjPlanes + 3) * m);
+        tape_lists[k].cnt = reinterpret_cast<int *>(tape_lists[k].items + (size_t)kListCap * m);
+      }
+    }
+  }
   if (want_grad && e == cudaSuccess) e = buf.planes(kAdjPlanes, n, adjA);
   if (want_grad && e == cudaSuccess) e = buf.planes(kAdjPlanes, n, adjB);
   if (want_grad && e == cudaSuccess) e = buf.planes(kAccPlanes, n, acc);
   if (want_grad && e == cudaSuccess) e = buf.planes(kRbPlanes, n, rb);
-  // every recomputed step's item lists and counts, for the reverse of its contacts
-  std::vector<ContactLists> tape_lists(tape.size());
-  for (size_t k = 0; k < tape.size() && e == cudaSuccess; k++) {
-    void *p = nullptr;
-    e = cudaMalloc(&p, (sizeof(unsigned) * kListCap + sizeof(int)) * (size_t)std::max<long>(n, 1));
-    if (e == cudaSuccess) {
-      buf.owned.push_back(p);
-      tape_lists[k].items = static_cast<unsigned *>(p);
-      tape_lists[k].cnt = reinterpret_cast<int *>(tape_lists[k].items + (size_t)kListCap * n);
-    }
-  }
   // per flume f: dsc[2 f], dsc[2 f + 1] the objective sums, pgr[6 f .. 6 f + 5] the parameter adjoints
   const size_t nsc = (size_t)8 * nf;
   double *dsc = nullptr;
@@ -1252,12 +1255,30 @@ extern "C" af3d_status af3d_adjoint(af3d_ctx *c, long steps, long ckpt_every, do
   enqueue_startup_pass(c);
   swap_accel_planes(c->cur);
   swap_accel_planes(c->alt);
+  // The last segment's steps record their tape slots here (the reverse starts with them).
+  const long seg_last = steps > 0 ? (steps - 1) / ckpt_every : 0, k_last = seg_last * ckpt_every;
+  const ContactLists own_lists = c->lists;
+  const Planes own_cur = c->cur;
+  // Step k of a segment starting at k0, its starting state, item lists and torque sums into its
+  // tape slot (a kept-order step neither swaps nor reallocates the plane sets).
+  auto taped_step = [&](long k, long k0, long k1) {
+    launch_state_copy(c->L(), c->cur, tape[k - k0], true);
+    c->lists = tape_lists[k - k0];
+    c->cur = with_tape_torque(c->cur, tape[k - k0]);
+    enqueue_fused_step(c, false, true, k + 1 < k1);
+    for (int q = 0; q < 3; q++) c->cur.p[TX + q] = own_cur.p[TX + q];
+    c->lists = own_lists;
+  };
   std::vector<double> t_start(steps + 1);
   double t = t_init;
   for (long k = 0; k < steps; k++) {
-    if (want_grad && k % ckpt_every == 0) launch_state_copy(c->L(), c->cur, ckpt[k / ckpt_every], true);
     t_start[k] = t;
-    enqueue_fused_step(c, false, false, k + 1 < steps);   // the last pass does not look ahead
+    if (want_grad && k >= k_last) {
+      taped_step(k, k_last, steps);
+    } else {
+      if (want_grad && k % ckpt_every == 0) launch_state_copy(c->L(), c->cur, ckpt[k / ckpt_every], true);
+      enqueue_fused_step(c, false, false, k + 1 < steps);   // the last pass does not look ahead
+    }
     t = t + dt;
   }
   t_start[steps] = t;
@@ -1274,35 +1295,31 @@ extern "C" af3d_status af3d_adjoint(af3d_ctx *c, long steps, long ckpt_every, do
   for (int f = 0; f < nf; f++) J[f] = sums[2 * f + 1] > 0.0 ? sums[2 * f] / sums[2 * f + 1] : 0.0;
 
   if (want_grad && n > 0) {
+    // every step's start time on the device (set by device-side copies, the host runs ahead)
+    double *t_dev = nullptr;
+    AF3D_CUDA(cudaMalloc((void **)&t_dev, sizeof(double) * (steps + 1)));
+    buf.owned.push_back(t_dev);
+    AF3D_CUDA(cudaMemcpyAsync(t_dev, t_start.data(), sizeof(double) * (steps + 1), cudaMemcpyHostToDevice, c->st));
     launch_adj_seed(c->L(), c->cur, adjA, c->d, c->fl_cur, dsc);
     for (long seg = (steps - 1) / ckpt_every; steps > 0 && seg >= 0; seg--) {
       const long k0 = seg * ckpt_every, k1 = std::min(steps, k0 + ckpt_every);
-      // recompute the segment, keeping every step's starting state
-      launch_state_copy(c->L(), c->cur, ckpt[seg], false);
-      c->look = false;   // the restored state has not been predicted
-      s = set_device_time(c, t_start[k0]);
-      if (s) return s;
-      const ContactLists own_lists = c->lists;
-      for (long k = k0; k < k1; k++) {
-        launch_state_copy(c->L(), c->cur, tape[k - k0], true);
-        c->lists = tape_lists[k - k0];
-        enqueue_fused_step(c, false, true, k + 1 < k1);
-        c->lists = own_lists;
-        s = copy_torque(c, tape[k - k0], true);
-        if (s) return s;
+      // recompute the segment into the tape (the last one was taped by the forward run)
+      if (seg != seg_last) {
+        launch_state_copy(c->L(), c->cur, ckpt[seg], false);
+        c->look = false;   // the restored state has not been predicted
+        AF3D_CUDA(cudaMemcpyAsync(&c->d->time, t_dev + k0, sizeof(double), cudaMemcpyDeviceToDevice, c->st));
+        for (long k = k0; k < k1; k++) taped_step(k, k0, k1);
       }
       // then each step backwards: its cell structure again, its torques from the tape
       for (long k = k1 - 1; k >= k0; k--) {
         launch_state_copy(c->L(), c->cur, tape[k - k0], false);
-        s = copy_torque(c, tape[k - k0], false);
-        if (s) return s;
-        s = set_device_time(c, t_start[k]);
-        if (s) return s;
+        AF3D_CUDA(cudaMemcpyAsync(&c->d->time, t_dev + k, sizeof(double), cudaMemcpyDeviceToDevice, c->st));
         enqueue_step_cells(c);
         AF3D_CUDA(cudaMemsetAsync(acc.p[0], 0, sizeof(double) * kAccPlanes * n, c->st));   // one block
-        launch_adj_forces_lists(c->L(), c->cur, adjA, adjB, acc, rb, c->d, c->fl_cur, c->nbr, c->cull,
-                                c->cells.start, c->cells.perm, tape_lists[k - k0], pgr);
-        launch_adj_predict(c->L(), c->cur, tape[k - k0], adjA, adjB, acc, rb, c->d, c->fl_cur);
+        const Planes Pk = with_tape_torque(c->cur, tape[k - k0]);
+        launch_adj_forces_lists(c->L(), Pk, adjA, adjB, acc, rb, c->d, c->fl_cur, c->nbr, c->cull, c->cells.start,
+                                c->cells.perm, tape_lists[k - k0], pgr);
+        launch_adj_predict(c->L(), Pk, tape[k - k0], adjA, adjB, acc, rb, c->d, c->fl_cur);
         std::swap(adjA, adjB);
       }
     }
