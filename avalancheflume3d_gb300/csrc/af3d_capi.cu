@@ -9,6 +9,7 @@
 // Device-side checks raise bits in a status word that af3d_step() and af3d_get_status() read
 // back; nothing calls exit().
 #include <algorithm>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -1212,17 +1213,19 @@ extern "C" af3d_status af3d_adjoint(af3d_ctx *c, long steps, long ckpt_every, do
   // checkpoints open every segment but the last, which the forward run tapes itself
   const long nck = steps > 0 ? (steps - 1) / ckpt_every : 0;
   AdjBuffers buf;
-  Planes state0{}, fin{}, adjA{}, adjB{}, acc{}, rb{};
+  Planes state0{}, fin{}, adjA{}, adjB{}, acc{}, rb{}, rnext{};
   std::vector<Planes> ckpt(nck), tape(want_grad ? std::min(ckpt_every, std::max<long>(steps, 1)) : 0);
   std::vector<ContactLists> tape_lists(tape.size());
+  std::vector<NbrRec *> tape_rec(tape.size());
   cudaError_t e = buf.planes(kAdjPlanes + 12, n, state0);   // with the sphere centres
   if (e == cudaSuccess) e = buf.planes(kAdjPlanes + 12, n, fin);
   for (long k = 0; k < nck && e == cudaSuccess && want_grad; k++) e = buf.planes(kAdjPlanes, n, ckpt[k]);
   if (!tape.empty() && e == cudaSuccess) {
-    // one block for the tape: per step its state, torque sums, item lists and list counts
+    // one block for the tape: per step its starting state and torque sums (27 planes), its
+    // clump records, item lists and list counts
     const size_t m = (size_t)std::max<long>(n, 1);
-    const size_t slot =
-        (sizeof(double) * (kAdjPlanes + 3) * m + (sizeof(unsigned) * kListCap + sizeof(int)) * m + 255) & ~(size_t)255;
+    const size_t slot = (sizeof(double) * (kAdjPlanes + 3) * m + sizeof(NbrRec) * m +
+                         (sizeof(unsigned) * kListCap + sizeof(int)) * m + 255) & ~(size_t)255;
     char *base = nullptr;
     e = cudaMalloc((void **)&base, slot * tape.size());
     if (e == cudaSuccess) {
@@ -1230,8 +1233,10 @@ extern "C" af3d_status af3d_adjoint(af3d_ctx *c, long steps, long ckpt_every, do
       for (size_t k = 0; k < tape.size(); k++) {
         double *pl = reinterpret_cast<double *>(base + slot * k);
         for (int i = 0; i < NPLANES; i++) tape[k].p[i] = i < kAdjPlanes + 3 ? pl + (size_t)i * m : nullptr;
-        tape_lists[k].items = reinterpret_cast<unsigned *>(pl + (size_t)(kAdjPlanes + 3) * m);
+        tape_rec[k] = reinterpret_cast<NbrRec *>(pl + (size_t)(kAdjPlanes + 3) * m);
+        tape_lists[k].items = reinterpret_cast<unsigned *>(tape_rec[k] + m);
         tape_lists[k].cnt = reinterpret_cast<int *>(tape_lists[k].items + (size_t)kListCap * m);
+        tape_lists[k].ovf = nullptr;
       }
     }
   }
@@ -1239,35 +1244,58 @@ extern "C" af3d_status af3d_adjoint(af3d_ctx *c, long steps, long ckpt_every, do
   if (want_grad && e == cudaSuccess) e = buf.planes(kAdjPlanes, n, adjB);
   if (want_grad && e == cudaSuccess) e = buf.planes(kAccPlanes, n, acc);
   if (want_grad && e == cudaSuccess) e = buf.planes(kRbPlanes, n, rb);
-  // per flume f: dsc[2 f], dsc[2 f + 1] the objective sums, pgr[6 f .. 6 f + 5] the parameter adjoints
+  if (want_grad && e == cudaSuccess) e = buf.planes(9, n, rnext);
+  // per flume f: dsc[2 f], dsc[2 f + 1] the objective sums, pgr[6 f .. 6 f + 5] the parameter
+  // adjoints; then per step: its list overflow flag (int), its start and end times (a pair)
   const size_t nsc = (size_t)8 * nf;
   double *dsc = nullptr;
-  if (e == cudaSuccess) e = cudaMalloc((void **)&dsc, sizeof(double) * nsc);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&dsc, sizeof(double) * (nsc + 3 * (size_t)(steps + 1)));
   if (e == cudaSuccess) buf.owned.push_back(dsc);
   if (e != cudaSuccess) return fail(AF3D_ERR_NOMEM, std::string("adjoint buffers: ") + cudaGetErrorString(e));
   double *pgr = dsc + 2 * nf;
-  AF3D_CUDA(cudaMemsetAsync(dsc, 0, sizeof(double) * nsc, c->st));
+  double *t_pair = dsc + nsc;   // [steps + 1][2]: {time, time_prev} during step k
+  int *ovf = reinterpret_cast<int *>(t_pair + 2 * (size_t)(steps + 1));
+  AF3D_CUDA(cudaMemsetAsync(dsc, 0, sizeof(double) * (nsc + 3 * (size_t)(steps + 1)), c->st));
+
+  // The context's own record buffers, item lists and torque planes, put back on every exit.
+  struct OwnPointers {
+    af3d_ctx *c;
+    NbrRec *nbr, *nbr_next;
+    ContactLists lists;
+    double *tq[3];
+    void restore() {
+      c->nbr = nbr;
+      c->nbr_next = nbr_next;
+      c->lists = lists;
+      for (int q = 0; q < 3; q++) c->cur.p[TX + q] = tq[q];
+    }
+    ~OwnPointers() { restore(); }
+  } own{c, c->nbr, c->nbr_next, c->lists, {c->cur.p[TX], c->cur.p[TX + 1], c->cur.p[TX + 2]}};
 
   // Forward: the start-up force pass (a_i of the first step), then `steps` steps keeping the
   // slot order, the state saved every ckpt_every steps.
   const double t_init = c->time, dt = c->sys[0].dt;
   launch_state_copy(c->L(), c->cur, state0, true, true);
   enqueue_startup_pass(c);
+  c->look = false;   // records of a previous run's look-ahead are stale now
   swap_accel_planes(c->cur);
   swap_accel_planes(c->alt);
   // The last segment's steps record their tape slots here (the reverse starts with them).
   const long seg_last = steps > 0 ? (steps - 1) / ckpt_every : 0, k_last = seg_last * ckpt_every;
-  const ContactLists own_lists = c->lists;
-  const Planes own_cur = c->cur;
-  // Step k of a segment starting at k0, its starting state, item lists and torque sums into its
-  // tape slot (a kept-order step neither swaps nor reallocates the plane sets).
+  // Step k of a segment [k0, k1) into its tape slot: its starting state, its clump records
+  // (written by the previous pass's look-ahead, or by this step's predictor), item lists, list
+  // counts and torque sums.  A kept-order step neither swaps nor reallocates the plane sets, and
+  // the record buffers only swap, so pointing them at the tape is enough.
   auto taped_step = [&](long k, long k0, long k1) {
     launch_state_copy(c->L(), c->cur, tape[k - k0], true);
+    if (!c->look) c->nbr = tape_rec[k - k0];
+    if (k + 1 < k1) c->nbr_next = tape_rec[k + 1 - k0];
     c->lists = tape_lists[k - k0];
+    c->lists.ovf = ovf + k;
     c->cur = with_tape_torque(c->cur, tape[k - k0]);
     enqueue_fused_step(c, false, true, k + 1 < k1);
-    for (int q = 0; q < 3; q++) c->cur.p[TX + q] = own_cur.p[TX + q];
-    c->lists = own_lists;
+    for (int q = 0; q < 3; q++) c->cur.p[TX + q] = own.tq[q];
+    c->lists = own.lists;
   };
   std::vector<double> t_start(steps + 1);
   double t = t_init;
@@ -1277,16 +1305,20 @@ extern "C" af3d_status af3d_adjoint(af3d_ctx *c, long steps, long ckpt_every, do
       taped_step(k, k_last, steps);
     } else {
       if (want_grad && k % ckpt_every == 0) launch_state_copy(c->L(), c->cur, ckpt[k / ckpt_every], true);
+      if (want_grad && k + 1 == k_last) c->nbr_next = tape_rec[0];   // the taped segment's first records
       enqueue_fused_step(c, false, false, k + 1 < steps);   // the last pass does not look ahead
     }
     t = t + dt;
   }
+  own.restore();
   t_start[steps] = t;
   c->time = t;
   launch_state_copy(c->L(), c->cur, fin, true, true);
   launch_adj_objective(c->L(), c->cur, c->d, c->fl_cur, dsc);
   std::vector<double> sums((size_t)2 * nf);
+  std::vector<int> ovf_h(steps + 1, 0);
   AF3D_CUDA(cudaMemcpyAsync(sums.data(), dsc, sizeof(double) * 2 * nf, cudaMemcpyDeviceToHost, c->st));
+  AF3D_CUDA(cudaMemcpyAsync(ovf_h.data(), ovf, sizeof(int) * (steps + 1), cudaMemcpyDeviceToHost, c->st));
   int flags = 0;
   af3d_status s = read_status(c, &flags);
   if (s) return s;
@@ -1295,29 +1327,53 @@ extern "C" af3d_status af3d_adjoint(af3d_ctx *c, long steps, long ckpt_every, do
   for (int f = 0; f < nf; f++) J[f] = sums[2 * f + 1] > 0.0 ? sums[2 * f] / sums[2 * f + 1] : 0.0;
 
   if (want_grad && n > 0) {
-    // every step's start time on the device (set by device-side copies, the host runs ahead)
-    double *t_dev = nullptr;
-    AF3D_CUDA(cudaMalloc((void **)&t_dev, sizeof(double) * (steps + 1)));
-    buf.owned.push_back(t_dev);
-    AF3D_CUDA(cudaMemcpyAsync(t_dev, t_start.data(), sizeof(double) * (steps + 1), cudaMemcpyHostToDevice, c->st));
+    // every step's times on the device (set by device-side copies, the host runs ahead): step k
+    // runs at time t_start[k + 1] after its clock advance, with time_prev t_start[k]
+    std::vector<double> tp(2 * (size_t)(steps + 1), 0.0);
+    for (long k = 0; k < steps; k++) {
+      tp[2 * k] = t_start[k + 1];
+      tp[2 * k + 1] = t_start[k];
+    }
+    static_assert(offsetof(DevScalars, time_prev) == offsetof(DevScalars, time) + sizeof(double), "time pair");
+    AF3D_CUDA(cudaMemcpyAsync(t_pair, tp.data(), sizeof(double) * tp.size(), cudaMemcpyHostToDevice, c->st));
     launch_adj_seed(c->L(), c->cur, adjA, c->d, c->fl_cur, dsc);
+    Planes rnext_src = fin;   // R1 of each segment's last step: the next segment's starting R
     for (long seg = (steps - 1) / ckpt_every; steps > 0 && seg >= 0; seg--) {
       const long k0 = seg * ckpt_every, k1 = std::min(steps, k0 + ckpt_every);
       // recompute the segment into the tape (the last one was taped by the forward run)
       if (seg != seg_last) {
+        for (int q = 0; q < 9; q++)   // tape slot 0 still holds segment seg + 1's starting state
+          AF3D_CUDA(cudaMemcpyAsync(rnext.p[q], tape[0].p[R00 + q], sizeof(double) * n, cudaMemcpyDeviceToDevice,
+                                    c->st));
+        for (int q = 0; q < 9; q++) rnext_src.p[R00 + q] = rnext.p[q];
         launch_state_copy(c->L(), c->cur, ckpt[seg], false);
         c->look = false;   // the restored state has not been predicted
-        AF3D_CUDA(cudaMemcpyAsync(&c->d->time, t_dev + k0, sizeof(double), cudaMemcpyDeviceToDevice, c->st));
+        AF3D_CUDA(cudaMemcpyAsync(&c->d->time, t_pair + 2 * k0 + 1, sizeof(double), cudaMemcpyDeviceToDevice,
+                                  c->st));
         for (long k = k0; k < k1; k++) taped_step(k, k0, k1);
+        own.restore();
+        AF3D_CUDA(cudaMemcpyAsync(ovf_h.data() + k0, ovf + k0, sizeof(int) * (k1 - k0), cudaMemcpyDeviceToHost,
+                                  c->st));
+        AF3D_CUDA(cudaStreamSynchronize(c->st));
       }
-      // then each step backwards: its cell structure again, its torques from the tape
+      // then each step backwards from its tape slot: records, lists, torque sums, and R1 (the
+      // next step's starting R).  A step whose lists overflowed rebuilds its cell structure for
+      // the per-clump walk of the overflowed clumps.
       for (long k = k1 - 1; k >= k0; k--) {
-        launch_state_copy(c->L(), c->cur, tape[k - k0], false);
-        AF3D_CUDA(cudaMemcpyAsync(&c->d->time, t_dev + k, sizeof(double), cudaMemcpyDeviceToDevice, c->st));
-        enqueue_step_cells(c);
+        AF3D_CUDA(cudaMemcpyAsync(&c->d->time, t_pair + 2 * k, 2 * sizeof(double), cudaMemcpyDeviceToDevice, c->st));
+        Planes Pk = with_tape_torque(c->cur, tape[k - k0]);
+        const Planes &r1 = k + 1 < k1 ? tape[k + 1 - k0] : rnext_src;
+        for (int q = 0; q < 9; q++) Pk.p[R00 + q] = r1.p[R00 + q];
+        const NbrRec *rec = tape_rec[k - k0];
+        if (ovf_h[k]) {
+          launch_state_copy(c->L(), c->cur, tape[k - k0], false);
+          AF3D_CUDA(cudaMemcpyAsync(&c->d->time, t_pair + 2 * k + 1, sizeof(double), cudaMemcpyDeviceToDevice,
+                                    c->st));
+          enqueue_step_cells(c);   // the same records again, and the cells
+          rec = c->nbr;
+        }
         AF3D_CUDA(cudaMemsetAsync(acc.p[0], 0, sizeof(double) * kAccPlanes * n, c->st));   // one block
-        const Planes Pk = with_tape_torque(c->cur, tape[k - k0]);
-        launch_adj_forces_lists(c->L(), Pk, adjA, adjB, acc, rb, c->d, c->fl_cur, c->nbr, c->cull, c->cells.start,
+        launch_adj_forces_lists(c->L(), Pk, adjA, adjB, acc, rb, c->d, c->fl_cur, rec, c->cull, c->cells.start,
                                 c->cells.perm, tape_lists[k - k0], pgr);
         launch_adj_predict(c->L(), Pk, tape[k - k0], adjA, adjB, acc, rb, c->d, c->fl_cur);
         std::swap(adjA, adjB);
@@ -1360,6 +1416,7 @@ extern "C" af3d_status af3d_adjoint(af3d_ctx *c, long steps, long ckpt_every, do
   c->sorted = false;
   c->records_valid = false;
   c->cells_valid = false;
+  c->look = false;
   c->since_sort = kResortEvery;
   c->cc += steps;
   flags = 0;

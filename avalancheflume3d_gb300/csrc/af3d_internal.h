@@ -111,11 +111,14 @@ struct DevScalars {
 // Per-clump item lists of one force pass, from the list phase to the force phase of the force
 // kernel: entry e of slot s at items[e * n + s] (an item is a boundary (routine, sphere) or a
 // particle (partner slot, sph_id) contact).  With cnt, the pass also records each clump's list
-// layout there (pack_list_counts), which lets the adjoint reverse the pass from the same lists.
+// layout there (pack_list_counts), which lets the adjoint reverse the pass from the same lists,
+// and with ovf sets *ovf when any clump's lists overflowed (its contacts then ran by the
+// per-clump walk, which needs the pass's cell structure).
 constexpr int kListCap = 32;
 struct ContactLists {
   unsigned *items;   // [kListCap][n]
   int *cnt;          // [n] or null
+  int *ovf;          // or null
 };
 
 // A clump's list layout as one int: -1 when its lists overflowed, else the item count | the

@@ -75,14 +75,14 @@ def parse_args():
     p.add_argument("--adjoint-steps", type=int, default=1000,
                    help="steps of the adjoint measurement (0 skips it)")
     p.add_argument("--adjoint-ckpt", type=int, default=1000,
-                   help="checkpoint interval of the adjoint (its tape, ~350 B per clump and step, holds "
+                   help="checkpoint interval of the adjoint (its tape, 540 B per clump and step, holds "
                         "this many steps; at the default the whole run fits and nothing is recomputed)")
     p.add_argument("--adjoint-batch", type=int, default=64,
                    help="parameter samples of the batched (calibration) adjoint (0 skips it)")
     p.add_argument("--adjoint-batch-steps", type=int, default=200)
-    p.add_argument("--adjoint-batch-ckpt", type=int, default=200,
+    p.add_argument("--adjoint-batch-ckpt", type=int, default=100,
                    help="checkpoint interval of the batched adjoint (its tape holds this many steps "
-                        "of all samples: 146 GB at the defaults)")
+                        "of all samples: 113 GB at the defaults)")
     p.add_argument("--trace-contacts", type=int, default=0,
                    help="print active contacts every this many pre-roll steps (diagnostic)")
     return p.parse_args()

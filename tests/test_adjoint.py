@@ -260,3 +260,51 @@ def test_ensemble_adjoint_equals_each_flume_alone(af3d):
             a, b = ens[key][lo:hi], one[key]
             assert np.allclose(a, b, rtol=1e-9, atol=1e-12 * float(np.abs(b).max())), (f, key)
         lo = hi
+
+
+def test_adjoint_with_overflowed_contact_lists(af3d, base, oracle, tangent):
+    """Five clumps piled almost on one spot give a clump more sphere contacts than its item lists
+    hold (32), every step: its contacts run by the per-clump walk in the forward pass, and the
+    reverse rebuilds that step's cell structure for it.  Checked against the tangent-linear model
+    like the regular run (to 1e-7), with the overflow itself checked on the initial state."""
+    from oracle.pyoracle import CELL_PAR, PARTICLE, SYSTEM_PAR, rotate_slope, sphere_centres, state_tangent
+    _, sys, fun, pp0 = base
+    pp = pp0.copy()
+    rmax = float(sys["rmax"])
+    i0 = N - 40   # inside the dense block on the bed
+    rng = np.random.default_rng(23)
+    pile = np.arange(i0 + 1, i0 + 5)
+    pp["rr"][pile] = pp["rr"][i0] + (rng.random((len(pile), 3)) - 0.5) * 0.6 * rmax
+    sphere_centres(pp)
+    rotate_slope(pp, sys)
+    s = pp["rr_s"]
+    d = np.linalg.norm(s[i0][:, None, None, :] - s[np.arange(N) != i0][None, :, :, :], axis=-1)
+    assert int(np.sum(d < 2.0 * pp["radius"][i0])) > 40
+    steps = 40
+    out = _adjoint(af3d, sys, fun, pp, steps=steps, ckpt=15)
+    rng = np.random.default_rng(29)
+    names = list(out["params"])
+    dsys = np.zeros(tangent.ndirs, dtype=SYSTEM_PAR)
+    for k, name in enumerate(names):
+        dsys[k][name] = float(sys[name])
+    dr, dphi = rng.standard_normal((N, 3)) * rmax, rng.standard_normal((N, 3))
+    dv, dw = rng.standard_normal((N, 3)) * 10.0, rng.standard_normal((N, 3)) * 30.0
+    dpp = np.zeros((tangent.ndirs, N), dtype=PARTICLE)
+    dpp[6] = state_tangent(pp, sys, dr=dr, dphi=dphi)
+    dpp[7] = state_tangent(pp, sys, dv=dv, dw=dw)
+    cp = np.zeros((), dtype=CELL_PAR)
+    cp["ntags"] = 128
+    cp["rr_max"], cp["rr_min"] = oracle.cell_dim(pp, sys)
+    s8 = sys.copy()
+    s8["rmax"] *= 8.0
+    oracle.grid_from_bbox(cp, s8)
+    J, dJ, _ = tangent.run(sys, fun, cp, pp, steps, dsys=dsys, dpp=dpp)
+    dR = np.stack([dpp[6]["Rmatx"], dpp[6]["Rmaty"], dpp[6]["Rmatz"]], 1)
+    adj = [out["params"][k] * float(sys[k]) for k in names]
+    adj.append(float(np.sum(out["r0"] * dr) + np.sum(out["R0"] * dR)))
+    adj.append(float(np.sum(out["v0"] * dv) + np.sum(out["w0"] * dw)))
+    adj = np.array(adj)
+    assert out["J"] == pytest.approx(J, rel=1e-12)
+    scale = float(np.abs(dJ).max())
+    bad = [(k, adj[k], dJ[k]) for k in range(8) if abs(adj[k] - dJ[k]) > 1e-7 * max(abs(dJ[k]), 1e-3 * scale)]
+    assert not bad, list(zip(adj, dJ))
