@@ -32,13 +32,14 @@ UNITS = [
     ("af3d_kernels.cu", "af3d_kernels", ["-fmad=false", "-Xptxas", "-v"]),
     ("af3d_kernels.cu", "af3d_kernels_fast", ["-fmad=true", "-DAF3D_FAST", "-Xptxas", "-v"]),
     ("af3d_adjoint.cu", "af3d_adjoint", ["-fmad=false"]),
+    ("af3d_adjoint_rot.cu", "af3d_adjoint_rot", ["-fmad=true"]),
     ("af3d_cells.cu", "af3d_cells", []),
     ("af3d_capi.cu", "af3d_capi", []),
     ("af3d_peaks.cu", "af3d_peaks", []),
 ]
 HOST_UNITS = [("af3d_hostio.cpp", "af3d_hostio", ["-O2", "-ffp-contract=off"])]
 
-HEADERS = ["af3d_internal.h", "af3d_physics.cuh", "af3d_cellwalk.cuh"]
+HEADERS = ["af3d_internal.h", "af3d_physics.cuh", "af3d_cellwalk.cuh", "af3d_adjoint.cuh"]
 
 
 def _run(cmd: list[str]) -> str:

@@ -227,8 +227,52 @@ def run_reference(args):
             "config": config_dict(args, cfg, {"cpu_threads": threads}),
             "cpu_baseline": {"value": value, "unit": "clump-steps/s", "cores": threads, "kind": "port",
                              "sample": sample},
-            "e2e": {"value": value, "unit": "clump-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": value, "unit": "clump-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "reference_gpu": measure_reference_gpu(args, sys_, fun, pp)}
     print(json.dumps(line), flush=True)
+
+
+def measure_reference_gpu(args, sys_, fun, pp):
+    """The reference's OWN device kernels (its *_dev twins, compiled from its sources into
+    oracle/_ref/dev) in avalanche_dev.cu:636-693's sequence on cuda:0, on the full workload:
+    the start-up pass of avalanche_dev.cu:335-360, W + K steps each checked before launch (the
+    reference's cell binning checks no bounds), then the same W + K steps again from a snapshot,
+    the last K timed with CUDA events.  31 launches per step, 256 threads per block; the grid
+    as cell_dim derives it, with 16 slots per cell."""
+    try:
+        import torch
+        if not torch.cuda.is_available():
+            return {"unavailable": "no CUDA device"}
+        from oracle import ref_dev
+        if not ref_dev.available():
+            return {"unavailable": "reference device kernels not built (the reference tree was absent at build time)"}
+        from oracle.pyoracle import Oracle, grid_for
+        cp = grid_for(pp, sys_, 16, Oracle())
+        stream = torch.cuda.current_stream()
+        run = ref_dev.RefDeviceRun(sys_, fun, cp, pp, stream=stream.cuda_stream)
+        try:
+            run.seed_accel()
+            snap = run.snapshot()
+            run.step_checked(args.warmup + args.steps)
+            run.restore(snap)
+            run.step(args.warmup)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            l0 = run.launches
+            e0.record(stream)
+            run.step(args.steps)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            launches = run.launches - l0
+        finally:
+            run.close()
+        return {"value": args.n * args.steps / (ms / 1e3), "unit": "clump-steps/s", "ms_per_step": ms / args.steps,
+                "steps": args.steps, "warmup": args.warmup, "launches_per_step": launches / args.steps,
+                "kernels": "the reference's *_dev kernels, nvcc -O2 for sm_103a, driven in "
+                           "avalanche_dev.cu:636-693's order (friction: the device variant, force_part.cu:487)"}
+    except Exception as e:   # the CPU reference line stands on its own
+        return {"unavailable": "%s: %s" % (type(e).__name__, e)}
 
 
 def measure_ensemble(args, stream):

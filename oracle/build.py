@@ -14,6 +14,14 @@ Three libraries:
   plus ``-fPIC`` and ``-ffp-contract=off``, linked with ``ref_shim.cu``.  Built
   only where the reference tree exists; used to pin the restatement and to
   generate ``tests/golden/``.  Nothing is copied out of the reference tree.
+* ``oracle/_ref/dev/*.cubin``: the reference's OWN device kernels (the ``*_dev``
+  twins the reference's GPU driver ``avalanche_dev.cu:636-693`` launches), one
+  module per source file, compiled from the same unmodified sources with the
+  Makefile's ``-O2`` (MakeAvalancheDev.mk) for sm_103a.  Built only where the
+  reference tree exists; the modules travel to the GPU machine, where
+  ``oracle/ref_dev.py`` loads them through the CUDA driver and runs the
+  reference's device step sequence (a GPU baseline and a parity check of the
+  engine against the reference's own kernels).
 
 Run ``python oracle/build.py`` or call :func:`build`.
 """
@@ -39,6 +47,14 @@ REF_UNITS = [
     "generate_particles", "get_accel", "init_Verlet", "place_particles", "rannew64",
     "rotate_vectors", "set_initial_velocity",
 ]
+
+
+# Reference translation units holding the device kernels of avalanche_dev.cu's step loop.
+REF_DEV_UNITS = [
+    "init_Verlet", "rotate_vectors", "clear_forces", "cells", "force_hop", "force_funnel", "force_walls",
+    "force_part", "force_flume", "get_accel", "finish_Verlet",
+]
+REF_DEV_DIR = os.path.join(REF_DIR, "dev")
 
 
 def _run(cmd: list[str]) -> None:
@@ -103,12 +119,32 @@ def build_ref(force: bool = False) -> str | None:
     return REF_SO
 
 
+def build_ref_dev(force: bool = False) -> str | None:
+    """The reference's device kernels as cubins (MakeAvalancheDev.mk's ``nvcc -c -O2``, here
+    ``-cubin`` for sm_103a), one per source file, into oracle/_ref/dev/."""
+    if not reference_available():
+        return None
+    os.makedirs(REF_DEV_DIR, exist_ok=True)
+    hdr = os.path.join(REFERENCE_DIR, "cabecera.hu")
+    jobs = []
+    for u in REF_DEV_UNITS:
+        src = os.path.join(REFERENCE_DIR, u + ".cu")
+        out = os.path.join(REF_DEV_DIR, u + ".cubin")
+        if force or not _newer(out, [src, hdr, __file__]):
+            jobs.append(["nvcc", "-cubin", "-O2", "-gencode", "arch=compute_103a,code=sm_103a", "-I", REFERENCE_DIR,
+                         "-o", out, src])
+    with ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 2)) as ex:
+        list(ex.map(_run, jobs))
+    return REF_DEV_DIR
+
+
 def build(force: bool = False) -> None:
     with ThreadPoolExecutor(max_workers=2) as ex:
         jobs = [ex.submit(build_oracle, force), ex.submit(build_tangent, force)]
         for j in jobs:
             j.result()
     build_ref(force)
+    build_ref_dev(force)
 
 
 if __name__ == "__main__":
