@@ -31,10 +31,15 @@ struct LawBar {
   double comp, km, gm, mu;
 };
 
-// Reverse of contact_law (af3d_physics.cuh) for a contact that produced a force, given the
-// adjoint fb of that force.  The law is re-evaluated in the same operations to take the same
-// branches.
-__device__ __forceinline__ void contact_law_rev(const ContactIn &ci, double dt, V3 fb, LawBar &lb) {
+// The contact law (contact_law, af3d_physics.cuh, exact mode) and its reverse in one pass.  The
+// forward part repeats contact_law's operations in its order (same branches, same force f); it
+// returns false when the contact produced no force.  Then, with the adjoints fb_tot, tb_tot of
+// the owner's force and torque sums and the lever e (torque += e x f), it forms the adjoints of
+// the law's inputs (lb) and adds that of the lever to e_b.  The derivative needs no bit-exact
+// quotient: one reciprocal of |vt| serves all of it.
+__device__ __forceinline__ bool contact_law_fwd_rev(const ContactIn &ci, double dt, V3 fb_tot, V3 tb_tot, V3 e,
+                                                    V3 &e_b, LawBar &lb) {
+  // forward, as contact_law
   const V3 dv = ci.dvvc, n = ci.n;
   const double vn = dv.x * n.x + dv.y * n.y + dv.z * n.z;
   V3 vt;
@@ -48,6 +53,11 @@ __device__ __forceinline__ void contact_law_rev(const ContactIn &ci, double dt, 
   tv.z = vt.z / vt_mag;
   const double vt_sig = dv.x * tv.x + dv.y * tv.y + dv.z * tv.z;
   const double normal = ci.km * ci.comp + ci.gm * (-vn);
+  if (ci.gate ? (normal <= 0.0) : !(normal > 0.0)) return false;
+  V3 f;
+  f.x = -normal * n.x;
+  f.y = -normal * n.y;
+  f.z = -normal * n.z;
   double xi = dt * vt_sig;
   const bool zeroed = ci.cns * normal < fabs(xi);
   if (zeroed) xi = 0.0;
@@ -56,41 +66,59 @@ __device__ __forceinline__ void contact_law_rev(const ContactIn &ci, double dt, 
   const double fsdt = 1.0e12 * m * xi + 2.0e6 * m * xi_dot;
   const bool tang = vt_mag > 0.0;
   const bool coul = tang && (fabs(fsdt) > ci.mu * normal || (ci.xi0 && xi == 0.0));
-
+  double q1 = 0.0, q3 = 0.0;
+  if (tang) {
+    q1 = (coul ? 0.8 * ci.mu * normal : fsdt * vt.x) / vt_mag;
+    const double q2 = (coul ? m : fsdt * vt.y) / (coul ? q1 : vt_mag);
+    q3 = (coul ? dt : fsdt * vt.z) / (coul ? q2 : vt_mag);
+    if (coul) {
+      const double af = q1 / (1.0 + q3 * q3);
+      f.x += af * vt.x;
+      f.y += af * vt.y;
+      f.z += af * vt.z;
+    } else {
+      if (vt.x != 0.0) f.x += q1;
+      if (vt.y != 0.0) f.y += q2;
+      if (vt.z != 0.0) f.z += q3;
+    }
+  }
+  // reverse: F += f, T += e x f
+  const V3 fb = fb_tot + cross(tb_tot, e);
+  e_b += cross(f, tb_tot);
   double normal_b = -dot(fb, n);
   V3 n_b = (-normal) * fb;
   V3 dv_b = mk(0.0, 0.0, 0.0), vt_b = mk(0.0, 0.0, 0.0);
   double vtmag_b = 0.0, mu_b = 0.0;
   if (tang) {
+    const double ivt = 1.0 / vt_mag;
     if (coul) {
-      // af = 0.8 mu N / |vt|;  t0 = m / af;  r = dt / t0;  f += af / (1 + r^2) vt
-      const double af = 0.8 * ci.mu * normal / vt_mag;
-      const double r = dt / (m / af);
-      const double den = 1.0 + r * r;
-      const double af2 = af / den;
+      // af = 0.8 mu N / |vt| (q1);  r = dt / (m / af) (q3);  f += af / (1 + r^2) vt
+      const double af = q1, r = q3;
+      const double iden = 1.0 / (1.0 + r * r);
+      const double af2 = af * iden;
       const double af2_b = dot(fb, vt);
       vt_b += af2 * fb;
-      const double af_b = af2_b * (1.0 - r * r) / (den * den);
-      mu_b += af_b * 0.8 * normal / vt_mag;
-      normal_b += af_b * 0.8 * ci.mu / vt_mag;
-      vtmag_b -= af_b * af / vt_mag;
+      const double af_b = af2_b * (1.0 - r * r) * (iden * iden);
+      mu_b += af_b * 0.8 * normal * ivt;
+      normal_b += af_b * 0.8 * ci.mu * ivt;
+      vtmag_b -= af_b * af * ivt;
     } else {
       // f_i += fsdt vt_i / |vt| for every component with vt_i != 0
-      const double g = fsdt / vt_mag;
+      const double g = fsdt * ivt;
       double g_b = 0.0;
       if (vt.x != 0.0) { vt_b.x += g * fb.x; g_b += fb.x * vt.x; }
       if (vt.y != 0.0) { vt_b.y += g * fb.y; g_b += fb.y * vt.y; }
       if (vt.z != 0.0) { vt_b.z += g * fb.z; g_b += fb.z * vt.z; }
-      const double fsdt_b = g_b / vt_mag;
-      vtmag_b -= g_b * g / vt_mag;
+      const double fsdt_b = g_b * ivt;
+      vtmag_b -= g_b * g * ivt;
       if (!zeroed) {
         // fsdt = m xi (1e12 + 2e6 / dt), xi = dt vt_sig, vt_sig = dv . vt / |vt|
         const double xi_b = fsdt_b * (1.0e12 * m + 2.0e6 * m / dt);
         const double vtsig_b = dt * xi_b;
         dv_b += vtsig_b * tv;
         const V3 tv_b = vtsig_b * dv;
-        vt_b += (1.0 / vt_mag) * tv_b;
-        vtmag_b -= dot(tv_b, vt) / (vt_mag * vt_mag);
+        vt_b += ivt * tv_b;
+        vtmag_b -= dot(tv_b, vt) * (ivt * ivt);
       }
     }
     vt_b += vtmag_b * tv;   // |vt| = sqrt(vt . vt)
@@ -110,6 +138,7 @@ __device__ __forceinline__ void contact_law_rev(const ContactIn &ci, double dt, 
   lb.dv = dv_b;
   lb.n = n_b;
   lb.mu = mu_b;
+  return true;
 }
 
 // Adjoint accumulators of one clump's contact inputs.
@@ -150,21 +179,19 @@ __device__ __forceinline__ void pair_rev(V3 rl, V3 vl, V3 wl, V3 s1, double rad1
   any = false;
   ContactIn ci;
   if (!pair_input(rl, vl, wl, s1, rad1, massl, m, sm, c, xi0, ci)) return;
-  V3 f;
-  if (!contact_law(ci.dvvc, ci.n, ci.comp, ci.km, ci.gm, ci.mass_t, ci.mu, ci.cns, c.dt, ci.xi0, ci.gate, f))
-    return;
+  const V3 rrc = ci.rrc;
+  const V3 e_l = rrc - rl;
+  // F += f; T += e_l x f
+  V3 e_l_b = mk(0.0, 0.0, 0.0);
+  LawBar lb;
+  if (!contact_law_fwd_rev(ci, c.dt, fb_tot, tb_tot, e_l, e_l_b, lb)) return;
   any = true;
   const V3 sp = mk(m.s[3 * sm], m.s[3 * sm + 1], m.s[3 * sm + 2]);
-  const V3 rm = mk(m.rx, m.ry, m.rz), vm_lin = mk(m.vx, m.vy, m.vz), wm = mk(m.wx, m.wy, m.wz);
+  const V3 rm = mk(m.rx, m.ry, m.rz), wm = mk(m.wx, m.wy, m.wz);
   const V3 d = sp - s1;
   const double dist = sqrt(d.x * d.x + d.y * d.y + d.z * d.z);
-  const V3 n = ci.n, rrc = ci.rrc;
-  const V3 e_l = rrc - rl, e_m = rrc - rm;
-  // F += f; T += e_l x f
-  const V3 f_b = fb_tot + cross(tb_tot, e_l);
-  V3 e_l_b = cross(f, tb_tot);
-  LawBar lb;
-  contact_law_rev(ci, c.dt, f_b, lb);
+  const V3 n = ci.n;
+  const V3 e_m = rrc - rm;
   const double meff = 0.5 * (m.msph + massl);
   par.kappa_pp += lb.km * 0.5 * meff;
   par.gamma_pp += lb.gm * 0.5 * meff;
@@ -347,13 +374,10 @@ __device__ __forceinline__ void wall_rev(int rt, const Sph &o, const Consts &c, 
   if (!wall_geom(rt, o, c, rrc, n, comp, gate, touch, aux)) return;
   ContactIn ci;
   wall_input(o, rrc, n, comp, c, gate, ci);
-  V3 f;
-  if (!contact_law(ci.dvvc, ci.n, ci.comp, ci.km, ci.gm, ci.mass_t, ci.mu, ci.cns, c.dt, ci.xi0, ci.gate, f)) return;
   const V3 e = rrc - o.r;
-  const V3 f_b = fb_tot + cross(tb_tot, e);
-  V3 e_b = cross(f, tb_tot);
+  V3 e_b = mk(0.0, 0.0, 0.0);
   LawBar lb;
-  contact_law_rev(ci, c.dt, f_b, lb);
+  if (!contact_law_fwd_rev(ci, c.dt, fb_tot, tb_tot, e, e_b, lb)) return;
   par.kappa_pw += lb.km * 0.5 * o.mwall;
   par.gamma_pw += lb.gm * 0.5 * o.mwall;
   par.mu_pw += lb.mu;

@@ -152,16 +152,34 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
-def traffic_from_profile():
-    """DRAM bytes per launch of the force kernel from the committed ncu summary, if any."""
+def from_profile(key):
+    """A per-launch figure of the force kernel (``traffic_bytes_per_launch``,
+    ``fp64_flops_per_launch``) from the committed ncu summary, if any."""
     fn = os.path.join(ROOT, "profiles", "lists_forces_flume262k.txt")
     try:
         for line in open(fn):
-            if line.startswith("traffic_bytes_per_launch:"):
+            if line.startswith(key + ":"):
                 return float(line.split(":", 1)[1])
     except OSError:
         pass
     return None
+
+
+def traffic_from_profile():
+    return from_profile("traffic_bytes_per_launch")
+
+
+def fp64_line(peak, t_forces, mode):
+    """The force kernel's FP64 roofline: its flops per launch (2 DFMA + DADD + DMUL, counted by
+    ncu on the fast-mode kernel of this workload) over the event-timed kernel time, against the
+    DFMA microbenchmark peak."""
+    d = {"peak_tflops": peak, "peak_source": "measured DFMA microbenchmark", "unit": "TFLOP/s"}
+    flops = from_profile("fp64_flops_per_launch")
+    if flops and t_forces > 0 and mode == "fast":
+        d.update({"flops_per_launch": flops, "achieved_tflops": flops / t_forces / 1e12,
+                  "frac": flops / t_forces / 1e12 / peak if peak > 0 else None,
+                  "flops_source": "profiles/lists_forces_flume262k.txt"})
+    return d
 
 
 def cpu_sample_state(cfg, sys_, fun, pp, m, acc=None, anga=None):
@@ -591,7 +609,7 @@ def run_engine(args):
                          "peak_source": peak_kind, "traffic": traffic_from_profile(),
                          "algorithmic_bytes_per_launch": alg,
                          "kernel_ms": prof[names.index("fused_forces")], "note": "FP64-issue bound; see fp64"},
-            "fp64": {"peak_tflops": fp64.value, "peak_source": "measured DFMA microbenchmark"},
+            "fp64": fp64_line(fp64.value, t_forces, args.fp_mode),
             "phase_ms": {k: float(v) for k, v in zip(names, prof)},
             "ensemble": ens,
             "adjoint": adj,
