@@ -222,11 +222,12 @@ __device__ __forceinline__ void predict_state(V3 &r, V3 &v, V3 &w, V3 a, V3 al, 
     // from the Maclaurin series of sin(t)/t and (1 - cos t)/t^2 in t^2 = |dO|^2 (truncated
     // after t^8 and t^10: the first omitted terms are below 2^-53 of the sums), no square
     // root, sine or cosine.
+    // Horner form in t2 with the series' coefficients (1/6, 1/120, 1/5040, 1/362880 and
+    // 1/2, 1/24, 1/720, 1/40320, 1/3628800): four multiply-adds each.
     const double t2 = mag2;
-    const double A = 1.0 - t2 * (1.0 / 6.0) * (1.0 - t2 * (1.0 / 20.0) * (1.0 - t2 * (1.0 / 42.0) *
-                                                                            (1.0 - t2 * (1.0 / 72.0))));
-    const double Bq = 0.5 * (1.0 - t2 * (1.0 / 12.0) * (1.0 - t2 * (1.0 / 30.0) * (1.0 - t2 * (1.0 / 56.0) *
-                                                                                    (1.0 - t2 * (1.0 / 90.0)))));
+    const double A = 1.0 + t2 * (-1.0 / 6.0 + t2 * (1.0 / 120.0 + t2 * (-1.0 / 5040.0 + t2 * (1.0 / 362880.0))));
+    const double Bq =
+        0.5 + t2 * (-1.0 / 24.0 + t2 * (1.0 / 720.0 + t2 * (-1.0 / 40320.0 + t2 * (1.0 / 3628800.0))));
     const double cc = 1.0 - t2 * Bq;
     const V3 sv = mk(A * dO.x, A * dO.y, A * dO.z);
     const V3 bv = mk(Bq * dO.x, Bq * dO.y, Bq * dO.z);
@@ -292,6 +293,21 @@ __device__ __forceinline__ void predict_state(V3 &r, V3 &v, V3 &w, V3 a, V3 al, 
   w.z += dt * al.z;
   // sphere centres r + (radius/sqrt2) R (+-1,+-1,+-1) (init_Verlet.cu:130-142)
   const double pos = kFast ? rad * (1.0 / kROOT2) : rad / kROOT2;
+  if (kFast) {
+    // the four patterns from two shared sums per row: (a + c, b - c, c - a, -(b + c)) with
+    // a = x + y, b = x - y
+    auto row = [&](double r0, const V3 &R, double &s0, double &s1, double &s2, double &s3) {
+      const double a = R.x + R.y, b = R.x - R.y;
+      s0 = r0 + pos * (a + R.z);
+      s1 = r0 + pos * (b - R.z);
+      s2 = r0 + pos * (R.z - a);
+      s3 = r0 - pos * (b + R.z);
+    };
+    row(r.x, Rx, sp[0].x, sp[1].x, sp[2].x, sp[3].x);
+    row(r.y, Ry, sp[0].y, sp[1].y, sp[2].y, sp[3].y);
+    row(r.z, Rz, sp[0].z, sp[1].z, sp[2].z, sp[3].z);
+    return;
+  }
   sp[0] = mk(r.x + pos * (Rx.x + Rx.y + Rx.z), r.y + pos * (Ry.x + Ry.y + Ry.z), r.z + pos * (Rz.x + Rz.y + Rz.z));
   sp[1] = mk(r.x + pos * (Rx.x - Rx.y - Rx.z), r.y + pos * (Ry.x - Ry.y - Ry.z), r.z + pos * (Rz.x - Rz.y - Rz.z));
   sp[2] = mk(r.x + pos * (-Rx.x - Rx.y + Rx.z), r.y + pos * (-Ry.x - Ry.y + Ry.z),
