@@ -177,6 +177,7 @@ af3d_status push_params(af3d_ctx *c) {
     fl[f].sys.time = c->time;
     fl[f].fun = c->fun[f];
     fl[f].tant = c->sys[f].sint / c->sys[f].cost;
+    fl[f].c = make_consts(c->sys[f], c->fun[f], fl[f].tant, c->phase, c->variant, &c->d->time);
   }
   AF3D_CUDA(cudaMemcpyAsync(c->flumes, fl.data(), sizeof(DevFlume) * c->nflumes, cudaMemcpyHostToDevice, c->st));
   AF3D_CUDA(cudaMemcpyAsync(&c->d->time, &c->time, sizeof(double), cudaMemcpyHostToDevice, c->st));
@@ -553,6 +554,7 @@ af3d_status af3d_create_ensemble(int nflumes, const af3d_system_par *sys, const 
     fl[f].gridf = grid_floats(c->grid[f]);
     fl[f].pending = c->grid[f];
     fl[f].tant = c->sys[f].sint / c->sys[f].cost;
+    fl[f].c = make_consts(c->sys[f], c->fun[f], fl[f].tant, phase, c->variant, &c->d->time);
   }
   DevScalars ds;
   std::memset(&ds, 0, sizeof ds);

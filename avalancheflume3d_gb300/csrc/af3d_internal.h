@@ -68,6 +68,40 @@ struct Cells {
   long cap;         // buckets available (ncell_total + N must fit)
 };
 
+// Scalars of one flume's system_par / Funnel used by the force routines.  A single-flume
+// context passes them to the fused force kernel as a __grid_constant__ parameter (constant-bank
+// operands, no registers held); the clock is read through `tp` (it advances on the device).
+struct Consts {
+  double dt, hdt;
+  double mu_pp, kappa_pp, gamma_pp, cns_pp;
+  double mu_pw, kappa_pw, gamma_pw, cns_pw;
+  double sint, cost, dy2, side_x, side_y;
+  double sinfi, cosfi, tanfi;
+  double tant;     // sint / cost
+  double inv_dt;   // 1 / dt (fast mode)
+  const double *tp;   // the device clock, DevScalars::time
+  float cost_f, sint_f, tanfi_f, cosfi_f, dy2_f, side_y_f;   // FP32 copies for the culling gates
+  int phase, variant;
+};
+
+// The constants of a flume from its parameters (the same values the device loads).
+__host__ __device__ inline Consts make_consts(const af3d_system_par &s, const af3d_funnel &fun, double tant, int phase, int variant,
+                          const double *tp) {
+  Consts c;
+  c.dt = s.dt; c.hdt = s.hdt;
+  c.mu_pp = s.mu_pp; c.kappa_pp = s.kappa_pp; c.gamma_pp = s.gamma_pp; c.cns_pp = s.fr_fact_pp;
+  c.mu_pw = s.mu_pw; c.kappa_pw = s.kappa_pw; c.gamma_pw = s.gamma_pw; c.cns_pw = s.fr_fact_pw;
+  c.sint = s.sint; c.cost = s.cost; c.dy2 = s.dy2; c.side_x = s.side.x; c.side_y = s.side.y;
+  c.sinfi = fun.sinfi; c.cosfi = fun.cosfi; c.tanfi = fun.tanfi;
+  c.tant = tant;
+  c.inv_dt = 1.0 / s.dt;
+  c.tp = tp;
+  c.cost_f = (float)s.cost; c.sint_f = (float)s.sint; c.tanfi_f = (float)fun.tanfi; c.cosfi_f = (float)fun.cosfi;
+  c.dy2_f = (float)s.dy2; c.side_y_f = (float)s.side.y;
+  c.phase = phase; c.variant = variant;
+  return c;
+}
+
 // One flume of the context (a plain drop-in run has one; a batched ensemble has many).  Every
 // flume has its own system_par (friction, restitution, slope, ...), Funnel and cell grid; all
 // flumes share dt and advance in lockstep.
@@ -92,6 +126,7 @@ struct DevFlume {
   double          tant;       // sys.sint / sys.cost (force_flume.cu's tangent), set by the host
   unsigned long long bbox[8]; // re-grid scratch: ordered-int min/max of x, y, z, max vx, min vz
   af3d_cell_par   pending;    // grid derived by the last re-grid, committed when it fits
+  Consts          c;          // make_consts of sys, fun, tant and the context's phase/variant
 };
 
 // Per-context device scalars (one struct in global memory).
@@ -136,40 +171,6 @@ struct LookAhead {
   Cells cells;
   const long long *id;
 };
-
-// Scalars of one flume's system_par / Funnel used by the force routines.  A single-flume
-// context passes them to the fused force kernel as a __grid_constant__ parameter (constant-bank
-// operands, no registers held); the clock is read through `tp` (it advances on the device).
-struct Consts {
-  double dt, hdt;
-  double mu_pp, kappa_pp, gamma_pp, cns_pp;
-  double mu_pw, kappa_pw, gamma_pw, cns_pw;
-  double sint, cost, dy2, side_x, side_y;
-  double sinfi, cosfi, tanfi;
-  double tant;     // sint / cost
-  double inv_dt;   // 1 / dt (fast mode)
-  const double *tp;   // the device clock, DevScalars::time
-  float cost_f, sint_f, tanfi_f, cosfi_f, dy2_f, side_y_f;   // FP32 copies for the culling gates
-  int phase, variant;
-};
-
-// The constants of a flume from its parameters (the same values the device loads).
-__host__ __device__ inline Consts make_consts(const af3d_system_par &s, const af3d_funnel &fun, double tant, int phase, int variant,
-                          const double *tp) {
-  Consts c;
-  c.dt = s.dt; c.hdt = s.hdt;
-  c.mu_pp = s.mu_pp; c.kappa_pp = s.kappa_pp; c.gamma_pp = s.gamma_pp; c.cns_pp = s.fr_fact_pp;
-  c.mu_pw = s.mu_pw; c.kappa_pw = s.kappa_pw; c.gamma_pw = s.gamma_pw; c.cns_pw = s.fr_fact_pw;
-  c.sint = s.sint; c.cost = s.cost; c.dy2 = s.dy2; c.side_x = s.side.x; c.side_y = s.side.y;
-  c.sinfi = fun.sinfi; c.cosfi = fun.cosfi; c.tanfi = fun.tanfi;
-  c.tant = tant;
-  c.inv_dt = 1.0 / s.dt;
-  c.tp = tp;
-  c.cost_f = (float)s.cost; c.sint_f = (float)s.sint; c.tanfi_f = (float)fun.tanfi; c.cosfi_f = (float)fun.cosfi;
-  c.dy2_f = (float)s.dy2; c.side_y_f = (float)s.side.y;
-  c.phase = phase; c.variant = variant;
-  return c;
-}
 
 // Which force routines a boundary kernel applies, in the reference's call order.
 enum Routine : int {

@@ -662,7 +662,7 @@ __device__ __forceinline__ int block_contacts(BlockQueue &bq, long bbase, long s
     } else {
       // the owner's flume may differ from this thread's at a flume boundary of an ensemble
       const int of = flume[bbase + lo];
-      const Consts co = of == flume[s] ? c : load_consts(d, of);
+      const Consts &co = of == flume[s] ? c : d->flumes[of].c;
       r = contact(co, fs, tq);
     }
     bq.flag[jb] = (unsigned char)r;
@@ -1215,8 +1215,9 @@ __global__ void __launch_bounds__(kBlock, AF3D_FORCES_MINB) k_lists_forces(Plane
     __syncthreads();
     fused_body<WRITE_FT, true>(kc, P, out, d, flume, nbr, cull, start, order, lists, listed, lc, n, warm, la, sh);
   } else {
+    // the flume's constants read where they lie (a reference, not a register copy)
     const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    const Consts c = load_consts(d, flume[s < n ? s : n - 1]);
+    const Consts &c = d->flumes[flume[s < n ? s : n - 1]].c;
     const int listed = lists_body<false>(c, d, flume, nbr, cull, start, order, csort, lists, n,
                                          sh.pl[threadIdx.x >> 5], lc);
     __syncthreads();
