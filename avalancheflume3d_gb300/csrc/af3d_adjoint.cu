@@ -599,7 +599,7 @@ __global__ void __launch_bounds__(kAdjCoopBlock, AF3D_ADJ_MINB) k_adj_forces(Pla
   const long wbase = blockIdx.x * (long)blockDim.x + (threadIdx.x & ~31u);
   ParamBar par = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
   const int f = flume[sv];
-  const Consts c = load_consts(d, f);
+  const Consts &c = d->flumes[f].c;
   const af3d_cell_par g = d->flumes[f].grid;
   const long long off = d->flumes[f].cell_off;
   const NbrRec &me = nbr[sv];
@@ -632,7 +632,7 @@ __global__ void __launch_bounds__(kAdjCoopBlock, AF3D_ADJ_MINB) k_adj_forces(Pla
       const unsigned it = aq.il.items[j - aq.il.base[lo]][lo];
       const long os = wbase + lo;
       const int of = flume[os];
-      const Consts co = of == f ? c : load_consts(d, of);
+      const Consts &co = of == f ? c : d->flumes[of].c;
       ItemBar ib;
       ParamBar ipar = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};   // this item's; the lane's flume or the owner's
       const int k = adj_item(nbr[os], it, co, mk(aq.fb[0][lo], aq.fb[1][lo], aq.fb[2][lo]),
@@ -670,7 +670,10 @@ struct AdjBlock {
   int wsum[3][kAdjListBlock / 32];
 };
 
-__global__ void __launch_bounds__(kAdjListBlock) k_adj_forces_l(Planes P, Planes in, Planes out, Planes acc,
+#ifndef AF3D_ADJ_LMINB
+#define AF3D_ADJ_LMINB 1
+#endif
+__global__ void __launch_bounds__(kAdjListBlock, AF3D_ADJ_LMINB) k_adj_forces_l(Planes P, Planes in, Planes out, Planes acc,
                                                                Planes rb, DevScalars *d, const int *__restrict__ flume,
                                                                const NbrRec *__restrict__ nbr,
                                                                const CullRec *__restrict__ cull,
@@ -685,7 +688,7 @@ __global__ void __launch_bounds__(kAdjListBlock) k_adj_forces_l(Planes P, Planes
   const long sv = valid ? s : n - 1;
   ParamBar par = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
   const int f = flume[sv];
-  const Consts c = load_consts(d, f);
+  const Consts &c = d->flumes[f].c;
   const NbrRec &me = nbr[sv];
   Own o;
   o.r = mk(me.rx, me.ry, me.rz);
@@ -757,7 +760,7 @@ __global__ void __launch_bounds__(kAdjListBlock) k_adj_forces_l(Planes P, Planes
       const unsigned it = lists.items[(long)idx * n + bbase + lo];
       const long os = bbase + lo;
       const int of = flume[os];
-      const Consts co = of == f ? c : load_consts(d, of);
+      const Consts &co = of == f ? c : d->flumes[of].c;
       ItemBar itb;
       ParamBar ipar = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
       const int k = adj_item(nbr[os], it, co, mk(ab.fb[0][lo], ab.fb[1][lo], ab.fb[2][lo]),
