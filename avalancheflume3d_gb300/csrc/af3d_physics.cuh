@@ -570,6 +570,19 @@ __device__ __forceinline__ void get_accel_one(V3 f, V3 t, V3 v, V3 w, V3 Rx, V3 
     a.z = f.z / m - adrag * v.z - kGRAV;
   }
   V3 wb, tb, ab;
+  if (kFast && I.x == I.y && I.y == I.z && I.x > 0.0 && isfinite(I.x) && isfinite(w.x) && isfinite(w.y) &&
+      isfinite(w.z)) {
+    // Fast mode, isotropic inertia: the Euler term C w_b x w_b is zero (C = 0), so the body-frame
+    // spin is not formed; alpha = R (R^T T) / I.
+    tb.x = t.x * Rx.x + t.y * Ry.x + t.z * Rz.x;
+    tb.y = t.x * Rx.y + t.y * Ry.y + t.z * Rz.y;
+    tb.z = t.x * Rx.z + t.y * Ry.z + t.z * Rz.z;
+    ab = mk(tb.x * iI, tb.y * iI, tb.z * iI);
+    al.x = ab.x * Rx.x + ab.y * Rx.y + ab.z * Rx.z;
+    al.y = ab.x * Ry.x + ab.y * Ry.y + ab.z * Ry.z;
+    al.z = ab.x * Rz.x + ab.y * Rz.y + ab.z * Rz.z;
+    return;
+  }
   wb.x = w.x * Rx.x + w.y * Ry.x + w.z * Rz.x;
   wb.y = w.x * Rx.y + w.y * Ry.y + w.z * Rz.y;
   wb.z = w.x * Rx.z + w.y * Ry.z + w.z * Rz.z;
