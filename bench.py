@@ -60,7 +60,7 @@ def parse_args():
                    help="seconds of untimed steps before the warm-up, so that the clock samples "
                         "cover the GPU under sustained load (0: none)")
     p.add_argument("--profile-steps", type=int, default=10)
-    p.add_argument("--e2e-steps", type=int, default=5)
+    p.add_argument("--e2e-steps", type=int, default=20)
     p.add_argument("--cpu-sample", type=int, default=16384, help="clumps in the CPU baseline sample")
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--no-cpu", action="store_true")
@@ -555,14 +555,19 @@ def run_engine(args):
         npp[:] = p_
         na[:] = a_
         nal[:] = al_
-        barrier()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for _ in range(args.e2e_steps):
+        def e2e_step():
             eng.import_particles(npp, na, nal)
             eng.step(1)
             lib().af3d_export_particles(eng._h, npp.ctypes.data_as(C.c_void_p), na.ctypes.data_as(C.c_void_p),
                                         nal.ctypes.data_as(C.c_void_p))
+
+        for _ in range(3):   # untimed warm-up of the same round trip
+            e2e_step()
+        barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            e2e_step()
         torch.cuda.synchronize()
         barrier()
         dt = replicas.max_over_ranks(R, time.perf_counter() - t0, dev)
