@@ -65,6 +65,7 @@ SIGNATURES = [
     ("af3d_abi_version", [], C.c_int),
     ("af3d_import_particles", [_P, _P, _P, _P], C.c_int),
     ("af3d_export_particles", [_P, _P, _P, _P], C.c_int),
+    ("af3d_step_host", [_P, _P, _P, _P, _P, _P, _P], C.c_int),
     ("af3d_set_system", [_P, _P], C.c_int),
     ("af3d_get_system", [_P, _P], C.c_int),
     ("af3d_set_grid", [_P, _P], C.c_int),

@@ -40,6 +40,8 @@ af3d_status fail(af3d_status code, const std::string &msg) {
 constexpr long kRegridEvery = 2000;   // avalanche_hst.cu:470 and :713 (cc % 2000 == 0)
 constexpr long kKernelsPerCellBuild = 7;   // predict/keys, 3 scan, scatter, rank, permute
 constexpr long kKernelsPerForcePass = 1;   // lists and forces in one kernel
+constexpr int kHostParts = 4;               // af3d_step_host: parts whose export overlaps the force pass
+constexpr long kForceBlock = 128;           // k_lists_forces' block: a part starts on a block boundary
 constexpr long kKernelsPerStep = kKernelsPerCellBuild + 1 + kKernelsPerForcePass;   // + time advance
 constexpr long kKernelsPerKeptStep = kKernelsPerStep - 1;    // a step without the permutation
 constexpr long kKernelsPerRegrid = 4;
@@ -119,6 +121,9 @@ struct af3d_ctx {
 
   StepGraph graphs[4];
   int graph_next = 0;
+  // af3d_step_host: the stream of its device-to-host copies and the events that release them
+  cudaStream_t xfer = nullptr;
+  cudaEvent_t part_done[kHostParts] = {};
   long launches = 0;          // kernels executed (graph replays included)
 
   Launch L() const { return Launch{st, n}; }
@@ -280,7 +285,8 @@ void predict_for(af3d_ctx *c, bool predict, bool keys, bool t_prev, bool records
 // A single-flume context passes its constants as a kernel parameter (from the host mirrors,
 // which push_params keeps equal to the device table; captured graphs are dropped whenever they
 // change).
-void forces_for(af3d_ctx *c, bool write_ft, const int *order, Planes out, bool warm = false, bool look = false) {
+void forces_for(af3d_ctx *c, bool write_ft, const int *order, Planes out, bool warm = false, bool look = false,
+                long s0 = 0, long count = -1) {
   const float4 *csort = order ? c->cells.csort : nullptr;
   Consts kc;
   const Consts *uni = nullptr;
@@ -292,10 +298,10 @@ void forces_for(af3d_ctx *c, bool write_ft, const int *order, Planes out, bool w
   if (look) la = LookAhead{c->nbr_next, c->cull_next, c->cells, c->id_cur};
   if (c->fp_mode == AF3D_FP_FAST)
     fast::launch_lists_forces(c->L(), c->cur, out, c->d, c->fl_cur, c->nbr, c->cull, c->cells.start, order, csort,
-                              c->lists, write_ft, uni, warm, la);
+                              c->lists, write_ft, uni, warm, la, s0, count);
   else
     launch_lists_forces(c->L(), c->cur, out, c->d, c->fl_cur, c->nbr, c->cull, c->cells.start, order, csort,
-                        c->lists, write_ft, uni, warm, la);
+                        c->lists, write_ft, uni, warm, la, s0, count);
 }
 
 void enqueue_cell_build(af3d_ctx *c, bool predict, bool t_prev, bool ft = true) {
@@ -595,6 +601,12 @@ af3d_status af3d_destroy(af3d_ctx *c) {
                   (void *)c->d_acc, (void *)c->d_anga, (void *)c->d_tmp, (void *)c->d_count})
     if (p) cudaFree(p);
   if (c->own_stream && c->st) cudaStreamDestroy(c->st);
+  if (c->xfer) {
+    cudaStreamSynchronize(c->xfer);
+    cudaStreamDestroy(c->xfer);
+  }
+  for (cudaEvent_t e : c->part_done)
+    if (e) cudaEventDestroy(e);
   delete c;
   return AF3D_OK;
 }
@@ -631,10 +643,13 @@ af3d_status af3d_set_fp_mode(af3d_ctx *c, int mode) {
   return AF3D_OK;
 }
 
-af3d_status af3d_import_particles(af3d_ctx *c, const af3d_particle *pp, const af3d_vec3 *acc,
-                                  const af3d_vec3 *anga) {
-  CHECK_CTX(c);
-  if (!pp && c->n > 0) return fail(AF3D_ERR_ARG, "null particle array");
+namespace {
+
+// The host particle array (and accelerations) into the plane set, enqueued on the context's
+// stream.  keep_order: every clump goes back to the slot it held; otherwise slot i receives
+// clump i.
+af3d_status enqueue_import(af3d_ctx *c, const af3d_particle *pp, const af3d_vec3 *acc, const af3d_vec3 *anga,
+                           bool keep_order) {
   const long n = std::max<long>(c->n, 1);
   if (!c->d_aos) AF3D_CUDA(cudaMalloc(&c->d_aos, sizeof(af3d_particle) * n));
   if (!c->d_acc) AF3D_CUDA(cudaMalloc(&c->d_acc, sizeof(double) * 3 * n));
@@ -644,13 +659,8 @@ af3d_status af3d_import_particles(af3d_ctx *c, const af3d_particle *pp, const af
     if (acc) AF3D_CUDA(cudaMemcpyAsync(c->d_acc, acc, sizeof(double) * 3 * c->n, cudaMemcpyHostToDevice, c->st));
     if (anga) AF3D_CUDA(cudaMemcpyAsync(c->d_anga, anga, sizeof(double) * 3 * c->n, cudaMemcpyHostToDevice, c->st));
   }
-  // A re-import keeps the slot order of the last permutation (every clump stays in its slot),
-  // so the next step need not permute; the first import puts clump i in slot i.
-  const bool keep_order = c->imported;
   launch_aos_to_planes(c->L(), c->d_aos, acc ? c->d_acc : nullptr, anga ? c->d_anga : nullptr, c->flume_of_id,
                        c->cur, c->id_cur, c->fl_cur, keep_order);
-  AF3D_CUDA(cudaStreamSynchronize(c->st));
-  AF3D_CUDA(cudaGetLastError());
   c->imported = true;
   c->records_valid = false;
   c->cells_valid = false;
@@ -660,6 +670,21 @@ af3d_status af3d_import_particles(af3d_ctx *c, const af3d_particle *pp, const af
     c->since_sort = kResortEvery;
     drop_graphs(c);
   }
+  return AF3D_OK;
+}
+
+}  // namespace
+
+af3d_status af3d_import_particles(af3d_ctx *c, const af3d_particle *pp, const af3d_vec3 *acc,
+                                  const af3d_vec3 *anga) {
+  CHECK_CTX(c);
+  if (!pp && c->n > 0) return fail(AF3D_ERR_ARG, "null particle array");
+  // A re-import keeps the slot order of the last permutation (every clump stays in its slot),
+  // so the next step need not permute; the first import puts clump i in slot i.
+  af3d_status s = enqueue_import(c, pp, acc, anga, c->imported);
+  if (s) return s;
+  AF3D_CUDA(cudaStreamSynchronize(c->st));
+  AF3D_CUDA(cudaGetLastError());
   if (!c->have_grid && c->n > 0) return regrid(c);
   return AF3D_OK;
 }
@@ -677,6 +702,77 @@ af3d_status af3d_export_particles(af3d_ctx *c, af3d_particle *pp, af3d_vec3 *acc
   AF3D_CUDA(cudaStreamSynchronize(c->st));
   AF3D_CUDA(cudaGetLastError());
   return AF3D_OK;
+}
+
+af3d_status af3d_step_host(af3d_ctx *c, const af3d_particle *in, const af3d_vec3 *acc_in,
+                           const af3d_vec3 *anga_in, af3d_particle *out, af3d_vec3 *acc_out,
+                           af3d_vec3 *anga_out) {
+  CHECK_CTX(c);
+  const long n = c->n;
+  if (n > 0 && (!in || !out)) return fail(AF3D_ERR_ARG, "null particle array");
+  // Import in input order: slot i holds clump i, so a part of the slots is a contiguous part of
+  // the host arrays.  The step keeps that order (the cell sort only orders the neighbour search).
+  af3d_status s = enqueue_import(c, in, acc_in, anga_in, false);
+  if (s) return s;
+  if (!c->have_grid || n == 0) {
+    // no grid yet (the import derives it) or nothing to overlap: the three calls in turn
+    AF3D_CUDA(cudaStreamSynchronize(c->st));
+    if (!c->have_grid && n > 0) {
+      s = regrid(c);
+      if (s) return s;
+    }
+    s = af3d_step(c, 1);
+    if (s) return s;
+    return af3d_export_particles(c, out, acc_out, anga_out);
+  }
+  if (!c->xfer) AF3D_CUDA(cudaStreamCreateWithFlags(&c->xfer, cudaStreamNonBlocking));
+  for (cudaEvent_t &e : c->part_done)
+    if (!e) AF3D_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  // The step (a kept-order step of af3d_step), its force pass in kHostParts launches of whole
+  // blocks; after each, the part's clumps go to the AoS staging buffer and, on the copy stream,
+  // to the host while the next part computes.
+  launch_advance_time(c->st, c->d);
+  predict_for(c, true, true, true, true);
+  launch_sort(c->L(), c->d, c->cells, c->id_cur, c->ntags, c->cull, false);
+  Planes after = c->cur;   // the plane set as the step leaves it (accelerations swapped)
+  swap_accel_planes(after);
+  const long per = (n + kHostParts - 1) / kHostParts;
+  const long part = (per + kForceBlock - 1) / kForceBlock * kForceBlock;
+  int parts = 0;
+  for (long s0 = 0; s0 < n; s0 += part, parts++) {
+    const long cnt = std::min(part, n - s0);
+    forces_for(c, false, c->cells.perm, c->cur, false, false, s0, cnt);
+    launch_planes_to_aos(c->L(), after, c->id_cur, c->fl_cur, c->d_aos, acc_out ? c->d_acc : nullptr,
+                         anga_out ? c->d_anga : nullptr, c->d, s0, cnt);
+    AF3D_CUDA(cudaEventRecord(c->part_done[parts], c->st));
+    AF3D_CUDA(cudaStreamWaitEvent(c->xfer, c->part_done[parts], 0));
+    AF3D_CUDA(cudaMemcpyAsync(out + s0, c->d_aos + s0, sizeof(af3d_particle) * cnt, cudaMemcpyDeviceToHost,
+                              c->xfer));
+    if (acc_out)
+      AF3D_CUDA(cudaMemcpyAsync(acc_out + s0, c->d_acc + 3 * s0, sizeof(double) * 3 * cnt, cudaMemcpyDeviceToHost,
+                                c->xfer));
+    if (anga_out)
+      AF3D_CUDA(cudaMemcpyAsync(anga_out + s0, c->d_anga + 3 * s0, sizeof(double) * 3 * cnt,
+                                cudaMemcpyDeviceToHost, c->xfer));
+  }
+  swap_accel_planes(c->cur);
+  swap_accel_planes(c->alt);
+  c->launches += 1 + (kKernelsPerKeptStep - kKernelsPerForcePass) + 2L * parts;
+  // af3d_step's bookkeeping for one step
+  c->time = c->time + c->sys[0].dt;
+  const bool do_regrid = c->cc % kRegridEvery == 0;
+  c->cc += 1;
+  c->cells_valid = true;
+  c->records_valid = false;
+  AF3D_CUDA(cudaStreamSynchronize(c->xfer));
+  if (do_regrid) {
+    s = regrid(c);
+    if (s) return s;
+  }
+  int flags = 0;
+  s = read_status(c, &flags);
+  if (s) return s;
+  return first_error(flags);
 }
 
 af3d_status af3d_set_flume_system(af3d_ctx *c, int f, const af3d_system_par *sys, const af3d_funnel *fun) {

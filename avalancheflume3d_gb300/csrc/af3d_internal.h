@@ -210,7 +210,7 @@ void launch_lists_forces (const Launch &L, Planes cur, Planes out, DevScalars *d
                           const NbrRec *nbr, const CullRec *cull, const int *start, const int *order,
                           const float4 *csort, ContactLists lists, bool write_ft,
                           const Consts *uniform = nullptr, bool warm = false,
-                          LookAhead look = LookAhead{});
+                          LookAhead look = LookAhead{}, long s0 = 0, long count = -1);
 void launch_boundary (const Launch &L, Planes cur, DevScalars *d, const int *flume, int routine);
 void launch_part (const Launch &L, Planes cur, DevScalars *d, const int *flume, const NbrRec *nbr,
                   const CullRec *cull, const int *start, int sph_id);
@@ -230,7 +230,8 @@ void launch_aos_to_planes (const Launch &L, const af3d_particle *aos, const doub
                            const double *anga, const int *flume_of_id, Planes cur, long long *id,
                            int *flume, bool keep_order);
 void launch_planes_to_aos (const Launch &L, Planes cur, const long long *id, const int *flume,
-                           af3d_particle *aos, double *acc, double *anga, DevScalars *d);
+                           af3d_particle *aos, double *acc, double *anga, DevScalars *d, long s0 = 0,
+                           long count = -1);
 void launch_contact_pairs (const Launch &L, Planes cur, DevScalars *d, const int *flume,
                            const NbrRec *nbr, const CullRec *cull, const int *start,
                            const long long *id, long long *out, unsigned long long *count, long cap,
@@ -270,7 +271,7 @@ void launch_lists_forces (const Launch &L, Planes cur, Planes out, DevScalars *d
                           const NbrRec *nbr, const CullRec *cull, const int *start, const int *order,
                           const float4 *csort, ContactLists lists, bool write_ft,
                           const Consts *uniform = nullptr, bool warm = false,
-                          LookAhead look = LookAhead{});
+                          LookAhead look = LookAhead{}, long s0 = 0, long count = -1);
 }  // namespace fast
 
 }  // namespace af3d

@@ -10,6 +10,7 @@
 //                  scattering) contributions: no atomics on forces
 // The per-routine C-ABI entry points use k_boundary / k_part / k_get_accel / k_finish_verlet,
 // which apply the same device functions to the F, T planes one routine at a time.
+#include <algorithm>
 #include <cfloat>
 
 #include "af3d_cellwalk.cuh"
@@ -84,8 +85,8 @@ __global__ void k_aos_to_planes(const af3d_particle *__restrict__ aos, const dou
 
 __global__ void k_planes_to_aos(Planes P, const long long *__restrict__ id, const int *__restrict__ flume,
                                 af3d_particle *aos, double *acc, double *anga, const DevScalars *d,
-                                long n) {
-  long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
+                                long s0, long n) {
+  long s = s0 + blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (s >= n) return;
   const af3d_system_par &sy = d->flumes[flume[s]].sys;
   const double cost = sy.cost, sint = sy.sint;
@@ -761,9 +762,9 @@ template <bool UNIFORM>
 __device__ __forceinline__ int lists_body(const Consts &c, const DevScalars *d, const int *__restrict__ flume,
                                            const NbrRec *__restrict__ nbr, const CullRec *__restrict__ cull,
                                            const int *__restrict__ start, const int *__restrict__ order,
-                                           const float4 *__restrict__ csort, ContactLists lists, long n,
-                                           PassLists &pl, ListCounts &lc) {
-  const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
+                                           const float4 *__restrict__ csort, ContactLists lists, long s0,
+                                           long n, PassLists &pl, ListCounts &lc) {
+  const long s = s0 + blockIdx.x * (long)blockDim.x + threadIdx.x;
   const bool valid = s < n;
   const long sv = valid ? s : n - 1;
   const int f = flume[sv];
@@ -775,7 +776,7 @@ __device__ __forceinline__ int lists_body(const Consts &c, const DevScalars *d, 
   const V3 r = mk(me.rx, me.ry, me.rz);
   const bool act = valid && !is_removed(*c.tp, r.x, c.side_x);
   bool slow = false;
-  const int k = build_item_lists(pl, lists.items + sv, n, blockIdx.x * (long)blockDim.x + (threadIdx.x & ~31u), sv,
+  const int k = build_item_lists(pl, lists.items + sv, n, s0 + blockIdx.x * (long)blockDim.x + (threadIdx.x & ~31u), sv,
                                  act, c.phase == AF3D_PHASE_AVALANCHE, r, c, g, gf, off, nbr, cull, start, order,
                                  csort, slow, lc);
   return slow ? -1 : k;
@@ -798,9 +799,9 @@ __device__ __forceinline__ void fused_body(const Consts &c, Planes P, Planes out
                                            const int *__restrict__ flume, const NbrRec *__restrict__ nbr,
                                            const CullRec *__restrict__ cull, const int *__restrict__ start,
                                            const int *__restrict__ order, ContactLists lists, int listed,
-                                           ListCounts lc, long n, bool warm, const LookAhead &la,
+                                           ListCounts lc, long s0, long n, bool warm, const LookAhead &la,
                                            ForceShared &sh) {
-  const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const long s = s0 + blockIdx.x * (long)blockDim.x + threadIdx.x;
   const bool valid = s < n;
   const long sv = valid ? s : n - 1;   // in-range slot for lanes past n (nothing is written for them)
   const int f = flume[sv];
@@ -815,7 +816,7 @@ __device__ __forceinline__ void fused_body(const Consts &c, Planes P, Planes out
   if (valid && removed && aval)
     for (int rt = R_HOP0; rt <= R_FCORNERS; rt++)
       if (bnd_may_touch(rt, o.r, B, c)) bnd_routine(rt, o, true, c, F, T);
-  const long bbase = blockIdx.x * (long)blockDim.x;
+  const long bbase = s0 + blockIdx.x * (long)blockDim.x;
   const int active = block_contacts<UNIFORM>(sh.bq, bbase, sv, valid && !removed, aval, B, o, c, g, off, d, flume,
                                              nbr, cull, start, order, lists.items, valid ? listed : 0, lc, n, F, T);
   NbrRec q;
@@ -1206,46 +1207,51 @@ __global__ void __launch_bounds__(kBlock, AF3D_FORCES_MINB) k_lists_forces(Plane
                                                          const int *__restrict__ order,
                                                          const float4 *__restrict__ csort, ContactLists lists,
                                                          const __grid_constant__ Consts kc, bool warm,
-                                                         const __grid_constant__ LookAhead la, long n) {
+                                                         const __grid_constant__ LookAhead la, long s0, long n) {
   __shared__ ForceShared sh;
   ListCounts lc;
   if constexpr (UNIFORM) {
-    const int listed = lists_body<true>(kc, d, flume, nbr, cull, start, order, csort, lists, n,
+    const int listed = lists_body<true>(kc, d, flume, nbr, cull, start, order, csort, lists, s0, n,
                                         sh.pl[threadIdx.x >> 5], lc);
     __syncthreads();
-    fused_body<WRITE_FT, true>(kc, P, out, d, flume, nbr, cull, start, order, lists, listed, lc, n, warm, la, sh);
+    fused_body<WRITE_FT, true>(kc, P, out, d, flume, nbr, cull, start, order, lists, listed, lc, s0, n, warm, la,
+                               sh);
   } else {
     // the flume's constants read where they lie (a reference, not a register copy)
-    const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    const long s = s0 + blockIdx.x * (long)blockDim.x + threadIdx.x;
     const Consts &c = d->flumes[flume[s < n ? s : n - 1]].c;
-    const int listed = lists_body<false>(c, d, flume, nbr, cull, start, order, csort, lists, n,
+    const int listed = lists_body<false>(c, d, flume, nbr, cull, start, order, csort, lists, s0, n,
                                          sh.pl[threadIdx.x >> 5], lc);
     __syncthreads();
-    fused_body<WRITE_FT, false>(c, P, out, d, flume, nbr, cull, start, order, lists, listed, lc, n, warm, la, sh);
+    fused_body<WRITE_FT, false>(c, P, out, d, flume, nbr, cull, start, order, lists, listed, lc, s0, n, warm, la,
+                                sh);
   }
 }
 
 void launch_lists_forces(const Launch &L, Planes cur, Planes out, DevScalars *d, const int *flume,
                          const NbrRec *nbr, const CullRec *cull, const int *start, const int *order,
                          const float4 *csort, ContactLists lists, bool write_ft, const Consts *uniform, bool warm,
-                         LookAhead look) {
-  if (L.n <= 0) return;
+                         LookAhead look, long s0, long count) {
+  // slots [s0, s0 + count) of L.n (count < 0: to the end); s0 a multiple of kBlock, so the
+  // launch's blocks are those of the whole pass
+  const long m = count < 0 ? L.n - s0 : std::min(count, L.n - s0);
+  if (L.n <= 0 || m <= 0 || s0 % kBlock != 0) return;
   const Consts kc = uniform ? *uniform : Consts{};
-  const int g = grid_for(L.n);
+  const int g = grid_for(m);
   if (uniform) {
     if (write_ft)
       k_lists_forces<true, true><<<g, kBlock, 0, L.st>>>(cur, out, d, flume, nbr, cull, start, order, csort, lists, kc,
-                                                        warm, look, L.n);
+                                                        warm, look, s0, L.n);
     else
       k_lists_forces<false, true><<<g, kBlock, 0, L.st>>>(cur, out, d, flume, nbr, cull, start, order, csort, lists,
-                                                         kc, warm, look, L.n);
+                                                         kc, warm, look, s0, L.n);
   } else {
     if (write_ft)
       k_lists_forces<true, false><<<g, kBlock, 0, L.st>>>(cur, out, d, flume, nbr, cull, start, order, csort, lists,
-                                                         kc, warm, look, L.n);
+                                                         kc, warm, look, s0, L.n);
     else
       k_lists_forces<false, false><<<g, kBlock, 0, L.st>>>(cur, out, d, flume, nbr, cull, start, order, csort, lists,
-                                                          kc, warm, look, L.n);
+                                                          kc, warm, look, s0, L.n);
   }
 }
 
@@ -1298,9 +1304,10 @@ void launch_aos_to_planes(const Launch &L, const af3d_particle *aos, const doubl
 }
 
 void launch_planes_to_aos(const Launch &L, Planes cur, const long long *id, const int *flume,
-                          af3d_particle *aos, double *acc, double *anga, DevScalars *d) {
-  if (L.n <= 0) return;
-  k_planes_to_aos<<<grid_for(L.n), kBlock, 0, L.st>>>(cur, id, flume, aos, acc, anga, d, L.n);
+                          af3d_particle *aos, double *acc, double *anga, DevScalars *d, long s0, long count) {
+  const long m = count < 0 ? L.n - s0 : std::min(count, L.n - s0);
+  if (L.n <= 0 || m <= 0) return;
+  k_planes_to_aos<<<grid_for(m), kBlock, 0, L.st>>>(cur, id, flume, aos, acc, anga, d, s0, L.n);
 }
 
 void launch_contact_pairs(const Launch &L, Planes cur, DevScalars *d, const int *flume,

@@ -101,6 +101,19 @@ class Engine:
         self._call("af3d_export_particles", ptr(pp), ptr(a), ptr(al))
         return (pp, a, al) if with_accel else pp
 
+    def step_host(self, pp: np.ndarray, acc: np.ndarray | None = None, anga: np.ndarray | None = None,
+                  out: np.ndarray | None = None, acc_out: np.ndarray | None = None,
+                  anga_out: np.ndarray | None = None) -> None:
+        """af3d_step_host: import pp (and accelerations), one step, export into out (default: pp
+        itself) and acc_out/anga_out, with the export overlapping the force pass."""
+        pp = np.ascontiguousarray(pp, dtype=PARTICLE)
+        assert pp.shape == (self.n,)
+        out = pp if out is None else out
+        assert out.dtype == PARTICLE and out.shape == (self.n,) and out.flags.c_contiguous
+        for a in (acc, anga, acc_out, anga_out):
+            assert a is None or (a.dtype == np.float64 and a.shape == (self.n, 3) and a.flags.c_contiguous)
+        self._call("af3d_step_host", ptr(pp), ptr(acc), ptr(anga), ptr(out), ptr(acc_out), ptr(anga_out))
+
     def set_system(self, sys: np.ndarray) -> None:
         """system_par of flume 0 (the only flume of a plain context)."""
         s = np.array(sys, dtype=SYSTEM_PAR).reshape(1).copy()
