@@ -40,7 +40,10 @@ af3d_status fail(af3d_status code, const std::string &msg) {
 constexpr long kRegridEvery = 2000;   // avalanche_hst.cu:470 and :713 (cc % 2000 == 0)
 constexpr long kKernelsPerCellBuild = 7;   // predict/keys, 3 scan, scatter, rank, permute
 constexpr long kKernelsPerForcePass = 1;   // lists and forces in one kernel
-constexpr int kHostParts = 4;               // af3d_step_host: parts whose export overlaps the force pass
+#ifndef AF3D_HOST_PARTS
+#define AF3D_HOST_PARTS 4
+#endif
+constexpr int kHostParts = AF3D_HOST_PARTS;   // af3d_step_host: parts whose copies overlap the step
 constexpr long kForceBlock = 128;           // k_lists_forces' block: a part starts on a block boundary
 constexpr long kKernelsPerStep = kKernelsPerCellBuild + 1 + kKernelsPerForcePass;   // + time advance
 constexpr long kKernelsPerKeptStep = kKernelsPerStep - 1;    // a step without the permutation
@@ -123,7 +126,7 @@ struct af3d_ctx {
   int graph_next = 0;
   // af3d_step_host: the stream of its device-to-host copies and the events that release them
   cudaStream_t xfer = nullptr;
-  cudaEvent_t part_done[kHostParts] = {};
+  cudaEvent_t part_done[kHostParts] = {}, part_in[kHostParts] = {};
   long launches = 0;          // kernels executed (graph replays included)
 
   Launch L() const { return Launch{st, n}; }
@@ -271,13 +274,16 @@ af3d_status regrid(af3d_ctx *c) {
 // clear_cell + clear_ocup + cell_locate: keys (optionally fused with the predictor), counting
 // sort, permutation of every plane into the new order, neighbour records.
 // The predictor and force launchers of the context's FP64 mode (the other kernels have one form).
-void predict_for(af3d_ctx *c, bool predict, bool keys, bool t_prev, bool records = false) {
+void predict_for(af3d_ctx *c, bool predict, bool keys, bool t_prev, bool records = false, long s0 = 0,
+                 long count = -1) {
   NbrRec *nbr = records ? c->nbr : nullptr;
   CullRec *cull = records ? c->cull : nullptr;
   if (c->fp_mode == AF3D_FP_FAST)
-    fast::launch_predict(c->L(), c->cur, c->d, predict, keys, t_prev, c->cells, c->id_cur, c->fl_cur, nbr, cull);
+    fast::launch_predict(c->L(), c->cur, c->d, predict, keys, t_prev, c->cells, c->id_cur, c->fl_cur, nbr, cull,
+                         s0, count);
   else
-    launch_predict(c->L(), c->cur, c->d, predict, keys, t_prev, c->cells, c->id_cur, c->fl_cur, nbr, cull);
+    launch_predict(c->L(), c->cur, c->d, predict, keys, t_prev, c->cells, c->id_cur, c->fl_cur, nbr, cull, s0,
+                   count);
 }
 
 // order: null when the slots were just permuted into (cell, id) order; out: where the corrected
@@ -607,6 +613,8 @@ af3d_status af3d_destroy(af3d_ctx *c) {
   }
   for (cudaEvent_t e : c->part_done)
     if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : c->part_in)
+    if (e) cudaEventDestroy(e);
   delete c;
   return AF3D_OK;
 }
@@ -710,35 +718,64 @@ af3d_status af3d_step_host(af3d_ctx *c, const af3d_particle *in, const af3d_vec3
   CHECK_CTX(c);
   const long n = c->n;
   if (n > 0 && (!in || !out)) return fail(AF3D_ERR_ARG, "null particle array");
-  // Import in input order: slot i holds clump i, so a part of the slots is a contiguous part of
-  // the host arrays.  The step keeps that order (the cell sort only orders the neighbour search).
-  af3d_status s = enqueue_import(c, in, acc_in, anga_in, false);
-  if (s) return s;
   if (!c->have_grid || n == 0) {
     // no grid yet (the import derives it) or nothing to overlap: the three calls in turn
-    AF3D_CUDA(cudaStreamSynchronize(c->st));
-    if (!c->have_grid && n > 0) {
-      s = regrid(c);
-      if (s) return s;
-    }
+    af3d_status s = af3d_import_particles(c, in, acc_in, anga_in);
+    if (s) return s;
     s = af3d_step(c, 1);
     if (s) return s;
     return af3d_export_particles(c, out, acc_out, anga_out);
   }
+  const long m = n;
+  if (!c->d_aos) AF3D_CUDA(cudaMalloc(&c->d_aos, sizeof(af3d_particle) * m));
+  if (!c->d_acc) AF3D_CUDA(cudaMalloc(&c->d_acc, sizeof(double) * 3 * m));
+  if (!c->d_anga) AF3D_CUDA(cudaMalloc(&c->d_anga, sizeof(double) * 3 * m));
   if (!c->xfer) AF3D_CUDA(cudaStreamCreateWithFlags(&c->xfer, cudaStreamNonBlocking));
   for (cudaEvent_t &e : c->part_done)
     if (!e) AF3D_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-  // The step (a kept-order step of af3d_step), its force pass in kHostParts launches of whole
-  // blocks; after each, the part's clumps go to the AoS staging buffer and, on the copy stream,
-  // to the host while the next part computes.
+  for (cudaEvent_t &e : c->part_in)
+    if (!e) AF3D_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  const long per = (n + kHostParts - 1) / kHostParts;
+  const long part = (per + kForceBlock - 1) / kForceBlock * kForceBlock;
+  // Import in input order (slot i holds clump i), so a part of the slots is a contiguous part of
+  // the host arrays; the step keeps that order (the cell sort only orders the neighbour search).
+  // Each part's copy to the device (copy stream) releases its conversion to planes and its
+  // predictor (the step's stream) while the next part copies.  The copy stream waits for the
+  // context's stream first: the staging buffers may still be in use.
+  AF3D_CUDA(cudaEventRecord(c->part_done[0], c->st));
+  AF3D_CUDA(cudaStreamWaitEvent(c->xfer, c->part_done[0], 0));
+  drop_graphs(c);   // the slot order changes (the next af3d_step permutes when it is due)
   launch_advance_time(c->st, c->d);
-  predict_for(c, true, true, true, true);
+  int parts = 0;
+  for (long s0 = 0; s0 < n; s0 += part, parts++) {
+    const long cnt = std::min(part, n - s0);
+    AF3D_CUDA(cudaMemcpyAsync(c->d_aos + s0, in + s0, sizeof(af3d_particle) * cnt, cudaMemcpyHostToDevice,
+                              c->xfer));
+    if (acc_in)
+      AF3D_CUDA(cudaMemcpyAsync(c->d_acc + 3 * s0, acc_in + s0, sizeof(double) * 3 * cnt, cudaMemcpyHostToDevice,
+                                c->xfer));
+    if (anga_in)
+      AF3D_CUDA(cudaMemcpyAsync(c->d_anga + 3 * s0, anga_in + s0, sizeof(double) * 3 * cnt,
+                                cudaMemcpyHostToDevice, c->xfer));
+    AF3D_CUDA(cudaEventRecord(c->part_in[parts], c->xfer));
+    AF3D_CUDA(cudaStreamWaitEvent(c->st, c->part_in[parts], 0));
+    launch_aos_to_planes(c->L(), c->d_aos, acc_in ? c->d_acc : nullptr, anga_in ? c->d_anga : nullptr,
+                         c->flume_of_id, c->cur, c->id_cur, c->fl_cur, false, s0, cnt);
+    predict_for(c, true, true, true, true, s0, cnt);
+  }
+  c->imported = true;
+  c->records_valid = false;
+  c->cells_valid = false;
+  c->sorted = false;
+  c->look = false;
+  c->since_sort = kResortEvery;
+  // The rest of the step (a kept-order step of af3d_step): the sort, then the force pass in
+  // kHostParts launches of whole blocks; after each, the part's clumps go to the AoS staging
+  // buffer and, on the copy stream, to the host while the next part computes.
   launch_sort(c->L(), c->d, c->cells, c->id_cur, c->ntags, c->cull, false);
   Planes after = c->cur;   // the plane set as the step leaves it (accelerations swapped)
   swap_accel_planes(after);
-  const long per = (n + kHostParts - 1) / kHostParts;
-  const long part = (per + kForceBlock - 1) / kForceBlock * kForceBlock;
-  int parts = 0;
+  parts = 0;
   for (long s0 = 0; s0 < n; s0 += part, parts++) {
     const long cnt = std::min(part, n - s0);
     forces_for(c, false, c->cells.perm, c->cur, false, false, s0, cnt);
@@ -757,7 +794,7 @@ af3d_status af3d_step_host(af3d_ctx *c, const af3d_particle *in, const af3d_vec3
   }
   swap_accel_planes(c->cur);
   swap_accel_planes(c->alt);
-  c->launches += 1 + (kKernelsPerKeptStep - kKernelsPerForcePass) + 2L * parts;
+  c->launches += (kKernelsPerKeptStep - kKernelsPerForcePass - 1) + 4L * parts;
   // af3d_step's bookkeeping for one step
   c->time = c->time + c->sys[0].dt;
   const bool do_regrid = c->cc % kRegridEvery == 0;
@@ -765,6 +802,7 @@ af3d_status af3d_step_host(af3d_ctx *c, const af3d_particle *in, const af3d_vec3
   c->cells_valid = true;
   c->records_valid = false;
   AF3D_CUDA(cudaStreamSynchronize(c->xfer));
+  af3d_status s = AF3D_OK;
   if (do_regrid) {
     s = regrid(c);
     if (s) return s;

@@ -187,7 +187,7 @@ struct Launch {
 // records of every clump at its own slot.
 void launch_predict (const Launch &L, Planes cur, DevScalars *d, bool predict, bool keys, bool t_prev,
                      Cells cells, const long long *id, const int *flume, NbrRec *nbr = nullptr,
-                     CullRec *cull = nullptr);
+                     CullRec *cull = nullptr, long s0 = 0, long count = -1);
 // Exclusive scan of the bucket counts, scatter by arrival, then the deterministic (bucket, id)
 // rank: fills cells.start[0..nbuckets] and cells.perm, checks the ntags capacity and leaves the
 // count array zeroed.  nbuckets = ncell_total + N is read on the device.
@@ -228,7 +228,7 @@ void launch_commit_grids (cudaStream_t st, DevScalars *d, int nflumes, long n, l
 // (keep_order false), else at the slot the clump already holds (the slot order is kept).
 void launch_aos_to_planes (const Launch &L, const af3d_particle *aos, const double *acc,
                            const double *anga, const int *flume_of_id, Planes cur, long long *id,
-                           int *flume, bool keep_order);
+                           int *flume, bool keep_order, long s0 = 0, long count = -1);
 void launch_planes_to_aos (const Launch &L, Planes cur, const long long *id, const int *flume,
                            af3d_particle *aos, double *acc, double *anga, DevScalars *d, long s0 = 0,
                            long count = -1);
@@ -266,7 +266,7 @@ void launch_state_copy (const Launch &L, Planes P, Planes tape, bool to_tape, bo
 namespace fast {
 void launch_predict (const Launch &L, Planes cur, DevScalars *d, bool predict, bool keys, bool t_prev,
                      Cells cells, const long long *id, const int *flume, NbrRec *nbr = nullptr,
-                     CullRec *cull = nullptr);
+                     CullRec *cull = nullptr, long s0 = 0, long count = -1);
 void launch_lists_forces (const Launch &L, Planes cur, Planes out, DevScalars *d, const int *flume,
                           const NbrRec *nbr, const CullRec *cull, const int *start, const int *order,
                           const float4 *csort, ContactLists lists, bool write_ft,

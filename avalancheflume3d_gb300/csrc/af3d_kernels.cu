@@ -49,8 +49,8 @@ __device__ __forceinline__ void raise_status(DevScalars *d, int err) {
 // keep_order: slot s keeps the clump it holds (id[s]); otherwise slot s receives clump s.
 __global__ void k_aos_to_planes(const af3d_particle *__restrict__ aos, const double *__restrict__ acc,
                                 const double *__restrict__ anga, const int *__restrict__ flume_of_id,
-                                Planes P, long long *id, int *flume, bool keep_order, long n) {
-  long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
+                                Planes P, long long *id, int *flume, bool keep_order, long s0, long n) {
+  long s = s0 + blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (s >= n) return;
   const long long i = keep_order ? id[s] : s;
   const af3d_particle &q = aos[i];
@@ -352,10 +352,10 @@ template <bool PREDICT, bool KEYS, bool RECORDS>
 __global__ void __launch_bounds__(kBlock) k_predict(Planes P, DevScalars *d, bool t_prev, Cells cells,
                                                     const long long *__restrict__ id,
                                                     const int *__restrict__ flume, NbrRec *nbr,
-                                                    CullRec *cull, long n) {
+                                                    CullRec *cull, long s0, long n) {
   __shared__ double s_nbr[RECORDS ? kPermBlock * kRecStride : 1];
   __shared__ CullRec s_cull[RECORDS ? kPermBlock : 1];
-  const long base = blockIdx.x * (long)blockDim.x;
+  const long base = s0 + blockIdx.x * (long)blockDim.x;
   const long s = base + threadIdx.x;
   const bool valid = s < n;
   if (!RECORDS && !valid) return;
@@ -1164,19 +1164,22 @@ namespace fast {
 #endif
 
 void launch_predict(const Launch &L, Planes cur, DevScalars *d, bool predict, bool keys, bool t_prev,
-                    Cells cells, const long long *id, const int *flume, NbrRec *nbr, CullRec *cull) {
-  if (L.n <= 0) return;
-  const unsigned g = grid_for(L.n);
+                    Cells cells, const long long *id, const int *flume, NbrRec *nbr, CullRec *cull, long s0,
+                    long count) {
+  // slots [s0, s0 + count) of L.n (count < 0: to the end); s0 a multiple of kBlock
+  const long m = count < 0 ? L.n - s0 : std::min(count, L.n - s0);
+  if (L.n <= 0 || m <= 0 || s0 % kBlock != 0) return;
+  const unsigned g = grid_for(m);
   if (predict && keys && nbr)
-    k_predict<true, true, true><<<g, kBlock, 0, L.st>>>(cur, d, t_prev, cells, id, flume, nbr, cull, L.n);
+    k_predict<true, true, true><<<g, kBlock, 0, L.st>>>(cur, d, t_prev, cells, id, flume, nbr, cull, s0, L.n);
   else if (predict && keys)
-    k_predict<true, true, false><<<g, kBlock, 0, L.st>>>(cur, d, t_prev, cells, id, flume, nbr, cull, L.n);
+    k_predict<true, true, false><<<g, kBlock, 0, L.st>>>(cur, d, t_prev, cells, id, flume, nbr, cull, s0, L.n);
   else if (predict)
-    k_predict<true, false, false><<<g, kBlock, 0, L.st>>>(cur, d, t_prev, cells, id, flume, nbr, cull, L.n);
+    k_predict<true, false, false><<<g, kBlock, 0, L.st>>>(cur, d, t_prev, cells, id, flume, nbr, cull, s0, L.n);
   else if (keys && nbr)
-    k_predict<false, true, true><<<g, kBlock, 0, L.st>>>(cur, d, t_prev, cells, id, flume, nbr, cull, L.n);
+    k_predict<false, true, true><<<g, kBlock, 0, L.st>>>(cur, d, t_prev, cells, id, flume, nbr, cull, s0, L.n);
   else if (keys)
-    k_predict<false, true, false><<<g, kBlock, 0, L.st>>>(cur, d, t_prev, cells, id, flume, nbr, cull, L.n);
+    k_predict<false, true, false><<<g, kBlock, 0, L.st>>>(cur, d, t_prev, cells, id, flume, nbr, cull, s0, L.n);
 }
 
 void launch_permute_records(const Launch &L, Planes src, Planes dst, const int *perm,
@@ -1298,9 +1301,11 @@ void launch_commit_grids(cudaStream_t st, DevScalars *d, int nflumes, long n, lo
 
 void launch_aos_to_planes(const Launch &L, const af3d_particle *aos, const double *acc,
                           const double *anga, const int *flume_of_id, Planes cur, long long *id,
-                          int *flume, bool keep_order) {
-  if (L.n <= 0) return;
-  k_aos_to_planes<<<grid_for(L.n), kBlock, 0, L.st>>>(aos, acc, anga, flume_of_id, cur, id, flume, keep_order, L.n);
+                          int *flume, bool keep_order, long s0, long count) {
+  const long m = count < 0 ? L.n - s0 : std::min(count, L.n - s0);
+  if (L.n <= 0 || m <= 0) return;
+  k_aos_to_planes<<<grid_for(m), kBlock, 0, L.st>>>(aos, acc, anga, flume_of_id, cur, id, flume, keep_order, s0,
+                                                    L.n);
 }
 
 void launch_planes_to_aos(const Launch &L, Planes cur, const long long *id, const int *flume,

@@ -576,8 +576,8 @@ def run_engine(args):
         e2e = {"value": world * args.n * args.e2e_steps / dt, "unit": "clump-steps/s",
                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                "what": "per step: af3d_step_host on pinned host arrays (import of the AoS + a_i, one "
-                       "step, export of the AoS + a_i in place; the export of each quarter of the "
-                       "clumps overlaps the force pass of the next)"}
+                       "step, export of the AoS + a_i in place; the copies of each quarter of the "
+                       "clumps overlap the work on the others)"}
 
     ens = None
     if world == 1 and args.ensemble_flumes > 0:
