@@ -8,13 +8,14 @@ from ._lib import (CELL_PAR, FP_EXACT, FP_FAST, FRICTION_DEV, FRICTION_HST, FUNN
                    PHASE_AVALANCHE, PHASE_FILL, SYSTEM_PAR, EngineError, LIB_PATH, lib)
 from .engine import (Engine, Rannew64, calculate_particle_parameters, derive_system, error_check,
                      generate_particles, lattice_block, load_datainput, place_particles,
-                     read_last_config, set_initial_velocity, sphere_centres, write_last_config)
+                     read_last_config, set_initial_velocity, sphere_centres, write_last_config,
+                     append_snapshot)
 
 __all__ = [
     "Engine", "EngineError", "lib", "LIB_PATH", "PARTICLE", "SYSTEM_PAR", "FUNNEL", "CELL_PAR",
     "INPUTS", "FRICTION_HST", "FRICTION_DEV", "PHASE_FILL", "PHASE_AVALANCHE", "FP_EXACT", "FP_FAST",
     "load_datainput",
-    "derive_system", "error_check", "write_last_config", "read_last_config", "Rannew64",
+    "derive_system", "error_check", "write_last_config", "read_last_config", "append_snapshot", "Rannew64",
     "generate_particles", "calculate_particle_parameters", "place_particles",
     "set_initial_velocity", "sphere_centres", "lattice_block",
 ]

@@ -66,6 +66,8 @@ SIGNATURES = [
     ("af3d_import_particles", [_P, _P, _P, _P], C.c_int),
     ("af3d_export_particles", [_P, _P, _P, _P], C.c_int),
     ("af3d_step_host", [_P, _P, _P, _P, _P, _P, _P], C.c_int),
+    ("af3d_save_checkpoint", [_P, C.c_char_p], C.c_int),
+    ("af3d_load_checkpoint", [_P, C.c_char_p], C.c_int),
     ("af3d_set_system", [_P, _P], C.c_int),
     ("af3d_get_system", [_P, _P], C.c_int),
     ("af3d_set_grid", [_P, _P], C.c_int),
@@ -111,6 +113,8 @@ SIGNATURES = [
     ("af3d_error_check", [_P, C.c_char_p, C.c_size_t], C.c_int),
     ("af3d_write_last_config", [C.c_char_p, C.c_int, C.c_double, C.c_long, C.c_long, _P, C.c_long], C.c_int),
     ("af3d_read_last_config", [C.c_char_p, _P, _P, _P, _P, _P, C.c_long], C.c_int),
+    ("af3d_append_snapshot", [C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p, _P, C.c_long, _P, C.c_int],
+     C.c_int),
     ("af3d_rng_seed", [_P, C.c_long], None),
     ("af3d_rng_next", [_P], C.c_double),
     ("af3d_generate_particles", [_P, _P], None),

@@ -9,6 +9,7 @@
 // Device-side checks raise bits in a status word that af3d_step() and af3d_get_status() read
 // back; nothing calls exit().
 #include <algorithm>
+#include <cstdint>
 #include <cstddef>
 #include <cstdio>
 #include <cstring>
@@ -811,6 +812,114 @@ af3d_status af3d_step_host(af3d_ctx *c, const af3d_particle *in, const af3d_vec3
   s = read_status(c, &flags);
   if (s) return s;
   return first_error(flags);
+}
+
+namespace {
+
+// Lossless checkpoint file: this header, then per flume its system_par, Funnel and cell_par,
+// then the particles (AoS, id order), a_i and alpha_i, all as raw host bytes.
+struct CheckpointHeader {
+  char magic[8];       // "AF3DCKP1"
+  uint32_t layout;     // sizeof of particle, system_par, cell_par packed (a layout check)
+  int32_t nflumes;
+  int64_t n, ntags, cc;
+  int32_t phase, variant, fp_mode, have_grid;
+  double time;
+};
+constexpr char kCheckpointMagic[8] = {'A', 'F', '3', 'D', 'C', 'K', 'P', '1'};
+constexpr uint32_t kCheckpointLayout =
+    (uint32_t)sizeof(af3d_particle) | (uint32_t)sizeof(af3d_system_par) << 10 | (uint32_t)sizeof(af3d_cell_par) << 20;
+
+}  // namespace
+
+af3d_status af3d_save_checkpoint(af3d_ctx *c, const char *path) {
+  CHECK_STATE(c);
+  if (!path) return fail(AF3D_ERR_ARG, "null path");
+  af3d_status s = pull_params(c);
+  if (s) return s;
+  const long n = c->n;
+  std::vector<af3d_particle> pp((size_t)n);
+  std::vector<af3d_vec3> a((size_t)n), al((size_t)n);
+  s = af3d_export_particles(c, pp.data(), a.data(), al.data());
+  if (s) return s;
+  CheckpointHeader h{};
+  std::memcpy(h.magic, kCheckpointMagic, 8);
+  h.layout = kCheckpointLayout;
+  h.nflumes = c->nflumes;
+  h.n = n;
+  h.ntags = c->ntags;
+  h.cc = c->cc;
+  h.phase = c->phase;
+  h.variant = c->variant;
+  h.fp_mode = c->fp_mode;
+  h.have_grid = c->have_grid ? 1 : 0;
+  h.time = c->time;
+  FILE *fp = fopen(path, "wb");
+  if (!fp) return fail(AF3D_ERR_IO, std::string("cannot write ") + path);
+  bool ok = fwrite(&h, sizeof h, 1, fp) == 1;
+  for (int f = 0; f < c->nflumes && ok; f++) {
+    af3d_system_par sy = c->sys[f];
+    sy.time = c->time;
+    ok = fwrite(&sy, sizeof sy, 1, fp) == 1 && fwrite(&c->fun[f], sizeof(af3d_funnel), 1, fp) == 1 &&
+         fwrite(&c->grid[f], sizeof(af3d_cell_par), 1, fp) == 1;
+  }
+  if (ok && n > 0)
+    ok = fwrite(pp.data(), sizeof(af3d_particle), (size_t)n, fp) == (size_t)n &&
+         fwrite(a.data(), sizeof(af3d_vec3), (size_t)n, fp) == (size_t)n &&
+         fwrite(al.data(), sizeof(af3d_vec3), (size_t)n, fp) == (size_t)n;
+  ok = (fclose(fp) == 0) && ok;
+  return ok ? AF3D_OK : fail(AF3D_ERR_IO, std::string("write failed: ") + path);
+}
+
+af3d_status af3d_load_checkpoint(af3d_ctx *c, const char *path) {
+  CHECK_CTX(c);
+  if (!path) return fail(AF3D_ERR_ARG, "null path");
+  FILE *fp = fopen(path, "rb");
+  if (!fp) return fail(AF3D_ERR_IO, std::string("cannot read ") + path);
+  CheckpointHeader h{};
+  bool ok = fread(&h, sizeof h, 1, fp) == 1 && std::memcmp(h.magic, kCheckpointMagic, 8) == 0 &&
+            h.layout == kCheckpointLayout;
+  if (ok && (h.n != c->n || h.nflumes != c->nflumes || h.ntags != c->ntags)) {
+    fclose(fp);
+    return fail(AF3D_ERR_ARG, "checkpoint of another context shape (clumps, flumes or ntags differ)");
+  }
+  std::vector<af3d_system_par> sys(ok ? (size_t)h.nflumes : 0);
+  std::vector<af3d_funnel> fun(sys.size());
+  std::vector<af3d_cell_par> grid(sys.size());
+  for (size_t f = 0; f < sys.size() && ok; f++)
+    ok = fread(&sys[f], sizeof(af3d_system_par), 1, fp) == 1 && fread(&fun[f], sizeof(af3d_funnel), 1, fp) == 1 &&
+         fread(&grid[f], sizeof(af3d_cell_par), 1, fp) == 1;
+  const size_t n = ok ? (size_t)h.n : 0;
+  std::vector<af3d_particle> pp(n);
+  std::vector<af3d_vec3> a(n), al(n);
+  if (ok && n > 0)
+    ok = fread(pp.data(), sizeof(af3d_particle), n, fp) == n && fread(a.data(), sizeof(af3d_vec3), n, fp) == n &&
+         fread(al.data(), sizeof(af3d_vec3), n, fp) == n;
+  fclose(fp);
+  if (!ok) return fail(AF3D_ERR_IO, std::string("not a readable checkpoint: ") + path);
+  // parameters, clock, phase and modes; then the state; then the grids and the step counter
+  af3d_status s = pull_params(c);
+  if (s) return s;
+  for (int f = 0; f < c->nflumes; f++) {
+    c->sys[f] = sys[f];
+    c->fun[f] = fun[f];
+  }
+  c->time = h.time;
+  c->phase = h.phase;
+  c->variant = h.variant;
+  s = push_params(c);
+  if (s) return s;
+  s = af3d_set_fp_mode(c, h.fp_mode);
+  if (s) return s;
+  s = af3d_import_particles(c, pp.data(), a.data(), al.data());
+  if (s) return s;
+  if (h.have_grid)
+    for (int f = 0; f < c->nflumes; f++) {
+      s = af3d_set_flume_grid(c, f, &grid[f]);
+      if (s) return s;
+    }
+  c->cc = h.cc;
+  return AF3D_OK;
 }
 
 af3d_status af3d_set_flume_system(af3d_ctx *c, int f, const af3d_system_par *sys, const af3d_funnel *fun) {

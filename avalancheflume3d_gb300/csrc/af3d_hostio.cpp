@@ -1,5 +1,6 @@
 // af3d_hostio.cpp -- host-only parts of the C ABI: DataInput.dat, the derived parameters,
-// error_check, last_config.dat, and the initial-state generators.  No GPU involved.
+// error_check, last_config.dat, the snapshot files, and the initial-state generators.  No GPU
+// involved.
 //
 // Compiled with -ffp-contract=off so the derived parameters come out bit-identical to the
 // reference's start-up arithmetic (avalanche_hst.cu:84-102, 187-195) on any host.
@@ -154,6 +155,85 @@ af3d_status af3d_write_last_config(const char *path, int aval_start, double time
             p.Rmatz.x, p.Rmatz.y, p.Rmatz.z, p.vv.x, p.vv.y, p.vv.z, p.ww.x, p.ww.y, p.ww.z);
   }
   return fclose(fp) == 0 ? AF3D_OK : AF3D_ERR_IO;
+}
+
+af3d_status af3d_append_snapshot(const char *xyz_path, const char *vel_path, const char *vmean_path,
+                                 const char *xcm_path, const af3d_particle *pp, long n,
+                                 const af3d_system_par *sys, int phase) {
+  // avalanche_hst.cu:507-586 (fill phase) and :750-841 (avalanche phase), one output frame
+  if (!sys || n < 0 || (n > 0 && !pp)) return AF3D_ERR_ARG;
+  const bool aval = phase == AF3D_PHASE_AVALANCHE;
+  const double xfinal = (kLFUNNEL + sys->Lflume) * sys->cost;   // avalanche_hst.cu:116
+  auto open = [](const char *path, FILE **fp) {
+    *fp = path ? fopen(path, "a") : nullptr;
+    return !path || *fp;
+  };
+  FILE *xyz, *vel, *vm, *xc;
+  if (!open(xyz_path, &xyz)) return AF3D_ERR_IO;
+  if (!open(vel_path, &vel)) {
+    if (xyz) fclose(xyz);
+    return AF3D_ERR_IO;
+  }
+  if (!open(vmean_path, &vm)) {
+    if (xyz) fclose(xyz);
+    if (vel) fclose(vel);
+    return AF3D_ERR_IO;
+  }
+  if (!open(aval ? xcm_path : nullptr, &xc)) {
+    if (xyz) fclose(xyz);
+    if (vel) fclose(vel);
+    if (vm) fclose(vm);
+    return AF3D_ERR_IO;
+  }
+  if (xyz) fprintf(xyz, "%ld\n\n", 4 * n + 2);
+  if (vel) fprintf(vel, "%ld\n\n", n + 2);
+  double vmean = 0.0, wmean = 0.0;
+  for (long i = 0; i < n; i++) {
+    const af3d_particle &p = pp[i];
+    if (xyz)
+      for (int k = 0; k < 4; k++)
+        fprintf(xyz, "%lf %lf %lf %lf %ld\n", p.radius, p.rr_s[k].x, p.rr_s[k].y, p.rr_s[k].z, i);
+    if (vel) fprintf(vel, "%lf %lf %lf %lf %lf %ld\n", p.rr.x, p.rr.y, p.rr.z, p.vv.x, p.ww.y, i);
+    double vm2 = p.vv.x * p.vv.x;
+    vm2 += p.vv.y * p.vv.y;
+    vm2 += p.vv.z * p.vv.z;
+    vmean += std::sqrt(vm2);
+    double wm2 = p.ww.x * p.ww.x;
+    wm2 += p.ww.y * p.ww.y;
+    wm2 += p.ww.z * p.ww.z;
+    wmean += std::sqrt(wm2);
+  }
+  // ghost atoms that keep the rendered cell size constant
+  if (xyz) {
+    if (aval)
+      fprintf(xyz, "0.0001 %lf %lf %lf %ld\n", sys->side.x, kYFUNNEL, sys->side.z, n);
+    else
+      fprintf(xyz, "0.000001 %lf %lf %lf %ld\n", xfinal, kYFUNNEL, sys->side.z, n);
+    fprintf(xyz, "0.000001 0.000000 0.000000 0.000000 %ld\n", n);
+  }
+  if (vel) {
+    fprintf(vel, "%lf %lf %lf 0.000000 0.000000 %ld\n", xfinal, kYFUNNEL, sys->side.z, n);
+    fprintf(vel, "0.000000 0.000000 0.000000 0.000000 0.000000 %ld\n", n);
+  }
+  vmean /= n;
+  wmean /= n;
+  if (vm) fprintf(vm, "%lf, %lf, %lf\n", sys->time - sys->dt, vmean, wmean);
+  if (xc) {
+    double xcm = 0.0, zcm = 0.0;
+    for (long i = 0; i < n; i++) {
+      const double xmass = pp[i].mass * pp[i].rr.x;
+      const double zmass = pp[i].mass * pp[i].rr.z;
+      xcm += xmass;
+      zcm += zmass;
+    }
+    xcm /= sys->tot_mass;
+    zcm /= sys->tot_mass;
+    fprintf(xc, "%lf, %lf, %lf\n", sys->time - sys->dt, xcm, zcm);
+  }
+  bool ok = true;
+  for (FILE *f : {xyz, vel, vm, xc})
+    if (f) ok = fclose(f) == 0 && ok;
+  return ok ? AF3D_OK : AF3D_ERR_IO;
 }
 
 af3d_status af3d_read_last_config(const char *path, int *aval_start, double *time, long *cc, long *jj,

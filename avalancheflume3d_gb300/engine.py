@@ -114,6 +114,15 @@ class Engine:
             assert a is None or (a.dtype == np.float64 and a.shape == (self.n, 3) and a.flags.c_contiguous)
         self._call("af3d_step_host", ptr(pp), ptr(acc), ptr(anga), ptr(out), ptr(acc_out), ptr(anga_out))
 
+    def save_checkpoint(self, path: str) -> None:
+        """af3d_save_checkpoint: the whole context state, losslessly, to `path`."""
+        self._call("af3d_save_checkpoint", str(path).encode())
+
+    def load_checkpoint(self, path: str) -> None:
+        """af3d_load_checkpoint: a checkpoint of a context of the same shape."""
+        self._call("af3d_load_checkpoint", str(path).encode())
+        self.sys = self.get_system() if not self.ensemble else self.sys
+
     def set_system(self, sys: np.ndarray) -> None:
         """system_par of flume 0 (the only flume of a plain context)."""
         s = np.array(sys, dtype=SYSTEM_PAR).reshape(1).copy()
@@ -306,6 +315,17 @@ def read_last_config(path: str, pp: np.ndarray):
     check(lib().af3d_read_last_config(path.encode(), C.byref(a), C.byref(t), C.byref(cc), C.byref(jj),
                                       ptr(pp), len(pp)), "af3d_read_last_config")
     return a.value, t.value, cc.value, jj.value
+
+
+def append_snapshot(pp: np.ndarray, sys: np.ndarray, phase: int, xyz: str | None = None, vel: str | None = None,
+                    vmean: str | None = None, xcm: str | None = None) -> None:
+    """One frame of the reference's snapshot files (.xyz spheres, velocity field, mean-velocity
+    and centre-of-mass CSV lines), appended to the given paths (None: skipped)."""
+    pp = np.ascontiguousarray(pp, dtype=PARTICLE)
+    s = np.array(sys, dtype=SYSTEM_PAR).reshape(1)
+    enc = lambda x: None if x is None else str(x).encode()
+    check(lib().af3d_append_snapshot(enc(xyz), enc(vel), enc(vmean), enc(xcm), ptr(pp), len(pp), ptr(s), int(phase)),
+          "af3d_append_snapshot")
 
 
 class Rannew64:

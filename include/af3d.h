@@ -252,6 +252,14 @@ af3d_status af3d_contact_pairs_noalloc (af3d_ctx *ctx, long *out, long cap, long
    since the previous call; the counter restarts at zero. */
 af3d_status af3d_contact_count (af3d_ctx *ctx, long *count);
 
+/* Lossless binary checkpoint of a context (no counterpart in the reference, whose
+   last_config.dat is %lf text): parameters of every flume, clock, step counter, phase, friction
+   variant, FP64 mode, cell grids, the particles and a_i, alpha_i as raw bytes.  Loading it into
+   a context of the same shape (clumps, flumes, ntags) continues the run bit for bit as if it
+   had not stopped. */
+af3d_status af3d_save_checkpoint (af3d_ctx *ctx, const char *path);
+af3d_status af3d_load_checkpoint (af3d_ctx *ctx, const char *path);
+
 /* ---- host I/O (no GPU) ----------------------------------------------------------------- */
 /* Parse DataInput.dat: first token of each of the 16 lines (avalanche_hst.cu:34-81). */
 af3d_status af3d_load_datainput (const char *path, af3d_inputs *in);
@@ -264,6 +272,17 @@ af3d_status af3d_write_last_config (const char *path, int aval_start, double tim
                                     long jj, const af3d_particle *pp, long n);
 af3d_status af3d_read_last_config (const char *path, int *aval_start, double *time, long *cc,
                                    long *jj, af3d_particle *pp, long n);
+/* One output frame of the reference's snapshot files (avalanche_hst.cu:507-586 in the fill
+   phase, :750-841 in the avalanche phase), appended to each file whose path is non-NULL:
+     xyz_path    the .xyz frame (snapshots_hst.xyz): 4 n + 2 atoms, radius and centre of every
+                 sphere, then two ghost atoms that fix the rendered cell
+     vel_path    the velocity-field frame (velocities_hst.xyz): r, v.x, w.y per clump + 2 ghosts
+     vmean_path  mean_velocity_hst.csv: "time - dt, mean |v|, mean |w|"
+     xcm_path    xcm_hst.csv (avalanche phase only): "time - dt, x_cm, z_cm" over sys->tot_mass
+   pp in id order (as exported), sys with the current time. */
+af3d_status af3d_append_snapshot (const char *xyz_path, const char *vel_path, const char *vmean_path,
+                                  const char *xcm_path, const af3d_particle *pp, long n,
+                                  const af3d_system_par *sys, int phase);
 
 /* ---- initial-state generators (host; generate_particles.cu, place_particles.cu,
    set_initial_velocity.cu, rannew64.cu, calculate_particle_parameters.cu) ------------------- */

@@ -172,6 +172,53 @@ def test_last_config_round_trip(af3d, tmp_path):
     assert text[:4] == ["1", "0.123457", "20001", "3"] and len(text) == 4 + n
 
 
+@pytest.mark.parametrize("phase", [0, 1])
+def test_snapshot_frames_in_the_reference_format(af3d, tmp_path, phase):
+    """af3d_append_snapshot writes the frames of avalanche_hst.cu:507-586 (fill phase) and
+    :750-841 (avalanche phase): the same format strings, the same ghost atoms, the same sums."""
+    import math
+    from oracle.pyoracle import dense_state
+    from tests.states import flume_system
+    n = 7
+    sys, _ = flume_system(n, time=0.25 if phase == 1 else -0.5)
+    pp = dense_state(n, 3, sys)
+    pp["vv"] = np.random.default_rng(1).standard_normal((n, 3))
+    pp["ww"] = np.random.default_rng(2).standard_normal((n, 3))
+    sys["tot_mass"] = float(np.sum(pp["mass"]))
+    paths = {k: str(tmp_path / (k + ".out")) for k in ("xyz", "vel", "vmean", "xcm")}
+    for _ in range(2):   # two frames appended
+        af3d.append_snapshot(pp, sys, phase, **paths)
+    xfinal = (70.0 + float(sys["Lflume"])) * float(sys["cost"])
+    side = sys["side"]
+    want_xyz = ["%d" % (4 * n + 2), ""]
+    for i in range(n):
+        for k in range(4):
+            want_xyz.append("%f %f %f %f %d" % (pp["radius"][i], *pp["rr_s"][i][k], i))
+    if phase == 1:
+        want_xyz.append("0.0001 %f %f %f %d" % (side[0], 30.0, side[2], n))
+    else:
+        want_xyz.append("0.000001 %f %f %f %d" % (xfinal, 30.0, side[2], n))
+    want_xyz.append("0.000001 0.000000 0.000000 0.000000 %d" % n)
+    assert open(paths["xyz"]).read().splitlines() == want_xyz * 2
+    want_vel = ["%d" % (n + 2), ""]
+    for i in range(n):
+        want_vel.append("%f %f %f %f %f %d" % (*pp["rr"][i], pp["vv"][i][0], pp["ww"][i][1], i))
+    want_vel.append("%f %f %f 0.000000 0.000000 %d" % (xfinal, 30.0, side[2], n))
+    want_vel.append("0.000000 0.000000 0.000000 0.000000 0.000000 %d" % n)
+    assert open(paths["vel"]).read().splitlines() == want_vel * 2
+    vm = sum(math.sqrt((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]) for v in pp["vv"]) / n
+    wm = sum(math.sqrt((w[0] * w[0] + w[1] * w[1]) + w[2] * w[2]) for w in pp["ww"]) / n
+    t = float(sys["time"]) - float(sys["dt"])
+    assert open(paths["vmean"]).read().splitlines() == ["%f, %f, %f" % (t, vm, wm)] * 2
+    if phase == 1:
+        xcm = sum(pp["mass"][i] * pp["rr"][i][0] for i in range(n)) / float(sys["tot_mass"])
+        zcm = sum(pp["mass"][i] * pp["rr"][i][2] for i in range(n)) / float(sys["tot_mass"])
+        assert open(paths["xcm"]).read().splitlines() == ["%f, %f, %f" % (t, xcm, zcm)] * 2
+    else:
+        import os
+        assert not os.path.exists(paths["xcm"])   # the fill phase writes no centre of mass
+
+
 def test_lattice_block_workload(af3d):
     from avalancheflume3d_gb300.workloads import flume_2k, flume_state
     sys, fun, pp = flume_state(flume_2k())
