@@ -63,3 +63,27 @@ def test_step_host_without_accelerations(af3d):
         out = np.zeros_like(pp0)
         b.step_host(pp0, out=out)
         assert out.tobytes() == want.tobytes()
+
+
+def test_step_host_on_an_ensemble(af3d):
+    """Two flumes back to back in one context: the fused call matches the three calls."""
+    from tests.states import flume_system, wall_state
+    syss, funs, pps = [], [], []
+    for k, m in enumerate((300, 220)):
+        s, f = flume_system(m, mu_pp=0.3 + 0.2 * k)
+        syss.append(s)
+        funs.append(f)
+        pps.append(wall_state(m, 20 + k, s))
+    sys, fun, pp0 = np.stack(syss), np.stack(funs), np.concatenate(pps)
+    with af3d.Engine(sys, fun) as a, af3d.Engine(sys, fun) as b:
+        for e in (a, b):
+            e.import_particles(pp0)
+            e.step(2)
+        pa = a.export_particles(with_accel=False)
+        pb = pa.copy()
+        for _ in range(2):
+            a.import_particles(pa)
+            a.step(1)
+            pa = a.export_particles(with_accel=False)
+            b.step_host(pb)
+            assert pb.tobytes() == pa.tobytes()
