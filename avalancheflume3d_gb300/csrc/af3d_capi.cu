@@ -1455,22 +1455,42 @@ extern "C" af3d_status af3d_adjoint(af3d_ctx *c, long steps, long ckpt_every, do
     ~ModeBack() { c->fp_mode = m; }
   } mode_back{c, mode};
   drop_graphs(c);
-  // checkpoints open every segment but the last, which the forward run tapes itself
-  const long nck = steps > 0 ? (steps - 1) / ckpt_every : 0;
   AdjBuffers buf;
   Planes state0{}, fin{}, adjA{}, adjB{}, acc{}, rb{}, rnext{};
-  std::vector<Planes> ckpt(nck), tape(want_grad ? std::min(ckpt_every, std::max<long>(steps, 1)) : 0);
-  std::vector<ContactLists> tape_lists(tape.size());
-  std::vector<NbrRec *> tape_rec(tape.size());
   cudaError_t e = buf.planes(kAdjPlanes + 12, n, state0);   // with the sphere centres
   if (e == cudaSuccess) e = buf.planes(kAdjPlanes + 12, n, fin);
-  for (long k = 0; k < nck && e == cudaSuccess && want_grad; k++) e = buf.planes(kAdjPlanes, n, ckpt[k]);
+  if (want_grad && e == cudaSuccess) e = buf.planes(kAdjPlanes, n, adjA);
+  if (want_grad && e == cudaSuccess) e = buf.planes(kAdjPlanes, n, adjB);
+  if (want_grad && e == cudaSuccess) e = buf.planes(kAccPlanes, n, acc);
+  if (want_grad && e == cudaSuccess) e = buf.planes(kRbPlanes, n, rb);
+  if (want_grad && e == cudaSuccess) e = buf.planes(9, n, rnext);
+  // The tape: per step its starting state and torque sums (27 planes), its clump records, item
+  // lists and list counts, in one block.  It holds C = ckpt_every steps when they fit in the
+  // free device memory (with a reserve), else the largest C, halving, that does: the results do
+  // not depend on C.  Checkpoints open every segment but the last, which the forward run tapes
+  // itself.
+  const size_t m = (size_t)std::max<long>(n, 1);
+  const size_t slot = (sizeof(double) * (kAdjPlanes + 3) * m + sizeof(NbrRec) * m +
+                       (sizeof(unsigned) * kListCap + sizeof(int)) * m + 255) & ~(size_t)255;
+  const size_t ckpt_bytes = sizeof(double) * kAdjPlanes * m;
+  long C = std::min(ckpt_every, std::max<long>(steps, 1));
+  if (want_grad && e == cudaSuccess) {
+    size_t free_b = 0, total_b = 0;
+    e = cudaMemGetInfo(&free_b, &total_b);
+    const size_t reserve = (size_t)2 << 30;
+    const size_t avail = free_b > reserve ? free_b - reserve : 0;
+    auto need = [&](long cseg) {
+      const long nck_c = steps > 0 ? (steps - 1) / cseg : 0;
+      return slot * (size_t)cseg + ckpt_bytes * (size_t)nck_c;
+    };
+    while (C > 1 && need(C) > avail) C = (C + 1) / 2;
+  }
+  const long nck = steps > 0 ? (steps - 1) / C : 0;
+  std::vector<Planes> ckpt(want_grad ? nck : 0), tape(want_grad ? C : 0);
+  std::vector<ContactLists> tape_lists(tape.size());
+  std::vector<NbrRec *> tape_rec(tape.size());
+  for (size_t k = 0; k < ckpt.size() && e == cudaSuccess; k++) e = buf.planes(kAdjPlanes, n, ckpt[k]);
   if (!tape.empty() && e == cudaSuccess) {
-    // one block for the tape: per step its starting state and torque sums (27 planes), its
-    // clump records, item lists and list counts
-    const size_t m = (size_t)std::max<long>(n, 1);
-    const size_t slot = (sizeof(double) * (kAdjPlanes + 3) * m + sizeof(NbrRec) * m +
-                         (sizeof(unsigned) * kListCap + sizeof(int)) * m + 255) & ~(size_t)255;
     char *base = nullptr;
     e = cudaMalloc((void **)&base, slot * tape.size());
     if (e == cudaSuccess) {
@@ -1485,11 +1505,6 @@ extern "C" af3d_status af3d_adjoint(af3d_ctx *c, long steps, long ckpt_every, do
       }
     }
   }
-  if (want_grad && e == cudaSuccess) e = buf.planes(kAdjPlanes, n, adjA);
-  if (want_grad && e == cudaSuccess) e = buf.planes(kAdjPlanes, n, adjB);
-  if (want_grad && e == cudaSuccess) e = buf.planes(kAccPlanes, n, acc);
-  if (want_grad && e == cudaSuccess) e = buf.planes(kRbPlanes, n, rb);
-  if (want_grad && e == cudaSuccess) e = buf.planes(9, n, rnext);
   // per flume f: dsc[2 f], dsc[2 f + 1] the objective sums, pgr[6 f .. 6 f + 5] the parameter
   // adjoints; then per step: its list overflow flag (int), its start and end times (a pair)
   const size_t nsc = (size_t)8 * nf;
@@ -1518,7 +1533,7 @@ extern "C" af3d_status af3d_adjoint(af3d_ctx *c, long steps, long ckpt_every, do
   } own{c, c->nbr, c->nbr_next, c->lists, {c->cur.p[TX], c->cur.p[TX + 1], c->cur.p[TX + 2]}};
 
   // Forward: the start-up force pass (a_i of the first step), then `steps` steps keeping the
-  // slot order, the state saved every ckpt_every steps.
+  // slot order, the state saved every C steps.
   const double t_init = c->time, dt = c->sys[0].dt;
   launch_state_copy(c->L(), c->cur, state0, true, true);
   enqueue_startup_pass(c);
@@ -1526,7 +1541,7 @@ extern "C" af3d_status af3d_adjoint(af3d_ctx *c, long steps, long ckpt_every, do
   swap_accel_planes(c->cur);
   swap_accel_planes(c->alt);
   // The last segment's steps record their tape slots here (the reverse starts with them).
-  const long seg_last = steps > 0 ? (steps - 1) / ckpt_every : 0, k_last = seg_last * ckpt_every;
+  const long seg_last = steps > 0 ? (steps - 1) / C : 0, k_last = seg_last * C;
   // Step k of a segment [k0, k1) into its tape slot: its starting state, its clump records
   // (written by the previous pass's look-ahead, or by this step's predictor), item lists, list
   // counts and torque sums.  A kept-order step neither swaps nor reallocates the plane sets, and
@@ -1549,7 +1564,7 @@ extern "C" af3d_status af3d_adjoint(af3d_ctx *c, long steps, long ckpt_every, do
     if (want_grad && k >= k_last) {
       taped_step(k, k_last, steps);
     } else {
-      if (want_grad && k % ckpt_every == 0) launch_state_copy(c->L(), c->cur, ckpt[k / ckpt_every], true);
+      if (want_grad && k % C == 0) launch_state_copy(c->L(), c->cur, ckpt[k / C], true);
       if (want_grad && k + 1 == k_last) c->nbr_next = tape_rec[0];   // the taped segment's first records
       enqueue_fused_step(c, false, false, k + 1 < steps);   // the last pass does not look ahead
     }
@@ -1583,8 +1598,8 @@ extern "C" af3d_status af3d_adjoint(af3d_ctx *c, long steps, long ckpt_every, do
     AF3D_CUDA(cudaMemcpyAsync(t_pair, tp.data(), sizeof(double) * tp.size(), cudaMemcpyHostToDevice, c->st));
     launch_adj_seed(c->L(), c->cur, adjA, c->d, c->fl_cur, dsc);
     Planes rnext_src = fin;   // R1 of each segment's last step: the next segment's starting R
-    for (long seg = (steps - 1) / ckpt_every; steps > 0 && seg >= 0; seg--) {
-      const long k0 = seg * ckpt_every, k1 = std::min(steps, k0 + ckpt_every);
+    for (long seg = (steps - 1) / C; steps > 0 && seg >= 0; seg--) {
+      const long k0 = seg * C, k1 = std::min(steps, k0 + C);
       // recompute the segment into the tape (the last one was taped by the forward run)
       if (seg != seg_last) {
         for (int q = 0; q < 9; q++)   // tape slot 0 still holds segment seg + 1's starting state

@@ -80,9 +80,9 @@ def parse_args():
     p.add_argument("--adjoint-batch", type=int, default=64,
                    help="parameter samples of the batched (calibration) adjoint (0 skips it)")
     p.add_argument("--adjoint-batch-steps", type=int, default=200)
-    p.add_argument("--adjoint-batch-ckpt", type=int, default=100,
+    p.add_argument("--adjoint-batch-ckpt", type=int, default=200,
                    help="checkpoint interval of the batched adjoint (its tape holds this many steps "
-                        "of all samples: 113 GB at the defaults)")
+                        "of all samples, 226 GB at the defaults; the library halves it until it fits)")
     p.add_argument("--trace-contacts", type=int, default=0,
                    help="print active contacts every this many pre-roll steps (diagnostic)")
     return p.parse_args()

@@ -210,10 +210,12 @@ af3d_status af3d_fp64_peak (double *tflops);
    steps (fixed cell grid, no re-grid), and returns per flume f J[f] = the mass-weighted mean
    downslope position sum m (x cos(tilt) - z sin(tilt)) / sum m of its clumps at the end.  With
    any gradient pointer non-NULL it then runs the hand-written adjoint of those steps backwards
-   from a tape of ckpt_every steps (540 B per clump and step: each step's starting state, torque
-   sums, clump records and contact item lists); the last min(steps, ckpt_every) steps are taped
-   as the forward run goes, each earlier segment of ckpt_every steps restarts from a checkpoint
-   of its starting state (192 B per clump) and is recomputed into the tape.  It returns
+   from a tape of C steps (540 B per clump and step: each step's starting state, torque sums,
+   clump records and contact item lists), C = min(steps, ckpt_every), halved until the tape and
+   the checkpoints fit in the free device memory less 2 GB (the results do not depend on C); the
+   last C steps are taped as the forward run goes, each earlier segment of C steps restarts from
+   a checkpoint of its starting state (192 B per clump) and is recomputed into the tape.  It
+   returns
      param_grad[6 f + k]  dJ[f]/d(kappa_pp, gamma_pp, mu_pp, kappa_pw, gamma_pw, mu_pw)[k] of
                           flume f's system_par
      dr0, dv0, dw0        dJ[f]/d(initial r, v, omega) per clump id, f the clump's flume (the
