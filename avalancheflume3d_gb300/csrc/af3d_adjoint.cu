@@ -97,7 +97,7 @@ __device__ __forceinline__ bool contact_law_fwd_rev(const ContactIn &ci, double 
       const double iden = 1.0 / (1.0 + r * r);
       const double af2 = af * iden;
       const double af2_b = dot(fb, vt);
-      vt_b += af2 * fb;
+      vt_b = madd(af2, fb, vt_b);
       const double af_b = af2_b * (1.0 - r * r) * (iden * iden);
       mu_b += af_b * 0.8 * normal * ivt;
       normal_b += af_b * 0.8 * ci.mu * ivt;
@@ -115,13 +115,13 @@ __device__ __forceinline__ bool contact_law_fwd_rev(const ContactIn &ci, double 
         // fsdt = m xi (1e12 + 2e6 / dt), xi = dt vt_sig, vt_sig = dv . vt / |vt|
         const double xi_b = fsdt_b * (1.0e12 * m + 2.0e6 * m / dt);
         const double vtsig_b = dt * xi_b;
-        dv_b += vtsig_b * tv;
+        dv_b = madd(vtsig_b, tv, dv_b);
         const V3 tv_b = vtsig_b * dv;
-        vt_b += ivt * tv_b;
+        vt_b = madd(ivt, tv_b, vt_b);
         vtmag_b -= dot(tv_b, vt) * (ivt * ivt);
       }
     }
-    vt_b += vtmag_b * tv;   // |vt| = sqrt(vt . vt)
+    vt_b = madd(vtmag_b, tv, vt_b);   // |vt| = sqrt(vt . vt)
   }
   // normal = km comp - gm vn
   lb.km = normal_b * ci.comp;
@@ -131,10 +131,10 @@ __device__ __forceinline__ bool contact_law_fwd_rev(const ContactIn &ci, double 
   // vt = dv - vn n
   dv_b += vt_b;
   vn_b -= dot(vt_b, n);
-  n_b -= vn * vt_b;
+  n_b = madd(-vn, vt_b, n_b);
   // vn = dv . n
-  dv_b += vn_b * n;
-  n_b += vn_b * dv;
+  dv_b = madd(vn_b, n, dv_b);
+  n_b = madd(vn_b, dv, n_b);
   lb.dv = dv_b;
   lb.n = n_b;
   lb.mu = mu_b;
@@ -209,9 +209,9 @@ __device__ __forceinline__ void pair_rev(V3 rl, V3 vl, V3 wl, V3 s1, double rad1
   ob.r -= e_l_b;
   pr_b = (-1.0) * e_m_b;
   // rrc = s1 + rad1 n;  comp = sep - dist;  n = d / dist;  d = sp - s1
-  V3 n_b = lb.n + rad1 * rrc_b;
+  V3 n_b = madd(rad1, rrc_b, lb.n);
   const double dist_b = -lb.comp;
-  const V3 d_b = (1.0 / dist) * (n_b - dot(n, n_b) * n) + dist_b * n;
+  const V3 d_b = madd(dist_b, n, (1.0 / dist) * madd(-dot(n, n_b), n, n_b));
   ob.s += rrc_b;
   ob.s -= d_b;
   ps_b = d_b;

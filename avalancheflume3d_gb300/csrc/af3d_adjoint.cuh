@@ -30,9 +30,14 @@ __device__ __forceinline__ V3 &operator-=(V3 &a, V3 b) {
   a.x -= b.x; a.y -= b.y; a.z -= b.z;
   return a;
 }
-__device__ __forceinline__ double dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+// Products of the reverse pass, with explicit multiply-adds: they form derivatives only (no
+// branch depends on them), so they need not repeat the forward's rounding.
+__device__ __forceinline__ double dot(V3 a, V3 b) { return fma(a.x, b.x, fma(a.y, b.y, a.z * b.z)); }
+__device__ __forceinline__ V3 madd(double k, V3 a, V3 y) {   // y + k a
+  return mk(fma(k, a.x, y.x), fma(k, a.y, y.y), fma(k, a.z, y.z));
+}
 __device__ __forceinline__ V3 cross(V3 a, V3 b) {
-  return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+  return mk(fma(a.y, b.z, -(a.z * b.y)), fma(a.z, b.x, -(a.x * b.z)), fma(a.x, b.y, -(a.y * b.x)));
 }
 __device__ __forceinline__ void atomic_add3(const Planes &P, int x, long s, V3 v) {
   atomicAdd(&P.p[x][s], v.x);
