@@ -50,12 +50,13 @@ constexpr long kKernelsPerStep = kKernelsPerCellBuild + 1 + kKernelsPerForcePass
 constexpr long kKernelsPerKeptStep = kKernelsPerStep - 1;    // a step without the permutation
 constexpr long kKernelsPerRegrid = 4;
 // The clumps are moved into (cell, id) order by a permutation of every plane at most this many
-// steps apart; the steps in between keep the slot order and reach the sorted order through the
-// sort's index array.  Results do not depend on it (every sum runs in (sph_id, cell, id) order);
-// it bounds how far the slot order may drift from the spatial order.
+// steps apart (the context's `resort_every`, by default kResortEvery); the steps in between keep
+// the slot order and reach the sorted order through the sort's index array.  Results do not
+// depend on it (every sum runs in (sph_id, cell, id) order); it bounds how far the slot order
+// may drift from the spatial order.  A long captured graph covers one such period (its first
+// step permutes), so the interval is even (the pointer period of the plane sets is 2).
 constexpr long kResortEvery = 64;
-
-constexpr long kGraphSteps = 64;   // steps per long graph (a multiple of the pointer period 2)
+constexpr long kResortChoices[] = {16, 32, 64, 128, 256};   // what af3d_autotune times
 
 // Pointer state of the context that a captured sequence of steps depends on and changes.
 struct PtrState {
@@ -116,6 +117,7 @@ struct af3d_ctx {
   bool records_valid = false;   // records reflect the current planes
   bool cells_valid = false;     // start[] describes the current layout
   bool sorted = false;          // the slots are in the (cell, id) order of the last sort
+  long resort_every = kResortEvery;   // steps between permutations = steps per long graph
   long since_sort = kResortEvery;   // steps since the planes were last permuted
 
   af3d_particle *d_aos = nullptr;
@@ -362,22 +364,22 @@ long kernels_of(long len, bool resort_first, bool look_first) {
 }
 
 af3d_status run_steps(af3d_ctx *c, long m) {
-  // Captured graphs of 64 steps (the first one permuting the planes) while at least 64 steps
-  // remain, then of two steps (permuting first only when the last permutation is due); an odd
+  // Captured graphs of resort_every steps (the first one permuting the planes) while that many
+  // steps remain, then of two steps (permuting first only when the last permutation is due); an odd
   // last step is enqueued directly.  A graph is replayed when the context is in the pointer
   // state it was captured from, and leaves the context in the state it ended in.  A force pass
   // looks ahead (runs the next step's predictor) when the next step of the run keeps the slot
   // order; a permuting step predicts from the planes itself.
   auto resorts = [&](long since, long left) {   // does the next batch of `left` steps permute first?
     if (left >= 2) {
-      const long l = left >= kGraphSteps ? kGraphSteps : 2;
-      return l == kGraphSteps || since + l > kResortEvery;
+      const long l = left >= c->resort_every ? c->resort_every : 2;
+      return l == c->resort_every || since + l > c->resort_every;
     }
-    return since + 1 > kResortEvery;
+    return since + 1 > c->resort_every;
   };
   while (m >= 2) {
-    const long len = m >= kGraphSteps ? kGraphSteps : 2;
-    const bool resort_first = len == kGraphSteps || c->since_sort + len > kResortEvery;
+    const long len = m >= c->resort_every ? c->resort_every : 2;
+    const bool resort_first = len == c->resort_every || c->since_sort + len > c->resort_every;
     const long since_after = resort_first ? len - 1 : c->since_sort + len;
     const bool look_last = m > len && !resorts(since_after, m - len);
     const bool look_first = c->look;
@@ -417,7 +419,7 @@ af3d_status run_steps(af3d_ctx *c, long m) {
     m -= len;
   }
   if (m == 1) {
-    const bool resort = c->since_sort + 1 > kResortEvery;
+    const bool resort = c->since_sort + 1 > c->resort_every;
     const bool look_first = c->look;
     enqueue_fused_step(c, resort);
     c->since_sort = resort ? 0 : c->since_sort + 1;
@@ -676,7 +678,7 @@ af3d_status enqueue_import(af3d_ctx *c, const af3d_particle *pp, const af3d_vec3
   c->sorted = false;
   c->look = false;
   if (!keep_order) {
-    c->since_sort = kResortEvery;
+    c->since_sort = c->resort_every;
     drop_graphs(c);
   }
   return AF3D_OK;
@@ -769,7 +771,7 @@ af3d_status af3d_step_host(af3d_ctx *c, const af3d_particle *in, const af3d_vec3
   c->cells_valid = false;
   c->sorted = false;
   c->look = false;
-  c->since_sort = kResortEvery;
+  c->since_sort = c->resort_every;
   // The rest of the step (a kept-order step of af3d_step): the sort, then the force pass in
   // kHostParts launches of whole blocks; after each, the part's clumps go to the AoS staging
   // buffer and, on the copy stream, to the host while the next part computes.
@@ -1149,6 +1151,67 @@ af3d_status af3d_step(af3d_ctx *c, long k) {
   return first_error(flags);
 }
 
+af3d_status af3d_set_resort_every(af3d_ctx *c, long steps) {
+  CHECK_CTX(c);
+  if (steps < 2 || steps > 4096 || steps % 2) return fail(AF3D_ERR_ARG, "resort interval: even, 2..4096");
+  if (steps != c->resort_every) drop_graphs(c);
+  c->resort_every = steps;
+  c->since_sort = std::min(c->since_sort, steps);
+  return AF3D_OK;
+}
+
+af3d_status af3d_autotune(af3d_ctx *c, long steps_per_trial, long *resort_every, double *ms_per_step) {
+  CHECK_STATE(c);
+  if (steps_per_trial < 0) return fail(AF3D_ERR_ARG, "negative trial length");
+  if (!c->have_grid) return fail(AF3D_ERR_ARG, "no grid");
+  // Every candidate interval: one untimed period (its graph is captured), then whole periods
+  // timed; a trial that crossed a re-grid is run again.  Every step taken is a step of the run:
+  // the trajectory does not depend on the interval, so tuning costs time only.
+  long best = c->resort_every;
+  double best_ms = 0.0;
+  cudaEvent_t e0, e1;
+  AF3D_CUDA(cudaEventCreate(&e0));
+  AF3D_CUDA(cudaEventCreate(&e1));
+  struct Events {
+    cudaEvent_t a, b;
+    ~Events() {
+      cudaEventDestroy(a);
+      cudaEventDestroy(b);
+    }
+  } events{e0, e1};
+  int ic = 0;
+  for (long cand : kResortChoices) {
+    af3d_status s = af3d_set_resort_every(c, cand);
+    if (s) return s;
+    s = af3d_step(c, cand);
+    if (s) return s;
+    const long k = std::max(2 * cand, (steps_per_trial + cand - 1) / cand * cand);
+    double ms = 0.0;
+    for (int attempt = 0; attempt < 2; attempt++) {
+      const long cc0 = c->cc;
+      AF3D_CUDA(cudaEventRecord(e0, c->st));
+      s = af3d_step(c, k);
+      if (s) return s;
+      AF3D_CUDA(cudaEventRecord(e1, c->st));
+      AF3D_CUDA(cudaEventSynchronize(e1));
+      float t = 0.0f;
+      AF3D_CUDA(cudaEventElapsedTime(&t, e0, e1));
+      ms = t / k;
+      if (cc0 / kRegridEvery == (c->cc - 1) / kRegridEvery) break;   // no re-grid inside
+    }
+    if (ms_per_step) ms_per_step[ic] = ms;
+    ic++;
+    if (best_ms == 0.0 || ms < best_ms) {
+      best_ms = ms;
+      best = cand;
+    }
+  }
+  af3d_status s = af3d_set_resort_every(c, best);
+  if (s) return s;
+  if (resort_every) *resort_every = best;
+  return AF3D_OK;
+}
+
 af3d_status af3d_step_profile(af3d_ctx *c, long k, double *ms) {
   CHECK_STATE(c);
   if (k < 0 || !ms) return fail(AF3D_ERR_ARG, "bad argument");
@@ -1158,10 +1221,10 @@ af3d_status af3d_step_profile(af3d_ctx *c, long k, double *ms) {
   for (long i = 0; i < k; i++) {
     // The steps af3d_step runs, one at a time (the planes are permuted when that is due; a pass
     // looks ahead when the next step keeps the slot order and no re-grid comes between).
-    const bool resort = c->since_sort + 1 > kResortEvery;
+    const bool resort = c->since_sort + 1 > c->resort_every;
     const bool warm = !resort && c->look;
     const bool regrid_after = c->cc % kRegridEvery == 0;
-    const bool look = i + 1 < k && !regrid_after && !((resort ? 0 : c->since_sort + 1) + 1 > kResortEvery);
+    const bool look = i + 1 < k && !regrid_after && !((resort ? 0 : c->since_sort + 1) + 1 > c->resort_every);
     AF3D_CUDA(cudaEventRecord(ev[0], c->st));
     if (!warm) launch_advance_time(c->st, c->d);
     AF3D_CUDA(cudaEventRecord(ev[1], c->st));
@@ -1677,7 +1740,7 @@ extern "C" af3d_status af3d_adjoint(af3d_ctx *c, long steps, long ckpt_every, do
   c->records_valid = false;
   c->cells_valid = false;
   c->look = false;
-  c->since_sort = kResortEvery;
+  c->since_sort = c->resort_every;
   c->cc += steps;
   flags = 0;
   s = read_status(c, &flags);

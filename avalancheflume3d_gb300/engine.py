@@ -114,6 +114,23 @@ class Engine:
             assert a is None or (a.dtype == np.float64 and a.shape == (self.n, 3) and a.flags.c_contiguous)
         self._call("af3d_step_host", ptr(pp), ptr(acc), ptr(anga), ptr(out), ptr(acc_out), ptr(anga_out))
 
+    def set_resort_every(self, steps: int) -> None:
+        """af3d_set_resort_every: steps between permutations of the planes into cell order."""
+        self._call("af3d_set_resort_every", int(steps))
+
+    RESORT_CHOICES = (16, 32, 64, 128, 256)
+
+    def autotune(self, steps_per_trial: int = 256, timings: dict | None = None) -> int:
+        """af3d_autotune: time each permutation interval on real steps of the run, keep the
+        fastest, return it (the trajectory does not depend on it); `timings` receives each
+        interval's ms per step."""
+        r = C.c_long()
+        ms = np.zeros(len(self.RESORT_CHOICES))
+        self._call("af3d_autotune", int(steps_per_trial), C.byref(r), ptr(ms))
+        if timings is not None:
+            timings.update(zip(self.RESORT_CHOICES, ms.tolist()))
+        return r.value
+
     def save_checkpoint(self, path: str) -> None:
         """af3d_save_checkpoint: the whole context state, losslessly, to `path`."""
         self._call("af3d_save_checkpoint", str(path).encode())

@@ -229,6 +229,22 @@ af3d_status af3d_fp64_peak (double *tflops);
 af3d_status af3d_adjoint (af3d_ctx *ctx, long steps, long ckpt_every, double *J, double *param_grad,
                           af3d_vec3 *dr0, double *dR0, af3d_vec3 *dv0, af3d_vec3 *dw0);
 
+/* No counterpart in the reference.  The fused path keeps the slot order between permutations of
+   every plane into (cell, id) order, `steps` apart (even, 2..4096; default 64); one captured
+   graph covers one period.  Results do not depend on it (every sum runs in the reference's
+   order); it trades the permutation's cost against the drift of the slot order from the
+   spatial order. */
+af3d_status af3d_set_resort_every (af3d_ctx *ctx, long steps);
+/* Autotuner (no counterpart in the reference): times af3d_step with each permutation interval in
+   16, 32, 64, 128, 256 (one untimed period, then at least steps_per_trial steps, whole periods)
+   and keeps the fastest, returned in *resort_every (may be NULL), with each interval's time per
+   step in ms_per_step[5] (may be NULL).  Every step it takes is a
+   step of the run -- the trajectory is bit-identical whatever the interval -- so it costs time,
+   not accuracy.  The kernels' other shape parameters are fixed: 128-thread blocks (the force
+   kernel's shared-memory queues), one clump per thread with its contact items pooled over the
+   block, and the reference's cell size (the summation order depends on the cells). */
+af3d_status af3d_autotune (af3d_ctx *ctx, long steps_per_trial, long *resort_every, double *ms_per_step);
+
 /* Status bits raised on the device since the last call (bitmask of 1 << AF3D_ERR_*); clears. */
 af3d_status af3d_get_status (af3d_ctx *ctx, int *flags);
 
