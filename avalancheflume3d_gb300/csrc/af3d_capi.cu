@@ -39,7 +39,7 @@ af3d_status fail(af3d_status code, const std::string &msg) {
   } while (0)
 
 constexpr long kRegridEvery = 2000;   // avalanche_hst.cu:470 and :713 (cc % 2000 == 0)
-constexpr long kKernelsPerCellBuild = 7;   // predict/keys, 3 scan, scatter, rank, permute
+constexpr long kKernelsPerCellBuild = 6;   // predict/keys, 2 scan, scatter, rank, permute
 constexpr long kKernelsPerForcePass = 1;   // lists and forces in one kernel
 #ifndef AF3D_HOST_PARTS
 #define AF3D_HOST_PARTS 4

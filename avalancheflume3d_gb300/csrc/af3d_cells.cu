@@ -3,7 +3,7 @@
 // Replaces the fixed-capacity slot table of cells.cu (clear_cell / clear_ocup / cell_locate).
 // The predictor kernel has already written every clump's bucket key and its atomic arrival rank
 // inside the bucket.  Here:
-//   1. exclusive scan of the bucket counts  -> start[b]      (three-kernel reduce-then-scan)
+//   1. exclusive scan of the bucket counts  -> start[b]      (two-kernel reduce-then-scan)
 //   2. scatter old slots by arrival          -> tmp_slot
 //   3. rank every clump inside its bucket by clump id (buckets hold a handful of clumps), which
 //      makes the final order deterministic and equal to the reference's ascending-id insertion
@@ -91,55 +91,17 @@ __global__ void k_scan_partials(const int *__restrict__ count, int *block_sums, 
   if (threadIdx.x == 0) block_sums[blockIdx.x] = tot;
 }
 
-// One block of kTopThreads threads scans the per-tile sums in place (exclusive): each thread
-// takes kTopItems consecutive tiles, so one block-wide scan covers kTopThreads * kTopItems tiles.
-constexpr int kTopThreads = 1024;
-constexpr int kTopItems = 8;
-
-__global__ void __launch_bounds__(kTopThreads) k_scan_top(int *block_sums, long ntiles, int *start,
-                                                          const DevScalars *d, long n) {
-  __shared__ int warp_tot[kTopThreads / 32];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const long nb = n_buckets(d, n);
-  int carry = 0;
-  for (long b0 = 0; b0 < ntiles; b0 += (long)kTopThreads * kTopItems) {
-    const long i0 = b0 + (long)threadIdx.x * kTopItems;
-    int v[kTopItems];
-    int sum = 0;
-#pragma unroll
-    for (int i = 0; i < kTopItems; i++) {
-      v[i] = i0 + i < ntiles ? block_sums[i0 + i] : 0;
-      sum += v[i];
-    }
-    const int incl = warp_incl_scan(sum);
-    if (lane == 31) warp_tot[wid] = incl;
-    __syncthreads();
-    if (wid == 0) {
-      const int t = warp_tot[lane];
-      const int ti = warp_incl_scan(t);
-      warp_tot[lane] = ti - t;
-    }
-    __syncthreads();
-    int e = carry + warp_tot[wid] + incl - sum;
-#pragma unroll
-    for (int i = 0; i < kTopItems; i++) {
-      if (i0 + i < ntiles) block_sums[i0 + i] = e;
-      e += v[i];
-    }
-    // the chunk total: the last thread's running value
-    __shared__ int chunk_total;
-    if (threadIdx.x == kTopThreads - 1) chunk_total = e - carry;
-    __syncthreads();
-    carry += chunk_total;
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) start[nb] = (int)n;   // every clump has exactly one bucket
-}
-
+// Each tile adds the sum of the tile sums before it (k_scan_partials' raw sums; integer sums
+// are exact in any order), so no separate pass scans them.
 __global__ void k_scan_final(const int *__restrict__ count, const int *__restrict__ block_sums,
                              int *start, const DevScalars *d, long n) {
   const long nb = n_buckets(d, n);
+  if (blockIdx.x == 0 && threadIdx.x == 0) start[nb] = (int)n;   // every clump has one bucket
   if (blockIdx.x * (long)kTile >= nb) return;   // a tile past the buckets in use
+  int part = 0;
+  for (long t = threadIdx.x; t < (long)blockIdx.x; t += kScanThreads) part += block_sums[t];
+  __shared__ int tile_off;
+  block_excl_scan(part, &tile_off);
   const long base = blockIdx.x * (long)kTile + threadIdx.x * (long)kScanItems;
   int v[kScanItems];
   load_counts(count, base, nb, v);
@@ -147,7 +109,7 @@ __global__ void k_scan_final(const int *__restrict__ count, const int *__restric
 #pragma unroll
   for (int i = 0; i < kScanItems; i++) sum += v[i];
   __shared__ int tot;
-  int e = block_excl_scan(sum, &tot) + block_sums[blockIdx.x];
+  int e = block_excl_scan(sum, &tot) + tile_off;
   int o[kScanItems];
 #pragma unroll
   for (int i = 0; i < kScanItems; i++) {
@@ -204,7 +166,6 @@ void launch_sort(const Launch &L, DevScalars *d, Cells c, const long long *id, l
   // so a captured graph stays valid across device-side re-grids.
   const long ntiles = scan_tiles(c.cap);
   k_scan_partials<<<(unsigned)ntiles, kScanThreads, 0, L.st>>>(c.count, c.block_sums, d, advance, L.n);
-  k_scan_top<<<1, kTopThreads, 0, L.st>>>(c.block_sums, ntiles, c.start, d, L.n);
   k_scan_final<<<(unsigned)ntiles, kScanThreads, 0, L.st>>>(c.count, c.block_sums, c.start, d, L.n);
   if (L.n <= 0) return;
   const unsigned g = (unsigned)((L.n + 127) / 128);
