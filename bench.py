@@ -216,6 +216,27 @@ def time_cpu(sys_, fun, pp, threads, seconds, acc=None, anga=None, min_steps=2, 
     return len(pp) * k / dt, k, dt
 
 
+def _replica_worker(seconds):
+    """One single-thread replica of the reference's host routines (the restated port) on the
+    2,048-clump flume (dense bed layer), timed for `seconds`."""
+    from avalancheflume3d_gb300.workloads import flume_2k, flume_state
+    s, f, p = flume_state(flume_2k(layout="bed"))
+    return time_cpu(s, f, p, 1, seconds)
+
+
+def measure_cpu_replicas(procs, seconds):
+    """Independent single-thread runs, one per host core, of the 2,048-clump flume: the host's
+    throughput ceiling for many small flumes (the ensemble's CPU counterpart).  A spawned pool,
+    started before any GPU use of this process."""
+    import multiprocessing as mp
+    with mp.get_context("spawn").Pool(procs) as pool:
+        res = pool.map(_replica_worker, [seconds] * procs)
+    return {"value": sum(r[0] for r in res), "unit": "clump-steps/s", "processes": procs,
+            "steps_per_process": [r[1] for r in res],
+            "sample": "%d independent single-thread runs of the 2,048-clump flume (dense bed layer), "
+                      "%.0f s each, all at once" % (procs, seconds)}
+
+
 def run_reference(args):
     from avalancheflume3d_gb300 import replicas
     if replicas.from_env().rank != 0:
@@ -246,6 +267,7 @@ def run_reference(args):
             "cpu_baseline": {"value": value, "unit": "clump-steps/s", "cores": threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": "clump-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "cpu_replicas": measure_cpu_replicas(threads, args.cpu_seconds),
             "reference_gpu": measure_reference_gpu(args, sys_, fun, pp)}
     print(json.dumps(line), flush=True)
 
