@@ -68,6 +68,7 @@ SIGNATURES = [
     ("af3d_step_host", [_P, _P, _P, _P, _P, _P, _P], C.c_int),
     ("af3d_save_checkpoint", [_P, C.c_char_p], C.c_int),
     ("af3d_set_resort_every", [_P, C.c_long], C.c_int),
+    ("af3d_prepare_steps", [_P, C.c_long], C.c_int),
     ("af3d_autotune", [_P, C.c_long, _P, _P], C.c_int),
     ("af3d_load_checkpoint", [_P, C.c_char_p], C.c_int),
     ("af3d_set_system", [_P, _P], C.c_int),

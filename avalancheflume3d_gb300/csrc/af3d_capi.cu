@@ -363,7 +363,9 @@ long kernels_of(long len, bool resort_first, bool look_first) {
   return first + (len - 1) * warm;
 }
 
-af3d_status run_steps(af3d_ctx *c, long m) {
+// launch false: capture (and cache) the graphs m steps would replay without running anything;
+// the caller restores the context's step state afterwards.
+af3d_status run_steps(af3d_ctx *c, long m, bool launch = true) {
   // Captured graphs of resort_every steps (the first one permuting the planes) while that many
   // steps remain, then of two steps (permuting first only when the last permutation is due); an odd
   // last step is enqueued directly.  A graph is replayed when the context is in the pointer
@@ -411,14 +413,14 @@ af3d_status run_steps(af3d_ctx *c, long m) {
         return fail(AF3D_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
       }
     }
-    AF3D_CUDA(cudaGraphLaunch(g->exec, c->st));
+    if (launch) AF3D_CUDA(cudaGraphLaunch(g->exec, c->st));
     set_ptr_state(c, g->end);
     c->sorted = false;   // the last captured step keeps the slot order
     c->since_sort = since_after;
-    c->launches += kernels_of(len, resort_first, look_first);
+    if (launch) c->launches += kernels_of(len, resort_first, look_first);
     m -= len;
   }
-  if (m == 1) {
+  if (m == 1 && launch) {
     const bool resort = c->since_sort + 1 > c->resort_every;
     const bool look_first = c->look;
     enqueue_fused_step(c, resort);
@@ -1149,6 +1151,23 @@ af3d_status af3d_step(af3d_ctx *c, long k) {
   af3d_status s = read_status(c, &flags);
   if (s) return s;
   return first_error(flags);
+}
+
+af3d_status af3d_prepare_steps(af3d_ctx *c, long k) {
+  CHECK_STATE(c);
+  if (k < 0) return fail(AF3D_ERR_ARG, "negative step count");
+  if (!c->have_grid) return fail(AF3D_ERR_ARG, "no grid");
+  // The graphs the next af3d_step(ctx, k) replays up to its first re-grid, captured now (a
+  // re-grid may move the cell buffers, so later ones are captured when they come).
+  const PtrState p0 = ptr_state(c);
+  const long since0 = c->since_sort;
+  const bool sorted0 = c->sorted;
+  const long to_regrid = (kRegridEvery - c->cc % kRegridEvery) % kRegridEvery;
+  const af3d_status s = run_steps(c, std::min(k, to_regrid + 1), false);
+  set_ptr_state(c, p0);
+  c->since_sort = since0;
+  c->sorted = sorted0;
+  return s;
 }
 
 af3d_status af3d_set_resort_every(af3d_ctx *c, long steps) {

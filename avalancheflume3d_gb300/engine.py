@@ -114,6 +114,10 @@ class Engine:
             assert a is None or (a.dtype == np.float64 and a.shape == (self.n, 3) and a.flags.c_contiguous)
         self._call("af3d_step_host", ptr(pp), ptr(acc), ptr(anga), ptr(out), ptr(acc_out), ptr(anga_out))
 
+    def prepare_steps(self, k: int) -> None:
+        """af3d_prepare_steps: capture the graphs the next step(k) replays, running nothing."""
+        self._call("af3d_prepare_steps", int(k))
+
     def set_resort_every(self, steps: int) -> None:
         """af3d_set_resort_every: steps between permutations of the planes into cell order."""
         self._call("af3d_set_resort_every", int(steps))

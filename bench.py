@@ -334,6 +334,7 @@ def measure_ensemble(args, stream):
     warm = K + 1
 
     def timed(eng):
+        eng.prepare_steps(K)   # the graphs are captured before the timed region
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
@@ -393,7 +394,8 @@ def _adjoint_cost(sys_, fun, pp, K, ckpt, stream):
         eng.import_particles(pp)
         eng.forces()
         eng.swap_accel()
-        eng.step(K)                      # warm-up (captures the graphs)
+        eng.step(K)                      # warm-up
+        eng.prepare_steps(K)             # the timed steps' graphs, captured before they are timed
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
@@ -457,6 +459,7 @@ def time_other_mode(eng, modes, other, args, stream, R, dev, world):
     from avalancheflume3d_gb300 import replicas
     eng.set_fp_mode(modes[other])
     eng.step(2)
+    eng.prepare_steps(args.steps)
     torch.cuda.synchronize()
     o0, o1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     o0.record(stream)
@@ -519,6 +522,7 @@ def run_engine(args):
                 torch.cuda.synchronize()
     eng = make_engine(trace_preroll=True)
     eng.step(args.warmup)
+    eng.prepare_steps(args.steps)   # capture the timed steps' graphs now (nothing runs)
     grid = eng.get_grid()
     ncell3 = int(grid["ncell3"])
     eng.contact_count()   # restart the counter

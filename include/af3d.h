@@ -229,6 +229,10 @@ af3d_status af3d_fp64_peak (double *tflops);
 af3d_status af3d_adjoint (af3d_ctx *ctx, long steps, long ckpt_every, double *J, double *param_grad,
                           af3d_vec3 *dr0, double *dR0, af3d_vec3 *dv0, af3d_vec3 *dw0);
 
+/* No counterpart in the reference.  Captures now, without running anything or changing the
+   state, the CUDA graphs the next af3d_step(ctx, k) will replay (up to its first re-grid), so
+   that their capture does not fall inside a timed or latency-critical call. */
+af3d_status af3d_prepare_steps (af3d_ctx *ctx, long k);
 /* No counterpart in the reference.  The fused path keeps the slot order between permutations of
    every plane into (cell, id) order, `steps` apart (even, 2..4096; default 64); one captured
    graph covers one period.  Results do not depend on it (every sum runs in the reference's

@@ -65,3 +65,21 @@ def test_interval_argument_checks(af3d):
         for bad in (0, 1, 3, 5000):
             with pytest.raises(af3d.EngineError):
                 e.set_resort_every(bad)
+
+
+def test_prepare_steps_changes_nothing(af3d):
+    """af3d_prepare_steps captures graphs without running them: the state is untouched and the
+    steps that follow give the same bytes as steps that capture as they go."""
+    sys, fun, pp = _state()
+    with af3d.Engine(sys, fun) as a, af3d.Engine(sys, fun) as b:
+        for e in (a, b):
+            e.import_particles(pp)
+            e.step(5)
+        before = a.export_particles()
+        a.prepare_steps(150)
+        for x, y in zip(a.export_particles(), before):
+            assert x.tobytes() == y.tobytes()
+        a.step(150)
+        b.step(150)
+        for x, y in zip(a.export_particles(), b.export_particles()):
+            assert x.tobytes() == y.tobytes()
