@@ -630,7 +630,9 @@ def run_engine(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic",
             "config": config_dict(args, cfg, {"parallelism": "replicas" if world > 1 else "single",
-                                              "cells": ncell3, "fp_mode": args.fp_mode}),
+                                              "cells": ncell3, "fp_mode": args.fp_mode,
+                                              "graphs": "captured before the timed steps "
+                                                        "(af3d_prepare_steps)"}),
             "other_fp_mode": other_line,
             "contacts_per_s": world * contacts / (ms / 1e3),
             "contacts_per_step": contacts / args.steps,
