@@ -18,6 +18,7 @@ CSRC = os.path.join(PKG, "csrc")
 ROOT = os.path.dirname(PKG)
 INCLUDE = os.path.join(ROOT, "include")
 LIB = os.path.join(PKG, "libaf3d.so")
+PROGRAM = os.path.join(PKG, "af3d_avalanche")
 OBJ = os.path.join(PKG, "_build")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -79,6 +80,13 @@ def build(force: bool = False, verbose: bool = False) -> str:
         tmp = LIB + ".tmp%d" % os.getpid()
         _run([NVCC, "-shared"] + ARCH + ["-o", tmp] + objs)
         os.replace(tmp, LIB)
+    # the reference's simulation program over the C ABI, linked against the library beside it
+    src = os.path.join(CSRC, "af3d_avalanche.cpp")
+    if force or _stale(PROGRAM, [src, LIB, os.path.join(INCLUDE, "af3d.h")]):
+        tmp = PROGRAM + ".tmp%d" % os.getpid()
+        _run(["g++", "-O2", "-std=c++17", "-I", INCLUDE, "-o", tmp, src, "-L" + PKG, "-laf3d",
+              "-Wl,-rpath,$ORIGIN"])
+        os.replace(tmp, PROGRAM)
     if verbose:
         for l in logs:
             sys.stdout.write(l)

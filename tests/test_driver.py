@@ -1,0 +1,85 @@
+"""af3d_avalanche, the reference's simulation program over the C ABI (csrc/af3d_avalanche.cpp):
+its command line on the CPU, and on the GPU a short run (hopper filling, door, avalanche) whose
+output files have the reference's shapes and whose final state is the one the same calls give
+from Python, byte for byte."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+DATAINPUT = """512         Number of particles.
+15.0        Flume and width.
+75.0        Hopper height.
+0.17979588  Minimum sphere radius.
+0.17979588  Maximum sphere radius.
+10.0        Initial velocity.
+1.0e-6      Time step.
+0.6         Particle-wall coefficient of restitution.
+0.4         Particle-wall coefficient of friction.
+0.6         Particle-particle coefficient of restitution.
+0.4         Particle-particle coefficient of friction.
+1.0e-4      Collision time.
+140.0       Flume length.
+35.0        Flume tilt in degrees.
+9           Number of tagged particles in cells.
+1           Print flag.
+"""
+
+
+@pytest.fixture(scope="module")
+def program():
+    from avalancheflume3d_gb300 import build
+    build.build()
+    return build.PROGRAM
+
+
+def test_command_line(program, tmp_path):
+    r = subprocess.run([program, "--bogus"], capture_output=True, text=True)
+    assert r.returncode == 2 and "usage: af3d_avalanche" in r.stderr
+    r = subprocess.run([program, "--input", str(tmp_path / "missing.dat")], capture_output=True, text=True)
+    assert r.returncode == 1 and "missing.dat" in r.stderr
+
+
+@pytest.mark.gpu
+def test_short_run_matches_the_same_calls_from_python(program, tmp_path):
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import avalancheflume3d_gb300 as af3d
+    (tmp_path / "DataInput.dat").write_text(DATAINPUT)
+    fill, every, aval = 400, 200, 400
+    r = subprocess.run([program, "--max-fill-steps", str(fill), "--out-every", str(every), "--t-end",
+                        repr(aval * 1e-6 - 0.5e-6), "--checkpoint", "final.ckpt"],
+                       cwd=tmp_path, capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "Opening hopper... Avalanche starts!" in r.stdout
+    n = 512
+    lines = lambda f: (tmp_path / f).read_text().splitlines()
+    assert len(lines("mean_velocity_hst.csv")) == fill // every + aval // every
+    assert len(lines("xcm_hst.csv")) == aval // every
+    assert len(lines("snapshots_hst.xyz")) == (fill // every + aval // every) * (4 * n + 4)
+    assert len(lines("last_config.dat")) == 4 + n
+    # the same calls from Python
+    v = af3d.load_datainput(str(tmp_path / "DataInput.dat"))
+    sys, fun = af3d.derive_system(v)
+    pp = af3d.generate_particles(sys)
+    af3d.calculate_particle_parameters(pp)
+    af3d.place_particles(sys, pp)
+    af3d.set_initial_velocity(sys, pp)
+    af3d.sphere_centres(pp)
+    sys["tot_mass"] = float(np.sum(pp["mass"]))
+    with af3d.Engine(sys, fun, ntags=int(v["ntags"]), phase=af3d.PHASE_FILL) as e:
+        e.import_particles(pp)
+        e.forces()
+        e.swap_accel()
+        e.step(fill)
+        e.open_door()
+        e.step(aval)
+        want = e.export_particles()
+    raw = np.fromfile(tmp_path / "final.ckpt", dtype=np.uint8)
+    off = 64 + 256 + 24 + 168   # header, then the flume's system_par, Funnel, cell_par
+    got = raw[off:off + 408 * n].view(af3d.PARTICLE)
+    assert got.tobytes() == want[0].tobytes()
+    acc = raw[off + 408 * n:off + 432 * n].view(np.float64).reshape(n, 3)
+    assert acc.tobytes() == want[1].tobytes()
