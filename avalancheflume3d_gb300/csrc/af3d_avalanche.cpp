@@ -16,6 +16,7 @@
 //
 // Usage: af3d_avalanche [--input DataInput.dat] [--t-end 2.0] [--out-every 20000]
 //                       [--fp exact|fast] [--max-fill-steps N] [--checkpoint PATH]
+//                       [--resume PATH]   (a checkpoint written by --checkpoint: the run continues)
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -35,6 +36,7 @@ struct Options {
   bool fast = false;
   long max_fill_steps = -1;   // < 0: no limit
   std::string checkpoint;
+  std::string resume;
 };
 
 bool parse(int argc, char **argv, Options &o) {
@@ -54,10 +56,11 @@ bool parse(int argc, char **argv, Options &o) {
     else if (a == "--fp" && (v = value("--fp"))) o.fast = std::string(v) == "fast";
     else if (a == "--max-fill-steps" && (v = value("--max-fill-steps"))) o.max_fill_steps = std::atol(v);
     else if (a == "--checkpoint" && (v = value("--checkpoint"))) o.checkpoint = v;
+    else if (a == "--resume" && (v = value("--resume"))) o.resume = v;
     else {
       std::fprintf(stderr,
                    "usage: af3d_avalanche [--input DataInput.dat] [--t-end S] [--out-every N] "
-                   "[--fp exact|fast] [--max-fill-steps N] [--checkpoint PATH]\n");
+                   "[--fp exact|fast] [--max-fill-steps N] [--checkpoint PATH] [--resume PATH]\n");
       return false;
     }
     if (!v) return false;
@@ -126,8 +129,14 @@ int main(int argc, char **argv) {
     ~Destroy() { af3d_destroy(c); }
   } destroy{ctx};
   if (o.fast && !ok(af3d_set_fp_mode(ctx, AF3D_FP_FAST), "af3d_set_fp_mode")) return 1;
-  if (!ok(af3d_import_particles(ctx, pp.data(), nullptr, nullptr), "import")) return 1;
-  if (!ok(af3d_forces(ctx), "start-up force pass") || !ok(af3d_swap_accel(ctx), "swap")) return 1;
+  if (o.resume.empty()) {
+    if (!ok(af3d_import_particles(ctx, pp.data(), nullptr, nullptr), "import")) return 1;
+    if (!ok(af3d_forces(ctx), "start-up force pass") || !ok(af3d_swap_accel(ctx), "swap")) return 1;
+  } else {
+    // a run saved by --checkpoint continues where it stopped (phase, clock, state, grid)
+    if (!ok(af3d_load_checkpoint(ctx, o.resume.c_str()), "resume")) return 1;
+    if (o.fast && !ok(af3d_set_fp_mode(ctx, AF3D_FP_FAST), "af3d_set_fp_mode")) return 1;
+  }
 
   long jj = 0;
   // One output frame: the particles back on the host, the snapshot files and last_config.dat.
@@ -146,11 +155,13 @@ int main(int argc, char **argv) {
     return true;
   };
 
-  // Hopper filling
-  std::printf("Filling hopper...\n");
+  // Hopper filling (a resumed run whose door was open -- side.x past the hopper's wall at
+  // x = 15, avalanche_hst.cu:607 -- goes straight on with the avalanche)
   if (!ok(af3d_get_system(ctx, &sys), "get_system")) return 1;
+  const bool resumed_open = !o.resume.empty() && sys.side.x > 15.0;
+  if (!resumed_open) std::printf("Filling hopper...\n");
   long cc = 0;
-  while (sys.time < 0.0 && (o.max_fill_steps < 0 || cc < o.max_fill_steps)) {
+  while (!resumed_open && sys.time < 0.0 && (o.max_fill_steps < 0 || cc < o.max_fill_steps)) {
     long k = steps_until(sys.time, 0.0, sys.dt, o.out_every);
     if (o.max_fill_steps >= 0) k = std::min(k, o.max_fill_steps - cc);
     if (k <= 0) break;
@@ -162,9 +173,11 @@ int main(int argc, char **argv) {
     if (vmean < 0.1 * sys.v0) break;
   }
 
-  // The door opens; the avalanche runs
-  if (!ok(af3d_open_door(ctx), "af3d_open_door")) return 1;
-  std::printf("Opening hopper... Avalanche starts!\n");
+  // The door opens (unless it was open already); the avalanche runs
+  if (!resumed_open) {
+    if (!ok(af3d_open_door(ctx), "af3d_open_door")) return 1;
+    std::printf("Opening hopper... Avalanche starts!\n");
+  }
   if (!ok(af3d_get_system(ctx, &sys), "get_system")) return 1;
   cc = 0;
   while (sys.time < o.t_end) {

@@ -83,3 +83,29 @@ def test_short_run_matches_the_same_calls_from_python(program, tmp_path):
     assert got.tobytes() == want[0].tobytes()
     acc = raw[off + 408 * n:off + 432 * n].view(np.float64).reshape(n, 3)
     assert acc.tobytes() == want[1].tobytes()
+
+
+@pytest.mark.gpu
+def test_resumed_run_continues_bit_for_bit(program, tmp_path):
+    """A run stopped with --checkpoint and continued with --resume ends in the bytes of the run
+    that did not stop."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    for d in ("straight", "first", "second"):
+        (tmp_path / d).mkdir()
+        (tmp_path / d / "DataInput.dat").write_text(DATAINPUT)
+    run = lambda d, *a: subprocess.run([program, *a], cwd=tmp_path / d, capture_output=True, text=True)
+    r = run("straight", "--max-fill-steps", "200", "--out-every", "100", "--t-end", repr(400e-6 - 0.5e-6),
+            "--checkpoint", "end.ckpt")
+    assert r.returncode == 0, r.stderr
+    r = run("first", "--max-fill-steps", "200", "--out-every", "100", "--t-end", repr(200e-6 - 0.5e-6),
+            "--checkpoint", "mid.ckpt")
+    assert r.returncode == 0, r.stderr
+    r = run("second", "--resume", str(tmp_path / "first" / "mid.ckpt"), "--out-every", "100", "--t-end",
+            repr(400e-6 - 0.5e-6), "--checkpoint", "end.ckpt")
+    assert r.returncode == 0, r.stderr
+    assert "Opening hopper" not in r.stdout   # the door was open already
+    a = (tmp_path / "straight" / "end.ckpt").read_bytes()
+    b = (tmp_path / "second" / "end.ckpt").read_bytes()
+    assert a == b
