@@ -740,8 +740,20 @@ af3d_status af3d_step_host(af3d_ctx *c, const af3d_particle *in, const af3d_vec3
     if (!e) AF3D_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   for (cudaEvent_t &e : c->part_in)
     if (!e) AF3D_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-  const long per = (n + kHostParts - 1) / kHostParts;
-  const long part = (per + kForceBlock - 1) / kForceBlock * kForceBlock;
+  // Part boundaries on whole blocks.  The first part to leave the device (force pass, then copy
+  // out) and the last part to arrive (copy in, then conversion and predictor) are the ones
+  // whose work nothing overlaps, so they get an eighth of the clumps and the other three share
+  // the rest: `out_at` splits the export, `in_at` (the mirror image) the import.
+  auto round_up = [](long x) { return (x + kForceBlock - 1) / kForceBlock * kForceBlock; };
+  long out_at[kHostParts + 1], in_at[kHostParts + 1];
+  out_at[0] = 0;
+  out_at[1] = std::min(n, round_up((n + 7) / 8));
+  for (int j = 2; j <= kHostParts; j++)
+    out_at[j] = std::min(n, out_at[1] + round_up((n - out_at[1]) * (j - 1) / (kHostParts - 1)));
+  out_at[kHostParts] = n;
+  in_at[0] = 0;
+  for (int j = 1; j < kHostParts; j++) in_at[j] = std::min(n, round_up((n - (n + 7) / 8) * j / (kHostParts - 1)));
+  in_at[kHostParts] = n;
   // Import in input order (slot i holds clump i), so a part of the slots is a contiguous part of
   // the host arrays; the step keeps that order (the cell sort only orders the neighbour search).
   // Each part's copy to the device (copy stream) releases its conversion to planes and its
@@ -752,8 +764,9 @@ af3d_status af3d_step_host(af3d_ctx *c, const af3d_particle *in, const af3d_vec3
   drop_graphs(c);   // the slot order changes (the next af3d_step permutes when it is due)
   launch_advance_time(c->st, c->d);
   int parts = 0;
-  for (long s0 = 0; s0 < n; s0 += part, parts++) {
-    const long cnt = std::min(part, n - s0);
+  for (int j = 0; j < kHostParts; j++) {
+    const long s0 = in_at[j], cnt = in_at[j + 1] - s0;
+    if (cnt <= 0) continue;
     AF3D_CUDA(cudaMemcpyAsync(c->d_aos + s0, in + s0, sizeof(af3d_particle) * cnt, cudaMemcpyHostToDevice,
                               c->xfer));
     if (acc_in)
@@ -767,6 +780,7 @@ af3d_status af3d_step_host(af3d_ctx *c, const af3d_particle *in, const af3d_vec3
     launch_aos_to_planes(c->L(), c->d_aos, acc_in ? c->d_acc : nullptr, anga_in ? c->d_anga : nullptr,
                          c->flume_of_id, c->cur, c->id_cur, c->fl_cur, false, s0, cnt);
     predict_for(c, true, true, true, true, s0, cnt);
+    parts++;
   }
   c->imported = true;
   c->records_valid = false;
@@ -780,9 +794,11 @@ af3d_status af3d_step_host(af3d_ctx *c, const af3d_particle *in, const af3d_vec3
   launch_sort(c->L(), c->d, c->cells, c->id_cur, c->ntags, c->cull, false);
   Planes after = c->cur;   // the plane set as the step leaves it (accelerations swapped)
   swap_accel_planes(after);
+  const int in_parts = parts;
   parts = 0;
-  for (long s0 = 0; s0 < n; s0 += part, parts++) {
-    const long cnt = std::min(part, n - s0);
+  for (int j = 0; j < kHostParts; j++) {
+    const long s0 = out_at[j], cnt = out_at[j + 1] - s0;
+    if (cnt <= 0) continue;
     forces_for(c, false, c->cells.perm, c->cur, false, false, s0, cnt);
     launch_planes_to_aos(c->L(), after, c->id_cur, c->fl_cur, c->d_aos, acc_out ? c->d_acc : nullptr,
                          anga_out ? c->d_anga : nullptr, c->d, s0, cnt);
@@ -796,10 +812,11 @@ af3d_status af3d_step_host(af3d_ctx *c, const af3d_particle *in, const af3d_vec3
     if (anga_out)
       AF3D_CUDA(cudaMemcpyAsync(anga_out + s0, c->d_anga + 3 * s0, sizeof(double) * 3 * cnt,
                                 cudaMemcpyDeviceToHost, c->xfer));
+    parts++;
   }
   swap_accel_planes(c->cur);
   swap_accel_planes(c->alt);
-  c->launches += (kKernelsPerKeptStep - kKernelsPerForcePass - 1) + 4L * parts;
+  c->launches += (kKernelsPerKeptStep - kKernelsPerForcePass - 1) + 2L * in_parts + 2L * parts;
   // af3d_step's bookkeeping for one step
   c->time = c->time + c->sys[0].dt;
   const bool do_regrid = c->cc % kRegridEvery == 0;
