@@ -124,9 +124,10 @@ af3d_status af3d_export_particles (af3d_ctx *ctx, af3d_particle *pp, af3d_vec3 *
    acc_in, anga_in), af3d_step(ctx, 1) and af3d_export_particles(out, acc_out, anga_out) in one
    call, with the same results (in and out may be the same arrays; acc_in/anga_in NULL: zero
    accelerations; acc_out/anga_out NULL: not written).  The clumps are imported in input order
-   (slot i holds clump i) and the step keeps that order, so each quarter of the clumps is copied
-   in, on a copy stream of its own, while the previous one is converted and predicted, and copied
-   out while the force pass of the next one runs.  There is no
+   (slot i holds clump i) and the step keeps that order, so each of four parts of the clumps is
+   copied in, on a copy stream of its own, while the previous one is converted and predicted,
+   and copied out while the force pass of the next one runs (the part nothing overlaps at each
+   end holds an eighth of the clumps).  There is no
    counterpart in the reference: it replaces the host-master step of its loop
    (avalanche_hst.cu:668-710 with the particle array on the host) by one call. */
 af3d_status af3d_step_host (af3d_ctx *ctx, const af3d_particle *in, const af3d_vec3 *acc_in,
