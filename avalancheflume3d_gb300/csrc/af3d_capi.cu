@@ -742,17 +742,18 @@ af3d_status af3d_step_host(af3d_ctx *c, const af3d_particle *in, const af3d_vec3
     if (!e) AF3D_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   // Part boundaries on whole blocks.  The first part to leave the device (force pass, then copy
   // out) and the last part to arrive (copy in, then conversion and predictor) are the ones
-  // whose work nothing overlaps, so they get an eighth of the clumps and the other three share
-  // the rest: `out_at` splits the export, `in_at` (the mirror image) the import.
+  // whose work nothing overlaps, so they get half a part's share of the clumps and the others
+  // share the rest: `out_at` splits the export, `in_at` (the mirror image) the import.
   auto round_up = [](long x) { return (x + kForceBlock - 1) / kForceBlock * kForceBlock; };
+  const long edge = (n + 2 * kHostParts - 1) / (2 * kHostParts);
   long out_at[kHostParts + 1], in_at[kHostParts + 1];
   out_at[0] = 0;
-  out_at[1] = std::min(n, round_up((n + 7) / 8));
+  out_at[1] = std::min(n, round_up(edge));
   for (int j = 2; j <= kHostParts; j++)
     out_at[j] = std::min(n, out_at[1] + round_up((n - out_at[1]) * (j - 1) / (kHostParts - 1)));
   out_at[kHostParts] = n;
   in_at[0] = 0;
-  for (int j = 1; j < kHostParts; j++) in_at[j] = std::min(n, round_up((n - (n + 7) / 8) * j / (kHostParts - 1)));
+  for (int j = 1; j < kHostParts; j++) in_at[j] = std::min(n, round_up((n - edge) * j / (kHostParts - 1)));
   in_at[kHostParts] = n;
   // Import in input order (slot i holds clump i), so a part of the slots is a contiguous part of
   // the host arrays; the step keeps that order (the cell sort only orders the neighbour search).
