@@ -110,8 +110,10 @@ SIGNATURES = [
     ("af3d_get_cells", [_P, _P, _P, _P], C.c_int),
     ("af3d_contact_pairs", [_P, _P, C.c_long, _P, C.c_int], C.c_int),
     ("af3d_contact_count", [_P, _P], C.c_int),
+    ("af3d_list_overflows", [_P, _P], C.c_int),
     ("af3d_contact_pairs_noalloc", [_P, _P, C.c_long, _P, C.c_int], C.c_int),
     ("af3d_load_datainput", [C.c_char_p, _P], C.c_int),
+    ("af3d_read_datainput", [_P, _P], C.c_int),
     ("af3d_derive_system", [_P, _P, _P], C.c_int),
     ("af3d_error_check", [_P, C.c_char_p, C.c_size_t], C.c_int),
     ("af3d_write_last_config", [C.c_char_p, C.c_int, C.c_double, C.c_long, C.c_long, _P, C.c_long], C.c_int),

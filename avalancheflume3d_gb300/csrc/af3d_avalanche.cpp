@@ -15,6 +15,8 @@
 //   through af3d_step (fused, graph-replayed, device re-grid every 2000 steps).
 //
 // Usage: af3d_avalanche [--input DataInput.dat] [--t-end 2.0] [--out-every 20000]
+//   (without --input, or with --input -, the 16 lines of DataInput.dat are read from standard
+//   input, as the reference reads them: af3d_avalanche < DataInput.dat)
 //                       [--fp exact|fast] [--max-fill-steps N] [--checkpoint PATH]
 //                       [--resume PATH]   (a checkpoint written by --checkpoint: the run continues)
 #include <algorithm>
@@ -30,7 +32,7 @@
 namespace {
 
 struct Options {
-  std::string input = "DataInput.dat";
+  std::string input = "-";   // standard input, as avalanche_hst.cu:34-81 reads it
   double t_end = 2.0;   // avalanche_hst.cu:633
   long out_every = 20000;
   bool fast = false;
@@ -99,8 +101,10 @@ int main(int argc, char **argv) {
   Options o;
   if (!parse(argc, argv, o)) return 2;
   af3d_inputs in;
-  if (af3d_load_datainput(o.input.c_str(), &in) != AF3D_OK) {
-    std::fprintf(stderr, "cannot read the 16 lines of %s\n", o.input.c_str());
+  const bool from_stdin = o.input == "-";
+  if ((from_stdin ? af3d_read_datainput(stdin, &in) : af3d_load_datainput(o.input.c_str(), &in)) != AF3D_OK) {
+    std::fprintf(stderr, "cannot read the 16 lines of %s\n", from_stdin ? "DataInput.dat on standard input"
+                                                                         : o.input.c_str());
     return 1;
   }
   af3d_system_par sys;

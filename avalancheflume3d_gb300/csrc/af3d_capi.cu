@@ -1386,8 +1386,13 @@ af3d_status af3d_contact_pairs(af3d_ctx *c, long *out, long cap, long *count, in
   CHECK_STATE(c);
   af3d_status s = ensure_records(c);
   if (s) return s;
-  long long *d_out = nullptr;
-  if (cap > 0) AF3D_CUDA(cudaMalloc(&d_out, sizeof(long long) * 3 * cap));
+  // the staging buffer is freed on every exit path, the early error returns included
+  struct Staging {
+    long long *p = nullptr;
+    ~Staging() { if (p) cudaFree(p); }
+  } staging;
+  if (cap > 0) AF3D_CUDA(cudaMalloc(&staging.p, sizeof(long long) * 3 * cap));
+  long long *d_out = staging.p;
   AF3D_CUDA(cudaMemsetAsync(c->d_count, 0, sizeof(unsigned long long), c->st));
   launch_contact_pairs(c->L(), c->cur, c->d, c->fl_cur, c->nbr, c->cull, c->cells.start, c->id_cur, d_out,
                        c->d_count, cap, active);
@@ -1398,7 +1403,6 @@ af3d_status af3d_contact_pairs(af3d_ctx *c, long *out, long cap, long *count, in
   if (cap > 0 && out)
     AF3D_CUDA(cudaMemcpy(out, d_out, sizeof(long long) * 3 * std::min<long>(cap, (long)cnt),
                          cudaMemcpyDeviceToHost));
-  if (d_out) cudaFree(d_out);
   return AF3D_OK;
 }
 
@@ -1408,6 +1412,17 @@ af3d_status af3d_contact_count(af3d_ctx *c, long *count) {
   unsigned long long v = 0, zero = 0;
   AF3D_CUDA(cudaMemcpyAsync(&v, &c->d->contacts, sizeof(v), cudaMemcpyDeviceToHost, c->st));
   AF3D_CUDA(cudaMemcpyAsync(&c->d->contacts, &zero, sizeof(zero), cudaMemcpyHostToDevice, c->st));
+  AF3D_CUDA(cudaStreamSynchronize(c->st));
+  *count = (long)v;
+  return AF3D_OK;
+}
+
+af3d_status af3d_list_overflows(af3d_ctx *c, long *count) {
+  CHECK_CTX(c);
+  if (!count) return fail(AF3D_ERR_ARG, "null argument");
+  unsigned long long v = 0, zero = 0;
+  AF3D_CUDA(cudaMemcpyAsync(&v, &c->d->overflows, sizeof(v), cudaMemcpyDeviceToHost, c->st));
+  AF3D_CUDA(cudaMemcpyAsync(&c->d->overflows, &zero, sizeof(zero), cudaMemcpyHostToDevice, c->st));
   AF3D_CUDA(cudaStreamSynchronize(c->st));
   *count = (long)v;
   return AF3D_OK;

@@ -36,10 +36,8 @@ bool first_token(FILE *fp, const char *fmt, void *out) {
 
 extern "C" {
 
-af3d_status af3d_load_datainput(const char *path, af3d_inputs *in) {
-  if (!path || !in) return AF3D_ERR_ARG;
-  FILE *fp = fopen(path, "r");
-  if (!fp) return AF3D_ERR_IO;
+af3d_status af3d_read_datainput(FILE *fp, af3d_inputs *in) {
+  if (!fp || !in) return AF3D_ERR_ARG;
   af3d_inputs v{};
   // avalanche_hst.cu:34-81: the first token of each of 16 lines, in this order.
   bool ok = first_token(fp, "%ld", &v.npart) && first_token(fp, "%lf", &v.width) &&
@@ -50,10 +48,18 @@ af3d_status af3d_load_datainput(const char *path, af3d_inputs *in) {
             first_token(fp, "%lf", &v.mu_pp) && first_token(fp, "%lf", &v.t_coll) &&
             first_token(fp, "%lf", &v.Lflume) && first_token(fp, "%lf", &v.tilt_deg) &&
             first_token(fp, "%ld", &v.ntags) && first_token(fp, "%d", &v.print_flag);
-  fclose(fp);
   if (!ok) return AF3D_ERR_IO;
   *in = v;
   return AF3D_OK;
+}
+
+af3d_status af3d_load_datainput(const char *path, af3d_inputs *in) {
+  if (!path || !in) return AF3D_ERR_ARG;
+  FILE *fp = fopen(path, "r");
+  if (!fp) return AF3D_ERR_IO;
+  const af3d_status s = af3d_read_datainput(fp, in);
+  fclose(fp);
+  return s;
 }
 
 af3d_status af3d_derive_system(const af3d_inputs *in, af3d_system_par *sys, af3d_funnel *fun) {

@@ -138,6 +138,7 @@ struct DevScalars {
   int             status;     // bitmask of 1 << AF3D_ERR_*
   int             nflumes;
   unsigned long long contacts; // active sphere-sphere contacts summed over fused force passes
+  unsigned long long overflows; // clumps whose item lists overflowed, over fused force passes
   long long       ncell_total; // sum of the flumes' ncell3: the first removed-clump bucket
   long long       pending;     // > 0: a re-grid derived grids needing this many cell buckets
   DevFlume       *flumes;      // [nflumes]

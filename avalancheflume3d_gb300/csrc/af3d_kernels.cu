@@ -824,6 +824,7 @@ __device__ __forceinline__ void fused_body(const Consts &c, Planes P, Planes out
   if (valid) {
     if (lists.cnt) lists.cnt[s] = pack_list_counts(listed, lc.pre, lc.pair);
     if (lists.ovf && listed < 0) *lists.ovf = 1;
+    if (listed < 0) atomicAdd(&d->overflows, 1ull);   // rare: counted for the diagnostics
     if (WRITE_FT) {
       store3(P, FX, s, F);
       store3(P, TX, s, T);

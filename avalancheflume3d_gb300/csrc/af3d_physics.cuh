@@ -7,10 +7,23 @@
 // sin/cos come from CUDA's libm, which may differ from the host libm in the last bit.
 //
 // Fast mode (built with -DAF3D_FAST -fmad=true): the same FP64 physics with multiply-adds
-// contracted, normals and tangents from a reciprocal square root instead of sqrt and three
-// divisions, and quotients by a shared divisor taken as products with one reciprocal.  Each of
-// these changes a result by a few units in the last place, so forces agree with the reference
-// to ~1e-14 relative rather than bit for bit.
+// contracted, normals and tangents from a reciprocal square root instead of three divisions,
+// and quotients by a shared divisor taken as products with one reciprocal.  Each of these
+// changes a result by a few units in the last place, so forces agree with the reference to
+// ~1e-14 relative rather than bit for bit.
+//
+// Geometry stays exact in both modes.  The distances that decide whether a contact exists, and
+// whose difference from the radius is the contact's compression, are evaluated with
+// non-contracting intrinsics (__dmul_rn, __dadd_rn, __dsub_rn: never fused into a multiply-add)
+// in the reference's order, and the centre distance of a sphere pair or a funnel corner is the
+// correctly rounded sqrt: the squared distance of two sphere centres, the slope-frame
+// coordinates, the distance to the flume bed and to the funnel walls.  A compression is a
+// difference of nearly equal numbers: the plane distances cancel coordinates of up to ~100 cm,
+// a sphere-pair distance cancels against the radii, down to compressions of 1e-7 cm or less in
+// a freshly loaded contact, so a different last bit (~1e-14 cm for a plane, ~3e-17 cm for a
+// pair) would change such a contact's force by up to ~1e-7 (plane) or ~1e-9 (pair) of itself.
+// Kept exact, the fast mode takes every overlap decision and computes every compression as the
+// exact mode does.
 #pragma once
 
 #include "af3d_internal.h"
@@ -222,9 +235,11 @@ __device__ __forceinline__ bool apply_law(const ContactIn &ci, V3 r, const Const
   return true;
 }
 
-// rotate_vectors.cu:28-30 (lab -> slope frame) and force_funnel.cu:88-93 (slope -> lab).
+// rotate_vectors.cu:28-30 (lab -> slope frame; uncontracted in both modes) and
+// force_funnel.cu:88-93 (slope -> lab).
 __device__ __forceinline__ V3 to_slope(V3 r, double cost, double sint) {
-  return mk(r.x * cost - r.z * sint, r.y, r.x * sint + r.z * cost);
+  return mk(__dsub_rn(__dmul_rn(r.x, cost), __dmul_rn(r.z, sint)), r.y,
+            __dadd_rn(__dmul_rn(r.x, sint), __dmul_rn(r.z, cost)));
 }
 __device__ __forceinline__ V3 to_lab(V3 q, double cost, double sint) {
   return mk(q.x * cost + q.z * sint, q.y, q.z * cost - q.x * sint);
@@ -269,8 +284,8 @@ __device__ __forceinline__ bool funnel_sphere(const Sph &o, const Consts &c, Con
   V3 q = to_slope(o.s, c.cost, c.sint), qc, nr, rrc, n;
   double dist, comp = 0.0;
   int touch = 0;
-  if (q.x > kLFUNNEL - ri * c.sinfi) return false;
-  dist = fabs(q.y - q.x * c.tanfi) * c.cosfi;
+  if (q.x > __dsub_rn(kLFUNNEL, __dmul_rn(ri, c.sinfi))) return false;
+  dist = fabs(__dsub_rn(q.y, __dmul_rn(q.x, c.tanfi))) * c.cosfi;
   if (dist <= ri) {
     touch = 1;
     qc = mk(q.x + dist * c.sinfi, q.y - dist * c.cosfi, q.z);
@@ -279,7 +294,7 @@ __device__ __forceinline__ bool funnel_sphere(const Sph &o, const Consts &c, Con
     n = to_lab(nr, c.cost, c.sint);
     comp = ri - dist;
   }
-  dist = fabs(kYFUNNEL - q.y - q.x * c.tanfi) * c.cosfi;
+  dist = fabs(__dsub_rn(kYFUNNEL - q.y, __dmul_rn(q.x, c.tanfi))) * c.cosfi;
   if (dist <= ri) {
     touch = 2;
     qc = mk(q.x + dist * c.sinfi, q.y + dist * c.cosfi, q.z);
@@ -298,7 +313,7 @@ __device__ __forceinline__ bool fcorners_sphere(const Sph &o, const Consts &c, C
   const double ri = o.rad;
   const double yfun_l = c.dy2, yfun_r = c.side_y + c.dy2, hsy = c.dy2 + c.side_y / 2.0;
   V3 q = to_slope(o.s, c.cost, c.sint);
-  if (q.x < kLFUNNEL - ri * c.sinfi || q.x > kLFUNNEL + ri) return false;
+  if (q.x < __dsub_rn(kLFUNNEL, __dmul_rn(ri, c.sinfi)) || q.x > kLFUNNEL + ri) return false;
   if (q.y > yfun_r || q.y < yfun_l) return false;
   double yc = (q.y <= hsy) ? yfun_l : yfun_r;
   double sep2 = ri * ri;
@@ -307,13 +322,13 @@ __device__ __forceinline__ bool fcorners_sphere(const Sph &o, const Consts &c, C
   double dist2 = d.x * d.x;
   if (dist2 > sep2) return false;
   d.y = yc - q.y;
-  dist2 += d.y * d.y;
+  dist2 = __dadd_rn(dist2, __dmul_rn(d.y, d.y));
   if (dist2 > sep2) return false;
   double dist;
   V3 nr;
   if (kFast) {
     const double inv = rsqrt(dist2);
-    dist = dist2 * inv;
+    dist = sqrt(dist2);   // correctly rounded: the compression ri - dist is the exact mode's
     nr = mk(d.x * inv, d.y * inv, 0.0);
   } else {
     dist = sqrt(dist2);
@@ -347,7 +362,7 @@ __device__ __forceinline__ bool flume_sphere(const Sph &o, const Consts &c, Cont
   const double ri = o.rad;
   const double tant = c.tant;   // c.sint / c.cost, formed once per flume by the host
   const V3 s = o.s;
-  double rect = -tant * s.x - s.z;
+  double rect = __dsub_rn(__dmul_rn(-tant, s.x), s.z);
   double dist = fabs(c.cost * rect);
   if (!(dist <= ri)) return false;
   const V3 n = mk(-c.sint, 0.0, -c.cost);
@@ -482,8 +497,8 @@ __device__ __forceinline__ bool spheres_overlap(const V3 &s1, double rad_1, cons
   d.y = m.s[3 * sm + 1] - s1.y;
   d.z = m.s[3 * sm + 2] - s1.z;
   dist2 = d.x * d.x;
-  dist2 += d.y * d.y;
-  dist2 += d.z * d.z;
+  dist2 = __dadd_rn(dist2, __dmul_rn(d.y, d.y));   // uncontracted in both modes
+  dist2 = __dadd_rn(dist2, __dmul_rn(d.z, d.z));
   return dist2 < sep2;
 }
 
@@ -499,7 +514,7 @@ __device__ __forceinline__ bool pair_input(const V3 &rrl, const V3 &vvl, const V
   double dist;
   if (kFast) {
     const double inv = rsqrt(dist2);
-    dist = dist2 * inv;
+    dist = sqrt(dist2);   // correctly rounded: the compression sep - dist is the exact mode's
     ci.n = mk(d.x * inv, d.y * inv, d.z * inv);
   } else {
     dist = sqrt(dist2);

@@ -299,6 +299,13 @@ class Engine:
         self._call("af3d_contact_count", C.byref(c))
         return c.value
 
+    def list_overflows(self) -> int:
+        """Clumps whose item lists overflowed in the fused force passes since the last call
+        (their contacts ran by the per-clump cell walk)."""
+        c = C.c_long()
+        self._call("af3d_list_overflows", C.byref(c))
+        return c.value
+
 
 # ---- host I/O and generators (no GPU) ----
 
@@ -362,6 +369,16 @@ class Rannew64:
     @property
     def ref(self):
         return C.byref(self._s)
+
+    def clone(self) -> "Rannew64":
+        """An independent generator in this one's state."""
+        g = Rannew64.__new__(Rannew64)
+        g._s = RNG.from_buffer_copy(self._s)
+        return g
+
+    def assign(self, other: "Rannew64") -> None:
+        """Take over `other`'s state."""
+        C.memmove(C.addressof(self._s), C.addressof(other._s), C.sizeof(RNG))
 
 
 def generate_particles(sys: np.ndarray) -> np.ndarray:

@@ -45,7 +45,9 @@ class FlumeConfig:
     v0: float = 0.0              # initial speed in the reference's random directions
     seed: int = 20240613         # rannew64 seed of the orientations
     hopper_height: float | None = None
-    layout: str = "lattice"      # "lattice" | "pile" | "bed" (see flume_state)
+    size_spread: float = 0.0     # per-clump size factor ~ U[1 - spread, 1 + spread] (polydisperse)
+    ntags: int = 9               # DataInput.dat line 15: slots per cell (at most ntags - 1 clumps)
+    layout: str = "lattice"      # "lattice" | "pile" | "bed" (see flume_state); "funnel" (see funnel_state)
     overlap: float | None = None  # how far each clump is pressed into its support [cm]:
                                   # pile 2e-5 (default), bed 0 (default; gravity loads the layer)
 
@@ -64,12 +66,13 @@ def flume_inputs(cfg: FlumeConfig) -> np.ndarray:
     v = np.zeros((), dtype=INPUTS)
     v["npart"] = cfg.n
     v["width"], v["hopper_height"] = cfg.width, height
-    v["rmin"] = v["rmax"] = cfg.radius
+    v["rmin"] = cfg.radius * (1.0 - cfg.size_spread)
+    v["rmax"] = cfg.radius * (1.0 + cfg.size_spread)
     v["v0"], v["dt"] = cfg.v0, cfg.dt
     v["eps_pw"] = v["eps_pp"] = cfg.restitution
     v["mu_pw"], v["mu_pp"] = cfg.mu_pw, cfg.mu_pp
     v["t_coll"], v["Lflume"], v["tilt_deg"] = cfg.t_coll, cfg.Lflume, cfg.tilt_deg
-    v["ntags"], v["print_flag"] = 9, 0
+    v["ntags"], v["print_flag"] = cfg.ntags, 0
     return v
 
 
@@ -95,10 +98,13 @@ def flume_state(cfg: FlumeConfig):
     packed pile the hopper-fill phase ends with, every resting contact carrying load.  Once the
     door is open the pile falls freely, so its contacts relax within a few tens of steps.
     layout "bed": the same packing built on the flume bed instead, in the slope frame (floor
-    z' = 0, side walls y = dy2 and dy2 + width, 1 cm clear of the funnel exit and the flume end)
-    and turned rigidly into the lab frame: a dense layer that gravity keeps pressed on the bed
-    while it slides, the state of an avalanche in full flow.
-    With v0 > 0 the velocities follow the reference's set_initial_velocity (seed 26752658)."""
+    z' = 0, side walls y = dy2 and dy2 + width, 1 cm clear of the funnel exit and of the flume
+    end, see bed_pile) and turned rigidly into the lab frame: a dense layer that gravity keeps
+    pressed on the bed while it slides, the state of an avalanche in full flow.
+    With v0 > 0 the velocities follow the reference's set_initial_velocity (seed 26752658).
+    layout "funnel": see funnel_state."""
+    if cfg.layout == "funnel":
+        return funnel_state(cfg)
     sys, fun = flume_system_of(cfg)
     pp = np.zeros(cfg.n, dtype=PARTICLE)
     pp["radius"] = cfg.radius
@@ -111,9 +117,8 @@ def flume_state(cfg: FlumeConfig):
                               2.0e-5 if cfg.overlap is None else cfg.overlap, rng)
     elif cfg.layout == "bed":
         dy2 = float(sys["dy2"])
-        placed = lattice_pile(pp, (LFUNNEL + 1.0, dy2, 0.0), (LFUNNEL + cfg.Lflume - 1.0, dy2 + cfg.width, 1e9),
-                              cfg.pitch, 0.0 if cfg.overlap is None else cfg.overlap, rng)
-        slope_to_lab(pp, sys)
+        placed = bed_pile(pp, sys, (LFUNNEL + 1.0, dy2, 0.0), (LFUNNEL + cfg.Lflume - 1.0, dy2 + cfg.width, 1e9),
+                          cfg.pitch, 0.0 if cfg.overlap is None else cfg.overlap, rng)
     else:
         placed = lattice_block(pp, (0.0, YHOP_L, HOP_HEIGHT), (HOP_WIDTH, YHOP_R, top), cfg.pitch, rng)
     if placed != cfg.n:
@@ -123,6 +128,103 @@ def flume_state(cfg: FlumeConfig):
     slope_frame(pp, sys)
     sys["tot_mass"] = float(pp["mass"].sum())
     return sys, fun, pp
+
+
+def size_factors(cfg: FlumeConfig, rng: Rannew64) -> np.ndarray:
+    """Per-clump size factors 1 + spread (2u - 1), u from rannew64 in clump order (all ones when
+    the configuration is monodisperse)."""
+    if cfg.size_spread <= 0.0:
+        return np.ones(cfg.n)
+    return np.array([1.0 + cfg.size_spread * (2.0 * rng() - 1.0) for _ in range(cfg.n)])
+
+
+def funnel_state(cfg: FlumeConfig):
+    """(system_par, Funnel, particle array) of a hopper discharging through the funnel onto the
+    flume, at the moment the door opens (time 0, avalanche phase, side.x = xfinal): every
+    boundary routine of the reference has clumps to act on.
+
+    Each clump is scaled by its own factor (sphere radius and tetrahedron edge together, mass and
+    inertia from calculate_particle_parameters' formulas), drawn from rannew64 before the
+    orientations.  The clumps are built as lattice piles (`lattice_pile`, each clump lowered
+    onto the floor or the clumps already placed, random orientations kept inside the box walls):
+      * the first half in the hopper box x in [0, 15], y in [7.5, 22.5] on the door plane z = 25
+        (lab frame): the pile the filling phase ends with, falling once the door is open and
+        loading the hopper's side walls;
+      * the second half on the bed in the slope frame: the funnel section x' in [1, 69] cut into
+        strips 4 cm long, each strip's box spanning y between the converging funnel walls at its
+        narrow end, and the flume x' in [71, 70 + L - 1] between its side walls (see bed_pile);
+        the flume section gets at most 10 clumps per lattice column, the funnel strips the rest
+        in proportion to their areas, then the layer is turned rigidly into the lab frame.  The layer touches the funnel walls, the funnel
+        corners, the flume side walls and the bed.
+    A strip's clumps keep every sphere inside the strip's box, so clumps of neighbouring strips
+    do not overlap; the hopper pile lies upslope of the bed (x' <= 0.5)."""
+    sys, fun = flume_system_of(cfg)
+    pp = np.zeros(cfg.n, dtype=PARTICLE)
+    rng = Rannew64(cfg.seed)
+    pp["radius"] = cfg.radius * size_factors(cfg, rng)
+    pp["density"] = cfg.density
+    calculate_particle_parameters(pp)
+    overlap = 0.0 if cfg.overlap is None else cfg.overlap
+    n_hop = cfg.n // 2
+    top = HOP_HEIGHT + float(sys["side"][2])
+    hop = pp[:n_hop].copy()
+    placed = lattice_pile(hop, (0.0, YHOP_L, HOP_HEIGHT), (HOP_WIDTH, YHOP_R, top), cfg.pitch, overlap, rng)
+    if placed != n_hop:
+        raise ValueError("the hopper holds %d of %d clumps below its top" % (placed, n_hop))
+    pp[:n_hop] = hop
+    dy2 = float(sys["dy2"])
+    tanfi = dy2 / LFUNNEL
+    boxes = []
+    x0 = 1.0
+    while x0 < LFUNNEL - 1.0 - 1e-9:
+        x1 = min(x0 + 4.0, LFUNNEL - 1.0)
+        boxes.append(((x0, x1 * tanfi, 0.0), (x1, 30.0 - x1 * tanfi, 1e9)))
+        x0 = x1
+    boxes.append(((LFUNNEL + 1.0, dy2, 0.0), (LFUNNEL + cfg.Lflume - 1.0, dy2 + cfg.width, 1e9)))
+    cols = np.array([np.floor((hi[0] - lo[0]) / cfg.pitch) * np.floor((hi[1] - lo[1]) / cfg.pitch)
+                     for lo, hi in boxes])
+    n_bed = cfg.n - n_hop
+    # the flume section holds at most 10 clumps per column (a layer a few cm deep; deeper, its
+    # top would reach past the flume end), the funnel strips the rest in proportion to their areas
+    flume_share = min(int(10 * cols[-1]), int(n_bed * cols[-1] / cols.sum()))
+    share = np.floor((n_bed - flume_share) * cols / cols[:-1].sum()).astype(np.int64)
+    share[-1] = flume_share
+    share[np.argmax(cols[:-1])] += n_bed - int(share.sum())
+    start = n_hop
+    for (lo, hi), m in zip(boxes, share):
+        part = pp[start:start + m].copy()
+        if bed_pile(part, sys, lo, hi, cfg.pitch, overlap, rng) != m:
+            raise ValueError("a bed strip holds fewer clumps than its share")
+        pp[start:start + m] = part
+        start += m
+    slope_frame(pp, sys)
+    sys["tot_mass"] = float(pp["mass"].sum())
+    return sys, fun, pp
+
+
+def bed_pile(pp: np.ndarray, sys: np.ndarray, lo, hi, pitch: float, overlap: float, rng: Rannew64,
+             margin: float = 1.0) -> int:
+    """lattice_pile on the bed in the slope frame (box lo..hi in slope-frame coordinates), turned
+    into the lab frame.  The box's downslope end is pulled back, and the pile built again from the
+    same generator state, until every clump centre lies `margin` upslope of the flume end x =
+    side.x in the lab frame: the top of a deep layer reaches farther downslope in the lab frame
+    than its foot, and a clump past side.x is removed at the first step (init_Verlet.cu:29-33).
+    Returns the clumps placed."""
+    c, s = float(sys["cost"]), float(sys["sint"])
+    limit = float(sys["side"][0]) - margin
+    x_hi = float(hi[0])
+    for _ in range(16):
+        part = pp.copy()
+        g = rng.clone()
+        placed = lattice_pile(part, lo, (x_hi, hi[1], hi[2]), pitch, overlap, g)
+        over = float(np.max(part["rr"][:placed, 0] * c + part["rr"][:placed, 2] * s)) - limit if placed else 0.0
+        if over <= 0.0 or placed < len(pp):
+            pp[:] = part
+            rng.assign(g)
+            slope_to_lab(pp, sys)
+            return placed
+        x_hi -= over / c + pitch
+    raise ValueError("the bed layer does not fit upslope of the flume end")
 
 
 def slope_to_lab(pp: np.ndarray, sys: np.ndarray) -> None:
@@ -161,6 +263,17 @@ def flume_2k(**kw) -> FlumeConfig:
 
 def flume_262k(**kw) -> FlumeConfig:
     kw = {"n": 262144, "tilt_deg": 35.0, "width": 20.0, "Lflume": 200.0, **kw}
+    return FlumeConfig(**kw)
+
+
+# FUNNEL_524K: 524,288 polydisperse clumps (size factor U[0.8, 1.2]) in the reference's hopper,
+# funnel and 40 cm x 4 cm flume at 30 deg (the 2,048-clump geometry), half in the hopper and half
+# on the funnel and flume bed (funnel_state); the lattice pitch 4.5 mm; hopper 100 cm high.  The
+# densest cells of this packing hold 8 of the smaller clumps, the most 9 slots allow, so the
+# cells get 16 slots.
+def funnel_524k(**kw) -> FlumeConfig:
+    kw = {"n": 524288, "tilt_deg": 30.0, "width": 4.0, "Lflume": 40.0, "size_spread": 0.2, "pitch": 0.45,
+          "hopper_height": 100.0, "layout": "funnel", "seed": 3145739, "ntags": 16, **kw}
     return FlumeConfig(**kw)
 
 

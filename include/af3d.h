@@ -19,6 +19,7 @@
 
 #include <stddef.h>
 #include <stdint.h>
+#include <stdio.h>
 
 #ifdef __cplusplus
 extern "C" {
@@ -274,6 +275,11 @@ af3d_status af3d_contact_pairs_noalloc (af3d_ctx *ctx, long *out, long cap, long
 /* Active sphere-sphere contacts summed over the fused force passes (af3d_step, af3d_forces)
    since the previous call; the counter restarts at zero. */
 af3d_status af3d_contact_count (af3d_ctx *ctx, long *count);
+/* Clumps whose contact item lists overflowed (more than 32 items, 32 partners passing the
+   centre test or 48 candidates), summed over the fused force passes since the previous call;
+   the counter restarts at zero.  Such a clump's contacts run by the per-clump cell walk, in
+   the same summation order (force_part.cu:88-106's walk, one pass per sph_id). */
+af3d_status af3d_list_overflows (af3d_ctx *ctx, long *count);
 
 /* Lossless binary checkpoint of a context (no counterpart in the reference, whose
    last_config.dat is %lf text): parameters of every flume, clock, step counter, phase, friction
@@ -284,7 +290,11 @@ af3d_status af3d_save_checkpoint (af3d_ctx *ctx, const char *path);
 af3d_status af3d_load_checkpoint (af3d_ctx *ctx, const char *path);
 
 /* ---- host I/O (no GPU) ----------------------------------------------------------------- */
-/* Parse DataInput.dat: first token of each of the 16 lines (avalanche_hst.cu:34-81). */
+/* Parse DataInput.dat from an open stream: the first token of each of the next 16 lines, in
+   avalanche_hst.cu:34-81's order (the reference reads them from stdin).  The stream is left
+   open. */
+af3d_status af3d_read_datainput (FILE *fp, af3d_inputs *in);
+/* The same from a file path. */
 af3d_status af3d_load_datainput (const char *path, af3d_inputs *in);
 /* Derived parameters of avalanche_hst.cu:84-102 and :187-195 (time = -1, side.x = HOP_WIDTH). */
 af3d_status af3d_derive_system (const af3d_inputs *in, af3d_system_par *sys, af3d_funnel *fun);

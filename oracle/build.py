@@ -33,7 +33,11 @@ import sys
 from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REFERENCE_DIR = os.environ.get("AF3D_REFERENCE_DIR", "/root/reference")
+# The reference checkout: AF3D_REFERENCE_DIR, else a directory named "reference" beside this
+# repository's root.  Where neither holds the reference's sources, oracle/_ref is not built and
+# the tests that need it are skipped.
+REFERENCE_DIR = os.environ.get("AF3D_REFERENCE_DIR") or os.path.join(
+    os.path.dirname(os.path.dirname(HERE)), "reference")
 ORACLE_SO = os.path.join(HERE, "liboracle_af3d.so")
 TANGENT_SO = os.path.join(HERE, "liboracle_tangent.so")
 REF_DIR = os.path.join(HERE, "_ref")
