@@ -52,6 +52,7 @@ ERRORS = {1: "ARG", 2: "CUDA", 3: "NOMEM", 4: "GRID_ESCAPE", 5: "NEGATIVE_CELL",
 FRICTION_HST, FRICTION_DEV = 0, 1
 PHASE_FILL, PHASE_AVALANCHE = 0, 1
 FP_EXACT, FP_FAST = 0, 1
+OBJ_CENTROID, OBJ_RUNOUT = 0, 1
 
 # (name, argtypes, restype) of every exported entry point of include/af3d.h.
 _P = C.c_void_p
@@ -102,6 +103,7 @@ SIGNATURES = [
     ("af3d_step", [_P, C.c_long], C.c_int),
     ("af3d_get_status", [_P, _P], C.c_int),
     ("af3d_adjoint", [_P, C.c_long, C.c_long, _P, _P, _P, _P, _P, _P], C.c_int),
+    ("af3d_set_objective", [_P, C.c_int, C.c_double], C.c_int),
     ("af3d_step_profile", [_P, C.c_long, _P], C.c_int),
     ("af3d_kernel_launches", [_P, _P], C.c_int),
     ("af3d_fp64_peak", [_P], C.c_int),

@@ -48,23 +48,52 @@ def rotation_gradient(R: np.ndarray, R_b: np.ndarray) -> np.ndarray:
     return np.stack([gx, gy, gz], axis=1)
 
 
+def downslope(pp: np.ndarray, sys) -> np.ndarray:
+    """x_rot = x cos(tilt) - z sin(tilt) of every clump centre (rotate_vectors.cu:28)."""
+    return pp["rr"][:, 0] * float(sys["cost"]) - pp["rr"][:, 2] * float(sys["sint"])
+
+
+def runout(pp: np.ndarray, sys, length: float) -> float:
+    """The runout objective of af3d_set_objective on a host state: length * ln(sum m exp(x /
+    length) / sum m) over the downslope positions x, evaluated about the largest x."""
+    x = downslope(pp, sys)
+    m = pp["mass"]
+    xmax = float(np.max(x))
+    return xmax + length * math.log(float(np.sum(m * np.exp((x - xmax) / length))) / float(np.sum(m)))
+
+
 def flume_run_function():
-    """A torch.autograd.Function: J = FlumeRun.apply(positions, engine_factory, steps, ckpt) with
-    J's gradient with respect to the initial clump positions from the engine's adjoint."""
+    """A torch.autograd.Function over the engine's adjoint:
+
+        J = FlumeRun.apply(r0, make_engine, steps, ckpt_every, runout)
+
+    r0 is an (n, 3) tensor of initial clump positions; make_engine(r0 as a numpy array) returns
+    an Engine with the state imported (the sphere centres placed at r0); runout is None for the
+    deposit centroid or the runout length scale.  J is a scalar for a single flume, or a tensor
+    of one J per flume for an ensemble.  Its gradient with respect to r0 comes from
+    af3d_adjoint (the sphere centres follow r0): for an ensemble each clump's gradient is
+    scaled by the incoming gradient of its own flume's J."""
     import torch
 
     class FlumeRun(torch.autograd.Function):
         @staticmethod
-        def forward(ctx, r0, make_engine, steps, ckpt_every):
+        def forward(ctx, r0, make_engine, steps, ckpt_every, runout_length=None):
             eng = make_engine(r0.detach().cpu().numpy())
-            out = eng.adjoint(int(steps), int(ckpt_every), gradients=True)
-            eng.close()
-            ctx.save_for_backward(torch.as_tensor(out["r0"], dtype=r0.dtype, device=r0.device))
-            return torch.tensor(out["J"], dtype=r0.dtype, device=r0.device)
+            try:
+                out = eng.adjoint(int(steps), int(ckpt_every), gradients=True, runout=runout_length)
+                flume_of = np.repeat(np.arange(eng.nflumes), eng.flume_sizes)
+                ensemble = eng.ensemble
+            finally:
+                eng.close()
+            ctx.save_for_backward(torch.as_tensor(out["r0"], dtype=r0.dtype, device=r0.device),
+                                  torch.as_tensor(flume_of, device=r0.device))
+            ctx.ensemble = ensemble
+            return torch.as_tensor(np.asarray(out["J"], dtype=np.float64), dtype=r0.dtype, device=r0.device)
 
         @staticmethod
         def backward(ctx, gJ):
-            (g,) = ctx.saved_tensors
-            return gJ * g, None, None, None
+            g, flume_of = ctx.saved_tensors
+            scale = gJ[flume_of] if ctx.ensemble else gJ
+            return g * (scale[:, None] if ctx.ensemble else scale), None, None, None, None
 
     return FlumeRun

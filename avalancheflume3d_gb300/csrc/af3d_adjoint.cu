@@ -795,36 +795,80 @@ __global__ void __launch_bounds__(kAdjListBlock, AF3D_ADJ_LMINB) k_adj_forces_l(
   add_params(param_b, f, par);
 }
 
-// Objective sums per flume: sums[2 f] = sum of m x_rot, sums[2 f + 1] = sum of m.
-__global__ void k_adj_objective(Planes P, DevScalars *d, const int *__restrict__ flume, double *sums, long n) {
+// The objectives, per flume f, over its clumps' final downslope positions x = x_rot
+// (rotate_vectors.cu:28) with masses m:
+//   deposit centroid (length <= 0):  J = sum m x / sum m
+//   runout (length l > 0):           J = l ln(sum m exp(x / l) / sum m), the mass-weighted
+//                                    soft maximum of x: the front of the deposit as l -> 0, the
+//                                    centroid as l -> infinity; evaluated as
+//                                    x_max + l ln(sum m exp((x - x_max) / l) / sum m)
+// Three sums per flume: sums[3 f] = sum m x (centroid) or sum m exp((x - x_max) / l) (runout),
+// sums[3 f + 1] = sum m, sums[3 f + 2] = x_max as an order-preserving integer (runout only;
+// zero, below every key, before the first pass).
+__device__ __forceinline__ unsigned long long order_key(double x) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double from_order_key(unsigned long long k) {
+  const unsigned long long u = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+  return __longlong_as_double((long long)u);
+}
+
+__device__ __forceinline__ double final_xrot(const Planes &P, const af3d_system_par &sy, long s) {
+  return P.p[RX][s] * sy.cost - P.p[RZ][s] * sy.sint;
+}
+
+// Runout, first pass: x_max per flume.
+__global__ void k_adj_xmax(Planes P, DevScalars *d, const int *__restrict__ flume, double *sums, long n) {
+  const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const int f = flume[s];
+  atomicMax(reinterpret_cast<unsigned long long *>(sums + 3 * f + 2), order_key(final_xrot(P, d->flumes[f].sys, s)));
+}
+
+__global__ void k_adj_objective(Planes P, DevScalars *d, const int *__restrict__ flume, double *sums, double length,
+                                long n) {
   const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
   const long sv = s < n ? s : n - 1;
   const int f = flume[sv];
   double mx = 0.0, m = 0.0;
   if (s < n) {
-    const af3d_system_par &sy = d->flumes[f].sys;
+    const double x = final_xrot(P, d->flumes[f].sys, s);
     m = P.p[MASS][s];
-    mx = m * (P.p[RX][s] * sy.cost - P.p[RZ][s] * sy.sint);
+    if (length > 0.0) {
+      const double xmax = from_order_key(reinterpret_cast<const unsigned long long *>(sums)[3 * f + 2]);
+      mx = m * exp((x - xmax) / length);
+    } else {
+      mx = m * x;
+    }
   }
   const int f0 = __shfl_sync(0xffffffffu, f, 0);
   if (__all_sync(0xffffffffu, f == f0)) {
-    warp_reduce_add(sums + 2 * f0, mx);
-    warp_reduce_add(sums + 2 * f0 + 1, m);
+    warp_reduce_add(sums + 3 * f0, mx);
+    warp_reduce_add(sums + 3 * f0 + 1, m);
   } else if (s < n) {
-    atomicAdd(sums + 2 * f, mx);
-    atomicAdd(sums + 2 * f + 1, m);
+    atomicAdd(sums + 3 * f, mx);
+    atomicAdd(sums + 3 * f + 1, m);
   }
 }
 
-// Seed: the adjoint of the final state for the sum over flumes of J_f = sum_m x_rot / sum_m
-// (the flumes are independent, so each flume's gradients are those of its own J_f).
+// Seed: the adjoint of the final state for the sum over flumes of J_f (the flumes are
+// independent, so each flume's gradients are those of its own J_f): dJ/dx = m / sum m
+// (centroid) or m exp((x - x_max) / l) / sum m exp((x - x_max) / l) (runout), and
+// dx/dr = (cos, 0, -sin).
 __global__ void k_adj_seed(Planes P, Planes adj, DevScalars *d, const int *__restrict__ flume, const double *sums,
-                           long n) {
+                           double length, long n) {
   const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (s >= n) return;
   const int f = flume[s];
   const af3d_system_par &sy = d->flumes[f].sys;
-  const double w = P.p[MASS][s] / sums[2 * f + 1];
+  double w;
+  if (length > 0.0) {
+    const double xmax = from_order_key(reinterpret_cast<const unsigned long long *>(sums)[3 * f + 2]);
+    w = P.p[MASS][s] * exp((final_xrot(P, sy, s) - xmax) / length) / sums[3 * f];
+  } else {
+    w = P.p[MASS][s] / sums[3 * f + 1];
+  }
   for (int k = 0; k < NADJ; k++) adj.p[k][s] = 0.0;
   st3(adj, AR, s, mk(w * sy.cost, 0.0, -w * sy.sint));
 }
@@ -874,14 +918,16 @@ void launch_adj_forces_lists(const Launch &L, Planes P, Planes in, Planes out, P
                                                  param_b, L.n);
 }
 
-void launch_adj_objective(const Launch &L, Planes P, DevScalars *d, const int *flume, double *sums) {
+void launch_adj_objective(const Launch &L, Planes P, DevScalars *d, const int *flume, double *sums, double length) {
   if (L.n <= 0) return;
-  k_adj_objective<<<blocks(L.n), kAdjBlock, 0, L.st>>>(P, d, flume, sums, L.n);
+  if (length > 0.0) k_adj_xmax<<<blocks(L.n), kAdjBlock, 0, L.st>>>(P, d, flume, sums, L.n);
+  k_adj_objective<<<blocks(L.n), kAdjBlock, 0, L.st>>>(P, d, flume, sums, length, L.n);
 }
 
-void launch_adj_seed(const Launch &L, Planes P, Planes adj, DevScalars *d, const int *flume, const double *sums) {
+void launch_adj_seed(const Launch &L, Planes P, Planes adj, DevScalars *d, const int *flume, const double *sums,
+                     double length) {
   if (L.n <= 0) return;
-  k_adj_seed<<<blocks(L.n), kAdjBlock, 0, L.st>>>(P, adj, d, flume, sums, L.n);
+  k_adj_seed<<<blocks(L.n), kAdjBlock, 0, L.st>>>(P, adj, d, flume, sums, length, L.n);
 }
 
 void launch_state_copy(const Launch &L, Planes P, Planes tape, bool to_tape, bool spheres) {

@@ -9,6 +9,7 @@
 // Device-side checks raise bits in a status word that af3d_step() and af3d_get_status() read
 // back; nothing calls exit().
 #include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <cstddef>
 #include <cstdio>
@@ -94,6 +95,7 @@ struct af3d_ctx {
   int phase = AF3D_PHASE_AVALANCHE;
   int variant = AF3D_FRICTION_HST;
   int fp_mode = AF3D_FP_EXACT;
+  double obj_length = 0.0;   // objective of af3d_adjoint: 0 deposit centroid, > 0 runout length scale
   long cc = 0;                        // steps done in the current phase
   bool imported = false;
 
@@ -645,6 +647,19 @@ af3d_status af3d_set_friction(af3d_ctx *c, int variant) {
     return fail(AF3D_ERR_ARG, "unknown friction variant");
   c->variant = variant;
   return push_params(c);
+}
+
+af3d_status af3d_set_objective(af3d_ctx *c, int objective, double length) {
+  CHECK_CTX(c);
+  if (objective == AF3D_OBJ_CENTROID) {
+    c->obj_length = 0.0;
+  } else if (objective == AF3D_OBJ_RUNOUT) {
+    if (!(length > 0.0) || !std::isfinite(length)) return fail(AF3D_ERR_ARG, "the runout length scale must be > 0");
+    c->obj_length = length;
+  } else {
+    return fail(AF3D_ERR_ARG, "unknown objective");
+  }
+  return AF3D_OK;
 }
 
 af3d_status af3d_set_fp_mode(af3d_ctx *c, int mode) {
@@ -1620,14 +1635,14 @@ extern "C" af3d_status af3d_adjoint(af3d_ctx *c, long steps, long ckpt_every, do
       }
     }
   }
-  // per flume f: dsc[2 f], dsc[2 f + 1] the objective sums, pgr[6 f .. 6 f + 5] the parameter
+  // per flume f: dsc[3 f .. 3 f + 2] the objective sums, pgr[6 f .. 6 f + 5] the parameter
   // adjoints; then per step: its list overflow flag (int), its start and end times (a pair)
-  const size_t nsc = (size_t)8 * nf;
+  const size_t nsc = (size_t)9 * nf;
   double *dsc = nullptr;
   if (e == cudaSuccess) e = cudaMalloc((void **)&dsc, sizeof(double) * (nsc + 3 * (size_t)(steps + 1)));
   if (e == cudaSuccess) buf.owned.push_back(dsc);
   if (e != cudaSuccess) return fail(AF3D_ERR_NOMEM, std::string("adjoint buffers: ") + cudaGetErrorString(e));
-  double *pgr = dsc + 2 * nf;
+  double *pgr = dsc + 3 * nf;
   double *t_pair = dsc + nsc;   // [steps + 1][2]: {time, time_prev} during step k
   int *ovf = reinterpret_cast<int *>(t_pair + 2 * (size_t)(steps + 1));
   AF3D_CUDA(cudaMemsetAsync(dsc, 0, sizeof(double) * (nsc + 3 * (size_t)(steps + 1)), c->st));
@@ -1689,17 +1704,31 @@ extern "C" af3d_status af3d_adjoint(af3d_ctx *c, long steps, long ckpt_every, do
   t_start[steps] = t;
   c->time = t;
   launch_state_copy(c->L(), c->cur, fin, true, true);
-  launch_adj_objective(c->L(), c->cur, c->d, c->fl_cur, dsc);
-  std::vector<double> sums((size_t)2 * nf);
+  launch_adj_objective(c->L(), c->cur, c->d, c->fl_cur, dsc, c->obj_length);
+  std::vector<double> sums((size_t)3 * nf);
   std::vector<int> ovf_h(steps + 1, 0);
-  AF3D_CUDA(cudaMemcpyAsync(sums.data(), dsc, sizeof(double) * 2 * nf, cudaMemcpyDeviceToHost, c->st));
+  AF3D_CUDA(cudaMemcpyAsync(sums.data(), dsc, sizeof(double) * 3 * nf, cudaMemcpyDeviceToHost, c->st));
   AF3D_CUDA(cudaMemcpyAsync(ovf_h.data(), ovf, sizeof(int) * (steps + 1), cudaMemcpyDeviceToHost, c->st));
   int flags = 0;
   af3d_status s = read_status(c, &flags);
   if (s) return s;
   s = first_error(flags);
   if (s) return s;
-  for (int f = 0; f < nf; f++) J[f] = sums[2 * f + 1] > 0.0 ? sums[2 * f] / sums[2 * f + 1] : 0.0;
+  for (int f = 0; f < nf; f++) {
+    const double S = sums[3 * f], M = sums[3 * f + 1];
+    if (!(M > 0.0)) {
+      J[f] = 0.0;
+    } else if (c->obj_length > 0.0) {
+      uint64_t key;   // x_max as the device's order-preserving integer
+      std::memcpy(&key, &sums[3 * f + 2], sizeof key);
+      const uint64_t u = (key >> 63) ? (key & 0x7fffffffffffffffull) : ~key;
+      double xmax;
+      std::memcpy(&xmax, &u, sizeof xmax);
+      J[f] = xmax + c->obj_length * std::log(S / M);
+    } else {
+      J[f] = S / M;
+    }
+  }
 
   if (want_grad && n > 0) {
     // every step's times on the device (set by device-side copies, the host runs ahead): step k
@@ -1711,7 +1740,7 @@ extern "C" af3d_status af3d_adjoint(af3d_ctx *c, long steps, long ckpt_every, do
     }
     static_assert(offsetof(DevScalars, time_prev) == offsetof(DevScalars, time) + sizeof(double), "time pair");
     AF3D_CUDA(cudaMemcpyAsync(t_pair, tp.data(), sizeof(double) * tp.size(), cudaMemcpyHostToDevice, c->st));
-    launch_adj_seed(c->L(), c->cur, adjA, c->d, c->fl_cur, dsc);
+    launch_adj_seed(c->L(), c->cur, adjA, c->d, c->fl_cur, dsc, c->obj_length);
     Planes rnext_src = fin;   // R1 of each segment's last step: the next segment's starting R
     for (long seg = (steps - 1) / C; steps > 0 && seg >= 0; seg--) {
       const long k0 = seg * C, k1 = std::min(steps, k0 + C);

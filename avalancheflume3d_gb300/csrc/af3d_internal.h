@@ -256,8 +256,11 @@ void launch_adj_forces_lists (const Launch &L, Planes P, Planes in, Planes out, 
 void launch_adj_predict (const Launch &L, Planes P, Planes tape, Planes in, Planes out, Planes acc, Planes rb,
                          DevScalars *d, const int *flume);
 void launch_adj_startup (const Launch &L, Planes P, Planes in, Planes out, Planes acc, Planes rb);
-void launch_adj_objective (const Launch &L, Planes P, DevScalars *d, const int *flume, double *sums);
-void launch_adj_seed (const Launch &L, Planes P, Planes adj, DevScalars *d, const int *flume, const double *sums);
+// Objective sums (3 per flume, zeroed before) and the adjoint seed of the final state; length
+// > 0: the runout soft maximum with that length scale, else the deposit centroid.
+void launch_adj_objective (const Launch &L, Planes P, DevScalars *d, const int *flume, double *sums, double length);
+void launch_adj_seed (const Launch &L, Planes P, Planes adj, DevScalars *d, const int *flume, const double *sums,
+                      double length);
 // The 24 state planes (with spheres: 36, the sphere centres too) between the plane set and a
 // tape slot (to_tape: planes -> tape).
 void launch_state_copy (const Launch &L, Planes P, Planes tape, bool to_tape, bool spheres = false);

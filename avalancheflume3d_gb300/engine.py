@@ -21,7 +21,8 @@ import ctypes as C
 
 import numpy as np
 
-from ._lib import (CELL_PAR, FP_EXACT, FRICTION_HST, FUNNEL, INPUTS, PARTICLE, PHASE_AVALANCHE, RNG,
+from ._lib import (CELL_PAR, FP_EXACT, FRICTION_HST, FUNNEL, INPUTS, OBJ_CENTROID, OBJ_RUNOUT, PARTICLE,
+                   PHASE_AVALANCHE, RNG,
                    SYSTEM_PAR, EngineError, Vec3, check, lib, ptr)
 
 
@@ -237,13 +238,19 @@ class Engine:
         self._call("af3d_step", int(k))
 
     # ---- adjoint ----
-    def adjoint(self, steps: int, ckpt_every: int = 500, gradients: bool = True) -> dict:
-        """Start-up force pass + `steps` exact steps from the imported state, J = mass-weighted
-        mean downslope position at the end and (gradients=True) dJ/d(parameters, initial state)
-        from the hand-written adjoint (af3d_adjoint).  Leaves the context at the final state.
+    def adjoint(self, steps: int, ckpt_every: int = 500, gradients: bool = True, runout: float | None = None) -> dict:
+        """Start-up force pass + `steps` exact steps from the imported state, J at the end and
+        (gradients=True) dJ/d(parameters, initial state) from the hand-written adjoint
+        (af3d_adjoint).  J is the mass-weighted mean downslope position (the deposit centroid),
+        or with ``runout`` = l > 0 [cm] the runout l ln(sum m exp(x / l) / sum m), a soft maximum
+        of the downslope positions.  Leaves the context at the final state.
 
         For an ensemble, ``J`` is an array over flumes and every ``params`` entry an array of
         each flume's own derivative; the per-clump gradients are those of the clump's flume."""
+        if runout is None:
+            self._call("af3d_set_objective", OBJ_CENTROID, 0.0)
+        else:
+            self._call("af3d_set_objective", OBJ_RUNOUT, float(runout))
         names = ("kappa_pp", "gamma_pp", "mu_pp", "kappa_pw", "gamma_pw", "mu_pw")
         J = np.zeros(self.nflumes)
         out = {}

@@ -384,13 +384,13 @@ def measure_ensemble(args, stream):
             "geometry": "40 cm x 4 cm flume, reference hopper and funnel; per-flume slope 25-40 deg"}
 
 
-def _adjoint_cost(sys_, fun, pp, K, ckpt, stream):
+def _adjoint_cost(sys_, fun, pp, K, ckpt, stream, friction):
     """(forward seconds for K graph-replayed exact steps, adjoint seconds for af3d_adjoint over
     the same K steps from the same state, the adjoint's output)."""
     import torch
     from avalancheflume3d_gb300 import Engine, FP_EXACT
 
-    with Engine(sys_, fun, stream=stream.cuda_stream, fp_mode=FP_EXACT) as eng:
+    with Engine(sys_, fun, stream=stream.cuda_stream, fp_mode=FP_EXACT, friction=friction) as eng:
         eng.import_particles(pp)
         eng.forces()
         eng.swap_accel()
@@ -403,10 +403,10 @@ def _adjoint_cost(sys_, fun, pp, K, ckpt, stream):
         e1.record(stream)
         torch.cuda.synchronize()
         t_fwd = e0.elapsed_time(e1) / 1e3
-    with Engine(sys_, fun, stream=stream.cuda_stream) as eng:
+    with Engine(sys_, fun, stream=stream.cuda_stream, friction=friction) as eng:
         eng.import_particles(pp)
         eng.adjoint(min(K, 2 * ckpt), ckpt)   # warm-up
-    with Engine(sys_, fun, stream=stream.cuda_stream) as eng:
+    with Engine(sys_, fun, stream=stream.cuda_stream, friction=friction) as eng:
         eng.import_particles(pp)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -422,24 +422,37 @@ def measure_adjoint(args, stream):
     (graph replay).  Adjoint: af3d_adjoint over the same K steps from the same state (start-up
     pass, forward with checkpoints every C steps, segment recompute, reverse), timed end to end.
     Then the same as a calibration batch: the flume in S copies with sampled (mu_pp, mu_pw,
-    restitution) in one ensemble context, every copy's gradients from one backward sweep."""
+    restitution) in one ensemble context, every copy's gradients from one backward sweep.
+
+    Both run the device friction variant (force_part.cu:487), whose particle-particle contacts
+    take the Coulomb branch when sliding: in the host variant (force_part.cu:224) that branch
+    cannot fire for these sphere masses at dt = 2e-6 s, so dJ/dmu_pp is identically zero there.
+    The single run also reports the gradients of the runout objective (a soft maximum of the
+    downslope positions, length scale 1 cm) from a second adjoint call."""
+    from avalancheflume3d_gb300 import Engine, FRICTION_DEV
     from avalancheflume3d_gb300.adjoint import config_gradients
     from avalancheflume3d_gb300.workloads import adjoint_batch, flume_2k, flume_state
     cfg = flume_2k(n=32768, tilt_deg=35.0, Lflume=80.0, layout="bed")
     sys_, fun, pp = flume_state(cfg)
     K = args.adjoint_steps
-    t_fwd, t_adj, out = _adjoint_cost(sys_, fun, pp, K, args.adjoint_ckpt, stream)
+    t_fwd, t_adj, out = _adjoint_cost(sys_, fun, pp, K, args.adjoint_ckpt, stream, FRICTION_DEV)
+    with Engine(sys_, fun, stream=stream.cuda_stream, friction=FRICTION_DEV) as eng:
+        eng.import_particles(pp)
+        run_out = eng.adjoint(K, args.adjoint_ckpt, runout=1.0)
     res = {"workload": "flume 32,768 clumps, 80 cm x 4 cm at 35 deg, dense bed layer, exact FP64",
+           "friction": "device variant (force_part.cu:487); dJ/dmu_pp is identically 0 in the host variant",
            "steps": K, "ckpt_every": args.adjoint_ckpt, "ms_per_step_forward": 1e3 * t_fwd / K,
            "ms_per_step_adjoint": 1e3 * t_adj / K, "adjoint_over_forward": t_adj / t_fwd,
            "what": "adjoint = the whole af3d_adjoint call (forward with checkpoints, segment recompute, "
                    "reverse, gradient gather) per step, over a graph-replayed exact forward step",
            "J": out["J"], "dJ_dparams": out["params"],
-           "dJ_dconfig": config_gradients(cfg, out["params"])}
+           "dJ_dconfig": config_gradients(cfg, out["params"]),
+           "runout": {"objective": "1 cm ln(sum m exp(x_rot / 1 cm) / sum m)", "J": run_out["J"],
+                      "dJ_dparams": run_out["params"], "dJ_dconfig": config_gradients(cfg, run_out["params"])}}
     S, Kb = args.adjoint_batch, args.adjoint_batch_steps
     if S > 0 and Kb > 0:
         cfgs, bsys, bfun, bpp = adjoint_batch(cfg, S)
-        tb_fwd, tb_adj, bout = _adjoint_cost(bsys, bfun, bpp, Kb, args.adjoint_batch_ckpt, stream)
+        tb_fwd, tb_adj, bout = _adjoint_cost(bsys, bfun, bpp, Kb, args.adjoint_batch_ckpt, stream, FRICTION_DEV)
         g0 = config_gradients(cfgs[0], {k: float(v[0]) for k, v in bout["params"].items()})
         res["batch"] = {
             "samples": S, "clumps": int(len(bpp)), "steps": Kb, "ckpt_every": args.adjoint_batch_ckpt,

@@ -96,6 +96,8 @@ enum { AF3D_FP_EXACT = 0, AF3D_FP_FAST = 1 };
 
 /* Phase of the reference loop: hopper filling (avalanche_hst.cu:401-601) or avalanche (:618-856). */
 enum { AF3D_PHASE_FILL = 0, AF3D_PHASE_AVALANCHE = 1 };
+/* Objectives of af3d_adjoint (no counterpart in the reference; af3d_set_objective). */
+enum { AF3D_OBJ_CENTROID = 0, AF3D_OBJ_RUNOUT = 1 };
 
 typedef struct af3d_ctx af3d_ctx;
 
@@ -209,8 +211,9 @@ af3d_status af3d_fp64_peak (double *tflops);
 
 /* ---- adjoint (no counterpart in the reference) --------------------------------------------
    Runs, from the imported state (a_i = alpha_i = 0), the start-up force pass and `steps` exact
-   steps (fixed cell grid, no re-grid), and returns per flume f J[f] = the mass-weighted mean
-   downslope position sum m (x cos(tilt) - z sin(tilt)) / sum m of its clumps at the end.  With
+   steps (fixed cell grid, no re-grid), and returns per flume f the objective J[f] at the end:
+   by default the mass-weighted mean downslope position sum m (x cos(tilt) - z sin(tilt)) / sum m
+   of its clumps, or the runout (af3d_set_objective).  With
    any gradient pointer non-NULL it then runs the hand-written adjoint of those steps backwards
    from a tape of C steps (540 B per clump and step: each step's starting state, torque sums,
    clump records and contact item lists), C = min(steps, ckpt_every), halved until the tape and
@@ -230,6 +233,15 @@ af3d_status af3d_fp64_peak (double *tflops);
    left at the final state of the forward run. */
 af3d_status af3d_adjoint (af3d_ctx *ctx, long steps, long ckpt_every, double *J, double *param_grad,
                           af3d_vec3 *dr0, double *dR0, af3d_vec3 *dv0, af3d_vec3 *dw0);
+/* No counterpart in the reference.  The objective J[f] af3d_adjoint evaluates and
+   differentiates, over flume f's clumps' final downslope positions x = x_rot
+   (rotate_vectors.cu:28) with masses m:
+     AF3D_OBJ_CENTROID (default)  the deposit centroid, sum m x / sum m (length ignored)
+     AF3D_OBJ_RUNOUT              the runout, length * ln(sum m exp(x / length) / sum m): a
+                                  mass-weighted soft maximum of x, the front of the deposit as
+                                  length -> 0 (a smooth stand-in for the front's position, whose
+                                  exact maximum has no useful derivative); length > 0 [cm]. */
+af3d_status af3d_set_objective (af3d_ctx *ctx, int objective, double length);
 
 /* No counterpart in the reference.  Captures now, without running anything or changing the
    state, the CUDA graphs the next af3d_step(ctx, k) will replay (up to its first re-grid), so

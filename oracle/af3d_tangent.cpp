@@ -153,6 +153,12 @@ void drop(unsigned char *out, const S &in, int nlong, int nreal) {
 
 extern "C" __attribute__((visibility("default"))) int tlm_directions(void) { return kDirs; }
 
+/* Host threads of the per-clump loops (the oracle's own OpenMP loops over clumps, each
+   writing only its own clump's entries, so the result does not depend on the count). */
+extern "C" __attribute__((visibility("default"))) void tlm_set_threads(int nthreads) {
+  orc_set_threads(nthreads);
+}
+
 /* The start-up force pass (orc_forces, then a_i = a_f) and `steps` orc_step calls of the phase
    and friction variant, from the state (sys, fun, cell, pp[n]) in the reference's layouts, with
    accelerations zero at the start.  ndir <= tlm_directions() directions: dsys[k] (a system_par,

@@ -91,7 +91,7 @@ def build_tangent(force: bool = False) -> str:
     if force or not _newer(TANGENT_SO, deps):
         tmp = TANGENT_SO + ".tmp%d" % os.getpid()
         _run(["g++", "-O2", "-fPIC", "-shared", "-std=c++17", "-ffp-contract=off", "-fvisibility=hidden",
-              "-o", tmp, src, "-lm"])
+              "-fopenmp", "-o", tmp, src, "-lm"])
         os.replace(tmp, TANGENT_SO)
     return TANGENT_SO
 

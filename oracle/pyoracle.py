@@ -484,6 +484,10 @@ class Tangent:
         self.lib.tlm_run.argtypes = [C.c_void_p] * 4 + [C.c_long, C.c_int, C.c_void_p, C.c_void_p, C.c_long,
                                                         C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
         self.ndirs = int(self.lib.tlm_directions())
+        self.lib.tlm_set_threads.argtypes = [C.c_int]
+
+    def set_threads(self, n: int) -> None:
+        self.lib.tlm_set_threads(int(n))
 
     def run(self, sys, fun, cp, pp, steps, phase=PHASE_AVALANCHE, variant=FRICTION_HST, dsys=None, dpp=None):
         """Start-up force pass + `steps` steps; returns (J, dJ[ndir], final state).  dsys: array

@@ -50,24 +50,57 @@ def _xrot(pp, sys):
     return pp["rr"][:, 0] * float(sys["cost"]) - pp["rr"][:, 2] * float(sys["sint"])
 
 
-def _J(af3d, sys, fun, pp, ref, steps=STEPS, phase=1):
-    """J - J(ref positions) from the exported final state (host, fixed order)."""
-    with af3d.Engine(sys, fun, phase=phase) as eng:
+def _final(af3d, sys, fun, pp, steps=STEPS, phase=1, friction=0):
+    """The exported final state of the forward run the adjoint differentiates."""
+    with af3d.Engine(sys, fun, phase=phase, friction=friction) as eng:
         eng.import_particles(pp)
         eng.adjoint(steps, gradients=False)
-        p = eng.export_particles(with_accel=False)
+        return eng.export_particles(with_accel=False)
+
+
+def _J(af3d, sys, fun, pp, ref, steps=STEPS, phase=1, friction=0):
+    """J - J(ref positions) from the exported final state (host, fixed order)."""
+    p = _final(af3d, sys, fun, pp, steps, phase, friction)
     m = p["mass"]
     return float(np.sum(m * (_xrot(p, sys) - ref)) / np.sum(m))
 
 
-def _adjoint(af3d, sys, fun, pp, steps=STEPS, ckpt=40, phase=1):
-    with af3d.Engine(sys, fun, phase=phase) as eng:
+def _runout_difference(pa, pb, sys, length):
+    """J(pa) - J(pb) of the runout objective, l ln(sum m e^(x/l) / sum m), in a form free of
+    cancellation: l log1p(sum m e^((xb - c)/l) expm1((xa - xb)/l) / sum m e^((xb - c)/l))."""
+    xa, xb = _xrot(pa, sys), _xrot(pb, sys)
+    m = pb["mass"]
+    wb = m * np.exp((xb - float(np.max(xb))) / length)
+    return length * float(np.log1p(np.sum(wb * np.expm1((xa - xb) / length)) / np.sum(wb)))
+
+
+def _adjoint(af3d, sys, fun, pp, steps=STEPS, ckpt=40, phase=1, friction=0, runout=None):
+    with af3d.Engine(sys, fun, phase=phase, friction=friction) as eng:
         eng.import_particles(pp)
-        return eng.adjoint(steps, ckpt)
+        return eng.adjoint(steps, ckpt, runout=runout)
 
 
 def _close(adj, fd, scale):
     return abs(adj - fd) <= TOL * max(abs(fd), 1e-3 * scale)
+
+
+def _fd_agrees(Jat, h, adj, scale):
+    """Whether the adjoint derivative `adj` agrees with finite differences of J(delta) = Jat(delta)
+    at step h.  First the central difference, to the bar.  The forward run is only piecewise
+    smooth: a perturbation can move a discrete event (a contact starting or ending a step
+    earlier, a gate or the Coulomb branch switching) or change the rounding of a chaotic run,
+    and the adjoint is the derivative of the piece the unperturbed run is on.  Where J is that
+    rough at the scale h, its forward and backward differences disagree; the central
+    difference is then uncertain by half their spread, and the adjoint must lie within it.
+    (The tangent-linear tests check the same derivatives along the same pieces without finite
+    differences.)  Returns (agrees, central difference, "central" or "rough")."""
+    jp, jm = Jat(h), Jat(-h)
+    central = (jp - jm) / (2 * h)
+    if _close(adj, central, scale):
+        return True, central, "central"
+    j0 = Jat(0.0)
+    spread = 0.5 * abs((jp - j0) / h - (j0 - jm) / h)
+    return abs(adj - central) <= spread, central, "rough"
 
 
 def test_adjoint_zero_steps(af3d, base):
@@ -80,29 +113,43 @@ def test_adjoint_zero_steps(af3d, base):
     assert np.all(out["R0"] == 0.0)
 
 
+@pytest.mark.parametrize("friction", [0, 1])
 @pytest.mark.parametrize("phase_time", [0.0, -0.5])
-def test_adjoint_parameters_vs_finite_differences(af3d, base, phase_time):
+def test_adjoint_parameters_vs_finite_differences(af3d, base, phase_time, friction):
+    """Both friction variants.  In the host variant (force_part.cu:224) a particle-particle
+    contact whose tangential displacement survives the xi gate has |xi| <= mu N 1e-12, so its
+    shear force is at most m mu N (1 + 2e-6 / dt), below mu N for the sphere masses and time
+    step here: the Coulomb cap never fires, mu_pp enters only through the gate's decision, and
+    dJ/dmu_pp is exactly zero.  The device variant (force_part.cu:487) also takes the Coulomb
+    branch when the gate zeroed xi, so sliding contacts carry mu_pp and its gradient."""
     from oracle.pyoracle import PHASE_AVALANCHE, PHASE_FILL
     _, sys0, fun, pp = base
     sys = sys0.copy()
     sys["time"] = phase_time
     phase = PHASE_FILL if phase_time < 0 else PHASE_AVALANCHE
     ref = _xrot(pp, sys)
-    out = _adjoint(af3d, sys, fun, pp, phase=phase)
+    out = _adjoint(af3d, sys, fun, pp, phase=phase, friction=friction)
     grads = out["params"]
     scale = max(abs(v * float(sys[k])) for k, v in grads.items())   # |dJ/dlog theta|
     rows, bad = [], []
     for k, g in grads.items():
-        h = REL * float(sys[k])
-        sp, sm = sys.copy(), sys.copy()
-        sp[k] += h
-        sm[k] -= h
-        fd = (_J(af3d, sp, fun, pp, ref, phase=phase) - _J(af3d, sm, fun, pp, ref, phase=phase)) / (2 * h)
-        rows.append((k, g * float(sys[k]), fd * float(sys[k])))
-        if not _close(g * float(sys[k]), fd * float(sys[k]), scale):
+        theta = float(sys[k])
+
+        def Jat(delta, k=k, theta=theta):   # J at theta (1 + delta), in units of log theta
+            sd = sys.copy()
+            sd[k] = theta + delta * theta
+            return _J(af3d, sd, fun, pp, ref, phase=phase, friction=friction)
+        ok, fd, which = _fd_agrees(Jat, REL, g * theta, scale)
+        rows.append((k, g * theta, fd, which))
+        if not ok:
             bad.append(k)
     assert not bad, rows
     assert sum(abs(r[2]) > 1e-3 * scale for r in rows) >= 4, rows   # the run exercises both laws
+    assert sum(r[3] != "central" for r in rows) <= 1, rows        # a rough parameter is the exception
+    if friction == 0:
+        assert grads["mu_pp"] == 0.0, rows
+    else:
+        assert abs(grads["mu_pp"] * float(sys["mu_pp"])) > 1e-3 * scale, rows
 
 
 def test_adjoint_positions_vs_finite_differences(af3d, base):
@@ -164,13 +211,20 @@ def test_adjoint_orientations_vs_finite_differences(af3d, base):
     assert not bad, rows
 
 
-def test_adjoint_vs_tangent_linear_model(af3d, base, oracle, tangent):
+@pytest.mark.parametrize("friction", [0, 1])
+@pytest.mark.parametrize("phase_time", [0.0, -0.5])
+def test_adjoint_vs_tangent_linear_model(af3d, base, oracle, tangent, friction, phase_time):
     """The adjoint against the FP64 CPU tangent-linear model (the oracle over dual numbers) on
     the same run: eight directional derivatives -- each contact-law parameter, a random
-    perturbation of positions and orientations, and one of velocities and spins -- to 1e-7."""
-    from oracle.pyoracle import CELL_PAR, PARTICLE, SYSTEM_PAR, state_tangent
-    _, sys, fun, pp = base
-    out = _adjoint(af3d, sys, fun, pp)
+    perturbation of positions and orientations, and one of velocities and spins -- to 1e-7, in
+    both phases and both friction variants (the device variant differentiates the
+    particle-particle Coulomb branch, force_part.cu:487)."""
+    from oracle.pyoracle import CELL_PAR, PARTICLE, PHASE_AVALANCHE, PHASE_FILL, SYSTEM_PAR, state_tangent
+    _, sys0, fun, pp = base
+    sys = sys0.copy()
+    sys["time"] = phase_time
+    phase = PHASE_FILL if phase_time < 0 else PHASE_AVALANCHE
+    out = _adjoint(af3d, sys, fun, pp, friction=friction, phase=phase)
     rng = np.random.default_rng(17)
     names = list(out["params"])
     dsys = np.zeros(tangent.ndirs, dtype=SYSTEM_PAR)
@@ -188,7 +242,7 @@ def test_adjoint_vs_tangent_linear_model(af3d, base, oracle, tangent):
     s8 = sys.copy()
     s8["rmax"] *= 8.0
     oracle.grid_from_bbox(cp, s8)
-    J, dJ, _ = tangent.run(sys, fun, cp, pp, STEPS, dsys=dsys, dpp=dpp)
+    J, dJ, _ = tangent.run(sys, fun, cp, pp, STEPS, phase=phase, variant=friction, dsys=dsys, dpp=dpp)
     dR = np.stack([dpp[6]["Rmatx"], dpp[6]["Rmaty"], dpp[6]["Rmatz"]], 1)
     adj =[out["params"][k] * float(sys[k]) for k in names]
     adj.append(float(np.sum(out["r0"] * dr) + np.sum(out["R0"] * dR)))
@@ -198,6 +252,8 @@ def test_adjoint_vs_tangent_linear_model(af3d, base, oracle, tangent):
     scale = float(np.abs(dJ).max())
     bad = [(k, adj[k], dJ[k]) for k in range(8) if abs(adj[k] - dJ[k]) > 1e-7 * max(abs(dJ[k]), 1e-3 * scale)]
     assert not bad, list(zip(adj, dJ))
+    if friction == 1:
+        assert abs(dJ[names.index("mu_pp")]) > 1e-3 * scale, list(zip(names, adj, dJ))
 
 
 def test_adjoint_configuration_chain_vs_finite_differences(af3d, base):
@@ -308,3 +364,155 @@ def test_adjoint_with_overflowed_contact_lists(af3d, base, oracle, tangent):
     scale = float(np.abs(dJ).max())
     bad = [(k, adj[k], dJ[k]) for k in range(8) if abs(adj[k] - dJ[k]) > 1e-7 * max(abs(dJ[k]), 1e-3 * scale)]
     assert not bad, list(zip(adj, dJ))
+
+
+RUNOUT_L = 10.0   # cm: the soft maximum weights the clumps within a few l of the front
+
+
+def test_runout_objective_value(af3d, base):
+    """af3d_adjoint's runout J equals the host evaluation on the exported final state."""
+    from avalancheflume3d_gb300.adjoint import runout
+    _, sys, fun, pp = base
+    with af3d.Engine(sys, fun) as eng:
+        eng.import_particles(pp)
+        J = eng.adjoint(STEPS, gradients=False, runout=RUNOUT_L)["J"]
+        p = eng.export_particles(with_accel=False)
+    assert J == pytest.approx(runout(p, sys, RUNOUT_L), rel=1e-13)
+    assert J > np.percentile(_xrot(p, sys), 95)
+
+
+@pytest.mark.parametrize("friction", [0, 1])
+def test_runout_gradients_vs_finite_differences(af3d, base, friction):
+    """Gradients of the runout objective (a soft maximum of the downslope positions, length
+    scale 10 cm) with respect to the contact-law parameters and to the initial positions of the
+    clumps nearest the front, against central finite differences of the same forward run."""
+    from oracle.pyoracle import sphere_centres
+    _, sys, fun, pp = base
+    out = _adjoint(af3d, sys, fun, pp, friction=friction, runout=RUNOUT_L)
+    grads = out["params"]
+    base_state = _final(af3d, sys, fun, pp, friction=friction)
+    scale = max(abs(v * float(sys[k])) for k, v in grads.items())
+    rows, bad = [], []
+    for k, g in grads.items():
+        h = REL * float(sys[k])
+        sp, sm = sys.copy(), sys.copy()
+        sp[k] += h
+        sm[k] -= h
+        fd = (_runout_difference(_final(af3d, sp, fun, pp, friction=friction), base_state, sys, RUNOUT_L) -
+              _runout_difference(_final(af3d, sm, fun, pp, friction=friction), base_state, sys, RUNOUT_L)) / (2 * h)
+        rows.append((k, g * float(sys[k]), fd * float(sys[k])))
+        if not _close(g * float(sys[k]), fd * float(sys[k]), scale):
+            bad.append(k)
+    assert not bad, rows
+    assert sum(abs(r[2]) > 1e-3 * scale for r in rows) >= 2, rows
+    g = out["r0"]
+    pick = np.argsort(-_xrot(pp, sys))[:3]
+    h = 1e-6 * float(pp["radius"][0])
+    gscale = float(np.abs(g).max())
+    for i in pick:
+        for ax in (0, 2):
+            qp, qm = pp.copy(), pp.copy()
+            qp["rr"][i, ax] += h
+            qm["rr"][i, ax] -= h
+            sphere_centres(qp)
+            sphere_centres(qm)
+            fd = (_runout_difference(_final(af3d, sys, fun, qp, friction=friction), base_state, sys, RUNOUT_L) -
+                  _runout_difference(_final(af3d, sys, fun, qm, friction=friction), base_state, sys, RUNOUT_L)) / (2 * h)
+            rows.append((int(i), ax, g[i, ax], fd))
+            if not _close(g[i, ax], fd, gscale):
+                bad.append((int(i), ax))
+    assert not bad, rows
+
+
+def _moved(pp, r0):
+    """pp with its clump centres at r0 (the sphere centres follow)."""
+    from oracle.pyoracle import sphere_centres
+    q = pp.copy()
+    q["rr"] = r0
+    sphere_centres(q)
+    return q
+
+
+def test_flume_run_function_autograd(af3d, base):
+    """The torch.autograd.Function: torch.autograd.grad of J with respect to the initial
+    positions equals the engine's adjoint, for one flume and (scaled per flume by the incoming
+    gradient) for an ensemble."""
+    torch = pytest.importorskip("torch")
+    from avalancheflume3d_gb300.adjoint import flume_run_function
+    _, sys, fun, pp = base
+    FlumeRun = flume_run_function()
+    steps, ckpt = 40, 20
+
+    def make(r0):
+        eng = af3d.Engine(sys, fun)
+        eng.import_particles(_moved(pp, r0))
+        return eng
+
+    r0 = torch.tensor(pp["rr"], dtype=torch.float64, requires_grad=True)
+    J = FlumeRun.apply(r0, make, steps, ckpt, None)
+    (g,) = torch.autograd.grad(3.0 * J, r0)
+    want = _adjoint(af3d, sys, fun, pp, steps=steps, ckpt=ckpt)
+    assert float(J.detach()) == pytest.approx(want["J"], rel=1e-13)
+    assert np.allclose(g.numpy(), 3.0 * want["r0"], rtol=1e-9, atol=1e-12 * float(np.abs(want["r0"]).max()))
+    # an ensemble of two copies with different friction: J has one entry per flume
+    sys2 = sys.copy()
+    sys2["mu_pw"] = 0.25
+    sys2["fr_fact_pw"] = 0.25 / 1.0e12
+    syss, funs = np.stack([sys, sys2]), np.stack([fun, fun])
+
+    def make_ens(r0):
+        eng = af3d.Engine(syss, funs)
+        eng.import_particles(np.concatenate([_moved(pp, r0[:N]), _moved(pp, r0[N:])]))
+        return eng
+
+    r0e = torch.tensor(np.concatenate([pp["rr"], pp["rr"]]), dtype=torch.float64, requires_grad=True)
+    Je = FlumeRun.apply(r0e, make_ens, steps, ckpt, None)
+    assert Je.shape == (2,)
+    (ge,) = torch.autograd.grad(2.0 * Je[0] - 5.0 * Je[1], r0e)
+    with af3d.Engine(syss, funs) as eng:
+        eng.import_particles(np.concatenate([pp, pp]))
+        we = eng.adjoint(steps, ckpt)
+    assert np.allclose(Je.detach().numpy(), we["J"], rtol=1e-13)
+    wg = np.concatenate([2.0 * we["r0"][:N], -5.0 * we["r0"][N:]])
+    assert np.allclose(ge.numpy(), wg, rtol=1e-9, atol=1e-12 * float(np.abs(wg).max()))
+
+
+def test_adjoint_configs4_flume_vs_tangent_linear_model(af3d, oracle, tangent):
+    """The adjoint configuration itself: 32,768 clumps of the 80 cm x 4 cm flume at 35 deg (dense
+    bed layer), the device friction variant (every parameter has a gradient), 1,000 exact steps
+    with a checkpoint every 250 (three segments recomputed), against the FP64 tangent-linear model
+    on the same run (all host threads): the six contact-law parameters and one random
+    perturbation of the positions and orientations, to 1e-7.  (Over this many clumps and steps,
+    finite differences of J are dominated by discrete events -- contacts starting a step
+    earlier or later under the perturbation -- which the piecewise-smooth derivative excludes by
+    definition; the tangent-linear model follows the same pieces.)"""
+    import os
+    from oracle.pyoracle import CELL_PAR, PARTICLE, SYSTEM_PAR, state_tangent
+    from avalancheflume3d_gb300.workloads import flume_2k, flume_state
+    cfg = flume_2k(n=32768, tilt_deg=35.0, Lflume=80.0, layout="bed")
+    sys, fun, pp = flume_state(cfg)
+    n, steps = len(pp), 1000
+    out = _adjoint(af3d, sys, fun, pp, steps=steps, ckpt=250, friction=1)
+    names = list(out["params"])
+    dsys = np.zeros(7, dtype=SYSTEM_PAR)
+    for k, name in enumerate(names):
+        dsys[k][name] = float(sys[name])
+    rng = np.random.default_rng(41)
+    dr, dphi = rng.standard_normal((n, 3)) * float(sys["rmax"]), rng.standard_normal((n, 3))
+    dpp = np.zeros((7, n), dtype=PARTICLE)
+    dpp[6] = state_tangent(pp, sys, dr=dr, dphi=dphi)
+    cp = np.zeros((), dtype=CELL_PAR)
+    cp["ntags"] = 9
+    cp["rr_max"], cp["rr_min"] = oracle.cell_dim(pp, sys)
+    oracle.grid_from_bbox(cp, sys)
+    tangent.set_threads(os.cpu_count() or 1)
+    J, dJ, _ = tangent.run(sys, fun, cp, pp, steps, variant=1, dsys=dsys, dpp=dpp)
+    dR = np.stack([dpp[6]["Rmatx"], dpp[6]["Rmaty"], dpp[6]["Rmatz"]], 1)
+    adj = [out["params"][k] * float(sys[k]) for k in names]
+    adj.append(float(np.sum(out["r0"] * dr) + np.sum(out["R0"] * dR)))
+    assert out["J"] == pytest.approx(J, rel=1e-12)
+    scale = float(np.abs(dJ).max())
+    bad = [(k, adj[k], dJ[k]) for k in range(7) if abs(adj[k] - dJ[k]) > 1e-7 * max(abs(dJ[k]), 1e-3 * scale)]
+    assert not bad, list(zip(names + ["state"], adj, dJ))
+    pscale = float(np.abs(dJ[:6]).max())
+    assert all(abs(d) > 1e-4 * pscale for d in dJ[:6]), list(zip(names, dJ))
