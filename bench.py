@@ -64,6 +64,8 @@ def parse_args():
     p.add_argument("--cpu-sample", type=int, default=16384, help="clumps in the CPU baseline sample")
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-configs", action="store_true",
+                   help="skip the extra configurations (2,048-clump flume, 524,288-clump funnel and hopper)")
     p.add_argument("--fp-mode", choices=["exact", "fast"], default="fast",
                    help="FP64 mode of the timed steps (the other mode is timed beside it)")
     p.add_argument("--no-other-mode", action="store_true", help="do not time the other FP64 mode")
@@ -355,6 +357,13 @@ def measure_ensemble(args, stream):
     contacts = eng.contact_count()
     n_total = len(pp)
     first = eng.first_id.copy()
+    # The kernels' own time per step (CUDA events around each kernel group of profiled steps):
+    # what a single persistent launch could at best bring the graph-replayed step down to.
+    import ctypes as C
+    from avalancheflume3d_gb300 import lib
+    prof = np.zeros(6)
+    lib().af3d_step_profile(eng._h, 16, prof.ctypes.data_as(C.c_void_p))
+    prof /= 16
     eng.close()
     del eng
     value = n_total * K / t_ens
@@ -379,6 +388,10 @@ def measure_ensemble(args, stream):
                                  "what": "every %d-th flume alone in a plain context, one after another"
                                          % stride},
             "speedup_vs_sequential": value / seq,
+            "kernel_ms_per_step": float(prof.sum()),
+            "launch_overhead_ms_per_step": 1e3 * t_ens / K - float(prof.sum()),
+            "launch_note": "graph-replayed step time minus the summed kernel-group times of profiled steps: "
+                           "the most a single persistent launch could save",
             "flagged_by_error_check": len(ensemble_flagged(cfgs)),
             "graph_steps": 64, "layout": args.layout + " in each hopper, door open at t = 0",
             "geometry": "40 cm x 4 cm flume, reference hopper and funnel; per-flume slope 25-40 deg"}
@@ -464,6 +477,56 @@ def measure_adjoint(args, stream):
             "J_range": [float(bout["J"].min()), float(bout["J"].max())],
             "dJ_dconfig_sample0": g0}
     return res
+
+
+def measure_config(name, cfg, steps, warmup, mode, stream, cpu_seconds=0.0):
+    """One more configuration, timed like the headline (graph-replayed af3d_step, CUDA events on
+    the engine's stream, after `warmup` steps and a start-up force pass): ms per step, clump-
+    and contact-throughput, the per-kernel split of a profiled pass and the force kernel's HBM
+    roofline (B = 448 N + 8 C per launch).  With cpu_seconds > 0 also the oracle port on one
+    host core on the same state (a bounded window of steps)."""
+    import ctypes as C
+    import torch
+    from avalancheflume3d_gb300 import Engine, lib
+    from avalancheflume3d_gb300.workloads import flume_state
+    sys_, fun, pp = flume_state(cfg)
+    with Engine(sys_, fun, ntags=cfg.ntags, stream=stream.cuda_stream, fp_mode=mode) as eng:
+        eng.import_particles(pp)
+        eng.forces()
+        eng.swap_accel()
+        eng.step(warmup)
+        eng.prepare_steps(steps)
+        eng.contact_count()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        eng.step(steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        contacts = eng.contact_count()
+        ncell3 = int(eng.get_grid()["ncell3"])
+        names = ["time_advance", "predict_keys", "cell_sort", "permute_records", "fused_forces", "regrid"]
+        prof = np.zeros(len(names))
+        nprof = max(2, min(10, steps))
+        lib().af3d_step_profile(eng._h, nprof, prof.ctypes.data_as(C.c_void_p))
+        prof /= nprof
+    peaks, peak_kind = measured_peaks()
+    t_forces = prof[names.index("fused_forces")] / 1e3
+    alg = BYTES_PER_CLUMP * len(pp) + BYTES_PER_CELL * ncell3
+    out = {"workload": name, "clumps": len(pp), "cells": ncell3, "steps": steps, "warmup": warmup,
+           "value": len(pp) * steps / (ms / 1e3), "unit": "clump-steps/s", "ms_per_step": ms / steps,
+           "contacts_per_step": contacts / steps, "contacts_per_s": contacts / (ms / 1e3),
+           "phase_ms": {k: float(v) for k, v in zip(names, prof)},
+           "roofline": {"kernel": "k_lists_forces", "algorithmic_bytes_per_launch": alg,
+                        "achieved": alg / t_forces / 1e9 if t_forces > 0 else None, "unit": "GB/s",
+                        "peak": peaks.get("hbm_gbs"), "peak_source": peak_kind,
+                        "frac": alg / t_forces / 1e9 / peaks["hbm_gbs"] if t_forces > 0 else None}}
+    if cpu_seconds > 0:
+        val, k, dt = time_cpu(sys_, fun, pp, 1, cpu_seconds)
+        out["cpu_baseline"] = {"value": val, "unit": "clump-steps/s", "cores": 1, "kind": "port",
+                               "sample": "the whole state, %d steps in %.1f s, 1 thread" % (k, dt)}
+    return out
 
 
 def time_other_mode(eng, modes, other, args, stream, R, dev, world):
@@ -618,6 +681,18 @@ def run_engine(args):
                        "step, export of the AoS + a_i in place; the copies of each quarter of the "
                        "clumps overlap the work on the others)"}
 
+    configs = {}
+    if world == 1 and not args.no_configs:
+        from avalancheflume3d_gb300.workloads import flume_2k, funnel_524k
+        mode = modes[args.fp_mode]
+        configs["flume2k"] = measure_config(
+            "flume2k: 2,048 clumps, 40 cm x 4 cm flume at 30 deg, dense bed layer", flume_2k(layout="bed"),
+            1000, 20, mode, stream, 0.0 if args.no_cpu else min(5.0, args.cpu_seconds))
+        configs["funnel524k"] = measure_config(
+            "funnel524k: 524,288 polydisperse clumps (size factor U[0.8, 1.2]), reference hopper, funnel and "
+            "40 cm x 4 cm flume at 30 deg; half in the hopper, half on the funnel and flume bed", funnel_524k(),
+            args.steps, args.warmup, mode, stream)
+
     ens = None
     if world == 1 and args.ensemble_flumes > 0:
         ens = measure_ensemble(args, stream)
@@ -659,6 +734,7 @@ def run_engine(args):
                          "kernel_ms": prof[names.index("fused_forces")], "note": "FP64-issue bound; see fp64"},
             "fp64": fp64_line(fp64.value, t_forces, args.fp_mode),
             "phase_ms": {k: float(v) for k, v in zip(names, prof)},
+            "configs": configs or None,
             "ensemble": ens,
             "adjoint": adj,
             "cpu_baseline": cpu,
