@@ -104,6 +104,9 @@ SIGNATURES = [
     ("af3d_get_status", [_P, _P], C.c_int),
     ("af3d_adjoint", [_P, C.c_long, C.c_long, _P, _P, _P, _P, _P, _P], C.c_int),
     ("af3d_set_objective", [_P, C.c_int, C.c_double], C.c_int),
+    ("af3d_set_force_block", [_P, C.c_int], C.c_int),
+    ("af3d_get_force_block", [_P, _P], C.c_int),
+    ("af3d_autotune_shapes", [_P, C.c_long, _P, _P, _P, _P], C.c_int),
     ("af3d_step_profile", [_P, C.c_long, _P], C.c_int),
     ("af3d_kernel_launches", [_P, _P], C.c_int),
     ("af3d_fp64_peak", [_P], C.c_int),

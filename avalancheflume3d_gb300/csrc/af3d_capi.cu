@@ -46,7 +46,6 @@ constexpr long kKernelsPerForcePass = 1;   // lists and forces in one kernel
 #define AF3D_HOST_PARTS 4
 #endif
 constexpr int kHostParts = AF3D_HOST_PARTS;   // af3d_step_host: parts whose copies overlap the step
-constexpr long kForceBlock = 128;           // k_lists_forces' block: a part starts on a block boundary
 constexpr long kKernelsPerStep = kKernelsPerCellBuild + 1 + kKernelsPerForcePass;   // + time advance
 constexpr long kKernelsPerKeptStep = kKernelsPerStep - 1;    // a step without the permutation
 constexpr long kKernelsPerRegrid = 4;
@@ -79,6 +78,31 @@ struct StepGraph {
 
 }  // namespace
 
+namespace {
+
+// The force kernel's shape whose last wave of blocks is fullest for n clumps on `sms` SMs: a
+// launch of b blocks on sms * minb resident slots runs ceil(b / slots) waves, and the work of
+// b / slots of them; fewer blocks than slots: the shape that spreads them over more SMs.  Ties
+// keep the larger block.  af3d_autotune measures instead.
+int force_shape_for(long n, int sms) {
+  if (n <= 0 || sms <= 0) return 0;
+  int best = 0;
+  double best_fill = -1.0;
+  for (int i = 0; i < kForceShapes; i++) {
+    const double blocks = (double)((n + kForceShapeBlock[i] - 1) / kForceShapeBlock[i]);
+    const double slots = (double)sms * kForceShapeMinb[i];
+    const double waves = blocks / slots;
+    const double fill = waves >= 1.0 ? waves / std::ceil(waves) : std::min(blocks, (double)sms) / sms;
+    if (fill > best_fill + 1e-9) {
+      best_fill = fill;
+      best = i;
+    }
+  }
+  return best;
+}
+
+}  // namespace
+
 struct af3d_ctx {
   int device = 0;
   long n = 0;
@@ -95,6 +119,7 @@ struct af3d_ctx {
   int phase = AF3D_PHASE_AVALANCHE;
   int variant = AF3D_FRICTION_HST;
   int fp_mode = AF3D_FP_EXACT;
+  int force_shape = 0;       // index into kForceShapeBlock / kForceShapeMinb
   double obj_length = 0.0;   // objective of af3d_adjoint: 0 deposit centroid, > 0 runout length scale
   long cc = 0;                        // steps done in the current phase
   bool imported = false;
@@ -309,10 +334,10 @@ void forces_for(af3d_ctx *c, bool write_ft, const int *order, Planes out, bool w
   if (look) la = LookAhead{c->nbr_next, c->cull_next, c->cells, c->id_cur};
   if (c->fp_mode == AF3D_FP_FAST)
     fast::launch_lists_forces(c->L(), c->cur, out, c->d, c->fl_cur, c->nbr, c->cull, c->cells.start, order, csort,
-                              c->lists, write_ft, uni, warm, la, s0, count);
+                              c->lists, write_ft, uni, warm, la, s0, count, c->force_shape);
   else
     launch_lists_forces(c->L(), c->cur, out, c->d, c->fl_cur, c->nbr, c->cull, c->cells.start, order, csort,
-                        c->lists, write_ft, uni, warm, la, s0, count);
+                        c->lists, write_ft, uni, warm, la, s0, count, c->force_shape);
 }
 
 void enqueue_cell_build(af3d_ctx *c, bool predict, bool t_prev, bool ft = true) {
@@ -525,6 +550,9 @@ af3d_status af3d_create_ensemble(int nflumes, const af3d_system_par *sys, const 
   c->ntags = ntags;
   c->phase = phase;
   cudaError_t e = cudaGetDevice(&c->device);
+  int sms = 0;
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+  c->force_shape = force_shape_for(c->n, sms);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
     delete c;
@@ -759,7 +787,7 @@ af3d_status af3d_step_host(af3d_ctx *c, const af3d_particle *in, const af3d_vec3
   // out) and the last part to arrive (copy in, then conversion and predictor) are the ones
   // whose work nothing overlaps, so they get half a part's share of the clumps and the others
   // share the rest: `out_at` splits the export, `in_at` (the mirror image) the import.
-  auto round_up = [](long x) { return (x + kForceBlock - 1) / kForceBlock * kForceBlock; };
+  auto round_up = [](long x) { return (x + kForceAlign - 1) / kForceAlign * kForceAlign; };
   const long edge = (n + 2 * kHostParts - 1) / (2 * kHostParts);
   long out_at[kHostParts + 1], in_at[kHostParts + 1];
   out_at[0] = 0;
@@ -1209,6 +1237,77 @@ af3d_status af3d_set_resort_every(af3d_ctx *c, long steps) {
   if (steps != c->resort_every) drop_graphs(c);
   c->resort_every = steps;
   c->since_sort = std::min(c->since_sort, steps);
+  return AF3D_OK;
+}
+
+af3d_status af3d_set_force_block(af3d_ctx *c, int block) {
+  CHECK_CTX(c);
+  for (int i = 0; i < kForceShapes; i++)
+    if (kForceShapeBlock[i] == block) {
+      if (i != c->force_shape) drop_graphs(c);   // graphs hold the force launches' shape
+      c->force_shape = i;
+      return AF3D_OK;
+    }
+  return fail(AF3D_ERR_ARG, "force block: 64, 96 or 128 threads");
+}
+
+af3d_status af3d_get_force_block(af3d_ctx *c, int *block) {
+  CHECK_CTX(c);
+  if (!block) return fail(AF3D_ERR_ARG, "null argument");
+  *block = kForceShapeBlock[c->force_shape];
+  return AF3D_OK;
+}
+
+af3d_status af3d_autotune_shapes(af3d_ctx *c, long steps_per_trial, long *resort_every, int *force_block,
+                                 double *ms_interval, double *ms_block) {
+  CHECK_STATE(c);
+  long every = 0;
+  af3d_status s = af3d_autotune(c, steps_per_trial, &every, ms_interval);
+  if (s) return s;
+  // Then each force-kernel shape at that interval: one untimed period (its graph is captured),
+  // then whole periods timed, a trial that crossed a re-grid run again.  Results do not depend
+  // on the shape, so these are ordinary steps of the run as well.
+  cudaEvent_t e0, e1;
+  AF3D_CUDA(cudaEventCreate(&e0));
+  AF3D_CUDA(cudaEventCreate(&e1));
+  struct Events {
+    cudaEvent_t a, b;
+    ~Events() {
+      cudaEventDestroy(a);
+      cudaEventDestroy(b);
+    }
+  } events{e0, e1};
+  int best = c->force_shape;
+  double best_ms = 0.0;
+  const long k = std::max(2 * every, (steps_per_trial + every - 1) / every * every);
+  for (int i = 0; i < kForceShapes; i++) {
+    s = af3d_set_force_block(c, kForceShapeBlock[i]);
+    if (s) return s;
+    s = af3d_step(c, every);
+    if (s) return s;
+    double ms = 0.0;
+    for (int attempt = 0; attempt < 2; attempt++) {
+      const long cc0 = c->cc;
+      AF3D_CUDA(cudaEventRecord(e0, c->st));
+      s = af3d_step(c, k);
+      if (s) return s;
+      AF3D_CUDA(cudaEventRecord(e1, c->st));
+      AF3D_CUDA(cudaEventSynchronize(e1));
+      float t = 0.0f;
+      AF3D_CUDA(cudaEventElapsedTime(&t, e0, e1));
+      ms = t / k;
+      if (cc0 / kRegridEvery == (c->cc - 1) / kRegridEvery) break;   // no re-grid inside
+    }
+    if (ms_block) ms_block[i] = ms;
+    if (best_ms == 0.0 || ms < best_ms) {
+      best_ms = ms;
+      best = i;
+    }
+  }
+  s = af3d_set_force_block(c, kForceShapeBlock[best]);
+  if (s) return s;
+  if (resort_every) *resort_every = every;
+  if (force_block) *force_block = kForceShapeBlock[best];
   return AF3D_OK;
 }
 

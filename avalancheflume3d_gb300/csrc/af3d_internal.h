@@ -144,6 +144,17 @@ struct DevScalars {
   DevFlume       *flumes;      // [nflumes]
 };
 
+// Shapes of the fused force kernel: threads per block (the pool of clumps whose contact items a
+// block processes together) and resident blocks per SM (the register budget, 65536 / (block x
+// blocks)).  Results do not depend on the shape; af3d_autotune times them, and a new context
+// starts with the one whose last wave of blocks is fullest on its device (force_shape_for).
+constexpr int kForceShapes = 3;
+constexpr int kForceShapeBlock[kForceShapes] = {128, 96, 64};
+constexpr int kForceShapeMinb[kForceShapes] = {5, 6, 10};
+// Steps whose force pass runs in parts (af3d_step_host) cut the clumps at multiples of every
+// shape's block.
+constexpr long kForceAlign = 384;
+
 // Per-clump item lists of one force pass, from the list phase to the force phase of the force
 // kernel: entry e of slot s at items[e * n + s] (an item is a boundary (routine, sphere) or a
 // particle (partner slot, sph_id) contact).  With cnt, the pass also records each clump's list
@@ -211,7 +222,7 @@ void launch_lists_forces (const Launch &L, Planes cur, Planes out, DevScalars *d
                           const NbrRec *nbr, const CullRec *cull, const int *start, const int *order,
                           const float4 *csort, ContactLists lists, bool write_ft,
                           const Consts *uniform = nullptr, bool warm = false,
-                          LookAhead look = LookAhead{}, long s0 = 0, long count = -1);
+                          LookAhead look = LookAhead{}, long s0 = 0, long count = -1, int shape = 0);
 void launch_boundary (const Launch &L, Planes cur, DevScalars *d, const int *flume, int routine);
 void launch_part (const Launch &L, Planes cur, DevScalars *d, const int *flume, const NbrRec *nbr,
                   const CullRec *cull, const int *start, int sph_id);
@@ -275,7 +286,7 @@ void launch_lists_forces (const Launch &L, Planes cur, Planes out, DevScalars *d
                           const NbrRec *nbr, const CullRec *cull, const int *start, const int *order,
                           const float4 *csort, ContactLists lists, bool write_ft,
                           const Consts *uniform = nullptr, bool warm = false,
-                          LookAhead look = LookAhead{}, long s0 = 0, long count = -1);
+                          LookAhead look = LookAhead{}, long s0 = 0, long count = -1, int shape = 0);
 }  // namespace fast
 
 }  // namespace af3d

@@ -19,13 +19,7 @@ namespace af3d {
 
 namespace {
 
-constexpr int kBlock = 128;
-// Resident blocks per SM requested for the force kernel (register budget 65536 / (128 x n)):
-// five (102 registers, some spilled) measured fastest in both FP64 modes on the 262,144-clump
-// bed, ahead of 3, 4, 6 and 8.
-#ifndef AF3D_FORCES_MINB
-#define AF3D_FORCES_MINB 5
-#endif
+constexpr int kBlock = 128;   // the per-clump kernels other than the fused force kernel
 
 inline unsigned grid_for(long n, int block = kBlock) {
   return (unsigned)((n + block - 1) / block);
@@ -171,6 +165,7 @@ constexpr int kRecStride = kRecWords + 1;
 
 // The block's records, staged in shared memory and written out as contiguous 16-byte stores.
 // Every thread of a kPermBlock-thread block calls this (slots past n contribute nothing).
+template <int NB>
 __device__ __forceinline__ void store_records(bool valid, long base, long n, const NbrRec &q, const CullRec &cr,
                                               NbrRec *nbr, CullRec *cull, double *s_nbr, CullRec *s_cull) {
   if (valid) {
@@ -180,17 +175,17 @@ __device__ __forceinline__ void store_records(bool valid, long base, long n, con
     s_cull[threadIdx.x] = cr;
   }
   __syncthreads();
-  const long cnt = n - base < kPermBlock ? n - base : kPermBlock;
+  const long cnt = n - base < NB ? n - base : NB;
   const int nw = (int)(cnt * kRecWords) / 2;   // double2 words of the block's records
   double2 *b = reinterpret_cast<double2 *>(nbr + base);
-  for (int i = threadIdx.x; i < nw; i += kPermBlock) {
+  for (int i = threadIdx.x; i < nw; i += NB) {
     const int w0 = 2 * i, r0 = w0 / kRecWords, k0 = w0 - r0 * kRecWords;   // k0 even, k0 + 1 < 24
     b[i] = make_double2(s_nbr[r0 * kRecStride + k0], s_nbr[r0 * kRecStride + k0 + 1]);
   }
   const int m16 = (int)(cnt * (long)(sizeof(CullRec) / 16));
   const float4 *c = reinterpret_cast<const float4 *>(s_cull);
   float4 *e = reinterpret_cast<float4 *>(cull + base);
-  for (int i = threadIdx.x; i < m16; i += kPermBlock) e[i] = c[i];
+  for (int i = threadIdx.x; i < m16; i += NB) e[i] = c[i];
 }
 
 // ------------------------------------------------------------------ init_Verlet (+ cell keys)
@@ -400,7 +395,7 @@ __global__ void __launch_bounds__(kBlock) k_predict(Planes P, DevScalars *d, boo
       cells.rank_tmp[s] = atomicAdd(&cells.count[key], 1);
     }
   }
-  if (RECORDS) store_records(valid, base, n, q, cr, nbr, cull, s_nbr, s_cull);
+  if (RECORDS) store_records<kPermBlock>(valid, base, n, q, cr, nbr, cull, s_nbr, s_cull);
 }
 
 // ------------------------------------------------------------------ permutation + records
@@ -436,7 +431,7 @@ __global__ void __launch_bounds__(kPermBlock) k_permute(Planes src, Planes dst, 
     make_records(load3(dst, RX, s), load3(dst, VX, s), load3(dst, WX, s), sp, dst.p[RAD][s], dst.p[MSPH][s],
                  dst.p[MWALL][s], q, cr);
   }
-  store_records(s < n, base, n, q, cr, nbr, cull, s_nbr, s_cull);
+  store_records<kPermBlock>(s < n, base, n, q, cr, nbr, cull, s_nbr, s_cull);
 }
 
 // ------------------------------------------------------------------ particle contacts
@@ -550,19 +545,21 @@ __device__ __forceinline__ int particle_contacts(long s, const Own &o, const Con
 // process (and for removed clumps).  A clump whose lists overflowed runs alone afterwards, in
 // the same order.
 constexpr int kBatch = 256;
+template <int NB>
 struct BlockQueue {
-  int base[kBlock + 1];   // exclusive prefix of the clumps' item counts
-  int pbase[kBlock + 1];  // ... of their particle item counts (kind-sorted pass)
-  int qbase[kBlock + 1];  // ... of their boundary item counts (kind-sorted pass)
-  int npre[kBlock];       // boundary items before the particle items, per clump
-  int wsum[3][kBlock / 32];
+  int base[NB + 1];   // exclusive prefix of the clumps' item counts
+  int pbase[NB + 1];  // ... of their particle item counts (kind-sorted pass)
+  int qbase[NB + 1];  // ... of their boundary item counts (kind-sorted pass)
+  int npre[NB];       // boundary items before the particle items, per clump
+  int wsum[3][NB / 32];
   double res[6][kBatch];  // [component][item in the batch]
   unsigned char flag[kBatch];
 };
 
 // The thread whose range [base[t], base[t+1]) holds position j.
+template <int NB>
 __device__ __forceinline__ int block_owner_of(const int *base, int j) {
-  int lo = 0, hi = kBlock - 1;
+  int lo = 0, hi = NB - 1;
   while (lo < hi) {
     const int mid = (lo + hi + 1) >> 1;
     if (base[mid] <= j) lo = mid; else hi = mid - 1;
@@ -571,7 +568,8 @@ __device__ __forceinline__ int block_owner_of(const int *base, int j) {
 }
 
 // Block-wide exclusive prefixes of three per-thread counts (all threads call this).
-__device__ __forceinline__ void block_prefix3(BlockQueue &bq, int a, int b, int c) {
+template <int NB>
+__device__ __forceinline__ void block_prefix3(BlockQueue<NB> &bq, int a, int b, int c) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   int v[3] = {a, b, c};
 #pragma unroll
@@ -590,13 +588,13 @@ __device__ __forceinline__ void block_prefix3(BlockQueue &bq, int a, int b, int 
   for (int q = 0; q < 3; q++) {
     int wofs = 0, total = 0;
 #pragma unroll
-    for (int w = 0; w < kBlock / 32; w++) {
+    for (int w = 0; w < NB / 32; w++) {
       const int t = bq.wsum[q][w];
       wofs += w < warp ? t : 0;
       total += t;
     }
     dst[q][tid] = wofs + v[q] - own[q];
-    if (tid == kBlock - 1) dst[q][kBlock] = total;
+    if (tid == NB - 1) dst[q][NB] = total;
   }
   __syncthreads();
 }
@@ -604,8 +602,8 @@ __device__ __forceinline__ void block_prefix3(BlockQueue &bq, int a, int b, int 
 // UNIFORM: every clump of the launch belongs to one flume, whose constants `c` are (a
 // reference to) a kernel parameter.  lc: the clump's list layout (pre boundary items, particle
 // items, the rest boundary items).
-template <bool UNIFORM>
-__device__ __forceinline__ int block_contacts(BlockQueue &bq, long bbase, long s, bool act, bool aval,
+template <int NB, bool UNIFORM>
+__device__ __forceinline__ int block_contacts(BlockQueue<NB> &bq, long bbase, long s, bool act, bool aval,
                                               double B, const Own &o, const Consts &c,
                                               const af3d_cell_par &g, long long off,
                                               const DevScalars *d, const int *__restrict__ flume,
@@ -622,9 +620,9 @@ __device__ __forceinline__ int block_contacts(BlockQueue &bq, long bbase, long s
   const int nitems = act && listed > 0 ? listed : 0;
   const int npair = nitems > 0 ? lc.pair : 0;
   bq.npre[tid] = nitems > 0 ? lc.pre : 0;
-  block_prefix3(bq, nitems, npair, nitems - npair);
-  const int base = bq.base[tid], total = bq.base[kBlock];
-  const int ptotal = bq.pbase[kBlock];
+  block_prefix3<NB>(bq, nitems, npair, nitems - npair);
+  const int base = bq.base[tid], total = bq.base[NB];
+  const int ptotal = bq.pbase[NB];
   // One item: its contact into the batch's result slot jb.
   auto process = [&](int lo, int idx, int jb) {
     const unsigned it = items[(long)idx * n + bbase + lo];   // written in this launch
@@ -693,20 +691,20 @@ __device__ __forceinline__ int block_contacts(BlockQueue &bq, long bbase, long s
   const bool kind_order = total <= kBatch;
   for (int b0 = 0; b0 < total; b0 += kBatch) {
     const int bn = total - b0 < kBatch ? total - b0 : kBatch;
-    for (int r0 = warp * 32; r0 < bn; r0 += kBlock) {
+    for (int r0 = warp * 32; r0 < bn; r0 += NB) {
       const int i = r0 + lane;
       if (i < bn) {
         int lo, idx;
         if (kind_order && i < ptotal) {
-          lo = block_owner_of(bq.pbase, i);
+          lo = block_owner_of<NB>(bq.pbase, i);
           idx = bq.npre[lo] + (i - bq.pbase[lo]);
         } else if (kind_order) {
           const int ib = i - ptotal;
-          lo = block_owner_of(bq.qbase, ib);
+          lo = block_owner_of<NB>(bq.qbase, ib);
           const int b = ib - bq.qbase[lo], np = bq.npre[lo];
           idx = b < np ? b : b + (bq.pbase[lo + 1] - bq.pbase[lo]);
         } else {
-          lo = block_owner_of(bq.base, b0 + i);   // the thread whose list holds item b0 + i
+          lo = block_owner_of<NB>(bq.base, b0 + i);   // the thread whose list holds item b0 + i
           idx = b0 + i - bq.base[lo];
         }
         process(lo, idx, kind_order ? bq.base[lo] + idx : i);
@@ -784,23 +782,23 @@ __device__ __forceinline__ int lists_body(const Consts &c, const DevScalars *d, 
 
 // Shared memory of the force kernel: the list phase, the force phase and the look-ahead's record
 // staging run one after another.
+template <int NB>
 union ForceShared {
-  PassLists pl[kBlock / 32];
-  BlockQueue bq;
+  PassLists pl[NB / 32];
+  BlockQueue<NB> bq;
   struct {
-    double nbr[kPermBlock * kRecStride];
-    CullRec cull[kPermBlock];
+    double nbr[NB * kRecStride];
+    CullRec cull[NB];
   } rec;
 };
-static_assert(kPermBlock == kBlock, "record staging covers one block");
 
-template <bool WRITE_FT, bool UNIFORM>
+template <int NB, bool WRITE_FT, bool UNIFORM>
 __device__ __forceinline__ void fused_body(const Consts &c, Planes P, Planes out, DevScalars *d,
                                            const int *__restrict__ flume, const NbrRec *__restrict__ nbr,
                                            const CullRec *__restrict__ cull, const int *__restrict__ start,
                                            const int *__restrict__ order, ContactLists lists, int listed,
                                            ListCounts lc, long s0, long n, bool warm, const LookAhead &la,
-                                           ForceShared &sh) {
+                                           ForceShared<NB> &sh) {
   const long s = s0 + blockIdx.x * (long)blockDim.x + threadIdx.x;
   const bool valid = s < n;
   const long sv = valid ? s : n - 1;   // in-range slot for lanes past n (nothing is written for them)
@@ -817,7 +815,7 @@ __device__ __forceinline__ void fused_body(const Consts &c, Planes P, Planes out
     for (int rt = R_HOP0; rt <= R_FCORNERS; rt++)
       if (bnd_may_touch(rt, o.r, B, c)) bnd_routine(rt, o, true, c, F, T);
   const long bbase = s0 + blockIdx.x * (long)blockDim.x;
-  const int active = block_contacts<UNIFORM>(sh.bq, bbase, sv, valid && !removed, aval, B, o, c, g, off, d, flume,
+  const int active = block_contacts<NB, UNIFORM>(sh.bq, bbase, sv, valid && !removed, aval, B, o, c, g, off, d, flume,
                                              nbr, cull, start, order, lists.items, valid ? listed : 0, lc, n, F, T);
   NbrRec q;
   CullRec cr;
@@ -893,7 +891,7 @@ __device__ __forceinline__ void fused_body(const Consts &c, Planes P, Planes out
   warp_count(d, active);
   if (la.nbr) {
     __syncthreads();   // the force phase's shared memory is free again
-    store_records(valid, bbase, n, q, cr, la.nbr, la.cull, sh.rec.nbr, sh.rec.cull);
+    store_records<NB>(valid, bbase, n, q, cr, la.nbr, la.cull, sh.rec.nbr, sh.rec.cull);
   }
 }
 
@@ -1202,8 +1200,8 @@ void launch_build_records(const Launch &L, Planes cur, NbrRec *nbr, CullRec *cul
 // resident on one SM are in different phases most of the time, so the latency-bound walk of
 // some overlaps the FP64-bound contact laws of others.  The lists pass through global memory
 // (the block's own entries, visible to its threads after the barrier).
-template <bool WRITE_FT, bool UNIFORM>
-__global__ void __launch_bounds__(kBlock, AF3D_FORCES_MINB) k_lists_forces(Planes P, Planes out, DevScalars *d,
+template <int NB, int MINB, bool WRITE_FT, bool UNIFORM>
+__global__ void __launch_bounds__(NB, MINB) k_lists_forces(Planes P, Planes out, DevScalars *d,
                                                          const int *__restrict__ flume,
                                                          const NbrRec *__restrict__ nbr,
                                                          const CullRec *__restrict__ cull,
@@ -1212,13 +1210,13 @@ __global__ void __launch_bounds__(kBlock, AF3D_FORCES_MINB) k_lists_forces(Plane
                                                          const float4 *__restrict__ csort, ContactLists lists,
                                                          const __grid_constant__ Consts kc, bool warm,
                                                          const __grid_constant__ LookAhead la, long s0, long n) {
-  __shared__ ForceShared sh;
+  __shared__ ForceShared<NB> sh;
   ListCounts lc;
   if constexpr (UNIFORM) {
     const int listed = lists_body<true>(kc, d, flume, nbr, cull, start, order, csort, lists, s0, n,
                                         sh.pl[threadIdx.x >> 5], lc);
     __syncthreads();
-    fused_body<WRITE_FT, true>(kc, P, out, d, flume, nbr, cull, start, order, lists, listed, lc, s0, n, warm, la,
+    fused_body<NB, WRITE_FT, true>(kc, P, out, d, flume, nbr, cull, start, order, lists, listed, lc, s0, n, warm, la,
                                sh);
   } else {
     // the flume's constants read where they lie (a reference, not a register copy)
@@ -1227,36 +1225,54 @@ __global__ void __launch_bounds__(kBlock, AF3D_FORCES_MINB) k_lists_forces(Plane
     const int listed = lists_body<false>(c, d, flume, nbr, cull, start, order, csort, lists, s0, n,
                                          sh.pl[threadIdx.x >> 5], lc);
     __syncthreads();
-    fused_body<WRITE_FT, false>(c, P, out, d, flume, nbr, cull, start, order, lists, listed, lc, s0, n, warm, la,
+    fused_body<NB, WRITE_FT, false>(c, P, out, d, flume, nbr, cull, start, order, lists, listed, lc, s0, n, warm, la,
                                 sh);
+  }
+}
+
+template <int NB, int MINB>
+void launch_lists_forces_shape(const Launch &L, Planes cur, Planes out, DevScalars *d, const int *flume,
+                               const NbrRec *nbr, const CullRec *cull, const int *start, const int *order,
+                               const float4 *csort, ContactLists lists, bool write_ft, const Consts *uniform,
+                               bool warm, LookAhead look, long s0, long m) {
+  const Consts kc = uniform ? *uniform : Consts{};
+  const unsigned g = grid_for(m, NB);
+  if (uniform) {
+    if (write_ft)
+      k_lists_forces<NB, MINB, true, true><<<g, NB, 0, L.st>>>(cur, out, d, flume, nbr, cull, start, order, csort,
+                                                              lists, kc, warm, look, s0, L.n);
+    else
+      k_lists_forces<NB, MINB, false, true><<<g, NB, 0, L.st>>>(cur, out, d, flume, nbr, cull, start, order, csort,
+                                                               lists, kc, warm, look, s0, L.n);
+  } else {
+    if (write_ft)
+      k_lists_forces<NB, MINB, true, false><<<g, NB, 0, L.st>>>(cur, out, d, flume, nbr, cull, start, order, csort,
+                                                               lists, kc, warm, look, s0, L.n);
+    else
+      k_lists_forces<NB, MINB, false, false><<<g, NB, 0, L.st>>>(cur, out, d, flume, nbr, cull, start, order, csort,
+                                                                lists, kc, warm, look, s0, L.n);
   }
 }
 
 void launch_lists_forces(const Launch &L, Planes cur, Planes out, DevScalars *d, const int *flume,
                          const NbrRec *nbr, const CullRec *cull, const int *start, const int *order,
                          const float4 *csort, ContactLists lists, bool write_ft, const Consts *uniform, bool warm,
-                         LookAhead look, long s0, long count) {
-  // slots [s0, s0 + count) of L.n (count < 0: to the end); s0 a multiple of kBlock, so the
-  // launch's blocks are those of the whole pass
+                         LookAhead look, long s0, long count, int shape) {
+  // slots [s0, s0 + count) of L.n (count < 0: to the end); s0 a multiple of the shape's block,
+  // so the launch's blocks are those of the whole pass
   const long m = count < 0 ? L.n - s0 : std::min(count, L.n - s0);
-  if (L.n <= 0 || m <= 0 || s0 % kBlock != 0) return;
-  const Consts kc = uniform ? *uniform : Consts{};
-  const int g = grid_for(m);
-  if (uniform) {
-    if (write_ft)
-      k_lists_forces<true, true><<<g, kBlock, 0, L.st>>>(cur, out, d, flume, nbr, cull, start, order, csort, lists, kc,
-                                                        warm, look, s0, L.n);
-    else
-      k_lists_forces<false, true><<<g, kBlock, 0, L.st>>>(cur, out, d, flume, nbr, cull, start, order, csort, lists,
-                                                         kc, warm, look, s0, L.n);
-  } else {
-    if (write_ft)
-      k_lists_forces<true, false><<<g, kBlock, 0, L.st>>>(cur, out, d, flume, nbr, cull, start, order, csort, lists,
-                                                         kc, warm, look, s0, L.n);
-    else
-      k_lists_forces<false, false><<<g, kBlock, 0, L.st>>>(cur, out, d, flume, nbr, cull, start, order, csort, lists,
-                                                          kc, warm, look, s0, L.n);
-  }
+  if (L.n <= 0 || m <= 0 || shape < 0 || shape >= kForceShapes || s0 % kForceShapeBlock[shape] != 0) return;
+  static_assert(kForceShapes == 3 && kForceShapeBlock[0] == 128 && kForceShapeBlock[1] == 96 &&
+                    kForceShapeBlock[2] == 64, "the instantiated shapes");
+  if (shape == 0)
+    launch_lists_forces_shape<128, kForceShapeMinb[0]>(L, cur, out, d, flume, nbr, cull, start, order, csort,
+                                                       lists, write_ft, uniform, warm, look, s0, m);
+  else if (shape == 1)
+    launch_lists_forces_shape<96, kForceShapeMinb[1]>(L, cur, out, d, flume, nbr, cull, start, order, csort,
+                                                      lists, write_ft, uniform, warm, look, s0, m);
+  else
+    launch_lists_forces_shape<64, kForceShapeMinb[2]>(L, cur, out, d, flume, nbr, cull, start, order, csort,
+                                                      lists, write_ft, uniform, warm, look, s0, m);
 }
 
 void launch_boundary(const Launch &L, Planes cur, DevScalars *d, const int *flume, int routine) {

@@ -136,6 +136,29 @@ class Engine:
             timings.update(zip(self.RESORT_CHOICES, ms.tolist()))
         return r.value
 
+    FORCE_BLOCKS = (128, 96, 64)
+
+    def set_force_block(self, block: int) -> None:
+        """af3d_set_force_block: threads per block of the fused force kernel (64, 96 or 128)."""
+        self._call("af3d_set_force_block", int(block))
+
+    def force_block(self) -> int:
+        b = C.c_int()
+        self._call("af3d_get_force_block", C.byref(b))
+        return b.value
+
+    def autotune_shapes(self, steps_per_trial: int = 256, timings: dict | None = None) -> tuple[int, int]:
+        """af3d_autotune_shapes: the permutation interval, then the force kernel's block, each the
+        fastest on real steps of the run; returns (interval, block).  `timings` receives
+        {"interval": {every: ms}, "block": {block: ms}}."""
+        r, b = C.c_long(), C.c_int()
+        mi, mb = np.zeros(len(self.RESORT_CHOICES)), np.zeros(len(self.FORCE_BLOCKS))
+        self._call("af3d_autotune_shapes", int(steps_per_trial), C.byref(r), C.byref(b), ptr(mi), ptr(mb))
+        if timings is not None:
+            timings["interval"] = dict(zip(self.RESORT_CHOICES, mi.tolist()))
+            timings["block"] = dict(zip(self.FORCE_BLOCKS, mb.tolist()))
+        return r.value, b.value
+
     def save_checkpoint(self, path: str) -> None:
         """af3d_save_checkpoint: the whole context state, losslessly, to `path`."""
         self._call("af3d_save_checkpoint", str(path).encode())

@@ -64,6 +64,8 @@ def parse_args():
     p.add_argument("--cpu-sample", type=int, default=16384, help="clumps in the CPU baseline sample")
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-autotune", dest="autotune", action="store_false",
+                   help="skip the autotuner (the timed context keeps the default shapes)")
     p.add_argument("--no-configs", action="store_true",
                    help="skip the extra configurations (2,048-clump flume, 524,288-clump funnel and hopper)")
     p.add_argument("--fp-mode", choices=["exact", "fast"], default="fast",
@@ -351,6 +353,11 @@ def measure_ensemble(args, stream):
     eng.import_particles(pp)
     eng.forces()
     eng.swap_accel()
+    tuned = None
+    if args.autotune:
+        timings = {}
+        every, block = eng.autotune_shapes(64, timings)
+        tuned = {"resort_every": every, "force_block": block, "ms_per_step": timings}
     eng.step(warm)
     eng.contact_count()
     t_ens = timed(eng)
@@ -388,6 +395,7 @@ def measure_ensemble(args, stream):
                                  "what": "every %d-th flume alone in a plain context, one after another"
                                          % stride},
             "speedup_vs_sequential": value / seq,
+            "tuned": tuned,
             "kernel_ms_per_step": float(prof.sum()),
             "launch_overhead_ms_per_step": 1e3 * t_ens / K - float(prof.sum()),
             "launch_note": "graph-replayed step time minus the summed kernel-group times of profiled steps: "
@@ -506,6 +514,7 @@ def measure_config(name, cfg, steps, warmup, mode, stream, cpu_seconds=0.0):
         ms = e0.elapsed_time(e1)
         contacts = eng.contact_count()
         ncell3 = int(eng.get_grid()["ncell3"])
+        block = eng.force_block()
         names = ["time_advance", "predict_keys", "cell_sort", "permute_records", "fused_forces", "regrid"]
         prof = np.zeros(len(names))
         nprof = max(2, min(10, steps))
@@ -517,7 +526,7 @@ def measure_config(name, cfg, steps, warmup, mode, stream, cpu_seconds=0.0):
     out = {"workload": name, "clumps": len(pp), "cells": ncell3, "steps": steps, "warmup": warmup,
            "value": len(pp) * steps / (ms / 1e3), "unit": "clump-steps/s", "ms_per_step": ms / steps,
            "contacts_per_step": contacts / steps, "contacts_per_s": contacts / (ms / 1e3),
-           "phase_ms": {k: float(v) for k, v in zip(names, prof)},
+           "force_block": block, "phase_ms": {k: float(v) for k, v in zip(names, prof)},
            "roofline": {"kernel": "k_lists_forces", "algorithmic_bytes_per_launch": alg,
                         "achieved": alg / t_forces / 1e9 if t_forces > 0 else None, "unit": "GB/s",
                         "peak": peaks.get("hbm_gbs"), "peak_source": peak_kind,
@@ -590,13 +599,24 @@ def run_engine(args):
     # sampling period.  The load window runs on its own context, so the timed steps start from
     # the same state whatever the speed of the code.
     clocks = ClockSampler(local)
-    if args.clock_window > 0:
+    tuned = None
+    if args.clock_window > 0 or args.autotune:
         with make_engine() as warm:
             t_end = time.perf_counter() + args.clock_window
+            if args.autotune:
+                # the project's autotuner on a context of its own (untimed): the permutation
+                # interval, then the force kernel's block, each the fastest on real steps
+                timings = {}
+                every, block = warm.autotune_shapes(64, timings)
+                tuned = {"resort_every": every, "force_block": block, "ms_per_step": timings,
+                         "what": "af3d_autotune_shapes on the workload's own steps before the timed run"}
             while time.perf_counter() < t_end:
                 warm.step(64)
                 torch.cuda.synchronize()
     eng = make_engine(trace_preroll=True)
+    if tuned:
+        eng.set_resort_every(tuned["resort_every"])
+        eng.set_force_block(tuned["force_block"])
     eng.step(args.warmup)
     eng.prepare_steps(args.steps)   # capture the timed steps' graphs now (nothing runs)
     grid = eng.get_grid()
@@ -618,6 +638,7 @@ def run_engine(args):
     barrier()
     ms = e0.elapsed_time(e1)
     clk = clocks.stop()
+    eng_block = eng.force_block()
     contacts = eng.contact_count()
     launches1 = C.c_long()
     lib().af3d_kernel_launches(eng._h, C.byref(launches1))
@@ -734,6 +755,8 @@ def run_engine(args):
                          "kernel_ms": prof[names.index("fused_forces")], "note": "FP64-issue bound; see fp64"},
             "fp64": fp64_line(fp64.value, t_forces, args.fp_mode),
             "phase_ms": {k: float(v) for k, v in zip(names, prof)},
+            "tuned": tuned,
+            "force_block": eng_block,
             "configs": configs or None,
             "ensemble": ens,
             "adjoint": adj,
