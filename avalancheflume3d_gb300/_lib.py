@@ -110,6 +110,7 @@ SIGNATURES = [
     ("af3d_step_profile", [_P, C.c_long, _P], C.c_int),
     ("af3d_kernel_launches", [_P, _P], C.c_int),
     ("af3d_fp64_peak", [_P], C.c_int),
+    ("af3d_check_fp64_bits", [_P, C.c_long, _P], C.c_int),
     ("af3d_get_forces", [_P, _P, _P], C.c_int),
     ("af3d_get_accels", [_P, _P, _P], C.c_int),
     ("af3d_get_cells", [_P, _P, _P, _P], C.c_int),

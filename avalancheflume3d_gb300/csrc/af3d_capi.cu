@@ -1439,6 +1439,12 @@ af3d_status af3d_kernel_launches(af3d_ctx *c, long *count) {
   return AF3D_OK;
 }
 
+af3d_status af3d_check_fp64_bits(const double *x, long n, int *bad) {
+  if (n < 0 || (n > 0 && (!x || !bad))) return fail(AF3D_ERR_ARG, "bad argument");
+  AF3D_CUDA(check_fp64_bits(x, n, bad));
+  return AF3D_OK;
+}
+
 af3d_status af3d_fp64_peak(double *tflops) {
   if (!tflops) return fail(AF3D_ERR_ARG, "null argument");
   int dev = 0, sms = 0;

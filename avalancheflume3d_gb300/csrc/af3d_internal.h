@@ -252,6 +252,8 @@ void launch_cells_by_id (const Launch &L, const int *key, const long long *id, D
                          long long *cell_of_id);
 // DFMA throughput microbenchmark (TFLOP/s, 2 flops per DFMA), bounded to ~0.1 s.
 cudaError_t measure_dfma (int sms, double *tflops);
+// Per element of x, a bit for each integer-pipe FP64 helper that disagrees with the hardware.
+cudaError_t check_fp64_bits (const double *x, long n, int *bad);
 
 // Adjoint of the exact step (af3d_adjoint.cu).  Planes of 24 state adjoints (r, v, w, R rows,
 // a_i, alpha_i), 21 scattered parts (r1, v1, w1, sphere centres), 9 own R1 parts.

@@ -119,7 +119,7 @@ __global__ void k_planes_to_aos(Planes P, const long long *__restrict__ id, cons
 
 // ------------------------------------------------------------------ neighbour records
 
-__device__ __forceinline__ float f_up(double x) { return __double2float_ru(x); }
+__device__ __forceinline__ float f_up(double x) { return to_float_ru(x); }
 
 // Packed FP64 neighbour record and conservative FP32 culling record of one clump.
 // The culling bounds are formed in FP32 from the FP32-rounded coordinates.  M32 = max |coordinate|
@@ -139,12 +139,12 @@ __device__ __forceinline__ void make_records(V3 r, V3 v, V3 w, const V3 *sp, dou
     q.s[3 * k] = sp[k].x; q.s[3 * k + 1] = sp[k].y; q.s[3 * k + 2] = sp[k].z;
   }
   q.rad = rad; q.msph = msph; q.mwall = mwall;
-  const float cx = (float)r.x, cy = (float)r.y, cz = (float)r.z;
+  const float cx = to_float_rn(r.x), cy = to_float_rn(r.y), cz = to_float_rn(r.z);
   float M = fmaxf(fmaxf(fabsf(cx), fabsf(cy)), fabsf(cz));
   float ext = 0.0f;
   float4 sf[4];
   for (int k = 0; k < 4; k++) {
-    sf[k] = make_float4((float)sp[k].x, (float)sp[k].y, (float)sp[k].z, 0.0f);
+    sf[k] = make_float4(to_float_rn(sp[k].x), to_float_rn(sp[k].y), to_float_rn(sp[k].z), 0.0f);
     M = fmaxf(M, fmaxf(fmaxf(fabsf(sf[k].x), fabsf(sf[k].y)), fabsf(sf[k].z)));
     const float dx = sf[k].x - cx, dy = sf[k].y - cy, dz = sf[k].z - cz;
     ext = fmaxf(ext, sqrtf(__fmaf_rn(dz, dz, __fmaf_rn(dy, dy, dx * dx))));
@@ -192,7 +192,7 @@ __device__ __forceinline__ void store_records(bool valid, long base, long n, con
 
 // Cell coordinate of cells.cu:69-77 (multiplication by cs_inv, then `== ncell -> ncell-1`).
 __device__ __forceinline__ long bin_axis(double x, double xmin, double inv, long n) {
-  long i = (long)(inv * (x - xmin));
+  long i = (long)trunc_to_ll(inv * (x - xmin));
   if (i == n) i--;
   return i;
 }
@@ -213,7 +213,7 @@ __device__ __forceinline__ void predict_state(V3 &r, V3 &v, V3 &w, V3 a, V3 al, 
   const double mag2 = dO.x * dO.x + dO.y * dO.y + dO.z * dO.z;
   double mag, imag = 0.0;
   V3 dRx, dRy, dRz;
-  if (kFast && mag2 > 0.0 && mag2 < kSmallAngle2) {
+  if (kFast && in_open_range_bits(mag2, 0.0, kSmallAngle2)) {
     // Fast mode, |dO| < 2^-5: the Rodrigues matrix c I + (sin/|dO|) [dO]x + ((1-c)/|dO|^2) dO dO^T
     // from the Maclaurin series of sin(t)/t and (1 - cos t)/t^2 in t^2 = |dO|^2 (truncated
     // after t^8 and t^10: the first omitted terms are below 2^-53 of the sums), no square
@@ -269,7 +269,10 @@ __device__ __forceinline__ void predict_state(V3 &r, V3 &v, V3 &w, V3 a, V3 al, 
   if (kFast) {
     // 1/sqrt(n2) for a column norm n2 within 2^-26 of 1 (a rotation times a rotation):
     // one Newton step from 1, 1.5 - n2/2, whose error 3/8 (n2 - 1)^2 is below 2^-54.
-    auto inv_norm = [](double n2) { return fabs(n2 - 1.0) < 1.4901161193847656e-08 ? 1.5 - 0.5 * n2 : rsqrt(n2); };
+    auto inv_norm = [](double n2) {   // |n2 - 1| < 2^-26, tested on the bits
+      return in_open_range_bits(n2, 1.0 - 1.4901161193847656e-08, 1.0 + 1.4901161193847656e-08) ? 1.5 - 0.5 * n2
+                                                                                                 : rsqrt(n2);
+    };
     double in = inv_norm(Tx.x * Tx.x + Ty.x * Ty.x + Tz.x * Tz.x);
     Rx.x = Tx.x * in; Ry.x = Ty.x * in; Rz.x = Tz.x * in;
     in = inv_norm(Tx.y * Tx.y + Ty.y * Ty.y + Tz.y * Tz.y);
@@ -317,7 +320,7 @@ __device__ __forceinline__ void predict_state(V3 &r, V3 &v, V3 &w, V3 a, V3 al, 
 __device__ __forceinline__ long bucket_key(V3 r, const DevFlume &fl, DevScalars *d, long long id, double t) {
   const af3d_cell_par &g = fl.grid;
   if (is_removed(t, r.x, fl.sys.side.x)) return d->ncell_total + id;
-  if (!(isfinite(r.x) && isfinite(r.y) && isfinite(r.z))) {
+  if (!(finite_bits(r.x) && finite_bits(r.y) && finite_bits(r.z))) {
     raise_status(d, AF3D_ERR_NAN);
     return d->ncell_total + id;
   }
@@ -851,8 +854,8 @@ __device__ __forceinline__ void fused_body(const Consts &c, Planes P, Planes out
       // finish_Verlet.cu:43-48
       v2 = mk(v.x + c.hdt * (a.x - ai.x), v.y + c.hdt * (a.y - ai.y), v.z + c.hdt * (a.z - ai.z));
       w2 = mk(w.x + c.hdt * (al.x - ali.x), w.y + c.hdt * (al.y - ali.y), w.z + c.hdt * (al.z - ali.z));
-      if (!(isfinite(a.x) && isfinite(a.y) && isfinite(a.z) && isfinite(al.x) && isfinite(al.y) &&
-            isfinite(al.z)))
+      if (!(finite_bits(a.x) && finite_bits(a.y) && finite_bits(a.z) && finite_bits(al.x) && finite_bits(al.y) &&
+            finite_bits(al.z)))
         raise_status(d, AF3D_ERR_NAN);
     } else {
       v2 = mk(0.0, 0.0, 0.0);                 // finish_Verlet.cu:28-32

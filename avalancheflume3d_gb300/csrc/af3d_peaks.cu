@@ -5,6 +5,7 @@
 // measures that bound on the device at hand: 8 independent DFMA chains per thread, 8 resident
 // blocks per SM, a fixed iteration count (no data-dependent loop), one store per thread.
 #include "af3d_internal.h"
+#include "af3d_physics.cuh"
 
 namespace af3d {
 
@@ -45,6 +46,45 @@ cudaError_t measure_dfma(int sms, double *tflops) {
   cudaEventDestroy(t1);
   cudaFree(out);
   *tflops = ms > 0 ? 2.0 * 8.0 * kIters * (double)blocks * threads / (ms * 1e-3) / 1e12 : 0.0;
+  return e;
+}
+
+namespace {
+
+// The integer-pipe helpers of af3d_physics.cuh against the hardware instructions they replace:
+// per element, one bit per helper that disagreed.
+__global__ void k_check_bits(const double *x, int *bad, long n) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double v = x[i];
+  int b = 0;
+  if (__float_as_uint(to_float_rn(v)) != __float_as_uint((float)v)) b |= 1;
+  if (__float_as_uint(to_float_ru(v)) != __float_as_uint(__double2float_ru(v))) b |= 2;
+  if (isfinite(v) && fabs(v) < 9.2e18 && trunc_to_ll(v) != (long long)v) b |= 4;
+  if (finite_bits(v) != (bool)isfinite(v)) b |= 8;
+  if (nonzero_bits(v) != (v != 0.0)) b |= 16;
+  const double lo = 1.0 - 1.4901161193847656e-08, hi = 1.0 + 1.4901161193847656e-08;
+  if (!(v < 0.0) && in_open_range_bits(v, lo, hi) != (fabs(v - 1.0) < 1.4901161193847656e-08)) b |= 32;
+  if (!(v < 0.0) && in_open_range_bits(v, 0.0, 9.765625e-04) != (v > 0.0 && v < 9.765625e-04)) b |= 64;
+  bad[i] = b;
+}
+
+}  // namespace
+
+cudaError_t check_fp64_bits(const double *x, long n, int *bad) {
+  if (n <= 0) return cudaSuccess;
+  double *dx = nullptr;
+  int *db = nullptr;
+  cudaError_t e = cudaMalloc(&dx, sizeof(double) * n);
+  if (e == cudaSuccess) e = cudaMalloc(&db, sizeof(int) * n);
+  if (e == cudaSuccess) e = cudaMemcpy(dx, x, sizeof(double) * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    k_check_bits<<<(unsigned)((n + 255) / 256), 256>>>(dx, db, n);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(bad, db, sizeof(int) * n, cudaMemcpyDeviceToHost);
+  cudaFree(dx);
+  cudaFree(db);
   return e;
 }
 

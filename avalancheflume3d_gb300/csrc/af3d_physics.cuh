@@ -60,6 +60,65 @@ __device__ __forceinline__ V3 mk(double x, double y, double z) {
   return r;
 }
 
+// ---- FP64 tests and conversions on the integer pipe ----------------------------------------
+// The FP64 pipe of this GPU retires one warp instruction per ~19 SM cycles, and conversions and
+// comparisons of doubles occupy it like arithmetic does.  These helpers take the same decisions
+// and give the same bits as the hardware instructions they replace, from the operands' bit
+// patterns, on the integer pipe; values outside their fast range (zero, subnormal or huge
+// results, infinities, NaN) fall back to the hardware conversion.
+
+// isfinite(x): the exponent field is not all ones.
+__device__ __forceinline__ bool finite_bits(double x) {
+  return ((unsigned)(__double_as_longlong(x) >> 32) & 0x7FF00000u) != 0x7FF00000u;
+}
+
+// x != 0.0 (true for NaN, false for both zeros).
+__device__ __forceinline__ bool nonzero_bits(double x) {
+  return (__double_as_longlong(x) << 1) != 0;
+}
+
+// lo < x < hi for 0 <= lo < hi finite and x >= +0 or NaN (false for NaN, as the FP compare).
+__device__ __forceinline__ bool in_open_range_bits(double x, double lo, double hi) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned long long l = (unsigned long long)__double_as_longlong(lo);
+  return b - l - 1ull < (unsigned long long)__double_as_longlong(hi) - l - 1ull;
+}
+
+// (float)x, round to nearest even: the top 23 mantissa bits, rounded on the 29 below.
+__device__ __forceinline__ float to_float_rn(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+  const int e = (int)((hi >> 20) & 0x7FFu) - 896;   // the float's biased exponent
+  if (e <= 0 || e >= 255) return (float)x;
+  const unsigned m = ((hi & 0xFFFFFu) << 3) | (lo >> 29), rest = lo & 0x1FFFFFFFu;
+  unsigned f = (hi & 0x80000000u) | ((unsigned)e << 23) | m;
+  f += (rest > 0x10000000u) | ((rest == 0x10000000u) & (m & 1u));   // a carry into the exponent is right
+  return __uint_as_float(f);
+}
+
+// __double2float_ru(x), rounded toward +infinity.
+__device__ __forceinline__ float to_float_ru(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+  const int e = (int)((hi >> 20) & 0x7FFu) - 896;
+  if (e <= 0 || e >= 255) return __double2float_ru(x);
+  const unsigned m = ((hi & 0xFFFFFu) << 3) | (lo >> 29), rest = lo & 0x1FFFFFFFu;
+  unsigned f = (hi & 0x80000000u) | ((unsigned)e << 23) | m;
+  f += (rest != 0u) & !(hi >> 31);   // away from zero for positive x, toward zero for negative
+  return __uint_as_float(f);
+}
+
+// (long long)x, truncated toward zero.
+__device__ __forceinline__ long long trunc_to_ll(double x) {
+  const long long b = __double_as_longlong(x);
+  const int e = (int)((b >> 52) & 0x7FF) - 1023;
+  if (e < 0) return 0;                      // |x| < 1, zeros and subnormals included
+  if (e > 51) return (long long)x;          // integral already, or not finite
+  const unsigned long long m = ((unsigned long long)b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+  const long long i = (long long)(m >> (52 - e));
+  return b < 0 ? -i : i;
+}
+
 // The constants of flume f, loaded per thread (contexts with several flumes).
 __device__ __forceinline__ Consts load_consts(const DevScalars *d, int f) {
   const DevFlume &fl = d->flumes[f];
@@ -101,9 +160,9 @@ __device__ __forceinline__ bool contact_law_fast(V3 dvvc, V3 n, double comp, dou
       f.z += a * vt.z;
     } else {
       const double q = fsdt * inv_vt;
-      if (vt.x != 0.0) f.x += q * vt.x;
-      if (vt.y != 0.0) f.y += q * vt.y;
-      if (vt.z != 0.0) f.z += q * vt.z;
+      if (nonzero_bits(vt.x)) f.x += q * vt.x;
+      if (nonzero_bits(vt.y)) f.y += q * vt.y;
+      if (nonzero_bits(vt.z)) f.z += q * vt.z;
     }
   }
   return true;
@@ -148,9 +207,9 @@ __device__ __forceinline__ bool contact_law(V3 dvvc, V3 n, double comp, double k
       f.y += af * vt.y;
       f.z += af * vt.z;
     } else {
-      if (vt.x != 0.0) f.x += q1;
-      if (vt.y != 0.0) f.y += q2;
-      if (vt.z != 0.0) f.z += q3;
+      if (nonzero_bits(vt.x)) f.x += q1;
+      if (nonzero_bits(vt.y)) f.y += q2;
+      if (nonzero_bits(vt.z)) f.z += q3;
     }
   }
   return true;

@@ -208,6 +208,11 @@ af3d_status af3d_kernel_launches (af3d_ctx *ctx, long *count);
 /* Measured FP64 fused-multiply-add throughput of the current device in TFLOP/s (2 flops per
    DFMA), from a bounded ~0.1 s microbenchmark: the denominator of the FP64 roofline. */
 af3d_status af3d_fp64_peak (double *tflops);
+/* Self-check of the kernels' integer-pipe FP64 helpers (no counterpart in the reference): the
+   conversions to float (to nearest, toward +infinity) and to a 64-bit integer, and the
+   finiteness, non-zero and range tests the kernels take from the bit patterns, against the
+   hardware instructions, for each x[i]; bad[i] gets one bit per helper that disagreed. */
+af3d_status af3d_check_fp64_bits (const double *x, long n, int *bad);
 
 /* ---- adjoint (no counterpart in the reference) --------------------------------------------
    Runs, from the imported state (a_i = alpha_i = 0), the start-up force pass and `steps` exact

@@ -173,3 +173,34 @@ def test_fast_rotation_over_the_angle_range(af3d, oracle):
     for f in ("Rmatx", "Rmaty", "Rmatz"):
         assert float(np.max(np.abs(got[f] - want[f]))) <= 1e-14, f
     assert float(np.max(np.abs(got["rr_s"] - want["rr_s"]))) <= 1e-14 * max(1.0, float(np.abs(want["rr_s"]).max()))
+
+
+def test_integer_pipe_fp64_helpers(af3d):
+    """The kernels convert and test doubles on the integer pipe (the FP64 pipe is the force
+    kernel's bottleneck): conversions to float to nearest and toward +infinity, truncation to a
+    64-bit integer, and the finiteness, non-zero and open-range tests must give the hardware's
+    bits on every input: random bit patterns over the whole exponent range, rounding ties and
+    their neighbours, float-range edges, zeros, subnormals, infinities and NaN."""
+    import ctypes as C
+    rng = np.random.default_rng(97)
+    bits = rng.integers(0, 2 ** 63, 200000, dtype=np.int64).view(np.uint64)
+    bits[::2] |= np.uint64(1 << 63)
+    x = bits.view(np.float64)
+    mags = (rng.random(200000) * 2 - 1) * 10.0 ** rng.integers(-45, 40, 200000)
+    # ties of the float rounding: 29 low mantissa bits exactly half, and one unit either side
+    base = (rng.random(20000) + 1.0) * 2.0 ** rng.integers(-120, 120, 20000)
+    b = base.view(np.uint64) & ~np.uint64(0x1FFFFFFF)
+    ties = np.concatenate([(b | np.uint64(0x10000000)), (b | np.uint64(0x0FFFFFFF)),
+                           (b | np.uint64(0x10000001)), b]).view(np.float64)
+    f32 = np.float32
+    edges = np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 5e-324, -5e-324, 2.2250738585072014e-308,
+                      float(np.finfo(f32).max), -float(np.finfo(f32).max), float(np.finfo(f32).tiny),
+                      float(np.finfo(f32).tiny) / 2, 3.4028235677973366e38, 3.4028235677973362e38,
+                      1e39, 1.0, 1.0 - 2 ** -26, 1.0 + 2 ** -26, 1.0 - 2 ** -27, 1.0 + 2 ** -27,
+                      9.765625e-04, np.nextafter(9.765625e-04, 0), 0.5, 2.0 ** 52, 2.0 ** 52 + 0.5,
+                      2.0 ** 63, -2.0 ** 62, 123456789.99999, -0.999999])
+    x = np.ascontiguousarray(np.concatenate([x, mags, ties, edges]))
+    bad = np.zeros(len(x), dtype=np.int32)
+    assert af3d.lib().af3d_check_fp64_bits(x.ctypes.data_as(C.c_void_p), len(x),
+                                            bad.ctypes.data_as(C.c_void_p)) == 0
+    assert not bad.any(), [(float(x[i]), int(bad[i])) for i in np.nonzero(bad)[0][:10]]
