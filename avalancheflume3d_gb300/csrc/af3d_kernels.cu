@@ -163,18 +163,19 @@ constexpr int kPermBlock = 128;
 constexpr int kRecWords = (int)(sizeof(NbrRec) / 8);   // 24
 constexpr int kRecStride = kRecWords + 1;
 
-// The block's records, staged in shared memory and written out as contiguous 16-byte stores.
-// Every thread of a kPermBlock-thread block calls this (slots past n contribute nothing).
-template <int NB>
-__device__ __forceinline__ void store_records(bool valid, long base, long n, const NbrRec &q, const CullRec &cr,
-                                              NbrRec *nbr, CullRec *cull, double *s_nbr, CullRec *s_cull) {
-  if (valid) {
-    const double *qw = reinterpret_cast<const double *>(&q);
+// One thread's records into the block's shared-memory staging.
+__device__ __forceinline__ void stage_record(const NbrRec &q, const CullRec &cr, double *s_nbr, CullRec *s_cull) {
+  const double *qw = reinterpret_cast<const double *>(&q);
 #pragma unroll
-    for (int k = 0; k < kRecWords; k++) s_nbr[threadIdx.x * kRecStride + k] = qw[k];
-    s_cull[threadIdx.x] = cr;
-  }
-  __syncthreads();
+  for (int k = 0; k < kRecWords; k++) s_nbr[threadIdx.x * kRecStride + k] = qw[k];
+  s_cull[threadIdx.x] = cr;
+}
+
+// The block's staged records written out as contiguous 16-byte stores (after a barrier that
+// follows the staging).
+template <int NB>
+__device__ __forceinline__ void copy_records(long base, long n, NbrRec *nbr, CullRec *cull, const double *s_nbr,
+                                             const CullRec *s_cull) {
   const long cnt = n - base < NB ? n - base : NB;
   const int nw = (int)(cnt * kRecWords) / 2;   // double2 words of the block's records
   double2 *b = reinterpret_cast<double2 *>(nbr + base);
@@ -186,6 +187,16 @@ __device__ __forceinline__ void store_records(bool valid, long base, long n, con
   const float4 *c = reinterpret_cast<const float4 *>(s_cull);
   float4 *e = reinterpret_cast<float4 *>(cull + base);
   for (int i = threadIdx.x; i < m16; i += NB) e[i] = c[i];
+}
+
+// The block's records, staged in shared memory and written out as contiguous 16-byte stores.
+// Every thread of an NB-thread block calls this (slots past n contribute nothing).
+template <int NB>
+__device__ __forceinline__ void store_records(bool valid, long base, long n, const NbrRec &q, const CullRec &cr,
+                                              NbrRec *nbr, CullRec *cull, double *s_nbr, CullRec *s_cull) {
+  if (valid) stage_record(q, cr, s_nbr, s_cull);
+  __syncthreads();
+  copy_records<NB>(base, n, nbr, cull, s_nbr, s_cull);
 }
 
 // ------------------------------------------------------------------ init_Verlet (+ cell keys)
@@ -602,14 +613,61 @@ __device__ __forceinline__ void block_prefix3(BlockQueue<NB> &bq, int a, int b, 
   __syncthreads();
 }
 
+__device__ __forceinline__ Own own_from_record(const NbrRec &q) {
+  Own o;
+  o.r = mk(q.rx, q.ry, q.rz);
+  o.v = mk(q.vx, q.vy, q.vz);
+  o.w = mk(q.wx, q.wy, q.wz);
+  for (int k = 0; k < 4; k++) o.s[k] = mk(q.s[3 * k], q.s[3 * k + 1], q.s[3 * k + 2]);
+  o.rad = q.rad;
+  o.msph = q.msph;
+  o.mwall = q.mwall;
+  return o;
+}
+
+__device__ __forceinline__ Own own_from_planes(const Planes &P, long s) {
+  Own o;
+  o.r = load3(P, RX, s);
+  o.v = load3(P, VX, s);
+  o.w = load3(P, WX, s);
+  for (int k = 0; k < 4; k++) o.s[k] = load3(P, S0X + 3 * k, s);
+  o.rad = P.p[RAD][s];
+  o.msph = P.p[MSPH][s];
+  o.mwall = P.p[MWALL][s];
+  return o;
+}
+
+// The contacts of a clump whose item lists overflowed, by the per-clump cell walk, added to
+// (F, T) in the reference's order: the boundary routines before the particles, the sixteen
+// sph_id passes, the routines after.  Not inlined: it runs rarely, and inlined its registers
+// and spills would weigh on the pooled path of every clump.  The clump's state, bound and
+// grid are read here again.
+struct SlowSums {
+  V3 F, T;
+  int active;
+};
+__device__ __noinline__ SlowSums slow_contacts(long s, int pre0, int pre1, int post0, int post1, const Consts &c,
+                                               const DevScalars *d, const int *__restrict__ flume,
+                                               const NbrRec *__restrict__ nbr, const CullRec *__restrict__ cull,
+                                               const int *__restrict__ start, const int *__restrict__ order, V3 F,
+                                               V3 T) {
+  const Own o = own_from_record(nbr[s]);
+  const double B = (double)cull[s].c.w;
+  const DevFlume &fl = d->flumes[flume[s]];
+  for (int rt = pre0; rt <= pre1; rt++)
+    if (bnd_may_touch(rt, o.r, B, c)) bnd_routine(rt, o, false, c, F, T);
+  const int active = contacts_by_pass(s, o, c, fl.grid, fl.cell_off, nbr, cull, start, order, 0xffffu, F, T);
+  for (int rt = post0; rt <= post1; rt++)
+    if (bnd_may_touch(rt, o.r, B, c)) bnd_routine(rt, o, false, c, F, T);
+  return SlowSums{F, T, active};
+}
+
 // UNIFORM: every clump of the launch belongs to one flume, whose constants `c` are (a
 // reference to) a kernel parameter.  lc: the clump's list layout (pre boundary items, particle
 // items, the rest boundary items).
 template <int NB, bool UNIFORM>
 __device__ __forceinline__ int block_contacts(BlockQueue<NB> &bq, long bbase, long s, bool act, bool aval,
-                                              double B, const Own &o, const Consts &c,
-                                              const af3d_cell_par &g, long long off,
-                                              const DevScalars *d, const int *__restrict__ flume,
+                                              const Consts &c, const DevScalars *d, const int *__restrict__ flume,
                                               const NbrRec *__restrict__ nbr,
                                               const CullRec *__restrict__ cull,
                                               const int *__restrict__ start,
@@ -718,37 +776,12 @@ __device__ __forceinline__ int block_contacts(BlockQueue<NB> &bq, long bbase, lo
     __syncthreads();
   }
   if (slow) {
-    for (int rt = pre0; rt <= pre1; rt++)
-      if (bnd_may_touch(rt, o.r, B, c)) bnd_routine(rt, o, false, c, F, T);
-    active += contacts_by_pass(s, o, c, g, off, nbr, cull, start, order, 0xffffu, F, T);
-    for (int rt = post0; rt <= post1; rt++)
-      if (bnd_may_touch(rt, o.r, B, c)) bnd_routine(rt, o, false, c, F, T);
+    const SlowSums r = slow_contacts(s, pre0, pre1, post0, post1, c, d, flume, nbr, cull, start, order, F, T);
+    F = r.F;
+    T = r.T;
+    active += r.active;
   }
   return active;
-}
-
-__device__ __forceinline__ Own own_from_record(const NbrRec &q) {
-  Own o;
-  o.r = mk(q.rx, q.ry, q.rz);
-  o.v = mk(q.vx, q.vy, q.vz);
-  o.w = mk(q.wx, q.wy, q.wz);
-  for (int k = 0; k < 4; k++) o.s[k] = mk(q.s[3 * k], q.s[3 * k + 1], q.s[3 * k + 2]);
-  o.rad = q.rad;
-  o.msph = q.msph;
-  o.mwall = q.mwall;
-  return o;
-}
-
-__device__ __forceinline__ Own own_from_planes(const Planes &P, long s) {
-  Own o;
-  o.r = load3(P, RX, s);
-  o.v = load3(P, VX, s);
-  o.w = load3(P, WX, s);
-  for (int k = 0; k < 4; k++) o.s[k] = load3(P, S0X + 3 * k, s);
-  o.rad = P.p[RAD][s];
-  o.msph = P.p[MSPH][s];
-  o.mwall = P.p[MWALL][s];
-  return o;
 }
 
 __device__ __forceinline__ void warp_count(DevScalars *d, int active) {
@@ -806,22 +839,20 @@ __device__ __forceinline__ void fused_body(const Consts &c, Planes P, Planes out
   const bool valid = s < n;
   const long sv = valid ? s : n - 1;   // in-range slot for lanes past n (nothing is written for them)
   const int f = flume[sv];
-  const af3d_cell_par g = d->flumes[f].grid;
-  const long long off = d->flumes[f].cell_off;
-  const Own o = own_from_record(nbr[sv]);
-  const bool removed = is_removed(*c.tp, o.r.x, c.side_x);
-  const double B = (double)cull[sv].c.w;   // sphere offsets + radius, rounded up
+  const bool removed = is_removed(*c.tp, nbr[sv].rx, c.side_x);
   V3 F = mk(0.0, 0.0, 0.0), T = mk(0.0, 0.0, 0.0);
   const bool aval = c.phase == AF3D_PHASE_AVALANCHE;
   // Removed clumps get hop, funnel and fcorners only (walls, part and flume skip them).
-  if (valid && removed && aval)
+  if (valid && removed && aval) {
+    const Own o = own_from_record(nbr[sv]);
+    const double B = (double)cull[sv].c.w;   // sphere offsets + radius, rounded up
     for (int rt = R_HOP0; rt <= R_FCORNERS; rt++)
       if (bnd_may_touch(rt, o.r, B, c)) bnd_routine(rt, o, true, c, F, T);
+  }
   const long bbase = s0 + blockIdx.x * (long)blockDim.x;
-  const int active = block_contacts<NB, UNIFORM>(sh.bq, bbase, sv, valid && !removed, aval, B, o, c, g, off, d, flume,
-                                             nbr, cull, start, order, lists.items, valid ? listed : 0, lc, n, F, T);
-  NbrRec q;
-  CullRec cr;
+  const int active = block_contacts<NB, UNIFORM>(sh.bq, bbase, sv, valid && !removed, aval, c, d, flume, nbr, cull,
+                                                 start, order, lists.items, valid ? listed : 0, lc, n, F, T);
+  if (la.nbr) __syncthreads();   // the force phase's shared memory is free for the record staging
   if (valid) {
     if (lists.cnt) lists.cnt[s] = pack_list_counts(listed, lc.pre, lc.pair);
     if (lists.ovf && listed < 0) *lists.ovf = 1;
@@ -885,7 +916,12 @@ __device__ __forceinline__ void fused_body(const Consts &c, Planes P, Planes out
         store3(P, RN10, s, Ry);
         store3(P, RN20, s, Rz);
       }
-      make_records(rn, vn, wn, sp, P.p[RAD][s], P.p[MSPH][s], P.p[MWALL][s], q, cr);
+      {
+        NbrRec q;
+        CullRec cr;
+        make_records(rn, vn, wn, sp, P.p[RAD][s], P.p[MSPH][s], P.p[MWALL][s], q, cr);
+        stage_record(q, cr, sh.rec.nbr, sh.rec.cull);
+      }
       const long key = bucket_key(rn, fl, d, la.id[s], t_next);
       la.cells.key[s] = (int)key;
       la.cells.rank_tmp[s] = atomicAdd(&la.cells.count[key], 1);
@@ -893,8 +929,8 @@ __device__ __forceinline__ void fused_body(const Consts &c, Planes P, Planes out
   }
   warp_count(d, active);
   if (la.nbr) {
-    __syncthreads();   // the force phase's shared memory is free again
-    store_records<NB>(valid, bbase, n, q, cr, la.nbr, la.cull, sh.rec.nbr, sh.rec.cull);
+    __syncthreads();   // every record of the block is staged
+    copy_records<NB>(bbase, n, la.nbr, la.cull, sh.rec.nbr, sh.rec.cull);
   }
 }
 
