@@ -662,6 +662,14 @@ __device__ __noinline__ SlowSums slow_contacts(long s, int pre0, int pre1, int p
   return SlowSums{F, T, active};
 }
 
+// A boundary item's contact, prepared for the law.  Not inlined: the seven routines' input code
+// inlined into the pooled item loop raised its register pressure enough to spill on every
+// clump's path (636 bytes of spill stores against 212), while boundary items are a minority of
+// the items.
+__device__ __noinline__ bool bnd_input_call(int rt, const Sph &q, const Consts &co, ContactIn &ci) {
+  return bnd_input(rt, q, co, ci);
+}
+
 // UNIFORM: every clump of the launch belongs to one flume, whose constants `c` are (a
 // reference to) a kernel parameter.  lc: the clump's list layout (pre boundary items, particle
 // items, the rest boundary items).
@@ -702,7 +710,7 @@ __device__ __forceinline__ int block_contacts(BlockQueue<NB> &bq, long bbase, lo
         q.s = mk(me.s[3 * ns], me.s[3 * ns + 1], me.s[3 * ns + 2]);
         q.rad = me.rad;
         q.mwall = me.mwall;
-        kind = bnd_input(rt, q, co, ci) ? 2 : 0;
+        kind = bnd_input_call(rt, q, co, ci) ? 2 : 0;
       } else {
         const int t = (int)(it >> 4), p = (int)(it & 15u);
         const V3 vl = mk(me.vx, me.vy, me.vz), wl = mk(me.wx, me.wy, me.wz);
