@@ -231,10 +231,17 @@ __device__ __forceinline__ void predict_state(V3 &r, V3 &v, V3 &w, V3 a, V3 al, 
     // root, sine or cosine.
     // Horner form in t2 with the series' coefficients (1/6, 1/120, 1/5040, 1/362880 and
     // 1/2, 1/24, 1/720, 1/40320, 1/3628800): four multiply-adds each.
+    // Below |dO| = 2^-10 (t2 < 2^-20, the usual case) the series end after t^4: the first
+    // omitted terms, t^6 / 5040 and t^6 / 40320, are below 2^-72.
     const double t2 = mag2;
-    const double A = 1.0 + t2 * (-1.0 / 6.0 + t2 * (1.0 / 120.0 + t2 * (-1.0 / 5040.0 + t2 * (1.0 / 362880.0))));
-    const double Bq =
-        0.5 + t2 * (-1.0 / 24.0 + t2 * (1.0 / 720.0 + t2 * (-1.0 / 40320.0 + t2 * (1.0 / 3628800.0))));
+    double A, Bq;
+    if (in_open_range_bits(t2, 0.0, 9.5367431640625e-07)) {
+      A = 1.0 + t2 * (-1.0 / 6.0 + t2 * (1.0 / 120.0));
+      Bq = 0.5 + t2 * (-1.0 / 24.0 + t2 * (1.0 / 720.0));
+    } else {
+      A = 1.0 + t2 * (-1.0 / 6.0 + t2 * (1.0 / 120.0 + t2 * (-1.0 / 5040.0 + t2 * (1.0 / 362880.0))));
+      Bq = 0.5 + t2 * (-1.0 / 24.0 + t2 * (1.0 / 720.0 + t2 * (-1.0 / 40320.0 + t2 * (1.0 / 3628800.0))));
+    }
     const double cc = 1.0 - t2 * Bq;
     const V3 sv = mk(A * dO.x, A * dO.y, A * dO.z);
     const V3 bv = mk(Bq * dO.x, Bq * dO.y, Bq * dO.z);
@@ -304,14 +311,15 @@ __device__ __forceinline__ void predict_state(V3 &r, V3 &v, V3 &w, V3 a, V3 al, 
   // sphere centres r + (radius/sqrt2) R (+-1,+-1,+-1) (init_Verlet.cu:130-142)
   const double pos = kFast ? rad * (1.0 / kROOT2) : rad / kROOT2;
   if (kFast) {
-    // the four patterns from two shared sums per row: (a + c, b - c, c - a, -(b + c)) with
-    // a = x + y, b = x - y
+    // the four patterns (a + c, b - c, c - a, -(b + c)) with a = x + y, b = x - y, from the
+    // two partial sums r0 + pos c and r0 - pos c: eight operations per row
     auto row = [&](double r0, const V3 &R, double &s0, double &s1, double &s2, double &s3) {
       const double a = R.x + R.y, b = R.x - R.y;
-      s0 = r0 + pos * (a + R.z);
-      s1 = r0 + pos * (b - R.z);
-      s2 = r0 + pos * (R.z - a);
-      s3 = r0 - pos * (b + R.z);
+      const double up = r0 + pos * R.z, dn = r0 - pos * R.z;
+      s0 = up + pos * a;
+      s2 = up - pos * a;
+      s1 = dn + pos * b;
+      s3 = dn - pos * b;
     };
     row(r.x, Rx, sp[0].x, sp[1].x, sp[2].x, sp[3].x);
     row(r.y, Ry, sp[0].y, sp[1].y, sp[2].y, sp[3].y);
