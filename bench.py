@@ -66,6 +66,9 @@ def parse_args():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-autotune", dest="autotune", action="store_false",
                    help="skip the autotuner (the timed context keeps the default shapes)")
+    p.add_argument("--force-block", type=int, default=0,
+                   help="force kernel block of the timed context (64, 96, 128; 0: the default or the "
+                        "autotuner's choice)")
     p.add_argument("--no-configs", action="store_true",
                    help="skip the extra configurations (2,048-clump flume, 524,288-clump funnel and hopper)")
     p.add_argument("--fp-mode", choices=["exact", "fast"], default="fast",
@@ -617,6 +620,8 @@ def run_engine(args):
     if tuned:
         eng.set_resort_every(tuned["resort_every"])
         eng.set_force_block(tuned["force_block"])
+    if args.force_block:
+        eng.set_force_block(args.force_block)
     eng.step(args.warmup)
     eng.prepare_steps(args.steps)   # capture the timed steps' graphs now (nothing runs)
     grid = eng.get_grid()
