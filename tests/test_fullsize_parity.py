@@ -20,7 +20,7 @@ Bars, as for the small states (force_part.cu:11-266, cells.cu:40-111, avalanche_
   * fast FP64 mode, the timed state: F, T, a and alpha within 1e-10 relative per clump (a clump
     whose net force nearly cancels is measured against 1e-6 of the largest norm instead);
     contact-pair sets identical to the exact mode's;
-  * 20 fused steps from the timed state (af3d_step, with the device re-grid after the first) in
+  * 100 fused steps from the timed state (af3d_step, with the device re-grid after the first) in
     either mode: every position, velocity, spin, rotation row and sphere centre within 1e-8
     relative.
 """
@@ -35,7 +35,7 @@ pytestmark = pytest.mark.gpu
 
 FORCE_RTOL = 1e-10
 TRAJ_RTOL = 1e-8
-STEPS = 20
+STEPS = 100
 WARMUP = 5
 
 
