@@ -79,6 +79,7 @@ struct Consts {
   double sinfi, cosfi, tanfi;
   double tant;     // sint / cost
   double inv_dt;   // 1 / dt (fast mode)
+  double qk_pp, qg_pp, hk_pw, hg_pw;   // kappa_pp / 4, gamma_pp / 4, kappa_pw / 2, gamma_pw / 2 (fast mode)
   const double *tp;   // the device clock, DevScalars::time
   float cost_f, sint_f, tanfi_f, cosfi_f, dy2_f, side_y_f;   // FP32 copies for the culling gates
   int phase, variant;
@@ -95,6 +96,8 @@ __host__ __device__ inline Consts make_consts(const af3d_system_par &s, const af
   c.sinfi = fun.sinfi; c.cosfi = fun.cosfi; c.tanfi = fun.tanfi;
   c.tant = tant;
   c.inv_dt = 1.0 / s.dt;
+  c.qk_pp = 0.25 * s.kappa_pp; c.qg_pp = 0.25 * s.gamma_pp;
+  c.hk_pw = 0.5 * s.kappa_pw; c.hg_pw = 0.5 * s.gamma_pw;
   c.tp = tp;
   c.cost_f = (float)s.cost; c.sint_f = (float)s.sint; c.tanfi_f = (float)fun.tanfi; c.cosfi_f = (float)fun.cosfi;
   c.dy2_f = (float)s.dy2; c.side_y_f = (float)s.side.y;

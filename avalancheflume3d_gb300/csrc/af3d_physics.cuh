@@ -269,8 +269,13 @@ struct ContactIn {
 // and the same tail in every boundary routine).
 __device__ __forceinline__ void wall_input(const Sph &o, V3 rrc, V3 n, double comp, const Consts &c,
                                            bool gate, ContactIn &ci) {
-  ci.km = 0.5 * c.kappa_pw * o.mwall;
-  ci.gm = 0.5 * c.gamma_pw * o.mwall;
+  if (kFast) {   // the same law with the constant halves formed once per flume
+    ci.km = c.hk_pw * o.mwall;
+    ci.gm = c.hg_pw * o.mwall;
+  } else {
+    ci.km = 0.5 * c.kappa_pw * o.mwall;
+    ci.gm = 0.5 * c.gamma_pw * o.mwall;
+  }
   V3 vvc = point_velocity(o.v, o.w, rrc, o.r);
   ci.dvvc = mk(-vvc.x, -vvc.y, -vvc.z);
   ci.n = n;
@@ -567,9 +572,15 @@ __device__ __forceinline__ bool pair_input(const V3 &rrl, const V3 &vvl, const V
   V3 d;
   double dist2, sep;
   if (!spheres_overlap(s1, rad_1, m, sm, d, dist2, sep)) return false;
-  const double meff = 0.5 * (m.msph + massl);
-  ci.km = 0.5 * c.kappa_pp * meff;
-  ci.gm = 0.5 * c.gamma_pp * meff;
+  if (kFast) {   // 0.5 kappa 0.5 (m1 + m2) with kappa / 4 formed once per flume
+    const double msum = m.msph + massl;
+    ci.km = c.qk_pp * msum;
+    ci.gm = c.qg_pp * msum;
+  } else {
+    const double meff = 0.5 * (m.msph + massl);
+    ci.km = 0.5 * c.kappa_pp * meff;
+    ci.gm = 0.5 * c.gamma_pp * meff;
+  }
   double dist;
   if (kFast) {
     const double inv = rsqrt(dist2);
@@ -632,7 +643,9 @@ __device__ __forceinline__ double signed_zero_product(double a, double b) {
 // (fast mode: im = 1/m and iI = 1/I.x, formed once at import, replace the divisions)
 __device__ __forceinline__ void get_accel_one(V3 f, V3 t, V3 v, V3 w, V3 Rx, V3 Ry, V3 Rz, double m,
                                               double adrag0, V3 I, V3 &a, V3 &al, double im, double iI) {
-  double vmag = sqrt(v.x * v.x + v.y * v.y + v.z * v.z);
+  const double v2 = v.x * v.x + v.y * v.y + v.z * v.z;
+  // fast mode: |v| from the reciprocal square root (the drag term is ~1e-3 of gravity here)
+  double vmag = kFast ? (v2 == 0.0 ? 0.0 : v2 * rsqrt(v2)) : sqrt(v2);   // NaN stays NaN
   double adrag = adrag0 * vmag;
   if (kFast) {
     a.x = f.x * im - adrag * v.x;
