@@ -725,7 +725,7 @@ __device__ __forceinline__ int block_contacts(BlockQueue<NB> &bq, long bbase, lo
         const int k = p & 3;
         const V3 s1 = mk(me.s[3 * k], me.s[3 * k + 1], me.s[3 * k + 2]);
         kind = pair_input(rl, vl, wl, s1, me.rad, me.msph, nbr[t], p >> 2, co,
-                          co.variant == AF3D_FRICTION_DEV, ci) ? 1 : 0;
+                          co.variant == AF3D_FRICTION_DEV, ci, true) ? 1 : 0;
       }
       int r = kind == 1 ? 1 : 0;
       if (kind && apply_law(ci, rl, co, fs, tq)) r = kind == 1 ? 2 : 3;

@@ -142,7 +142,9 @@ __device__ __forceinline__ bool contact_law_fast(V3 dvvc, V3 n, double comp, dou
   const double vt2 = vt.x * vt.x + vt.y * vt.y + vt.z * vt.z;
   const double inv_vt = rsqrt(vt2);          // +inf for vt = 0: the tangential part is then NaN
   const double vt_mag = vt2 * inv_vt;        // and skipped, as in the exact law
-  const double vt_sig = (dvvc.x * vt.x + dvvc.y * vt.y + dvvc.z * vt.z) * inv_vt;
+  // dvvc . vt / |vt| = |vt| up to the rounding of vt's orthogonality to n, which the exact law
+  // also rounds: the fast law takes |vt| itself
+  const double vt_sig = vt_mag;
   const double normal = km * comp + gm * (-vn);
   if (gate ? (normal <= 0.0) : !(normal > 0.0)) return false;
   f = mk(-normal * n.x, -normal * n.y, -normal * n.z);
@@ -553,7 +555,7 @@ __device__ __forceinline__ bool bnd_may_touch_f(int routine, float4 p, float B, 
 // square and rounding is monotone, fused or not), so the last comparison alone takes the same
 // decision, NaN included.  The list kernel and pair_input run this same function.
 __device__ __forceinline__ bool spheres_overlap(const V3 &s1, double rad_1, const NbrRec &m, int sm, V3 &d,
-                                                double &dist2, double &sep) {
+                                                double &dist2, double &sep, bool known = false) {
   const double rad_2 = m.rad;
   sep = rad_1 + rad_2;
   const double sep2 = sep * sep;
@@ -563,15 +565,16 @@ __device__ __forceinline__ bool spheres_overlap(const V3 &s1, double rad_1, cons
   dist2 = d.x * d.x;
   dist2 = __dadd_rn(dist2, __dmul_rn(d.y, d.y));   // uncontracted in both modes
   dist2 = __dadd_rn(dist2, __dmul_rn(d.z, d.z));
-  return dist2 < sep2;
+  return known || dist2 < sep2;   // known: an item of the lists, which this same test kept
 }
 
+// listed: the pair is an item of the lists, whose overlap test (this one) it passed.
 __device__ __forceinline__ bool pair_input(const V3 &rrl, const V3 &vvl, const V3 &wwl, const V3 &s1,
                                            double rad_1, double massl, const NbrRec &m, int sm,
-                                           const Consts &c, bool xi0, ContactIn &ci) {
+                                           const Consts &c, bool xi0, ContactIn &ci, bool listed = false) {
   V3 d;
   double dist2, sep;
-  if (!spheres_overlap(s1, rad_1, m, sm, d, dist2, sep)) return false;
+  if (!spheres_overlap(s1, rad_1, m, sm, d, dist2, sep, listed)) return false;
   if (kFast) {   // 0.5 kappa 0.5 (m1 + m2) with kappa / 4 formed once per flume
     const double msum = m.msph + massl;
     ci.km = c.qk_pp * msum;
