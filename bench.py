@@ -15,10 +15,14 @@ bare release block of the configuration (optionally with the reference's random 
 velocities ``--v0`` and a release ``--preroll``), which has almost no contacts.  Synthetic data;
 the state (~350 MB) is larger than L2.
 
-Timed: exactly K fused steps (graph replays, af3d_step) after W warm-up steps, CUDA events on
-the engine's stream, barrier + synchronize on both sides, max over ranks.  Then, outside the
-timed region: a profiled pass (CUDA events between the kernels) for the roofline of the dominant
-kernel, the end-to-end figure through the C ABI with host buffers, and the CPU baseline.
+Before timing, the project's autotuner (af3d_autotune_shapes) picks the permutation interval and
+the force kernel's block on a context of its own (untimed; ``--no-autotune`` keeps the
+defaults).  Timed: exactly K fused steps (graph replays, af3d_step) after W warm-up steps, CUDA
+events on the engine's stream, barrier + synchronize on both sides, max over ranks.  Then,
+outside the timed region: the other FP64 mode, a profiled pass (CUDA events between the kernels)
+for the roofline of the dominant kernel, the end-to-end figures through the C ABI with host
+buffers (every step, and once per 2000 steps as the reference's device driver copies), the
+2,048- and 524,288-clump configurations, the batched ensemble, the adjoint and the CPU baseline.
 
 ``--impl reference`` times the reference's CPU implementation of the step (the oracle port of
 the reference's host routines, all host threads) on a bounded sample of the same workload.
@@ -61,6 +65,8 @@ def parse_args():
                         "cover the GPU under sustained load (0: none)")
     p.add_argument("--profile-steps", type=int, default=10)
     p.add_argument("--e2e-steps", type=int, default=20)
+    p.add_argument("--e2e-round-trip", type=int, default=2000,
+                   help="steps per host round trip of the second end-to-end figure (0: skip)")
     p.add_argument("--cpu-sample", type=int, default=16384, help="clumps in the CPU baseline sample")
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--no-cpu", action="store_true")
@@ -706,6 +712,31 @@ def run_engine(args):
                "what": "per step: af3d_step_host on pinned host arrays (import of the AoS + a_i, one "
                        "step, export of the AoS + a_i in place; the copies of each quarter of the "
                        "clumps overlap the work on the others)"}
+        # The reference's own device driver copies the particles back every 2000 steps
+        # (avalanche_dev.cu:741, for its re-grid and output): the same round trip through the C
+        # ABI once per 2000 fused steps, beside the per-step contract above.
+        if args.e2e_round_trip > 0:
+            K = args.e2e_round_trip
+            p_ptr, a_ptr, al_ptr = ptrs
+
+            def trip():
+                for fn, argv in (("af3d_import_particles", (eng._h, p_ptr, a_ptr, al_ptr)),
+                                 ("af3d_step", (eng._h, K)),
+                                 ("af3d_export_particles", (eng._h, p_ptr, a_ptr, al_ptr))):
+                    st = getattr(lib(), fn)(*argv)
+                    if st != 0:
+                        raise RuntimeError("%s failed: %d" % (fn, st))
+
+            trip()   # untimed: its graphs are captured here
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            trip()
+            torch.cuda.synchronize()
+            dtk = replicas.max_over_ranks(R, time.perf_counter() - t0, dev)
+            e2e["round_trip"] = {"value": world * args.n * K / dtk, "unit": "clump-steps/s", "steps_per_trip": K,
+                                 "h2d_bytes_per_trip": nbytes, "d2h_bytes_per_trip": nbytes,
+                                 "what": "import of the AoS + a_i, %d fused steps (af3d_step), export of the "
+                                         "AoS + a_i, as the reference's device driver copies every 2000 steps" % K}
 
     configs = {}
     if world == 1 and not args.no_configs:
