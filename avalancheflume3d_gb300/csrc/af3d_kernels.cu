@@ -264,8 +264,7 @@ __device__ __forceinline__ void predict_state(V3 &r, V3 &v, V3 &w, V3 a, V3 al, 
         sincos(mag, &sn, &c);
       } else {
         u = mk(dO.x / mag, dO.y / mag, dO.z / mag);
-        c = cos(mag);
-        sn = sin(mag);
+        sincos(mag, &sn, &c);   // init_Verlet.cu's cos and sin, from one argument reduction
       }
       const double omc = 1.0 - c;
       dRx = mk(omc * u.x * u.x + c, omc * u.x * u.y - sn * u.z, omc * u.x * u.z + sn * u.y);
