@@ -67,7 +67,8 @@ def parse_args():
     p.add_argument("--e2e-steps", type=int, default=20)
     p.add_argument("--e2e-round-trip", type=int, default=2000,
                    help="steps per host round trip of the second end-to-end figure (0: skip)")
-    p.add_argument("--cpu-sample", type=int, default=16384, help="clumps in the CPU baseline sample")
+    p.add_argument("--cpu-sample", type=int, default=0,
+                   help="clumps of the CPU legs: 0 for the whole workload, else the clumps furthest upslope")
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-autotune", dest="autotune", action="store_false",
@@ -256,8 +257,8 @@ def run_reference(args):
         return
     threads = os.cpu_count() or 1
     cfg, (sys_, fun, pp) = workload(args)
-    m = min(args.n, max(args.cpu_sample, 65536))
-    s, f, q = cpu_sample_state(cfg, sys_, fun, pp, m)[:3]
+    m = min(args.n, args.cpu_sample) if args.cpu_sample > 0 else args.n
+    s, f, q = cpu_sample_state(cfg, sys_, fun, pp, m)[:3] if m < args.n else (sys_, fun, pp)
     from oracle.pyoracle import Oracle, OracleRun
     o = Oracle()
     o.set_threads(threads)
@@ -270,8 +271,12 @@ def run_reference(args):
     run.step(args.steps, cc0=pre + args.warmup)
     dt = time.perf_counter() - t0
     value = m * args.steps / dt
-    sample = ("the %d clumps furthest upslope (a full-depth section of the input) as their own system, "
-              "%d release steps, then %d timed steps" % (m, pre, args.steps))
+    if m < args.n:
+        sample = ("the %d clumps furthest upslope (a full-depth section of the input) as their own system, "
+                  "%d release steps, then %d timed steps" % (m, pre, args.steps))
+    else:
+        sample = ("the whole workload (%d clumps): start-up force pass, %d warm-up steps, then %d timed steps"
+                  % (m, args.warmup, args.steps))
     line = {"metric": METRIC, "value": value, "unit": "clump-steps/s", "impl": "reference",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1000.0 * dt / args.steps * (args.n / m), "higher_is_better": True,
@@ -760,12 +765,16 @@ def run_engine(args):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         p_, a_, al_ = eng.export_particles()
-        m = min(args.cpu_sample, args.n)
-        s, f, q, qa, qal = cpu_sample_state(cfg, eng.get_system(), fun, p_, m, a_, al_)
+        m = min(args.cpu_sample, args.n) if args.cpu_sample > 0 else args.n
+        if m < args.n:
+            s, f, q, qa, qal = cpu_sample_state(cfg, eng.get_system(), fun, p_, m, a_, al_)
+            what = "the %d clumps furthest upslope in the timed state (a full-depth section) as their own system" % m
+        else:
+            s, f, q, qa, qal = eng.get_system(), fun, p_, a_, al_
+            what = "the whole timed state (%d clumps)" % m
         val, k, dt = time_cpu(s, f, q, 1, args.cpu_seconds, acc=qa, anga=qal)
         cpu = {"value": val, "unit": "clump-steps/s", "cores": 1, "kind": "port",
-               "sample": "the %d clumps furthest upslope in the timed state (a full-depth section) as "
-                         "their own system, %d steps in %.1f s, 1 thread" % (m, k, dt)}
+               "sample": "%s, %d steps in %.1f s, 1 thread" % (what, k, dt)}
 
     eng.close()
     if rank == 0:
