@@ -4,7 +4,8 @@ statistics.  16 seeds of a dense layer on the bed of the 40 cm x 4 cm flume, 300
 both FP64 modes; per seed the runout (the 95th percentile of the downslope position), the
 deposit centroid (mass-weighted mean downslope position) and the mean downslope velocity, each
 measured as its change since the start.  The seed-averaged changes must agree with the oracle's
-within 2%.  The oracle runs in a spawn process pool, one seed per process."""
+within 2%.  The oracle runs in a spawn process pool, one seed per process.  The same check at the
+2,048-clump flume's full 50,000-step horizon compares with the oracle's committed observables."""
 import multiprocessing as mp
 import os
 
@@ -73,3 +74,46 @@ def test_observables_16_seeds(oracle_changes, mode):
     assert np.all(np.abs(want) > 0)
     rel = np.abs(got - want) / np.abs(want)
     assert np.all(rel <= 0.02), (got, want, rel)
+
+
+# The 2,048-clump flume over its full 50,000-step horizon (0.1 s), 16 seeds, against the oracle's
+# observables committed in tests/golden/observables_flume2k.npz (tests/golden/make_observables.py:
+# single-threaded oracle runs of about 10 minutes each).  The 16 seeds run on the GPU as one
+# batched ensemble, whose flumes evolve exactly as they do alone.
+@pytest.fixture(scope="module")
+def flume2k_golden():
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "observables_flume2k.npz")
+    with np.load(path) as z:
+        return {k: z[k] for k in z.files}
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("layout", ["lattice", "bed"])
+def test_observables_flume2k_full_horizon(flume2k_golden, layout, mode):
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import avalancheflume3d_gb300 as af3d
+    from avalancheflume3d_gb300.workloads import ensemble_state, flume_2k
+    g = flume2k_golden
+    li = list(g["layouts"]).index(layout)
+    seeds = [int(s) for s in g["seeds"]]
+    sys, fun, pp = ensemble_state([flume_2k(layout=layout, seed=s) for s in seeds])
+    with af3d.Engine(sys, fun, fp_mode=mode) as eng:
+        eng.import_particles(pp)
+        eng.forces()
+        eng.swap_accel()
+        eng.step(int(g["steps"]))
+        assert eng.status() == 0
+        p1 = eng.export_particles(with_accel=False)
+        spans = [eng.flume_slice(f) for f in range(len(seeds))]
+    before = np.array([_observables(pp[s], sys[f], pp["mass"][s]) for f, s in enumerate(spans)])
+    after = np.array([_observables(p1[s], sys[f], p1["mass"][s]) for f, s in enumerate(spans)])
+    # the same initial states as the oracle's (generated by the same host routines)
+    np.testing.assert_allclose(before, g["before"][li], rtol=1e-9, atol=1e-12)
+    got = (after - before).mean(0)
+    want = (g["after"][li] - g["before"][li]).mean(0)
+    assert np.all(np.abs(want) > 0)
+    rel = np.abs(got - want) / np.abs(want)
+    print("flume2k %s mode %d: relative differences (runout, centroid, velocity)" % (layout, mode), rel)
+    assert np.all(rel <= 0.02), (layout, mode, got, want, rel)
