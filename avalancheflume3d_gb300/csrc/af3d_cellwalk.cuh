@@ -170,7 +170,10 @@ __device__ __forceinline__ void for_neighbour_slots_pre(const Search &q, const a
 constexpr int kLaneItems = kListCap;
 constexpr unsigned kBndItem = 0xFFFFFF00u;   // boundary item: kBndItem | routine << 2 | sphere
 
-constexpr int kPassCap = 32;   // partners per clump that pass the centre test
+// Partners per clump that pass the centre test; a clump with more takes the per-clump walk.  The
+// benchmark states have at most 10 (262,144-clump bed, 524,288-clump polydisperse funnel); the
+// cap sets most of the list phase's shared memory, which the L1 cache shares.
+constexpr int kPassCap = 24;
 constexpr unsigned kSlotMask = 0x3FFFFFFFu;   // pass entry: position or slot | (x offset + 1) << 30
 
 // Per-warp partner lists of the two-stage gather in shared memory, one column per lane
@@ -179,9 +182,11 @@ struct PassLists {
   unsigned pass_t[kPassCap][32];         // partner position, then slot | (cell x offset + 1) << 30
   unsigned short pass_m[kPassCap][32];   // their 16-bit sphere-pair masks
   int pbase[33];
-  unsigned cand[kLaneItems][32];         // candidate sphere pairs in item order: entry << 4 | sph_id-1
+  unsigned short cand[kLaneItems][32];   // candidate sphere pairs in item order: entry << 4 | sph_id-1
+                                         // (0x8000: rejected by the overlap test)
   int cbase[33];
 };
+static_assert(((kPassCap - 1) << 4 | 15) < 0x8000, "candidate entries are 15-bit");
 
 // Item lists held in shared memory (the adjoint's cooperative reverse).
 struct ItemLists {
@@ -366,7 +371,7 @@ __device__ __forceinline__ int build_item_lists(PassLists &pl, unsigned *col, lo
             slow = true;
             break;
           }
-          pl.cand[ncand++][lane] = ((unsigned)k << 4) | (unsigned)p;
+          pl.cand[ncand++][lane] = (unsigned short)(((unsigned)k << 4) | (unsigned)p);
         }
     }
     if (slow) ncand = 0;
@@ -385,7 +390,7 @@ __device__ __forceinline__ int build_item_lists(PassLists &pl, unsigned *col, lo
       V3 d;
       double dist2, sep;
       if (!spheres_overlap(s1, mo.rad, nbr[pl.pass_t[k][ow] & kSlotMask], p >> 2, d, dist2, sep))
-        pl.cand[ci][ow] = e | 0x80000000u;
+        pl.cand[ci][ow] = (unsigned short)(e | 0x8000u);
     }
   }
   __syncwarp();
@@ -393,7 +398,7 @@ __device__ __forceinline__ int build_item_lists(PassLists &pl, unsigned *col, lo
 #pragma unroll 1
     for (int i = 0; i < ncand; i++) {
       const unsigned e = pl.cand[i][lane];
-      if (e & 0x80000000u) continue;
+      if (e & 0x8000u) continue;
       const unsigned t = pl.pass_t[e >> 4][lane] & kSlotMask;
       col[stride * nitems++] = (t << 4) | (e & 15u);   // (partner slot, sph_id-1)
     }

@@ -163,19 +163,23 @@ constexpr int kPermBlock = 128;
 constexpr int kRecWords = (int)(sizeof(NbrRec) / 8);   // 24
 constexpr int kRecStride = kRecWords + 1;
 
-// One thread's records into the block's shared-memory staging.
-__device__ __forceinline__ void stage_record(const NbrRec &q, const CullRec &cr, double *s_nbr, CullRec *s_cull) {
+// One thread's neighbour record into the block's shared-memory staging.
+__device__ __forceinline__ void stage_nbr_record(const NbrRec &q, double *s_nbr) {
   const double *qw = reinterpret_cast<const double *>(&q);
 #pragma unroll
   for (int k = 0; k < kRecWords; k++) s_nbr[threadIdx.x * kRecStride + k] = qw[k];
+}
+
+// One thread's records into the block's shared-memory staging.
+__device__ __forceinline__ void stage_record(const NbrRec &q, const CullRec &cr, double *s_nbr, CullRec *s_cull) {
+  stage_nbr_record(q, s_nbr);
   s_cull[threadIdx.x] = cr;
 }
 
-// The block's staged records written out as contiguous 16-byte stores (after a barrier that
-// follows the staging).
+// The block's staged neighbour records written out as contiguous 16-byte stores (after a
+// barrier that follows the staging).
 template <int NB>
-__device__ __forceinline__ void copy_records(long base, long n, NbrRec *nbr, CullRec *cull, const double *s_nbr,
-                                             const CullRec *s_cull) {
+__device__ __forceinline__ void copy_nbr_records(long base, long n, NbrRec *nbr, const double *s_nbr) {
   const long cnt = n - base < NB ? n - base : NB;
   const int nw = (int)(cnt * kRecWords) / 2;   // double2 words of the block's records
   double2 *b = reinterpret_cast<double2 *>(nbr + base);
@@ -183,6 +187,14 @@ __device__ __forceinline__ void copy_records(long base, long n, NbrRec *nbr, Cul
     const int w0 = 2 * i, r0 = w0 / kRecWords, k0 = w0 - r0 * kRecWords;   // k0 even, k0 + 1 < 24
     b[i] = make_double2(s_nbr[r0 * kRecStride + k0], s_nbr[r0 * kRecStride + k0 + 1]);
   }
+}
+
+// ... and the culling records with them.
+template <int NB>
+__device__ __forceinline__ void copy_records(long base, long n, NbrRec *nbr, CullRec *cull, const double *s_nbr,
+                                             const CullRec *s_cull) {
+  copy_nbr_records<NB>(base, n, nbr, s_nbr);
+  const long cnt = n - base < NB ? n - base : NB;
   const int m16 = (int)(cnt * (long)(sizeof(CullRec) / 16));
   const float4 *c = reinterpret_cast<const float4 *>(s_cull);
   float4 *e = reinterpret_cast<float4 *>(cull + base);
@@ -832,14 +844,16 @@ __device__ __forceinline__ int lists_body(const Consts &c, const DevScalars *d, 
 }
 
 // Shared memory of the force kernel: the list phase, the force phase and the look-ahead's record
-// staging run one after another.
+// staging run one after another.  Kept small because the SM's L1 cache gets what the resident
+// blocks' shared memory leaves of 256 KB: at 96 threads and 6 blocks an SM, 20.3 KB per block
+// (the list phase's) leaves ~124 KB of L1 for the walk's, records' and spills' lines, where
+// 30.8 KB left 60 KB (0.275 -> 0.269 ms per pass on the 262,144-clump bed).
 template <int NB>
 union ForceShared {
   PassLists pl[NB / 32];
   BlockQueue<NB> bq;
   struct {
     double nbr[NB * kRecStride];
-    CullRec cull[NB];
   } rec;
 };
 
@@ -935,7 +949,8 @@ __device__ __forceinline__ void fused_body(const Consts &c, Planes P, Planes out
         NbrRec q;
         CullRec cr;
         make_records(rn, vn, wn, sp, P.p[RAD][s], P.p[MSPH][s], P.p[MWALL][s], q, cr);
-        stage_record(q, cr, sh.rec.nbr, sh.rec.cull);
+        stage_nbr_record(q, sh.rec.nbr);
+        la.cull[s] = cr;   // stored directly: staged too, it would set the block's shared memory size
       }
       const long key = bucket_key(rn, fl, d, la.id[s], t_next);
       la.cells.key[s] = (int)key;
@@ -944,8 +959,8 @@ __device__ __forceinline__ void fused_body(const Consts &c, Planes P, Planes out
   }
   warp_count(d, active);
   if (la.nbr) {
-    __syncthreads();   // every record of the block is staged
-    copy_records<NB>(bbase, n, la.nbr, la.cull, sh.rec.nbr, sh.rec.cull);
+    __syncthreads();   // every neighbour record of the block is staged
+    copy_nbr_records<NB>(bbase, n, la.nbr, sh.rec.nbr);
   }
 }
 

@@ -306,7 +306,7 @@ af3d_status af3d_contact_pairs_noalloc (af3d_ctx *ctx, long *out, long cap, long
 /* Active sphere-sphere contacts summed over the fused force passes (af3d_step, af3d_forces)
    since the previous call; the counter restarts at zero. */
 af3d_status af3d_contact_count (af3d_ctx *ctx, long *count);
-/* Clumps whose contact item lists overflowed (more than 32 items, 32 partners passing the
+/* Clumps whose contact item lists overflowed (more than 32 items, 24 partners passing the
    centre test or 48 candidates), summed over the fused force passes since the previous call;
    the counter restarts at zero.  Such a clump's contacts run by the per-clump cell walk, in
    the same summation order (force_part.cu:88-106's walk, one pass per sph_id). */

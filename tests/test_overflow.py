@@ -2,14 +2,14 @@
 oracle.
 
 A clump's contacts normally run from its item list: at most 32 items (boundary and sphere-pair
-items), built from at most 32 partners that pass the FP32 centre test.  A clump with more runs
+items), built from at most 24 partners that pass the FP32 centre test.  A clump with more runs
 alone after its block's pooled items, by the per-clump cell walk (one walk per sph_id, the order
 of force_part.cu:88-106's sixteen launches), with the same summation order.  These states force
 that path:
 
   * pile:  five clumps piled almost on one spot inside a dense packing, so one clump has more
            than 32 overlapping sphere pairs (the item cap);
-  * crowd: forty clumps crowded within one clump's bounding radius, so a clump has more than 32
+  * crowd: forty clumps crowded within one clump's bounding radius, so a clump has more than 24
            partners that pass the centre test (the partner cap);
   * poly:  the pile in a polydisperse packing (size factors in (0.8, 1.2]).
 
