@@ -40,7 +40,7 @@ af3d_status fail(af3d_status code, const std::string &msg) {
   } while (0)
 
 constexpr long kRegridEvery = 2000;   // avalanche_hst.cu:470 and :713 (cc % 2000 == 0)
-constexpr long kKernelsPerCellBuild = 6;   // predict/keys, 2 scan, scatter, rank, permute
+constexpr long kKernelsPerCellBuild = 5;   // predict/keys, scan, scatter, rank, permute
 constexpr long kKernelsPerForcePass = 1;   // lists and forces in one kernel
 #ifndef AF3D_HOST_PARTS
 #define AF3D_HOST_PARTS 4
@@ -242,12 +242,13 @@ af3d_status ensure_buckets(af3d_ctx *c, long ncell_total) {
   AF3D_CUDA(cudaStreamSynchronize(c->st));
   cudaFree(c->cells.count);
   cudaFree(c->cells.start);
-  cudaFree(c->cells.block_sums);
-  c->cells.count = c->cells.start = c->cells.block_sums = nullptr;
+  cudaFree(c->cells.tile_count);
+  c->cells.count = c->cells.start = c->cells.tile_count = nullptr;
   AF3D_CUDA(cudaMalloc(&c->cells.count, sizeof(int) * cap));
   AF3D_CUDA(cudaMalloc(&c->cells.start, sizeof(int) * (cap + 1)));
-  AF3D_CUDA(cudaMalloc(&c->cells.block_sums, sizeof(int) * (scan_tiles(cap) + 1)));
+  AF3D_CUDA(cudaMalloc(&c->cells.tile_count, sizeof(int) * (scan_tiles(cap) + 1)));
   AF3D_CUDA(cudaMemsetAsync(c->cells.count, 0, sizeof(int) * cap, c->st));
+  AF3D_CUDA(cudaMemsetAsync(c->cells.tile_count, 0, sizeof(int) * (scan_tiles(cap) + 1), c->st));
   c->cells.cap = cap;
   c->cells_valid = false;
   drop_graphs(c);
@@ -638,7 +639,7 @@ af3d_status af3d_destroy(af3d_ctx *c) {
                   (void *)c->fl_cur, (void *)c->fl_alt, (void *)c->flume_of_id, (void *)c->nbr,
                   (void *)c->cull, (void *)c->lists.items, (void *)c->nbr_next, (void *)c->cull_next, (void *)c->cells.key, (void *)c->cells.rank_tmp, (void *)c->cells.tmp_slot,
                   (void *)c->cells.perm, (void *)c->cells.csort, (void *)c->cells.count, (void *)c->cells.start,
-                  (void *)c->cells.block_sums, (void *)c->d, (void *)c->flumes, (void *)c->d_aos,
+                  (void *)c->cells.tile_count, (void *)c->d, (void *)c->flumes, (void *)c->d_aos,
                   (void *)c->d_acc, (void *)c->d_anga, (void *)c->d_tmp, (void *)c->d_count})
     if (p) cudaFree(p);
   if (c->own_stream && c->st) cudaStreamDestroy(c->st);

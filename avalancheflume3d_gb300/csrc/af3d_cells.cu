@@ -2,8 +2,9 @@
 //
 // Replaces the fixed-capacity slot table of cells.cu (clear_cell / clear_ocup / cell_locate).
 // The predictor kernel has already written every clump's bucket key and its atomic arrival rank
-// inside the bucket.  Here:
-//   1. exclusive scan of the bucket counts  -> start[b]      (two-kernel reduce-then-scan)
+// inside the bucket, and counted it in its bucket's scan tile.  Here:
+//   1. exclusive scan of the bucket counts  -> start[b]      (one pass: each tile starts from the
+//                                                            tile counts before it)
 //   2. scatter old slots by arrival          -> tmp_slot
 //   3. rank every clump inside its bucket by clump id (buckets hold a handful of clumps), which
 //      makes the final order deterministic and equal to the reference's ascending-id insertion
@@ -18,6 +19,7 @@ namespace {
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = 16;   // consecutive buckets per thread, moved as four int4
 constexpr int kTile = kScanThreads * kScanItems;
+static_assert(kTile == kScanTile, "the producers count clumps per kScanTile buckets");
 
 // The kScanItems counts of one thread starting at bucket `base` (a multiple of kScanItems, so
 // the vector loads are 16-byte aligned); buckets at or past nb read as zero.
@@ -67,39 +69,21 @@ __device__ __forceinline__ int block_excl_scan(int v, int *total) {
 // Buckets in use: every flume's cells plus one private bucket per clump for the clumps not binned.
 __device__ __forceinline__ long n_buckets(const DevScalars *d, long n) { return d->ncell_total + n; }
 
+// Each tile adds the clump counts of the tiles before it (counted at arrival; integer sums are
+// exact in any order), then scans its own buckets.
 // advance: block 0 also performs k_advance_time's time += dt (steps whose predictor ran in the
 // previous force pass start with the sort; nothing before the force pass reads the clock).
-__global__ void k_scan_partials(const int *__restrict__ count, int *block_sums, DevScalars *d, bool advance,
-                                long n) {
+__global__ void k_scan_final(const int *__restrict__ count, const int *__restrict__ tile_count,
+                             int *start, DevScalars *d, bool advance, long n) {
   if (advance && blockIdx.x == 0 && threadIdx.x == 0) {
     d->time_prev = d->time;
     d->time = d->time + d->flumes[0].sys.dt;
   }
   const long nb = n_buckets(d, n);
-  const long base = blockIdx.x * (long)kTile + threadIdx.x * (long)kScanItems;
-  __shared__ int tot;
-  if (blockIdx.x * (long)kTile >= nb) {   // a tile past the buckets in use
-    if (threadIdx.x == 0) block_sums[blockIdx.x] = 0;
-    return;
-  }
-  int c[kScanItems];
-  load_counts(count, base, nb, c);
-  int v = 0;
-#pragma unroll
-  for (int i = 0; i < kScanItems; i++) v += c[i];
-  block_excl_scan(v, &tot);
-  if (threadIdx.x == 0) block_sums[blockIdx.x] = tot;
-}
-
-// Each tile adds the sum of the tile sums before it (k_scan_partials' raw sums; integer sums
-// are exact in any order), so no separate pass scans them.
-__global__ void k_scan_final(const int *__restrict__ count, const int *__restrict__ block_sums,
-                             int *start, const DevScalars *d, long n) {
-  const long nb = n_buckets(d, n);
   if (blockIdx.x == 0 && threadIdx.x == 0) start[nb] = (int)n;   // every clump has one bucket
   if (blockIdx.x * (long)kTile >= nb) return;   // a tile past the buckets in use
   int part = 0;
-  for (long t = threadIdx.x; t < (long)blockIdx.x; t += kScanThreads) part += block_sums[t];
+  for (long t = threadIdx.x; t < (long)blockIdx.x; t += kScanThreads) part += tile_count[t];
   __shared__ int tile_off;
   block_excl_scan(part, &tile_off);
   const long base = blockIdx.x * (long)kTile + threadIdx.x * (long)kScanItems;
@@ -134,17 +118,18 @@ __global__ void k_scatter(const int *__restrict__ key, const int *__restrict__ r
   tmp_slot[start[key[s]] + rank_tmp[s]] = (int)s;
 }
 
-// Also returns the bucket count to zero, so the count array is all-zero at the next build
-// whatever the grid then is (the scan has consumed it already).
+// Also returns the bucket count and its tile's count to zero, so both arrays are all-zero at the
+// next build whatever the grid then is (the scan has consumed them already).
 __global__ void k_rank(const int *__restrict__ key, const int *__restrict__ start,
                        const int *__restrict__ tmp_slot, const long long *__restrict__ id, int *perm,
-                       const CullRec *__restrict__ cull, float4 *csort, int *count, DevScalars *d,
-                       long ntags, long n) {
+                       const CullRec *__restrict__ cull, float4 *csort, int *count, int *tile_count,
+                       DevScalars *d, long ntags, long n) {
   const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (s >= n) return;
   const long ncell3 = d->ncell_total;
   const int k = key[s];
   count[k] = 0;
+  tile_count[k / kTile] = 0;
   const int b = start[k], e = start[k + 1];
   const long long me = id[s];
   int r = 0;
@@ -165,12 +150,12 @@ void launch_sort(const Launch &L, DevScalars *d, Cells c, const long long *id, l
   // Launch sizes follow the capacity; the kernels read the bucket count in use from the device,
   // so a captured graph stays valid across device-side re-grids.
   const long ntiles = scan_tiles(c.cap);
-  k_scan_partials<<<(unsigned)ntiles, kScanThreads, 0, L.st>>>(c.count, c.block_sums, d, advance, L.n);
-  k_scan_final<<<(unsigned)ntiles, kScanThreads, 0, L.st>>>(c.count, c.block_sums, c.start, d, L.n);
+  k_scan_final<<<(unsigned)ntiles, kScanThreads, 0, L.st>>>(c.count, c.tile_count, c.start, d, advance, L.n);
   if (L.n <= 0) return;
   const unsigned g = (unsigned)((L.n + 127) / 128);
   k_scatter<<<g, 128, 0, L.st>>>(c.key, c.rank_tmp, c.start, c.tmp_slot, L.n);
-  k_rank<<<g, 128, 0, L.st>>>(c.key, c.start, c.tmp_slot, id, c.perm, cull, c.csort, c.count, d, ntags, L.n);
+  k_rank<<<g, 128, 0, L.st>>>(c.key, c.start, c.tmp_slot, id, c.perm, cull, c.csort, c.count, c.tile_count, d,
+                              ntags, L.n);
 }
 
 }  // namespace af3d

@@ -10,6 +10,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include "../../include/af3d.h"
@@ -64,9 +65,26 @@ struct Cells {
   float4 *csort;    // [N]   FP32 culling centre of the clump at each position of that order
   int *count;       // [cap] bucket sizes (all zero between builds)
   int *start;       // [cap+1] exclusive scan of count
-  int *block_sums;  // [scan_tiles(cap)] scan scratch
+  int *tile_count;  // [scan_tiles(cap)] clumps per kScanTile buckets (all zero between builds)
   long cap;         // buckets available (ncell_total + N must fit)
 };
+
+// Buckets per tile of the sort's scan.
+constexpr int kScanTile = 4096;
+
+// A clump's arrival in bucket `key`: returns its rank among the bucket's arrivals, and counts it
+// in the key's scan tile too, so that the sort's scan starts from the tile counts instead of
+// summing every bucket in a pass of its own.  A warp's clumps lie mostly in one tile (slots are
+// in spatial order), so the lanes arriving together add to each tile once: one atomic per
+// distinct tile instead of one per clump, which contended on the tile's counter.
+__device__ __forceinline__ int arrive_in_bucket(const Cells &c, long key) {
+  namespace cg = cooperative_groups;
+  const int tile = (int)(key / kScanTile);
+  const cg::coalesced_group here = cg::coalesced_threads();
+  const cg::coalesced_group same = cg::labeled_partition(here, tile);
+  if (same.thread_rank() == 0) atomicAdd(&c.tile_count[tile], (int)same.size());
+  return atomicAdd(&c.count[key], 1);
+}
 
 // Scalars of one flume's system_par / Funnel used by the force routines.  A single-flume
 // context passes them to the fused force kernel as a __grid_constant__ parameter (constant-bank

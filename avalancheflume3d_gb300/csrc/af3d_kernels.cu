@@ -425,7 +425,7 @@ __global__ void __launch_bounds__(kBlock) k_predict(Planes P, DevScalars *d, boo
     if (KEYS) {
       const long key = bucket_key(r, fl, d, id[s], d->time);
       cells.key[s] = (int)key;
-      cells.rank_tmp[s] = atomicAdd(&cells.count[key], 1);
+      cells.rank_tmp[s] = arrive_in_bucket(cells, key);
     }
   }
   if (RECORDS) store_records<kPermBlock>(valid, base, n, q, cr, nbr, cull, s_nbr, s_cull);
@@ -954,7 +954,7 @@ __device__ __forceinline__ void fused_body(const Consts &c, Planes P, Planes out
       }
       const long key = bucket_key(rn, fl, d, la.id[s], t_next);
       la.cells.key[s] = (int)key;
-      la.cells.rank_tmp[s] = atomicAdd(&la.cells.count[key], 1);
+      la.cells.rank_tmp[s] = arrive_in_bucket(la.cells, key);
     }
   }
   warp_count(d, active);
