@@ -89,6 +89,7 @@ int force_shape_for(long n, int sms) {
   int best = 0;
   double best_fill = -1.0;
   for (int i = 0; i < kForceShapes; i++) {
+    if (!kForceShapeDefault[i]) continue;
     const double blocks = (double)((n + kForceShapeBlock[i] - 1) / kForceShapeBlock[i]);
     const double slots = (double)sms * kForceShapeMinb[i];
     const double waves = blocks / slots;
@@ -1249,7 +1250,7 @@ af3d_status af3d_set_force_block(af3d_ctx *c, int block) {
       c->force_shape = i;
       return AF3D_OK;
     }
-  return fail(AF3D_ERR_ARG, "force block: 64, 96 or 128 threads");
+  return fail(AF3D_ERR_ARG, "force block: 64, 96, 128 or 192 threads");
 }
 
 af3d_status af3d_get_force_block(af3d_ctx *c, int *block) {

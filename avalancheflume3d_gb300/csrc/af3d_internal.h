@@ -167,14 +167,20 @@ struct DevScalars {
 
 // Shapes of the fused force kernel: threads per block (the pool of clumps whose contact items a
 // block processes together) and resident blocks per SM (the register budget, 65536 / (block x
-// blocks)).  Results do not depend on the shape; af3d_autotune times them, and a new context
-// starts with the one whose last wave of blocks is fullest on its device (force_shape_for).
-constexpr int kForceShapes = 3;
-constexpr int kForceShapeBlock[kForceShapes] = {128, 96, 64};
-constexpr int kForceShapeMinb[kForceShapes] = {5, 6, 10};
+// blocks)).  Results do not depend on the shape; af3d_autotune_shapes times them, and a new
+// context starts with the default shape whose last wave of blocks is fullest on its device
+// (force_shape_for).  192 x 3 is tuned but not a default: its larger pool wastes fewer lanes in
+// the last round of contact laws, which pays in the exact mode's heavier law, but at a few
+// blocks per SM it spreads small counts over fewer SMs.
+constexpr int kForceShapes = 4;
+constexpr int kForceShapeBlock[kForceShapes] = {128, 96, 64, 192};
+constexpr int kForceShapeMinb[kForceShapes] = {5, 6, 10, 3};
+constexpr bool kForceShapeDefault[kForceShapes] = {true, true, true, false};
 // Steps whose force pass runs in parts (af3d_step_host) cut the clumps at multiples of every
 // shape's block.
 constexpr long kForceAlign = 384;
+static_assert(kForceAlign % 128 == 0 && kForceAlign % 96 == 0 && kForceAlign % 64 == 0 && kForceAlign % 192 == 0,
+              "a multiple of every shape's block");
 
 // Per-clump item lists of one force pass, from the list phase to the force phase of the force
 // kernel: entry e of slot s at items[e * n + s] (an item is a boundary (routine, sphere) or a

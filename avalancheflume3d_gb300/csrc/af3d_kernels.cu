@@ -1331,17 +1331,20 @@ void launch_lists_forces(const Launch &L, Planes cur, Planes out, DevScalars *d,
   // so the launch's blocks are those of the whole pass
   const long m = count < 0 ? L.n - s0 : std::min(count, L.n - s0);
   if (L.n <= 0 || m <= 0 || shape < 0 || shape >= kForceShapes || s0 % kForceShapeBlock[shape] != 0) return;
-  static_assert(kForceShapes == 3 && kForceShapeBlock[0] == 128 && kForceShapeBlock[1] == 96 &&
-                    kForceShapeBlock[2] == 64, "the instantiated shapes");
+  static_assert(kForceShapes == 4 && kForceShapeBlock[0] == 128 && kForceShapeBlock[1] == 96 &&
+                    kForceShapeBlock[2] == 64 && kForceShapeBlock[3] == 192, "the instantiated shapes");
   if (shape == 0)
     launch_lists_forces_shape<128, kForceShapeMinb[0]>(L, cur, out, d, flume, nbr, cull, start, order, csort,
                                                        lists, write_ft, uniform, warm, look, s0, m);
   else if (shape == 1)
     launch_lists_forces_shape<96, kForceShapeMinb[1]>(L, cur, out, d, flume, nbr, cull, start, order, csort,
                                                       lists, write_ft, uniform, warm, look, s0, m);
-  else
+  else if (shape == 2)
     launch_lists_forces_shape<64, kForceShapeMinb[2]>(L, cur, out, d, flume, nbr, cull, start, order, csort,
                                                       lists, write_ft, uniform, warm, look, s0, m);
+  else
+    launch_lists_forces_shape<192, kForceShapeMinb[3]>(L, cur, out, d, flume, nbr, cull, start, order, csort,
+                                                       lists, write_ft, uniform, warm, look, s0, m);
 }
 
 void launch_boundary(const Launch &L, Planes cur, DevScalars *d, const int *flume, int routine) {

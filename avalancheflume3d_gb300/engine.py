@@ -136,10 +136,10 @@ class Engine:
             timings.update(zip(self.RESORT_CHOICES, ms.tolist()))
         return r.value
 
-    FORCE_BLOCKS = (128, 96, 64)
+    FORCE_BLOCKS = (128, 96, 64, 192)
 
     def set_force_block(self, block: int) -> None:
-        """af3d_set_force_block: threads per block of the fused force kernel (64, 96 or 128)."""
+        """af3d_set_force_block: threads per block of the fused force kernel (64, 96, 128 or 192)."""
         self._call("af3d_set_force_block", int(block))
 
     def force_block(self) -> int:

@@ -552,11 +552,15 @@ def measure_config(name, cfg, steps, warmup, mode, stream, cpu_seconds=0.0):
     return out
 
 
-def time_other_mode(eng, modes, other, args, stream, R, dev, world):
-    """K steps of the other FP64 mode on the same state (after the timed region)."""
+def time_other_mode(eng, modes, other, args, stream, R, dev, world, tuned=None):
+    """K steps of the other FP64 mode on the same state (after the timed region), with the
+    shapes the autotuner picked for that mode (`tuned`) when it ran."""
     import torch
     from avalancheflume3d_gb300 import replicas
     eng.set_fp_mode(modes[other])
+    if tuned:
+        eng.set_resort_every(tuned["resort_every"])
+        eng.set_force_block(tuned["force_block"])
     eng.step(2)
     eng.prepare_steps(args.steps)
     torch.cuda.synchronize()
@@ -566,8 +570,11 @@ def time_other_mode(eng, modes, other, args, stream, R, dev, world):
     o1.record(stream)
     torch.cuda.synchronize()
     ms_other = replicas.max_over_ranks(R, o0.elapsed_time(o1), dev)
-    return {"fp_mode": other, "value": world * args.n * args.steps / (ms_other / 1e3),
-            "ms_per_step": ms_other / args.steps, "steps": args.steps}
+    line = {"fp_mode": other, "value": world * args.n * args.steps / (ms_other / 1e3),
+            "ms_per_step": ms_other / args.steps, "steps": args.steps, "force_block": eng.force_block()}
+    if tuned:
+        line["tuned"] = tuned
+    return line
 
 
 def run_engine(args):
@@ -627,6 +634,16 @@ def run_engine(args):
             while time.perf_counter() < t_end:
                 warm.step(64)
                 torch.cuda.synchronize()
+    # the other FP64 mode's shapes, tuned the same way on a context of its own (untimed): the
+    # exact mode's heavier contact law favours a larger block pool
+    other = "exact" if args.fp_mode == "fast" else "fast"
+    tuned_other = None
+    if args.autotune and not args.no_other_mode:
+        with make_engine() as warm:
+            warm.set_fp_mode(modes[other])
+            timings = {}
+            every, block = warm.autotune_shapes(64, timings)
+            tuned_other = {"resort_every": every, "force_block": block, "ms_per_step": timings}
     eng = make_engine(trace_preroll=True)
     if tuned:
         eng.set_resort_every(tuned["resort_every"])
@@ -663,11 +680,13 @@ def run_engine(args):
     value = world * args.n * args.steps / (ms / 1e3)
 
     # The other FP64 mode on the same state, same step count (outside the timed region).
-    other = "exact" if args.fp_mode == "fast" else "fast"
     other_line = None
     if not args.no_other_mode:
-        other_line = time_other_mode(eng, modes, other, args, stream, R, dev, world)
+        other_line = time_other_mode(eng, modes, other, args, stream, R, dev, world, tuned_other)
     eng.set_fp_mode(modes[args.fp_mode])
+    eng.set_force_block(eng_block)
+    if tuned:
+        eng.set_resort_every(tuned["resort_every"])
 
     # Roofline of the dominant kernel from CUDA events between the kernels (profiled steps after
     # the timed region, same stream).

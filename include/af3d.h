@@ -265,16 +265,16 @@ af3d_status af3d_set_resort_every (af3d_ctx *ctx, long steps);
    step of the run -- the trajectory is bit-identical whatever the interval -- so it costs time,
    not accuracy. */
 af3d_status af3d_autotune (af3d_ctx *ctx, long steps_per_trial, long *resort_every, double *ms_per_step);
-/* The fused force kernel's block (no counterpart in the reference): 64, 96 or 128 threads, one
-   clump per thread, the block's clumps pooling their contact items; each runs at the resident
-   blocks per SM that measured fastest for it (10, 6 and 5).  Results do not depend on it.  A
-   new context starts with the block whose last wave is fullest for its clump count on the
-   current device; af3d_set_force_block overrides it. */
+/* The fused force kernel's block (no counterpart in the reference): 64, 96, 128 or 192 threads,
+   one clump per thread, the block's clumps pooling their contact items; each runs at the
+   resident blocks per SM that measured fastest for it (10, 6, 5 and 3).  Results do not depend
+   on it.  A new context starts with the block of 64, 96 and 128 whose last wave is fullest for
+   its clump count on the current device; af3d_set_force_block overrides it. */
 af3d_status af3d_set_force_block (af3d_ctx *ctx, int block);
 af3d_status af3d_get_force_block (af3d_ctx *ctx, int *block);
 /* Autotuner over both shape parameters (no counterpart in the reference): af3d_autotune (the
-   permutation interval, its times in ms_interval[5]), then each force block (64, 96, 128, its
-   times in ms_block[3]) at that interval, one untimed period and whole periods timed; keeps the
+   permutation interval, its times in ms_interval[5]), then each force block (128, 96, 64, 192,
+   its times in ms_block[4] in that order) at that interval, one untimed period and whole periods timed; keeps the
    fastest of each.  Every step it takes is a step of the run.  The kernels' remaining shape
    parameters are not tuned: one clump per thread (the block pools its clumps' contact items,
    which replaces a clumps-per-warp choice), and the reference's cell size (a smaller cell

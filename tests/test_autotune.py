@@ -87,7 +87,7 @@ def test_prepare_steps_changes_nothing(af3d):
 
 @pytest.mark.parametrize("mode", ["exact", "fast"])
 def test_results_do_not_depend_on_the_force_block(af3d, mode, oracle):
-    """The fused force kernel's block (64, 96 or 128 clumps pooling their contact items) changes
+    """The fused force kernel's block (64, 96, 128 or 192 clumps pooling their contact items) changes
     no bit: one force pass (and, in exact mode, the oracle's) and 120 steps, single flume and a
     three-flume ensemble."""
     from oracle.pyoracle import OracleRun
@@ -97,7 +97,7 @@ def test_results_do_not_depend_on_the_force_block(af3d, mode, oracle):
     run = OracleRun(oracle, sys, fun, pp)
     assert run.forces() == 0
     outs = []
-    for block in (128, 96, 64):
+    for block in (128, 96, 64, 192):
         with af3d.Engine(sys, fun, fp_mode=fp) as e:
             e.set_force_block(block)
             assert e.force_block() == block
@@ -119,7 +119,7 @@ def test_results_do_not_depend_on_the_force_block(af3d, mode, oracle):
         s, f = flume_system(n, tilt=tilt)
         flumes.append((s, f, wall_state(n, seed, s)))
     ens = []
-    for block in (128, 96, 64):
+    for block in (128, 96, 64, 192):
         with af3d.Engine(np.stack([x[0] for x in flumes]), np.stack([x[1] for x in flumes]), fp_mode=fp) as e:
             e.set_force_block(block)
             e.import_particles(np.concatenate([x[2] for x in flumes]))
@@ -132,7 +132,8 @@ def test_results_do_not_depend_on_the_force_block(af3d, mode, oracle):
 
 def test_force_block_default_and_checks(af3d):
     """A new context starts with the block whose last wave of blocks is fullest on this device
-    (the rule of force_shape_for), and only 64, 96 and 128 are accepted."""
+    (the rule of force_shape_for, over 64, 96 and 128), and only 64, 96, 128 and 192 are
+    accepted."""
     import math
     import torch
     sms = torch.cuda.get_device_properties(0).multi_processor_count
@@ -153,6 +154,8 @@ def test_force_block_default_and_checks(af3d):
         s["npart"] = n
         with af3d.Engine(s, fun) as e:
             assert e.force_block() == rule(n), n
+            e.set_force_block(192)
+            assert e.force_block() == 192
             for bad in (0, 32, 100, 256):
                 with pytest.raises(af3d.EngineError):
                     e.set_force_block(bad)
@@ -166,9 +169,9 @@ def test_autotune_shapes_steps_are_steps_of_the_run(af3d):
         t0 = float(a.get_system()["time"])
         timings = {}
         every, block = a.autotune_shapes(32, timings)
-        assert every in (16, 32, 64, 128, 256) and block in (64, 96, 128)
+        assert every in (16, 32, 64, 128, 256) and block in (64, 96, 128, 192)
         assert a.force_block() == block
-        assert set(timings["block"]) == {64, 96, 128} and all(v > 0 for v in timings["block"].values())
+        assert set(timings["block"]) == {64, 96, 128, 192} and all(v > 0 for v in timings["block"].values())
         k = int(round((float(a.get_system()["time"]) - t0) / float(sys["dt"])))
         a.step(50)
         tuned = a.export_particles()
