@@ -273,9 +273,9 @@ af3d_status af3d_autotune (af3d_ctx *ctx, long steps_per_trial, long *resort_eve
 af3d_status af3d_set_force_block (af3d_ctx *ctx, int block);
 af3d_status af3d_get_force_block (af3d_ctx *ctx, int *block);
 /* Autotuner over both shape parameters (no counterpart in the reference): af3d_autotune (the
-   permutation interval, its times in ms_interval[5]), then each force block (128, 96, 64, 192,
-   its times in ms_block[4] in that order) at that interval, one untimed period and whole periods timed; keeps the
-   fastest of each.  Every step it takes is a step of the run.  The kernels' remaining shape
+   permutation interval, its times in ms_interval[5]), then each force block (128, 96, 64 and
+   192, its times in ms_block[4] in that order) at that interval, one untimed period and whole
+   periods timed; keeps the fastest of each.  Every step it takes is a step of the run.  The kernels' remaining shape
    parameters are not tuned: one clump per thread (the block pools its clumps' contact items,
    which replaces a clumps-per-warp choice), and the reference's cell size (a smaller cell
    would miss contacts, a larger one only adds candidates to every walk). */
