@@ -193,6 +193,11 @@ def fp64_line(peak, t_forces, mode):
         d.update({"flops_per_launch": flops, "achieved_tflops": flops / t_forces / 1e12,
                   "frac": flops / t_forces / 1e12 / peak if peak > 0 else None,
                   "flops_source": "profiles/lists_forces_flume262k.txt"})
+        # the FP64 pipe also issues compares, conversions and lanes a warp leaves idle: its busy
+        # fraction (ncu sm__pipe_fp64_cycles_active) is the bound flops alone understate
+        busy = from_profile("fp64_pipe_busy_frac")
+        if busy is not None:
+            d["pipe_busy_frac"] = busy
     return d
 
 
