@@ -17,7 +17,7 @@ the state (~350 MB) is larger than L2.
 
 Before timing, the project's autotuner (af3d_autotune_shapes) picks the permutation interval and
 the force kernel's block on a context of its own (untimed; ``--no-autotune`` keeps the
-defaults).  Timed: exactly K fused steps (graph replays, af3d_step) after W warm-up steps, CUDA
+defaults), once for the timed FP64 mode and once for the other one.  Timed: exactly K fused steps (graph replays, af3d_step) after W warm-up steps, CUDA
 events on the engine's stream, barrier + synchronize on both sides, max over ranks.  Then,
 outside the timed region: the other FP64 mode, a profiled pass (CUDA events between the kernels)
 for the roofline of the dominant kernel, the end-to-end figures through the C ABI with host
@@ -25,7 +25,8 @@ buffers (every step, and once per 2000 steps as the reference's device driver co
 2,048- and 524,288-clump configurations, the batched ensemble, the adjoint and the CPU baseline.
 
 ``--impl reference`` times the reference's CPU implementation of the step (the oracle port of
-the reference's host routines, all host threads) on a bounded sample of the same workload.
+the reference's host routines, all host threads) on the same workload (``--cpu-sample M``
+takes a section of M clumps instead).
 """
 from __future__ import annotations
 
